@@ -1,0 +1,174 @@
+/*
+ * seidart_gb300 -- C ABI of the GB300 FDTD time-stepping backend.
+ *
+ * Drop-in for the in-process solver boundary of SeidarT: the f2py-exposed
+ * Fortran subroutines
+ *   seismic2(nx, nz, dx, dz, npoints_pml, src, nstep, OUTPUT_SINGLE)
+ *       legacy/fortran/seismicfdtd.f95:12
+ *   seismic25(nx, ny, nz, dx, dy, dz, npoints_pml, src, nstep, OUTPUT_SINGLE)
+ *       legacy/fortran/seismicfdtd.f95:388
+ *   electromag2(nx, nz, dx, dz, npoints_pml, src, nstep, OUTPUT_SINGLE)
+ *       legacy/fortran/electromagfdtd.f95:10
+ *   electromag25(nx, ny, nz, dx, dy, dz, npoints_pml, src, nstep, OUTPUT_SINGLE)
+ *       legacy/fortran/electromagfdtd.f95:619
+ * called from legacy/prjrun_101424.py:691-808, and of the `seidartfdtd`
+ * process the current driver launches (src/seidart/routines/classes.py:907-924).
+ * Where the Fortran reads its inputs from .dat files in the working directory
+ * (material_rw / loadcpml / loadsource, legacy/fortran/readwrite_routines.f95:9-37,
+ * 451-470) this library takes the same arrays as host pointers; where it writes
+ * one snapshot file per step (write_image2/3, readwrite_routines.f95:473-527)
+ * this library records receiver traces on the device and exposes every field.
+ *
+ * Conventions
+ *   - All sizes are FULL-grid sizes (CPML included), the nx/ny/nz the Fortran
+ *     receives.  Arrays on the host are x fastest (Fortran order): 2-D index
+ *     i + NX*k, 2.5-D index i + NX*(j + NY*k).  Indices are 0-based: the
+ *     Fortran cell (i, k) is (i-1, k-1) here.
+ *   - Material arrays are FP64 (NX, NZ) planes; in 2.5-D they are y-invariant,
+ *     as in the Fortran (seismicfdtd.f95:399-405, electromagfdtd.f95:633-638).
+ *   - Fields are computed in FP32 on the GPU.  dt, the CPML profiles and the
+ *     derived update coefficients are computed in FP64 on the host.
+ *   - The library never allocates device memory: the caller passes one device
+ *     buffer of sfd_state_bytes() bytes that holds every field, CPML memory
+ *     variable, coefficient, source and trace of the handle.
+ *   - Every call returns SFD_OK (0) or a negative SFD_ERR_* code and sets a
+ *     thread-local message readable with sfd_last_error().  No call exits or
+ *     traps.
+ *   - One handle is bound to one CUDA stream; calls on a handle must be
+ *     serialised by the caller; different handles are independent.
+ */
+#ifndef SEIDART_GB300_H
+#define SEIDART_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Solver kinds: the Fortran subroutine each one replaces. */
+#define SFD_SEISMIC2 1     /* seismicfdtd.f95:12-385    */
+#define SFD_SEISMIC25 2    /* seismicfdtd.f95:388-949   */
+#define SFD_ELECTROMAG2 3  /* electromagfdtd.f95:10-326 */
+#define SFD_ELECTROMAG25 4 /* electromagfdtd.f95:619-1092 */
+
+/* Return codes. */
+#define SFD_OK 0
+#define SFD_ERR_BAD_ARG -1
+#define SFD_ERR_STATE -2    /* call out of order (e.g. run before set_model) */
+#define SFD_ERR_CUDA -3
+#define SFD_ERR_UNSTABLE -4 /* field norm above 1e25 or NaN (seismicfdtd.f95:378-379) */
+#define SFD_ERR_TIMEOUT -5  /* a bounded device wait gave up */
+
+
+typedef struct sfd_config {
+  int32_t kind;        /* SFD_SEISMIC2 ... SFD_ELECTROMAG25 */
+  int32_t nx, ny, nz;  /* full grid incl. CPML; ny = 1 for 2-D */
+  int32_t npml;        /* CPML thickness in cells (npoints_pml) */
+  int32_t nstep;       /* length of the source time functions = max steps */
+  int32_t nrec;        /* receivers recorded every step */
+  int32_t flags;       /* reserved, must be 0 */
+  double dx, dy, dz;   /* grid steps (m); dy ignored in 2-D */
+  double dt;           /* time step (s), computed by the caller in FP64 */
+} sfd_config;
+
+typedef struct sfd_handle_s sfd_handle;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int32_t sfd_version(void);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* sfd_last_error(void);
+
+/* Number of material planes sfd_set_model expects for a kind:
+ *   SEISMIC2     9: c11 c13 c15 c33 c35 c55 rho gamma_x gamma_z
+ *                   (seismicfdtd.f95:147-159)
+ *   SEISMIC25   25: c11 c12 c13 c14 c15 c16 c22 c23 c24 c25 c26 c33 c34 c35
+ *                   c36 c44 c45 c46 c55 c56 c66 rho gamma_x gamma_y gamma_z
+ *                   (seismicfdtd.f95:476-497; the legacy routine has no
+ *                   attenuation: gamma = 0 reproduces it, nonzero gamma applies
+ *                   v <- v (1 - gamma) + ... as seismic2 does at :334, 355)
+ *   ELECTROMAG2  6: eps11 eps13 eps33 sig11 sig13 sig33
+ *                   (electromagfdtd.f95:146-151)
+ *   ELECTROMAG25 12: eps11 eps12 eps13 eps22 eps23 eps33
+ *                    sig11 sig12 sig13 sig22 sig23 sig33
+ *                    (electromagfdtd.f95:729-740) */
+int32_t sfd_model_planes(int32_t kind);
+
+/* Number of fields and receiver channels of a kind.
+ *   SEISMIC2:     vx vz sigmaxx sigmazz sigmaxz                 channels vx vz
+ *   SEISMIC25:    vx vy vz sigmaxx sigmayy sigmazz sigmaxy sigmaxz sigmayz
+ *                                                               channels vx vy vz
+ *   ELECTROMAG2:  Ex Ez Hy                                      channels Ex Ez
+ *   ELECTROMAG25: Ex Ey Ez Hx Hy Hz                             channels Ex Ey Ez */
+int32_t sfd_num_fields(int32_t kind);
+int32_t sfd_num_channels(int32_t kind);
+/* Number of CPML memory variables (the Fortran memory_* arrays). */
+int32_t sfd_num_memory(int32_t kind);
+
+/* Bytes of device memory a handle of this configuration needs. */
+int32_t sfd_state_bytes(const sfd_config* cfg, size_t* bytes);
+
+/* Create a handle over a caller-owned device buffer (>= sfd_state_bytes,
+ * 256-byte aligned).  `stream` is a cudaStream_t (NULL = legacy default
+ * stream).  Fields, memory variables and traces start at zero. */
+int32_t sfd_create(const sfd_config* cfg, void* dev_state, size_t state_bytes, void* stream,
+                   sfd_handle** out);
+
+/* Material planes, host FP64, sfd_model_planes(kind) planes of NX*NZ values
+ * (count = planes*NX*NZ).  Replaces the material_rw reads of the Fortran. */
+int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count);
+
+/* CPML profiles, host FP64: for each axis (x, [y,] z) the arrays
+ * K, a, b, K_half, a_half, b_half of the axis length, concatenated
+ * (count = 6*(NX + [NY +] NZ)).  Replaces the loadcpml reads
+ * (seismicfdtd.f95:202-220).  a and a_half must vanish outside the npml-cell
+ * strips at both ends of each axis. */
+int32_t sfd_set_cpml(sfd_handle* h, const double* profiles, int64_t count);
+
+/* Point source at full-grid cell (i, j, k) (j = 0 in 2-D) with time
+ * functions srcfn, host FP64, ncomp x nstep values, component-major
+ * (x, z in 2-D; x, y, z in 2.5-D).  The value added at step t is
+ * srcfn[c][t] * dt / rho (seismic) or * dt / eps_ii (EM), as in
+ * seismicfdtd.f95:360-361 and electromagfdtd.f95:300-301.  Requires the model. */
+int32_t sfd_set_source(sfd_handle* h, int32_t i, int32_t j, int32_t k, const double* srcfn,
+                       int32_t ncomp, int32_t nstep);
+
+/* Receiver cells, host int32 (i, j, k) triples, nrec = cfg.nrec. */
+int32_t sfd_set_receivers(sfd_handle* h, const int32_t* ijk, int32_t nrec);
+
+/* Zero every field, memory variable and trace and rewind to step 0. */
+int32_t sfd_reset(sfd_handle* h);
+
+/* Copy one field between the device state and a host FP32 array of the full
+ * grid (count = NX*NY*NZ).  Writing sets initial conditions (the
+ * initialcondition*.dat files of classes.py:882-898).  Reads synchronise. */
+int32_t sfd_set_field(sfd_handle* h, int32_t field, const float* host, int64_t count);
+int32_t sfd_get_field(sfd_handle* h, int32_t field, float* host, int64_t count);
+/* One CPML memory variable expanded to the full grid (zero off its strips). */
+int32_t sfd_get_memory(sfd_handle* h, int32_t index, float* host, int64_t count);
+
+/* Advance nsteps time steps (asynchronous on the handle's stream).  The
+ * source and the trace index follow the handle's step counter. */
+int32_t sfd_run(sfd_handle* h, int64_t nsteps);
+
+/* Synchronise and report: steps done and the largest field norm seen by the
+ * last sfd_run.  Returns SFD_ERR_UNSTABLE when that norm exceeded 1e25 or was
+ * NaN (the Fortran stops at seismicfdtd.f95:378-379; here the run completes
+ * and the status reports it). */
+int32_t sfd_status(sfd_handle* h, int64_t* step, double* maxnorm);
+
+/* Receiver traces [step][channel][receiver], FP32: copy to host
+ * (count = nstep*nchan*nrec) or the device pointer. */
+int32_t sfd_get_traces(sfd_handle* h, float* host, int64_t count);
+const float* sfd_traces_device(const sfd_handle* h);
+
+/* Release the handle (the caller frees its device buffer afterwards). */
+int32_t sfd_destroy(sfd_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SEIDART_GB300_H */

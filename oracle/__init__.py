@@ -1,0 +1,127 @@
+"""FP64 CPU oracle of the FDTD path -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg may
+use this package, and only as the checker or the timed CPU baseline.  The
+product (seidart_gb300) never imports it.
+
+``liboracle.so`` (built from fdtd_oracle.cpp by the Makefile here) restates the
+reference's legacy Fortran loops in double precision; see the header of
+fdtd_oracle.cpp for the file:line of every loop.  Parity status: unpinned
+(the reference has no tests or golden vectors for this path, and its Fortran
+cannot be compiled on these machines).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+SEISMIC2, SEISMIC25, ELECTROMAG2, ELECTROMAG25 = 1, 2, 3, 4
+NFIELDS = {SEISMIC2: 5, SEISMIC25: 9, ELECTROMAG2: 3, ELECTROMAG25: 6}
+NMEM = {SEISMIC2: 8, SEISMIC25: 18, ELECTROMAG2: 4, ELECTROMAG25: 12}
+NCH = {SEISMIC2: 2, SEISMIC25: 3, ELECTROMAG2: 2, ELECTROMAG25: 3}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    """Compile liboracle.so with the Makefile in this directory."""
+    src = HERE / "fdtd_oracle.cpp"
+    if force or not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
+        subprocess.run(["make", "-s", "-C", str(HERE), "liboracle.so"] + (["-B"] if force else []), check=True)
+    return LIB
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = C.CDLL(str(LIB))
+            dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
+            i, d = C.c_int, C.c_double
+            common_tail = [dp, dp, i, i, dp, i, i, i, dp, dp, i, ip, dp, dp, ip]
+            L.orc_electromag2.argtypes = [i, i, d, d, d] + common_tail
+            L.orc_seismic2.argtypes = [i, i, d, d, d] + common_tail
+            tail3 = [dp, dp, i, i, i, dp, i, i, i, dp, dp, i, ip, dp, dp, ip]
+            L.orc_seismic25.argtypes = [i, i, i, d, d, d, d] + tail3
+            L.orc_electromag25.argtypes = [i, i, i, d, d, d, d] + tail3
+            for f in (L.orc_electromag2, L.orc_seismic2, L.orc_seismic25, L.orc_electromag25):
+                f.restype = C.c_int
+            L.orc_num_threads.restype = C.c_int
+            _lib = L
+        return _lib
+
+
+@dataclass
+class OracleState:
+    kind: int
+    shape: tuple          # (NZ, NX) or (NZ, NY, NX)
+    fields: np.ndarray    # (nfields, *shape)
+    memory: np.ndarray    # (nmem, *shape)
+    step: int = 0
+
+    @classmethod
+    def zeros(cls, kind, shape):
+        return cls(kind, tuple(shape), np.zeros((NFIELDS[kind],) + tuple(shape)),
+                   np.zeros((NMEM[kind],) + tuple(shape)))
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def run(kind, grid, planes, packed_profiles, src_ijk, srcfn, rec_ijk, nsteps, state: OracleState = None):
+    """Advance ``nsteps`` steps of the FP64 oracle.  Returns (state, traces,
+    maxnorm, blew_up); traces is (nsteps, nch, nrec)."""
+    L = lib()
+    three = kind in (SEISMIC25, ELECTROMAG25)
+    shape = (grid.nz, grid.ny, grid.nx) if three else (grid.nz, grid.nx)
+    if state is None:
+        state = OracleState.zeros(kind, shape)
+    planes = np.ascontiguousarray(planes, dtype=np.float64)
+    prof = np.ascontiguousarray(packed_profiles, dtype=np.float64)
+    srcfn = np.ascontiguousarray(srcfn, dtype=np.float64)
+    rec = np.ascontiguousarray(np.asarray(rec_ijk, dtype=np.int32).reshape(-1, 3))
+    nrec = rec.shape[0]
+    traces = np.zeros((nsteps, NCH[kind], max(nrec, 1)))
+    maxnorm = C.c_double(0.0)
+    blew = C.c_int(0)
+    i, j, k = (int(v) for v in src_ijk)
+    recp = rec.ctypes.data_as(C.POINTER(C.c_int)) if nrec else None
+    if kind == ELECTROMAG2:
+        n = L.orc_electromag2(grid.nx, grid.nz, grid.dx, grid.dz, grid.dt, _d(prof), _d(planes), i, k, _d(srcfn),
+                              srcfn.shape[1], state.step, nsteps, _d(state.fields), _d(state.memory), nrec, recp,
+                              _d(traces), C.byref(maxnorm), C.byref(blew))
+    elif kind == SEISMIC2:
+        n = L.orc_seismic2(grid.nx, grid.nz, grid.dx, grid.dz, grid.dt, _d(prof), _d(planes), i, k, _d(srcfn),
+                           srcfn.shape[1], state.step, nsteps, _d(state.fields), _d(state.memory), nrec, recp,
+                           _d(traces), C.byref(maxnorm), C.byref(blew))
+    elif kind == SEISMIC25:
+        n = L.orc_seismic25(grid.nx, grid.ny, grid.nz, grid.dx, grid.dy, grid.dz, grid.dt, _d(prof), _d(planes),
+                            i, j, k, _d(srcfn), srcfn.shape[1], state.step, nsteps, _d(state.fields),
+                            _d(state.memory), nrec, recp, _d(traces), C.byref(maxnorm), C.byref(blew))
+    elif kind == ELECTROMAG25:
+        n = L.orc_electromag25(grid.nx, grid.ny, grid.nz, grid.dx, grid.dy, grid.dz, grid.dt, _d(prof), _d(planes),
+                               i, j, k, _d(srcfn), srcfn.shape[1], state.step, nsteps, _d(state.fields),
+                               _d(state.memory), nrec, recp, _d(traces), C.byref(maxnorm), C.byref(blew))
+    else:
+        raise ValueError(kind)
+    state.step += n
+    return state, traces[:n, :, :nrec], float(maxnorm.value), bool(blew.value)
+
+
+def num_threads() -> int:
+    return int(lib().orc_num_threads())
+
+
+def set_threads(n: int) -> None:
+    os.environ["OMP_NUM_THREADS"] = str(n)

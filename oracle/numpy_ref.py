@@ -1,0 +1,145 @@
+"""Second, independent FP64 restatement of electromag2 and seismic2 in
+vectorised numpy -- TEST INFRASTRUCTURE ONLY.
+
+Written from the Fortran (legacy/fortran/electromagfdtd.f95:244-325,
+legacy/fortran/seismicfdtd.f95:243-384) with whole-array slices instead of
+loops, so that an indexing slip in one restatement shows up as a mismatch
+against the other (fdtd_oracle.cpp).  Arrays are (NZ, NX) = [k, i].
+"""
+from __future__ import annotations
+
+import numpy as np
+
+EPS0 = 8.85418782e-12
+MU0 = 4.0 * np.pi * 1.0e-7
+
+
+def _axes(prof, NX, NZ):
+    p = np.asarray(prof, dtype=np.float64)
+    x = p[:6 * NX].reshape(6, NX)
+    z = p[6 * NX:6 * NX + 6 * NZ].reshape(6, NZ)
+    return x, z  # rows: K, a, b, Kh, ah, bh
+
+
+def electromag2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None):
+    X, Z = _axes(prof, NX, NZ)
+    eps11, eps13, eps33, sig11, sig13, sig33 = np.asarray(mat, dtype=np.float64)
+    epsx, epsz = (eps11 + eps13) * EPS0, (eps13 + eps33) * EPS0
+    sigx, sigz = sig11 + sig13, sig13 + sig33
+    caEx = (1 - sigx * dt / (2 * epsx)) / (1 + sigx * dt / (2 * epsx))
+    cbEx = (dt / epsx) / (1 + sigx * dt / (2 * epsx))
+    caEz = (1 - sigz * dt / (2 * epsz)) / (1 + sigz * dt / (2 * epsz))
+    cbEz = (dt / epsz) / (1 + sigz * dt / (2 * epsz))
+    dbH = dt / MU0
+    Ex, Ez, Hy = (np.zeros((NZ, NX)) for _ in range(3))
+    mExz, mEzx, mHyz, mHyx = (np.zeros((NZ, NX)) for _ in range(4))
+    si, sk = src_ik
+    out = []
+    Kx, ax, bx, Kxh, axh, bxh = (X[q][None, :] for q in range(6))
+    Kz, az, bz, Kzh, azh, bzh = (Z[q][:, None] for q in range(6))
+    for t in range(nsteps):
+        # H: k in [0,NZ-2], i in [0,NX-2]
+        dEx = (Ex[1:, :-1] - Ex[:-1, :-1]) / dz
+        mExz[:-1, :-1] = bz[:-1] * mExz[:-1, :-1] + az[:-1] * dEx
+        vz = dEx / Kz[:-1] + mExz[:-1, :-1]
+        dEz = (Ez[:-1, 1:] - Ez[:-1, :-1]) / dx
+        mEzx[:-1, :-1] = bx[:, :-1] * mEzx[:-1, :-1] + ax[:, :-1] * dEz
+        vx = dEz / Kx[:, :-1] + mEzx[:-1, :-1]
+        Hy[:-1, :-1] = Hy[:-1, :-1] + dbH * (vx + vz)
+        # Ex: k in [1,NZ-2], i in [0,NX-2]
+        d = (Hy[1:-1, :-1] - Hy[:-2, :-1]) / dz
+        mHyz[1:-1, :-1] = bzh[1:-1] * mHyz[1:-1, :-1] + azh[1:-1] * d
+        d = d / Kzh[1:-1] + mHyz[1:-1, :-1]
+        Ex[1:-1, :-1] = ((caEx[1:-1, :-1] + caEx[:-2, :-1]) / 2) * Ex[1:-1, :-1] + \
+            ((cbEx[1:-1, :-1] + cbEx[:-2, :-1]) / 2) * d
+        # Ez: k in [0,NZ-2], i in [1,NX-2]
+        d = (Hy[:-1, 1:-1] - Hy[:-1, :-2]) / dx
+        mHyx[:-1, 1:-1] = bxh[:, 1:-1] * mHyx[:-1, 1:-1] + axh[:, 1:-1] * d
+        d = d / Kxh[:, 1:-1] + mHyx[:-1, 1:-1]
+        Ez[:-1, 1:-1] = ((caEz[:-1, 1:-1] + caEz[:-1, :-2]) / 2) * Ez[:-1, 1:-1] + \
+            ((cbEz[:-1, 1:-1] + cbEz[:-1, :-2]) / 2) * d
+        Ex[sk, si] += srcfn[0][t] * dt / eps11[sk, si]
+        Ez[sk, si] += srcfn[1][t] * dt / eps33[sk, si]
+        Ex[:, 0] = 0; Ex[:, NX - 2] = 0; Ex[0, :] = 0; Ex[NZ - 1, :] = 0
+        Ez[:, 0] = 0; Ez[:, NX - 1] = 0; Ez[0, :] = 0; Ez[NZ - 2, :] = 0
+        Hy[:, 0] = 0; Hy[:, NX - 2] = 0; Hy[0, :] = 0; Hy[NZ - 2, :] = 0
+        if rec is not None:
+            out.append(np.stack([Ex[rec[:, 2], rec[:, 0]], Ez[rec[:, 2], rec[:, 0]]]))
+    return np.stack([Ex, Ez, Hy]), np.stack([mExz, mEzx, mHyz, mHyx]), (np.stack(out) if out else None)
+
+
+def seismic2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None):
+    X, Z = _axes(prof, NX, NZ)
+    c11, c13, c15, c33, c35, c55, rho, gx, gz = np.asarray(mat, dtype=np.float64)
+    vx, vz, sxx, szz, sxz = (np.zeros((NZ, NX)) for _ in range(5))
+    m_vxx, m_vzz, m_vxz, m_vzx, m_sxx, m_szz, m_sxzx, m_sxzz = (np.zeros((NZ, NX)) for _ in range(8))
+    si, sk = src_ik
+    Kx, ax, bx, Kxh, axh, bxh = (X[q][None, :] for q in range(6))
+    Kz, az, bz, Kzh, azh, bzh = (Z[q][:, None] for q in range(6))
+    # b_x_half read with the z index (seismicfdtd.f95:255); 0 past the x axis
+    q3 = np.zeros(NZ)
+    n = min(NX, NZ)
+    q3[:n] = X[5][:n]
+    q3 = q3[:, None]
+    out = []
+    for t in range(nsteps):
+        # loop 1: k in [1, NZ-1], i in [0, NX-2]
+        s1 = (slice(1, NZ), slice(0, NX - 1))
+        dvx_dx = (vx[1:, 1:] - vx[1:, :-1]) / dx
+        dvz_dz = (vz[1:, :-1] - vz[:-1, :-1]) / dz
+        dvz_dx = (vz[1:, 1:] - vz[1:, :-1]) / dx
+        dvx_dz = (vx[1:, :-1] - vx[:-1, :-1]) / dz
+        m_vxx[s1] = q3[1:] * m_vxx[s1] + axh[:, :-1] * dvx_dx
+        m_vzz[s1] = bz[1:] * m_vzz[s1] + az[1:] * dvz_dz
+        m_vxz[s1] = bzh[1:] * m_vxz[s1] + azh[1:] * dvx_dz
+        m_vzx[s1] = bx[:, :-1] * m_vzx[s1] + ax[:, :-1] * dvz_dx
+        dvx_dx = dvx_dx / Kxh[:, :-1] + m_vxx[s1]
+        dvz_dz = dvz_dz / Kz[1:] + m_vzz[s1]
+        dvz_dx = dvz_dx / Kx[:, :-1] + m_vzx[s1]
+        dvx_dz = dvx_dz / Kzh[1:] + m_vxz[s1]
+        av = lambda c: (c[1:, 1:] + 2 * c[1:, :-1] + c[:-1, :-1]) / 4
+        sxx[s1] = sxx[s1] + (av(c11) * dvx_dx + av(c13) * dvz_dz + av(c15) * (dvz_dx + dvx_dz)) * dt
+        szz[s1] = szz[s1] + (av(c13) * dvx_dx + av(c33) * dvz_dz + av(c35) * (dvz_dx + dvx_dz)) * dt
+        # loop 2: k in [0, NZ-2], i in [1, NX-1]
+        s2 = (slice(0, NZ - 1), slice(1, NX))
+        dvx_dx = (vx[:-1, 1:] - vx[:-1, :-1]) / dx
+        dvz_dz = (vz[1:, 1:] - vz[:-1, 1:]) / dz
+        dvz_dx = (vz[:-1, 1:] - vz[:-1, :-1]) / dx
+        dvx_dz = (vx[1:, 1:] - vx[:-1, 1:]) / dz
+        m_vxx[s2] = bxh[:, 1:] * m_vxx[s2] + axh[:, 1:] * dvx_dx
+        m_vzz[s2] = bz[:-1] * m_vzz[s2] + az[:-1] * dvz_dz
+        m_vxz[s2] = bzh[:-1] * m_vxz[s2] + azh[:-1] * dvx_dz
+        m_vzx[s2] = bx[:, 1:] * m_vzx[s2] + ax[:, 1:] * dvz_dx
+        dvx_dx = dvx_dx / Kxh[:, 1:] + m_vxx[s2]
+        dvz_dz = dvz_dz / Kz[:-1] + m_vzz[s2]
+        dvz_dx = dvz_dx / Kx[:, 1:] + m_vzx[s2]
+        dvx_dz = dvx_dz / Kzh[:-1] + m_vxz[s2]
+        bv = lambda c: (c[1:, 1:] + 2 * c[:-1, 1:] + c[:-1, :-1]) / 4
+        sxz[s2] = sxz[s2] + (bv(c15) * dvx_dx + bv(c35) * dvz_dz + bv(c55) * (dvz_dx + dvx_dz)) * dt
+        # vx: k in [1, NZ-1], i in [1, NX-1]
+        s3 = (slice(1, NZ), slice(1, NX))
+        d1 = (sxx[1:, 1:] - sxx[1:, :-1]) / dx
+        d2 = (sxz[1:, 1:] - sxz[:-1, 1:]) / dz
+        m_sxx[s3] = bx[:, 1:] * m_sxx[s3] + ax[:, 1:] * d1
+        m_sxzz[s3] = bz[1:] * m_sxzz[s3] + az[1:] * d2
+        d1 = d1 / Kx[:, 1:] + m_sxx[s3]
+        d2 = d2 / Kz[1:] + m_sxzz[s3]
+        vx[s3] = vx[s3] * (1 - gx[s3]) + (d1 + d2) * dt / rho[s3]
+        # vz: k in [0, NZ-2], i in [0, NX-2]
+        s4 = (slice(0, NZ - 1), slice(0, NX - 1))
+        rbar = (2 * rho[s4] + rho[:-1, 1:] + rho[1:, :-1]) / 4
+        d1 = (sxz[:-1, 1:] - sxz[:-1, :-1]) / dx
+        d2 = (szz[1:, :-1] - szz[:-1, :-1]) / dz
+        m_sxzx[s4] = bxh[:, :-1] * m_sxzx[s4] + axh[:, :-1] * d1
+        m_szz[s4] = bzh[:-1] * m_szz[s4] + azh[:-1] * d2
+        d1 = d1 / Kxh[:, :-1] + m_sxzx[s4]
+        d2 = d2 / Kzh[:-1] + m_szz[s4]
+        vz[s4] = vz[s4] * (1 - gz[s4]) + (d1 + d2) * dt / rbar
+        vx[sk, si] += srcfn[0][t] * dt / rho[sk, si]
+        vz[sk, si] += srcfn[1][t] * dt / rho[sk, si]
+        for f in (vx, vz):
+            f[:, 0] = 0; f[:, NX - 1] = 0; f[0, :] = 0; f[NZ - 1, :] = 0
+        if rec is not None:
+            out.append(np.stack([vx[rec[:, 2], rec[:, 0]], vz[rec[:, 2], rec[:, 0]]]))
+    mem = np.stack([m_vxx, m_vzz, m_vxz, m_vzx, m_sxx, m_szz, m_sxzx, m_sxzz])
+    return np.stack([vx, vz, sxx, szz, sxz]), mem, (np.stack(out) if out else None)

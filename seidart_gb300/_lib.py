@@ -1,0 +1,112 @@
+"""ctypes binding of ``libseidart_gb300.so`` (the C ABI in include/seidart_gb300.h).
+
+The library is built in-tree by ``seidart_gb300.build``.  There is no
+fallback: if the shared library is missing or does not load, every solver call
+raises :class:`LibraryMissingError`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libseidart_gb300.so"
+
+SEISMIC2, SEISMIC25, ELECTROMAG2, ELECTROMAG25 = 1, 2, 3, 4
+KIND_NAMES = {SEISMIC2: "seismic2", SEISMIC25: "seismic25", ELECTROMAG2: "electromag2", ELECTROMAG25: "electromag25"}
+KIND_BY_NAME = {v: k for k, v in KIND_NAMES.items()}
+
+SFD_OK, SFD_ERR_BAD_ARG, SFD_ERR_STATE, SFD_ERR_CUDA, SFD_ERR_UNSTABLE, SFD_ERR_TIMEOUT = 0, -1, -2, -3, -4, -5
+
+# Every exported symbol of include/seidart_gb300.h
+EXPORTS = (
+    "sfd_version", "sfd_last_error", "sfd_model_planes", "sfd_num_fields", "sfd_num_channels",
+    "sfd_num_memory", "sfd_state_bytes", "sfd_create", "sfd_set_model", "sfd_set_cpml",
+    "sfd_set_source", "sfd_set_receivers", "sfd_reset", "sfd_set_field", "sfd_get_field",
+    "sfd_get_memory", "sfd_run", "sfd_status", "sfd_get_traces", "sfd_traces_device", "sfd_destroy",
+)
+
+
+class LibraryMissingError(RuntimeError):
+    pass
+
+
+class SfdError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class UnstableError(SfdError):
+    pass
+
+
+class SfdConfig(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+        ("npml", C.c_int32), ("nstep", C.c_int32), ("nrec", C.c_int32), ("flags", C.c_int32),
+        ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double), ("dt", C.c_double),
+    ]
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def _declare(lib):
+    P = C.c_void_p
+    i32, i64, sz = C.c_int32, C.c_int64, C.c_size_t
+    dp, fp, ip = C.POINTER(C.c_double), C.POINTER(C.c_float), C.POINTER(C.c_int32)
+    sig = {
+        "sfd_version": (i32, []),
+        "sfd_last_error": (C.c_char_p, []),
+        "sfd_model_planes": (i32, [i32]),
+        "sfd_num_fields": (i32, [i32]),
+        "sfd_num_channels": (i32, [i32]),
+        "sfd_num_memory": (i32, [i32]),
+        "sfd_state_bytes": (i32, [C.POINTER(SfdConfig), C.POINTER(sz)]),
+        "sfd_create": (i32, [C.POINTER(SfdConfig), P, sz, P, C.POINTER(P)]),
+        "sfd_set_model": (i32, [P, dp, i64]),
+        "sfd_set_cpml": (i32, [P, dp, i64]),
+        "sfd_set_source": (i32, [P, i32, i32, i32, dp, i32, i32]),
+        "sfd_set_receivers": (i32, [P, ip, i32]),
+        "sfd_reset": (i32, [P]),
+        "sfd_set_field": (i32, [P, i32, fp, i64]),
+        "sfd_get_field": (i32, [P, i32, fp, i64]),
+        "sfd_get_memory": (i32, [P, i32, fp, i64]),
+        "sfd_run": (i32, [P, i64]),
+        "sfd_status": (i32, [P, C.POINTER(i64), dp]),
+        "sfd_get_traces": (i32, [P, fp, i64]),
+        "sfd_traces_device": (P, [P]),
+        "sfd_destroy": (i32, [P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+
+
+def lib():
+    """Load (once) and return the CUDA library; raise if it is not built."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not LIB_PATH.exists():
+                raise LibraryMissingError(
+                    f"{LIB_PATH} is not built; run `python -m seidart_gb300.build` (CUDA toolkit required)")
+            try:
+                handle = C.CDLL(str(LIB_PATH))
+            except OSError as e:
+                raise LibraryMissingError(f"cannot load {LIB_PATH}: {e}") from e
+            _declare(handle)
+            _lib = handle
+        return _lib
+
+
+def check(code: int) -> None:
+    if code == SFD_OK:
+        return
+    msg = lib().sfd_last_error().decode(errors="replace")
+    if code == SFD_ERR_UNSTABLE:
+        raise UnstableError(code, msg)
+    raise SfdError(code, msg)

@@ -1,0 +1,177 @@
+"""FP64 host computation of the CPML damping profiles, the time step and the
+Christoffel velocities that set them.
+
+The solvers consume one 1-D profile per axis and per grid offset (full node
+and half node): ``K``, ``a`` and ``b`` (``alpha`` and ``sigma`` are returned
+for inspection).  The profile shape follows the reference's 1-D writer
+(``legacy/prjrun_101424.py:174-303``: ``sigma = sigma_max d^NP``,
+``kappa = 1 + (kappa_max - 1) d^NP``, ``alpha = alpha_max (1 - d)^NPA``,
+``b = exp(-(sigma/kappa + alpha) dt)`` -- ``dt/eps0`` for EM -- and
+``a = sigma (b - 1) / (kappa sigma + kappa alpha)`` where ``|sigma| > 1e-6``;
+interior cells keep ``K = 1, a = 0, b = 0``).  ``sigma_max`` and
+``alpha_max`` follow the current driver's "global" mode
+(``src/seidart/routines/definitions.py:646-699``) or, with
+``mode="legacy"``, the legacy writer (``legacy/prjrun_101424.py:226-244``).
+
+Everything here is FP64 and runs once per model on the host.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+# src/seidart/routines/definitions.py:67-69
+CLIGHT = 2.99792458e8
+EPS0 = 8.85418782e-12
+MU0 = 4.0 * np.pi * 1.0e-7
+
+# Project-file defaults, src/seidart/routines/prjbuild.py:43-49
+DEFAULT_CPML = dict(alpha_max_scalar=1.0, kappa_max=5.0, NP=2.0, NPA=2.0, Rcoef=0.001)
+
+
+@dataclass
+class AxisProfile:
+    """CPML coefficients of one axis, full-node and half-node offsets."""
+    K: np.ndarray
+    a: np.ndarray
+    b: np.ndarray
+    K_half: np.ndarray
+    a_half: np.ndarray
+    b_half: np.ndarray
+    alpha: np.ndarray
+    alpha_half: np.ndarray
+    sigma: np.ndarray
+    sigma_half: np.ndarray
+
+    def packed(self) -> np.ndarray:
+        """K, a, b, K_half, a_half, b_half stacked (6, n): the solver layout."""
+        return np.stack([self.K, self.a, self.b, self.K_half, self.a_half, self.b_half])
+
+
+def _profile_1d(n, npml, delta, dt, sig_max, alpha_max, kappa_max, NP, NPA, seismic, half):
+    """One offset of one axis (legacy/prjrun_101424.py:174-303, cpml_parameters)."""
+    kappa = np.ones(n)
+    alpha = np.zeros(n)
+    sigma = np.zeros(n)
+    acoef = np.zeros(n)
+    bcoef = np.zeros(n)
+    dist = delta * np.arange(npml, dtype=np.float64)
+    if half:
+        dist = dist + delta / 2.0
+    dist = (delta * npml - dist) / (delta * npml)
+    scale = dt if seismic else dt / EPS0
+    for ind in range(npml):
+        for pos in (ind, n - 1 - ind):
+            sigma[pos] = sig_max * dist[ind] ** NP
+            kappa[pos] = 1.0 + (kappa_max - 1.0) * dist[ind] ** NP
+            alpha[pos] = alpha_max * (1.0 - dist[ind]) ** NPA
+            bcoef[pos] = math.exp(-(sigma[pos] / kappa[pos] + alpha[pos]) * scale)
+    alpha[alpha < 0.0] = 0.0
+    idx = np.abs(sigma) > 1.0e-6
+    acoef[idx] = sigma[idx] * (bcoef[idx] - 1.0) / (kappa[idx] * sigma[idx] + kappa[idx] * alpha[idx])
+    return kappa, acoef, bcoef, alpha, sigma
+
+
+def sigma_alpha_max(seismic: bool, npml: int, deltamin: float, f0: float, vmax: float,
+                    alpha_max_scalar=1.0, NP=2.0, Rcoef=0.001, dt=None, mode="driver",
+                    velocity_scaling_factor=1.0):
+    """Maximum CPML conductivity and alpha of one axis.
+
+    ``vmax`` is the largest wave speed (m/s) in the model.  For ``mode="driver"``
+    this is ``definitions.py:646-699`` ("global" smoothing); the EM branch is
+    written there in terms of ``clight / sqrt(eps_r)``, which is ``vmax``.
+    For ``mode="legacy"`` it is ``legacy/prjrun_101424.py:226-244``.
+    """
+    if mode == "driver":
+        if seismic:
+            s = -math.log(Rcoef) * (NP + 1) * velocity_scaling_factor * 0.7 * vmax / (2.0 * npml)
+            a = alpha_max_scalar * math.pi * f0
+        else:
+            s = -(NP + 1) * math.log(Rcoef) * EPS0 * vmax / (2.0 * npml * deltamin)
+            a = alpha_max_scalar * math.pi * EPS0 * f0
+    elif mode == "legacy":
+        if seismic:
+            quasi_cp_max = 0.7 * deltamin / (2.0 * dt)
+            s = -math.log(Rcoef) * (NP + 1) * quasi_cp_max / (2.0 * npml)
+            a = math.pi * f0
+        else:
+            # sig_opt_scalar of the legacy script is 1.2 (legacy/prjrun_101424.py:23)
+            s = 1.2 * ((NP + 1) / (deltamin * (MU0 / EPS0) ** 0.5))
+            a = alpha_max_scalar * 2 * math.pi * EPS0 * f0
+    else:
+        raise ValueError(f"unknown CPML mode {mode!r}")
+    return s, a
+
+
+def axis_profile(n: int, npml: int, delta: float, dt: float, sig_max: float, alpha_max: float,
+                 kappa_max=5.0, NP=2.0, NPA=2.0, seismic=True) -> AxisProfile:
+    """Full- and half-offset profiles of one axis of ``n`` cells (CPML included)."""
+    if npml < 1 or 2 * npml > n:
+        raise ValueError(f"npml={npml} does not fit an axis of {n} cells")
+    K, a, b, al, sg = _profile_1d(n, npml, delta, dt, sig_max, alpha_max, kappa_max, NP, NPA, seismic, False)
+    Kh, ah, bh, alh, sgh = _profile_1d(n, npml, delta, dt, sig_max, alpha_max, kappa_max, NP, NPA, seismic, True)
+    return AxisProfile(K, a, b, Kh, ah, bh, al, alh, sg, sgh)
+
+
+def build_profiles(shape, deltas, npml, dt, f0, vmax, seismic, params=None, mode="driver"):
+    """Profiles for every axis of a grid.
+
+    ``shape``/``deltas`` are (NX, NZ) or (NX, NY, NZ) full-grid sizes and steps.
+    Returns the list of AxisProfile in axis order (x, [y,] z).
+    """
+    p = dict(DEFAULT_CPML)
+    if params:
+        p.update(params)
+    deltamin = min(deltas)
+    sig, alp = sigma_alpha_max(seismic, npml, deltamin, f0, vmax, p["alpha_max_scalar"], p["NP"],
+                               p["Rcoef"], dt=dt, mode=mode)
+    return [axis_profile(n, npml, d, dt, sig, alp, p["kappa_max"], p["NP"], p["NPA"], seismic)
+            for n, d in zip(shape, deltas)]
+
+
+def pack_profiles(profiles) -> np.ndarray:
+    """Concatenate K, a, b, K_half, a_half, b_half of every axis (x, [y,] z)."""
+    return np.ascontiguousarray(np.concatenate([pr.packed().ravel() for pr in profiles]), dtype=np.float64)
+
+
+# ---------------------------------------------------------------------------
+# Christoffel velocities and the time step (src/seidart/routines/classes.py:469-492,
+# classes.py:1070-1121).
+
+_VOIGT = [[0, 5, 4], [5, 1, 3], [4, 3, 2]]
+
+
+def voigt_full(C6: np.ndarray) -> np.ndarray:
+    """6x6 Voigt stiffness -> 3x3x3x3 tensor."""
+    C = np.zeros((3, 3, 3, 3))
+    for i in range(3):
+        for j in range(3):
+            for k in range(3):
+                for l in range(3):
+                    C[i, j, k, l] = C6[_VOIGT[i][j], _VOIGT[k][l]]
+    return C
+
+
+def christoffel_velocities(C6: np.ndarray, rho: float, n: np.ndarray) -> np.ndarray:
+    """Phase velocities (3,) along unit direction ``n``."""
+    C = voigt_full(C6)
+    G = np.einsum("ijkl,j,l->ik", C, n, n) / rho
+    w = np.linalg.eigvalsh(G)
+    return np.sqrt(np.maximum(w, 0.0))
+
+
+def max_velocity(C6: np.ndarray, rho: float, dim: float) -> float:
+    """Maximum Christoffel velocity over the driver's direction set
+    (x, z, xz in 2-D; x, y, z, xy, xz, yz in 2.5-D; classes.py:1079-1083)."""
+    s = 1.0 / math.sqrt(2.0)
+    dirs = {"x": (1, 0, 0), "y": (0, 1, 0), "z": (0, 0, 1),
+            "xy": (s, s, 0), "xz": (s, 0, s), "yz": (0, s, s)}
+    keys = ["x", "z", "xz"] if dim == 2 else ["x", "y", "z", "xy", "xz", "yz"]
+    return max(float(christoffel_velocities(C6, rho, np.array(dirs[k], float)).max()) for k in keys)
+
+
+def time_step(cfl: float, vmax: float, deltas) -> float:
+    """dt = CFL / (vmax * sqrt(sum 1/delta^2)), classes.py:480-485."""
+    return cfl / (vmax * math.sqrt(sum(1.0 / d ** 2 for d in deltas)))

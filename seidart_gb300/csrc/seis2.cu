@@ -1,0 +1,209 @@
+// seismic2 (legacy/fortran/seismicfdtd.f95:12-385): 2-D anisotropic
+// velocity-stress scheme.  Two fused kernels per step:
+//   half1: both stress loops (:247-281 sigmaxx/sigmazz, :283-312 sigmaxz) for
+//          one cell per thread.  The four velocity-gradient memory variables
+//          are shared by the two loops in the Fortran, so at a cell that both
+//          loops visit they advance twice, first with the loop-1 stencil and
+//          then with the loop-2 stencil; each thread does the same in
+//          registers.  Loop 1 uses b_x_half at the z index (:255), read here
+//          from a table q3[k] that the host fills from b_x_half.
+//          Block (0,0) first records the receivers of the previous step.
+//   half2: vx (:317-336) and vz (:338-357) with the stress-gradient memory
+//          variables, attenuation, the source (:360-361), the Dirichlet edges
+//          (:365-375) and the per-block field norm (:378-379).
+#include "sfd_solvers.h"
+
+namespace sfd {
+
+namespace {
+
+constexpr int BX = 32, BY = 8;
+
+__global__ void __launch_bounds__(BX * BY) seis2_stress_kernel(Seis2Args a, int rel) {
+  const Ctl* ctl = a.io.ctl;
+  const int t = ctl->base + rel;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && t > ctl->run_start) {
+    const float* ch[2] = {a.vx, a.vz};
+    gather_receivers<2>(a.io.rec, a.io.nrec, a.io.traces, t - 1, ch, a.P, 1, false);
+  }
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int k = blockIdx.y * BY + threadIdx.y;
+  const int NX = a.NX, NZ = a.NZ, P = a.P, W = a.W;
+  if (i >= NX || k >= NZ) return;
+  const bool loop1 = (k >= 1) && (i <= NX - 2);  // :247-248
+  const bool loop2 = (k <= NZ - 2) && (i >= 1);  // :283-284
+  if (!loop1 && !loop2) return;
+  const size_t c = (size_t)k * P + i;
+  const bool xs = in_strip(i, NX, W), zs = in_strip(k, NZ, W);
+  const size_t mx = (size_t)k * (2 * W) + (xs ? strip_idx(i, NX, W) : 0);
+  const size_t mz = (size_t)(zs ? strip_idx(k, NZ, W) : 0) * P + i;
+  float m_vxx = 0.f, m_vzx = 0.f, m_vzz = 0.f, m_vxz = 0.f;
+  if (xs) { m_vxx = a.m_vxx[mx]; m_vzx = a.m_vzx[mx]; }
+  if (zs) { m_vzz = a.m_vzz[mz]; m_vxz = a.m_vxz[mz]; }
+  const float vx0 = a.vx[c], vz0 = a.vz[c];
+  const float ikx = a.X.ik[i], ikxh = a.X.ikh[i], ikz = a.Z.ik[k], ikzh = a.Z.ikh[k];
+  const float c11 = a.c11[c], c13 = a.c13[c], c15 = a.c15[c], c33 = a.c33[c], c35 = a.c35[c];
+
+  if (loop1) {
+    const float d_vx_x = a.vx[c + 1] - vx0;
+    const float d_vz_z = vz0 - a.vz[c - P];
+    const float d_vz_x = a.vz[c + 1] - vz0;
+    const float d_vx_z = vx0 - a.vx[c - P];
+    if (xs) {
+      m_vxx = a.q3[k] * m_vxx + a.X.adh[i] * d_vx_x;
+      m_vzx = a.X.b[i] * m_vzx + a.X.ad[i] * d_vz_x;
+    }
+    if (zs) {
+      m_vzz = a.Z.b[k] * m_vzz + a.Z.ad[k] * d_vz_z;
+      m_vxz = a.Z.bh[k] * m_vxz + a.Z.adh[k] * d_vx_z;
+    }
+    const float dvx_dx = d_vx_x * ikxh + m_vxx;
+    const float dvz_dz = d_vz_z * ikz + m_vzz;
+    const float dvz_dx = d_vz_x * ikx + m_vzx;
+    const float dvx_dz = d_vx_z * ikzh + m_vxz;
+    // (c(i+1,j) + 2 c(i,j) + c(i,j-1)) / 4, stiffness already scaled by dt
+    const float A11 = 0.25f * (a.c11[c + 1] + 2.f * c11 + a.c11[c - P]);
+    const float A13 = 0.25f * (a.c13[c + 1] + 2.f * c13 + a.c13[c - P]);
+    const float A15 = 0.25f * (a.c15[c + 1] + 2.f * c15 + a.c15[c - P]);
+    const float A33 = 0.25f * (a.c33[c + 1] + 2.f * c33 + a.c33[c - P]);
+    const float A35 = 0.25f * (a.c35[c + 1] + 2.f * c35 + a.c35[c - P]);
+    const float shear = dvz_dx + dvx_dz;
+    a.sxx[c] = a.sxx[c] + (A11 * dvx_dx + A13 * dvz_dz + A15 * shear);
+    a.szz[c] = a.szz[c] + (A13 * dvx_dx + A33 * dvz_dz + A35 * shear);
+  }
+  if (loop2) {
+    const float d_vx_x = vx0 - a.vx[c - 1];
+    const float d_vz_z = a.vz[c + P] - vz0;
+    const float d_vz_x = vz0 - a.vz[c - 1];
+    const float d_vx_z = a.vx[c + P] - vx0;
+    if (xs) {
+      m_vxx = a.X.bh[i] * m_vxx + a.X.adh[i] * d_vx_x;
+      m_vzx = a.X.b[i] * m_vzx + a.X.ad[i] * d_vz_x;
+    }
+    if (zs) {
+      m_vzz = a.Z.b[k] * m_vzz + a.Z.ad[k] * d_vz_z;
+      m_vxz = a.Z.bh[k] * m_vxz + a.Z.adh[k] * d_vx_z;
+    }
+    const float dvx_dx = d_vx_x * ikxh + m_vxx;
+    const float dvz_dz = d_vz_z * ikz + m_vzz;
+    const float dvz_dx = d_vz_x * ikx + m_vzx;
+    const float dvx_dz = d_vx_z * ikzh + m_vxz;
+    // (c(i,j+1) + 2 c(i,j) + c(i-1,j)) / 4
+    const float B15 = 0.25f * (a.c15[c + P] + 2.f * c15 + a.c15[c - 1]);
+    const float B35 = 0.25f * (a.c35[c + P] + 2.f * c35 + a.c35[c - 1]);
+    const float B55 = 0.25f * (a.c55[c + P] + 2.f * a.c55[c] + a.c55[c - 1]);
+    a.sxz[c] = a.sxz[c] + (B15 * dvx_dx + B35 * dvz_dz + B55 * (dvz_dx + dvx_dz));
+  }
+  if (xs) { a.m_vxx[mx] = m_vxx; a.m_vzx[mx] = m_vzx; }
+  if (zs) { a.m_vzz[mz] = m_vzz; a.m_vxz[mz] = m_vxz; }
+}
+
+__global__ void __launch_bounds__(BX * BY) seis2_velocity_kernel(Seis2Args a, int rel) {
+  const int t = a.io.ctl->base + rel;
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int k = blockIdx.y * BY + threadIdx.y;
+  const int NX = a.NX, NZ = a.NZ, P = a.P, W = a.W;
+  float norm = 0.0f;
+  if (i < NX && k < NZ) {
+    const size_t c = (size_t)k * P + i;
+    const bool xs = in_strip(i, NX, W), zs = in_strip(k, NZ, W);
+    const size_t mx = (size_t)k * (2 * W) + (xs ? strip_idx(i, NX, W) : 0);
+    const size_t mz = (size_t)(zs ? strip_idx(k, NZ, W) : 0) * P + i;
+    const bool interior = (i >= 1) && (i <= NX - 2) && (k >= 1) && (k <= NZ - 2);
+    float vx = 0.f, vz = 0.f;
+    if (interior) {
+      // vx, :317-336 (k in [1, NZ-1], i in [1, NX-1]); edges are zeroed below
+      {
+        const float d1 = a.sxx[c] - a.sxx[c - 1];
+        const float d2 = a.sxz[c] - a.sxz[c - P];
+        float v1 = d1 * a.X.ik[i], v2 = d2 * a.Z.ik[k];
+        if (xs) {
+          const float m = a.X.b[i] * a.m_sxx_x[mx] + a.X.ad[i] * d1;
+          a.m_sxx_x[mx] = m;
+          v1 += m;
+        }
+        if (zs) {
+          const float m = a.Z.b[k] * a.m_sxz_z[mz] + a.Z.ad[k] * d2;
+          a.m_sxz_z[mz] = m;
+          v2 += m;
+        }
+        vx = a.vx[c];
+        if (a.atten) vx *= a.gxp[c];
+        vx = vx + (v1 + v2) * a.dtrx[c];
+      }
+      // vz, :338-357 (k in [0, NZ-2], i in [0, NX-2])
+      {
+        const float d1 = a.sxz[c + 1] - a.sxz[c];
+        const float d2 = a.szz[c + P] - a.szz[c];
+        float v1 = d1 * a.X.ikh[i], v2 = d2 * a.Z.ikh[k];
+        if (xs) {
+          const float m = a.X.bh[i] * a.m_sxz_x[mx] + a.X.adh[i] * d1;
+          a.m_sxz_x[mx] = m;
+          v1 += m;
+        }
+        if (zs) {
+          const float m = a.Z.bh[k] * a.m_szz_z[mz] + a.Z.adh[k] * d2;
+          a.m_szz_z[mz] = m;
+          v2 += m;
+        }
+        vz = a.vz[c];
+        if (a.atten) vz *= a.gzp[c];
+        vz = vz + (v1 + v2) * a.dtrz[c];
+      }
+    } else {
+      // Cells on the outer edges: the Fortran loops still advance the memory
+      // variables there before the Dirichlet step zeroes the velocity.
+      if (k >= 1 && i >= 1) {  // vx loop covers i = NX-1 and k = NZ-1
+        const float d1 = a.sxx[c] - a.sxx[c - 1];
+        const float d2 = a.sxz[c] - a.sxz[c - P];
+        if (xs) a.m_sxx_x[mx] = a.X.b[i] * a.m_sxx_x[mx] + a.X.ad[i] * d1;
+        if (zs) a.m_sxz_z[mz] = a.Z.b[k] * a.m_sxz_z[mz] + a.Z.ad[k] * d2;
+      }
+      if (k <= NZ - 2 && i <= NX - 2) {  // vz loop covers i = 0 and k = 0
+        const float d1 = a.sxz[c + 1] - a.sxz[c];
+        const float d2 = a.szz[c + P] - a.szz[c];
+        if (xs) a.m_sxz_x[mx] = a.X.bh[i] * a.m_sxz_x[mx] + a.X.adh[i] * d1;
+        if (zs) a.m_szz_z[mz] = a.Z.bh[k] * a.m_szz_z[mz] + a.Z.adh[k] * d2;
+      }
+    }
+    // Source, :360-361 (added before the edges are zeroed, as in the Fortran)
+    if (i == a.io.si && k == a.io.sk) {
+      vx += a.io.src[t];
+      vz += a.io.src[a.io.nstep + t];
+    }
+    if (!interior) { vx = 0.f; vz = 0.f; }  // :365-375
+    a.vx[c] = vx;
+    a.vz[c] = vz;
+    norm = hypotf(vx, vz);
+  }
+  block_norm_to_slot(norm, a.io.slots, blockIdx.y * gridDim.x + blockIdx.x);
+}
+
+__global__ void seis2_finalize_kernel(Seis2Args a, int t_last) {
+  const float* ch[2] = {a.vx, a.vz};
+  gather_receivers<2>(a.io.rec, a.io.nrec, a.io.traces, t_last, ch, a.P, 1, false);
+}
+
+}  // namespace
+
+Launch seis2_launch(const Seis2Args& a) {
+  Launch L;
+  L.block = dim3(BX, BY, 1);
+  L.grid = dim3((a.NX + BX - 1) / BX, (a.NZ + BY - 1) / BY, 1);
+  L.nslots = L.grid.x * L.grid.y;
+  return L;
+}
+
+void seis2_half1(const Seis2Args& a, const Launch& L, int rel, cudaStream_t s) {
+  seis2_stress_kernel<<<L.grid, L.block, 0, s>>>(a, rel);
+}
+
+void seis2_half2(const Seis2Args& a, const Launch& L, int rel, cudaStream_t s) {
+  seis2_velocity_kernel<<<L.grid, L.block, 0, s>>>(a, rel);
+}
+
+void seis2_finalize(const Seis2Args& a, int t_last, cudaStream_t s) {
+  seis2_finalize_kernel<<<1, 256, 0, s>>>(a, t_last);
+}
+
+}  // namespace sfd

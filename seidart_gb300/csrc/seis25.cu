@@ -1,0 +1,289 @@
+// seismic25 (legacy/fortran/seismicfdtd.f95:388-949): 2.5-D anisotropic
+// velocity-stress scheme on (NX, NY, NZ) with y-invariant stiffness C(x, z).
+//
+// Each thread owns one (x, z) column and marches along y, so the 33 averaged
+// stiffness values the four stress loops need at that column (and the three
+// averaged densities of the velocity loops) are formed once per column
+// instead of once per cell.
+//   half1: the four stress loops (:616-678 sigmaxx/yy/zz, :681-725 sigmaxy,
+//          :728-771 sigmaxz, :774-815 sigmayz).  The nine velocity-gradient
+//          memory variables are shared by the loops in the Fortran and
+//          advance once per loop that visits a cell, in loop order; each
+//          thread applies the same sequence in registers.  The coefficient
+//          pairs written at :657 (c16) and :766 (c45) and the two derivatives
+//          :701-707 leave unscaled are kept as written.
+//   half2: vx, vy (:821-870) and vz (:872-896) with the stress-gradient
+//          memory variables, optional attenuation v <- v (1 - gamma), the
+//          source (:898-900), the six Dirichlet faces (:903-925) and the norm.
+#include "sfd_solvers.h"
+
+namespace sfd {
+
+namespace {
+
+constexpr int BX = 32, BZ = 4;
+
+// Plane indices of the 21 stiffness coefficients.
+enum { C11, C12, C13, C14, C15, C16, C22, C23, C24, C25, C26, C33, C34, C35, C36, C44, C45, C46, C55, C56, C66 };
+
+struct Col {
+  const float* C;
+  int P, NZ;
+  __device__ float at(int q, int i, int k) const { return C[((size_t)q * NZ + k) * P + i]; }
+  __device__ float sum4(int q, int i0, int k0, int i1, int k1, int i2, int k2, int i3, int k3) const {
+    return at(q, i0, k0) + at(q, i1, k1) + at(q, i2, k2) + at(q, i3, k3);
+  }
+};
+
+__global__ void __launch_bounds__(BX * BZ) seis25_stress_kernel(Seis25Args a, int rel) {
+  const Ctl* ctl = a.io.ctl;
+  const int t = ctl->base + rel;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && t > ctl->run_start) {
+    const float* ch[3] = {a.vx, a.vy, a.vz};
+    gather_receivers<3>(a.io.rec, a.io.nrec, a.io.traces, t - 1, ch, a.P, a.NY, true);
+  }
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int k = blockIdx.y * BZ + threadIdx.y;
+  const int NX = a.NX, NY = a.NY, NZ = a.NZ, P = a.P, W = a.W;
+  if (i >= NX || k >= NZ) return;
+  const int seg = (NY + a.ysplit - 1) / a.ysplit;
+  const int j0 = blockIdx.z * seg, j1 = min(NY, j0 + seg);
+  if (j0 >= j1) return;
+
+  const bool L1 = (k >= 1) && (i <= NX - 2);
+  const bool L2 = (k >= 1) && (i >= 1);
+  const bool L3 = (k <= NZ - 2) && (i >= 1);
+  const bool L4 = (k <= NZ - 2) && (i <= NX - 2);
+  if (!(L1 || L2 || L3 || L4)) return;
+
+  const Col cc{a.C, P, NZ};
+  // Loop-1 averages over (i+1,k) (i,k) (i,k-1) (i+1,k-1)
+  float p11 = 0, p12 = 0, p13 = 0, p14 = 0, p15 = 0, p16 = 0, p22 = 0, p23 = 0, p24 = 0, p25 = 0, p26 = 0;
+  float p33 = 0, p34 = 0, p35 = 0, p36 = 0;
+  if (L1) {
+#define S1(q) cc.sum4(q, i + 1, k, i, k, i, k - 1, i + 1, k - 1)
+    p11 = 0.25f * S1(C11); p12 = 0.25f * S1(C12); p13 = 0.25f * S1(C13);
+    p14 = 0.125f * S1(C14); p15 = 0.125f * S1(C15); p16 = 0.125f * S1(C16);
+    p22 = 0.25f * S1(C22); p23 = 0.25f * S1(C23); p24 = 0.125f * S1(C24); p25 = 0.125f * S1(C25);
+    p26 = 0.125f * S1(C26); p33 = 0.25f * S1(C33); p34 = 0.125f * S1(C34); p35 = 0.125f * S1(C35);
+    p36 = 0.125f * S1(C36);
+#undef S1
+  }
+  // Loop-2 averages over (i,k) (i-1,k) (i,k-1) (i-1,k-1)
+  float q16 = 0, q26 = 0, q36 = 0, q46 = 0, q56 = 0, q66 = 0;
+  if (L2) {
+#define S2(q) cc.sum4(q, i, k, i - 1, k, i, k - 1, i - 1, k - 1)
+    q16 = 0.25f * S2(C16); q26 = 0.25f * S2(C26); q36 = 0.25f * S2(C36);
+    q46 = 0.125f * S2(C46); q56 = 0.125f * S2(C56); q66 = 0.125f * S2(C66);
+#undef S2
+  }
+  // Loop-3 averages over (i,k+1) (i,k) (i-1,k) (i-1,k+1)
+  float r15 = 0, r25 = 0, r35 = 0, r45 = 0, r55 = 0, r56 = 0;
+  if (L3) {
+#define S3(q) cc.sum4(q, i, k + 1, i, k, i - 1, k, i - 1, k + 1)
+    r15 = 0.25f * S3(C15); r25 = 0.25f * S3(C25); r35 = 0.25f * S3(C35);
+    r45 = 0.125f * S3(C45); r55 = 0.125f * S3(C55); r56 = 0.125f * S3(C56);
+#undef S3
+  }
+  // Loop-4 averages over (i+1,k) (i,k) (i,k+1) (i+1,k+1)
+  float s14 = 0, s24 = 0, s34 = 0, s44 = 0, s45 = 0, s46 = 0;
+  if (L4) {
+#define S4(q) cc.sum4(q, i + 1, k, i, k, i, k + 1, i + 1, k + 1)
+    s14 = 0.25f * S4(C14); s24 = 0.25f * S4(C24); s34 = 0.25f * S4(C34);
+    s44 = 0.125f * S4(C44); s45 = 0.125f * S4(C45); s46 = 0.125f * S4(C46);
+#undef S4
+  }
+
+  const bool xs = in_strip(i, NX, W), zs = in_strip(k, NZ, W);
+  const int xsi = xs ? strip_idx(i, NX, W) : 0;
+  const int zsi = zs ? strip_idx(k, NZ, W) : 0;
+  const float ikx = a.X.ik[i], ikxh = a.X.ikh[i], adx = a.X.ad[i], adxh = a.X.adh[i];
+  const float bx = a.X.b[i], bxh = a.X.bh[i];
+  const float ikz = a.Z.ik[k], ikzh = a.Z.ikh[k], adz = a.Z.ad[k], adzh = a.Z.adh[k];
+  const float bz = a.Z.b[k], bzh = a.Z.bh[k];
+  const float idx = a.idx, idz = a.idz;
+  const size_t plane = (size_t)NY * P;      // one z-plane of a field
+
+  for (int j = j0; j < j1; ++j) {
+    const size_t c = ((size_t)k * NY + j) * P + i;
+    const bool ys = in_strip(j, NY, W);
+    const size_t mx = ((size_t)k * NY + j) * (2 * W) + xsi;
+    const size_t my = ((size_t)k * (2 * W) + (ys ? strip_idx(j, NY, W) : 0)) * P + i;
+    const size_t mz = ((size_t)zsi * NY + j) * P + i;
+    float mvxx = 0, mvyx = 0, mvzx = 0, mvxy = 0, mvyy = 0, mvzy = 0, mvxz = 0, mvyz = 0, mvzz = 0;
+    if (xs) { mvxx = a.m_vx_x[mx]; mvyx = a.m_vy_x[mx]; mvzx = a.m_vz_x[mx]; }
+    if (ys) { mvxy = a.m_vx_y[my]; mvyy = a.m_vy_y[my]; mvzy = a.m_vz_y[my]; }
+    if (zs) { mvxz = a.m_vx_z[mz]; mvyz = a.m_vy_z[mz]; mvzz = a.m_vz_z[mz]; }
+    const float iky = a.Y.ik[j], ikyh = a.Y.ikh[j], ady = a.Y.ad[j], adyh = a.Y.adh[j];
+    const float by = a.Y.b[j], byh = a.Y.bh[j];
+    const float vx0 = a.vx[c], vy0 = a.vy[c], vz0 = a.vz[c];
+
+    // ---- Loop 1: sigmaxx, sigmayy, sigmazz (j >= 1)
+    if (L1 && j >= 1) {
+      const float dxx = a.vx[c + 1] - vx0, dyx = a.vy[c + 1] - vy0, dzx = a.vz[c + 1] - vz0;
+      const float dyy = vy0 - a.vy[c - P], dxy = vx0 - a.vx[c - P], dzy = vz0 - a.vz[c - P];
+      const float dzz = vz0 - a.vz[c - plane], dxz = vx0 - a.vx[c - plane], dyz = vy0 - a.vy[c - plane];
+      if (xs) { mvxx = bxh * mvxx + adxh * dxx; mvyx = bxh * mvyx + adxh * dyx; mvzx = bxh * mvzx + adxh * dzx; }
+      if (ys) { mvyy = by * mvyy + ady * dyy; mvxy = by * mvxy + ady * dxy; mvzy = by * mvzy + ady * dzy; }
+      if (zs) { mvzz = bz * mvzz + adz * dzz; mvxz = bz * mvxz + adz * dxz; mvyz = bz * mvyz + adz * dyz; }
+      const float vxx = dxx * ikxh + mvxx, vyx = dyx * ikxh + mvyx, vzx = dzx * ikxh + mvzx;
+      const float vyy = dyy * iky + mvyy, vxy = dxy * iky + mvxy, vzy = dzy * iky + mvzy;
+      const float vzz = dzz * ikz + mvzz, vxz = dxz * ikz + mvxz, vyz = dyz * ikz + mvyz;
+      a.sxx[c] = a.sxx[c] + (p11 * vxx + p12 * vyy + p13 * vzz + p14 * (vyz + vzy) + p15 * (vxz + vzx) +
+                             p16 * (vxy + vzy));
+      a.syy[c] = a.syy[c] + (p12 * vxx + p22 * vyy + p23 * vzz + p24 * (vyz + vzy) + p25 * (vxz + vzx) +
+                             p26 * (vyx + vxy));
+      a.szz[c] = a.szz[c] + (p13 * vxx + p23 * vyy + p33 * vzz + p34 * (vyz + vzy) + p35 * (vxz + vzx) +
+                             p36 * (vyx + vxy));
+    }
+    // ---- Loop 2: sigmaxy (j <= NY-2)
+    if (L2 && j <= NY - 2) {
+      const float dxx = vx0 - a.vx[c - 1], dyx = vy0 - a.vy[c - 1], dzx = vz0 - a.vz[c - 1];
+      const float dyy = a.vy[c + P] - vy0, dxy = a.vx[c + P] - vx0, dzy = a.vz[c + P] - vz0;
+      const float dzz = vz0 - a.vz[c - plane], dxz = vx0 - a.vx[c - plane], dyz = vy0 - a.vy[c - plane];
+      if (xs) { mvxx = bx * mvxx + adx * dxx; mvyx = bx * mvyx + adx * dyx; mvzx = bx * mvzx + adx * dzx; }
+      if (ys) { mvyy = byh * mvyy + adyh * dyy; mvxy = byh * mvxy + adyh * dxy; mvzy = byh * mvzy + adyh * dzy; }
+      if (zs) { mvzz = bzh * mvzz + adzh * dzz; mvxz = bzh * mvxz + adzh * dxz; mvyz = bzh * mvyz + adzh * dyz; }
+      const float vxx = dxx * ikx + mvxx, vyx = dyx * ikx + mvyx;
+      const float vyy = dyy * ikyh + mvyy, vxy = dxy * ikyh + mvxy, vzy = dzy * ikyh + mvzy;
+      const float vzz = dzz * ikzh + mvzz, vyz = dyz * ikzh + mvyz;
+      const float vzx = dzx * idx, vxz = dxz * idz;  // left unscaled, :701-707
+      a.sxy[c] = a.sxy[c] + (q16 * vxx + q26 * vyy + q36 * vzz + q46 * (vzy + vyz) + q56 * (vzx + vxz) +
+                             q66 * (vyx + vxy));
+    }
+    // ---- Loop 3: sigmaxz (j >= 1)
+    if (L3 && j >= 1) {
+      const float dxx = vx0 - a.vx[c - 1], dyx = vy0 - a.vy[c - 1], dzx = vz0 - a.vz[c - 1];
+      const float dyy = vy0 - a.vy[c - P], dzy = vz0 - a.vz[c - P], dxy = vx0 - a.vx[c - P];
+      const float dzz = a.vz[c + plane] - vz0, dxz = a.vx[c + plane] - vx0, dyz = a.vy[c + plane] - vy0;
+      if (xs) { mvxx = bx * mvxx + adx * dxx; mvyx = bx * mvyx + adx * dyx; mvzx = bx * mvzx + adx * dzx; }
+      if (ys) { mvyy = by * mvyy + ady * dyy; mvxy = by * mvxy + ady * dxy; mvzy = by * mvzy + ady * dzy; }
+      if (zs) { mvzz = bzh * mvzz + adzh * dzz; mvxz = bzh * mvxz + adzh * dxz; mvyz = bzh * mvyz + adzh * dyz; }
+      const float vxx = dxx * ikx + mvxx, vyx = dyx * ikx + mvyx, vzx = dzx * ikx + mvzx;
+      const float vyy = dyy * iky + mvyy, vxy = dxy * iky + mvxy;
+      const float vzz = dzz * ikzh + mvzz, vxz = dxz * ikzh + mvxz;
+      a.sxz[c] = a.sxz[c] + (r15 * vxx + r25 * vyy + r35 * vzz + r45 * (vxz + vzx) + r55 * (vxz + vzx) +
+                             r56 * (vxy + vyx));
+    }
+    // ---- Loop 4: sigmayz (j <= NY-2)
+    if (L4 && j <= NY - 2) {
+      const float dxx = a.vx[c + 1] - vx0, dyx = a.vy[c + 1] - vy0, dzx = a.vz[c + 1] - vz0;
+      const float dyy = a.vy[c + P] - vy0, dxy = a.vx[c + P] - vx0, dzy = a.vz[c + P] - vz0;
+      const float dzz = a.vz[c + plane] - vz0, dxz = a.vx[c + plane] - vx0, dyz = a.vy[c + plane] - vy0;
+      if (xs) { mvxx = bxh * mvxx + adxh * dxx; mvyx = bxh * mvyx + adxh * dyx; mvzx = bxh * mvzx + adxh * dzx; }
+      if (ys) { mvyy = byh * mvyy + adyh * dyy; mvxy = byh * mvxy + adyh * dxy; mvzy = byh * mvzy + adyh * dzy; }
+      if (zs) { mvzz = bzh * mvzz + adzh * dzz; mvxz = bzh * mvxz + adzh * dxz; mvyz = bzh * mvyz + adzh * dyz; }
+      const float vxx = dxx * ikxh + mvxx, vyx = dyx * ikxh + mvyx, vzx = dzx * ikxh + mvzx;
+      const float vyy = dyy * ikyh + mvyy, vxy = dxy * ikyh + mvxy, vzy = dzy * ikyh + mvzy;
+      const float vzz = dzz * ikzh + mvzz, vxz = dxz * ikzh + mvxz, vyz = dyz * ikzh + mvyz;
+      a.syz[c] = a.syz[c] + (s14 * vxx + s24 * vyy + s34 * vzz + s44 * (vyz + vzy) + s45 * (vxz + vzx) +
+                             s46 * (vyx + vxy));
+    }
+    if (xs) { a.m_vx_x[mx] = mvxx; a.m_vy_x[mx] = mvyx; a.m_vz_x[mx] = mvzx; }
+    if (ys) { a.m_vx_y[my] = mvxy; a.m_vy_y[my] = mvyy; a.m_vz_y[my] = mvzy; }
+    if (zs) { a.m_vx_z[mz] = mvxz; a.m_vy_z[mz] = mvyz; a.m_vz_z[mz] = mvzz; }
+  }
+}
+
+__global__ void __launch_bounds__(BX * BZ) seis25_velocity_kernel(Seis25Args a, int rel) {
+  const int t = a.io.ctl->base + rel;
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int k = blockIdx.y * BZ + threadIdx.y;
+  const int NX = a.NX, NY = a.NY, NZ = a.NZ, P = a.P, W = a.W;
+  const int seg = (NY + a.ysplit - 1) / a.ysplit;
+  const int j0 = blockIdx.z * seg, j1 = min(NY, j0 + seg);
+  float norm = 0.0f;
+  if (i < NX && k < NZ && j0 < j1) {
+    const bool Vx = (k >= 1) && (i >= 1);
+    const bool Vy = (k >= 1) && (i <= NX - 2);
+    const bool Vz = (k <= NZ - 2) && (i <= NX - 2);
+    const size_t pc = (size_t)k * P + i;
+    const size_t p2 = (size_t)NZ * P;
+    const float dtrx = Vx ? a.dtr[pc] : 0.f, dtry = Vy ? a.dtr[p2 + pc] : 0.f, dtrz = Vz ? a.dtr[2 * p2 + pc] : 0.f;
+    float gx = 1.f, gy = 1.f, gz = 1.f;
+    if (a.atten) { gx = a.gp[pc]; gy = a.gp[p2 + pc]; gz = a.gp[2 * p2 + pc]; }
+    const bool xs = in_strip(i, NX, W), zs = in_strip(k, NZ, W);
+    const int xsi = xs ? strip_idx(i, NX, W) : 0;
+    const int zsi = zs ? strip_idx(k, NZ, W) : 0;
+    const float ikx = a.X.ik[i], ikxh = a.X.ikh[i], adx = a.X.ad[i], adxh = a.X.adh[i];
+    const float bx = a.X.b[i], bxh = a.X.bh[i];
+    const float ikz = a.Z.ik[k], ikzh = a.Z.ikh[k], adz = a.Z.ad[k], adzh = a.Z.adh[k];
+    const float bz = a.Z.b[k], bzh = a.Z.bh[k];
+    const size_t plane = (size_t)NY * P;
+    const bool xface = (i == 0) || (i == NX - 1) || (k == 0) || (k == NZ - 1);
+    for (int j = j0; j < j1; ++j) {
+      const size_t c = ((size_t)k * NY + j) * P + i;
+      const bool ys = in_strip(j, NY, W);
+      const size_t mx = ((size_t)k * NY + j) * (2 * W) + xsi;
+      const size_t my = ((size_t)k * (2 * W) + (ys ? strip_idx(j, NY, W) : 0)) * P + i;
+      const size_t mz = ((size_t)zsi * NY + j) * P + i;
+      const float iky = a.Y.ik[j], ikyh = a.Y.ikh[j], ady = a.Y.ad[j], adyh = a.Y.adh[j];
+      const float by = a.Y.b[j], byh = a.Y.bh[j];
+      float vx = a.vx[c], vy = a.vy[c], vz = a.vz[c];
+      if (Vx && j >= 1) {  // :821-845
+        const float d1 = a.sxx[c] - a.sxx[c - 1], d2 = a.sxy[c] - a.sxy[c - P], d3 = a.sxz[c] - a.sxz[c - plane];
+        float v1 = d1 * ikx, v2 = d2 * iky, v3 = d3 * ikz;
+        if (xs) { const float m = bx * a.m_sxx_x[mx] + adx * d1; a.m_sxx_x[mx] = m; v1 += m; }
+        if (ys) { const float m = by * a.m_sxy_y[my] + ady * d2; a.m_sxy_y[my] = m; v2 += m; }
+        if (zs) { const float m = bz * a.m_sxz_z[mz] + adz * d3; a.m_sxz_z[mz] = m; v3 += m; }
+        vx = vx * gx + (v1 + v2 + v3) * dtrx;
+      }
+      if (Vy && j <= NY - 2) {  // :847-869
+        const float d1 = a.sxy[c + 1] - a.sxy[c], d2 = a.syy[c + P] - a.syy[c], d3 = a.syz[c] - a.syz[c - plane];
+        float v1 = d1 * ikxh, v2 = d2 * ikyh, v3 = d3 * ikz;
+        if (xs) { const float m = bxh * a.m_sxy_x[mx] + adxh * d1; a.m_sxy_x[mx] = m; v1 += m; }
+        if (ys) { const float m = byh * a.m_syy_y[my] + adyh * d2; a.m_syy_y[my] = m; v2 += m; }
+        if (zs) { const float m = bz * a.m_syz_z[mz] + adz * d3; a.m_syz_z[mz] = m; v3 += m; }
+        vy = vy * gy + (v1 + v2 + v3) * dtry;
+      }
+      if (Vz && j >= 1) {  // :872-896
+        const float d1 = a.sxz[c + 1] - a.sxz[c], d2 = a.syz[c] - a.syz[c - P], d3 = a.szz[c + plane] - a.szz[c];
+        float v1 = d1 * ikxh, v2 = d2 * iky, v3 = d3 * ikzh;
+        if (xs) { const float m = bxh * a.m_sxz_x[mx] + adxh * d1; a.m_sxz_x[mx] = m; v1 += m; }
+        if (ys) { const float m = by * a.m_syz_y[my] + ady * d2; a.m_syz_y[my] = m; v2 += m; }
+        if (zs) { const float m = bzh * a.m_szz_z[mz] + adzh * d3; a.m_szz_z[mz] = m; v3 += m; }
+        vz = vz * gz + (v1 + v2 + v3) * dtrz;
+      }
+      if (i == a.io.si && j == a.io.sj && k == a.io.sk) {  // :898-900
+        vx += a.io.src[t];
+        vy += a.io.src[a.io.nstep + t];
+        vz += a.io.src[2 * a.io.nstep + t];
+      }
+      if (xface || j == 0 || j == NY - 1) { vx = 0.f; vy = 0.f; vz = 0.f; }  // :903-925
+      a.vx[c] = vx;
+      a.vy[c] = vy;
+      a.vz[c] = vz;
+      norm = fmaxf(norm, nan_to_inf(norm3df(vx, vy, vz)));
+    }
+  }
+  block_norm_to_slot(norm, a.io.slots, (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
+}
+
+__global__ void seis25_finalize_kernel(Seis25Args a, int t_last) {
+  const float* ch[3] = {a.vx, a.vy, a.vz};
+  gather_receivers<3>(a.io.rec, a.io.nrec, a.io.traces, t_last, ch, a.P, a.NY, true);
+}
+
+}  // namespace
+
+Launch seis25_launch(const Seis25Args& a) {
+  Launch L;
+  L.block = dim3(BX, BZ, 1);
+  L.grid = dim3((a.NX + BX - 1) / BX, (a.NZ + BZ - 1) / BZ, a.ysplit);
+  L.nslots = L.grid.x * L.grid.y * L.grid.z;
+  return L;
+}
+
+void seis25_half1(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s) {
+  seis25_stress_kernel<<<L.grid, L.block, 0, s>>>(a, rel);
+}
+
+void seis25_half2(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s) {
+  seis25_velocity_kernel<<<L.grid, L.block, 0, s>>>(a, rel);
+}
+
+void seis25_finalize(const Seis25Args& a, int t_last, cudaStream_t s) {
+  seis25_finalize_kernel<<<1, 256, 0, s>>>(a, t_last);
+}
+
+}  // namespace sfd

@@ -1,0 +1,758 @@
+// C ABI of the seidart_gb300 FDTD backend: handle management, FP64 host-side
+// coefficient folding, state layout in the caller's device buffer, and the
+// time loop (CUDA graphs of 32 steps, two fused kernels per step).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/seidart_gb300.h"
+#include "sfd_solvers.h"
+
+namespace sfd {
+
+__global__ void k_begin(Ctl* ctl, float* slots, int nslots, int step) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int s = tid; s < nslots; s += gridDim.x * blockDim.x) slots[s] = 0.0f;
+  if (tid == 0) {
+    ctl->base = step;
+    ctl->run_start = step;
+    ctl->maxnorm = 0.0f;
+    ctl->nan_seen = 0;
+  }
+}
+
+__global__ void k_advance(Ctl* ctl, int by) { ctl->base += by; }
+
+__global__ void k_reduce_slots(Ctl* ctl, const float* slots, int nslots) {
+  float m = 0.0f;
+  for (int s = threadIdx.x; s < nslots; s += blockDim.x) m = fmaxf(m, slots[s]);
+  __shared__ float red[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) ctl->maxnorm = m;
+  }
+}
+
+}  // namespace sfd
+
+using namespace sfd;
+
+namespace {
+
+constexpr double kPI = 3.141592653589793238462643;
+constexpr double kMu0 = 4.0 * kPI * 1.0e-7;
+constexpr double kEps0 = 8.85418782e-12;
+constexpr int kGraphSteps = 32;
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(SFD_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call)                                   \
+  do {                                             \
+    cudaError_t e_ = (call);                       \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+int nfields(int kind) {
+  switch (kind) {
+    case SFD_SEISMIC2: return 5;
+    case SFD_SEISMIC25: return 9;
+    case SFD_ELECTROMAG2: return 3;
+    case SFD_ELECTROMAG25: return 6;
+  }
+  return 0;
+}
+int nchan(int kind) { return (kind == SFD_SEISMIC25 || kind == SFD_ELECTROMAG25) ? 3 : 2; }
+int nplanes(int kind) {
+  switch (kind) {
+    case SFD_SEISMIC2: return 9;
+    case SFD_SEISMIC25: return 25;
+    case SFD_ELECTROMAG2: return 6;
+    case SFD_ELECTROMAG25: return 12;
+  }
+  return 0;
+}
+bool is3(int kind) { return kind == SFD_SEISMIC25 || kind == SFD_ELECTROMAG25; }
+
+// Strip axis of each memory variable, in the oracle's order.
+const char* mem_axes(int kind) {
+  switch (kind) {
+    case SFD_ELECTROMAG2: return "zxzx";              // dEx_dz dEz_dx dHy_dz dHy_dx
+    case SFD_SEISMIC2: return "xzzxxzxz";             // dvx_dx dvz_dz dvx_dz dvz_dx dsxx_dx dszz_dz dsxz_dx dsxz_dz
+    case SFD_SEISMIC25: return "xyzxyzxyzxyzxyxzyz";  // dv{x,y,z}_d{x,y,z}, dsxx_dx dsyy_dy dszz_dz dsxy_dx dsxy_dy dsxz_dx dsxz_dz dsyz_dy dsyz_dz
+    case SFD_ELECTROMAG25: return "yzzxyxyzxzyx";     // dEz_dy dEy_dz dEx_dz dEz_dx dEx_dy dEy_dx dHz_dy dHy_dz dHz_dx dHx_dz dHx_dy dHy_dx
+  }
+  return "";
+}
+int ncoef(int kind) {
+  switch (kind) {
+    case SFD_SEISMIC2: return 10;   // c11 c13 c15 c33 c35 c55 (x dt), dt/rho, dt/rho_avg, 1-gx, 1-gz
+    case SFD_SEISMIC25: return 27;  // 21 C x dt, 3 dt/rho_avg, 3 (1 - gamma)
+    case SFD_ELECTROMAG2: return 4;
+    case SFD_ELECTROMAG25: return 6;
+  }
+  return 0;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+int choose_ysplit(const sfd_config& c) {
+  if (!is3(c.kind)) return 1;
+  // enough columns x segments to fill 152 SMs a few times over
+  const long cols = (long)c.nx * c.nz;
+  int s = 1;
+  while (cols * s < 152L * 1024 * 2 && s * 8 <= c.ny) s *= 2;
+  return s;
+}
+
+struct Layout {
+  int P, NX, NY, NZ, W, ysplit, nslots;
+  size_t fsz;                // floats per field
+  size_t off_ctl, off_fields, off_mem[18], mem_sz[18], off_coef, coef_plane, off_axis[3], off_q3, off_src,
+      off_rec, off_traces, off_slots, total;
+};
+
+int grid_slots(const sfd_config& c, int P, int ysplit) {
+  (void)P;
+  if (is3(c.kind)) return ((c.nx + 31) / 32) * ((c.nz + 3) / 4) * ysplit;
+  return ((c.nx + 31) / 32) * ((c.nz + 7) / 8);
+}
+
+int validate_cfg(const sfd_config* c) {
+  if (!c) return fail(SFD_ERR_BAD_ARG, "config is NULL");
+  if (c->kind < SFD_SEISMIC2 || c->kind > SFD_ELECTROMAG25) return fail(SFD_ERR_BAD_ARG, "unknown solver kind %d", c->kind);
+  const bool three = is3(c->kind);
+  if (c->npml < 1) return fail(SFD_ERR_BAD_ARG, "npml must be >= 1 (got %d)", c->npml);
+  if (c->nx < 2 * c->npml + 2 || c->nz < 2 * c->npml + 2)
+    return fail(SFD_ERR_BAD_ARG, "grid %dx%d too small for npml=%d", c->nx, c->nz, c->npml);
+  if (three && c->ny < 2 * c->npml + 2) return fail(SFD_ERR_BAD_ARG, "ny=%d too small for npml=%d", c->ny, c->npml);
+  if (!three && c->ny != 1) return fail(SFD_ERR_BAD_ARG, "2-D solvers need ny = 1 (got %d)", c->ny);
+  if (c->nstep < 1) return fail(SFD_ERR_BAD_ARG, "nstep must be >= 1");
+  if (c->nrec < 0) return fail(SFD_ERR_BAD_ARG, "nrec must be >= 0");
+  if (c->flags != 0) return fail(SFD_ERR_BAD_ARG, "flags must be 0");
+  if (!(c->dt > 0) || !(c->dx > 0) || !(c->dz > 0) || (three && !(c->dy > 0)))
+    return fail(SFD_ERR_BAD_ARG, "dt and grid steps must be positive");
+  const double cells = (double)c->nx * c->ny * c->nz;
+  if (cells > 2.0e9) return fail(SFD_ERR_BAD_ARG, "grid of %.3g cells exceeds the 2^31 index range", cells);
+  return SFD_OK;
+}
+
+void make_layout(const sfd_config& c, Layout* L) {
+  L->NX = c.nx; L->NY = c.ny; L->NZ = c.nz; L->W = c.npml;
+  L->P = (c.nx + 31) & ~31;
+  L->ysplit = choose_ysplit(c);
+  L->nslots = grid_slots(c, L->P, L->ysplit);
+  L->fsz = (size_t)L->P * c.ny * c.nz;
+  size_t o = 0;
+  L->off_ctl = o; o += 256;
+  L->off_fields = o; o += align256(sizeof(float) * L->fsz * nfields(c.kind));
+  const char* ax = mem_axes(c.kind);
+  const int nm = (int)strlen(ax);
+  for (int m = 0; m < 18; ++m) { L->off_mem[m] = 0; L->mem_sz[m] = 0; }
+  for (int m = 0; m < nm; ++m) {
+    size_t n = 0;
+    if (ax[m] == 'x') n = (size_t)c.ny * c.nz * 2 * c.npml;
+    else if (ax[m] == 'y') n = (size_t)c.nz * 2 * c.npml * L->P;
+    else n = (size_t)2 * c.npml * c.ny * L->P;
+    L->off_mem[m] = o; L->mem_sz[m] = n;
+    o += align256(sizeof(float) * n);
+  }
+  L->coef_plane = (size_t)L->P * c.nz;
+  L->off_coef = o; o += align256(sizeof(float) * L->coef_plane * ncoef(c.kind));
+  const int nax = is3(c.kind) ? 3 : 2;
+  const int lens[3] = {c.nx, is3(c.kind) ? c.ny : c.nz, c.nz};
+  for (int a = 0; a < 3; ++a) L->off_axis[a] = 0;
+  for (int a = 0; a < nax; ++a) { L->off_axis[a] = o; o += align256(sizeof(float) * 6 * lens[a]); }
+  L->off_q3 = o; o += align256(sizeof(float) * c.nz);
+  L->off_src = o; o += align256(sizeof(float) * (size_t)nchan(c.kind) * c.nstep);
+  L->off_rec = o; o += align256(sizeof(int) * 3 * (size_t)std::max(1, c.nrec));
+  L->off_traces = o; o += align256(sizeof(float) * (size_t)c.nstep * nchan(c.kind) * std::max(1, c.nrec));
+  L->off_slots = o; o += align256(sizeof(float) * L->nslots);
+  L->total = o;
+}
+
+}  // namespace
+
+struct sfd_handle_s {
+  sfd_config cfg;
+  Layout L;
+  char* base;
+  cudaStream_t stream;       // caller's stream
+  cudaStream_t cap_stream;   // private stream used only to capture graphs
+  cudaGraphExec_t graph = nullptr;
+  bool have_model = false, have_cpml = false;
+  int64_t step = 0;
+  std::vector<double> src_scale[3];  // planes the source amplitude is divided by
+  Em2Args em2;
+  Seis2Args s2;
+  Seis25Args s25;
+  Em25Args em25;
+  Launch launch;
+  float* f(int q) const { return (float*)(base + L.off_fields) + (size_t)q * L.fsz; }
+  float* m(int q) const { return (float*)(base + L.off_mem[q]); }
+  float* coef(int q) const { return (float*)(base + L.off_coef) + (size_t)q * L.coef_plane; }
+  float* axis(int a) const { return (float*)(base + L.off_axis[a]); }
+  IoArgs io() const {
+    IoArgs io;
+    io.ctl = (Ctl*)(base + L.off_ctl);
+    io.slots = (float*)(base + L.off_slots);
+    io.src = (const float*)(base + L.off_src);
+    io.nstep = cfg.nstep;
+    io.si = io.sj = io.sk = -1;
+    io.rec = (const int*)(base + L.off_rec);
+    io.nrec = cfg.nrec;
+    io.traces = (float*)(base + L.off_traces);
+    return io;
+  }
+};
+
+namespace {
+
+void bind_args(sfd_handle* h) {
+  const Layout& L = h->L;
+  const sfd_config& c = h->cfg;
+  const int NX = c.nx, NY = c.ny, NZ = c.nz;
+  const IoArgs io = h->io();
+  switch (c.kind) {
+    case SFD_ELECTROMAG2: {
+      Em2Args& a = h->em2;
+      a.NX = NX; a.NZ = NZ; a.P = L.P; a.W = L.W;
+      a.Ex = h->f(0); a.Ez = h->f(1); a.Hy = h->f(2);
+      a.mExz = h->m(0); a.mEzx = h->m(1); a.mHyz = h->m(2); a.mHyx = h->m(3);
+      a.caEx = h->coef(0); a.cbEx = h->coef(1); a.caEz = h->coef(2); a.cbEz = h->coef(3);
+      a.X = make_axis(h->axis(0), NX); a.Z = make_axis(h->axis(1), NZ);
+      a.dbH = (float)(c.dt / kMu0);
+      a.io = io;
+      h->launch = em2_launch(a);
+      break;
+    }
+    case SFD_SEISMIC2: {
+      Seis2Args& a = h->s2;
+      a.NX = NX; a.NZ = NZ; a.P = L.P; a.W = L.W; a.atten = 0;
+      a.vx = h->f(0); a.vz = h->f(1); a.sxx = h->f(2); a.szz = h->f(3); a.sxz = h->f(4);
+      a.m_vxx = h->m(0); a.m_vzz = h->m(1); a.m_vxz = h->m(2); a.m_vzx = h->m(3);
+      a.m_sxx_x = h->m(4); a.m_szz_z = h->m(5); a.m_sxz_x = h->m(6); a.m_sxz_z = h->m(7);
+      a.c11 = h->coef(0); a.c13 = h->coef(1); a.c15 = h->coef(2); a.c33 = h->coef(3); a.c35 = h->coef(4);
+      a.c55 = h->coef(5); a.dtrx = h->coef(6); a.dtrz = h->coef(7); a.gxp = h->coef(8); a.gzp = h->coef(9);
+      a.q3 = (const float*)(h->base + L.off_q3);
+      a.X = make_axis(h->axis(0), NX); a.Z = make_axis(h->axis(1), NZ);
+      a.io = io;
+      h->launch = seis2_launch(a);
+      break;
+    }
+    case SFD_SEISMIC25: {
+      Seis25Args& a = h->s25;
+      a.NX = NX; a.NY = NY; a.NZ = NZ; a.P = L.P; a.W = L.W; a.atten = 0;
+      float** F[9] = {&a.vx, &a.vy, &a.vz, &a.sxx, &a.syy, &a.szz, &a.sxy, &a.sxz, &a.syz};
+      for (int q = 0; q < 9; ++q) *F[q] = h->f(q);
+      // oracle order: dvx_dx dvx_dy dvx_dz dvy_dx dvy_dy dvy_dz dvz_dx dvz_dy dvz_dz
+      a.m_vx_x = h->m(0); a.m_vx_y = h->m(1); a.m_vx_z = h->m(2);
+      a.m_vy_x = h->m(3); a.m_vy_y = h->m(4); a.m_vy_z = h->m(5);
+      a.m_vz_x = h->m(6); a.m_vz_y = h->m(7); a.m_vz_z = h->m(8);
+      // dsxx_dx dsyy_dy dszz_dz dsxy_dx dsxy_dy dsxz_dx dsxz_dz dsyz_dy dsyz_dz
+      a.m_sxx_x = h->m(9); a.m_syy_y = h->m(10); a.m_szz_z = h->m(11); a.m_sxy_x = h->m(12);
+      a.m_sxy_y = h->m(13); a.m_sxz_x = h->m(14); a.m_sxz_z = h->m(15); a.m_syz_y = h->m(16);
+      a.m_syz_z = h->m(17);
+      a.C = h->coef(0); a.dtr = h->coef(21); a.gp = h->coef(24);
+      a.X = make_axis(h->axis(0), NX); a.Y = make_axis(h->axis(1), NY); a.Z = make_axis(h->axis(2), NZ);
+      a.idx = (float)(1.0 / c.dx); a.idz = (float)(1.0 / c.dz);
+      a.ysplit = L.ysplit;
+      a.io = io;
+      h->launch = seis25_launch(a);
+      break;
+    }
+    case SFD_ELECTROMAG25: {
+      Em25Args& a = h->em25;
+      a.NX = NX; a.NY = NY; a.NZ = NZ; a.P = L.P; a.W = L.W;
+      a.Ex = h->f(0); a.Ey = h->f(1); a.Ez = h->f(2); a.Hx = h->f(3); a.Hy = h->f(4); a.Hz = h->f(5);
+      a.mEz_y = h->m(0); a.mEy_z = h->m(1); a.mEx_z = h->m(2); a.mEz_x = h->m(3); a.mEx_y = h->m(4);
+      a.mEy_x = h->m(5); a.mHz_y = h->m(6); a.mHy_z = h->m(7); a.mHz_x = h->m(8); a.mHx_z = h->m(9);
+      a.mHx_y = h->m(10); a.mHy_x = h->m(11);
+      a.caEx = h->coef(0); a.cbEx = h->coef(1); a.caEy = h->coef(2); a.cbEy = h->coef(3);
+      a.caEz = h->coef(4); a.cbEz = h->coef(5);
+      a.X = make_axis(h->axis(0), NX); a.Y = make_axis(h->axis(1), NY); a.Z = make_axis(h->axis(2), NZ);
+      a.dbH = (float)(c.dt / kMu0);
+      a.ysplit = L.ysplit;
+      a.io = io;
+      h->launch = em25_launch(a);
+      break;
+    }
+  }
+}
+
+void set_io_source(sfd_handle* h, int i, int j, int k) {
+  h->em2.io.si = h->s2.io.si = h->s25.io.si = h->em25.io.si = i;
+  h->em2.io.sj = h->s2.io.sj = h->s25.io.sj = h->em25.io.sj = j;
+  h->em2.io.sk = h->s2.io.sk = h->s25.io.sk = h->em25.io.sk = k;
+}
+
+void launch_half(sfd_handle* h, int which, int rel, cudaStream_t s) {
+  const Launch& L = h->launch;
+  switch (h->cfg.kind) {
+    case SFD_ELECTROMAG2: which == 0 ? em2_half1(h->em2, L, rel, s) : em2_half2(h->em2, L, rel, s); break;
+    case SFD_SEISMIC2: which == 0 ? seis2_half1(h->s2, L, rel, s) : seis2_half2(h->s2, L, rel, s); break;
+    case SFD_SEISMIC25: which == 0 ? seis25_half1(h->s25, L, rel, s) : seis25_half2(h->s25, L, rel, s); break;
+    case SFD_ELECTROMAG25: which == 0 ? em25_half1(h->em25, L, rel, s) : em25_half2(h->em25, L, rel, s); break;
+  }
+}
+
+void launch_finalize(sfd_handle* h, int t_last, cudaStream_t s) {
+  switch (h->cfg.kind) {
+    case SFD_ELECTROMAG2: em2_finalize(h->em2, t_last, s); break;
+    case SFD_SEISMIC2: seis2_finalize(h->s2, t_last, s); break;
+    case SFD_SEISMIC25: seis25_finalize(h->s25, t_last, s); break;
+    case SFD_ELECTROMAG25: em25_finalize(h->em25, t_last, s); break;
+  }
+}
+
+int ensure_graph(sfd_handle* h) {
+  if (h->graph) return SFD_OK;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
+  for (int s = 0; s < kGraphSteps; ++s) {
+    launch_half(h, 0, s, h->cap_stream);
+    launch_half(h, 1, s, h->cap_stream);
+  }
+  k_advance<<<1, 1, 0, h->cap_stream>>>((Ctl*)(h->base + h->L.off_ctl), kGraphSteps);
+  cudaError_t e = cudaStreamEndCapture(h->cap_stream, &g);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&h->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) { h->graph = nullptr; return cuda_fail(e, "cudaGraphInstantiate"); }
+  return SFD_OK;
+}
+
+void invalidate_graph(sfd_handle* h) {
+  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+}
+
+// Host FP64 -> device FP32 with row pitch P (rows of NX values).
+int upload_pitched(sfd_handle* h, float* dst, const std::vector<float>& src, int rows) {
+  CK(cudaMemcpy2DAsync(dst, sizeof(float) * h->L.P, src.data(), sizeof(float) * h->cfg.nx,
+                       sizeof(float) * h->cfg.nx, rows, cudaMemcpyHostToDevice, h->stream));
+  return SFD_OK;
+}
+
+bool check_strip(const double* v, int n, int W) {
+  for (int i = W; i < n - W; ++i)
+    if (v[i] != 0.0) return false;
+  return true;
+}
+
+bool all_finite(const double* v, size_t n) {
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(v[i])) return false;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t sfd_version(void) { return 100; }
+
+const char* sfd_last_error(void) { return g_err.c_str(); }
+
+int32_t sfd_model_planes(int32_t kind) { return nplanes(kind); }
+int32_t sfd_num_fields(int32_t kind) { return nfields(kind); }
+int32_t sfd_num_channels(int32_t kind) { return nfields(kind) ? nchan(kind) : 0; }
+int32_t sfd_num_memory(int32_t kind) { return (int32_t)strlen(mem_axes(kind)); }
+
+int32_t sfd_state_bytes(const sfd_config* cfg, size_t* bytes) {
+  g_err.clear();
+  int r = validate_cfg(cfg);
+  if (r) return r;
+  if (!bytes) return fail(SFD_ERR_BAD_ARG, "bytes is NULL");
+  Layout L;
+  make_layout(*cfg, &L);
+  *bytes = L.total;
+  return SFD_OK;
+}
+
+int32_t sfd_create(const sfd_config* cfg, void* dev_state, size_t state_bytes, void* stream, sfd_handle** out) {
+  g_err.clear();
+  int r = validate_cfg(cfg);
+  if (r) return r;
+  if (!out) return fail(SFD_ERR_BAD_ARG, "out is NULL");
+  *out = nullptr;
+  Layout L;
+  make_layout(*cfg, &L);
+  if (!dev_state) return fail(SFD_ERR_BAD_ARG, "device state buffer is NULL");
+  if (((uintptr_t)dev_state & 255) != 0) return fail(SFD_ERR_BAD_ARG, "device state buffer must be 256-byte aligned");
+  if (state_bytes < L.total)
+    return fail(SFD_ERR_BAD_ARG, "device state buffer has %zu bytes, needs %zu", state_bytes, L.total);
+  cudaPointerAttributes attr;
+  cudaError_t e = cudaPointerGetAttributes(&attr, dev_state);
+  if (e != cudaSuccess || attr.type != cudaMemoryTypeDevice) {
+    cudaGetLastError();
+    return fail(SFD_ERR_BAD_ARG, "state buffer is not device memory");
+  }
+  sfd_handle* h = new sfd_handle_s();
+  h->cfg = *cfg;
+  h->L = L;
+  h->base = (char*)dev_state;
+  h->stream = (cudaStream_t)stream;
+  e = cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaStreamCreateWithFlags"); }
+  bind_args(h);
+  e = cudaMemsetAsync(h->base, 0, L.total, h->stream);
+  if (e != cudaSuccess) { cudaStreamDestroy(h->cap_stream); delete h; return cuda_fail(e, "cudaMemsetAsync"); }
+  *out = h;
+  return SFD_OK;
+}
+
+int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
+  g_err.clear();
+  if (!h || !planes) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  const sfd_config& c = h->cfg;
+  const int NX = c.nx, NZ = c.nz;
+  const size_t N2 = (size_t)NX * NZ;
+  const int np = nplanes(c.kind);
+  if (count != (int64_t)np * (int64_t)N2)
+    return fail(SFD_ERR_BAD_ARG, "model needs %d planes of %dx%d = %lld values, got %lld", np, NX, NZ,
+                (long long)np * (long long)N2, (long long)count);
+  if (!all_finite(planes, (size_t)count)) return fail(SFD_ERR_BAD_ARG, "model contains NaN or Inf");
+  const double dt = c.dt;
+  auto P = [&](int q) { return planes + (size_t)q * N2; };
+  auto at = [&](const double* p, int i, int k) { return p[(size_t)i + (size_t)NX * k]; };
+  std::vector<std::vector<float>> out(ncoef(c.kind), std::vector<float>(N2, 0.0f));
+  int atten = 0;
+  switch (c.kind) {
+    case SFD_ELECTROMAG2: {
+      // electromagfdtd.f95:164-181
+      const double *e11 = P(0), *e13 = P(1), *e33 = P(2), *s11 = P(3), *s13 = P(4), *s33 = P(5);
+      for (size_t q = 0; q < N2; ++q) {
+        const double ex = (e11[q] + e13[q]) * kEps0, ez = (e13[q] + e33[q]) * kEps0;
+        const double sx = s11[q] + s13[q], sz = s13[q] + s33[q];
+        if (!(ex > 0) || !(ez > 0)) return fail(SFD_ERR_BAD_ARG, "permittivity must be positive (cell %zu)", q);
+        out[0][q] = (float)((1.0 - sx * dt / (2.0 * ex)) / (1.0 + sx * dt / (2.0 * ex)));
+        out[1][q] = (float)((dt / ex) / (1.0 + sx * dt / (2.0 * ex)));
+        out[2][q] = (float)((1.0 - sz * dt / (2.0 * ez)) / (1.0 + sz * dt / (2.0 * ez)));
+        out[3][q] = (float)((dt / ez) / (1.0 + sz * dt / (2.0 * ez)));
+      }
+      h->src_scale[0].assign(e11, e11 + N2);
+      h->src_scale[1].assign(e33, e33 + N2);
+      break;
+    }
+    case SFD_ELECTROMAG25: {
+      // electromagfdtd.f95:756-789
+      const double *e11 = P(0), *e12 = P(1), *e13 = P(2), *e22 = P(3), *e23 = P(4), *e33 = P(5);
+      const double *s11 = P(6), *s12 = P(7), *s13 = P(8), *s22 = P(9), *s23 = P(10), *s33 = P(11);
+      for (size_t q = 0; q < N2; ++q) {
+        const double ep[3] = {(e11[q] + e12[q] + e13[q]) * kEps0, (e12[q] + e22[q] + e23[q]) * kEps0,
+                              (e13[q] + e23[q] + e33[q]) * kEps0};
+        const double sg[3] = {s11[q] + s12[q] + s13[q], s12[q] + s22[q] + s23[q], s13[q] + s23[q] + s33[q]};
+        for (int d = 0; d < 3; ++d) {
+          if (!(ep[d] > 0)) return fail(SFD_ERR_BAD_ARG, "permittivity must be positive (cell %zu)", q);
+          out[2 * d][q] = (float)((1.0 - sg[d] * dt / (2.0 * ep[d])) / (1.0 + sg[d] * dt / (2.0 * ep[d])));
+          out[2 * d + 1][q] = (float)((dt / ep[d]) / (1.0 + sg[d] * dt / (2.0 * ep[d])));
+        }
+      }
+      h->src_scale[0].assign(e11, e11 + N2);
+      h->src_scale[1].assign(e22, e22 + N2);
+      h->src_scale[2].assign(e33, e33 + N2);
+      break;
+    }
+    case SFD_SEISMIC2: {
+      const double *rho = P(6), *gx = P(7), *gz = P(8);
+      for (int q = 0; q < 6; ++q)
+        for (size_t n = 0; n < N2; ++n) out[q][n] = (float)(P(q)[n] * dt);
+      for (size_t n = 0; n < N2; ++n)
+        if (!(rho[n] > 0)) return fail(SFD_ERR_BAD_ARG, "density must be positive (cell %zu)", n);
+      for (int k = 0; k < NZ; ++k)
+        for (int i = 0; i < NX; ++i) {
+          const size_t n = (size_t)i + (size_t)NX * k;
+          out[6][n] = (float)(dt / rho[n]);  // seismicfdtd.f95:334
+          if (i <= NX - 2 && k <= NZ - 2)    // seismicfdtd.f95:341, 355
+            out[7][n] = (float)(dt / ((2 * rho[n] + at(rho, i + 1, k) + at(rho, i, k + 1)) / 4));
+          out[8][n] = (float)(1.0 - gx[n]);
+          out[9][n] = (float)(1.0 - gz[n]);
+          if (gx[n] != 0.0 || gz[n] != 0.0) atten = 1;
+        }
+      h->src_scale[0].assign(rho, rho + N2);
+      h->src_scale[1].assign(rho, rho + N2);
+      h->s2.atten = atten;
+      break;
+    }
+    case SFD_SEISMIC25: {
+      const double* rho = P(21);
+      for (int q = 0; q < 21; ++q)
+        for (size_t n = 0; n < N2; ++n) out[q][n] = (float)(P(q)[n] * dt);
+      for (size_t n = 0; n < N2; ++n)
+        if (!(rho[n] > 0)) return fail(SFD_ERR_BAD_ARG, "density must be positive (cell %zu)", n);
+      for (int k = 0; k < NZ; ++k)
+        for (int i = 0; i < NX; ++i) {
+          const size_t n = (size_t)i + (size_t)NX * k;
+          const double r = rho[n];
+          if (i >= 1 && k >= 1)  // seismicfdtd.f95:826
+            out[21][n] = (float)(dt / ((4 * r + at(rho, i - 1, k) + at(rho, i, k - 1)) / 6));
+          if (i <= NX - 2 && k >= 1)  // :851
+            out[22][n] = (float)(dt / ((4 * r + at(rho, i + 1, k) + at(rho, i, k - 1)) / 6));
+          if (i <= NX - 2 && k <= NZ - 2)  // :877
+            out[23][n] = (float)(dt / ((at(rho, i + 1, k) + at(rho, i, k + 1) + 4 * r) / 6));
+          for (int d = 0; d < 3; ++d) {
+            const double g = P(22 + d)[n];
+            out[24 + d][n] = (float)(1.0 - g);
+            if (g != 0.0) atten = 1;
+          }
+        }
+      for (int d = 0; d < 3; ++d) h->src_scale[d].assign(rho, rho + N2);
+      h->s25.atten = atten;
+      break;
+    }
+  }
+  for (int q = 0; q < ncoef(c.kind); ++q) {
+    int r = upload_pitched(h, h->coef(q), out[q], NZ);
+    if (r) return r;
+  }
+  CK(cudaStreamSynchronize(h->stream));  // host vectors go out of scope
+  invalidate_graph(h);                   // kernel arguments (atten) may change
+  h->have_model = true;
+  return SFD_OK;
+}
+
+int32_t sfd_set_cpml(sfd_handle* h, const double* prof, int64_t count) {
+  g_err.clear();
+  if (!h || !prof) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  const sfd_config& c = h->cfg;
+  const bool three = is3(c.kind);
+  const int lens[3] = {c.nx, three ? c.ny : c.nz, c.nz};
+  const double deltas[3] = {c.dx, three ? c.dy : c.dz, c.dz};
+  const int nax = three ? 3 : 2;
+  int64_t need = 0;
+  for (int a = 0; a < nax; ++a) need += 6LL * lens[a];
+  if (count != need) return fail(SFD_ERR_BAD_ARG, "CPML profiles need %lld values, got %lld", (long long)need, (long long)count);
+  if (!all_finite(prof, (size_t)count)) return fail(SFD_ERR_BAD_ARG, "CPML profiles contain NaN or Inf");
+  const double* p = prof;
+  std::vector<float> q3(c.nz, 0.0f);
+  for (int a = 0; a < nax; ++a) {
+    const int n = lens[a];
+    const double *K = p, *A = p + n, *B = p + 2 * n, *Kh = p + 3 * n, *Ah = p + 4 * n, *Bh = p + 5 * n;
+    p += 6 * n;
+    static const char* nm = "xyz";
+    const char axn = three ? nm[a] : (a == 0 ? 'x' : 'z');
+    if (!check_strip(A, n, c.npml) || !check_strip(Ah, n, c.npml))
+      return fail(SFD_ERR_BAD_ARG, "CPML a-coefficients of axis %c are nonzero outside the %d-cell strips", axn, c.npml);
+    for (int i = 0; i < n; ++i)
+      if (!(K[i] > 0) || !(Kh[i] > 0)) return fail(SFD_ERR_BAD_ARG, "CPML kappa of axis %c must be positive", axn);
+    std::vector<float> t(6 * (size_t)n);
+    const double d = deltas[a];
+    for (int i = 0; i < n; ++i) {
+      t[i] = (float)(1.0 / (d * K[i]));
+      t[n + i] = (float)(A[i] / d);
+      t[2 * n + i] = (float)B[i];
+      t[3 * n + i] = (float)(1.0 / (d * Kh[i]));
+      t[4 * n + i] = (float)(Ah[i] / d);
+      t[5 * n + i] = (float)Bh[i];
+    }
+    CK(cudaMemcpyAsync(h->axis(a), t.data(), sizeof(float) * t.size(), cudaMemcpyHostToDevice, h->stream));
+    if (a == 0 && c.kind == SFD_SEISMIC2)  // b_x_half read at the z index, seismicfdtd.f95:255
+      for (int k = 0; k < c.nz; ++k) q3[k] = (k < c.nx) ? (float)Bh[k] : 0.0f;
+    CK(cudaStreamSynchronize(h->stream));
+  }
+  CK(cudaMemcpyAsync(h->base + h->L.off_q3, q3.data(), sizeof(float) * q3.size(), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->have_cpml = true;
+  return SFD_OK;
+}
+
+int32_t sfd_set_source(sfd_handle* h, int32_t i, int32_t j, int32_t k, const double* srcfn, int32_t ncomp,
+                       int32_t nstep) {
+  g_err.clear();
+  if (!h || !srcfn) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  const sfd_config& c = h->cfg;
+  if (!h->have_model) return fail(SFD_ERR_STATE, "sfd_set_source needs the model (sfd_set_model) first");
+  if (ncomp != nchan(c.kind)) return fail(SFD_ERR_BAD_ARG, "source needs %d components, got %d", nchan(c.kind), ncomp);
+  if (nstep < 1 || nstep > c.nstep) return fail(SFD_ERR_BAD_ARG, "source length %d outside [1, %d]", nstep, c.nstep);
+  const bool three = is3(c.kind);
+  if (i < 1 || i > c.nx - 3 || k < 1 || k > c.nz - 3 || (three && (j < 1 || j > c.ny - 3)) || (!three && j != 0))
+    return fail(SFD_ERR_BAD_ARG, "source cell (%d,%d,%d) must lie inside the grid, away from its outer two planes", i, j, k);
+  if (!all_finite(srcfn, (size_t)ncomp * nstep)) return fail(SFD_ERR_BAD_ARG, "source contains NaN or Inf");
+  const size_t n = (size_t)i + (size_t)c.nx * k;
+  std::vector<float> amp((size_t)ncomp * c.nstep, 0.0f);
+  for (int q = 0; q < ncomp; ++q) {
+    const double s = h->src_scale[q][n];
+    for (int t = 0; t < nstep; ++t) amp[(size_t)q * c.nstep + t] = (float)(srcfn[(size_t)q * nstep + t] * c.dt / s);
+  }
+  CK(cudaMemcpyAsync(h->base + h->L.off_src, amp.data(), sizeof(float) * amp.size(), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  set_io_source(h, i, j, k);
+  invalidate_graph(h);
+  return SFD_OK;
+}
+
+int32_t sfd_set_receivers(sfd_handle* h, const int32_t* ijk, int32_t nrec) {
+  g_err.clear();
+  if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
+  const sfd_config& c = h->cfg;
+  if (nrec != c.nrec) return fail(SFD_ERR_BAD_ARG, "configured for %d receivers, got %d", c.nrec, nrec);
+  if (nrec == 0) return SFD_OK;
+  if (!ijk) return fail(SFD_ERR_BAD_ARG, "NULL receiver array");
+  for (int r = 0; r < nrec; ++r) {
+    const int i = ijk[3 * r], j = ijk[3 * r + 1], k = ijk[3 * r + 2];
+    if (i < 0 || i >= c.nx || j < 0 || j >= c.ny || k < 0 || k >= c.nz)
+      return fail(SFD_ERR_BAD_ARG, "receiver %d at (%d,%d,%d) is outside the grid", r, i, j, k);
+  }
+  CK(cudaMemcpyAsync(h->base + h->L.off_rec, ijk, sizeof(int) * 3 * (size_t)nrec, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return SFD_OK;
+}
+
+int32_t sfd_reset(sfd_handle* h) {
+  g_err.clear();
+  if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
+  const Layout& L = h->L;
+  CK(cudaMemsetAsync(h->base + L.off_fields, 0, L.off_coef - L.off_fields, h->stream));
+  CK(cudaMemsetAsync(h->base + L.off_traces, 0, L.off_slots - L.off_traces, h->stream));
+  h->step = 0;
+  return SFD_OK;
+}
+
+int32_t sfd_set_field(sfd_handle* h, int32_t field, const float* host, int64_t count) {
+  g_err.clear();
+  if (!h || !host) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  const sfd_config& c = h->cfg;
+  if (field < 0 || field >= nfields(c.kind)) return fail(SFD_ERR_BAD_ARG, "field %d out of range", field);
+  if (count != (int64_t)c.nx * c.ny * c.nz) return fail(SFD_ERR_BAD_ARG, "field needs %d*%d*%d values", c.nx, c.ny, c.nz);
+  CK(cudaMemcpy2DAsync(h->f(field), sizeof(float) * h->L.P, host, sizeof(float) * c.nx, sizeof(float) * c.nx,
+                       (size_t)c.ny * c.nz, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return SFD_OK;
+}
+
+int32_t sfd_get_field(sfd_handle* h, int32_t field, float* host, int64_t count) {
+  g_err.clear();
+  if (!h || !host) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  const sfd_config& c = h->cfg;
+  if (field < 0 || field >= nfields(c.kind)) return fail(SFD_ERR_BAD_ARG, "field %d out of range", field);
+  if (count != (int64_t)c.nx * c.ny * c.nz) return fail(SFD_ERR_BAD_ARG, "field needs %d*%d*%d values", c.nx, c.ny, c.nz);
+  CK(cudaMemcpy2DAsync(host, sizeof(float) * c.nx, h->f(field), sizeof(float) * h->L.P, sizeof(float) * c.nx,
+                       (size_t)c.ny * c.nz, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return SFD_OK;
+}
+
+int32_t sfd_get_memory(sfd_handle* h, int32_t index, float* host, int64_t count) {
+  g_err.clear();
+  if (!h || !host) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  const sfd_config& c = h->cfg;
+  const char* ax = mem_axes(c.kind);
+  if (index < 0 || index >= (int)strlen(ax)) return fail(SFD_ERR_BAD_ARG, "memory variable %d out of range", index);
+  const int NX = c.nx, NY = c.ny, NZ = c.nz, W = c.npml, P = h->L.P;
+  if (count != (int64_t)NX * NY * NZ) return fail(SFD_ERR_BAD_ARG, "memory variable needs %d*%d*%d values", NX, NY, NZ);
+  std::vector<float> s(h->L.mem_sz[index]);
+  CK(cudaMemcpyAsync(s.data(), h->m(index), sizeof(float) * s.size(), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  auto sidx = [](int i, int n, int W_) { return i < W_ ? i : i - (n - 2 * W_); };
+  auto ins = [](int i, int n, int W_) { return i < W_ || i >= n - W_; };
+  for (int k = 0; k < NZ; ++k)
+    for (int j = 0; j < NY; ++j)
+      for (int i = 0; i < NX; ++i) {
+        float v = 0.0f;
+        if (ax[index] == 'x') {
+          if (ins(i, NX, W)) v = s[((size_t)k * NY + j) * 2 * W + sidx(i, NX, W)];
+        } else if (ax[index] == 'y') {
+          if (ins(j, NY, W)) v = s[((size_t)k * 2 * W + sidx(j, NY, W)) * P + i];
+        } else {
+          if (ins(k, NZ, W)) v = s[((size_t)sidx(k, NZ, W) * NY + j) * P + i];
+        }
+        host[(size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * k)] = v;
+      }
+  return SFD_OK;
+}
+
+int32_t sfd_run(sfd_handle* h, int64_t nsteps) {
+  g_err.clear();
+  if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
+  if (!h->have_model || !h->have_cpml) return fail(SFD_ERR_STATE, "sfd_run needs sfd_set_model and sfd_set_cpml first");
+  if (nsteps < 0) return fail(SFD_ERR_BAD_ARG, "nsteps must be >= 0");
+  if (h->step + nsteps > h->cfg.nstep)
+    return fail(SFD_ERR_BAD_ARG, "run to step %lld exceeds the %d source samples", (long long)(h->step + nsteps), h->cfg.nstep);
+  if (nsteps == 0) return SFD_OK;
+  const Layout& L = h->L;
+  Ctl* ctl = (Ctl*)(h->base + L.off_ctl);
+  float* slots = (float*)(h->base + L.off_slots);
+  k_begin<<<std::min(1024, (L.nslots + 255) / 256 + 1), 256, 0, h->stream>>>(ctl, slots, L.nslots, (int)h->step);
+  const int64_t chunks = nsteps / kGraphSteps;
+  const int rem = (int)(nsteps % kGraphSteps);
+  if (chunks > 0) {
+    int r = ensure_graph(h);
+    if (r) return r;
+    for (int64_t q = 0; q < chunks; ++q) CK(cudaGraphLaunch(h->graph, h->stream));
+  }
+  for (int s = 0; s < rem; ++s) {
+    launch_half(h, 0, s, h->stream);
+    launch_half(h, 1, s, h->stream);
+  }
+  launch_finalize(h, (int)(h->step + nsteps - 1), h->stream);
+  k_reduce_slots<<<1, 1024, 0, h->stream>>>(ctl, slots, L.nslots);
+  CK(cudaGetLastError());
+  h->step += nsteps;
+  return SFD_OK;
+}
+
+int32_t sfd_status(sfd_handle* h, int64_t* step, double* maxnorm) {
+  g_err.clear();
+  if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
+  Ctl ctl;
+  CK(cudaMemcpyAsync(&ctl, h->base + h->L.off_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (step) *step = h->step;
+  if (maxnorm) *maxnorm = (double)ctl.maxnorm;
+  if (!(ctl.maxnorm <= 1.0e25f))
+    return fail(SFD_ERR_UNSTABLE, "field norm %g exceeded 1e25 (code became unstable and blew up)", (double)ctl.maxnorm);
+  return SFD_OK;
+}
+
+int32_t sfd_get_traces(sfd_handle* h, float* host, int64_t count) {
+  g_err.clear();
+  if (!h || !host) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  const sfd_config& c = h->cfg;
+  const int64_t n = (int64_t)c.nstep * nchan(c.kind) * c.nrec;
+  if (count != n) return fail(SFD_ERR_BAD_ARG, "traces hold %lld values, got %lld", (long long)n, (long long)count);
+  if (n == 0) return SFD_OK;
+  CK(cudaMemcpyAsync(host, h->base + h->L.off_traces, sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return SFD_OK;
+}
+
+const float* sfd_traces_device(const sfd_handle* h) {
+  return h ? (const float*)(h->base + h->L.off_traces) : nullptr;
+}
+
+int32_t sfd_destroy(sfd_handle* h) {
+  g_err.clear();
+  if (!h) return SFD_OK;
+  cudaStreamSynchronize(h->stream);
+  invalidate_graph(h);
+  if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+  delete h;
+  return SFD_OK;
+}
+
+}  // extern "C"

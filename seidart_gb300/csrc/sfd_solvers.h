@@ -1,0 +1,104 @@
+// Host-side argument blocks and launchers of the four solvers.  One struct per
+// solver holds the device pointers of a handle; kernels take it by value.
+#pragma once
+#include <cuda_runtime.h>
+#include "sfd_common.cuh"
+
+namespace sfd {
+
+// Receivers + traces + control shared by all solvers.
+struct IoArgs {
+  Ctl* ctl;
+  float* slots;       // one norm slot per block of the second half-step kernel
+  const float* src;   // [ncomp][nstep] amplitudes already scaled by dt/rho or dt/eps
+  int nstep;
+  int si, sj, sk;     // source cell
+  const int* rec;     // [nrec][3]
+  int nrec;
+  float* traces;      // [nstep][nch][nrec]
+};
+
+struct Em2Args {
+  int NX, NZ, P, W;
+  float *Ex, *Ez, *Hy;
+  float *mExz, *mEzx, *mHyz, *mHyx;  // z-, x-, z-, x-strip
+  const float *caEx, *cbEx, *caEz, *cbEz;
+  AxisTab X, Z;
+  float dbH;
+  IoArgs io;
+};
+
+struct Seis2Args {
+  int NX, NZ, P, W;
+  int atten;
+  float *vx, *vz, *sxx, *szz, *sxz;
+  float *m_vxx, *m_vzz, *m_vxz, *m_vzx;      // x, z, z, x strips
+  float *m_sxx_x, *m_szz_z, *m_sxz_x, *m_sxz_z;  // x, z, x, z strips
+  const float *c11, *c13, *c15, *c33, *c35, *c55;  // stiffness * dt
+  const float *dtrx, *dtrz;                      // dt / rho, dt / rho_avg
+  const float *gxp, *gzp;                        // 1 - gamma
+  const float* q3;                               // b_x_half indexed by the z index
+  AxisTab X, Z;
+  IoArgs io;
+};
+
+struct Seis25Args {
+  int NX, NY, NZ, P, W;
+  int atten;
+  float *vx, *vy, *vz, *sxx, *syy, *szz, *sxy, *sxz, *syz;
+  // velocity-gradient memory (shared by the four stress loops)
+  float *m_vx_x, *m_vy_x, *m_vz_x;  // x-strip
+  float *m_vx_y, *m_vy_y, *m_vz_y;  // y-strip
+  float *m_vx_z, *m_vy_z, *m_vz_z;  // z-strip
+  // stress-gradient memory
+  float *m_sxx_x, *m_sxy_x, *m_sxz_x;  // x-strip
+  float *m_syy_y, *m_sxy_y, *m_syz_y;  // y-strip
+  float *m_szz_z, *m_sxz_z, *m_syz_z;  // z-strip
+  const float* C;     // 21 planes (stiffness * dt), pitch P, NZ rows each
+  const float* dtr;   // 3 planes: dt / rho_avg for vx, vy, vz
+  const float* gp;    // 3 planes: 1 - gamma_x, 1 - gamma_y, 1 - gamma_z
+  AxisTab X, Y, Z;
+  float idx, idz;     // 1/dx, 1/dz for the derivatives :701-707 leaves unscaled
+  int ysplit;         // y segments per column (work split of the y march)
+  IoArgs io;
+};
+
+struct Em25Args {
+  int NX, NY, NZ, P, W;
+  float *Ex, *Ey, *Ez, *Hx, *Hy, *Hz;
+  float *mEz_y, *mEy_z, *mEx_z, *mEz_x, *mEx_y, *mEy_x;
+  float *mHz_y, *mHy_z, *mHz_x, *mHx_z, *mHx_y, *mHy_x;
+  const float *caEx, *cbEx, *caEy, *cbEy, *caEz, *cbEz;
+  AxisTab X, Y, Z;
+  float dbH;
+  int ysplit;
+  IoArgs io;
+};
+
+// Launch geometry of a solver's two half-step kernels.
+struct Launch {
+  dim3 grid, block;
+  int nslots;
+};
+
+Launch em2_launch(const Em2Args& a);
+void em2_half1(const Em2Args& a, const Launch& L, int rel, cudaStream_t s);
+void em2_half2(const Em2Args& a, const Launch& L, int rel, cudaStream_t s);
+void em2_finalize(const Em2Args& a, int t_last, cudaStream_t s);
+
+Launch seis2_launch(const Seis2Args& a);
+void seis2_half1(const Seis2Args& a, const Launch& L, int rel, cudaStream_t s);
+void seis2_half2(const Seis2Args& a, const Launch& L, int rel, cudaStream_t s);
+void seis2_finalize(const Seis2Args& a, int t_last, cudaStream_t s);
+
+Launch seis25_launch(const Seis25Args& a);
+void seis25_half1(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s);
+void seis25_half2(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s);
+void seis25_finalize(const Seis25Args& a, int t_last, cudaStream_t s);
+
+Launch em25_launch(const Em25Args& a);
+void em25_half1(const Em25Args& a, const Launch& L, int rel, cudaStream_t s);
+void em25_half2(const Em25Args& a, const Launch& L, int rel, cudaStream_t s);
+void em25_finalize(const Em25Args& a, int t_last, cudaStream_t s);
+
+}  // namespace sfd

@@ -1,0 +1,228 @@
+"""Python host side of the FDTD backend: one :class:`FDTDSolver` per model/shot.
+
+This mirrors the in-process solver calls of the reference (the f2py
+subroutines ``seismic2``, ``seismic25``, ``electromag2``, ``electromag25`` of
+``legacy/fortran/seismicfdtd.f95`` and ``legacy/fortran/electromagfdtd.f95``,
+called from ``legacy/prjrun_101424.py:691-808``), with the inputs they read
+from ``.dat`` files passed as arrays.  The device state is one torch uint8
+tensor per solver; the kernels are the CUDA library's (no CPU path exists).
+
+Array conventions: materials are float64 arrays ``(planes, NZ, NX)`` (x
+fastest, the Fortran order of the reference's ``.dat`` records); fields are
+``(NZ, NX)`` in 2-D and ``(NZ, NY, NX)`` in 2.5-D; traces are
+``(nstep, channel, receiver)``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import ELECTROMAG2, ELECTROMAG25, SEISMIC2, SEISMIC25, SfdConfig, check
+
+MODEL_PLANES = {
+    SEISMIC2: ["c11", "c13", "c15", "c33", "c35", "c55", "rho", "gamma_x", "gamma_z"],
+    SEISMIC25: ["c11", "c12", "c13", "c14", "c15", "c16", "c22", "c23", "c24", "c25", "c26", "c33", "c34",
+                "c35", "c36", "c44", "c45", "c46", "c55", "c56", "c66", "rho", "gamma_x", "gamma_y", "gamma_z"],
+    ELECTROMAG2: ["eps11", "eps13", "eps33", "sig11", "sig13", "sig33"],
+    ELECTROMAG25: ["eps11", "eps12", "eps13", "eps22", "eps23", "eps33",
+                   "sig11", "sig12", "sig13", "sig22", "sig23", "sig33"],
+}
+FIELDS = {
+    SEISMIC2: ["vx", "vz", "sigmaxx", "sigmazz", "sigmaxz"],
+    SEISMIC25: ["vx", "vy", "vz", "sigmaxx", "sigmayy", "sigmazz", "sigmaxy", "sigmaxz", "sigmayz"],
+    ELECTROMAG2: ["Ex", "Ez", "Hy"],
+    ELECTROMAG25: ["Ex", "Ey", "Ez", "Hx", "Hy", "Hz"],
+}
+CHANNELS = {SEISMIC2: ["vx", "vz"], SEISMIC25: ["vx", "vy", "vz"],
+            ELECTROMAG2: ["Ex", "Ez"], ELECTROMAG25: ["Ex", "Ey", "Ez"]}
+MEMORY = {
+    ELECTROMAG2: ["dEx_dz", "dEz_dx", "dHy_dz", "dHy_dx"],
+    SEISMIC2: ["dvx_dx", "dvz_dz", "dvx_dz", "dvz_dx", "dsigmaxx_dx", "dsigmazz_dz", "dsigmaxz_dx", "dsigmaxz_dz"],
+    SEISMIC25: ["dvx_dx", "dvx_dy", "dvx_dz", "dvy_dx", "dvy_dy", "dvy_dz", "dvz_dx", "dvz_dy", "dvz_dz",
+                "dsigmaxx_dx", "dsigmayy_dy", "dsigmazz_dz", "dsigmaxy_dx", "dsigmaxy_dy", "dsigmaxz_dx",
+                "dsigmaxz_dz", "dsigmayz_dy", "dsigmayz_dz"],
+    ELECTROMAG25: ["dEz_dy", "dEy_dz", "dEx_dz", "dEz_dx", "dEx_dy", "dEy_dx",
+                   "dHz_dy", "dHy_dz", "dHz_dx", "dHx_dz", "dHx_dy", "dHy_dx"],
+}
+
+
+def is_25d(kind: int) -> bool:
+    return kind in (SEISMIC25, ELECTROMAG25)
+
+
+@dataclass
+class GridSpec:
+    """Full grid (CPML included) of one model."""
+    kind: int
+    nx: int
+    nz: int
+    dx: float
+    dz: float
+    dt: float
+    npml: int
+    ny: int = 1
+    dy: float = 1.0
+
+    @property
+    def shape(self):
+        return (self.nz, self.ny, self.nx) if is_25d(self.kind) else (self.nz, self.nx)
+
+    @property
+    def cells(self) -> int:
+        return self.nx * self.ny * self.nz
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class FDTDSolver:
+    """One FDTD model on the GPU, driven through the C ABI.
+
+    ``nstep`` is the number of source samples (the run length); ``nrec`` the
+    number of receivers.  The device state is allocated with torch on
+    ``device`` and bound to the current torch stream of that device.
+    """
+
+    def __init__(self, grid: GridSpec, nstep: int, nrec: int, device="cuda", stream=None):
+        import torch
+
+        self.grid = grid
+        self.kind = grid.kind
+        self.nstep = int(nstep)
+        self.nrec = int(nrec)
+        L = _lib.lib()
+        self._L = L
+        self.cfg = SfdConfig(kind=grid.kind, nx=grid.nx, ny=grid.ny if is_25d(grid.kind) else 1, nz=grid.nz,
+                             npml=grid.npml, nstep=self.nstep, nrec=self.nrec, flags=0,
+                             dx=grid.dx, dy=grid.dy, dz=grid.dz, dt=grid.dt)
+        nbytes = C.c_size_t(0)
+        check(L.sfd_state_bytes(C.byref(self.cfg), C.byref(nbytes)))
+        self.device = torch.device(device)
+        self.state = torch.empty(int(nbytes.value), dtype=torch.uint8, device=self.device)
+        if stream is None:
+            stream = torch.cuda.current_stream(self.device)
+        self.stream = stream
+        h = C.c_void_p()
+        check(L.sfd_create(C.byref(self.cfg), C.c_void_p(self.state.data_ptr()), C.c_size_t(self.state.numel()),
+                           C.c_void_p(stream.cuda_stream), C.byref(h)))
+        self._h = h
+        self.nch = L.sfd_num_channels(grid.kind)
+
+    # -- inputs ------------------------------------------------------------
+    def set_model(self, planes) -> None:
+        """Material planes: array (planes, NZ, NX) or dict name -> (NZ, NX)."""
+        names = MODEL_PLANES[self.kind]
+        if isinstance(planes, dict):
+            zero = np.zeros((self.grid.nz, self.grid.nx))
+            arr = np.stack([np.asarray(planes.get(n, zero), dtype=np.float64) for n in names])
+        else:
+            arr = np.asarray(planes, dtype=np.float64)
+        arr = np.ascontiguousarray(arr)
+        check(self._L.sfd_set_model(self._h, _dptr(arr), arr.size))
+
+    def set_cpml(self, profiles) -> None:
+        """Per-axis CPML profiles: list of cpml.AxisProfile or the packed FP64 vector."""
+        if isinstance(profiles, (list, tuple)):
+            from .cpml import pack_profiles
+            arr = pack_profiles(profiles)
+        else:
+            arr = np.ascontiguousarray(profiles, dtype=np.float64)
+        check(self._L.sfd_set_cpml(self._h, _dptr(arr), arr.size))
+
+    def set_source(self, ijk, srcfn) -> None:
+        """Source cell (i, j, k) (j = 0 in 2-D) and time functions (ncomp, nstep)."""
+        s = np.ascontiguousarray(srcfn, dtype=np.float64)
+        if s.ndim != 2:
+            raise ValueError("srcfn must be (ncomp, nstep)")
+        i, j, k = (int(v) for v in ijk)
+        check(self._L.sfd_set_source(self._h, i, j, k, _dptr(s), s.shape[0], s.shape[1]))
+
+    def set_receivers(self, ijk) -> None:
+        r = np.ascontiguousarray(np.asarray(ijk, dtype=np.int32).reshape(-1, 3))
+        check(self._L.sfd_set_receivers(self._h, r.ctypes.data_as(C.POINTER(C.c_int32)), r.shape[0]))
+
+    def set_field(self, name, values) -> None:
+        q = FIELDS[self.kind].index(name) if isinstance(name, str) else int(name)
+        v = np.ascontiguousarray(values, dtype=np.float32)
+        check(self._L.sfd_set_field(self._h, q, _fptr(v), v.size))
+
+    # -- time stepping -----------------------------------------------------
+    def run(self, nsteps: int) -> None:
+        check(self._L.sfd_run(self._h, int(nsteps)))
+
+    def status(self):
+        """(steps done, largest field norm of the last run); raises UnstableError."""
+        step = C.c_int64(0)
+        norm = C.c_double(0.0)
+        check(self._L.sfd_status(self._h, C.byref(step), C.byref(norm)))
+        return int(step.value), float(norm.value)
+
+    def reset(self) -> None:
+        check(self._L.sfd_reset(self._h))
+
+    # -- outputs -----------------------------------------------------------
+    def field(self, name) -> np.ndarray:
+        q = FIELDS[self.kind].index(name) if isinstance(name, str) else int(name)
+        out = np.empty(self.grid.shape, dtype=np.float32)
+        check(self._L.sfd_get_field(self._h, q, _fptr(out), out.size))
+        return out
+
+    def memory(self, name) -> np.ndarray:
+        q = MEMORY[self.kind].index(name) if isinstance(name, str) else int(name)
+        out = np.empty(self.grid.shape, dtype=np.float32)
+        check(self._L.sfd_get_memory(self._h, q, _fptr(out), out.size))
+        return out
+
+    def traces(self) -> np.ndarray:
+        out = np.empty((self.nstep, self.nch, self.nrec), dtype=np.float32)
+        check(self._L.sfd_get_traces(self._h, _fptr(out), out.size))
+        return out
+
+    def traces_tensor(self):
+        """Device view (nstep, nch, nrec) of the trace buffer (no copy)."""
+        import torch
+        ptr = self._L.sfd_traces_device(self._h)
+        off = int(ptr) - self.state.data_ptr()
+        n = self.nstep * self.nch * self.nrec
+        return self.state[off: off + 4 * n].view(torch.float32).view(self.nstep, self.nch, self.nrec)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.sfd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def run_shot(grid: GridSpec, planes, profiles, src_ijk, srcfn, rec_ijk, nsteps=None, device="cuda"):
+    """One complete shot: model + CPML + source + receivers in, traces out
+    (host arrays both ways).  Raises UnstableError like the Fortran stop."""
+    srcfn = np.asarray(srcfn, dtype=np.float64)
+    nstep = srcfn.shape[1]
+    rec = np.asarray(rec_ijk, dtype=np.int32).reshape(-1, 3)
+    with FDTDSolver(grid, nstep, rec.shape[0], device=device) as s:
+        s.set_model(planes)
+        s.set_cpml(profiles)
+        s.set_source(src_ijk, srcfn)
+        s.set_receivers(rec)
+        s.run(nstep if nsteps is None else nsteps)
+        s.status()
+        return s.traces()

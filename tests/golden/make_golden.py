@@ -1,0 +1,54 @@
+"""Regenerate the golden fixtures of tests/golden/ from the FP64 oracle.
+
+The reference publishes no golden vectors for its solvers and its Fortran
+cannot be compiled here, so these fixtures pin the oracle's own output for a
+few seeded small models (regression anchors for the oracle and parity targets
+for the GPU kernels).  Each .npz stores the case spec, the receiver traces and
+the L2 norm of every final field.
+
+Usage:  python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+from helpers import run_oracle  # noqa: E402
+from seidart_gb300 import ELECTROMAG2, ELECTROMAG25, SEISMIC2, SEISMIC25, KIND_NAMES  # noqa: E402
+from seidart_gb300 import synthetic as sy  # noqa: E402
+
+SPECS = [
+    # kind, seed, nx, nz, ny, npml, nstep
+    (ELECTROMAG2, 11, 41, 35, 1, 6, 150),
+    (SEISMIC2, 11, 41, 35, 1, 6, 150),
+    (SEISMIC25, 11, 33, 27, 19, 5, 80),
+    (ELECTROMAG25, 11, 33, 27, 19, 5, 80),
+]
+
+
+def case_of(spec):
+    kind, seed, nx, nz, ny, npml, nstep = spec
+    return sy.small_case(kind, seed=seed, nx=nx, nz=nz, ny=ny if ny > 1 else 24, npml=npml, nstep=nstep)
+
+
+def path_of(spec):
+    return os.path.join(HERE, f"{KIND_NAMES[spec[0]]}_s{spec[1]}.npz")
+
+
+def main():
+    for spec in SPECS:
+        case = case_of(spec)
+        st, tr, norm, blew = run_oracle(case)
+        assert not blew
+        np.savez_compressed(path_of(spec), spec=np.array(spec, dtype=np.int64), traces=tr,
+                            field_norms=np.array([np.linalg.norm(f) for f in st.fields]), maxnorm=norm)
+        print(path_of(spec), tr.shape)
+
+
+if __name__ == "__main__":
+    main()

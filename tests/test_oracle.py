@@ -1,0 +1,118 @@
+"""CPU tests of the FP64 oracle: agreement of two independent restatements,
+physical known-answer checks, and the blow-up detector."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle import numpy_ref
+from helpers import rel_l2, run_oracle
+from seidart_gb300 import ELECTROMAG2, ELECTROMAG25, SEISMIC2, SEISMIC25
+from seidart_gb300 import cpml as cp
+from seidart_gb300 import synthetic as sy
+from seidart_gb300.solver import GridSpec
+
+
+@pytest.mark.parametrize("kind,fn", [(ELECTROMAG2, numpy_ref.electromag2), (SEISMIC2, numpy_ref.seismic2)])
+@pytest.mark.parametrize("seed,nx,nz", [(1, 37, 29), (2, 26, 41)])
+def test_loop_and_slice_restatements_agree(kind, fn, seed, nx, nz):
+    c = sy.small_case(kind, seed=seed, nx=nx, nz=nz, npml=5, nstep=120)
+    g = c.grid
+    prof = cp.pack_profiles(c.profiles)
+    st, tr, _, blew = run_oracle(c)
+    assert not blew
+    F, M, T = fn(g.nx, g.nz, g.dx, g.dz, g.dt, prof, c.planes, (c.src_ijk[0], c.src_ijk[2]), c.srcfn, c.nstep,
+                 rec=c.rec_ijk)
+    # identical operation order in FP64: agreement to rounding
+    assert rel_l2(st.fields, F) < 1e-13
+    assert rel_l2(st.memory, M, floor=1e-300) < 1e-13
+    assert rel_l2(tr, T) < 1e-13
+
+
+@pytest.mark.parametrize("kind", [ELECTROMAG2, SEISMIC2, SEISMIC25, ELECTROMAG25])
+def test_split_runs_equal_one_run(kind):
+    c = sy.small_case(kind, seed=3, nx=30, nz=26, ny=18, npml=4, nstep=60)
+    st1, tr1, _, _ = run_oracle(c)
+    st2, a, _, _ = run_oracle(c, nsteps=25)
+    st2, b, _, _ = run_oracle(c, nsteps=35, state=st2)
+    assert np.array_equal(st1.fields, st2.fields)
+    assert np.array_equal(tr1, np.concatenate([a, b]))
+
+
+def _homogeneous_em(nx=260, nz=120, eps=4.0, npml=20, nstep=900):
+    d = 0.02
+    v = cp.CLIGHT / math.sqrt(eps)
+    dt = cp.time_step(0.5, v, (d, d))
+    planes = np.stack([np.full((nz, nx), eps), np.zeros((nz, nx)), np.full((nz, nx), eps),
+                       np.zeros((nz, nx)), np.zeros((nz, nx)), np.zeros((nz, nx))])
+    f0 = 600e6
+    prof = cp.build_profiles((nx, nz), (d, d), npml, dt, f0, v, seismic=False)
+    g = GridSpec(ELECTROMAG2, nx, nz, d, d, dt, npml)
+    src = np.zeros((2, nstep))
+    src[1] = sy.ricker(nstep, dt, f0)
+    return g, planes, prof, src, v
+
+
+def test_em_arrival_speed_matches_medium():
+    """Ez pulse in a homogeneous eps_r = 4 medium travels at c/2."""
+    g, planes, prof, src, v = _homogeneous_em()
+    sx, sz = 60, 60
+    rec = np.array([[sx + 40, 0, sz], [sx + 140, 0, sz]], dtype=np.int32)
+    st, tr, _, _ = oracle.run(ELECTROMAG2, g, planes, cp.pack_profiles(prof), (sx, 0, sz), src, rec, src.shape[1])
+    ez = tr[:, 1, :]
+    t1, t2 = (np.argmax(np.abs(ez[:, r])) for r in range(2))
+    vel = (100 * g.dx) / ((t2 - t1) * g.dt)
+    assert abs(vel / v - 1.0) < 0.03
+
+
+def test_elastic_p_arrival_speed_matches_medium():
+    """vz pulse in a homogeneous isotropic solid travels at the P velocity along z."""
+    nx, nz, npml, d = 120, 260, 20, 0.5
+    lam, mu, rho = 4e9, 3e9, 1000.0
+    vp = math.sqrt((lam + 2 * mu) / rho)
+    dt = cp.time_step(0.5, vp, (d, d))
+    nstep = 700
+    f0 = 250.0
+    z = np.zeros((nz, nx))
+    planes = np.stack([z + lam + 2 * mu, z + lam, z, z + lam + 2 * mu, z, z + mu, z + rho, z, z])
+    prof = cp.build_profiles((nx, nz), (d, d), npml, dt, f0, vp, seismic=True)
+    g = GridSpec(SEISMIC2, nx, nz, d, d, dt, npml)
+    src = np.zeros((2, nstep))
+    src[1] = sy.ricker(nstep, dt, f0)
+    rec = np.array([[60, 0, 100], [60, 0, 200]], dtype=np.int32)
+    st, tr, _, _ = oracle.run(SEISMIC2, g, planes, cp.pack_profiles(prof), (60, 0, 60), src, rec, nstep)
+    vz = tr[:, 1, :]
+    t1, t2 = (np.argmax(np.abs(vz[:, r])) for r in range(2))
+    vel = (100 * d) / ((t2 - t1) * dt)
+    assert abs(vel / vp - 1.0) < 0.03
+
+
+def test_em_cpml_absorbs():
+    """After the pulse has left the interior, the CPML has removed almost all of
+    its energy; with the CPML coefficients switched off (a = 0) the Dirichlet
+    box keeps it."""
+    g, planes, prof, src, v = _homogeneous_em(nx=140, nz=140, nstep=1600)
+    packed = cp.pack_profiles(prof)
+    rec = np.zeros((0, 3), dtype=np.int32)
+
+    def energy_after(p):
+        st, _, _, _ = oracle.run(ELECTROMAG2, g, planes, p, (70, 0, 70), src, rec, src.shape[1])
+        return float(np.sum(st.fields[0] ** 2 + st.fields[1] ** 2))
+
+    off = packed.copy()
+    nx, nz = g.nx, g.nz
+    for base, n in ((0, nx), (6 * nx, nz)):
+        for q in (1, 4):  # a, a_half
+            off[base + q * n: base + (q + 1) * n] = 0.0
+        for q in (0, 3):  # K, K_half
+            off[base + q * n: base + (q + 1) * n] = 1.0
+    assert energy_after(packed) < 1e-3 * energy_after(off)
+
+
+def test_blow_up_detected():
+    """dt far above the stability limit: the norm check of seismicfdtd.f95:378-379 fires."""
+    c = sy.small_case(SEISMIC2, seed=5, nx=40, nz=36, npml=5, nstep=400)
+    c.grid.dt *= 4.0
+    _, _, norm, blew = run_oracle(c)
+    assert blew and norm > 1e25
