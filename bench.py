@@ -1,0 +1,441 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the GB300 FDTD backend.
+
+Headline workload (one bench "step" = one complete shot): the 2-D anisotropic
+EM model, electromag2 on a 1000x500 interior + 20-cell CPML (1040x540 cells),
+three seeded random layers, 100 MHz Ricker Ex source, 6000 time steps, 100
+receivers, FP32 fields.  metric = Gcell-updates/s (full grid incl. CPML x
+time steps / wall time).  Inputs are seeded synthetic models with the
+workload's shapes and value ranges (the reference measures nothing public).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm on the host cores: the FP64
+restatement of the legacy Fortran loops (oracle/, OpenMP, all host threads),
+because the reference's own solver cannot be built or run on these machines.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Gcell-updates/s"
+WORKLOAD = "electromag2 plain 1040x540 cells (1000x500 + 20-cell CPML) x 6000 steps, 100 receivers"
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.tmp = None
+
+    def start(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.idx), "-lms", "200"], stdout=self.tmp,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.tmp.flush()
+        rows = [r.split(",") for r in Path(self.tmp.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.tmp.name)
+        sm, mx, reasons = [], [], set()
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for name, val in zip(self.NAMES, r[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes (FP32 = 4 B), per kernel launch and per cell update
+
+def strip_fractions(grid):
+    W = grid.npml
+    fx = min(1.0, 2 * W / grid.nx)
+    fz = min(1.0, 2 * W / grid.nz)
+    fy = min(1.0, 2 * W / grid.ny) if grid.ny > 1 else 0.0
+    return fx, fy, fz
+
+
+def em2_bytes(grid):
+    """electromag2.  H kernel: read Ex Ez Hy, write Hy; psi dEx_dz (z-strip), dEz_dx (x-strip).
+    E kernel: read Hy Ex Ez + caEx cbEx caEz cbEz, write Ex Ez; psi dHy_dz (z), dHy_dx (x).
+    Step (each field read and written once, each coefficient read once): 40 B + strip psi."""
+    fx, _, fz = strip_fractions(grid)
+    cells = grid.nx * grid.nz
+    psi = 8 * (fx + fz)
+    h = (16 + psi) * cells
+    e = (36 + psi) * cells
+    step = (40 + 2 * psi) * cells
+    return {"half1": h, "half2": e, "step": step, "per_cell_step": 40 + 2 * psi}
+
+
+def seis2_bytes(grid, atten=False):
+    """seismic2.  Stress kernel: read vx vz, read+write sxx szz sxz, 6 stiffness; 4 velocity-gradient psi
+    (2 on each strip).  Velocity kernel: read 3 stresses, read+write vx vz, dt/rho x2 (+2 gamma); 4 stress
+    psi.  Step: 5 fields read and written once + 8 (+2) coefficients + psi."""
+    fx, _, fz = strip_fractions(grid)
+    cells = grid.nx * grid.nz
+    g = 8 if atten else 0
+    psi = 16 * (fx + fz)
+    h1 = (8 + 24 + 24 + psi) * cells
+    h2 = (12 + 16 + 8 + g + psi) * cells
+    step = (40 + 32 + g + 2 * psi) * cells
+    return {"half1": h1, "half2": h2, "step": step, "per_cell_step": step / cells}
+
+
+def seis25_bytes(grid, atten=True):
+    """seismic25 with y-marching: coefficients (21 stiffness, 3 dt/rho, 3 gamma) are read once per (x,z)
+    column and amortised over NY.  Stress kernel: read 9 fields, write 6 stresses; velocity kernel: read
+    9 fields, write 3 velocities.  psi: 9 velocity-gradient (3 per axis) and 9 stress-gradient."""
+    fx, fy, fz = strip_fractions(grid)
+    cells = grid.nx * grid.ny * grid.nz
+    col = grid.nx * grid.nz
+    psi_axis = 3 * 8 * (fx + fy + fz)
+    h1 = (9 * 4 + 6 * 4 + psi_axis) * cells + 21 * 4 * col
+    h2 = (9 * 4 + 3 * 4 + psi_axis) * cells + 6 * 4 * col
+    step = (9 * 8 + 2 * psi_axis) * cells + 27 * 4 * col
+    return {"half1": h1, "half2": h2, "step": step, "per_cell_step": step / cells}
+
+
+# ---------------------------------------------------------------------------
+
+def make_solver(case, device):
+    from seidart_gb300.solver import FDTDSolver
+    s = FDTDSolver(case.grid, case.nstep, len(case.rec_ijk), device=device)
+    s.set_model(case.planes)
+    s.set_cpml(case.profiles)
+    s.set_source(case.src_ijk, case.srcfn)
+    s.set_receivers(case.rec_ijk)
+    return s
+
+
+def launches_per_shot(kind, nstep):
+    from seidart_gb300 import ELECTROMAG25
+    # begin + 2 per step + one advance per 32-step graph + finalize (+ H faces for EM25) + slot reduce
+    return 2 * nstep + nstep // 32 + 3 + (1 if kind == ELECTROMAG25 else 0)
+
+
+def time_shots(solver, nstep, K, W, flush, stream, sync_all=None):
+    import torch
+    for _ in range(W):
+        flush.zero_()
+        solver.reset()
+        solver.run(nstep)
+    solver.status()
+    torch.cuda.synchronize()
+    if sync_all:
+        sync_all()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(K):
+        flush.zero_()  # 256 MiB write: evicts the 129 MB L2 between shots
+        solver.reset()
+        solver.run(nstep)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if sync_all:
+        sync_all()
+    solver.status()
+    return ev0.elapsed_time(ev1) / K
+
+
+def kernel_times(solver, stream, n=200):
+    """Average duration (ms) of each half-step kernel launched alone, CUDA events on its stream."""
+    import torch
+    out = []
+    for which in (0, 1):
+        solver.reset()
+        solver.launch_half(which, 10)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        solver.launch_half(which, n)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out.append(e0.elapsed_time(e1) / n)
+    solver.reset()
+    return out
+
+
+def profile_traffic(name):
+    """dram bytes per launch recorded in profiles/<name>.md ("dram_bytes_per_launch: N"), else None."""
+    p = ROOT / "profiles" / f"{name}.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.strip().startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(case, seconds=10.0, chunk=100):
+    """FP64 oracle (restated legacy Fortran loops) on all host threads, time-bounded sample."""
+    import oracle
+    from seidart_gb300 import cpml as cp
+    prof = cp.pack_profiles(case.profiles)
+    st = None
+    done = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds and done + chunk <= case.nstep:
+        st, _, _, _ = oracle.run(case.grid.kind, case.grid, case.planes, prof, case.src_ijk, case.srcfn,
+                                 case.rec_ijk, chunk, state=st)
+        done += chunk
+    el = time.perf_counter() - t0
+    value = case.grid.cells * done / el / 1e9
+    return {"value": round(value, 4), "unit": METRIC, "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"{done} of {case.nstep} steps of the same workload, FP64, OpenMP ({el:.1f} s)"}
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm (FP64 oracle port) on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import oracle
+    from seidart_gb300 import cpml as cp, synthetic as sy
+    oracle.build()
+    case = sy.electromag2_layers(nstep=6000)
+    prof = cp.pack_profiles(case.profiles)
+    chunk = args.ref_chunk
+    st = None
+
+    def step():
+        nonlocal st
+        if st is not None and st.step + chunk > case.nstep:
+            st = None
+        st, _, _, _ = oracle.run(case.grid.kind, case.grid, case.planes, prof, case.src_ijk, case.srcfn,
+                                 case.rec_ijk, chunk, state=st)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    el = time.perf_counter() - t0
+    value = case.grid.cells * chunk * args.steps / el / 1e9
+    sample = f"{chunk} consecutive time steps of the workload per bench step, FP64 restatement of the legacy loops"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": METRIC, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * el / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_steps": chunk},
+        "cpu_baseline": {"value": round(value, 4), "unit": METRIC, "cores": oracle.num_threads(), "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    from seidart_gb300 import ELECTROMAG2, SEISMIC2, SEISMIC25, synthetic as sy
+    from seidart_gb300 import build as b
+    from seidart_gb300.solver import run_shot
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    b.build()
+
+    def sync_all():
+        if dist is not None:
+            dist.barrier()
+
+    stream = torch.cuda.current_stream(device)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
+    peak, peak_kind = _peaks()
+
+    # ---- headline: electromag2 plain, one shot per bench step --------------
+    case = sy.electromag2_layers(nstep=6000)
+    g = case.grid
+    solver = make_solver(case, device)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms = time_shots(solver, case.nstep, args.steps, args.warmup, flush, stream, sync_all)
+    ck = clocks.stop()
+    if dist is not None:
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    cells = g.cells
+    value = world * cells * case.nstep / (ms / 1e3) / 1e9
+    kt = kernel_times(solver, stream) if not args.headline_only else [1.0, 1.0]
+    byts = em2_bytes(g)
+    dom = int(np.argmax(kt))
+    dom_name = ["em2_h_kernel", "em2_e_kernel"][dom]
+    achieved = byts[["half1", "half2"][dom]] / (kt[dom] / 1e3) / 1e9
+    traffic = profile_traffic(f"{dom_name}_1040x540")
+    step_ms = ms / case.nstep
+    roofline = {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peak,
+                "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": int(byts[["half1", "half2"][dom]]),
+                "kernel_ms": [round(x, 5) for x in kt],
+                "note": "state (23 MB) is L2-resident during a shot; fraction is against the HBM copy peak"}
+    step_achieved = byts["step"] / (step_ms / 1e3) / 1e9
+    roofline_step = {"bytes_per_cell_update": round(byts["per_cell_step"], 2),
+                     "achieved": round(step_achieved, 1), "frac": round(step_achieved / peak, 4), "unit": "GB/s"}
+    solver.close()
+
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded layered permittivity/conductivity model)",
+        "config": {"workload": WORKLOAD, "time_steps_per_bench_step": case.nstep, "cells": cells,
+                   "l2": "256 MiB buffer written between shots (flush)", "parallelism": f"replicas x{world}"},
+        "gpu_launches": args.steps * launches_per_shot(ELECTROMAG2, case.nstep),
+        "roofline": roofline, "roofline_step": roofline_step,
+    }
+    if args.headline_only:
+        line.pop("roofline")
+    if ck:
+        line["clocks"] = ck
+
+    # ---- e2e through the public API with host buffers ----------------------
+    if args.e2e_steps > 0:
+        n_e2e = max(1, min(args.steps, args.e2e_steps))
+        run_shot(g, case.planes, case.profiles, case.src_ijk, case.srcfn, case.rec_ijk, device=device)
+        torch.cuda.synchronize()
+        sync_all()
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            tr = run_shot(g, case.planes, case.profiles, case.src_ijk, case.srcfn, case.rec_ijk, device=device)
+        torch.cuda.synchronize()
+        el = (time.perf_counter() - t0) / n_e2e
+        if dist is not None:
+            t = torch.tensor([el], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            el = float(t.item())
+        h2d = 4 * (4 * g.nx * g.nz + 6 * (g.nx + g.nz) + g.nz + 2 * case.nstep + 3 * len(case.rec_ijk))
+        d2h = tr.nbytes + 32
+        line["e2e"] = {"value": round(world * cells * case.nstep / el / 1e9, 3), "unit": METRIC,
+                       "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                       "ms_per_step": round(el * 1e3, 2),
+                       "path": "seidart_gb300.solver.run_shot (host arrays in, host traces out)"}
+
+    # ---- extra lines: the other plain configurations ------------------------
+    if not args.skip_extras:
+        extras = {}
+        c0 = sy.seismic2_firn_ice(nstep=2000)
+        s0 = make_solver(c0, device)
+        ms0 = time_shots(s0, c0.nstep, 5, 2, flush, stream)
+        b0 = seis2_bytes(c0.grid)
+        r0 = c0.grid.cells * c0.nstep / (ms0 / 1e3) / 1e9
+        extras["seismic2_plain"] = {"workload": "seismic2 firn/ice 440x240 cells x 2000 steps",
+                                    "value": round(r0, 3), "unit": METRIC, "ms_per_shot": round(ms0, 3),
+                                    "bytes_per_cell_update": round(b0["per_cell_step"], 1),
+                                    "hbm_frac": round(b0["per_cell_step"] * r0 / peak, 4)}
+        s0.close()
+        c2 = sy.seismic25_ice(nstep=3000)
+        s2 = make_solver(c2, device)
+        ms2 = time_shots(s2, c2.nstep, 2, 1, flush, stream)
+        kt2 = kernel_times(s2, stream, n=20)
+        b2 = seis25_bytes(c2.grid)
+        r2 = c2.grid.cells * c2.nstep / (ms2 / 1e3) / 1e9
+        extras["seismic25_plain"] = {"workload": "seismic25 ice 630x70x330 cells x 3000 steps",
+                                     "value": round(r2, 3), "unit": METRIC, "ms_per_shot": round(ms2, 2),
+                                     "bytes_per_cell_update": round(b2["per_cell_step"], 1),
+                                     "hbm_frac": round(b2["per_cell_step"] * r2 / peak, 4),
+                                     "kernel_ms": [round(x, 4) for x in kt2],
+                                     "kernel_frac": [round(b2[h] / (t / 1e3) / 1e9 / peak, 4)
+                                                     for h, t in zip(("half1", "half2"), kt2)]}
+        s2.close()
+        line["extras"] = extras
+
+    if rank == 0 and not args.skip_cpu:
+        line["cpu_baseline"] = cpu_baseline(case, seconds=args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-chunk", type=int, default=200, help="time steps per reference bench step")
+    ap.add_argument("--skip-extras", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="only the timed headline shots (for profiler runs): no e2e, extras or CPU leg")
+    args = ap.parse_args(argv)
+    if args.headline_only:
+        args.skip_extras = args.skip_cpu = True
+        args.e2e_steps = 0
+    if args.warmup < 3:
+        print("note: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -164,6 +164,12 @@ int32_t sfd_status(sfd_handle* h, int64_t* step, double* maxnorm);
 int32_t sfd_get_traces(sfd_handle* h, float* host, int64_t count);
 const float* sfd_traces_device(const sfd_handle* h);
 
+/* Profiling aid: launch half-step kernel `which` (0 = velocity/H half,
+ * 1 = stress/E half as ordered in the Fortran time loop) `count` times back
+ * to back on the handle's stream without the other half.  The fields are no
+ * longer a valid simulation afterwards; call sfd_reset before the next run. */
+int32_t sfd_launch_half(sfd_handle* h, int32_t which, int32_t count);
+
 /* Release the handle (the caller frees its device buffer afterwards). */
 int32_t sfd_destroy(sfd_handle* h);
 

@@ -23,7 +23,8 @@ EXPORTS = (
     "sfd_version", "sfd_last_error", "sfd_model_planes", "sfd_num_fields", "sfd_num_channels",
     "sfd_num_memory", "sfd_state_bytes", "sfd_create", "sfd_set_model", "sfd_set_cpml",
     "sfd_set_source", "sfd_set_receivers", "sfd_reset", "sfd_set_field", "sfd_get_field",
-    "sfd_get_memory", "sfd_run", "sfd_status", "sfd_get_traces", "sfd_traces_device", "sfd_destroy",
+    "sfd_get_memory", "sfd_run", "sfd_status", "sfd_get_traces", "sfd_traces_device", "sfd_launch_half",
+    "sfd_destroy",
 )
 
 
@@ -78,6 +79,7 @@ def _declare(lib):
         "sfd_status": (i32, [P, C.POINTER(i64), dp]),
         "sfd_get_traces": (i32, [P, fp, i64]),
         "sfd_traces_device": (P, [P]),
+        "sfd_launch_half": (i32, [P, i32, i32]),
         "sfd_destroy": (i32, [P]),
     }
     for name, (res, args) in sig.items():

@@ -741,6 +741,20 @@ int32_t sfd_get_traces(sfd_handle* h, float* host, int64_t count) {
   return SFD_OK;
 }
 
+int32_t sfd_launch_half(sfd_handle* h, int32_t which, int32_t count) {
+  g_err.clear();
+  if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
+  if (which != 0 && which != 1) return fail(SFD_ERR_BAD_ARG, "which must be 0 or 1");
+  if (count < 0) return fail(SFD_ERR_BAD_ARG, "count must be >= 0");
+  if (!h->have_model || !h->have_cpml) return fail(SFD_ERR_STATE, "sfd_launch_half needs sfd_set_model and sfd_set_cpml");
+  const Layout& L = h->L;
+  k_begin<<<std::min(1024, (L.nslots + 255) / 256 + 1), 256, 0, h->stream>>>((Ctl*)(h->base + L.off_ctl),
+                                                                            (float*)(h->base + L.off_slots), L.nslots, 0);
+  for (int q = 0; q < count; ++q) launch_half(h, which, 0, h->stream);
+  CK(cudaGetLastError());
+  return SFD_OK;
+}
+
 const float* sfd_traces_device(const sfd_handle* h) {
   return h ? (const float*)(h->base + h->L.off_traces) : nullptr;
 }

@@ -168,6 +168,11 @@ class FDTDSolver:
     def reset(self) -> None:
         check(self._L.sfd_reset(self._h))
 
+    def launch_half(self, which: int, count: int) -> None:
+        """Profiling aid: run one half-step kernel ``count`` times (state is
+        invalid afterwards; reset before the next run)."""
+        check(self._L.sfd_launch_half(self._h, int(which), int(count)))
+
     # -- outputs -----------------------------------------------------------
     def field(self, name) -> np.ndarray:
         q = FIELDS[self.kind].index(name) if isinstance(name, str) else int(name)
