@@ -61,6 +61,11 @@ extern "C" {
 #define SFD_ERR_UNSTABLE -4 /* field norm above 1e25 or NaN (seismicfdtd.f95:378-379) */
 #define SFD_ERR_TIMEOUT -5  /* a bounded device wait gave up */
 
+/* Flags (sfd_config.flags). */
+#define SFD_FLAG_TWO_PASS 1 /* 2-D kinds: two kernels per step (one per half-step,
+                               fields updated in place) instead of the default
+                               single-pass step over ping-pong copies */
+
 
 typedef struct sfd_config {
   int32_t kind;        /* SFD_SEISMIC2 ... SFD_ELECTROMAG25 */
@@ -68,7 +73,7 @@ typedef struct sfd_config {
   int32_t npml;        /* CPML thickness in cells (npoints_pml) */
   int32_t nstep;       /* length of the source time functions = max steps */
   int32_t nrec;        /* receivers recorded every step */
-  int32_t flags;       /* reserved, must be 0 */
+  int32_t flags;       /* SFD_FLAG_* */
   double dx, dy, dz;   /* grid steps (m); dy ignored in 2-D */
   double dt;           /* time step (s), computed by the caller in FP64 */
 } sfd_config;
@@ -164,14 +169,36 @@ int32_t sfd_status(sfd_handle* h, int64_t* step, double* maxnorm);
 int32_t sfd_get_traces(sfd_handle* h, float* host, int64_t count);
 const float* sfd_traces_device(const sfd_handle* h);
 
-/* Profiling aid: launch half-step kernel `which` (0 = velocity/H half,
- * 1 = stress/E half as ordered in the Fortran time loop) `count` times back
- * to back on the handle's stream without the other half.  The fields are no
- * longer a valid simulation afterwards; call sfd_reset before the next run. */
+/* Profiling aid: launch half-step kernel `which` (0 = first half-step of the
+ * Fortran time loop: H or stress; 1 = second: E or velocity) `count` times
+ * back to back on the handle's stream without the other half.  Single-pass
+ * handles launch their whole-step kernel.  The fields are no longer a valid
+ * simulation afterwards; call sfd_reset before the next run. */
 int32_t sfd_launch_half(sfd_handle* h, int32_t which, int32_t count);
 
 /* Release the handle (the caller frees its device buffer afterwards). */
 int32_t sfd_destroy(sfd_handle* h);
+
+/* ---- Batched runs ----------------------------------------------------------
+ * Many 2-D models (electromag2 shots, seismic2 models of any sizes, mixed)
+ * advance together in one persistent cooperative kernel launch with a grid
+ * barrier per time step.  Replaces the per-shot process loop of the driver
+ * (src/seidart/simulations/common_offset.py:143-284, one seidartfdtd call per
+ * source).  The handles must be single-pass 2-D handles on one stream with
+ * model and CPML set; each keeps its own state, source, receivers and traces.
+ * The batch needs a small device scratch buffer of sfd_batch_scratch_bytes. */
+typedef struct sfd_batch_s sfd_batch;
+int32_t sfd_batch_scratch_bytes(int32_t nmodels, size_t* bytes);
+int32_t sfd_batch_create(sfd_handle* const* handles, int32_t nmodels, void* dev_scratch, size_t bytes,
+                         sfd_batch** out);
+/* Tile rows per thread (1, 2, 4) and resident blocks per SM of the launch. */
+int32_t sfd_batch_set_tiling(sfd_batch* b, int32_t zb, int32_t blocks_per_sm);
+/* Advance every model nsteps steps (asynchronous). */
+int32_t sfd_batch_run(sfd_batch* b, int64_t nsteps);
+/* Synchronise; SFD_ERR_TIMEOUT if the grid barrier gave up, SFD_ERR_UNSTABLE
+ * (with *failed_model) if a model blew up. */
+int32_t sfd_batch_status(sfd_batch* b, int32_t* failed_model);
+int32_t sfd_batch_destroy(sfd_batch* b);
 
 #ifdef __cplusplus
 }

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/seidart_gb300.h"
+#include "batch.h"
 #include "sfd_solvers.h"
 
 namespace sfd {
@@ -130,11 +131,22 @@ int choose_ysplit(const sfd_config& c) {
   return s;
 }
 
+// Number of memory variables that the single-pass 2-D steps keep in two
+// copies (those of the first half-step, re-derived on tile halos).
+int npingpong_mem(int kind) {
+  switch (kind) {
+    case SFD_ELECTROMAG2: return 2;  // dEx_dz dEz_dx
+    case SFD_SEISMIC2: return 4;     // dvx_dx dvz_dz dvx_dz dvz_dx
+  }
+  return 0;
+}
+bool has_single_pass(int kind) { return kind == SFD_ELECTROMAG2 || kind == SFD_SEISMIC2; }
+
 struct Layout {
   int P, NX, NY, NZ, W, ysplit, nslots;
   size_t fsz;                // floats per field
-  size_t off_ctl, off_fields, off_mem[18], mem_sz[18], off_coef, coef_plane, off_axis[3], off_q3, off_src,
-      off_rec, off_traces, off_slots, total;
+  size_t off_ctl, off_fields, off_mem[18], mem_sz[18], off_fieldsB, off_memB[4], off_coef, coef_plane, off_axis[3],
+      off_q3, off_src, off_rec, off_traces, off_slots, total;
 };
 
 int grid_slots(const sfd_config& c, int P, int ysplit) {
@@ -154,7 +166,7 @@ int validate_cfg(const sfd_config* c) {
   if (!three && c->ny != 1) return fail(SFD_ERR_BAD_ARG, "2-D solvers need ny = 1 (got %d)", c->ny);
   if (c->nstep < 1) return fail(SFD_ERR_BAD_ARG, "nstep must be >= 1");
   if (c->nrec < 0) return fail(SFD_ERR_BAD_ARG, "nrec must be >= 0");
-  if (c->flags != 0) return fail(SFD_ERR_BAD_ARG, "flags must be 0");
+  if ((c->flags & ~SFD_FLAG_TWO_PASS) != 0) return fail(SFD_ERR_BAD_ARG, "unknown flags 0x%x", c->flags);
   if (!(c->dt > 0) || !(c->dx > 0) || !(c->dz > 0) || (three && !(c->dy > 0)))
     return fail(SFD_ERR_BAD_ARG, "dt and grid steps must be positive");
   const double cells = (double)c->nx * c->ny * c->nz;
@@ -182,6 +194,12 @@ void make_layout(const sfd_config& c, Layout* L) {
     L->off_mem[m] = o; L->mem_sz[m] = n;
     o += align256(sizeof(float) * n);
   }
+  L->off_fieldsB = 0;
+  for (int m = 0; m < 4; ++m) L->off_memB[m] = 0;
+  if (has_single_pass(c.kind) && !(c.flags & SFD_FLAG_TWO_PASS)) {
+    L->off_fieldsB = o; o += align256(sizeof(float) * L->fsz * nfields(c.kind));
+    for (int m = 0; m < npingpong_mem(c.kind); ++m) { L->off_memB[m] = o; o += align256(sizeof(float) * L->mem_sz[m]); }
+  }
   L->coef_plane = (size_t)L->P * c.nz;
   L->off_coef = o; o += align256(sizeof(float) * L->coef_plane * ncoef(c.kind));
   const int nax = is3(c.kind) ? 3 : 2;
@@ -192,7 +210,7 @@ void make_layout(const sfd_config& c, Layout* L) {
   L->off_src = o; o += align256(sizeof(float) * (size_t)nchan(c.kind) * c.nstep);
   L->off_rec = o; o += align256(sizeof(int) * 3 * (size_t)std::max(1, c.nrec));
   L->off_traces = o; o += align256(sizeof(float) * (size_t)c.nstep * nchan(c.kind) * std::max(1, c.nrec));
-  L->off_slots = o; o += align256(sizeof(float) * L->nslots);
+  L->off_slots = o; o += align256(sizeof(float) * L->nslots);  // ZB = 1 tiles: the largest grid
   L->total = o;
 }
 
@@ -204,8 +222,14 @@ struct sfd_handle_s {
   char* base;
   cudaStream_t stream;       // caller's stream
   cudaStream_t cap_stream;   // private stream used only to capture graphs
-  cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // indexed by the parity the graph starts from
   bool have_model = false, have_cpml = false;
+  bool single = false;  // single-pass 2-D steps (ping-pong state)
+  int cur = 0;          // copy holding the current state (single-pass only)
+  int zb = 2;           // rows per thread of the single-pass tiles
+  Em2Step em2s[2];      // [p]: reads copy p, writes copy 1-p
+  Seis2Step s2s[2];
+  Launch launch1;       // single-pass geometry
   int64_t step = 0;
   std::vector<double> src_scale[3];  // planes the source amplitude is divided by
   Em2Args em2;
@@ -213,8 +237,15 @@ struct sfd_handle_s {
   Seis25Args s25;
   Em25Args em25;
   Launch launch;
-  float* f(int q) const { return (float*)(base + L.off_fields) + (size_t)q * L.fsz; }
-  float* m(int q) const { return (float*)(base + L.off_mem[q]); }
+  // field q / memory variable q of copy `copy` (copy 1 exists for single-pass kinds)
+  float* fc(int q, int copy) const {
+    return (float*)(base + (copy ? L.off_fieldsB : L.off_fields)) + (size_t)q * L.fsz;
+  }
+  float* mc(int q, int copy) const {
+    return (float*)(base + ((copy && q < 4 && L.off_memB[q]) ? L.off_memB[q] : L.off_mem[q]));
+  }
+  float* f(int q) const { return fc(q, single ? cur : 0); }
+  float* m(int q) const { return mc(q, single ? cur : 0); }
   float* coef(int q) const { return (float*)(base + L.off_coef) + (size_t)q * L.coef_plane; }
   float* axis(int a) const { return (float*)(base + L.off_axis[a]); }
   IoArgs io() const {
@@ -242,27 +273,54 @@ void bind_args(sfd_handle* h) {
     case SFD_ELECTROMAG2: {
       Em2Args& a = h->em2;
       a.NX = NX; a.NZ = NZ; a.P = L.P; a.W = L.W;
-      a.Ex = h->f(0); a.Ez = h->f(1); a.Hy = h->f(2);
-      a.mExz = h->m(0); a.mEzx = h->m(1); a.mHyz = h->m(2); a.mHyx = h->m(3);
+      a.Ex = h->fc(0, 0); a.Ez = h->fc(1, 0); a.Hy = h->fc(2, 0);
+      a.mExz = h->mc(0, 0); a.mEzx = h->mc(1, 0); a.mHyz = h->mc(2, 0); a.mHyx = h->mc(3, 0);
       a.caEx = h->coef(0); a.cbEx = h->coef(1); a.caEz = h->coef(2); a.cbEz = h->coef(3);
       a.X = make_axis(h->axis(0), NX); a.Z = make_axis(h->axis(1), NZ);
       a.dbH = (float)(c.dt / kMu0);
       a.io = io;
       h->launch = em2_launch(a);
+      for (int p = 0; p < 2 && h->single; ++p) {
+        Em2Step& b = h->em2s[p];
+        b.NX = NX; b.NZ = NZ; b.P = L.P; b.W = L.W;
+        b.Ex0 = h->fc(0, p); b.Ez0 = h->fc(1, p); b.Hy0 = h->fc(2, p);
+        b.mExz0 = h->mc(0, p); b.mEzx0 = h->mc(1, p);
+        b.Ex1 = h->fc(0, 1 - p); b.Ez1 = h->fc(1, 1 - p); b.Hy1 = h->fc(2, 1 - p);
+        b.mExz1 = h->mc(0, 1 - p); b.mEzx1 = h->mc(1, 1 - p);
+        b.mHyz = h->mc(2, 0); b.mHyx = h->mc(3, 0);
+        b.caEx = a.caEx; b.cbEx = a.cbEx; b.caEz = a.caEz; b.cbEz = a.cbEz;
+        b.X = a.X; b.Z = a.Z; b.dbH = a.dbH; b.io = io;
+      }
+      if (h->single) h->launch1 = em2_step_launch(h->em2s[0], h->zb);
       break;
     }
     case SFD_SEISMIC2: {
       Seis2Args& a = h->s2;
       a.NX = NX; a.NZ = NZ; a.P = L.P; a.W = L.W; a.atten = 0;
-      a.vx = h->f(0); a.vz = h->f(1); a.sxx = h->f(2); a.szz = h->f(3); a.sxz = h->f(4);
-      a.m_vxx = h->m(0); a.m_vzz = h->m(1); a.m_vxz = h->m(2); a.m_vzx = h->m(3);
-      a.m_sxx_x = h->m(4); a.m_szz_z = h->m(5); a.m_sxz_x = h->m(6); a.m_sxz_z = h->m(7);
+      a.vx = h->fc(0, 0); a.vz = h->fc(1, 0); a.sxx = h->fc(2, 0); a.szz = h->fc(3, 0); a.sxz = h->fc(4, 0);
+      a.m_vxx = h->mc(0, 0); a.m_vzz = h->mc(1, 0); a.m_vxz = h->mc(2, 0); a.m_vzx = h->mc(3, 0);
+      a.m_sxx_x = h->mc(4, 0); a.m_szz_z = h->mc(5, 0); a.m_sxz_x = h->mc(6, 0); a.m_sxz_z = h->mc(7, 0);
       a.c11 = h->coef(0); a.c13 = h->coef(1); a.c15 = h->coef(2); a.c33 = h->coef(3); a.c35 = h->coef(4);
       a.c55 = h->coef(5); a.dtrx = h->coef(6); a.dtrz = h->coef(7); a.gxp = h->coef(8); a.gzp = h->coef(9);
       a.q3 = (const float*)(h->base + L.off_q3);
       a.X = make_axis(h->axis(0), NX); a.Z = make_axis(h->axis(1), NZ);
       a.io = io;
       h->launch = seis2_launch(a);
+      for (int p = 0; p < 2 && h->single; ++p) {
+        Seis2Step& b = h->s2s[p];
+        b.NX = NX; b.NZ = NZ; b.P = L.P; b.W = L.W; b.atten = a.atten;
+        b.vx0 = h->fc(0, p); b.vz0 = h->fc(1, p); b.sxx0 = h->fc(2, p); b.szz0 = h->fc(3, p); b.sxz0 = h->fc(4, p);
+        b.vx1 = h->fc(0, 1 - p); b.vz1 = h->fc(1, 1 - p); b.sxx1 = h->fc(2, 1 - p); b.szz1 = h->fc(3, 1 - p);
+        b.sxz1 = h->fc(4, 1 - p);
+        b.m_vxx0 = h->mc(0, p); b.m_vzz0 = h->mc(1, p); b.m_vxz0 = h->mc(2, p); b.m_vzx0 = h->mc(3, p);
+        b.m_vxx1 = h->mc(0, 1 - p); b.m_vzz1 = h->mc(1, 1 - p); b.m_vxz1 = h->mc(2, 1 - p);
+        b.m_vzx1 = h->mc(3, 1 - p);
+        b.m_sxx_x = h->mc(4, 0); b.m_szz_z = h->mc(5, 0); b.m_sxz_x = h->mc(6, 0); b.m_sxz_z = h->mc(7, 0);
+        b.c11 = a.c11; b.c13 = a.c13; b.c15 = a.c15; b.c33 = a.c33; b.c35 = a.c35; b.c55 = a.c55;
+        b.dtrx = a.dtrx; b.dtrz = a.dtrz; b.gxp = a.gxp; b.gzp = a.gzp; b.q3 = a.q3;
+        b.X = a.X; b.Z = a.Z; b.io = io;
+      }
+      if (h->single) h->launch1 = seis2_step_launch(h->s2s[0], h->zb);
       break;
     }
     case SFD_SEISMIC25: {
@@ -306,9 +364,20 @@ void bind_args(sfd_handle* h) {
 }
 
 void set_io_source(sfd_handle* h, int i, int j, int k) {
-  h->em2.io.si = h->s2.io.si = h->s25.io.si = h->em25.io.si = i;
-  h->em2.io.sj = h->s2.io.sj = h->s25.io.sj = h->em25.io.sj = j;
-  h->em2.io.sk = h->s2.io.sk = h->s25.io.sk = h->em25.io.sk = k;
+  IoArgs* ios[8] = {&h->em2.io, &h->s2.io, &h->s25.io, &h->em25.io,
+                    &h->em2s[0].io, &h->em2s[1].io, &h->s2s[0].io, &h->s2s[1].io};
+  for (IoArgs* io : ios) { io->si = i; io->sj = j; io->sk = k; }
+}
+
+void set_atten(sfd_handle* h, int atten) {
+  h->s2.atten = h->s2s[0].atten = h->s2s[1].atten = atten;
+  h->s25.atten = atten;
+}
+
+// One single-pass step reading copy p (graph capture passes p explicitly).
+void launch_step(sfd_handle* h, int p, int rel, cudaStream_t s) {
+  if (h->cfg.kind == SFD_ELECTROMAG2) em2_step(h->em2s[p], h->launch1, h->zb, rel, s);
+  else seis2_step(h->s2s[p], h->launch1, h->zb, rel, s);
 }
 
 void launch_half(sfd_handle* h, int which, int rel, cudaStream_t s) {
@@ -322,6 +391,11 @@ void launch_half(sfd_handle* h, int which, int rel, cudaStream_t s) {
 }
 
 void launch_finalize(sfd_handle* h, int t_last, cudaStream_t s) {
+  if (h->single) {
+    if (h->cfg.kind == SFD_ELECTROMAG2) em2_step_finalize(h->em2s[h->cur], t_last, s);
+    else seis2_step_finalize(h->s2s[h->cur], t_last, s);
+    return;
+  }
   switch (h->cfg.kind) {
     case SFD_ELECTROMAG2: em2_finalize(h->em2, t_last, s); break;
     case SFD_SEISMIC2: seis2_finalize(h->s2, t_last, s); break;
@@ -330,25 +404,30 @@ void launch_finalize(sfd_handle* h, int t_last, cudaStream_t s) {
   }
 }
 
-int ensure_graph(sfd_handle* h) {
-  if (h->graph) return SFD_OK;
+int ensure_graph(sfd_handle* h, int p) {
+  if (h->graph[p]) return SFD_OK;
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
   for (int s = 0; s < kGraphSteps; ++s) {
-    launch_half(h, 0, s, h->cap_stream);
-    launch_half(h, 1, s, h->cap_stream);
+    if (h->single) {
+      launch_step(h, (p + s) & 1, s, h->cap_stream);
+    } else {
+      launch_half(h, 0, s, h->cap_stream);
+      launch_half(h, 1, s, h->cap_stream);
+    }
   }
   k_advance<<<1, 1, 0, h->cap_stream>>>((Ctl*)(h->base + h->L.off_ctl), kGraphSteps);
   cudaError_t e = cudaStreamEndCapture(h->cap_stream, &g);
   if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-  e = cudaGraphInstantiate(&h->graph, g, 0);
+  e = cudaGraphInstantiate(&h->graph[p], g, 0);
   cudaGraphDestroy(g);
-  if (e != cudaSuccess) { h->graph = nullptr; return cuda_fail(e, "cudaGraphInstantiate"); }
+  if (e != cudaSuccess) { h->graph[p] = nullptr; return cuda_fail(e, "cudaGraphInstantiate"); }
   return SFD_OK;
 }
 
 void invalidate_graph(sfd_handle* h) {
-  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  for (int p = 0; p < 2; ++p)
+    if (h->graph[p]) { cudaGraphExecDestroy(h->graph[p]); h->graph[p] = nullptr; }
 }
 
 // Host FP64 -> device FP32 with row pitch P (rows of NX values).
@@ -417,6 +496,7 @@ int32_t sfd_create(const sfd_config* cfg, void* dev_state, size_t state_bytes, v
   h->L = L;
   h->base = (char*)dev_state;
   h->stream = (cudaStream_t)stream;
+  h->single = has_single_pass(cfg->kind) && !(cfg->flags & SFD_FLAG_TWO_PASS);
   e = cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaStreamCreateWithFlags"); }
   bind_args(h);
@@ -496,7 +576,7 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
         }
       h->src_scale[0].assign(rho, rho + N2);
       h->src_scale[1].assign(rho, rho + N2);
-      h->s2.atten = atten;
+      set_atten(h, atten);
       break;
     }
     case SFD_SEISMIC25: {
@@ -522,7 +602,7 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
           }
         }
       for (int d = 0; d < 3; ++d) h->src_scale[d].assign(rho, rho + N2);
-      h->s25.atten = atten;
+      set_atten(h, atten);
       break;
     }
   }
@@ -630,6 +710,7 @@ int32_t sfd_reset(sfd_handle* h) {
   CK(cudaMemsetAsync(h->base + L.off_fields, 0, L.off_coef - L.off_fields, h->stream));
   CK(cudaMemsetAsync(h->base + L.off_traces, 0, L.off_slots - L.off_traces, h->stream));
   h->step = 0;
+  h->cur = 0;
   return SFD_OK;
 }
 
@@ -701,13 +782,18 @@ int32_t sfd_run(sfd_handle* h, int64_t nsteps) {
   const int64_t chunks = nsteps / kGraphSteps;
   const int rem = (int)(nsteps % kGraphSteps);
   if (chunks > 0) {
-    int r = ensure_graph(h);
+    int r = ensure_graph(h, h->single ? h->cur : 0);
     if (r) return r;
-    for (int64_t q = 0; q < chunks; ++q) CK(cudaGraphLaunch(h->graph, h->stream));
+    for (int64_t q = 0; q < chunks; ++q) CK(cudaGraphLaunch(h->graph[h->single ? h->cur : 0], h->stream));
   }
   for (int s = 0; s < rem; ++s) {
-    launch_half(h, 0, s, h->stream);
-    launch_half(h, 1, s, h->stream);
+    if (h->single) {
+      launch_step(h, h->cur, s, h->stream);
+      h->cur ^= 1;
+    } else {
+      launch_half(h, 0, s, h->stream);
+      launch_half(h, 1, s, h->stream);
+    }
   }
   launch_finalize(h, (int)(h->step + nsteps - 1), h->stream);
   k_reduce_slots<<<1, 1024, 0, h->stream>>>(ctl, slots, L.nslots);
@@ -750,7 +836,14 @@ int32_t sfd_launch_half(sfd_handle* h, int32_t which, int32_t count) {
   const Layout& L = h->L;
   k_begin<<<std::min(1024, (L.nslots + 255) / 256 + 1), 256, 0, h->stream>>>((Ctl*)(h->base + L.off_ctl),
                                                                             (float*)(h->base + L.off_slots), L.nslots, 0);
-  for (int q = 0; q < count; ++q) launch_half(h, which, 0, h->stream);
+  for (int q = 0; q < count; ++q) {
+    if (h->single) {
+      launch_step(h, h->cur, 0, h->stream);  // the single-pass kernel is the whole step
+      h->cur ^= 1;
+    } else {
+      launch_half(h, which, 0, h->stream);
+    }
+  }
   CK(cudaGetLastError());
   return SFD_OK;
 }
@@ -766,6 +859,152 @@ int32_t sfd_destroy(sfd_handle* h) {
   invalidate_graph(h);
   if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
   delete h;
+  return SFD_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched runs: one persistent cooperative launch for many 2-D models.
+
+struct sfd_batch_s {
+  std::vector<sfd_handle*> h;
+  char* scratch = nullptr;
+  cudaStream_t stream = nullptr;
+  int zb = 2, bps = 4, nsm = 0;
+  unsigned long long limit_ns = 2000000000ull;  // barrier wait limit: 2 s
+  std::vector<BatchModel> models;
+  std::vector<int> steps;
+  GridBarrier* bar() const { return (GridBarrier*)scratch; }
+  int* dsteps() const { return (int*)(scratch + 256); }
+  BatchModel* dmodels() const { return (BatchModel*)(scratch + 256 + align256(sizeof(int) * h.size())); }
+};
+
+namespace {
+size_t batch_bytes(int n) { return 256 + align256(sizeof(int) * n) + align256(sizeof(BatchModel) * (size_t)n); }
+}  // namespace
+
+extern "C" {
+
+int32_t sfd_batch_scratch_bytes(int32_t nmodels, size_t* bytes) {
+  g_err.clear();
+  if (nmodels < 1 || !bytes) return fail(SFD_ERR_BAD_ARG, "need nmodels >= 1 and a bytes pointer");
+  *bytes = batch_bytes(nmodels);
+  return SFD_OK;
+}
+
+int32_t sfd_batch_create(sfd_handle* const* handles, int32_t n, void* dev_scratch, size_t bytes, sfd_batch** out) {
+  g_err.clear();
+  if (!handles || n < 1 || !out) return fail(SFD_ERR_BAD_ARG, "need handles, n >= 1 and out");
+  *out = nullptr;
+  if (!dev_scratch || ((uintptr_t)dev_scratch & 255)) return fail(SFD_ERR_BAD_ARG, "scratch must be 256-byte aligned device memory");
+  if (bytes < batch_bytes(n)) return fail(SFD_ERR_BAD_ARG, "batch scratch has %zu bytes, needs %zu", bytes, batch_bytes(n));
+  for (int m = 0; m < n; ++m) {
+    sfd_handle* h = handles[m];
+    if (!h) return fail(SFD_ERR_BAD_ARG, "handle %d is NULL", m);
+    if (!h->single) return fail(SFD_ERR_BAD_ARG, "handle %d: batches take single-pass 2-D handles (seismic2/electromag2, no SFD_FLAG_TWO_PASS)", m);
+    if (!h->have_model || !h->have_cpml) return fail(SFD_ERR_STATE, "handle %d has no model or CPML yet", m);
+    if (h->stream != handles[0]->stream) return fail(SFD_ERR_BAD_ARG, "all handles of a batch must share one stream");
+    for (int q = 0; q < m; ++q)
+      if (handles[q] == h) return fail(SFD_ERR_BAD_ARG, "handle %d appears twice", m);
+  }
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  sfd_batch* b = new sfd_batch_s();
+  b->h.assign(handles, handles + n);
+  b->scratch = (char*)dev_scratch;
+  b->stream = handles[0]->stream;
+  cudaError_t e = cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) { delete b; return cuda_fail(e, "cudaDeviceGetAttribute"); }
+  *out = b;
+  return SFD_OK;
+}
+
+int32_t sfd_batch_set_tiling(sfd_batch* b, int32_t zb, int32_t blocks_per_sm) {
+  g_err.clear();
+  if (!b) return fail(SFD_ERR_BAD_ARG, "NULL batch");
+  if (zb != 1 && zb != 2 && zb != 4) return fail(SFD_ERR_BAD_ARG, "zb must be 1, 2 or 4");
+  int maxb = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, batch_kernel_ptr(zb), 256, 0));
+  if (blocks_per_sm < 1 || blocks_per_sm > maxb)
+    return fail(SFD_ERR_BAD_ARG, "blocks_per_sm must be in [1, %d] for zb=%d", maxb, zb);
+  b->zb = zb;
+  b->bps = blocks_per_sm;
+  return SFD_OK;
+}
+
+int32_t sfd_batch_run(sfd_batch* b, int64_t nsteps) {
+  g_err.clear();
+  if (!b) return fail(SFD_ERR_BAD_ARG, "NULL batch");
+  if (nsteps < 0) return fail(SFD_ERR_BAD_ARG, "nsteps must be >= 0");
+  if (nsteps == 0) return SFD_OK;
+  const int n = (int)b->h.size();
+  for (int m = 0; m < n; ++m)
+    if (b->h[m]->step + nsteps > b->h[m]->cfg.nstep)
+      return fail(SFD_ERR_BAD_ARG, "model %d: run to step %lld exceeds its %d source samples", m,
+                  (long long)(b->h[m]->step + nsteps), b->h[m]->cfg.nstep);
+  int maxb = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, batch_kernel_ptr(b->zb), 256, 0));
+  const int bps = std::min(b->bps, maxb);
+  if (bps < 1) return fail(SFD_ERR_CUDA, "batch kernel does not fit on an SM");
+  b->models.assign(n, BatchModel());
+  b->steps.assign(n, 0);
+  int tile0 = 0;
+  for (int m = 0; m < n; ++m) {
+    sfd_handle* h = b->h[m];
+    BatchModel& md = b->models[m];
+    md.kind = h->cfg.kind == SFD_ELECTROMAG2 ? SFD_BATCH_EM2 : SFD_BATCH_SEIS2;
+    md.gx = (h->cfg.nx + 31) / 32;
+    const int gy = (h->cfg.nz + 8 * b->zb - 1) / (8 * b->zb);
+    md.tile0 = tile0;
+    md.ntiles = md.gx * gy;
+    md.nslots = md.ntiles;
+    md.cur = h->cur;
+    md.em2[0] = h->em2s[0];
+    md.em2[1] = h->em2s[1];
+    md.s2[0] = h->s2s[0];
+    md.s2[1] = h->s2s[1];
+    tile0 += md.ntiles;
+    b->steps[m] = (int)h->step;
+  }
+  const int total = tile0;
+  const int grid = std::max(1, std::min(total, bps * b->nsm));
+  CK(cudaMemcpyAsync(b->dsteps(), b->steps.data(), sizeof(int) * n, cudaMemcpyHostToDevice, b->stream));
+  CK(cudaMemcpyAsync(b->dmodels(), b->models.data(), sizeof(BatchModel) * n, cudaMemcpyHostToDevice, b->stream));
+  batch_begin(b->dmodels(), n, b->dsteps(), b->bar(), b->stream);
+  CK(batch_launch(b->zb, grid, b->dmodels(), n, total, (int)nsteps, b->bar(), b->limit_ns, b->stream));
+  batch_end(b->dmodels(), n, (int)nsteps, b->stream);
+  CK(cudaGetLastError());
+  for (sfd_handle* h : b->h) {
+    h->step += nsteps;
+    h->cur ^= (int)(nsteps & 1);
+  }
+  return SFD_OK;
+}
+
+int32_t sfd_batch_status(sfd_batch* b, int32_t* failed_model) {
+  g_err.clear();
+  if (!b) return fail(SFD_ERR_BAD_ARG, "NULL batch");
+  if (failed_model) *failed_model = -1;
+  GridBarrier bar;
+  CK(cudaMemcpyAsync(&bar, b->bar(), sizeof bar, cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  if (bar.err) return fail(SFD_ERR_TIMEOUT, "grid barrier of the batched kernel timed out");
+  for (size_t m = 0; m < b->h.size(); ++m) {
+    int r = sfd_status(b->h[m], nullptr, nullptr);
+    if (r != SFD_OK) {
+      if (failed_model) *failed_model = (int32_t)m;
+      return r;
+    }
+  }
+  return SFD_OK;
+}
+
+int32_t sfd_batch_destroy(sfd_batch* b) {
+  g_err.clear();
+  if (!b) return SFD_OK;
+  cudaStreamSynchronize(b->stream);
+  delete b;
   return SFD_OK;
 }
 

@@ -75,6 +75,35 @@ struct Em25Args {
   IoArgs io;
 };
 
+// Single-pass (fused) 2-D steps.  Each launch reads the "old" copy of every
+// field and of the memory variables that neighbouring tiles re-derive, and
+// writes the "new" copy; memory variables touched only by their owner cell
+// are updated in place.  A tile of TX x (8*ZB) cells recomputes the first
+// half-step on a one-cell halo so the second half-step needs no second pass.
+struct Em2Step {
+  int NX, NZ, P, W;
+  const float *Ex0, *Ez0, *Hy0, *mExz0, *mEzx0;  // old
+  float *Ex1, *Ez1, *Hy1, *mExz1, *mEzx1;        // new
+  float *mHyz, *mHyx;                            // in place
+  const float *caEx, *cbEx, *caEz, *cbEz;
+  AxisTab X, Z;
+  float dbH;
+  IoArgs io;
+};
+
+struct Seis2Step {
+  int NX, NZ, P, W;
+  int atten;
+  const float *vx0, *vz0, *sxx0, *szz0, *sxz0;
+  float *vx1, *vz1, *sxx1, *szz1, *sxz1;
+  const float *m_vxx0, *m_vzz0, *m_vxz0, *m_vzx0;  // velocity-gradient memory, old
+  float *m_vxx1, *m_vzz1, *m_vxz1, *m_vzx1;        // new
+  float *m_sxx_x, *m_szz_z, *m_sxz_x, *m_sxz_z;    // in place
+  const float *c11, *c13, *c15, *c33, *c35, *c55, *dtrx, *dtrz, *gxp, *gzp, *q3;
+  AxisTab X, Z;
+  IoArgs io;
+};
+
 // Launch geometry of a solver's two half-step kernels.
 struct Launch {
   dim3 grid, block;
@@ -100,5 +129,13 @@ Launch em25_launch(const Em25Args& a);
 void em25_half1(const Em25Args& a, const Launch& L, int rel, cudaStream_t s);
 void em25_half2(const Em25Args& a, const Launch& L, int rel, cudaStream_t s);
 void em25_finalize(const Em25Args& a, int t_last, cudaStream_t s);
+
+// Fused steps (one launch per time step); zb = rows per thread (1, 2 or 4).
+Launch em2_step_launch(const Em2Step& a, int zb);
+void em2_step(const Em2Step& a, const Launch& L, int zb, int rel, cudaStream_t s);
+void em2_step_finalize(const Em2Step& a, int t_last, cudaStream_t s);
+Launch seis2_step_launch(const Seis2Step& a, int zb);
+void seis2_step(const Seis2Step& a, const Launch& L, int zb, int rel, cudaStream_t s);
+void seis2_step_finalize(const Seis2Step& a, int t_last, cudaStream_t s);
 
 }  // namespace sfd

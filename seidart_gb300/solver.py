@@ -49,6 +49,9 @@ MEMORY = {
 }
 
 
+FLAG_TWO_PASS = 1
+
+
 def is_25d(kind: int) -> bool:
     return kind in (SEISMIC25, ELECTROMAG25)
 
@@ -86,12 +89,15 @@ def _fptr(a: np.ndarray):
 class FDTDSolver:
     """One FDTD model on the GPU, driven through the C ABI.
 
+    ``flags`` = ``FLAG_TWO_PASS`` selects, for the 2-D kinds, the two-kernel
+    step (fields updated in place) instead of the default single-pass step.
+
     ``nstep`` is the number of source samples (the run length); ``nrec`` the
     number of receivers.  The device state is allocated with torch on
     ``device`` and bound to the current torch stream of that device.
     """
 
-    def __init__(self, grid: GridSpec, nstep: int, nrec: int, device="cuda", stream=None):
+    def __init__(self, grid: GridSpec, nstep: int, nrec: int, device="cuda", stream=None, flags: int = 0):
         import torch
 
         self.grid = grid
@@ -101,7 +107,7 @@ class FDTDSolver:
         L = _lib.lib()
         self._L = L
         self.cfg = SfdConfig(kind=grid.kind, nx=grid.nx, ny=grid.ny if is_25d(grid.kind) else 1, nz=grid.nz,
-                             npml=grid.npml, nstep=self.nstep, nrec=self.nrec, flags=0,
+                             npml=grid.npml, nstep=self.nstep, nrec=self.nrec, flags=int(flags),
                              dx=grid.dx, dy=grid.dy, dz=grid.dz, dt=grid.dt)
         nbytes = C.c_size_t(0)
         check(L.sfd_state_bytes(C.byref(self.cfg), C.byref(nbytes)))

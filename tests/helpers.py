@@ -20,9 +20,9 @@ def run_oracle(case, nsteps=None, state=None):
                       case.srcfn, case.rec_ijk, n, state=state)
 
 
-def make_solver(case, device="cuda"):
+def make_solver(case, device="cuda", flags=0):
     from seidart_gb300.solver import FDTDSolver
-    s = FDTDSolver(case.grid, case.nstep, len(case.rec_ijk), device=device)
+    s = FDTDSolver(case.grid, case.nstep, len(case.rec_ijk), device=device, flags=flags)
     s.set_model(case.planes)
     s.set_cpml(case.profiles)
     s.set_source(case.src_ijk, case.srcfn)

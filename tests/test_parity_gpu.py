@@ -22,30 +22,38 @@ TOL_FIELD = 1e-5
 TOL_MEM = 1e-4
 
 CASES = [
-    # kind, seed, nx, nz, ny, npml, nstep
-    (ELECTROMAG2, 0, 45, 37, 1, 5, 160),
-    (ELECTROMAG2, 1, 70, 52, 1, 8, 100),
-    (SEISMIC2, 0, 45, 37, 1, 5, 160),
-    (SEISMIC2, 1, 70, 52, 1, 8, 100),
-    (SEISMIC2, 2, 30, 44, 1, 5, 120),   # NZ > NX: b_x_half read past the x axis
-    (SEISMIC25, 0, 37, 29, 21, 5, 90),
-    (SEISMIC25, 1, 50, 34, 26, 7, 70),
-    (ELECTROMAG25, 0, 37, 29, 21, 5, 90),
-    (ELECTROMAG25, 1, 50, 34, 26, 7, 70),
+    # kind, seed, nx, nz, ny, npml, nstep, flags (1 = two-pass form of the 2-D kinds)
+    (ELECTROMAG2, 0, 45, 37, 1, 5, 160, 0),
+    (ELECTROMAG2, 0, 45, 37, 1, 5, 160, 1),
+    (ELECTROMAG2, 1, 70, 52, 1, 8, 100, 0),
+    (ELECTROMAG2, 1, 70, 52, 1, 8, 100, 1),
+    (ELECTROMAG2, 3, 97, 67, 1, 9, 75, 0),
+    (SEISMIC2, 0, 45, 37, 1, 5, 160, 0),
+    (SEISMIC2, 0, 45, 37, 1, 5, 160, 1),
+    (SEISMIC2, 1, 70, 52, 1, 8, 100, 0),
+    (SEISMIC2, 1, 70, 52, 1, 8, 100, 1),
+    (SEISMIC2, 2, 30, 44, 1, 5, 120, 0),   # NZ > NX: b_x_half read past the x axis
+    (SEISMIC2, 2, 30, 44, 1, 5, 120, 1),
+    (SEISMIC2, 3, 97, 67, 1, 9, 75, 0),
+    (SEISMIC25, 0, 37, 29, 21, 5, 90, 0),
+    (SEISMIC25, 1, 50, 34, 26, 7, 70, 0),
+    (ELECTROMAG25, 0, 37, 29, 21, 5, 90, 0),
+    (ELECTROMAG25, 1, 50, 34, 26, 7, 70, 0),
 ]
 
 
 def _ids(c):
-    return f"{KIND_NAMES[c[0]]}-s{c[1]}-{c[2]}x{c[3]}" + (f"x{c[4]}" if c[4] > 1 else "")
+    return f"{KIND_NAMES[c[0]]}-s{c[1]}-{c[2]}x{c[3]}" + (f"x{c[4]}" if c[4] > 1 else "") + \
+        ("-twopass" if c[7] else "")
 
 
 @pytest.mark.parametrize("spec", CASES, ids=[_ids(c) for c in CASES])
 def test_parity_against_oracle(gpu, spec):
-    kind, seed, nx, nz, ny, npml, nstep = spec
+    kind, seed, nx, nz, ny, npml, nstep, flags = spec
     case = sy.small_case(kind, seed=seed, nx=nx, nz=nz, ny=max(ny, 2) if ny > 1 else 24, npml=npml, nstep=nstep)
     st, tr_ref, _, blew = run_oracle(case)
     assert not blew
-    with make_solver(case) as s:
+    with make_solver(case, flags=flags) as s:
         # uneven chunks: graph-captured 32-step blocks plus remainders
         done = 0
         for n in (37, 64, nstep):
