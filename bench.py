@@ -160,10 +160,110 @@ def make_solver(case, device):
     return s
 
 
-def launches_per_shot(kind, nstep):
+def launches_per_shot(kind, nstep, single_pass=True):
     from seidart_gb300 import ELECTROMAG25
-    # begin + 2 per step + one advance per 32-step graph + finalize (+ H faces for EM25) + slot reduce
-    return 2 * nstep + nstep // 32 + 3 + (1 if kind == ELECTROMAG25 else 0)
+    # begin + 1 (single-pass) or 2 kernels per step + one advance per 32-step graph + finalize
+    # (+ H faces for EM25) + slot reduce
+    per = 1 if single_pass else 2
+    return per * nstep + nstep // 32 + 3 + (1 if kind == ELECTROMAG25 else 0)
+
+
+def bench_batched(device, flush, stream, peak, plain_value, runs=2):
+    """The batched survey: 64 electromag2 shots of the layered 1000x500 model (sources every 15
+    cells) + 16 seeded seismic2 models of uneven size, 4000 steps, one persistent launch per run."""
+    import torch
+    from seidart_gb300 import ELECTROMAG2, synthetic as sy
+    from seidart_gb300.batch import Batch, autotune
+    shots, models = sy.batched_survey(nshots=64, nelastic=16, nstep=4000)
+    cases = shots + models
+    solvers = [make_solver(c, device) for c in cases]
+    b = Batch(solvers)
+    tune = autotune(b, steps=8, use_cache=False)
+    b.reset()
+    b.run(64)
+    b.status()
+    nstep = cases[0].nstep
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    total_ms = 0.0
+    for _ in range(runs):
+        flush.zero_()
+        b.reset()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        b.run(nstep)
+        ev1.record(stream)
+        b.status()
+        total_ms += ev0.elapsed_time(ev1)
+    ms = total_ms / runs
+    cells = sum(c.grid.cells for c in cases)
+    step_bytes = sum(em2_bytes(c.grid)["step"] if c.grid.kind == ELECTROMAG2 else seis2_bytes(c.grid)["step"]
+                     for c in cases)
+    value = cells * nstep / (ms / 1e3) / 1e9
+    achieved = step_bytes * nstep / (ms / 1e3) / 1e9
+    out = {"workload": "64 electromag2 shots 1040x540 + 16 seismic2 models (nx 200-1200, nz 100-600) x 4000 steps",
+           "value": round(value, 3), "unit": METRIC, "ms_per_run": round(ms, 2), "cells": cells,
+           "bytes_per_cell_update": round(step_bytes / cells, 2),
+           "roofline": {"bound": "hbm", "kernel": "batch_kernel", "achieved": round(achieved, 1), "peak": peak,
+                        "unit": "GB/s", "frac": round(achieved / peak, 4)},
+           "vs_plain_single_shot": round(value / plain_value, 3),
+           "tiling": {"rows_per_thread": tune["tiling"][0], "blocks_per_sm": tune["tiling"][1],
+                      "candidates_ms_per_step": {k: round(v * 1e3, 4) for k, v in tune["timings"].items()}},
+           "launches_per_run": 3}
+    b.close()
+    for s in solvers:
+        s.close()
+    return out
+
+
+def bench_adjoint(device, ckpt_every=200):
+    """Adjoint gradient on the layered electromag2 model (6000 steps, 100 receivers): misfit against
+    the unperturbed model's traces, current model with six +-5% Gaussian blobs in eps11 and eps33
+    (seed 6), checkpoints every 200 steps with recompute.  Reports backward / forward wall time."""
+    import torch
+    from seidart_gb300 import synthetic as sy
+    from seidart_gb300.adjoint import TraceModel
+    case = sy.electromag2_layers(nstep=6000)
+    base = case.planes
+    rng = np.random.default_rng(6)
+    nz, nx = base.shape[1:]
+    zz, xx = np.meshgrid(np.arange(nz), np.arange(nx), indexing="ij")
+    pert = np.zeros((nz, nx))
+    for _ in range(6):
+        cz, cx = rng.uniform(0.2, 0.8) * nz, rng.uniform(0.2, 0.8) * nx
+        pert += rng.choice([-1, 1]) * 0.05 * np.exp(-((zz - cz) ** 2 + (xx - cx) ** 2) / (2 * 25.0 ** 2))
+    cur = base.copy()
+    cur[0] = base[0] * (1 + pert)
+    cur[2] = base[2] * (1 + pert)
+    m = TraceModel(case.grid, base, case.profiles, case.src_ijk, case.srcfn, case.rec_ijk, ckpt_every=ckpt_every,
+                   device=device)
+    d_obs = m.forward(base[0], base[2], base[3])
+    m.forward(cur[0], cur[2], cur[3])  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tr = m.forward(cur[0], cur[2], cur[3])
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    resid = tr - d_obs
+    m.backward(resid)  # warm
+    t0 = time.perf_counter()
+    g11, g33, gs, _ = m.backward(resid)
+    t_bwd = time.perf_counter() - t0
+    # plain forward (no checkpoints) for the ratio's denominator
+    s = m.solver
+    s.reset()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.run(case.nstep)
+    s.status()
+    t_plain = time.perf_counter() - t0
+    m.close()
+    misfit = 0.5 * float((resid.double() ** 2).sum())
+    return {"workload": "electromag2 1040x540 x 6000 steps, gradient wrt eps11, eps33, sigma per cell",
+            "forward_s": round(t_plain, 4), "forward_with_checkpoints_s": round(t_fwd, 4),
+            "adjoint_s": round(t_bwd, 4), "adjoint_over_forward": round(t_bwd / t_plain, 3),
+            "checkpoints_every": ckpt_every, "misfit": misfit,
+            "grad_abs_max": [float(np.abs(g).max()) for g in (g11, g33, gs)]}
 
 
 def time_shots(solver, nstep, K, W, flush, stream, sync_all=None):
@@ -308,7 +408,7 @@ def run_ours(args):
     peak, peak_kind = _peaks()
 
     # ---- headline: electromag2 plain, one shot per bench step --------------
-    case = sy.electromag2_layers(nstep=6000)
+    case = sy.electromag2_layers(nstep=args.time_steps)
     g = case.grid
     solver = make_solver(case, device)
     clocks = ClockSampler(local)
@@ -323,16 +423,18 @@ def run_ours(args):
     value = world * cells * case.nstep / (ms / 1e3) / 1e9
     kt = kernel_times(solver, stream) if not args.headline_only else [1.0, 1.0]
     byts = em2_bytes(g)
-    dom = int(np.argmax(kt))
-    dom_name = ["em2_h_kernel", "em2_e_kernel"][dom]
-    achieved = byts[["half1", "half2"][dom]] / (kt[dom] / 1e3) / 1e9
+    # the single-pass handle runs one kernel per step: em2_step_kernel, the whole step's bytes
+    dom_name = "em2_step_kernel"
+    kstep = kt[0]
+    achieved = byts["step"] / (kstep / 1e3) / 1e9
+    dom = 0
     traffic = profile_traffic(f"{dom_name}_1040x540")
     step_ms = ms / case.nstep
     roofline = {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                 "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": int(byts[["half1", "half2"][dom]]),
-                "kernel_ms": [round(x, 5) for x in kt],
+                "algorithmic_bytes_per_launch": int(byts["step"]),
+                "kernel_ms": round(kstep, 5),
                 "note": "state (23 MB) is L2-resident during a shot; fraction is against the HBM copy peak"}
     step_achieved = byts["step"] / (step_ms / 1e3) / 1e9
     roofline_step = {"bytes_per_cell_update": round(byts["per_cell_step"], 2),
@@ -403,6 +505,10 @@ def run_ours(args):
                                                      for h, t in zip(("half1", "half2"), kt2)]}
         s2.close()
         line["extras"] = extras
+    if not args.skip_batched:
+        line.setdefault("extras", {})["batched"] = bench_batched(device, flush, stream, peak, value / world)
+    if not args.skip_adjoint:
+        line.setdefault("extras", {})["adjoint"] = bench_adjoint(device)
 
     if rank == 0 and not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline(case, seconds=args.cpu_seconds)
@@ -424,11 +530,15 @@ def main(argv=None):
     ap.add_argument("--ref-chunk", type=int, default=200, help="time steps per reference bench step")
     ap.add_argument("--skip-extras", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--time-steps", type=int, default=6000,
+                    help="time steps per headline shot (6000 = the workload; smaller only for profiler runs)")
+    ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--headline-only", action="store_true",
                     help="only the timed headline shots (for profiler runs): no e2e, extras or CPU leg")
     args = ap.parse_args(argv)
     if args.headline_only:
-        args.skip_extras = args.skip_cpu = True
+        args.skip_extras = args.skip_cpu = args.skip_batched = args.skip_adjoint = True
         args.e2e_steps = 0
     if args.warmup < 3:
         print("note: fewer than 3 warm-up steps", file=sys.stderr)

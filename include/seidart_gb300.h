@@ -179,6 +179,30 @@ int32_t sfd_launch_half(sfd_handle* h, int32_t which, int32_t count);
 /* Release the handle (the caller frees its device buffer afterwards). */
 int32_t sfd_destroy(sfd_handle* h);
 
+/* ---- Checkpoints ------------------------------------------------------------
+ * The dynamic state (every field and CPML memory variable) of a handle,
+ * copied to / from a caller-owned device buffer on the handle's stream.
+ * Loading also sets the step counter (the source index). */
+int32_t sfd_checkpoint_bytes(const sfd_handle* h, size_t* bytes);
+int32_t sfd_checkpoint_save(sfd_handle* h, void* dev_dst);
+int32_t sfd_checkpoint_load(sfd_handle* h, const void* dev_src, int64_t step);
+
+/* ---- Discrete adjoint (electromag2, single-pass handles) --------------------
+ * Gradient of J with respect to the six model planes, given dJ/d(trace)
+ * (device FP32 [nstep][2][nrec]; for J = 1/2 sum (d - d_obs)^2 this is the
+ * residual).  Usage: after a forward run that saved checkpoints every S
+ * steps, call sfd_adjoint_begin once, then for each checkpoint from the last
+ * to the first: sfd_checkpoint_load(h, ckpt, step), sfd_adjoint_segment(h,
+ * steps of that segment).  Each segment recomputes its forward states from
+ * the checkpoint and runs the adjoint steps backwards over them.  The
+ * workspace (sfd_adjoint_bytes) holds S+1 forward states.  No counterpart in
+ * the reference (SeidarT has no adjoint). */
+int32_t sfd_adjoint_bytes(const sfd_handle* h, int32_t seg_steps, size_t* bytes);
+int32_t sfd_adjoint_begin(sfd_handle* h, void* dev_work, size_t bytes, int32_t seg_steps, const float* dev_resid);
+int32_t sfd_adjoint_segment(sfd_handle* h, int64_t nsteps);
+/* dJ/d(eps11 eps13 eps33 sig11 sig13 sig33), host FP64, 6*NX*NZ values. */
+int32_t sfd_adjoint_gradient(sfd_handle* h, double* planes, int64_t count);
+
 /* ---- Batched runs ----------------------------------------------------------
  * Many 2-D models (electromag2 shots, seismic2 models of any sizes, mixed)
  * advance together in one persistent cooperative kernel launch with a grid

@@ -1,0 +1,155 @@
+"""Gradients of a receiver-trace misfit with respect to the electromag2 model.
+
+``TraceModel`` owns one single-pass electromag2 solver and its checkpoints.
+Its forward pass runs the whole shot, saving the dynamic state every
+``ckpt_every`` steps.  Its backward pass walks the checkpoints from the last
+to the first.  For each one it recomputes that segment's forward states on the
+device and runs the hand-written discrete adjoint kernels
+(``csrc/adjoint_em2.cu``) backwards over them.  ``sfd_adjoint_gradient`` then
+applies the FP64 chain rule from the update coefficients to the model planes.
+
+``traces = TraceMisfit.apply(eps11, eps33, sigma, model)`` is differentiable
+in torch: ``eps11``, ``eps33``, ``sigma`` (sig11 = sig33) are per-cell
+(NZ, NX) FP64 tensors, and the traces are (nstep, 2, nrec) FP32 on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+from .solver import FDTDSolver, GridSpec
+
+
+def _declare(L):
+    if getattr(L, "_adj_declared", False):
+        return
+    P, i32, i64, sz = C.c_void_p, C.c_int32, C.c_int64, C.c_size_t
+    for name, res, args in [
+        ("sfd_checkpoint_bytes", i32, [P, C.POINTER(sz)]),
+        ("sfd_checkpoint_save", i32, [P, P]),
+        ("sfd_checkpoint_load", i32, [P, P, i64]),
+        ("sfd_adjoint_bytes", i32, [P, i32, C.POINTER(sz)]),
+        ("sfd_adjoint_begin", i32, [P, P, sz, i32, P]),
+        ("sfd_adjoint_segment", i32, [P, i64]),
+        ("sfd_adjoint_gradient", i32, [P, C.POINTER(C.c_double), i64]),
+    ]:
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    L._adj_declared = True
+
+
+class TraceModel:
+    """An electromag2 shot whose eps11, eps33 and sigma can be differentiated.
+
+    ``base_planes``: (6, NZ, NX) FP64 model (eps11 eps13 eps33 sig11 sig13 sig33);
+    eps13 and sig13 stay fixed, the other planes are replaced by the inputs.
+    """
+
+    def __init__(self, grid: GridSpec, base_planes, profiles, src_ijk, srcfn, rec_ijk, ckpt_every=200,
+                 device="cuda"):
+        import torch
+
+        self.grid = grid
+        self.base = np.ascontiguousarray(base_planes, dtype=np.float64)
+        self.src_ijk = src_ijk
+        self.srcfn = np.asarray(srcfn, dtype=np.float64)
+        self.nstep = self.srcfn.shape[1]
+        self.ckpt_every = int(ckpt_every)
+        self.solver = FDTDSolver(grid, self.nstep, len(rec_ijk), device=device)
+        self.solver.set_model(self.base)
+        self.solver.set_cpml(profiles)
+        self.solver.set_source(src_ijk, self.srcfn)
+        self.solver.set_receivers(rec_ijk)
+        L = _lib.lib()
+        _declare(L)
+        self._L = L
+        h = self.solver._h
+        nb = C.c_size_t()
+        check(L.sfd_checkpoint_bytes(h, C.byref(nb)))
+        self.nseg = (self.nstep + self.ckpt_every - 1) // self.ckpt_every
+        self.ckpt = torch.empty((self.nseg, int(nb.value)), dtype=torch.uint8, device=self.solver.device)
+        nb2 = C.c_size_t()
+        check(L.sfd_adjoint_bytes(h, self.ckpt_every, C.byref(nb2)))
+        self.work = torch.empty(int(nb2.value), dtype=torch.uint8, device=self.solver.device)
+
+    def planes_for(self, eps11, eps33, sigma):
+        p = self.base.copy()
+        p[0] = np.asarray(eps11, dtype=np.float64)
+        p[2] = np.asarray(eps33, dtype=np.float64)
+        p[3] = np.asarray(sigma, dtype=np.float64)
+        p[5] = np.asarray(sigma, dtype=np.float64)
+        return p
+
+    def forward(self, eps11, eps33, sigma):
+        """Run the shot; returns the device trace tensor (nstep, 2, nrec)."""
+        s = self.solver
+        s.set_model(self.planes_for(eps11, eps33, sigma))
+        s.set_source(self.src_ijk, self.srcfn)  # the amplitude is divided by eps11 at the source
+        s.reset()
+        h = s._h
+        for q in range(self.nseg):
+            check(self._L.sfd_checkpoint_save(h, C.c_void_p(self.ckpt[q].data_ptr())))
+            s.run(min(self.ckpt_every, self.nstep - q * self.ckpt_every))
+        s.status()
+        return s.traces_tensor().clone()
+
+    def backward(self, resid):
+        """dJ/d(eps11, eps33, sigma) for dJ/d(traces) = resid (device FP32)."""
+        import torch
+
+        r = resid.detach().to(device=self.solver.device, dtype=torch.float32).contiguous()
+        h = self.solver._h
+        check(self._L.sfd_adjoint_begin(h, C.c_void_p(self.work.data_ptr()), C.c_size_t(self.work.numel()),
+                                        self.ckpt_every, C.c_void_p(r.data_ptr())))
+        for q in reversed(range(self.nseg)):
+            start = q * self.ckpt_every
+            n = min(self.ckpt_every, self.nstep - start)
+            check(self._L.sfd_checkpoint_load(h, C.c_void_p(self.ckpt[q].data_ptr()), start))
+            check(self._L.sfd_adjoint_segment(h, n))
+        g = np.empty((6, self.grid.nz, self.grid.nx))
+        check(self._L.sfd_adjoint_gradient(h, g.ctypes.data_as(C.POINTER(C.c_double)), g.size))
+        torch.cuda.synchronize(self.solver.device)
+        return g[0], g[2], g[3] + g[5], g
+
+    def close(self):
+        self.solver.close()
+
+
+def _make_function():
+    import torch
+
+    class TraceMisfit(torch.autograd.Function):
+        """traces = TraceMisfit.apply(eps11, eps33, sigma, model)."""
+
+        @staticmethod
+        def forward(ctx, eps11, eps33, sigma, model):
+            ctx.model = model
+            ctx.like = (eps11, eps33, sigma)
+            return model.forward(eps11.detach().cpu().numpy(), eps33.detach().cpu().numpy(),
+                                 sigma.detach().cpu().numpy())
+
+        @staticmethod
+        def backward(ctx, grad):
+            g11, g33, gs, _ = ctx.model.backward(grad)
+            outs = []
+            for g, like in zip((g11, g33, gs), ctx.like):
+                outs.append(torch.as_tensor(g, dtype=like.dtype, device=like.device))
+            return outs[0], outs[1], outs[2], None
+
+    return TraceMisfit
+
+
+class _Lazy:
+    _fn = None
+
+    def __getattr__(self, name):
+        if _Lazy._fn is None:
+            _Lazy._fn = _make_function()
+        return getattr(_Lazy._fn, name)
+
+
+TraceMisfit = _Lazy()

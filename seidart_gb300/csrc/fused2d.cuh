@@ -105,7 +105,7 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
         float d = dH * a.Z.ikh[k];
         if (in_strip(k, NZ, W)) {
           const size_t m = (size_t)strip_idx(k, NZ, W) * P + i;
-          const float psi = a.Z.bh[k] * a.mHyz[m] + a.Z.adh[k] * dH;
+          const float psi = a.Z.bh[k] * a.mHyz0[m] + a.Z.adh[k] * dH;
           a.mHyz[m] = psi;
           d += psi;
         }
@@ -116,7 +116,7 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
         float d = dH * a.X.ikh[i];
         if (in_strip(i, NX, W)) {
           const size_t m = (size_t)k * (2 * W) + strip_idx(i, NX, W);
-          const float psi = a.X.bh[i] * a.mHyx[m] + a.X.adh[i] * dH;
+          const float psi = a.X.bh[i] * a.mHyx0[m] + a.X.adh[i] * dH;
           a.mHyx[m] = psi;
           d += psi;
         }

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/seidart_gb300.h"
+#include "adjoint.h"
 #include "batch.h"
 #include "sfd_solvers.h"
 
@@ -232,6 +233,12 @@ struct sfd_handle_s {
   Launch launch1;       // single-pass geometry
   int64_t step = 0;
   std::vector<double> src_scale[3];  // planes the source amplitude is divided by
+  std::vector<double> model;         // FP64 model planes (kept for the adjoint's chain rule)
+  // adjoint workspace (electromag2)
+  char* adj = nullptr;
+  int adj_seg = 0;
+  int adj_cur = 0;
+  const float* adj_resid = nullptr;
   Em2Args em2;
   Seis2Args s2;
   Seis25Args s25;
@@ -288,6 +295,7 @@ void bind_args(sfd_handle* h) {
         b.Ex1 = h->fc(0, 1 - p); b.Ez1 = h->fc(1, 1 - p); b.Hy1 = h->fc(2, 1 - p);
         b.mExz1 = h->mc(0, 1 - p); b.mEzx1 = h->mc(1, 1 - p);
         b.mHyz = h->mc(2, 0); b.mHyx = h->mc(3, 0);
+        b.mHyz0 = b.mHyz; b.mHyx0 = b.mHyx;
         b.caEx = a.caEx; b.cbEx = a.cbEx; b.caEz = a.caEz; b.cbEz = a.cbEz;
         b.X = a.X; b.Z = a.Z; b.dbH = a.dbH; b.io = io;
       }
@@ -524,6 +532,7 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
   int atten = 0;
   switch (c.kind) {
     case SFD_ELECTROMAG2: {
+      h->model.assign(planes, planes + (size_t)count);
       // electromagfdtd.f95:164-181
       const double *e11 = P(0), *e13 = P(1), *e33 = P(2), *s11 = P(3), *s13 = P(4), *s33 = P(5);
       for (size_t q = 0; q < N2; ++q) {
@@ -1005,6 +1014,255 @@ int32_t sfd_batch_destroy(sfd_batch* b) {
   if (!b) return SFD_OK;
   cudaStreamSynchronize(b->stream);
   delete b;
+  return SFD_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Checkpoints and the electromag2 adjoint.
+
+namespace {
+
+size_t ckpt_bytes(const sfd_handle* h) {
+  size_t n = (size_t)nfields(h->cfg.kind) * h->L.fsz;
+  const int nm = (int)strlen(mem_axes(h->cfg.kind));
+  for (int m = 0; m < nm; ++m) n += h->L.mem_sz[m];
+  return n * sizeof(float);
+}
+
+// Adjoint workspace layout: two adjoint states, TH/MEx/MEz, four gradient
+// planes, the source accumulator, then seg+1 forward state slots.
+struct AdjLayout {
+  size_t field, zstrip, xstrip, state, lam[2], th, mex, mez, g[4], acc, slots, total;
+};
+
+AdjLayout adj_layout(const sfd_handle* h, int seg) {
+  AdjLayout A;
+  const Layout& L = h->L;
+  A.field = align256(sizeof(float) * L.fsz);
+  A.zstrip = align256(sizeof(float) * L.mem_sz[0]);  // dEx_dz: z-strip
+  A.xstrip = align256(sizeof(float) * L.mem_sz[1]);  // dEz_dx: x-strip
+  A.state = 3 * A.field + 2 * A.zstrip + 2 * A.xstrip;
+  size_t o = 0;
+  A.lam[0] = o; o += A.state;
+  A.lam[1] = o; o += A.state;
+  A.th = o; o += A.field;
+  A.mex = o; o += A.field;
+  A.mez = o; o += A.field;
+  for (int q = 0; q < 4; ++q) { A.g[q] = o; o += A.field; }
+  A.acc = o; o += 256;
+  A.slots = o; o += A.state * (size_t)(seg + 1);
+  A.total = o;
+  return A;
+}
+
+AdjState adj_state_at(const AdjLayout& A, char* base) {
+  AdjState S;
+  S.Ex = (float*)base;
+  S.Ez = (float*)(base + A.field);
+  S.Hy = (float*)(base + 2 * A.field);
+  S.A = (float*)(base + 3 * A.field);
+  S.C = (float*)(base + 3 * A.field + A.zstrip);
+  S.B = (float*)(base + 3 * A.field + 2 * A.zstrip);
+  S.D = (float*)(base + 3 * A.field + 2 * A.zstrip + A.xstrip);
+  return S;
+}
+
+int adj_check(const sfd_handle* h) {
+  if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
+  if (h->cfg.kind != SFD_ELECTROMAG2 || !h->single)
+    return fail(SFD_ERR_BAD_ARG, "the adjoint is implemented for single-pass electromag2 handles");
+  return SFD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t sfd_checkpoint_bytes(const sfd_handle* h, size_t* bytes) {
+  g_err.clear();
+  if (!h || !bytes) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  *bytes = ckpt_bytes(h);
+  return SFD_OK;
+}
+
+int32_t sfd_checkpoint_save(sfd_handle* h, void* dev_dst) {
+  g_err.clear();
+  if (!h || !dev_dst) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  char* d = (char*)dev_dst;
+  const size_t fb = sizeof(float) * h->L.fsz;
+  for (int q = 0; q < nfields(h->cfg.kind); ++q, d += fb)
+    CK(cudaMemcpyAsync(d, h->f(q), fb, cudaMemcpyDeviceToDevice, h->stream));
+  const int nm = (int)strlen(mem_axes(h->cfg.kind));
+  for (int m = 0; m < nm; ++m) {
+    const size_t mb = sizeof(float) * h->L.mem_sz[m];
+    CK(cudaMemcpyAsync(d, h->m(m), mb, cudaMemcpyDeviceToDevice, h->stream));
+    d += mb;
+  }
+  return SFD_OK;
+}
+
+int32_t sfd_checkpoint_load(sfd_handle* h, const void* dev_src, int64_t step) {
+  g_err.clear();
+  if (!h || !dev_src) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  if (step < 0 || step > h->cfg.nstep) return fail(SFD_ERR_BAD_ARG, "step %lld out of range", (long long)step);
+  const char* d = (const char*)dev_src;
+  const size_t fb = sizeof(float) * h->L.fsz;
+  for (int q = 0; q < nfields(h->cfg.kind); ++q, d += fb)
+    CK(cudaMemcpyAsync(h->f(q), d, fb, cudaMemcpyDeviceToDevice, h->stream));
+  const int nm = (int)strlen(mem_axes(h->cfg.kind));
+  for (int m = 0; m < nm; ++m) {
+    const size_t mb = sizeof(float) * h->L.mem_sz[m];
+    CK(cudaMemcpyAsync(h->m(m), d, mb, cudaMemcpyDeviceToDevice, h->stream));
+    d += mb;
+  }
+  h->step = step;
+  return SFD_OK;
+}
+
+int32_t sfd_adjoint_bytes(const sfd_handle* h, int32_t seg_steps, size_t* bytes) {
+  g_err.clear();
+  int r = adj_check(h);
+  if (r) return r;
+  if (seg_steps < 1 || !bytes) return fail(SFD_ERR_BAD_ARG, "need seg_steps >= 1 and bytes");
+  *bytes = adj_layout(h, seg_steps).total;
+  return SFD_OK;
+}
+
+int32_t sfd_adjoint_begin(sfd_handle* h, void* dev_work, size_t bytes, int32_t seg_steps, const float* dev_resid) {
+  g_err.clear();
+  int r = adj_check(h);
+  if (r) return r;
+  if (!dev_work || ((uintptr_t)dev_work & 255)) return fail(SFD_ERR_BAD_ARG, "workspace must be 256-byte aligned device memory");
+  if (seg_steps < 1) return fail(SFD_ERR_BAD_ARG, "seg_steps must be >= 1");
+  const AdjLayout A = adj_layout(h, seg_steps);
+  if (bytes < A.total) return fail(SFD_ERR_BAD_ARG, "adjoint workspace has %zu bytes, needs %zu", bytes, A.total);
+  if (h->cfg.nrec > 0 && !dev_resid) return fail(SFD_ERR_BAD_ARG, "residual traces are NULL");
+  h->adj = (char*)dev_work;
+  h->adj_seg = seg_steps;
+  h->adj_cur = 0;
+  h->adj_resid = dev_resid;
+  CK(cudaMemsetAsync(h->adj, 0, A.slots, h->stream));  // adjoint states, gradients, accumulators
+  return SFD_OK;
+}
+
+int32_t sfd_adjoint_segment(sfd_handle* h, int64_t nsteps) {
+  g_err.clear();
+  int r = adj_check(h);
+  if (r) return r;
+  if (!h->adj) return fail(SFD_ERR_STATE, "call sfd_adjoint_begin first");
+  if (nsteps < 1 || nsteps > h->adj_seg) return fail(SFD_ERR_BAD_ARG, "segment of %lld steps outside [1, %d]", (long long)nsteps, h->adj_seg);
+  const int64_t s0 = h->step;
+  if (s0 + nsteps > h->cfg.nstep) return fail(SFD_ERR_BAD_ARG, "segment runs past the source length");
+  const AdjLayout A = adj_layout(h, h->adj_seg);
+  const Layout& L = h->L;
+  const int NX = h->cfg.nx, NZ = h->cfg.nz;
+  // slot 0 <- current forward state
+  AdjState S0 = adj_state_at(A, h->adj + A.slots);
+  const size_t fb = sizeof(float) * L.fsz;
+  CK(cudaMemcpyAsync(S0.Ex, h->f(0), fb, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(S0.Ez, h->f(1), fb, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(S0.Hy, h->f(2), fb, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(S0.A, h->m(0), sizeof(float) * L.mem_sz[0], cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(S0.B, h->m(1), sizeof(float) * L.mem_sz[1], cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(S0.C, h->m(2), sizeof(float) * L.mem_sz[2], cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(S0.D, h->m(3), sizeof(float) * L.mem_sz[3], cudaMemcpyDeviceToDevice, h->stream));
+  // forward recompute: slot s -> slot s+1
+  k_begin<<<std::min(1024, (L.nslots + 255) / 256 + 1), 256, 0, h->stream>>>((Ctl*)(h->base + L.off_ctl),
+                                                                            (float*)(h->base + L.off_slots), L.nslots, (int)s0);
+  Em2Step st = h->em2s[0];
+  for (int64_t s = 0; s < nsteps; ++s) {
+    const AdjState a0 = adj_state_at(A, h->adj + A.slots + A.state * (size_t)s);
+    const AdjState a1 = adj_state_at(A, h->adj + A.slots + A.state * (size_t)(s + 1));
+    st.Ex0 = a0.Ex; st.Ez0 = a0.Ez; st.Hy0 = a0.Hy; st.mExz0 = a0.A; st.mEzx0 = a0.B; st.mHyz0 = a0.C; st.mHyx0 = a0.D;
+    st.Ex1 = a1.Ex; st.Ez1 = a1.Ez; st.Hy1 = a1.Hy; st.mExz1 = a1.A; st.mEzx1 = a1.B; st.mHyz = a1.C; st.mHyx = a1.D;
+    em2_step(st, h->launch1, h->zb, (int)s, h->stream);
+  }
+  // adjoint sweep over the segment, last step first
+  Em2Adj a;
+  const Em2Args& e = h->em2;
+  a.NX = NX; a.NZ = NZ; a.P = L.P; a.W = L.W;
+  a.caEx = e.caEx; a.cbEx = e.cbEx; a.caEz = e.caEz; a.cbEz = e.cbEz;
+  a.X = e.X; a.Z = e.Z; a.dbH = e.dbH;
+  a.TH = (float*)(h->adj + A.th); a.MEx = (float*)(h->adj + A.mex); a.MEz = (float*)(h->adj + A.mez);
+  a.gCAx = (float*)(h->adj + A.g[0]); a.gCBx = (float*)(h->adj + A.g[1]);
+  a.gCAz = (float*)(h->adj + A.g[2]); a.gCBz = (float*)(h->adj + A.g[3]);
+  a.srcacc = (float*)(h->adj + A.acc);
+  a.srcfn = (const float*)(h->base + L.off_src);
+  a.nstep = h->cfg.nstep; a.si = h->em2.io.si; a.sk = h->em2.io.sk;
+  a.rec = (const int*)(h->base + L.off_rec); a.nrec = h->cfg.nrec; a.resid = h->adj_resid;
+  for (int64_t s = nsteps - 1; s >= 0; --s) {
+    const AdjState S = adj_state_at(A, h->adj + A.slots + A.state * (size_t)s);
+    const AdjState Lc = adj_state_at(A, h->adj + A.lam[h->adj_cur]);
+    const AdjState Ln = adj_state_at(A, h->adj + A.lam[1 - h->adj_cur]);
+    adj_step(a, S, Lc, Ln, (int)(s0 + s), h->stream);
+    h->adj_cur ^= 1;
+  }
+  CK(cudaGetLastError());
+  return SFD_OK;
+}
+
+int32_t sfd_adjoint_gradient(sfd_handle* h, double* out, int64_t count) {
+  g_err.clear();
+  int r = adj_check(h);
+  if (r) return r;
+  if (!h->adj) return fail(SFD_ERR_STATE, "call sfd_adjoint_begin first");
+  const int NX = h->cfg.nx, NZ = h->cfg.nz, P = h->L.P;
+  const size_t N2 = (size_t)NX * NZ;
+  if (!out || count != (int64_t)(6 * N2)) return fail(SFD_ERR_BAD_ARG, "gradient needs 6 planes of %dx%d", NX, NZ);
+  const AdjLayout A = adj_layout(h, h->adj_seg);
+  std::vector<float> g[4];
+  for (int q = 0; q < 4; ++q) {
+    g[q].resize((size_t)P * NZ);
+    CK(cudaMemcpyAsync(g[q].data(), h->adj + A.g[q], sizeof(float) * g[q].size(), cudaMemcpyDeviceToHost, h->stream));
+  }
+  float acc[2];
+  CK(cudaMemcpyAsync(acc, h->adj + A.acc, sizeof acc, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  const double dt = h->cfg.dt;
+  const double *e11 = h->model.data(), *e13 = e11 + N2, *e33 = e11 + 2 * N2;
+  const double *s11 = e11 + 3 * N2, *s13 = e11 + 4 * N2, *s33 = e11 + 5 * N2;
+  double *g11 = out, *g13 = out + N2, *g33 = out + 2 * N2, *gs11 = out + 3 * N2, *gs13 = out + 4 * N2,
+         *gs33 = out + 5 * N2;
+  std::fill(out, out + 6 * N2, 0.0);
+  auto G = [&](int q, int i, int k) -> double {
+    if (i < 0 || i >= NX || k < 0 || k >= NZ) return 0.0;
+    return g[q][(size_t)k * P + i];
+  };
+  for (int k = 0; k < NZ; ++k)
+    for (int i = 0; i < NX; ++i) {
+      const size_t n = (size_t)i + (size_t)NX * k;
+      // caEx(i,k) enters CAx(i,k) and CAx(i,k+1); caEz(i,k) enters CAz(i,k) and CAz(i+1,k)
+      const double dcaX = 0.5 * (G(0, i, k) + G(0, i, k + 1)), dcbX = 0.5 * (G(1, i, k) + G(1, i, k + 1));
+      const double dcaZ = 0.5 * (G(2, i, k) + G(2, i + 1, k)), dcbZ = 0.5 * (G(3, i, k) + G(3, i + 1, k));
+      // ca = (1-u)/(1+u), cb = (dt/e)/(1+u), u = s dt / (2 e), e = (eps_a + eps_b) eps0 (electromagfdtd.f95:164-176)
+      auto chain = [&](double epsr, double sig, double dca, double dcb, double* de, double* ds) {
+        const double ep = epsr * kEps0;
+        const double u = sig * dt / (2.0 * ep);
+        const double w = 1.0 / ((1.0 + u) * (1.0 + u));
+        const double dca_de = 2.0 * u / ep * w, dca_ds = -dt / ep * w;
+        const double dcb_de = -dt / (ep * ep) * w, dcb_ds = -dt * dt / (2.0 * ep * ep) * w;
+        *de = (dca * dca_de + dcb * dcb_de) * kEps0;
+        *ds = dca * dca_ds + dcb * dcb_ds;
+      };
+      double deX, dsX, deZ, dsZ;
+      chain(e11[n] + e13[n], s11[n] + s13[n], dcaX, dcbX, &deX, &dsX);
+      chain(e13[n] + e33[n], s13[n] + s33[n], dcaZ, dcbZ, &deZ, &dsZ);
+      g11[n] = deX;
+      g33[n] = deZ;
+      g13[n] = deX + deZ;
+      gs11[n] = dsX;
+      gs33[n] = dsZ;
+      gs13[n] = dsX + dsZ;
+    }
+  // source: Ex(s) += srcx dt / eps11(s), Ez(s) += srcz dt / eps33(s) (electromagfdtd.f95:300-301)
+  const int si = h->em2.io.si, sk = h->em2.io.sk;
+  if (si >= 0) {
+    const size_t n = (size_t)si + (size_t)NX * sk;
+    g11[n] += -(double)acc[0] / e11[n];
+    g33[n] += -(double)acc[1] / e33[n];
+  }
   return SFD_OK;
 }
 

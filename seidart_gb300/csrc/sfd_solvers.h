@@ -84,7 +84,8 @@ struct Em2Step {
   int NX, NZ, P, W;
   const float *Ex0, *Ez0, *Hy0, *mExz0, *mEzx0;  // old
   float *Ex1, *Ez1, *Hy1, *mExz1, *mEzx1;        // new
-  float *mHyz, *mHyx;                            // in place
+  const float *mHyz0, *mHyx0;                    // second-half memory, read ...
+  float *mHyz, *mHyx;                            // ... and written (the same arrays except in adjoint recompute)
   const float *caEx, *cbEx, *caEz, *cbEz;
   AxisTab X, Z;
   float dbH;
