@@ -168,13 +168,27 @@ def launches_per_shot(kind, nstep, single_pass=True):
     return per * nstep + nstep // 32 + 3 + (1 if kind == ELECTROMAG25 else 0)
 
 
-def bench_batched(device, flush, stream, peak, plain_value, runs=2):
+def bench_plain(case, device, flush, stream, peak, bytes_fn, steps, warmup):
+    """One plain configuration: shots of `case`, kernel times, roofline fractions."""
+    s = make_solver(case, device)
+    ms = time_shots(s, case.nstep, max(1, steps), warmup, flush, stream)
+    kt = kernel_times(s, stream, n=20)
+    b = bytes_fn(case.grid)
+    r = case.grid.cells * case.nstep / (ms / 1e3) / 1e9
+    s.close()
+    return {"workload": f"{case.name}: {case.grid.cells} cells x {case.nstep} steps", "value": round(r, 3),
+            "unit": METRIC, "ms_per_shot": round(ms, 3), "bytes_per_cell_update": round(b["per_cell_step"], 1),
+            "hbm_frac": round(b["per_cell_step"] * r / peak, 4), "kernel_ms": [round(x, 4) for x in kt],
+            "kernel_frac": [round(b[h] / (t / 1e3) / 1e9 / peak, 4) for h, t in zip(("half1", "half2"), kt)]}
+
+
+def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000):
     """The batched survey: 64 electromag2 shots of the layered 1000x500 model (sources every 15
     cells) + 16 seeded seismic2 models of uneven size, 4000 steps, one persistent launch per run."""
     import torch
     from seidart_gb300 import ELECTROMAG2, synthetic as sy
     from seidart_gb300.batch import Batch, autotune
-    shots, models = sy.batched_survey(nshots=64, nelastic=16, nstep=4000)
+    shots, models = sy.batched_survey(nshots=64, nelastic=16, nstep=nstep)
     cases = shots + models
     solvers = [make_solver(c, device) for c in cases]
     b = Batch(solvers)
@@ -407,6 +421,22 @@ def run_ours(args):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
     peak, peak_kind = _peaks()
 
+    if args.only:
+        # one leg alone (profiler runs): prints that leg's record, not a bench line
+        if args.only == "seismic2":
+            rec = bench_plain(sy.seismic2_firn_ice(nstep=args.time_steps if args.time_steps != 6000 else 2000),
+                              device, flush, stream, peak, seis2_bytes, args.steps, args.warmup)
+        elif args.only == "seismic25":
+            rec = bench_plain(sy.seismic25_ice(nstep=args.time_steps if args.time_steps != 6000 else 3000),
+                              device, flush, stream, peak, seis25_bytes, args.steps, args.warmup)
+        elif args.only == "batched":
+            rec = bench_batched(device, flush, stream, peak, 1.0, runs=args.steps,
+                                nstep=args.time_steps if args.time_steps != 6000 else 4000)
+        else:
+            rec = bench_adjoint(device)
+        print(json.dumps({"only": args.only, **rec}), flush=True)
+        return 0
+
     # ---- headline: electromag2 plain, one shot per bench step --------------
     case = sy.electromag2_layers(nstep=args.time_steps)
     g = case.grid
@@ -480,30 +510,10 @@ def run_ours(args):
     # ---- extra lines: the other plain configurations ------------------------
     if not args.skip_extras:
         extras = {}
-        c0 = sy.seismic2_firn_ice(nstep=2000)
-        s0 = make_solver(c0, device)
-        ms0 = time_shots(s0, c0.nstep, 5, 2, flush, stream)
-        b0 = seis2_bytes(c0.grid)
-        r0 = c0.grid.cells * c0.nstep / (ms0 / 1e3) / 1e9
-        extras["seismic2_plain"] = {"workload": "seismic2 firn/ice 440x240 cells x 2000 steps",
-                                    "value": round(r0, 3), "unit": METRIC, "ms_per_shot": round(ms0, 3),
-                                    "bytes_per_cell_update": round(b0["per_cell_step"], 1),
-                                    "hbm_frac": round(b0["per_cell_step"] * r0 / peak, 4)}
-        s0.close()
-        c2 = sy.seismic25_ice(nstep=3000)
-        s2 = make_solver(c2, device)
-        ms2 = time_shots(s2, c2.nstep, 2, 1, flush, stream)
-        kt2 = kernel_times(s2, stream, n=20)
-        b2 = seis25_bytes(c2.grid)
-        r2 = c2.grid.cells * c2.nstep / (ms2 / 1e3) / 1e9
-        extras["seismic25_plain"] = {"workload": "seismic25 ice 630x70x330 cells x 3000 steps",
-                                     "value": round(r2, 3), "unit": METRIC, "ms_per_shot": round(ms2, 2),
-                                     "bytes_per_cell_update": round(b2["per_cell_step"], 1),
-                                     "hbm_frac": round(b2["per_cell_step"] * r2 / peak, 4),
-                                     "kernel_ms": [round(x, 4) for x in kt2],
-                                     "kernel_frac": [round(b2[h] / (t / 1e3) / 1e9 / peak, 4)
-                                                     for h, t in zip(("half1", "half2"), kt2)]}
-        s2.close()
+        extras["seismic2_plain"] = bench_plain(sy.seismic2_firn_ice(nstep=2000), device, flush, stream, peak,
+                                               seis2_bytes, 5, 2)
+        extras["seismic25_plain"] = bench_plain(sy.seismic25_ice(nstep=3000), device, flush, stream, peak,
+                                                seis25_bytes, 2, 1)
         line["extras"] = extras
     if not args.skip_batched:
         line.setdefault("extras", {})["batched"] = bench_batched(device, flush, stream, peak, value / world)
@@ -533,6 +543,8 @@ def main(argv=None):
     ap.add_argument("--time-steps", type=int, default=6000,
                     help="time steps per headline shot (6000 = the workload; smaller only for profiler runs)")
     ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--only", choices=["seismic2", "seismic25", "batched", "adjoint"],
+                    help="run one secondary leg alone and print its record (for profiler runs)")
     ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--headline-only", action="store_true",
                     help="only the timed headline shots (for profiler runs): no e2e, extras or CPU leg")

@@ -13,7 +13,7 @@ struct AdjState {
 
 struct Em2Adj {
   int NX, NZ, P, W;
-  const float *caEx, *cbEx, *caEz, *cbEz;
+  const float *CAx, *CBx, *CAz, *CBz;  // staggered-averaged coefficients
   AxisTab X, Z;
   float dbH;
   float *TH, *MEx, *MEz;            // adjoint of Hy', E-half parts of the E adjoints

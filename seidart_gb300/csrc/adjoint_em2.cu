@@ -9,6 +9,7 @@
 //   source, then Dirichlet masks on Ex', Ez', Hy'; receivers sample Ex', Ez'.
 // with dEx = Ex(i,k+1) - Ex(i,k), dEz = Ez(i+1,k) - Ez(i,k), dHz = Hy'(i,k) -
 // Hy'(i,k-1), dHx = Hy'(i,k) - Hy'(i-1,k), CAx = (caEx(i,k) + caEx(i,k-1))/2 etc.
+// (the averaged coefficients are stored per cell).
 // The adjoint step is the exact transpose, in reverse order, written as a
 // gather (each thread writes only its own cell):
 //   adj_e: masks, the E half transposed, the coefficient gradients
@@ -57,7 +58,7 @@ __device__ __forceinline__ float lam_masked_ez(const Em2Adj& a, const AdjState& 
 __device__ __forceinline__ float gx_at(const Em2Adj& a, const AdjState& L, int i, int k) {
   if (!ex_range(i, k, a.NX, a.NZ)) return 0.0f;
   const size_t c = (size_t)k * a.P + i;
-  const float cb = 0.5f * (a.cbEx[c] + a.cbEx[c - a.P]);
+  const float cb = a.CBx[c];
   float g = cb * lam_masked_ex(a, L, i, k) * (a.Z.ikh[k] + a.Z.adh[k]);
   if (in_strip(k, a.NZ, a.W)) g += L.C[(size_t)strip_idx(k, a.NZ, a.W) * a.P + i] * a.Z.adh[k];
   return g;
@@ -67,7 +68,7 @@ __device__ __forceinline__ float gx_at(const Em2Adj& a, const AdjState& L, int i
 __device__ __forceinline__ float gz_at(const Em2Adj& a, const AdjState& L, int i, int k) {
   if (!ez_range(i, k, a.NX, a.NZ)) return 0.0f;
   const size_t c = (size_t)k * a.P + i;
-  const float cb = 0.5f * (a.cbEz[c] + a.cbEz[c - 1]);
+  const float cb = a.CBz[c];
   float g = cb * lam_masked_ez(a, L, i, k) * (a.X.ikh[i] + a.X.adh[i]);
   if (in_strip(i, a.NX, a.W)) g += L.D[(size_t)k * (2 * a.W) + strip_idx(i, a.NX, a.W)] * a.X.adh[i];
   return g;
@@ -104,8 +105,7 @@ __global__ void __launch_bounds__(BX * BY) adj_e_kernel(Em2Adj a, AdjState S, Ad
   // Ex half transposed
   float mex = lex, mez = lez;
   if (ex_range(i, k, NX, NZ)) {
-    const float ca = 0.5f * (a.caEx[c] + a.caEx[c - P]);
-    const float cb = 0.5f * (a.cbEx[c] + a.cbEx[c - P]);
+    const float ca = a.CAx[c], cb = a.CBx[c];
     mex = ca * lex;
     const float dHz = hprime(a, S, i, k) - hprime(a, S, i, k - 1);
     float d = dHz * a.Z.ikh[k];
@@ -120,8 +120,7 @@ __global__ void __launch_bounds__(BX * BY) adj_e_kernel(Em2Adj a, AdjState S, Ad
     Ln.C[mz] = L.C[mz];
   }
   if (ez_range(i, k, NX, NZ)) {
-    const float ca = 0.5f * (a.caEz[c] + a.caEz[c - 1]);
-    const float cb = 0.5f * (a.cbEz[c] + a.cbEz[c - 1]);
+    const float ca = a.CAz[c], cb = a.CBz[c];
     mez = ca * lez;
     const float dHx = hprime(a, S, i, k) - hprime(a, S, i - 1, k);
     float d = dHx * a.X.ikh[i];

@@ -72,9 +72,7 @@ __global__ void __launch_bounds__(BX * BY) em2_e_kernel(Em2Args a, int rel) {
           a.mHyz[m] = psi;
           d += psi;
         }
-        const float ca = 0.5f * (a.caEx[c] + a.caEx[c - P]);
-        const float cb = 0.5f * (a.cbEx[c] + a.cbEx[c - P]);
-        ex = ca * ex + cb * d;
+        ex = a.CAx[c] * ex + a.CBx[c] * d;
       }
     }
     // Ez, :285-295 (k in [0, NZ-2], i in [1, NX-2])
@@ -89,9 +87,7 @@ __global__ void __launch_bounds__(BX * BY) em2_e_kernel(Em2Args a, int rel) {
           a.mHyx[m] = psi;
           d += psi;
         }
-        const float ca = 0.5f * (a.caEz[c] + a.caEz[c - 1]);
-        const float cb = 0.5f * (a.cbEz[c] + a.cbEz[c - 1]);
-        ez = ca * ez + cb * d;
+        ez = a.CAz[c] * ez + a.CBz[c] * d;
       }
     }
     // Source, :300-301
@@ -104,7 +100,7 @@ __global__ void __launch_bounds__(BX * BY) em2_e_kernel(Em2Args a, int rel) {
     if (i == 0 || i == NX - 1 || k == 0 || k == NZ - 2) ez = 0.0f;
     if (i <= NX - 2) a.Ex[c] = ex;
     if (k <= NZ - 2) a.Ez[c] = ez;
-    norm = hypotf(ex, ez);
+    norm = norm_monitor(ex, ez);
   }
   block_norm_to_slot(norm, a.io.slots, blockIdx.y * gridDim.x + blockIdx.x);
 }

@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(BX * BZ) em25_e_kernel(Em25Args a, int rel) {
       a.Ex[c] = ex;
       a.Ey[c] = ey;
       a.Ez[c] = ez;
-      norm = fmaxf(norm, nan_to_inf(norm3df(ex, ey, ez)));
+      norm = fmaxf(norm, norm_monitor(ex, ey, ez));
     }
   }
   block_norm_to_slot(norm, a.io.slots, (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);

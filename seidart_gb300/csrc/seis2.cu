@@ -42,7 +42,6 @@ __global__ void __launch_bounds__(BX * BY) seis2_stress_kernel(Seis2Args a, int 
   if (zs) { m_vzz = a.m_vzz[mz]; m_vxz = a.m_vxz[mz]; }
   const float vx0 = a.vx[c], vz0 = a.vz[c];
   const float ikx = a.X.ik[i], ikxh = a.X.ikh[i], ikz = a.Z.ik[k], ikzh = a.Z.ikh[k];
-  const float c11 = a.c11[c], c13 = a.c13[c], c15 = a.c15[c], c33 = a.c33[c], c35 = a.c35[c];
 
   if (loop1) {
     const float d_vx_x = a.vx[c + 1] - vx0;
@@ -61,12 +60,7 @@ __global__ void __launch_bounds__(BX * BY) seis2_stress_kernel(Seis2Args a, int 
     const float dvz_dz = d_vz_z * ikz + m_vzz;
     const float dvz_dx = d_vz_x * ikx + m_vzx;
     const float dvx_dz = d_vx_z * ikzh + m_vxz;
-    // (c(i+1,j) + 2 c(i,j) + c(i,j-1)) / 4, stiffness already scaled by dt
-    const float A11 = 0.25f * (a.c11[c + 1] + 2.f * c11 + a.c11[c - P]);
-    const float A13 = 0.25f * (a.c13[c + 1] + 2.f * c13 + a.c13[c - P]);
-    const float A15 = 0.25f * (a.c15[c + 1] + 2.f * c15 + a.c15[c - P]);
-    const float A33 = 0.25f * (a.c33[c + 1] + 2.f * c33 + a.c33[c - P]);
-    const float A35 = 0.25f * (a.c35[c + 1] + 2.f * c35 + a.c35[c - P]);
+    const float A11 = a.A11[c], A13 = a.A13[c], A15 = a.A15[c], A33 = a.A33[c], A35 = a.A35[c];
     const float shear = dvz_dx + dvx_dz;
     a.sxx[c] = a.sxx[c] + (A11 * dvx_dx + A13 * dvz_dz + A15 * shear);
     a.szz[c] = a.szz[c] + (A13 * dvx_dx + A33 * dvz_dz + A35 * shear);
@@ -88,10 +82,7 @@ __global__ void __launch_bounds__(BX * BY) seis2_stress_kernel(Seis2Args a, int 
     const float dvz_dz = d_vz_z * ikz + m_vzz;
     const float dvz_dx = d_vz_x * ikx + m_vzx;
     const float dvx_dz = d_vx_z * ikzh + m_vxz;
-    // (c(i,j+1) + 2 c(i,j) + c(i-1,j)) / 4
-    const float B15 = 0.25f * (a.c15[c + P] + 2.f * c15 + a.c15[c - 1]);
-    const float B35 = 0.25f * (a.c35[c + P] + 2.f * c35 + a.c35[c - 1]);
-    const float B55 = 0.25f * (a.c55[c + P] + 2.f * a.c55[c] + a.c55[c - 1]);
+    const float B15 = a.B15[c], B35 = a.B35[c], B55 = a.B55[c];
     a.sxz[c] = a.sxz[c] + (B15 * dvx_dx + B35 * dvz_dz + B55 * (dvz_dx + dvx_dz));
   }
   if (xs) { a.m_vxx[mx] = m_vxx; a.m_vzx[mx] = m_vzx; }
@@ -174,7 +165,7 @@ __global__ void __launch_bounds__(BX * BY) seis2_velocity_kernel(Seis2Args a, in
     if (!interior) { vx = 0.f; vz = 0.f; }  // :365-375
     a.vx[c] = vx;
     a.vz[c] = vz;
-    norm = hypotf(vx, vz);
+    norm = norm_monitor(vx, vz);
   }
   block_norm_to_slot(norm, a.io.slots, blockIdx.y * gridDim.x + blockIdx.x);
 }

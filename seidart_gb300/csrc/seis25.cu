@@ -35,7 +35,7 @@ struct Col {
   }
 };
 
-__global__ void __launch_bounds__(BX * BZ) seis25_stress_kernel(Seis25Args a, int rel) {
+__global__ void __launch_bounds__(BX * BZ, 5) seis25_stress_kernel(Seis25Args a, int rel) {
   const Ctl* ctl = a.io.ctl;
   const int t = ctl->base + rel;
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && t > ctl->run_start) {
@@ -104,25 +104,41 @@ __global__ void __launch_bounds__(BX * BZ) seis25_stress_kernel(Seis25Args a, in
   const float idx = a.idx, idz = a.idz;
   const size_t plane = (size_t)NY * P;      // one z-plane of a field
 
-  for (int j = j0; j < j1; ++j) {
-    const size_t c = ((size_t)k * NY + j) * P + i;
+  // Velocities are read-only in this kernel: read them through the
+  // non-coherent path, once per cell, and carry the y-neighbours in registers.
+  const float* __restrict__ VX = a.vx;
+  const float* __restrict__ VY = a.vy;
+  const float* __restrict__ VZ = a.vz;
+  const bool has_xm = i >= 1, has_xp = i <= NX - 2, has_zm = k >= 1, has_zp = k <= NZ - 2;
+  size_t c = ((size_t)k * NY + j0) * P + i;
+  float cvx = __ldg(VX + c), cvy = __ldg(VY + c), cvz = __ldg(VZ + c);
+  float pvx = 0.f, pvy = 0.f, pvz = 0.f;
+  if (j0 >= 1) { pvx = __ldg(VX + c - P); pvy = __ldg(VY + c - P); pvz = __ldg(VZ + c - P); }
+  for (int j = j0; j < j1; ++j, c += P) {
     const bool ys = in_strip(j, NY, W);
     const size_t mx = ((size_t)k * NY + j) * (2 * W) + xsi;
     const size_t my = ((size_t)k * (2 * W) + (ys ? strip_idx(j, NY, W) : 0)) * P + i;
     const size_t mz = ((size_t)zsi * NY + j) * P + i;
+    float nvx = 0.f, nvy = 0.f, nvz = 0.f;
+    if (j + 1 < NY) { nvx = __ldg(VX + c + P); nvy = __ldg(VY + c + P); nvz = __ldg(VZ + c + P); }
+    float xmx = 0.f, xmy = 0.f, xmz = 0.f, xpx = 0.f, xpy = 0.f, xpz = 0.f;
+    float zmx = 0.f, zmy = 0.f, zmz = 0.f, zpx = 0.f, zpy = 0.f, zpz = 0.f;
+    if (has_xm) { xmx = __ldg(VX + c - 1); xmy = __ldg(VY + c - 1); xmz = __ldg(VZ + c - 1); }
+    if (has_xp) { xpx = __ldg(VX + c + 1); xpy = __ldg(VY + c + 1); xpz = __ldg(VZ + c + 1); }
+    if (has_zm) { zmx = __ldg(VX + c - plane); zmy = __ldg(VY + c - plane); zmz = __ldg(VZ + c - plane); }
+    if (has_zp) { zpx = __ldg(VX + c + plane); zpy = __ldg(VY + c + plane); zpz = __ldg(VZ + c + plane); }
     float mvxx = 0, mvyx = 0, mvzx = 0, mvxy = 0, mvyy = 0, mvzy = 0, mvxz = 0, mvyz = 0, mvzz = 0;
     if (xs) { mvxx = a.m_vx_x[mx]; mvyx = a.m_vy_x[mx]; mvzx = a.m_vz_x[mx]; }
     if (ys) { mvxy = a.m_vx_y[my]; mvyy = a.m_vy_y[my]; mvzy = a.m_vz_y[my]; }
     if (zs) { mvxz = a.m_vx_z[mz]; mvyz = a.m_vy_z[mz]; mvzz = a.m_vz_z[mz]; }
     const float iky = a.Y.ik[j], ikyh = a.Y.ikh[j], ady = a.Y.ad[j], adyh = a.Y.adh[j];
     const float by = a.Y.b[j], byh = a.Y.bh[j];
-    const float vx0 = a.vx[c], vy0 = a.vy[c], vz0 = a.vz[c];
 
-    // ---- Loop 1: sigmaxx, sigmayy, sigmazz (j >= 1)
+    // ---- Loop 1: sigmaxx, sigmayy, sigmazz (j >= 1): x+, y-, z- differences
     if (L1 && j >= 1) {
-      const float dxx = a.vx[c + 1] - vx0, dyx = a.vy[c + 1] - vy0, dzx = a.vz[c + 1] - vz0;
-      const float dyy = vy0 - a.vy[c - P], dxy = vx0 - a.vx[c - P], dzy = vz0 - a.vz[c - P];
-      const float dzz = vz0 - a.vz[c - plane], dxz = vx0 - a.vx[c - plane], dyz = vy0 - a.vy[c - plane];
+      const float dxx = xpx - cvx, dyx = xpy - cvy, dzx = xpz - cvz;
+      const float dyy = cvy - pvy, dxy = cvx - pvx, dzy = cvz - pvz;
+      const float dzz = cvz - zmz, dxz = cvx - zmx, dyz = cvy - zmy;
       if (xs) { mvxx = bxh * mvxx + adxh * dxx; mvyx = bxh * mvyx + adxh * dyx; mvzx = bxh * mvzx + adxh * dzx; }
       if (ys) { mvyy = by * mvyy + ady * dyy; mvxy = by * mvxy + ady * dxy; mvzy = by * mvzy + ady * dzy; }
       if (zs) { mvzz = bz * mvzz + adz * dzz; mvxz = bz * mvxz + adz * dxz; mvyz = bz * mvyz + adz * dyz; }
@@ -136,11 +152,11 @@ __global__ void __launch_bounds__(BX * BZ) seis25_stress_kernel(Seis25Args a, in
       a.szz[c] = a.szz[c] + (p13 * vxx + p23 * vyy + p33 * vzz + p34 * (vyz + vzy) + p35 * (vxz + vzx) +
                              p36 * (vyx + vxy));
     }
-    // ---- Loop 2: sigmaxy (j <= NY-2)
+    // ---- Loop 2: sigmaxy (j <= NY-2): x-, y+, z-
     if (L2 && j <= NY - 2) {
-      const float dxx = vx0 - a.vx[c - 1], dyx = vy0 - a.vy[c - 1], dzx = vz0 - a.vz[c - 1];
-      const float dyy = a.vy[c + P] - vy0, dxy = a.vx[c + P] - vx0, dzy = a.vz[c + P] - vz0;
-      const float dzz = vz0 - a.vz[c - plane], dxz = vx0 - a.vx[c - plane], dyz = vy0 - a.vy[c - plane];
+      const float dxx = cvx - xmx, dyx = cvy - xmy, dzx = cvz - xmz;
+      const float dyy = nvy - cvy, dxy = nvx - cvx, dzy = nvz - cvz;
+      const float dzz = cvz - zmz, dxz = cvx - zmx, dyz = cvy - zmy;
       if (xs) { mvxx = bx * mvxx + adx * dxx; mvyx = bx * mvyx + adx * dyx; mvzx = bx * mvzx + adx * dzx; }
       if (ys) { mvyy = byh * mvyy + adyh * dyy; mvxy = byh * mvxy + adyh * dxy; mvzy = byh * mvzy + adyh * dzy; }
       if (zs) { mvzz = bzh * mvzz + adzh * dzz; mvxz = bzh * mvxz + adzh * dxz; mvyz = bzh * mvyz + adzh * dyz; }
@@ -151,11 +167,11 @@ __global__ void __launch_bounds__(BX * BZ) seis25_stress_kernel(Seis25Args a, in
       a.sxy[c] = a.sxy[c] + (q16 * vxx + q26 * vyy + q36 * vzz + q46 * (vzy + vyz) + q56 * (vzx + vxz) +
                              q66 * (vyx + vxy));
     }
-    // ---- Loop 3: sigmaxz (j >= 1)
+    // ---- Loop 3: sigmaxz (j >= 1): x-, y-, z+
     if (L3 && j >= 1) {
-      const float dxx = vx0 - a.vx[c - 1], dyx = vy0 - a.vy[c - 1], dzx = vz0 - a.vz[c - 1];
-      const float dyy = vy0 - a.vy[c - P], dzy = vz0 - a.vz[c - P], dxy = vx0 - a.vx[c - P];
-      const float dzz = a.vz[c + plane] - vz0, dxz = a.vx[c + plane] - vx0, dyz = a.vy[c + plane] - vy0;
+      const float dxx = cvx - xmx, dyx = cvy - xmy, dzx = cvz - xmz;
+      const float dyy = cvy - pvy, dzy = cvz - pvz, dxy = cvx - pvx;
+      const float dzz = zpz - cvz, dxz = zpx - cvx, dyz = zpy - cvy;
       if (xs) { mvxx = bx * mvxx + adx * dxx; mvyx = bx * mvyx + adx * dyx; mvzx = bx * mvzx + adx * dzx; }
       if (ys) { mvyy = by * mvyy + ady * dyy; mvxy = by * mvxy + ady * dxy; mvzy = by * mvzy + ady * dzy; }
       if (zs) { mvzz = bzh * mvzz + adzh * dzz; mvxz = bzh * mvxz + adzh * dxz; mvyz = bzh * mvyz + adzh * dyz; }
@@ -165,11 +181,11 @@ __global__ void __launch_bounds__(BX * BZ) seis25_stress_kernel(Seis25Args a, in
       a.sxz[c] = a.sxz[c] + (r15 * vxx + r25 * vyy + r35 * vzz + r45 * (vxz + vzx) + r55 * (vxz + vzx) +
                              r56 * (vxy + vyx));
     }
-    // ---- Loop 4: sigmayz (j <= NY-2)
+    // ---- Loop 4: sigmayz (j <= NY-2): x+, y+, z+
     if (L4 && j <= NY - 2) {
-      const float dxx = a.vx[c + 1] - vx0, dyx = a.vy[c + 1] - vy0, dzx = a.vz[c + 1] - vz0;
-      const float dyy = a.vy[c + P] - vy0, dxy = a.vx[c + P] - vx0, dzy = a.vz[c + P] - vz0;
-      const float dzz = a.vz[c + plane] - vz0, dxz = a.vx[c + plane] - vx0, dyz = a.vy[c + plane] - vy0;
+      const float dxx = xpx - cvx, dyx = xpy - cvy, dzx = xpz - cvz;
+      const float dyy = nvy - cvy, dxy = nvx - cvx, dzy = nvz - cvz;
+      const float dzz = zpz - cvz, dxz = zpx - cvx, dyz = zpy - cvy;
       if (xs) { mvxx = bxh * mvxx + adxh * dxx; mvyx = bxh * mvyx + adxh * dyx; mvzx = bxh * mvzx + adxh * dzx; }
       if (ys) { mvyy = byh * mvyy + adyh * dyy; mvxy = byh * mvxy + adyh * dxy; mvzy = byh * mvzy + adyh * dzy; }
       if (zs) { mvzz = bzh * mvzz + adzh * dzz; mvxz = bzh * mvxz + adzh * dxz; mvyz = bzh * mvyz + adzh * dyz; }
@@ -182,6 +198,8 @@ __global__ void __launch_bounds__(BX * BZ) seis25_stress_kernel(Seis25Args a, in
     if (xs) { a.m_vx_x[mx] = mvxx; a.m_vy_x[mx] = mvyx; a.m_vz_x[mx] = mvzx; }
     if (ys) { a.m_vx_y[my] = mvxy; a.m_vy_y[my] = mvyy; a.m_vz_y[my] = mvzy; }
     if (zs) { a.m_vx_z[mz] = mvxz; a.m_vy_z[mz] = mvyz; a.m_vz_z[mz] = mvzz; }
+    pvx = cvx; pvy = cvy; pvz = cvz;
+    cvx = nvx; cvy = nvy; cvz = nvz;
   }
 }
 
@@ -211,17 +229,31 @@ __global__ void __launch_bounds__(BX * BZ) seis25_velocity_kernel(Seis25Args a, 
     const float bz = a.Z.b[k], bzh = a.Z.bh[k];
     const size_t plane = (size_t)NY * P;
     const bool xface = (i == 0) || (i == NX - 1) || (k == 0) || (k == NZ - 1);
-    for (int j = j0; j < j1; ++j) {
-      const size_t c = ((size_t)k * NY + j) * P + i;
+    // Stresses are read-only here: one non-coherent load per value, sxy/syz at
+    // j-1 and syy at j+1 carried along the y march.
+    const float* __restrict__ SXX = a.sxx;
+    const float* __restrict__ SYY = a.syy;
+    const float* __restrict__ SZZ = a.szz;
+    const float* __restrict__ SXY = a.sxy;
+    const float* __restrict__ SXZ = a.sxz;
+    const float* __restrict__ SYZ = a.syz;
+    size_t c = ((size_t)k * NY + j0) * P + i;
+    float psxy = 0.f, psyz = 0.f;
+    if (j0 >= 1) { psxy = __ldg(SXY + c - P); psyz = __ldg(SYZ + c - P); }
+    float csyy = __ldg(SYY + c);
+    for (int j = j0; j < j1; ++j, c += P) {
       const bool ys = in_strip(j, NY, W);
       const size_t mx = ((size_t)k * NY + j) * (2 * W) + xsi;
       const size_t my = ((size_t)k * (2 * W) + (ys ? strip_idx(j, NY, W) : 0)) * P + i;
       const size_t mz = ((size_t)zsi * NY + j) * P + i;
       const float iky = a.Y.ik[j], ikyh = a.Y.ikh[j], ady = a.Y.ad[j], adyh = a.Y.adh[j];
       const float by = a.Y.b[j], byh = a.Y.bh[j];
+      const float csxx = __ldg(SXX + c), csxy = __ldg(SXY + c), csxz = __ldg(SXZ + c);
+      const float csyz = __ldg(SYZ + c), cszz = __ldg(SZZ + c);
+      const float nsyy = (j + 1 < NY) ? __ldg(SYY + c + P) : 0.f;
       float vx = a.vx[c], vy = a.vy[c], vz = a.vz[c];
       if (Vx && j >= 1) {  // :821-845
-        const float d1 = a.sxx[c] - a.sxx[c - 1], d2 = a.sxy[c] - a.sxy[c - P], d3 = a.sxz[c] - a.sxz[c - plane];
+        const float d1 = csxx - __ldg(SXX + c - 1), d2 = csxy - psxy, d3 = csxz - __ldg(SXZ + c - plane);
         float v1 = d1 * ikx, v2 = d2 * iky, v3 = d3 * ikz;
         if (xs) { const float m = bx * a.m_sxx_x[mx] + adx * d1; a.m_sxx_x[mx] = m; v1 += m; }
         if (ys) { const float m = by * a.m_sxy_y[my] + ady * d2; a.m_sxy_y[my] = m; v2 += m; }
@@ -229,7 +261,7 @@ __global__ void __launch_bounds__(BX * BZ) seis25_velocity_kernel(Seis25Args a, 
         vx = vx * gx + (v1 + v2 + v3) * dtrx;
       }
       if (Vy && j <= NY - 2) {  // :847-869
-        const float d1 = a.sxy[c + 1] - a.sxy[c], d2 = a.syy[c + P] - a.syy[c], d3 = a.syz[c] - a.syz[c - plane];
+        const float d1 = __ldg(SXY + c + 1) - csxy, d2 = nsyy - csyy, d3 = csyz - __ldg(SYZ + c - plane);
         float v1 = d1 * ikxh, v2 = d2 * ikyh, v3 = d3 * ikz;
         if (xs) { const float m = bxh * a.m_sxy_x[mx] + adxh * d1; a.m_sxy_x[mx] = m; v1 += m; }
         if (ys) { const float m = byh * a.m_syy_y[my] + adyh * d2; a.m_syy_y[my] = m; v2 += m; }
@@ -237,7 +269,7 @@ __global__ void __launch_bounds__(BX * BZ) seis25_velocity_kernel(Seis25Args a, 
         vy = vy * gy + (v1 + v2 + v3) * dtry;
       }
       if (Vz && j >= 1) {  // :872-896
-        const float d1 = a.sxz[c + 1] - a.sxz[c], d2 = a.syz[c] - a.syz[c - P], d3 = a.szz[c + plane] - a.szz[c];
+        const float d1 = __ldg(SXZ + c + 1) - csxz, d2 = csyz - psyz, d3 = __ldg(SZZ + c + plane) - cszz;
         float v1 = d1 * ikxh, v2 = d2 * iky, v3 = d3 * ikzh;
         if (xs) { const float m = bxh * a.m_sxz_x[mx] + adxh * d1; a.m_sxz_x[mx] = m; v1 += m; }
         if (ys) { const float m = by * a.m_syz_y[my] + ady * d2; a.m_syz_y[my] = m; v2 += m; }
@@ -253,7 +285,10 @@ __global__ void __launch_bounds__(BX * BZ) seis25_velocity_kernel(Seis25Args a, 
       a.vx[c] = vx;
       a.vy[c] = vy;
       a.vz[c] = vz;
-      norm = fmaxf(norm, nan_to_inf(norm3df(vx, vy, vz)));
+      norm = fmaxf(norm, norm_monitor(vx, vy, vz));
+      psxy = csxy;
+      psyz = csyz;
+      csyy = nsyy;
     }
   }
   block_norm_to_slot(norm, a.io.slots, (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);

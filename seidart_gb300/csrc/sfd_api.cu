@@ -113,7 +113,7 @@ const char* mem_axes(int kind) {
 }
 int ncoef(int kind) {
   switch (kind) {
-    case SFD_SEISMIC2: return 10;   // c11 c13 c15 c33 c35 c55 (x dt), dt/rho, dt/rho_avg, 1-gx, 1-gz
+    case SFD_SEISMIC2: return 12;   // A11 A13 A15 A33 A35 B15 B35 B55 (averaged, x dt), dt/rho, dt/rho_avg, 1-gx, 1-gz
     case SFD_SEISMIC25: return 27;  // 21 C x dt, 3 dt/rho_avg, 3 (1 - gamma)
     case SFD_ELECTROMAG2: return 4;
     case SFD_ELECTROMAG25: return 6;
@@ -282,7 +282,7 @@ void bind_args(sfd_handle* h) {
       a.NX = NX; a.NZ = NZ; a.P = L.P; a.W = L.W;
       a.Ex = h->fc(0, 0); a.Ez = h->fc(1, 0); a.Hy = h->fc(2, 0);
       a.mExz = h->mc(0, 0); a.mEzx = h->mc(1, 0); a.mHyz = h->mc(2, 0); a.mHyx = h->mc(3, 0);
-      a.caEx = h->coef(0); a.cbEx = h->coef(1); a.caEz = h->coef(2); a.cbEz = h->coef(3);
+      a.CAx = h->coef(0); a.CBx = h->coef(1); a.CAz = h->coef(2); a.CBz = h->coef(3);
       a.X = make_axis(h->axis(0), NX); a.Z = make_axis(h->axis(1), NZ);
       a.dbH = (float)(c.dt / kMu0);
       a.io = io;
@@ -296,7 +296,7 @@ void bind_args(sfd_handle* h) {
         b.mExz1 = h->mc(0, 1 - p); b.mEzx1 = h->mc(1, 1 - p);
         b.mHyz = h->mc(2, 0); b.mHyx = h->mc(3, 0);
         b.mHyz0 = b.mHyz; b.mHyx0 = b.mHyx;
-        b.caEx = a.caEx; b.cbEx = a.cbEx; b.caEz = a.caEz; b.cbEz = a.cbEz;
+        b.CAx = a.CAx; b.CBx = a.CBx; b.CAz = a.CAz; b.CBz = a.CBz;
         b.X = a.X; b.Z = a.Z; b.dbH = a.dbH; b.io = io;
       }
       if (h->single) h->launch1 = em2_step_launch(h->em2s[0], h->zb);
@@ -308,8 +308,9 @@ void bind_args(sfd_handle* h) {
       a.vx = h->fc(0, 0); a.vz = h->fc(1, 0); a.sxx = h->fc(2, 0); a.szz = h->fc(3, 0); a.sxz = h->fc(4, 0);
       a.m_vxx = h->mc(0, 0); a.m_vzz = h->mc(1, 0); a.m_vxz = h->mc(2, 0); a.m_vzx = h->mc(3, 0);
       a.m_sxx_x = h->mc(4, 0); a.m_szz_z = h->mc(5, 0); a.m_sxz_x = h->mc(6, 0); a.m_sxz_z = h->mc(7, 0);
-      a.c11 = h->coef(0); a.c13 = h->coef(1); a.c15 = h->coef(2); a.c33 = h->coef(3); a.c35 = h->coef(4);
-      a.c55 = h->coef(5); a.dtrx = h->coef(6); a.dtrz = h->coef(7); a.gxp = h->coef(8); a.gzp = h->coef(9);
+      a.A11 = h->coef(0); a.A13 = h->coef(1); a.A15 = h->coef(2); a.A33 = h->coef(3); a.A35 = h->coef(4);
+      a.B15 = h->coef(5); a.B35 = h->coef(6); a.B55 = h->coef(7);
+      a.dtrx = h->coef(8); a.dtrz = h->coef(9); a.gxp = h->coef(10); a.gzp = h->coef(11);
       a.q3 = (const float*)(h->base + L.off_q3);
       a.X = make_axis(h->axis(0), NX); a.Z = make_axis(h->axis(1), NZ);
       a.io = io;
@@ -324,7 +325,8 @@ void bind_args(sfd_handle* h) {
         b.m_vxx1 = h->mc(0, 1 - p); b.m_vzz1 = h->mc(1, 1 - p); b.m_vxz1 = h->mc(2, 1 - p);
         b.m_vzx1 = h->mc(3, 1 - p);
         b.m_sxx_x = h->mc(4, 0); b.m_szz_z = h->mc(5, 0); b.m_sxz_x = h->mc(6, 0); b.m_sxz_z = h->mc(7, 0);
-        b.c11 = a.c11; b.c13 = a.c13; b.c15 = a.c15; b.c33 = a.c33; b.c35 = a.c35; b.c55 = a.c55;
+        b.A11 = a.A11; b.A13 = a.A13; b.A15 = a.A15; b.A33 = a.A33; b.A35 = a.A35;
+        b.B15 = a.B15; b.B35 = a.B35; b.B55 = a.B55;
         b.dtrx = a.dtrx; b.dtrz = a.dtrz; b.gxp = a.gxp; b.gzp = a.gzp; b.q3 = a.q3;
         b.X = a.X; b.Z = a.Z; b.io = io;
       }
@@ -535,15 +537,30 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
       h->model.assign(planes, planes + (size_t)count);
       // electromagfdtd.f95:164-181
       const double *e11 = P(0), *e13 = P(1), *e33 = P(2), *s11 = P(3), *s13 = P(4), *s33 = P(5);
+      std::vector<double> ca[2], cb[2];
+      for (int d = 0; d < 2; ++d) { ca[d].resize(N2); cb[d].resize(N2); }
       for (size_t q = 0; q < N2; ++q) {
-        const double ex = (e11[q] + e13[q]) * kEps0, ez = (e13[q] + e33[q]) * kEps0;
-        const double sx = s11[q] + s13[q], sz = s13[q] + s33[q];
-        if (!(ex > 0) || !(ez > 0)) return fail(SFD_ERR_BAD_ARG, "permittivity must be positive (cell %zu)", q);
-        out[0][q] = (float)((1.0 - sx * dt / (2.0 * ex)) / (1.0 + sx * dt / (2.0 * ex)));
-        out[1][q] = (float)((dt / ex) / (1.0 + sx * dt / (2.0 * ex)));
-        out[2][q] = (float)((1.0 - sz * dt / (2.0 * ez)) / (1.0 + sz * dt / (2.0 * ez)));
-        out[3][q] = (float)((dt / ez) / (1.0 + sz * dt / (2.0 * ez)));
+        const double ep[2] = {(e11[q] + e13[q]) * kEps0, (e13[q] + e33[q]) * kEps0};
+        const double sg[2] = {s11[q] + s13[q], s13[q] + s33[q]};
+        for (int d = 0; d < 2; ++d) {
+          if (!(ep[d] > 0)) return fail(SFD_ERR_BAD_ARG, "permittivity must be positive (cell %zu)", q);
+          ca[d][q] = (1.0 - sg[d] * dt / (2.0 * ep[d])) / (1.0 + sg[d] * dt / (2.0 * ep[d]));
+          cb[d][q] = (dt / ep[d]) / (1.0 + sg[d] * dt / (2.0 * ep[d]));
+        }
       }
+      // staggered averages at the Ex points (k >= 1) and the Ez points (i >= 1), :282, :294
+      for (int k = 0; k < NZ; ++k)
+        for (int i = 0; i < NX; ++i) {
+          const size_t n = (size_t)i + (size_t)NX * k;
+          if (k >= 1) {
+            out[0][n] = (float)((ca[0][n] + ca[0][n - NX]) / 2);
+            out[1][n] = (float)((cb[0][n] + cb[0][n - NX]) / 2);
+          }
+          if (i >= 1) {
+            out[2][n] = (float)((ca[1][n] + ca[1][n - 1]) / 2);
+            out[3][n] = (float)((cb[1][n] + cb[1][n - 1]) / 2);
+          }
+        }
       h->src_scale[0].assign(e11, e11 + N2);
       h->src_scale[1].assign(e33, e33 + N2);
       break;
@@ -569,18 +586,33 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
     }
     case SFD_SEISMIC2: {
       const double *rho = P(6), *gx = P(7), *gz = P(8);
-      for (int q = 0; q < 6; ++q)
-        for (size_t n = 0; n < N2; ++n) out[q][n] = (float)(P(q)[n] * dt);
+      // loop-1 points (i <= NX-2, k >= 1): (c(i+1,k) + 2 c(i,k) + c(i,k-1)) / 4 for c11 c13 c15 c33 c35
+      // loop-2 points (k <= NZ-2, i >= 1): (c(i,k+1) + 2 c(i,k) + c(i-1,k)) / 4 for c15 c35 c55
+      const int A_src[5] = {0, 1, 2, 3, 4}, B_src[3] = {2, 4, 5};
+      for (int k = 0; k < NZ; ++k)
+        for (int i = 0; i < NX; ++i) {
+          const size_t n = (size_t)i + (size_t)NX * k;
+          if (i <= NX - 2 && k >= 1)
+            for (int q = 0; q < 5; ++q) {
+              const double* cc = P(A_src[q]);
+              out[q][n] = (float)((cc[n + 1] + 2 * cc[n] + cc[n - NX]) / 4 * dt);
+            }
+          if (k <= NZ - 2 && i >= 1)
+            for (int q = 0; q < 3; ++q) {
+              const double* cc = P(B_src[q]);
+              out[5 + q][n] = (float)((cc[n + NX] + 2 * cc[n] + cc[n - 1]) / 4 * dt);
+            }
+        }
       for (size_t n = 0; n < N2; ++n)
         if (!(rho[n] > 0)) return fail(SFD_ERR_BAD_ARG, "density must be positive (cell %zu)", n);
       for (int k = 0; k < NZ; ++k)
         for (int i = 0; i < NX; ++i) {
           const size_t n = (size_t)i + (size_t)NX * k;
-          out[6][n] = (float)(dt / rho[n]);  // seismicfdtd.f95:334
+          out[8][n] = (float)(dt / rho[n]);  // seismicfdtd.f95:334
           if (i <= NX - 2 && k <= NZ - 2)    // seismicfdtd.f95:341, 355
-            out[7][n] = (float)(dt / ((2 * rho[n] + at(rho, i + 1, k) + at(rho, i, k + 1)) / 4));
-          out[8][n] = (float)(1.0 - gx[n]);
-          out[9][n] = (float)(1.0 - gz[n]);
+            out[9][n] = (float)(dt / ((2 * rho[n] + at(rho, i + 1, k) + at(rho, i, k + 1)) / 4));
+          out[10][n] = (float)(1.0 - gx[n]);
+          out[11][n] = (float)(1.0 - gz[n]);
           if (gx[n] != 0.0 || gz[n] != 0.0) atten = 1;
         }
       h->src_scale[0].assign(rho, rho + N2);
@@ -1183,7 +1215,7 @@ int32_t sfd_adjoint_segment(sfd_handle* h, int64_t nsteps) {
   Em2Adj a;
   const Em2Args& e = h->em2;
   a.NX = NX; a.NZ = NZ; a.P = L.P; a.W = L.W;
-  a.caEx = e.caEx; a.cbEx = e.cbEx; a.caEz = e.caEz; a.cbEz = e.cbEz;
+  a.CAx = e.CAx; a.CBx = e.CBx; a.CAz = e.CAz; a.CBz = e.CBz;
   a.X = e.X; a.Z = e.Z; a.dbH = e.dbH;
   a.TH = (float*)(h->adj + A.th); a.MEx = (float*)(h->adj + A.mex); a.MEz = (float*)(h->adj + A.mez);
   a.gCAx = (float*)(h->adj + A.g[0]); a.gCBx = (float*)(h->adj + A.g[1]);

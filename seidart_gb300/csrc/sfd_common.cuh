@@ -55,6 +55,20 @@ __device__ __forceinline__ int strip_idx(int i, int n, int W) { return i < W ? i
 
 __device__ __forceinline__ float nan_to_inf(float v) { return (v != v) ? __int_as_float(0x7f800000) : v; }
 
+// Stability monitor value of one cell: |a| + |b| (+ |c|), which bounds the
+// 2-norm the Fortran tests (seismicfdtd.f95:378) from above within a factor
+// sqrt(2) (sqrt(3)); above 1e24 the exact 2-norm is returned, so the 1e25
+// threshold is tested exactly.  NaN propagates through the sum and comes back
+// as +inf.
+__device__ __forceinline__ float norm_monitor(float a, float b) {
+  const float m = fabsf(a) + fabsf(b);
+  return (m <= 1e24f) ? m : nan_to_inf(hypotf(a, b));
+}
+__device__ __forceinline__ float norm_monitor(float a, float b, float c) {
+  const float m = fabsf(a) + fabsf(b) + fabsf(c);
+  return (m <= 1e24f) ? m : nan_to_inf(norm3df(a, b, c));
+}
+
 // Block-wide max of v (every thread of the block must call it); thread 0 then
 // folds it into this block's slot.  No atomics: each block owns its slot.
 __device__ __forceinline__ void block_norm_to_slot(float v, float* slots, int slot) {

@@ -22,7 +22,9 @@ struct Em2Args {
   int NX, NZ, P, W;
   float *Ex, *Ez, *Hy;
   float *mExz, *mEzx, *mHyz, *mHyx;  // z-, x-, z-, x-strip
-  const float *caEx, *cbEx, *caEz, *cbEz;
+  // staggered-averaged update coefficients, (c(i,k) + c(i,k-1))/2 at Ex and
+  // (c(i,k) + c(i-1,k))/2 at Ez (electromagfdtd.f95:282, 294), formed in FP64
+  const float *CAx, *CBx, *CAz, *CBz;
   AxisTab X, Z;
   float dbH;
   IoArgs io;
@@ -34,7 +36,10 @@ struct Seis2Args {
   float *vx, *vz, *sxx, *szz, *sxz;
   float *m_vxx, *m_vzz, *m_vxz, *m_vzx;      // x, z, z, x strips
   float *m_sxx_x, *m_szz_z, *m_sxz_x, *m_sxz_z;  // x, z, x, z strips
-  const float *c11, *c13, *c15, *c33, *c35, *c55;  // stiffness * dt
+  // dt * averaged stiffness, formed in FP64: (c(i+1,j) + 2c(i,j) + c(i,j-1))/4
+  // at the normal-stress points (seismicfdtd.f95:270-280) and
+  // (c(i,j+1) + 2c(i,j) + c(i-1,j))/4 at the shear-stress points (:306-311)
+  const float *A11, *A13, *A15, *A33, *A35, *B15, *B35, *B55;
   const float *dtrx, *dtrz;                      // dt / rho, dt / rho_avg
   const float *gxp, *gzp;                        // 1 - gamma
   const float* q3;                               // b_x_half indexed by the z index
@@ -86,7 +91,7 @@ struct Em2Step {
   float *Ex1, *Ez1, *Hy1, *mExz1, *mEzx1;        // new
   const float *mHyz0, *mHyx0;                    // second-half memory, read ...
   float *mHyz, *mHyx;                            // ... and written (the same arrays except in adjoint recompute)
-  const float *caEx, *cbEx, *caEz, *cbEz;
+  const float *CAx, *CBx, *CAz, *CBz;  // staggered averages, as in Em2Args
   AxisTab X, Z;
   float dbH;
   IoArgs io;
@@ -100,7 +105,7 @@ struct Seis2Step {
   const float *m_vxx0, *m_vzz0, *m_vxz0, *m_vzx0;  // velocity-gradient memory, old
   float *m_vxx1, *m_vzz1, *m_vxz1, *m_vzx1;        // new
   float *m_sxx_x, *m_szz_z, *m_sxz_x, *m_sxz_z;    // in place
-  const float *c11, *c13, *c15, *c33, *c35, *c55, *dtrx, *dtrz, *gxp, *gzp, *q3;
+  const float *A11, *A13, *A15, *A33, *A35, *B15, *B35, *B55, *dtrx, *dtrz, *gxp, *gzp, *q3;
   AxisTab X, Z;
   IoArgs io;
 };
