@@ -1,0 +1,284 @@
+"""``seidartfdtd`` drop-in: the process the SeidarT driver launches.
+
+    python -m seidart_gb300.cli <project.json> seismic=<true|false> density_method=<m> [options]
+
+Same argv and the same working-directory files as the backend that
+``Model.run`` calls (``src/seidart/routines/classes.py:878-924``):
+
+* project JSON: ``Domain`` (dim, nx, ny, nz, dx, dy, dz, cpml, alpha_max_scalar,
+  kappa_max, NP, NPA, Rcoef) and ``Seismic``/``Electromagnetic`` ``Source``
+  (dt, time_steps, xind, yind, zind, source_frequency), as saved by
+  ``Model.save_to_json`` (``classes.py:787-836``);
+* material planes ``c11.dat ... c66.dat rho.dat`` (+ ``gamma_x/y/z.dat``) or
+  ``e11.dat ... e33.dat s11.dat ... s33.dat`` (``classes.py:608-750``);
+* source time functions ``seismicsource{x,y,z}.dat`` /
+  ``electromagneticsource{x,y,z}.dat`` (``sourcefunction.py:354-372``);
+* initial conditions ``initialcondition{V|E}{x,y,z}.dat`` (``classes.py:882-898``).
+
+All are Fortran records, x fastest, full grid (CPML included).  The CPML
+profiles are computed from the project's CPML parameters in FP64
+(``seidart_gb300.cpml``).  Outputs: one FP32 snapshot record per channel and
+per step, named ``{Vx,Vy,Vz|Ex,Ey,Ez}.{step:06d}.{xind}.{[yind.]}{zind}.dat``
+with 1-based steps, which is what ``Array.getrcx`` globs
+(``src/seidart/routines/arraybuild.py:199-240``).  ``--snapshot-every N``
+thins the snapshots and ``--receivers FILE --traces OUT.npy`` records
+receiver traces on the device instead.  The exit status is 0 on success, 2
+when the run became unstable, and 1 on any input error.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import sys
+import threading
+import queue
+from pathlib import Path
+
+import numpy as np
+
+from . import cpml as cp
+from . import fortran_io as fio
+from ._lib import ELECTROMAG2, ELECTROMAG25, SEISMIC2, SEISMIC25, SfdError, UnstableError
+from .solver import CHANNELS, FIELDS, MODEL_PLANES, GridSpec, is_25d
+
+# .dat file name of each model plane (the driver's column names, classes.py:608-679)
+_FILE_OF = {
+    "eps11": "e11", "eps12": "e12", "eps13": "e13", "eps22": "e22", "eps23": "e23", "eps33": "e33",
+    "sig11": "s11", "sig12": "s12", "sig13": "s13", "sig22": "s22", "sig23": "s23", "sig33": "s33",
+}
+_OPTIONAL = {"gamma_x", "gamma_y", "gamma_z"}
+
+
+class ProjectError(ValueError):
+    pass
+
+
+def parse_flag(args, name, default=None):
+    for a in args:
+        if a.startswith(name + "="):
+            return a.split("=", 1)[1]
+    return default
+
+
+def load_project(json_path, seismic: bool, workdir="."):
+    """Everything one run needs, read from the project JSON and the .dat files."""
+    with open(json_path) as f:
+        prj = json.load(f)
+    dom = prj["Domain"]
+    sec = prj["Seismic" if seismic else "Electromagnetic"]
+    src = sec["Source"]
+    dim = float(dom["dim"])
+    if dim not in (2.0, 2.5):
+        raise ProjectError(f"Domain.dim = {dim}: this backend runs 2 and 2.5-D models")
+    c = int(dom["cpml"])
+    nx, nz = int(dom["nx"]) + 2 * c, int(dom["nz"]) + 2 * c
+    ny = int(dom.get("ny", 1)) + 2 * c if dim == 2.5 else 1
+    dx, dz = float(dom["dx"]), float(dom["dz"])
+    dy = float(dom.get("dy", 1.0))
+    kind = (SEISMIC25 if dim == 2.5 else SEISMIC2) if seismic else (ELECTROMAG25 if dim == 2.5 else ELECTROMAG2)
+    dt = float(src["dt"])
+    nstep = int(src["time_steps"])
+    if nstep < 1 or not (dt > 0):
+        raise ProjectError("Source.time_steps and Source.dt must be positive")
+    grid = GridSpec(kind, nx, nz, dx, dz, dt, c, ny=ny, dy=dy)
+    wd = Path(workdir)
+    shape2 = (nz, nx)
+    planes = []
+    for name in MODEL_PLANES[kind]:
+        fn = wd / (_FILE_OF.get(name, name) + ".dat")
+        if not fn.exists():
+            if name in _OPTIONAL:
+                planes.append(np.zeros(shape2))
+                continue
+            raise ProjectError(f"missing model file {fn}")
+        planes.append(fio.read_plane(fn, shape2))
+    planes = np.stack(planes)
+    comps = ["x", "y", "z"] if is_25d(kind) else ["x", "z"]
+    stem = "seismicsource" if seismic else "electromagneticsource"
+    srcfn = []
+    for q in comps:
+        fn = wd / f"{stem}{q}.dat"
+        if fn.exists():
+            s = fio.read_record(fn, np.float64)
+            if s.size < nstep:
+                raise ProjectError(f"{fn}: {s.size} samples, need {nstep}")
+            srcfn.append(s[:nstep])
+        else:
+            srcfn.append(np.zeros(nstep))
+    srcfn = np.stack(srcfn)
+    xind, yind, zind = int(src.get("xind", 0)), int(src.get("yind", 0)), int(src.get("zind", 0))
+    src_ijk = (xind + c, (yind + c) if is_25d(kind) else 0, zind + c)
+    init = {}
+    letter = "V" if seismic else "E"
+    fshape = grid.shape
+    for q, ch in zip(comps, CHANNELS[kind]):
+        fn = wd / f"initialcondition{letter}{q}.dat"
+        if fn.exists():
+            a = fio.read_record(fn, np.float64)
+            if a.size == int(np.prod(fshape)) and np.any(a):
+                init[ch] = a.reshape(fshape)
+    f0 = float(src.get("source_frequency", 1.0))
+    params = {k: float(dom[k]) for k in ("alpha_max_scalar", "kappa_max", "NP", "NPA", "Rcoef") if k in dom}
+    vmax = max_speed(kind, planes)
+    deltas = (dx, dy, dz) if is_25d(kind) else (dx, dz)
+    shape = (nx, ny, nz) if is_25d(kind) else (nx, nz)
+    profiles = cp.build_profiles(shape, deltas, c, dt, f0, vmax, seismic=seismic, params=params)
+    return dict(kind=kind, grid=grid, planes=planes, profiles=profiles, srcfn=srcfn, src_ijk=src_ijk,
+                init=init, nstep=nstep, xind=xind, yind=yind, zind=zind, seismic=seismic, vmax=vmax)
+
+
+def max_speed(kind, planes):
+    """Largest wave speed of the model (the driver's global CPML velocity)."""
+    if kind in (ELECTROMAG2, ELECTROMAG25):
+        eps = planes[[0, 2]] if kind == ELECTROMAG2 else planes[[0, 3, 5]]
+        return cp.CLIGHT / math.sqrt(max(float(eps.min()), 1e-30))
+    names = MODEL_PLANES[kind]
+    idx = {n: q for q, n in enumerate(names)}
+    rho = planes[idx["rho"]].ravel()
+    voigt = {"c11": (0, 0), "c12": (0, 1), "c13": (0, 2), "c14": (0, 3), "c15": (0, 4), "c16": (0, 5),
+             "c22": (1, 1), "c23": (1, 2), "c24": (1, 3), "c25": (1, 4), "c26": (1, 5), "c33": (2, 2),
+             "c34": (2, 3), "c35": (2, 4), "c36": (2, 5), "c44": (3, 3), "c45": (3, 4), "c46": (3, 5),
+             "c55": (4, 4), "c56": (4, 5), "c66": (5, 5)}
+    cols = [n for n in names if n in voigt]
+    stack = np.stack([planes[idx[n]].ravel() for n in cols] + [rho], axis=1)
+    uniq = np.unique(stack, axis=0)
+    if len(uniq) > 4096:  # per-cell random media: a strided sample bounds the cost
+        uniq = uniq[:: max(1, len(uniq) // 4096)]
+    dim = 2.5 if kind == SEISMIC25 else 2
+    best = 0.0
+    for row in uniq:
+        C6 = np.zeros((6, 6))
+        for v, n in zip(row[:-1], cols):
+            a, b = voigt[n]
+            C6[a, b] = C6[b, a] = v
+        if kind == SEISMIC2:  # the 2-D model carries the x-z plane only; fill y as a copy of x
+            C6[1, 1], C6[0, 1], C6[1, 0] = C6[0, 0], C6[0, 2], C6[0, 2]
+            C6[1, 2], C6[2, 1], C6[3, 3], C6[5, 5] = C6[0, 2], C6[0, 2], C6[4, 4], C6[4, 4]
+        if row[-1] > 0:
+            best = max(best, cp.max_velocity(C6, row[-1], dim))
+    return best
+
+
+def read_receivers(path, grid):
+    """Receiver CSV with a header row and X, Y, Z columns in metres (the
+    driver's receiver file, arraybuild.py:142-196) -> full-grid (i, j, k)."""
+    rows = []
+    with open(path) as f:
+        lines = [ln.strip() for ln in f if ln.strip()]
+    for ln in lines[1:]:
+        vals = [float(v) for v in ln.replace(";", ",").split(",")]
+        if len(vals) == 2:
+            vals = [vals[0], 0.0, vals[1]]
+        rows.append(vals[:3])
+    xyz = np.asarray(rows, dtype=np.float64).reshape(-1, 3)
+    c = grid.npml
+    i = (xyz[:, 0] / grid.dx).astype(int) + c
+    k = (xyz[:, 2] / grid.dz).astype(int) + c
+    j = (xyz[:, 1] / grid.dy).astype(int) + c if is_25d(grid.kind) else np.zeros(len(xyz), int)
+    return np.stack([i, j, k], axis=1).astype(np.int32)
+
+
+class SnapshotWriter:
+    """Writes snapshot records on a background thread while the GPU runs on."""
+
+    def __init__(self, workdir):
+        self.q = queue.Queue(maxsize=8)
+        self.wd = Path(workdir)
+        self.err = None
+        self.t = threading.Thread(target=self._loop, daemon=True)
+        self.t.start()
+
+    def _loop(self):
+        while True:
+            item = self.q.get()
+            if item is None:
+                return
+            name, arr = item
+            try:
+                fio.write_record(self.wd / name, arr, np.float32)
+            except OSError as e:
+                self.err = e
+
+    def put(self, name, arr):
+        self.q.put((name, arr))
+
+    def close(self):
+        self.q.put(None)
+        self.t.join()
+        if self.err:
+            raise self.err
+
+
+def snapshot_name(ch, step, p):
+    ch = ch[0].upper() + ch[1:]  # Vx Vy Vz / Ex Ey Ez, write_image2/3 (readwrite_routines.f95:486)
+    if is_25d(p["kind"]):
+        return f"{ch}.{step:06d}.{p['xind']}.{p['yind']}.{p['zind']}.dat"
+    return f"{ch}.{step:06d}.{p['xind']}.{p['zind']}.dat"
+
+
+def run(argv=None) -> int:
+    ap = argparse.ArgumentParser(prog="seidartfdtd", description=__doc__,
+                                 formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("project")
+    ap.add_argument("flags", nargs="*", help="seismic=<true|false> density_method=<none|arithmetic|...>")
+    ap.add_argument("--workdir", default=".")
+    ap.add_argument("--snapshot-every", type=int, default=1, help="write snapshots every N steps (0 = none)")
+    ap.add_argument("--receivers", help="receiver CSV (X,Y,Z in metres)")
+    ap.add_argument("--traces", help="write receiver traces (nstep, channel, receiver) to this .npy")
+    ap.add_argument("--device", default="cuda")
+    a = ap.parse_args(argv)
+    seismic = str(parse_flag(a.flags, "seismic", "true")).lower() in ("true", "1", "yes")
+    density = str(parse_flag(a.flags, "density_method", "arithmetic")).lower()
+    try:
+        p = load_project(a.project, seismic, a.workdir)
+    except (ProjectError, ValueError, KeyError, OSError) as e:
+        print(f"seidartfdtd: {e}", file=sys.stderr)
+        return 1
+    if density not in ("none", "arithmetic"):
+        print(f"seidartfdtd: density_method={density}: the solver uses the staggered arithmetic density "
+              "averages of the reference loops (seismicfdtd.f95:341, 826-877)", file=sys.stderr)
+    from .solver import FDTDSolver
+    grid = p["grid"]
+    rec = read_receivers(a.receivers, grid) if a.receivers else np.zeros((0, 3), np.int32)
+    every = max(0, int(a.snapshot_every))
+    try:
+        with FDTDSolver(grid, p["nstep"], len(rec), device=a.device) as s:
+            s.set_model(p["planes"])
+            s.set_cpml(p["profiles"])
+            s.set_source(p["src_ijk"], p["srcfn"])
+            if len(rec):
+                s.set_receivers(rec)
+            for ch, v in p["init"].items():
+                s.set_field(ch, v.astype(np.float32))
+            chans = CHANNELS[p["kind"]]
+            writer = SnapshotWriter(a.workdir) if every else None
+            done = 0
+            while done < p["nstep"]:
+                n = min(every, p["nstep"] - done) if every else p["nstep"]
+                s.run(n)
+                done += n
+                if writer:
+                    for ch in chans:
+                        writer.put(snapshot_name(ch, done, p), s.field(ch))
+            if writer:
+                writer.close()
+            s.status()
+            if a.traces and len(rec):
+                np.save(a.traces, s.traces())
+    except UnstableError as e:
+        print(f"seidartfdtd: {e}", file=sys.stderr)
+        return 2
+    except SfdError as e:
+        print(f"seidartfdtd: {e}", file=sys.stderr)
+        return 1
+    return 0
+
+
+def main():
+    sys.exit(run())
+
+
+if __name__ == "__main__":
+    main()
