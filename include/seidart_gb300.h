@@ -140,6 +140,16 @@ int32_t sfd_set_cpml(sfd_handle* h, const double* profiles, int64_t count);
 int32_t sfd_set_source(sfd_handle* h, int32_t i, int32_t j, int32_t k, const double* srcfn,
                        int32_t ncomp, int32_t nstep);
 
+/* Make dst read src's update coefficients instead of its own (no copy): the
+ * shots of one survey share one model.  Same kind, grid, dt and flags
+ * (electromag2 or seismic2).  src must outlive dst; a later sfd_set_model on
+ * src changes both, one on dst detaches nothing (call it on src).  In a batch,
+ * consecutive handles sharing a model run their tiles back to back so the
+ * shared coefficients are read from HBM once per step.  Replaces the copy of
+ * the model files each shot of the driver's survey loop reads
+ * (src/seidart/simulations/common_offset.py:143-176). */
+int32_t sfd_share_model(sfd_handle* dst, const sfd_handle* src);
+
 /* Receiver cells, host int32 (i, j, k) triples, nrec = cfg.nrec. */
 int32_t sfd_set_receivers(sfd_handle* h, const int32_t* ijk, int32_t nrec);
 

@@ -22,7 +22,7 @@ SFD_OK, SFD_ERR_BAD_ARG, SFD_ERR_STATE, SFD_ERR_CUDA, SFD_ERR_UNSTABLE, SFD_ERR_
 EXPORTS = (
     "sfd_version", "sfd_last_error", "sfd_model_planes", "sfd_num_fields", "sfd_num_channels",
     "sfd_num_memory", "sfd_state_bytes", "sfd_create", "sfd_set_model", "sfd_set_cpml",
-    "sfd_set_source", "sfd_set_receivers", "sfd_reset", "sfd_set_field", "sfd_get_field",
+    "sfd_set_source", "sfd_share_model", "sfd_set_receivers", "sfd_reset", "sfd_set_field", "sfd_get_field",
     "sfd_get_memory", "sfd_run", "sfd_status", "sfd_get_traces", "sfd_traces_device", "sfd_launch_half",
     "sfd_destroy", "sfd_checkpoint_bytes", "sfd_checkpoint_save", "sfd_checkpoint_load", "sfd_adjoint_bytes",
     "sfd_adjoint_begin", "sfd_adjoint_segment", "sfd_adjoint_gradient", "sfd_batch_scratch_bytes", "sfd_batch_create", "sfd_batch_set_tiling", "sfd_batch_run",
@@ -73,6 +73,7 @@ def _declare(lib):
         "sfd_set_cpml": (i32, [P, dp, i64]),
         "sfd_set_source": (i32, [P, i32, i32, i32, dp, i32, i32]),
         "sfd_set_receivers": (i32, [P, ip, i32]),
+        "sfd_share_model": (i32, [P, P]),
         "sfd_reset": (i32, [P]),
         "sfd_set_field": (i32, [P, i32, fp, i64]),
         "sfd_get_field": (i32, [P, i32, fp, i64]),

@@ -22,7 +22,7 @@ from pathlib import Path
 from . import _lib
 from ._lib import check
 
-CANDIDATES = [(1, 4), (2, 4), (2, 3), (4, 2), (4, 3), (1, 3), (2, 2)]
+CANDIDATES = [(1, 3), (2, 3), (4, 3), (1, 2), (2, 2), (4, 2), (2, 1)]
 
 
 def _declare(L):
@@ -63,7 +63,7 @@ class Batch:
         b = C.c_void_p()
         check(L.sfd_batch_create(arr, n, C.c_void_p(self.scratch.data_ptr()), nbytes, C.byref(b)))
         self._b = b
-        self.tiling = (2, 4)
+        self.tiling = (2, 3)
 
     @property
     def cells(self) -> int:

@@ -26,6 +26,9 @@ struct Em2Adj {
   const float* resid;               // dJ/d(trace) [nstep][2][nrec]
 };
 
-void adj_step(const Em2Adj& a, const AdjState& S, const AdjState& L, const AdjState& Ln, int t, cudaStream_t s);
+// S: forward state before step t, S1: after it (its Hy is Hy' except on the
+// Dirichlet edges; its C and D are this step's memory variables).
+void adj_step(const Em2Adj& a, const AdjState& S, const AdjState& S1, const AdjState& L, const AdjState& Ln, int t,
+              cudaStream_t s);
 
 }  // namespace sfd

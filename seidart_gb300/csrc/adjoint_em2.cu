@@ -34,17 +34,19 @@ __device__ __forceinline__ bool ez_range(int i, int k, int NX, int NZ) { return 
 __device__ __forceinline__ bool h_range(int i, int k, int NX, int NZ) { return i <= NX - 2 && k <= NZ - 2; }
 
 // Hy' (after the H half of the step from state S) at (i, k) in the H range.
-__device__ __forceinline__ float hprime(const Em2Adj& a, const AdjState& S, int i, int k) {
+// Away from the Hy Dirichlet edges it equals the stored Hy of the next state
+// S1; on the edges (zeroed after the E half read them) it is recomputed.
+__device__ __forceinline__ float hprime(const Em2Adj& a, const AdjState& S, const AdjState& S1, int i, int k) {
   const int P = a.P, W = a.W, NX = a.NX, NZ = a.NZ;
   const size_t c = (size_t)k * P + i;
+  if (!hy_edge(i, k, NX, NZ)) return S1.Hy[c];
   const float dEx = S.Ex[c + P] - S.Ex[c];
   float vz = dEx * a.Z.ik[k];
   if (in_strip(k, NZ, W)) vz += a.Z.b[k] * S.A[(size_t)strip_idx(k, NZ, W) * P + i] + a.Z.ad[k] * dEx;
   const float dEz = S.Ez[c + 1] - S.Ez[c];
   float vx = dEz * a.X.ik[i];
   if (in_strip(i, NX, W)) vx += a.X.b[i] * S.B[(size_t)k * (2 * W) + strip_idx(i, NX, W)] + a.X.ad[i] * dEz;
-  const bool edge = hy_edge(i, k, NX, NZ);
-  return (edge ? 0.0f : S.Hy[c]) + a.dbH * (vx + vz);
+  return a.dbH * (vx + vz);  // the previous Hy on an edge is zero
 }
 
 __device__ __forceinline__ float lam_masked_ex(const Em2Adj& a, const AdjState& L, int i, int k) {
@@ -83,7 +85,8 @@ __global__ void __launch_bounds__(BX * BY) adj_inject_kernel(Em2Adj a, AdjState 
   atomicAdd(&L.Ez[c], a.resid[((size_t)t * 2 + 1) * a.nrec + r]);
 }
 
-__global__ void __launch_bounds__(BX * BY) adj_e_kernel(Em2Adj a, AdjState S, AdjState L, AdjState Ln, int t) {
+__global__ void __launch_bounds__(BX * BY) adj_e_kernel(Em2Adj a, AdjState S, AdjState S1, AdjState L, AdjState Ln,
+                                                        int t) {
   const int i = blockIdx.x * BX + threadIdx.x;
   const int k = blockIdx.y * BY + threadIdx.y;
   const int NX = a.NX, NZ = a.NZ, P = a.P, W = a.W;
@@ -107,11 +110,11 @@ __global__ void __launch_bounds__(BX * BY) adj_e_kernel(Em2Adj a, AdjState S, Ad
   if (ex_range(i, k, NX, NZ)) {
     const float ca = a.CAx[c], cb = a.CBx[c];
     mex = ca * lex;
-    const float dHz = hprime(a, S, i, k) - hprime(a, S, i, k - 1);
+    const float dHz = hprime(a, S, S1, i, k) - hprime(a, S, S1, i, k - 1);
     float d = dHz * a.Z.ikh[k];
     if (zs) {
       const float lc = L.C[mz];
-      d += a.Z.bh[k] * S.C[mz] + a.Z.adh[k] * dHz;  // C'
+      d += S1.C[mz];  // C' of this step, stored in the next state
       Ln.C[mz] = a.Z.bh[k] * (cb * lex + lc);
     }
     a.gCAx[c] += lex * S.Ex[c];
@@ -122,11 +125,11 @@ __global__ void __launch_bounds__(BX * BY) adj_e_kernel(Em2Adj a, AdjState S, Ad
   if (ez_range(i, k, NX, NZ)) {
     const float ca = a.CAz[c], cb = a.CBz[c];
     mez = ca * lez;
-    const float dHx = hprime(a, S, i, k) - hprime(a, S, i - 1, k);
+    const float dHx = hprime(a, S, S1, i, k) - hprime(a, S, S1, i - 1, k);
     float d = dHx * a.X.ikh[i];
     if (xs) {
       const float ld = L.D[mx];
-      d += a.X.bh[i] * S.D[mx] + a.X.adh[i] * dHx;  // D'
+      d += S1.D[mx];  // D' of this step
       Ln.D[mx] = a.X.bh[i] * (cb * lez + ld);
     }
     a.gCAz[c] += lez * S.Ez[c];
@@ -182,10 +185,11 @@ __global__ void __launch_bounds__(BX * BY) adj_h_kernel(Em2Adj a, AdjState L, Ad
 
 }  // namespace
 
-void adj_step(const Em2Adj& a, const AdjState& S, const AdjState& L, const AdjState& Ln, int t, cudaStream_t s) {
+void adj_step(const Em2Adj& a, const AdjState& S, const AdjState& S1, const AdjState& L, const AdjState& Ln, int t,
+              cudaStream_t s) {
   dim3 b(BX, BY), g((a.NX + BX - 1) / BX, (a.NZ + BY - 1) / BY);
   if (a.nrec > 0) adj_inject_kernel<<<(a.nrec + 255) / 256, 256, 0, s>>>(a, L, t);
-  adj_e_kernel<<<g, b, 0, s>>>(a, S, L, Ln, t);
+  adj_e_kernel<<<g, b, 0, s>>>(a, S, S1, L, Ln, t);
   adj_h_kernel<<<g, b, 0, s>>>(a, L, Ln);
 }
 

@@ -1,9 +1,9 @@
 // Batched time stepping: many 2-D models (electromag2 shots, seismic2 models
 // of uneven size) advance together in ONE persistent cooperative launch.
 //
-// Work list: every model is cut into the 32 x (8*ZB) tiles of its single-pass
-// step (fused2d.cuh); the tiles of all models are numbered consecutively
-// (model-major, then row-major within a model).  Each time step, block b
+// Work list: every model is cut into the tiles of its single-pass
+// step (fused2d.cuh); the tiles of all models are numbered consecutively,
+// group by group (BatchGroup: shots sharing a model interleave their tiles).  Each time step, block b
 // processes tiles b, b + G, b + 2G, ... with the tile bodies of the per-model
 // kernels, then all blocks meet at a grid barrier before the next step.  A
 // model's step reads the ping-pong copy p = (cur + s) & 1 and writes the
@@ -61,19 +61,21 @@ __device__ bool grid_barrier(GridBarrier* bar, unsigned nblocks, unsigned long l
 }
 
 template <int ZB>
-__global__ void __launch_bounds__(256, 4)
-    batch_kernel(const BatchModel* __restrict__ models, int nmodels, int total_tiles, int nsteps,
-                 GridBarrier* bar, unsigned long long limit_ns) {
-  __shared__ union {
-    float em2[8 * ZB + 1][33];
+__global__ void __launch_bounds__(256, 3)
+    batch_kernel(const BatchModel* __restrict__ models, const BatchGroup* __restrict__ groups, int ngroups,
+                 int total_tiles, int nsteps, GridBarrier* bar, unsigned long long limit_ns) {
+  __shared__ __align__(16) union {
+    float em2[8 * ZB + 1][kEm2Row];
     float s2[3][8 * ZB + 2][34];
   } sm;
   for (int s = 0; s < nsteps; ++s) {
-    int m = 0;
+    int g = 0;
     for (int tile = blockIdx.x; tile < total_tiles; tile += gridDim.x) {
-      while (m + 1 < nmodels && tile >= models[m + 1].tile0) ++m;  // tiles ascend per block
-      const BatchModel& md = models[m];
-      const int lt = tile - md.tile0;
+      while (g + 1 < ngroups && tile >= groups[g + 1].tile0) ++g;  // tiles ascend per block
+      const BatchGroup& gr = groups[g];
+      const int q = tile - gr.tile0;
+      const BatchModel& md = models[gr.first + q % gr.n];
+      const int lt = q / gr.n;
       const int bx = lt % md.gx, by = lt / md.gx;
       const int p = (md.cur + s) & 1;
       if (md.kind == SFD_BATCH_EM2) {
@@ -156,10 +158,10 @@ void batch_end(const BatchModel* models, int nmodels, int nsteps, cudaStream_t s
   batch_end_kernel<<<std::min(nmodels, 1024), 256, 0, s>>>(models, nmodels, nsteps);
 }
 
-cudaError_t batch_launch(int zb, int grid, const BatchModel* models, int nmodels, int total_tiles, int nsteps,
-                         GridBarrier* bar, unsigned long long limit_ns, cudaStream_t s) {
-  void* args[] = {(void*)&models, (void*)&nmodels, (void*)&total_tiles, (void*)&nsteps, (void*)&bar,
-                  (void*)&limit_ns};
+cudaError_t batch_launch(int zb, int grid, const BatchModel* models, const BatchGroup* groups, int ngroups,
+                         int total_tiles, int nsteps, GridBarrier* bar, unsigned long long limit_ns, cudaStream_t s) {
+  void* args[] = {(void*)&models, (void*)&groups, (void*)&ngroups, (void*)&total_tiles, (void*)&nsteps,
+                  (void*)&bar, (void*)&limit_ns};
   return cudaLaunchCooperativeKernel(batch_kernel_ptr(zb), dim3(grid), dim3(32, 8), args, 0, s);
 }
 

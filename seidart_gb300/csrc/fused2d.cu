@@ -23,7 +23,7 @@ constexpr int TX = 32, TY = 8;
 
 template <int ZB>
 __global__ void __launch_bounds__(TX * TY) em2_step_kernel(Em2Step a, int rel) {
-  __shared__ float sH[TY * ZB + 1][TX + 1];
+  __shared__ __align__(16) float sH[TY * ZB + 1][kEm2Row];
   em2_tile<ZB>(a, a.io.ctl->base + rel, blockIdx.x, blockIdx.y, gridDim.x, sH);
 }
 
@@ -48,7 +48,7 @@ __global__ void seis2_step_finalize_kernel(Seis2Step a, int t_last) {
 Launch em2_step_launch(const Em2Step& a, int zb) {
   Launch L;
   L.block = dim3(TX, TY, 1);
-  L.grid = dim3((a.NX + TX - 1) / TX, (a.NZ + TY * zb - 1) / (TY * zb), 1);
+  L.grid = dim3((a.NX + 4 * TX - 1) / (4 * TX), (a.NZ + TY * zb - 1) / (TY * zb), 1);  // 128-cell-wide tiles
   L.nslots = L.grid.x * L.grid.y;
   return L;
 }

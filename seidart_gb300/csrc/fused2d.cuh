@@ -37,52 +37,123 @@ __device__ __forceinline__ float em2_h_cell(const Em2Step& a, int i, int k, floa
   return __ldg(a.Hy0 + c) + a.dbH * (vx + vz);
 }
 
+__device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+__device__ __forceinline__ float& el(float4& v, int e) { return (&v.x)[e]; }
+__device__ __forceinline__ float el(const float4& v, int e) { return (&v.x)[e]; }
+
+// Shared-memory row width of the em2 tile: column 3 holds the x0-1 halo, the
+// 128 tile columns start at 4 so every thread's four cells are one 16-byte slot.
+constexpr int kEm2Row = 132;
+
+// Four consecutive cells per thread along x: the tile is 128 x (8*ZB) cells
+// and every field, coefficient and table access of a row is one 16-byte load
+// or store.
 template <int ZB>
-__device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by, int gridx, float (*sH)[33]) {
+__device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by, int gridx,
+                                         float (*sH)[kEm2Row]) {
   const int NX = a.NX, NZ = a.NZ, P = a.P, W = a.W;
   const int tx = threadIdx.x, ty = threadIdx.y;
   if (bx == 0 && by == 0 && t > a.io.ctl->run_start) {
     const float* ch[2] = {a.Ex0, a.Ez0};
     gather_receivers<2>(a.io.rec, a.io.nrec, a.io.traces, t - 1, ch, P, 1, false);
   }
-  const int x0 = bx * 32, z0 = by * (8 * ZB);
-  const int i = x0 + tx;
-  // ---- H half-step on the owned cells
+  const int x0 = bx * 128, z0 = by * (8 * ZB);
+  const int i0 = x0 + 4 * tx;
+  const bool active = i0 < NX;
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 ikx4 = zero4, adx4 = zero4, bx4 = zero4, ikxh4 = zero4, adxh4 = zero4, bxh4 = zero4;
+  if (active) {
+    ikx4 = ld4(a.X.ik + i0); adx4 = ld4(a.X.ad + i0); bx4 = ld4(a.X.b + i0);
+    ikxh4 = ld4(a.X.ikh + i0); adxh4 = ld4(a.X.adh + i0); bxh4 = ld4(a.X.bh + i0);
+  }
+  const int sx = 4 + 4 * tx;  // shared-memory column of element 0
+
+  // One row of the H half-step for this thread's four cells (k <= NZ-2).
+  // Writes the new Hy values to hv; when `own`, also stores Hy and the memory
+  // variables of the new copy.
+  auto h_row = [&](int k, bool own, float4& hv) {
+    const int c0 = k * P + i0;
+    const float4 hy = active ? ld4(a.Hy0 + c0) : zero4;
+    const float4 ex = active ? ld4(a.Ex0 + c0) : zero4;
+    const float4 exn = active ? ld4(a.Ex0 + c0 + P) : zero4;
+    const float4 ez = active ? ld4(a.Ez0 + c0) : zero4;
+    float ez_next = __shfl_down_sync(0xffffffffu, ez.x, 1);
+    if (tx == 31) ez_next = (i0 + 4 < NX) ? __ldg(a.Ez0 + c0 + 4) : 0.f;
+    const bool zs = in_strip(k, NZ, W);
+    const int zrow = (zs ? strip_idx(k, NZ, W) : 0) * P + i0;
+    const float4 pz0 = (zs && active) ? ld4(a.mExz0 + zrow) : zero4;
+    const float ikz = __ldg(a.Z.ik + k), adz = __ldg(a.Z.ad + k), bz = __ldg(a.Z.b + k);
+    float4 pz1 = pz0, hy1 = hy;
 #pragma unroll
-  for (int r = 0; r < ZB; ++r) {
-    const int k = z0 + ty + 8 * r;
-    if (i < NX && k < NZ) {
-      const int c = k * P + i;
-      float h;
-      if (i <= NX - 2 && k <= NZ - 2) {
-        float pz = 0.f, px = 0.f;
-        bool zs, xs;
-        h = em2_h_cell(a, i, k, pz, px, zs, xs);
-        if (zs) a.mExz1[strip_idx(k, NZ, W) * P + i] = pz;
-        if (xs) a.mEzx1[k * (2 * W) + strip_idx(i, NX, W)] = px;
-        const bool edge = (i == 0) | (i == NX - 2) | (k == 0) | (k == NZ - 2);  // :314-317
-        a.Hy1[c] = edge ? 0.0f : h;
-      } else {
-        h = __ldg(a.Hy0 + c);
-        a.Hy1[c] = h;
-        if (in_strip(k, NZ, W)) {
-          const int m = strip_idx(k, NZ, W) * P + i;
-          a.mExz1[m] = __ldg(a.mExz0 + m);
+    for (int e = 0; e < 4; ++e) {
+      const int i = i0 + e;
+      if (i <= NX - 2) {
+        const float dEx = el(exn, e) - el(ex, e);
+        float vz = dEx * ikz;
+        if (zs) {
+          el(pz1, e) = bz * el(pz0, e) + adz * dEx;
+          vz += el(pz1, e);
         }
+        const float dEz = (e < 3 ? el(ez, e + 1) : ez_next) - el(ez, e);
+        float vx = dEz * el(ikx4, e);
         if (in_strip(i, NX, W)) {
+          const int m = k * (2 * W) + strip_idx(i, NX, W);
+          const float px = el(bx4, e) * __ldg(a.mEzx0 + m) + el(adx4, e) * dEz;
+          if (own) a.mEzx1[m] = px;
+          vx += px;
+        }
+        el(hv, e) = el(hy, e) + a.dbH * (vx + vz);
+        const bool edge = (i == 0) | (i == NX - 2) | (k == 0) | (k == NZ - 2);  // :314-317
+        el(hy1, e) = edge ? 0.0f : el(hv, e);
+      } else {
+        el(hv, e) = el(hy, e);
+        if (own && i < NX && in_strip(i, NX, W)) {
           const int m = k * (2 * W) + strip_idx(i, NX, W);
           a.mEzx1[m] = __ldg(a.mEzx0 + m);
         }
       }
-      sH[ty + 8 * r + 1][tx + 1] = h;
+    }
+    if (own && active) {
+      st4(a.Hy1 + c0, hy1);
+      if (zs) st4(a.mExz1 + zrow, pz1);
+    }
+  };
+
+  // ---- H half-step on the owned rows
+#pragma unroll
+  for (int r = 0; r < ZB; ++r) {
+    const int k = z0 + ty + 8 * r;  // uniform across the warp
+    if (k < NZ) {
+      float4 hv = zero4;
+      if (k <= NZ - 2) {
+        h_row(k, true, hv);
+      } else if (active) {  // row NZ-1 lies outside the H loop: carried over
+        const int c0 = k * P + i0;
+        hv = ld4(a.Hy0 + c0);
+        st4(a.Hy1 + c0, hv);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int i = i0 + e;
+          if (i < NX && in_strip(i, NX, W)) {
+            const int m = k * (2 * W) + strip_idx(i, NX, W);
+            a.mEzx1[m] = __ldg(a.mEzx0 + m);
+          }
+        }
+        if (in_strip(k, NZ, W)) {
+          const int zrow = strip_idx(k, NZ, W) * P + i0;
+          st4(a.mExz1 + zrow, ld4(a.mExz0 + zrow));
+        }
+      }
+      *reinterpret_cast<float4*>(&sH[ty + 8 * r + 1][sx]) = hv;
     }
   }
   // ---- halo (not stored): warp 0 takes row z0-1, warp 1 column x0-1
   if (ty == 0) {
-    if (z0 > 0 && i <= NX - 2) {
-      float pz, px;
-      bool zs, xs;
-      sH[0][tx + 1] = em2_h_cell(a, i, z0 - 1, pz, px, zs, xs);
+    if (z0 > 0) {
+      float4 hv = zero4;
+      h_row(z0 - 1, false, hv);
+      *reinterpret_cast<float4*>(&sH[0][sx]) = hv;
     }
   } else if (ty == 1) {
     for (int q = tx; q < 8 * ZB; q += 32) {
@@ -90,56 +161,67 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
       if (x0 > 0 && k <= NZ - 2) {
         float pz, px;
         bool zs, xs;
-        sH[q + 1][0] = em2_h_cell(a, x0 - 1, k, pz, px, zs, xs);
+        sH[q + 1][3] = em2_h_cell(a, x0 - 1, k, pz, px, zs, xs);
       }
     }
   }
   __syncthreads();
-  // ---- E half-step, source, Dirichlet, norm on the owned cells
+  // ---- E half-step, source, Dirichlet, norm on the owned rows
   float norm = 0.0f;
-  if (i < NX) {
-    const bool xs = in_strip(i, NX, W);
-    const int xsi = xs ? strip_idx(i, NX, W) : 0;
-    const float ikxh = __ldg(a.X.ikh + i), bxh = __ldg(a.X.bh + i), adxh = __ldg(a.X.adh + i);
 #pragma unroll
-    for (int r = 0; r < ZB; ++r) {
-      const int k = z0 + ty + 8 * r;
-      if (k < NZ) {
-        const int c = k * P + i;
-        const int kk = ty + 8 * r + 1, ii = tx + 1;
-        float ex = __ldg(a.Ex0 + c), ez = __ldg(a.Ez0 + c);
+  for (int r = 0; r < ZB; ++r) {
+    const int k = z0 + ty + 8 * r;
+    if (k < NZ && active) {
+      const int c0 = k * P + i0;
+      const int kk = ty + 8 * r + 1;
+      float4 ex = ld4(a.Ex0 + c0), ez = ld4(a.Ez0 + c0);
+      const float4 cax = ld4(a.CAx + c0), cbx = ld4(a.CBx + c0), caz = ld4(a.CAz + c0), cbz = ld4(a.CBz + c0);
+      const float4 h = *reinterpret_cast<const float4*>(&sH[kk][sx]);
+      const float4 hm = *reinterpret_cast<const float4*>(&sH[kk - 1][sx]);
+      const float hl = sH[kk][sx - 1];
+      const bool zs = in_strip(k, NZ, W);
+      const int zrow = (zs ? strip_idx(k, NZ, W) : 0) * P + i0;
+      const float4 pc0 = zs ? *reinterpret_cast<const float4*>(a.mHyz0 + zrow) : zero4;
+      float4 pc1 = pc0;
+      const float ikzh = __ldg(a.Z.ikh + k), adzh = __ldg(a.Z.adh + k), bzh = __ldg(a.Z.bh + k);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int i = i0 + e;
+        if (i >= NX) break;
+        float exv = el(ex, e), ezv = el(ez, e);
         if (i <= NX - 2 && k >= 1 && k <= NZ - 2) {  // :273-283
-          const float dH = sH[kk][ii] - sH[kk - 1][ii];
-          float d = dH * __ldg(a.Z.ikh + k);
-          if (in_strip(k, NZ, W)) {
-            const int m = strip_idx(k, NZ, W) * P + i;
-            const float psi = __ldg(a.Z.bh + k) * a.mHyz0[m] + __ldg(a.Z.adh + k) * dH;
-            a.mHyz[m] = psi;
-            d += psi;
+          const float dH = el(h, e) - el(hm, e);
+          float d = dH * ikzh;
+          if (zs) {
+            el(pc1, e) = bzh * el(pc0, e) + adzh * dH;
+            d += el(pc1, e);
           }
-          ex = __ldg(a.CAx + c) * ex + __ldg(a.CBx + c) * d;
+          exv = el(cax, e) * exv + el(cbx, e) * d;
         }
         if (k <= NZ - 2 && i >= 1 && i <= NX - 2) {  // :285-295
-          const float dH = sH[kk][ii] - sH[kk][ii - 1];
-          float d = dH * ikxh;
-          if (xs) {
-            const int m = k * (2 * W) + xsi;
-            const float psi = bxh * a.mHyx0[m] + adxh * dH;
+          const float dH = el(h, e) - (e == 0 ? hl : el(h, e - 1));
+          float d = dH * el(ikxh4, e);
+          if (in_strip(i, NX, W)) {
+            const int m = k * (2 * W) + strip_idx(i, NX, W);
+            const float psi = el(bxh4, e) * a.mHyx0[m] + el(adxh4, e) * dH;
             a.mHyx[m] = psi;
             d += psi;
           }
-          ez = __ldg(a.CAz + c) * ez + __ldg(a.CBz + c) * d;
+          ezv = el(caz, e) * ezv + el(cbz, e) * d;
         }
         if (i == a.io.si && k == a.io.sk) {  // :300-301
-          ex += a.io.src[t];
-          ez += a.io.src[a.io.nstep + t];
+          exv += a.io.src[t];
+          ezv += a.io.src[a.io.nstep + t];
         }
-        if (i == 0 || i == NX - 2 || k == 0 || k == NZ - 1) ex = 0.0f;  // :304-312
-        if (i == 0 || i == NX - 1 || k == 0 || k == NZ - 2) ez = 0.0f;
-        a.Ex1[c] = ex;
-        a.Ez1[c] = ez;
-        norm = fmaxf(norm, norm_monitor(ex, ez));
+        if (i == 0 || i == NX - 2 || k == 0 || k == NZ - 1) exv = 0.0f;  // :304-312
+        if (i == 0 || i == NX - 1 || k == 0 || k == NZ - 2) ezv = 0.0f;
+        el(ex, e) = exv;
+        el(ez, e) = ezv;
+        norm = fmaxf(norm, norm_monitor(exv, ezv));
       }
+      st4(a.Ex1 + c0, ex);
+      st4(a.Ez1 + c0, ez);
+      if (zs) st4(a.mHyz + zrow, pc1);
     }
   }
   block_norm_to_slot(norm, a.io.slots, by * gridx + bx);

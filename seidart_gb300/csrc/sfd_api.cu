@@ -74,6 +74,15 @@ int cuda_fail(cudaError_t e, const char* what) {
   return fail(SFD_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
+}  // namespace
+
+namespace sfd {
+// Replace the calling thread's error message (used by the static-scratch entry point).
+void set_error(const char* msg) { g_err = msg ? msg : ""; }
+}  // namespace sfd
+
+namespace {
+
 #define CK(call)                                   \
   do {                                             \
     cudaError_t e_ = (call);                       \
@@ -206,7 +215,7 @@ void make_layout(const sfd_config& c, Layout* L) {
   const int nax = is3(c.kind) ? 3 : 2;
   const int lens[3] = {c.nx, is3(c.kind) ? c.ny : c.nz, c.nz};
   for (int a = 0; a < 3; ++a) L->off_axis[a] = 0;
-  for (int a = 0; a < nax; ++a) { L->off_axis[a] = o; o += align256(sizeof(float) * 6 * lens[a]); }
+  for (int a = 0; a < nax; ++a) { L->off_axis[a] = o; o += align256(sizeof(float) * 6 * axis_stride(lens[a])); }
   L->off_q3 = o; o += align256(sizeof(float) * c.nz);
   L->off_src = o; o += align256(sizeof(float) * (size_t)nchan(c.kind) * c.nstep);
   L->off_rec = o; o += align256(sizeof(int) * 3 * (size_t)std::max(1, c.nrec));
@@ -484,6 +493,17 @@ int32_t sfd_state_bytes(const sfd_config* cfg, size_t* bytes) {
 }
 
 int32_t sfd_create(const sfd_config* cfg, void* dev_state, size_t state_bytes, void* stream, sfd_handle** out) {
+  return sfd::create_handle(cfg, dev_state, state_bytes, stream, true, out);
+}
+
+}  // extern "C"
+
+namespace sfd {
+
+// Handle creation; `graphs` = false creates no capture stream and runs every
+// step with plain launches.
+int32_t create_handle(const sfd_config* cfg, void* dev_state, size_t state_bytes, void* stream, bool graphs,
+                      sfd_handle** out) {
   g_err.clear();
   int r = validate_cfg(cfg);
   if (r) return r;
@@ -507,14 +527,21 @@ int32_t sfd_create(const sfd_config* cfg, void* dev_state, size_t state_bytes, v
   h->base = (char*)dev_state;
   h->stream = (cudaStream_t)stream;
   h->single = has_single_pass(cfg->kind) && !(cfg->flags & SFD_FLAG_TWO_PASS);
-  e = cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking);
-  if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaStreamCreateWithFlags"); }
+  h->cap_stream = nullptr;
+  if (graphs) {
+    e = cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaStreamCreateWithFlags"); }
+  }
   bind_args(h);
   e = cudaMemsetAsync(h->base, 0, L.total, h->stream);
   if (e != cudaSuccess) { cudaStreamDestroy(h->cap_stream); delete h; return cuda_fail(e, "cudaMemsetAsync"); }
   *out = h;
   return SFD_OK;
 }
+
+}  // namespace sfd
+
+extern "C" {
 
 int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
   g_err.clear();
@@ -681,15 +708,16 @@ int32_t sfd_set_cpml(sfd_handle* h, const double* prof, int64_t count) {
       return fail(SFD_ERR_BAD_ARG, "CPML a-coefficients of axis %c are nonzero outside the %d-cell strips", axn, c.npml);
     for (int i = 0; i < n; ++i)
       if (!(K[i] > 0) || !(Kh[i] > 0)) return fail(SFD_ERR_BAD_ARG, "CPML kappa of axis %c must be positive", axn);
-    std::vector<float> t(6 * (size_t)n);
+    const int st = axis_stride(n);
+    std::vector<float> t(6 * (size_t)st, 0.0f);
     const double d = deltas[a];
     for (int i = 0; i < n; ++i) {
       t[i] = (float)(1.0 / (d * K[i]));
-      t[n + i] = (float)(A[i] / d);
-      t[2 * n + i] = (float)B[i];
-      t[3 * n + i] = (float)(1.0 / (d * Kh[i]));
-      t[4 * n + i] = (float)(Ah[i] / d);
-      t[5 * n + i] = (float)Bh[i];
+      t[st + i] = (float)(A[i] / d);
+      t[2 * st + i] = (float)B[i];
+      t[3 * st + i] = (float)(1.0 / (d * Kh[i]));
+      t[4 * st + i] = (float)(Ah[i] / d);
+      t[5 * st + i] = (float)Bh[i];
     }
     CK(cudaMemcpyAsync(h->axis(a), t.data(), sizeof(float) * t.size(), cudaMemcpyHostToDevice, h->stream));
     if (a == 0 && c.kind == SFD_SEISMIC2)  // b_x_half read at the z index, seismicfdtd.f95:255
@@ -820,8 +848,8 @@ int32_t sfd_run(sfd_handle* h, int64_t nsteps) {
   Ctl* ctl = (Ctl*)(h->base + L.off_ctl);
   float* slots = (float*)(h->base + L.off_slots);
   k_begin<<<std::min(1024, (L.nslots + 255) / 256 + 1), 256, 0, h->stream>>>(ctl, slots, L.nslots, (int)h->step);
-  const int64_t chunks = nsteps / kGraphSteps;
-  const int rem = (int)(nsteps % kGraphSteps);
+  const int64_t chunks = h->cap_stream ? nsteps / kGraphSteps : 0;
+  const int rem = (int)(nsteps - chunks * kGraphSteps);
   if (chunks > 0) {
     int r = ensure_graph(h, h->single ? h->cur : 0);
     if (r) return r;
@@ -917,12 +945,26 @@ struct sfd_batch_s {
   std::vector<BatchModel> models;
   std::vector<int> steps;
   GridBarrier* bar() const { return (GridBarrier*)scratch; }
+  std::vector<BatchGroup> groups;
   int* dsteps() const { return (int*)(scratch + 256); }
   BatchModel* dmodels() const { return (BatchModel*)(scratch + 256 + align256(sizeof(int) * h.size())); }
+  BatchGroup* dgroups() const {
+    return (BatchGroup*)(scratch + 256 + align256(sizeof(int) * h.size()) + align256(sizeof(BatchModel) * h.size()));
+  }
 };
 
 namespace {
-size_t batch_bytes(int n) { return 256 + align256(sizeof(int) * n) + align256(sizeof(BatchModel) * (size_t)n); }
+size_t batch_bytes(int n) {
+  return 256 + align256(sizeof(int) * n) + align256(sizeof(BatchModel) * (size_t)n) +
+         align256(sizeof(BatchGroup) * (size_t)n);
+}
+
+// Models that read the same coefficient planes and have the same geometry.
+bool same_group(const sfd_handle* a, const sfd_handle* b) {
+  if (a->cfg.kind != b->cfg.kind || a->cfg.nx != b->cfg.nx || a->cfg.nz != b->cfg.nz) return false;
+  if (a->cfg.kind == SFD_ELECTROMAG2) return a->em2s[0].CAx == b->em2s[0].CAx;
+  return a->s2s[0].A11 == b->s2s[0].A11;
+}
 }  // namespace
 
 extern "C" {
@@ -990,14 +1032,12 @@ int32_t sfd_batch_run(sfd_batch* b, int64_t nsteps) {
   if (bps < 1) return fail(SFD_ERR_CUDA, "batch kernel does not fit on an SM");
   b->models.assign(n, BatchModel());
   b->steps.assign(n, 0);
-  int tile0 = 0;
   for (int m = 0; m < n; ++m) {
     sfd_handle* h = b->h[m];
     BatchModel& md = b->models[m];
     md.kind = h->cfg.kind == SFD_ELECTROMAG2 ? SFD_BATCH_EM2 : SFD_BATCH_SEIS2;
-    md.gx = (h->cfg.nx + 31) / 32;
+    md.gx = md.kind == SFD_BATCH_EM2 ? (h->cfg.nx + 127) / 128 : (h->cfg.nx + 31) / 32;  // em2 tiles are 128 wide
     const int gy = (h->cfg.nz + 8 * b->zb - 1) / (8 * b->zb);
-    md.tile0 = tile0;
     md.ntiles = md.gx * gy;
     md.nslots = md.ntiles;
     md.cur = h->cur;
@@ -1005,15 +1045,31 @@ int32_t sfd_batch_run(sfd_batch* b, int64_t nsteps) {
     md.em2[1] = h->em2s[1];
     md.s2[0] = h->s2s[0];
     md.s2[1] = h->s2s[1];
-    tile0 += md.ntiles;
     b->steps[m] = (int)h->step;
+  }
+  b->groups.clear();
+  int tile0 = 0;
+  for (int m = 0; m < n;) {
+    int e = m + 1;
+    while (e < n && same_group(b->h[m], b->h[e])) ++e;
+    BatchGroup g;
+    g.first = m;
+    g.n = e - m;
+    g.tile0 = tile0;
+    g.ntiles = g.n * b->models[m].ntiles;
+    tile0 += g.ntiles;
+    b->groups.push_back(g);
+    m = e;
   }
   const int total = tile0;
   const int grid = std::max(1, std::min(total, bps * b->nsm));
   CK(cudaMemcpyAsync(b->dsteps(), b->steps.data(), sizeof(int) * n, cudaMemcpyHostToDevice, b->stream));
   CK(cudaMemcpyAsync(b->dmodels(), b->models.data(), sizeof(BatchModel) * n, cudaMemcpyHostToDevice, b->stream));
+  CK(cudaMemcpyAsync(b->dgroups(), b->groups.data(), sizeof(BatchGroup) * b->groups.size(), cudaMemcpyHostToDevice,
+                     b->stream));
   batch_begin(b->dmodels(), n, b->dsteps(), b->bar(), b->stream);
-  CK(batch_launch(b->zb, grid, b->dmodels(), n, total, (int)nsteps, b->bar(), b->limit_ns, b->stream));
+  CK(batch_launch(b->zb, grid, b->dmodels(), b->dgroups(), (int)b->groups.size(), total, (int)nsteps, b->bar(),
+                  b->limit_ns, b->stream));
   batch_end(b->dmodels(), n, (int)nsteps, b->stream);
   CK(cudaGetLastError());
   for (sfd_handle* h : b->h) {
@@ -1226,9 +1282,10 @@ int32_t sfd_adjoint_segment(sfd_handle* h, int64_t nsteps) {
   a.rec = (const int*)(h->base + L.off_rec); a.nrec = h->cfg.nrec; a.resid = h->adj_resid;
   for (int64_t s = nsteps - 1; s >= 0; --s) {
     const AdjState S = adj_state_at(A, h->adj + A.slots + A.state * (size_t)s);
+    const AdjState S1 = adj_state_at(A, h->adj + A.slots + A.state * (size_t)(s + 1));
     const AdjState Lc = adj_state_at(A, h->adj + A.lam[h->adj_cur]);
     const AdjState Ln = adj_state_at(A, h->adj + A.lam[1 - h->adj_cur]);
-    adj_step(a, S, Lc, Ln, (int)(s0 + s), h->stream);
+    adj_step(a, S, S1, Lc, Ln, (int)(s0 + s), h->stream);
     h->adj_cur ^= 1;
   }
   CK(cudaGetLastError());
@@ -1295,6 +1352,49 @@ int32_t sfd_adjoint_gradient(sfd_handle* h, double* out, int64_t count) {
     g11[n] += -(double)acc[0] / e11[n];
     g33[n] += -(double)acc[1] / e33[n];
   }
+  return SFD_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int32_t sfd_share_model(sfd_handle* dst, const sfd_handle* src) {
+  g_err.clear();
+  if (!dst || !src || dst == src) return fail(SFD_ERR_BAD_ARG, "need two different handles");
+  const sfd_config &a = dst->cfg, &b = src->cfg;
+  if (a.kind != b.kind || a.nx != b.nx || a.ny != b.ny || a.nz != b.nz || a.dt != b.dt || a.flags != b.flags)
+    return fail(SFD_ERR_BAD_ARG, "handles differ in kind, grid, dt or flags");
+  if (!src->have_model) return fail(SFD_ERR_STATE, "the source handle has no model");
+  switch (a.kind) {
+    case SFD_ELECTROMAG2: {
+      const Em2Args& e = src->em2;
+      dst->em2.CAx = e.CAx; dst->em2.CBx = e.CBx; dst->em2.CAz = e.CAz; dst->em2.CBz = e.CBz;
+      for (int p = 0; p < 2; ++p) {
+        dst->em2s[p].CAx = e.CAx; dst->em2s[p].CBx = e.CBx; dst->em2s[p].CAz = e.CAz; dst->em2s[p].CBz = e.CBz;
+      }
+      break;
+    }
+    case SFD_SEISMIC2: {
+      const Seis2Args& e = src->s2;
+      Seis2Args& d = dst->s2;
+      d.A11 = e.A11; d.A13 = e.A13; d.A15 = e.A15; d.A33 = e.A33; d.A35 = e.A35; d.B15 = e.B15; d.B35 = e.B35;
+      d.B55 = e.B55; d.dtrx = e.dtrx; d.dtrz = e.dtrz; d.gxp = e.gxp; d.gzp = e.gzp;
+      for (int p = 0; p < 2; ++p) {
+        Seis2Step& t = dst->s2s[p];
+        t.A11 = e.A11; t.A13 = e.A13; t.A15 = e.A15; t.A33 = e.A33; t.A35 = e.A35; t.B15 = e.B15; t.B35 = e.B35;
+        t.B55 = e.B55; t.dtrx = e.dtrx; t.dtrz = e.dtrz; t.gxp = e.gxp; t.gzp = e.gzp;
+      }
+      set_atten(dst, src->s2.atten);
+      break;
+    }
+    default:
+      return fail(SFD_ERR_BAD_ARG, "model sharing is implemented for electromag2 and seismic2");
+  }
+  for (int q = 0; q < 3; ++q) dst->src_scale[q] = src->src_scale[q];
+  dst->model = src->model;
+  dst->have_model = true;
+  invalidate_graph(dst);
   return SFD_OK;
 }
 

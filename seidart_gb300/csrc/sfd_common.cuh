@@ -39,14 +39,19 @@ struct AxisTab {
   const float* bh;
 };
 
+// Each table row is padded to a multiple of 32 floats so 16-byte vector
+// loads of four consecutive entries stay aligned.
+__host__ __device__ inline int axis_stride(int n) { return (n + 31) & ~31; }
+
 __host__ __device__ inline AxisTab make_axis(const float* base, int n) {
+  const int s = axis_stride(n);
   AxisTab t;
   t.ik = base;
-  t.ad = base + n;
-  t.b = base + 2 * n;
-  t.ikh = base + 3 * n;
-  t.adh = base + 4 * n;
-  t.bh = base + 5 * n;
+  t.ad = base + s;
+  t.b = base + 2 * s;
+  t.ikh = base + 3 * s;
+  t.adh = base + 4 * s;
+  t.bh = base + 5 * s;
   return t;
 }
 

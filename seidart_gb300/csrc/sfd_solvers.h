@@ -136,6 +136,17 @@ void em25_half1(const Em25Args& a, const Launch& L, int rel, cudaStream_t s);
 void em25_half2(const Em25Args& a, const Launch& L, int rel, cudaStream_t s);
 void em25_finalize(const Em25Args& a, int t_last, cudaStream_t s);
 
+}  // namespace sfd
+
+struct sfd_config;
+struct sfd_handle_s;
+
+namespace sfd {
+
+int32_t create_handle(const sfd_config* cfg, void* dev_state, size_t state_bytes, void* stream, bool graphs,
+                      sfd_handle_s** out);
+void set_error(const char* msg);
+
 // Fused steps (one launch per time step); zb = rows per thread (1, 2 or 4).
 Launch em2_step_launch(const Em2Step& a, int zb);
 void em2_step(const Em2Step& a, const Launch& L, int zb, int rel, cudaStream_t s);

@@ -143,6 +143,11 @@ class FDTDSolver:
             arr = np.ascontiguousarray(profiles, dtype=np.float64)
         check(self._L.sfd_set_cpml(self._h, _dptr(arr), arr.size))
 
+    def share_model(self, other: "FDTDSolver") -> None:
+        """Read ``other``'s update coefficients instead of a copy (shots of one model)."""
+        check(self._L.sfd_share_model(self._h, other._h))
+        self._model_owner = other  # keeps the coefficients alive
+
     def set_source(self, ijk, srcfn) -> None:
         """Source cell (i, j, k) (j = 0 in 2-D) and time functions (ncomp, nstep)."""
         s = np.ascontiguousarray(srcfn, dtype=np.float64)
