@@ -189,6 +189,24 @@ int32_t sfd_launch_half(sfd_handle* h, int32_t which, int32_t count);
 /* Release the handle (the caller frees its device buffer afterwards). */
 int32_t sfd_destroy(sfd_handle* h);
 
+/* ---- One shot without device allocation --------------------------------------
+ * For callers that cannot call cudaMalloc (a host application that owns every
+ * device allocation and exposes no allocator, a plugin whose process forbids
+ * new device allocations, a fixed memory budget).  Runs one electromag2 shot
+ * with the whole device state in a file-scope device array of 32 MiB that
+ * every GPU loading this library holds until exit; larger configurations are
+ * rejected with SFD_ERR_BAD_ARG.  Inputs and outputs are host arrays: model
+ * (6 planes as sfd_set_model), profiles (as sfd_set_cpml), source cell and
+ * time functions (2 x nstep, as sfd_set_source), receivers (nrec (i,j,k)
+ * triples) and traces out (nstep x 2 x nrec FP32).  Each call clears the
+ * array first; calls whose GPU work overlaps race on it.  The first call on a
+ * device looks up the array's address and should come before any stream
+ * capture.  No counterpart in the reference: it is an addition for callers
+ * that cannot allocate. */
+int32_t sfd_electromag2_run_static(const sfd_config* cfg, const double* model, const double* profiles,
+                                   int32_t isrc, int32_t ksrc, const double* srcfn, const int32_t* rec_ijk,
+                                   float* traces, void* stream);
+
 /* ---- Checkpoints ------------------------------------------------------------
  * The dynamic state (every field and CPML memory variable) of a handle,
  * copied to / from a caller-owned device buffer on the handle's stream.
