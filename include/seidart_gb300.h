@@ -65,6 +65,10 @@ extern "C" {
 #define SFD_FLAG_TWO_PASS 1 /* 2-D kinds: two kernels per step (one per half-step,
                                fields updated in place) instead of the default
                                single-pass step over ping-pong copies */
+#define SFD_FLAG_STREAMING 2 /* 2-D single-pass kinds: one launch per step even
+                               when the grid fits on chip (by default a run of
+                               a grid that fits in the SMs' shared memory is
+                               one launch with the state held on chip) */
 
 
 typedef struct sfd_config {
@@ -171,7 +175,8 @@ int32_t sfd_run(sfd_handle* h, int64_t nsteps);
 /* Synchronise and report: steps done and the largest field norm seen by the
  * last sfd_run.  Returns SFD_ERR_UNSTABLE when that norm exceeded 1e25 or was
  * NaN (the Fortran stops at seismicfdtd.f95:378-379; here the run completes
- * and the status reports it). */
+ * and the status reports it), SFD_ERR_TIMEOUT when an on-chip run gave up
+ * waiting for a neighbouring tile (the state is then that before the run). */
 int32_t sfd_status(sfd_handle* h, int64_t* step, double* maxnorm);
 
 /* Receiver traces [step][channel][receiver], FP32: copy to host
@@ -185,6 +190,13 @@ const float* sfd_traces_device(const sfd_handle* h);
  * handles launch their whole-step kernel.  The fields are no longer a valid
  * simulation afterwards; call sfd_reset before the next run. */
 int32_t sfd_launch_half(sfd_handle* h, int32_t which, int32_t count);
+
+/* Whether sfd_run keeps this handle's whole state on chip (one launch per run,
+ * one CTA per tile of the grid): 1 yes, 0 no (one launch per step).  Decided
+ * on the current device from its SM count and shared memory.  tiles and
+ * tile_rows (may be NULL) receive the number of tiles and of tile rows.  No
+ * counterpart in the reference: its time loop has one execution form. */
+int32_t sfd_on_chip(sfd_handle* h, int32_t* tiles, int32_t* tile_rows);
 
 /* Release the handle (the caller frees its device buffer afterwards). */
 int32_t sfd_destroy(sfd_handle* h);

@@ -1,0 +1,81 @@
+// SM-resident 2-D time stepping: a whole run in one cooperative launch, with
+// every tile's fields, coefficients and memory variables held in shared
+// memory for all of its steps.
+//
+// The grid is cut into ntx x ntz tiles of TW x TZ cells, one CTA per tile and
+// at most one CTA per SM.  Per step a CTA exchanges only its one-cell edges
+// with its neighbours, through small edge arrays in global memory (L2); the
+// edge words carry their step, which is the only synchronisation between
+// tiles.  Global memory holds the state only before and after the run.
+#pragma once
+#include <cuda_runtime.h>
+#include "sfd_solvers.h"
+
+namespace sfd {
+
+// Largest number of tile rows, and of tiles in one tile row; the edge arrays
+// of a handle are sized for it.
+constexpr int kResMaxTiles1D = 32;
+// Largest number of tiles (CTAs, at most one per SM) of one on-chip run.
+constexpr int kResMaxTiles = 256;
+// Threads of a CTA: up to 31 warps own the cells (four cells of one row per
+// thread), the last warp moves the tile's edges to and from the neighbouring
+// tiles.
+constexpr int kResThreads = 1024;
+constexpr int kResCellThreads = kResThreads - 32;
+// Receivers a CTA lists in shared memory; a tile holding more scans the
+// whole receiver list every step instead.
+constexpr int kResMaxLocalRec = 256;
+
+// Tiling of one on-chip run: ntz tile rows, each cut into its own tiles.
+// tile[b] packs x0 | x1 << 16, z0 | z1 << 16, row | (index in row) << 16 and
+// the tile count of its row; column bounds are multiples of 4 (except NX).
+// Tiles that hold CPML strip or boundary cells take the longer update and are
+// made smaller.
+struct ResPlan {
+  int ntiles, ntz;
+  int4 tile[kResMaxTiles];
+  size_t smem;  // dynamic shared memory of the largest tile
+};
+
+// Edge arrays inside a handle's state buffer.  Every edge value travels as
+// one 8-byte word {value, tag}, the tag being one more than the step that
+// reads the value, so a reader polls the words it needs until their tags
+// match and needs no separate flag, fence or second load.  Two copies,
+// selected by the parity of the reading step.
+struct ResScratch {
+  uint2* erow;  // [2 parity][2 fields][kResMaxTiles1D][P]: edge rows
+  uint2* ecol;  // [2 parity][2 fields][kResMaxTiles1D][NZp]: edge columns
+  int NZp;
+};
+
+__host__ __device__ inline int res_nzp(int NZ) { return (NZ + 31) & ~31; }
+inline size_t res_scratch_bytes(int P, int NZ) {
+  return sizeof(uint2) * 4 * kResMaxTiles1D * ((size_t)P + (size_t)res_nzp(NZ));
+}
+
+struct Em2Resident {
+  int NX, NZ, P, W;
+  float *Ex, *Ez, *Hy;               // current copy: read before, written after the run
+  float *mExz, *mEzx, *mHyz, *mHyx;  // z-, x-, z-, x-strip memory variables of the current copy
+  const float *CAx, *CBx, *CAz, *CBz;
+  AxisTab X, Z;
+  float dbH;
+  IoArgs io;
+  ResPlan plan;
+  ResScratch r;
+  int t0, nsteps;
+  unsigned long long limit_ns;  // longest wait for a neighbour before the run is abandoned
+};
+
+// Pick the tiling of an NX x NZ electromag2 grid with npml-cell strips for
+// `max_ctas` CTAs of at most `max_smem` bytes of shared memory.  Returns
+// false when the grid does not fit on chip.
+bool em2_resident_plan(int NX, int NZ, int npml, int max_ctas, size_t max_smem, ResPlan* out);
+size_t em2_resident_smem(int TW, int TZ);
+// Set the kernel's shared-memory limit (once per device) and return how many
+// CTAs of `smem` bytes fit on one SM.
+cudaError_t em2_resident_prepare(const ResPlan& plan, int* ctas_per_sm);
+cudaError_t em2_resident_launch(const Em2Resident& a, cudaStream_t s);
+
+}  // namespace sfd

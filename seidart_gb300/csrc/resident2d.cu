@@ -1,0 +1,683 @@
+// SM-resident electromag2 run: every time step of an sfd_run in one
+// cooperative launch, with the whole state on chip.
+//
+// Tile (bx, bz) of TW x TZ cells (ResPlan) belongs to one CTA for the whole run.  Cell
+// thread (tx, ty) owns the cells 4tx..4tx+3 of tile row ty and keeps their
+// Ex, Ez and Hy in registers from the first step to the last; the update
+// coefficients and the CPML memory variables stay in shared memory.  The per-cell arithmetic is that of the single-pass tile
+// (fused2d.cuh), i.e. the loops of legacy/fortran/electromagfdtd.f95:249-321,
+// so the streaming and on-chip forms give the same fields.
+//
+// Inside a tile, the values a thread needs from its neighbours pass through
+// four shared-memory arrays:
+//   H half-step: Hy(i,k) needs Ex(i,k+1) -- the row of the thread below
+//     (sExRow) -- and Ez(i+4,k) -- the first column of the thread to the right
+//     (sEzCol);
+//   E half-step: Ex(i,k) needs Hy(i,k-1) -- the row of the thread above
+//     (sHyRow) -- and Ez(i,k) needs Hy(i-1,k) -- the last column of the thread
+//     to the left (sHyCol).
+// Between tiles the same edges travel through global memory (L2) as 8-byte
+// words {value, tag} (resident.h), tag = s + 1 for the step s that reads
+// them, in the copy of parity s & 1.  Cell threads on a tile edge write their
+// words as soon as they are computed; the last warp of the CTA polls the
+// neighbours' words during each half-step and copies them into the halo
+// entries of those arrays (row TZ, column TXT, row 0, column 0) before the
+// barrier that ends the half-step.  A tile can be at most one step ahead of a neighbour
+// that reads its edges, so two copies keep a word from being overwritten
+// before it is read.  The polling warp gives up after limit_ns (%globaltimer)
+// or when another tile has given up, records the failure in the control block,
+// and the CTA leaves the run at the next barrier; the host reports
+// SFD_ERR_TIMEOUT.  The launch is cooperative, so all tiles are co-resident
+// and a correct run never reaches the limit.
+//
+// Threads whose four cells are away from the CPML strips, the Dirichlet
+// planes and the source take a short path; the others apply the strip
+// recursions and, through per-cell masks fixed at the start, the loop bounds,
+// Dirichlet planes and source of the Fortran -- the same operations in the
+// same order.
+#include <algorithm>
+#include <vector>
+
+#include "fused2d.cuh"
+#include "resident.h"
+
+namespace sfd {
+
+namespace {
+
+__device__ __forceinline__ unsigned long long res_timer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void ll_put4(uint2* p, float4 v, unsigned tag) {
+  asm volatile("st.volatile.global.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(p), "r"(__float_as_uint(v.x)), "r"(tag),
+               "r"(__float_as_uint(v.y)), "r"(tag));
+  asm volatile("st.volatile.global.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(p + 2), "r"(__float_as_uint(v.z)),
+               "r"(tag), "r"(__float_as_uint(v.w)), "r"(tag));
+}
+
+__device__ __forceinline__ void ll_put1(uint2* p, float v, unsigned tag) {
+  asm volatile("st.volatile.global.v2.u32 [%0], {%1, %2};" ::"l"(p), "r"(__float_as_uint(v)), "r"(tag));
+}
+
+__device__ __forceinline__ uint4 ld_vol4(const uint2* p) {
+  uint4 r;
+  asm volatile("ld.volatile.global.v4.u32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+               : "l"(p));
+  return r;
+}
+
+__device__ __forceinline__ uint2 ld_vol2(const uint2* p) {
+  uint2 r;
+  asm volatile("ld.volatile.global.v2.u32 {%0, %1}, [%2];" : "=r"(r.x), "=r"(r.y) : "l"(p));
+  return r;
+}
+
+// Called every few unsuccessful polls: false once the limit has passed or
+// any tile has given up.
+__device__ __noinline__ bool keep_polling(Ctl* ctl, unsigned long long limit_ns, unsigned long long& t0) {
+  const unsigned long long now = res_timer_ns();
+  if (t0 == 0) t0 = now;
+  if (*(volatile int*)&ctl->err) return false;
+  if (now - t0 > limit_ns) {
+    atomicExch(&ctl->err, 1);
+    return false;
+  }
+  return true;
+}
+
+// One warp: copy `nrow` row words (rsrc) into rdst[q] and `ncol` column words
+// (csrc) into cdst[c * cstride], each once its tag reads `tag`.  Each lane
+// issues the loads of all its pending words before testing any, so one round
+// trip to L2 serves them all.  At most 32 * kResFetchPerLane words.  False
+// (on every lane) if a wait gave up.
+constexpr int kResFetchPerLane = 8;
+__device__ __noinline__ bool fetch_edges(const uint2* rsrc, float* rdst, int nrow, const uint2* csrc, float* cdst, int cstride,
+                            int ncol, unsigned tag, Ctl* ctl, unsigned long long limit_ns) {
+  const int lane = threadIdx.x & 31;
+  const int n = nrow + ncol;
+  unsigned pending = 0;
+#pragma unroll
+  for (int k = 0; k < kResFetchPerLane; ++k)
+    if (lane + 32 * k < n) pending |= 1u << k;
+  bool ok = true;
+  unsigned long long t0 = 0;
+  uint2 v[kResFetchPerLane];
+  for (int it = 1; pending; ++it) {
+#pragma unroll
+    for (int k = 0; k < kResFetchPerLane; ++k) {
+      const int q = lane + 32 * k;
+      if (pending & (1u << k)) v[k] = ld_vol2(q < nrow ? rsrc + q : csrc + (q - nrow));
+    }
+#pragma unroll
+    for (int k = 0; k < kResFetchPerLane; ++k) {
+      const int q = lane + 32 * k;
+      if ((pending & (1u << k)) && v[k].y == tag) {
+        if (q < nrow) rdst[q] = __uint_as_float(v[k].x);
+        else cdst[(q - nrow) * cstride] = __uint_as_float(v[k].x);
+        pending &= ~(1u << k);
+      }
+    }
+    if (pending && (it & 7) == 0 && !keep_polling(ctl, limit_ns, t0)) {
+      ok = false;
+      break;
+    }
+  }
+  return __all_sync(0xffffffffu, ok);
+}
+
+__device__ __forceinline__ float4 lds4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void sts4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+__device__ __forceinline__ float2 lds2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ void sts2(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
+__device__ __forceinline__ float2 ld2(const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); }
+__device__ __forceinline__ float& el2(float2& v, int q) { return (&v.x)[q]; }
+__device__ __forceinline__ float el2(const float2& v, int q) { return (&v.x)[q]; }
+
+// Per-cell masks of a thread, four bits each (bit e = cell 4tx+e), fixed for
+// the run and packed in one word.
+enum : unsigned {
+  kMH = 0,     // Hy is updated (:249-262: i <= NX-2, k <= NZ-2)
+  kMEX = 4,    // Ex is updated (:273-283: i <= NX-2, 1 <= k <= NZ-2)
+  kMEZ = 8,    // Ez is updated (:285-295: 1 <= i <= NX-2, k <= NZ-2)
+  kMEXZ = 12,  // Ex is a Dirichlet plane (:304-312)
+  kMEZZ = 16,  // Ez is a Dirichlet plane
+  kMHYZ = 20,  // the stored Hy is a Dirichlet plane (:314-317)
+  kMCELL = 24  // i < NX
+};
+__device__ __forceinline__ bool mbit(unsigned m, unsigned field, int e) { return (m >> (field + e)) & 1u; }
+
+__global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __grid_constant__ Em2Resident a) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ int s_abort, s_nrec;
+  __shared__ int s_rec[2 * kResMaxLocalRec];  // (receiver, tile cell) pairs
+  const int NX = a.NX, NZ = a.NZ, P = a.P, W = a.W;
+  const int tile = blockIdx.x;
+  const int4 te = a.plan.tile[tile];
+  const int x0 = te.x & 0xffff, z0 = te.y & 0xffff, bz = te.z & 0xffff, bx = te.z >> 16;
+  const int nxt = (te.x >> 16) - x0, nzt = (te.y >> 16) - z0;
+  const int TW = (nxt + 3) & ~3, TZ = nzt;  // this tile's shared-memory layout
+  const int TXT = TW >> 2, SX = TXT + 1;
+  const int nc4 = TXT;
+  // row edges are indexed by tile row and global x, column edges by the index
+  // in the tile row and global z, so a tile row may be cut unlike its neighbours
+  const bool up = bz > 0, down = bz < a.plan.ntz - 1, left = bx > 0, right = bx < te.w - 1;
+  const int tid = threadIdx.x;
+  const bool xwarp = tid >= kResCellThreads;
+  // Threads take the tile's four-cell groups in class order -- interior
+  // groups, then CPML strip groups, then groups with a boundary plane or the
+  // source -- so each warp runs one update path instead of several in turn.
+  const int ngroups = TXT * nzt;
+  int g = -1;
+  {
+    __shared__ int s_cnt[32][3];
+    __shared__ unsigned short s_map[kResCellThreads];
+    int cls = 3;
+    if (!xwarp && tid < ngroups) {
+      const int gi = x0 + 4 * (tid % TXT), gk = z0 + tid / TXT;
+      bool edge = gi < 1 || gi + 3 > NX - 3 || gk < 1 || gk > NZ - 3 ||
+                  (gk == a.io.sk && a.io.si >= gi && a.io.si < gi + 4);
+      bool strp = in_strip(gk, NZ, W) || in_strip(gi, NX, W) || in_strip(gi + 3, NX, W);
+      cls = edge ? 2 : (strp ? 1 : 0);
+    }
+    const unsigned lane = tid & 31, warp = tid >> 5;
+    unsigned mine = 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const unsigned b = __ballot_sync(0xffffffffu, cls == c);
+      if (lane == 0) s_cnt[warp][c] = __popc(b);
+      if (cls == c) mine = __popc(b & ((1u << lane) - 1u));
+    }
+    __syncthreads();
+    if (tid == 0) {
+      int run = 0;
+      for (int c = 0; c < 3; ++c)
+        for (int w = 0; w < 32; ++w) {
+          const int n = s_cnt[w][c];
+          s_cnt[w][c] = run;
+          run += n;
+        }
+    }
+    __syncthreads();
+    if (cls < 3) s_map[s_cnt[warp][cls] + mine] = (unsigned short)tid;
+    __syncthreads();
+    if (!xwarp && tid < ngroups) g = s_map[tid];
+  }
+  const int tx = g >= 0 ? g % TXT : 0, ty = g >= 0 ? g / TXT : 0;
+  const bool cell = g >= 0;
+  const int i0 = x0 + 4 * tx, k = z0 + ty;
+  const int CS = TZ * TW, so = ty * TW + 4 * tx;
+  float* sCAx = smem;  // update coefficients, [TZ][TW] each
+  float* sCBx = sCAx + CS;
+  float* sCAz = sCBx + CS;
+  float* sCBz = sCAz + CS;
+  float* sMExz = sCBz + CS;  // CPML memory variables of strip cells, [TZ][TW] each
+  float* sMEzx = sMExz + CS;
+  float* sMHyz = sMEzx + CS;
+  float* sMHyx = sMHyz + CS;
+  float* sExRow = sMHyx + CS;            // [TZ+1][TW]: Ex of row ty; row TZ = first row of the tile below
+  float* sHyRow = sExRow + (TZ + 1) * TW;  // [TZ+1][TW]: Hy of row ty at row ty+1; row 0 = tile above
+  float* sIkx = sHyRow + (TZ + 1) * TW;    // [TW]: 1/(dx K) at the Ez nodes of the tile's columns
+  float* sIkxh = sIkx + TW;                // [TW]: the same at the half nodes
+  // scalar arrays last: every array above starts on a 16-byte boundary (TW is a multiple of 4)
+  float* sEzCol = sIkxh + TW;              // [TZ][SX]: first Ez column of thread tx; column TXT = tile right
+  float* sHyCol = sEzCol + TZ * SX;        // [TZ][SX]: column tx+1 = last Hy column of tx; column 0 = tile left
+  const int nsm = 8 * CS + 2 * (TZ + 1) * TW + 2 * TZ * SX + 2 * TW;
+  const int NZp = a.r.NZp;
+  // edge words: field 0 = first Ex row / first Ez column, 1 = last Hy row / column
+  auto erow = [&](int par, int f, int b) { return a.r.erow + (size_t)((par * 2 + f) * kResMaxTiles1D + b) * P; };
+  auto ecol = [&](int par, int f, int b) { return a.r.ecol + (size_t)((par * 2 + f) * kResMaxTiles1D + b) * NZp; };
+  Ctl* ctl = a.io.ctl;
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+
+  for (int q = tid; q < nsm; q += blockDim.x) smem[q] = 0.0f;
+  if (tid == 0) {
+    s_nrec = 0;
+    s_abort = 0;
+  }
+  __syncthreads();
+
+  // ---- load the cells
+  float4 ex = zero4, ez = zero4, hy = zero4;
+  float ikz = 0.0f, ikzh = 0.0f;
+  bool fast = false, xs = false, zs = false;
+  int se = -1;  // element holding the source
+  unsigned m = 0;
+  if (cell && ty == 0) {
+    sts4(sIkx + 4 * tx, ld4(a.X.ik + i0));
+    sts4(sIkxh + 4 * tx, ld4(a.X.ikh + i0));
+  }
+  if (cell) {
+    const int g = k * P + i0;
+    ex = ld4(a.Ex + g);
+    ez = ld4(a.Ez + g);
+    hy = ld4(a.Hy + g);
+    sts4(sCAx + so, ld4(a.CAx + g));
+    sts4(sCBx + so, ld4(a.CBx + g));
+    sts4(sCAz + so, ld4(a.CAz + g));
+    sts4(sCBz + so, ld4(a.CBz + g));
+    ikz = __ldg(a.Z.ik + k);
+    ikzh = __ldg(a.Z.ikh + k);
+    zs = in_strip(k, NZ, W);
+    if (zs) {
+      const int zrow = strip_idx(k, NZ, W) * P + i0;
+      sts4(sMExz + so, ld4(a.mExz + zrow));
+      sts4(sMHyz + so, ld4(a.mHyz + zrow));
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int i = i0 + e;
+      if (i >= NX) continue;
+      m |= 1u << (kMCELL + e);
+      if (in_strip(i, NX, W)) {
+        xs = true;
+        const int mm = k * (2 * W) + strip_idx(i, NX, W);
+        sMEzx[so + e] = a.mEzx[mm];
+        sMHyx[so + e] = a.mHyx[mm];
+      }
+      if (i <= NX - 2 && k <= NZ - 2) m |= 1u << (kMH + e);
+      if (i <= NX - 2 && k >= 1 && k <= NZ - 2) m |= 1u << (kMEX + e);
+      if (k <= NZ - 2 && i >= 1 && i <= NX - 2) m |= 1u << (kMEZ + e);
+      if (i == 0 || i == NX - 2 || k == 0 || k == NZ - 1) m |= 1u << (kMEXZ + e);
+      if (i == 0 || i == NX - 1 || k == 0 || k == NZ - 2) m |= 1u << (kMEZZ + e);
+      if (i <= NX - 2 && k <= NZ - 2 && (i == 0 || i == NX - 2 || k == 0 || k == NZ - 2)) m |= 1u << (kMHYZ + e);
+      if (k == a.io.sk && i == a.io.si) se = e;
+    }
+    // all four cells updated, none on a Dirichlet plane, in a strip or the source
+    fast = se < 0 && (m & 0xffffffu) == 0x000fffu && !xs && !zs;
+    sts4(sExRow + so, ex);
+    sEzCol[ty * SX + tx] = ez.x;
+    if (left && tx == 0) ll_put1(ecol(0, 0, bx) + k, ez.x, 1u);
+    if (up && ty == 0) ll_put4(erow(0, 0, bz) + i0, ex, 1u);
+  }
+  // receivers of this tile
+  for (int q = tid; q < a.io.nrec; q += blockDim.x) {
+    const int i = a.io.rec[3 * q], kk = a.io.rec[3 * q + 2];
+    if (i >= x0 && i < x0 + nxt && kk >= z0 && kk < z0 + nzt) {
+      const int pos = atomicAdd(&s_nrec, 1);
+      if (pos < kResMaxLocalRec) {
+        s_rec[2 * pos] = q;
+        s_rec[2 * pos + 1] = (kk - z0) * TW + (i - x0);
+      }
+    }
+  }
+  if (xwarp) {  // edges of the tiles below and to the right for step 0
+    if (!fetch_edges(down ? erow(0, 0, bz + 1) + x0 : nullptr, sExRow + TZ * TW, down ? 4 * nc4 : 0,
+                     right ? ecol(0, 0, bx + 1) + z0 : nullptr, sEzCol + TXT, SX, right ? nzt : 0, 1u, ctl,
+                     a.limit_ns) &&
+        (tid & 31) == 0)
+      s_abort = 1;
+  }
+  __syncthreads();
+  const int nloc = s_nrec;
+  unsigned recm = 0;  // own cells that are receivers
+  if (cell) {
+    for (int q = 0; q < min(nloc, kResMaxLocalRec); ++q) {
+      const int c = s_rec[2 * q + 1];
+      if (c >= so && c < so + 4) recm |= 1u << (c - so);
+    }
+    if (nloc > kResMaxLocalRec) {
+      for (int q = 0; q < a.io.nrec; ++q) {
+        const int i = a.io.rec[3 * q];
+        if (a.io.rec[3 * q + 2] == k && i >= i0 && i < i0 + 4) recm |= 1u << (i - i0);
+      }
+    }
+  }
+  const float dbH = a.dbH;
+
+  float nrm = 0.0f;
+  bool ok = s_abort == 0;
+  for (int s = 0; s < a.nsteps && ok; ++s) {
+    const int t = a.t0 + s;
+    const int par = s & 1;
+    const unsigned tag = (unsigned)s + 1u;
+
+    // ================= H half-step (electromagfdtd.f95:249-262)
+    if (cell) {
+      const float4 exn = lds4(sExRow + so + TW);
+      const float ezn = sEzCol[ty * SX + tx + 1];
+      const float4 ikx4 = lds4(sIkx + 4 * tx);
+      float4 hv;
+      if (fast) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const float dEx = el(exn, e) - el(ex, e);
+          const float dEz = (e < 3 ? el(ez, e + 1) : ezn) - el(ez, e);
+          el(hv, e) = el(hy, e) + dbH * (dEz * el(ikx4, e) + dEx * ikz);
+        }
+      } else {  // strip, bound or plane cells: two cells at a time, masks applied as selects
+        const bool hall = ((m >> kMH) & 15u) == 15u;
+        float adz = 0.0f, bzc = 0.0f;
+        if (zs) {
+          adz = __ldg(a.Z.ad + k);
+          bzc = __ldg(a.Z.b + k);
+        }
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+          float2 pz = make_float2(0.f, 0.f), px = pz, adx = pz, bxx = pz;
+          if (zs) pz = lds2(sMExz + so + 2 * hh);
+          if (xs) {
+            px = lds2(sMEzx + so + 2 * hh);
+            adx = ld2(a.X.ad + i0 + 2 * hh);
+            bxx = ld2(a.X.b + i0 + 2 * hh);
+          }
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            const int e = 2 * hh + q;
+            const bool on = hall || mbit(m, kMH, e);
+            const float dEx = el(exn, e) - el(ex, e);
+            float vz = dEx * ikz;
+            if (zs) {
+              const float p = bzc * el2(pz, q) + adz * dEx;
+              el2(pz, q) = on ? p : el2(pz, q);
+              vz += el2(pz, q);
+            }
+            const float dEz = (e < 3 ? el(ez, e + 1) : ezn) - el(ez, e);
+            float vx = dEz * el(ikx4, e);
+            if (xs) {
+              const float p = el2(bxx, q) * el2(px, q) + el2(adx, q) * dEz;
+              el2(px, q) = on ? p : el2(px, q);
+              vx += el2(px, q);
+            }
+            const float h = el(hy, e) + dbH * (vx + vz);
+            el(hv, e) = on ? h : el(hy, e);
+          }
+          if (zs) sts2(sMExz + so + 2 * hh, pz);
+          if (xs) sts2(sMEzx + so + 2 * hh, px);
+        }
+      }
+      hy = hv;
+      sts4(sHyRow + so + TW, hv);
+      sHyCol[ty * SX + tx + 1] = hv.w;
+      if (right && tx == TXT - 1) ll_put1(ecol(par, 1, bx) + k, hv.w, tag);
+      if (down && ty == nzt - 1) ll_put4(erow(par, 1, bz) + i0, hv, tag);
+    } else if (xwarp) {  // Hy row above and column on the left for this step's E half
+      if (!fetch_edges(up ? erow(par, 1, bz - 1) + x0 : nullptr, sHyRow, up ? 4 * nc4 : 0,
+                       left ? ecol(par, 1, bx - 1) + z0 : nullptr, sHyCol, SX, left ? nzt : 0, tag, ctl,
+                       a.limit_ns) &&
+          (tid & 31) == 0)
+        s_abort = 1;
+    }
+    __syncthreads();
+    if (s_abort) {
+      ok = false;
+      break;
+    }
+
+    // ================= E half-step, source, Dirichlet planes, norm (:273-321)
+    if (cell) {
+      const float4 hm = lds4(sHyRow + so);
+      const float hl = sHyCol[ty * SX + tx];
+      const float4 h = hy;
+      if (fast) {
+        const float4 cax = lds4(sCAx + so), cbx = lds4(sCBx + so), caz = lds4(sCAz + so), cbz = lds4(sCBz + so);
+        const float4 ikxh4 = lds4(sIkxh + 4 * tx);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const float dHz = el(h, e) - el(hm, e);
+          const float exv = el(cax, e) * el(ex, e) + el(cbx, e) * (dHz * ikzh);
+          const float dHx = el(h, e) - (e == 0 ? hl : el(h, e - 1));
+          const float ezv = el(caz, e) * el(ez, e) + el(cbz, e) * (dHx * el(ikxh4, e));
+          el(ex, e) = exv;
+          el(ez, e) = ezv;
+          nrm = fmaxf(nrm, norm_monitor(exv, ezv));
+        }
+      } else {  // strip, bound or plane cells: two cells at a time, masks applied as selects
+        const bool plain = se < 0 && (m & 0xffffffu) == 0x000fffu;
+        float adz = 0.0f, bzc = 0.0f;
+        if (zs) {
+          adz = __ldg(a.Z.adh + k);
+          bzc = __ldg(a.Z.bh + k);
+        }
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+          const float2 cax = lds2(sCAx + so + 2 * hh), cbx = lds2(sCBx + so + 2 * hh);
+          const float2 caz = lds2(sCAz + so + 2 * hh), cbz = lds2(sCBz + so + 2 * hh);
+          const float2 ikxh = lds2(sIkxh + 4 * tx + 2 * hh);
+          float2 pz = make_float2(0.f, 0.f), px = pz, adx = pz, bxx = pz;
+          if (zs) pz = lds2(sMHyz + so + 2 * hh);
+          if (xs) {
+            px = lds2(sMHyx + so + 2 * hh);
+            adx = ld2(a.X.adh + i0 + 2 * hh);
+            bxx = ld2(a.X.bh + i0 + 2 * hh);
+          }
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            const int e = 2 * hh + q;
+            const bool upx = plain || mbit(m, kMEX, e), upz = plain || mbit(m, kMEZ, e);
+            const float dHz = el(h, e) - el(hm, e);
+            float d = dHz * ikzh;
+            if (zs) {
+              const float p = bzc * el2(pz, q) + adz * dHz;
+              el2(pz, q) = upx ? p : el2(pz, q);
+              d += el2(pz, q);
+            }
+            float exv = el2(cax, q) * el(ex, e) + el2(cbx, q) * d;
+            exv = upx ? exv : el(ex, e);
+            const float dHx = el(h, e) - (e == 0 ? hl : el(h, e - 1));
+            float d2 = dHx * el2(ikxh, q);
+            if (xs) {
+              const float p = el2(bxx, q) * el2(px, q) + el2(adx, q) * dHx;
+              el2(px, q) = upz ? p : el2(px, q);
+              d2 += el2(px, q);
+            }
+            float ezv = el2(caz, q) * el(ez, e) + el2(cbz, q) * d2;
+            ezv = upz ? ezv : el(ez, e);
+            if (e == se) {  // :300-301
+              exv += a.io.src[t];
+              ezv += a.io.src[a.io.nstep + t];
+            }
+            if (!plain) {  // :304-312
+              if (mbit(m, kMEXZ, e)) exv = 0.0f;
+              if (mbit(m, kMEZZ, e)) ezv = 0.0f;
+            }
+            el(ex, e) = exv;
+            el(ez, e) = ezv;
+            if (plain || mbit(m, kMCELL, e)) nrm = fmaxf(nrm, norm_monitor(exv, ezv));
+          }
+          if (zs) sts2(sMHyz + so + 2 * hh, pz);
+          if (xs) sts2(sMHyx + so + 2 * hh, px);
+        }
+        if (!plain && ((m >> kMHYZ) & 15u)) {  // the stored Hy keeps its Dirichlet planes at zero
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            if (mbit(m, kMHYZ, e)) el(hy, e) = 0.0f;
+        }
+      }
+      sts4(sExRow + so, ex);
+      sEzCol[ty * SX + tx] = ez.x;
+      if (left && tx == 0) ll_put1(ecol(par ^ 1, 0, bx) + k, ez.x, tag + 1u);
+      if (up && ty == 0) ll_put4(erow(par ^ 1, 0, bz) + i0, ex, tag + 1u);
+      if (recm) {  // receivers of step t
+        float* tr = a.io.traces + (size_t)t * 2 * a.io.nrec;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          if (!(recm & (1u << e))) continue;
+          if (nloc <= kResMaxLocalRec) {
+            for (int q = 0; q < nloc; ++q)
+              if (s_rec[2 * q + 1] == so + e) {
+                tr[s_rec[2 * q]] = el(ex, e);
+                tr[a.io.nrec + s_rec[2 * q]] = el(ez, e);
+              }
+          } else {
+            for (int q = 0; q < a.io.nrec; ++q)
+              if (a.io.rec[3 * q] == i0 + e && a.io.rec[3 * q + 2] == k) {
+                tr[q] = el(ex, e);
+                tr[a.io.nrec + q] = el(ez, e);
+              }
+          }
+        }
+      }
+    } else if (xwarp && s + 1 < a.nsteps) {  // Ex row below and Ez column to the right for step s+1
+      if (!fetch_edges(down ? erow(par ^ 1, 0, bz + 1) + x0 : nullptr, sExRow + TZ * TW, down ? 4 * nc4 : 0,
+                       right ? ecol(par ^ 1, 0, bx + 1) + z0 : nullptr, sEzCol + TXT, SX, right ? nzt : 0, tag + 1u,
+                       ctl, a.limit_ns) &&
+          (tid & 31) == 0)
+        s_abort = 1;
+    }
+    __syncthreads();
+    if (s_abort) ok = false;
+  }
+  if (!ok) return;  // the state is left as it was loaded; the host reports the timeout
+
+  // ---- write the cells back
+  if (cell) {
+    const int g = k * P + i0;
+    st4(a.Ex + g, ex);
+    st4(a.Ez + g, ez);
+    st4(a.Hy + g, hy);
+    if (zs) {
+      const int zrow = strip_idx(k, NZ, W) * P + i0;
+      st4(a.mExz + zrow, lds4(sMExz + so));
+      st4(a.mHyz + zrow, lds4(sMHyz + so));
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int i = i0 + e;
+      if (i < NX && in_strip(i, NX, W)) {
+        const int mm = k * (2 * W) + strip_idx(i, NX, W);
+        a.mEzx[mm] = sMEzx[so + e];
+        a.mHyx[mm] = sMHyx[so + e];
+      }
+    }
+  }
+  block_norm_to_slot(nrm, a.io.slots, tile);
+}
+
+}  // namespace
+
+size_t em2_resident_smem(int TW, int TZ) {
+  const size_t SX = (size_t)TW / 4 + 1;
+  return sizeof(float) * (8 * (size_t)TZ * TW + 2 * ((size_t)TZ + 1) * TW + 2 * (size_t)TZ * SX + 2 * (size_t)TW);
+}
+
+namespace {
+
+// Cost model of the planner, in four-cell groups: a group in a CPML strip or
+// on a boundary plane takes the longer update.
+constexpr double kGeneralCost = 4.0;
+
+// Cut n items of weight 1 + beta * gen[q] into `parts` runs of about equal
+// weight; bounds[0] = 0, bounds[parts] = n.  False if a run would be empty.
+bool cut_weighted(int n, const std::vector<int>& gen, double beta, int parts, int* bounds) {
+  std::vector<double> acc(n + 1, 0.0);
+  for (int q = 0; q < n; ++q) acc[q + 1] = acc[q] + 1.0 + beta * gen[q];
+  bounds[0] = 0;
+  int q = 0;
+  for (int c = 1; c < parts; ++c) {
+    const double target = acc[n] * c / parts;
+    while (q < n && acc[q] < target) ++q;
+    q = std::max(q, bounds[c - 1] + 1);
+    if (q > n - (parts - c)) return false;
+    bounds[c] = q;
+  }
+  bounds[parts] = n;
+  return true;
+}
+
+}  // namespace
+
+bool em2_resident_plan(int NX, int NZ, int npml, int max_ctas, size_t max_smem, ResPlan* out) {
+  const int W = npml;
+  const int ng = (NX + 3) / 4;  // four-cell column groups
+  std::vector<int> gcol(ng), grow(NZ);
+  for (int g = 0; g < ng; ++g) {
+    int gen = 4 * g + 3 >= NX ? 1 : 0;
+    for (int i = 4 * g; i < std::min(NX, 4 * g + 4); ++i) gen |= (i < W || i >= NX - W || i < 1 || i > NX - 3) ? 1 : 0;
+    gcol[g] = gen;
+  }
+  for (int k = 0; k < NZ; ++k) grow[k] = (k < W || k >= NZ - W || k < 1 || k > NZ - 3) ? 1 : 0;
+  std::vector<int> pr(NZ + 1, 0);
+  for (int k = 0; k < NZ; ++k) pr[k + 1] = pr[k] + grow[k];
+  max_ctas = std::min(max_ctas, kResMaxTiles);
+
+  // Cut tile row [z0, z1) into tiles of cost <= C, greedily from the left;
+  // returns the tile count (or a count above max_ctas if impossible) and
+  // the group bounds in `cuts`.
+  auto cut_row = [&](int z0, int z1, double C, std::vector<int>* cuts) {
+    const int nr = z1 - z0, gr = pr[z1] - pr[z0];
+    int count = 0, g0 = 0;
+    double cost = 0.0;
+    if (cuts) cuts->assign(1, 0);
+    for (int g = 0; g < ng; ++g) {
+      const double cg = gcol[g] ? kGeneralCost * nr : gr * kGeneralCost + (nr - gr);
+      const int ngp = g - g0 + 1;
+      const bool over = cost + cg + 1.0 + nr > C || ngp * nr > kResCellThreads ||
+                        4 * ngp + nr > 32 * kResFetchPerLane || em2_resident_smem(4 * ngp, nr) > max_smem;
+      if (over && g > g0) {
+        ++count;
+        if (cuts) cuts->push_back(g);
+        g0 = g;
+        cost = 0.0;
+      }
+      const int ngp1 = g - g0 + 1;
+      if (ngp1 * nr > kResCellThreads || 4 * ngp1 + nr > 32 * kResFetchPerLane ||
+          em2_resident_smem(4 * ngp1, nr) > max_smem || cg + 1.0 + nr > C)
+        return max_ctas + 1;  // one group alone does not fit
+      cost += cg + 1.0;
+    }
+    ++count;
+    if (cuts) cuts->push_back(ng);
+    return count > kResMaxTiles1D ? max_ctas + 1 : count;
+  };
+
+  const double betas[] = {0.0, 1.0, 2.0, 3.0, 5.0, 8.0};
+  double best = 0.0;
+  bool found = false;
+  int best_rows[kResMaxTiles1D + 1], best_ntz = 0;
+  int rb[kResMaxTiles1D + 1];
+  for (int ntz = 1; ntz <= std::min(kResMaxTiles1D, NZ); ++ntz) {
+    for (double bzw : betas) {
+      if (!cut_weighted(NZ, grow, bzw, ntz, rb)) continue;
+      double lo = 0.0, hi = 1e12;
+      auto tiles_at = [&](double C) {
+        int total = 0;
+        for (int r = 0; r < ntz && total <= max_ctas; ++r) total += cut_row(rb[r], rb[r + 1], C, nullptr);
+        return total;
+      };
+      if (tiles_at(hi) > max_ctas) continue;
+      for (int it = 0; it < 40 && hi - lo > 0.5; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        (tiles_at(mid) <= max_ctas ? hi : lo) = mid;
+      }
+      if (!found || hi < best * (1.0 - 1e-9)) {
+        best = hi;
+        found = true;
+        best_ntz = ntz;
+        for (int r = 0; r <= ntz; ++r) best_rows[r] = rb[r];
+      }
+    }
+  }
+  if (!found) return false;
+  out->ntz = best_ntz;
+  out->ntiles = 0;
+  out->smem = 0;
+  std::vector<int> cuts;
+  for (int r = 0; r < best_ntz; ++r) {
+    const int z0 = best_rows[r], z1 = best_rows[r + 1];
+    const int n = cut_row(z0, z1, best, &cuts);
+    for (int c = 0; c < n; ++c) {
+      const int x0 = 4 * cuts[c], x1 = std::min(NX, 4 * cuts[c + 1]);
+      out->tile[out->ntiles++] = make_int4(x0 | (x1 << 16), z0 | (z1 << 16), r | (c << 16), n);
+      out->smem = std::max(out->smem, em2_resident_smem((x1 - x0 + 3) & ~3, z1 - z0));
+    }
+  }
+  return true;
+}
+
+cudaError_t em2_resident_prepare(const ResPlan& plan, int* ctas_per_sm) {
+  cudaError_t e = cudaFuncSetAttribute(em2_resident_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, em2_resident_kernel, kResThreads, plan.smem);
+}
+
+cudaError_t em2_resident_launch(const Em2Resident& a, cudaStream_t s) {
+  void* args[] = {(void*)&a};
+  return cudaLaunchCooperativeKernel((const void*)em2_resident_kernel, dim3(a.plan.ntiles),
+                                     dim3(kResThreads), args, a.plan.smem, s);
+}
+
+}  // namespace sfd

@@ -8,12 +8,14 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
 #include "../../include/seidart_gb300.h"
 #include "adjoint.h"
 #include "batch.h"
+#include "resident.h"
 #include "sfd_solvers.h"
 
 namespace sfd {
@@ -26,6 +28,7 @@ __global__ void k_begin(Ctl* ctl, float* slots, int nslots, int step) {
     ctl->run_start = step;
     ctl->maxnorm = 0.0f;
     ctl->nan_seen = 0;
+    ctl->err = 0;
   }
 }
 
@@ -156,7 +159,7 @@ struct Layout {
   int P, NX, NY, NZ, W, ysplit, nslots;
   size_t fsz;                // floats per field
   size_t off_ctl, off_fields, off_mem[18], mem_sz[18], off_fieldsB, off_memB[4], off_coef, coef_plane, off_axis[3],
-      off_q3, off_src, off_rec, off_traces, off_slots, total;
+      off_q3, off_src, off_rec, off_traces, off_slots, off_res, total;
 };
 
 int grid_slots(const sfd_config& c, int P, int ysplit) {
@@ -176,7 +179,7 @@ int validate_cfg(const sfd_config* c) {
   if (!three && c->ny != 1) return fail(SFD_ERR_BAD_ARG, "2-D solvers need ny = 1 (got %d)", c->ny);
   if (c->nstep < 1) return fail(SFD_ERR_BAD_ARG, "nstep must be >= 1");
   if (c->nrec < 0) return fail(SFD_ERR_BAD_ARG, "nrec must be >= 0");
-  if ((c->flags & ~SFD_FLAG_TWO_PASS) != 0) return fail(SFD_ERR_BAD_ARG, "unknown flags 0x%x", c->flags);
+  if ((c->flags & ~(SFD_FLAG_TWO_PASS | SFD_FLAG_STREAMING)) != 0) return fail(SFD_ERR_BAD_ARG, "unknown flags 0x%x", c->flags);
   if (!(c->dt > 0) || !(c->dx > 0) || !(c->dz > 0) || (three && !(c->dy > 0)))
     return fail(SFD_ERR_BAD_ARG, "dt and grid steps must be positive");
   const double cells = (double)c->nx * c->ny * c->nz;
@@ -221,6 +224,11 @@ void make_layout(const sfd_config& c, Layout* L) {
   L->off_rec = o; o += align256(sizeof(int) * 3 * (size_t)std::max(1, c.nrec));
   L->off_traces = o; o += align256(sizeof(float) * (size_t)c.nstep * nchan(c.kind) * std::max(1, c.nrec));
   L->off_slots = o; o += align256(sizeof(float) * L->nslots);  // ZB = 1 tiles: the largest grid
+  L->off_res = 0;
+  if (c.kind == SFD_ELECTROMAG2 && !(c.flags & (SFD_FLAG_TWO_PASS | SFD_FLAG_STREAMING))) {
+    L->off_res = o;  // step counters and edge arrays of on-chip runs
+    o += align256(res_scratch_bytes(L->P, c.nz));
+  }
   L->total = o;
 }
 
@@ -240,6 +248,8 @@ struct sfd_handle_s {
   Em2Step em2s[2];      // [p]: reads copy p, writes copy 1-p
   Seis2Step s2s[2];
   Launch launch1;       // single-pass geometry
+  int res_state = 0;    // on-chip runs: 0 not yet checked, 1 usable, -1 not usable
+  ResPlan res_plan;
   int64_t step = 0;
   std::vector<double> src_scale[3];  // planes the source amplitude is divided by
   std::vector<double> model;         // FP64 model planes (kept for the adjoint's chain rule)
@@ -421,6 +431,80 @@ void launch_finalize(sfd_handle* h, int t_last, cudaStream_t s) {
     case SFD_SEISMIC25: seis25_finalize(h->s25, t_last, s); break;
     case SFD_ELECTROMAG25: em25_finalize(h->em25, t_last, s); break;
   }
+}
+
+// Whether runs of this handle can keep the whole state on chip (decided on
+// the first run, on the device that is current then).
+bool resident_usable(sfd_handle* h) {
+  if (h->res_state) return h->res_state > 0;
+  h->res_state = -1;
+  if (!h->L.off_res || !h->single) return false;
+  int dev = 0, nsm = 0, coop = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (!coop) return false;
+  const size_t static_smem = 8192;  // receiver list, thread map and reduction buffers of the kernel
+  // Plans are searched once per grid shape and device (the search takes
+  // tens of milliseconds; a survey creates one handle per shot).
+  struct PlanKey {
+    int nx, nz, npml, ctas, dev;
+    size_t smem;
+  };
+  static std::mutex plan_mu;
+  static std::vector<std::pair<PlanKey, std::pair<bool, ResPlan>>> plans;
+  const PlanKey key{h->cfg.nx, h->cfg.nz, h->cfg.npml, std::min(nsm, h->L.nslots), dev, (size_t)optin - static_smem};
+  ResPlan plan;
+  bool fits = false, cached = false;
+  {
+    std::lock_guard<std::mutex> lock(plan_mu);
+    for (const auto& e : plans)
+      if (e.first.nx == key.nx && e.first.nz == key.nz && e.first.npml == key.npml && e.first.ctas == key.ctas &&
+          e.first.dev == key.dev && e.first.smem == key.smem) {
+        fits = e.second.first;
+        plan = e.second.second;
+        cached = true;
+        break;
+      }
+  }
+  if (!cached) {
+    fits = em2_resident_plan(key.nx, key.nz, key.npml, key.ctas, key.smem, &plan);
+    std::lock_guard<std::mutex> lock(plan_mu);
+    plans.push_back({key, {fits, plan}});
+  }
+  if (!fits) return false;
+  int per_sm = 0;
+  if (em2_resident_prepare(plan, &per_sm) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    return false;
+  }
+  h->res_plan = plan;
+  h->res_state = 1;
+  return true;
+}
+
+Em2Resident resident_args(const sfd_handle* h, int64_t nsteps) {
+  Em2Resident r;
+  const Em2Step& b = h->em2s[h->cur];
+  r.NX = b.NX; r.NZ = b.NZ; r.P = b.P; r.W = b.W;
+  r.Ex = h->fc(0, h->cur); r.Ez = h->fc(1, h->cur); r.Hy = h->fc(2, h->cur);
+  r.mExz = h->mc(0, h->cur); r.mEzx = h->mc(1, h->cur); r.mHyz = h->mc(2, 0); r.mHyx = h->mc(3, 0);
+  r.CAx = b.CAx; r.CBx = b.CBx; r.CAz = b.CAz; r.CBz = b.CBz;
+  r.X = b.X; r.Z = b.Z; r.dbH = b.dbH;
+  r.io = b.io;
+  r.plan = h->res_plan;
+  char* base = h->base + h->L.off_res;
+  r.r.erow = (uint2*)base;
+  r.r.NZp = res_nzp(h->cfg.nz);
+  r.r.ecol = r.r.erow + 4 * kResMaxTiles1D * (size_t)h->L.P;
+  r.t0 = (int)h->step;
+  r.nsteps = (int)nsteps;
+  r.limit_ns = 2000000000ull;
+  return r;
 }
 
 int ensure_graph(sfd_handle* h, int p) {
@@ -848,6 +932,15 @@ int32_t sfd_run(sfd_handle* h, int64_t nsteps) {
   Ctl* ctl = (Ctl*)(h->base + L.off_ctl);
   float* slots = (float*)(h->base + L.off_slots);
   k_begin<<<std::min(1024, (L.nslots + 255) / 256 + 1), 256, 0, h->stream>>>(ctl, slots, L.nslots, (int)h->step);
+  if (resident_usable(h)) {  // the whole run in one launch, state on chip
+    // tags from an earlier run must not match: clear every edge word
+    CK(cudaMemsetAsync(h->base + L.off_res, 0, res_scratch_bytes(L.P, L.NZ), h->stream));
+    CK(em2_resident_launch(resident_args(h, nsteps), h->stream));
+    k_reduce_slots<<<1, 1024, 0, h->stream>>>(ctl, slots, L.nslots);
+    CK(cudaGetLastError());
+    h->step += nsteps;
+    return SFD_OK;
+  }
   const int64_t chunks = h->cap_stream ? nsteps / kGraphSteps : 0;
   const int rem = (int)(nsteps - chunks * kGraphSteps);
   if (chunks > 0) {
@@ -871,6 +964,15 @@ int32_t sfd_run(sfd_handle* h, int64_t nsteps) {
   return SFD_OK;
 }
 
+int32_t sfd_on_chip(sfd_handle* h, int32_t* tiles_x, int32_t* tiles_z) {  // tiles, tile rows
+  g_err.clear();
+  if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
+  const bool on = resident_usable(h);
+  if (tiles_x) *tiles_x = on ? h->res_plan.ntiles : 0;
+  if (tiles_z) *tiles_z = on ? h->res_plan.ntz : 0;
+  return on ? 1 : 0;
+}
+
 int32_t sfd_status(sfd_handle* h, int64_t* step, double* maxnorm) {
   g_err.clear();
   if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
@@ -879,6 +981,7 @@ int32_t sfd_status(sfd_handle* h, int64_t* step, double* maxnorm) {
   CK(cudaStreamSynchronize(h->stream));
   if (step) *step = h->step;
   if (maxnorm) *maxnorm = (double)ctl.maxnorm;
+  if (ctl.err) return fail(SFD_ERR_TIMEOUT, "on-chip run: a neighbouring tile did not answer within 2 s");
   if (!(ctl.maxnorm <= 1.0e25f))
     return fail(SFD_ERR_UNSTABLE, "field norm %g exceeded 1e25 (code became unstable and blew up)", (double)ctl.maxnorm);
   return SFD_OK;

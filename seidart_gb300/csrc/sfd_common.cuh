@@ -23,7 +23,8 @@ namespace sfd {
 struct Ctl {
   int base;       // global index of the step the next launch with rel = 0 computes
   int run_start;  // first step of the current sfd_run
-  int pad0, pad1;
+  int err;       // a bounded device wait of the last run gave up
+  int pad1;
   float maxnorm;  // largest field norm of the last run (after finalize)
   int nan_seen;
   int pad2, pad3;

@@ -50,6 +50,7 @@ MEMORY = {
 
 
 FLAG_TWO_PASS = 1
+FLAG_STREAMING = 2
 
 
 def is_25d(kind: int) -> bool:
@@ -91,6 +92,9 @@ class FDTDSolver:
 
     ``flags`` = ``FLAG_TWO_PASS`` selects, for the 2-D kinds, the two-kernel
     step (fields updated in place) instead of the default single-pass step.
+    ``FLAG_STREAMING`` keeps one launch per step even where the grid would
+    fit on chip (by default an electromag2 grid that fits in the SMs' shared
+    memory runs a whole ``run`` in one launch with the state held on chip).
 
     ``nstep`` is the number of source samples (the run length); ``nrec`` the
     number of receivers.  The device state is allocated with torch on
@@ -183,6 +187,15 @@ class FDTDSolver:
         """Profiling aid: run one half-step kernel ``count`` times (state is
         invalid afterwards; reset before the next run)."""
         check(self._L.sfd_launch_half(self._h, int(which), int(count)))
+
+    def on_chip(self):
+        """(tiles, tile rows) when ``run`` keeps the whole state on chip (one
+        launch per run, one CTA per tile), else None (one launch per step)."""
+        tx, tz = C.c_int32(), C.c_int32()
+        rc = self._L.sfd_on_chip(self._h, C.byref(tx), C.byref(tz))
+        if rc < 0:
+            check(rc)
+        return (tx.value, tz.value) if rc == 1 else None
 
     # -- outputs -----------------------------------------------------------
     def field(self, name) -> np.ndarray:

@@ -59,7 +59,7 @@ def test_state_bytes(L):
     (dict(nx=10), "too small"),
     (dict(npml=0), "npml"),
     (dict(dt=0.0), "positive"),
-    (dict(flags=2), "flags"),
+    (dict(flags=4), "flags"),
     (dict(kind=_lib.SEISMIC25, ny=4), "ny="),
 ])
 def test_bad_config_rejected(L, bad, frag):

@@ -8,6 +8,7 @@ from helpers import make_solver, rel_l2, run_oracle
 from seidart_gb300 import ELECTROMAG2, SEISMIC2
 from seidart_gb300 import synthetic as sy
 from seidart_gb300.batch import Batch, autotune
+from seidart_gb300.solver import FLAG_STREAMING
 
 pytestmark = pytest.mark.gpu
 
@@ -31,7 +32,8 @@ def test_batch_matches_oracle_and_single_runs(gpu, zb, bps):
         _, ref, _, _ = run_oracle(c)
         tr = s.traces()
         assert rel_l2(tr, ref) <= 1e-5
-        with make_solver(c) as one:
+        # the batch runs the tiles of the one-launch-per-step form: same arithmetic, bit for bit
+        with make_solver(c, flags=FLAG_STREAMING) as one:
             one.run(c.nstep)
             one.status()
             assert np.array_equal(one.traces(), tr), "batched and single runs must agree bit for bit"

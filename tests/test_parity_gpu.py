@@ -22,12 +22,17 @@ TOL_FIELD = 1e-5
 TOL_MEM = 1e-4
 
 CASES = [
-    # kind, seed, nx, nz, ny, npml, nstep, flags (1 = two-pass form of the 2-D kinds)
+    # kind, seed, nx, nz, ny, npml, nstep, flags (1 = two-pass form of the 2-D
+    # kinds, 2 = one launch per step; electromag2 with 0 runs on chip)
     (ELECTROMAG2, 0, 45, 37, 1, 5, 160, 0),
     (ELECTROMAG2, 0, 45, 37, 1, 5, 160, 1),
+    (ELECTROMAG2, 0, 45, 37, 1, 5, 160, 2),
     (ELECTROMAG2, 1, 70, 52, 1, 8, 100, 0),
     (ELECTROMAG2, 1, 70, 52, 1, 8, 100, 1),
+    (ELECTROMAG2, 1, 70, 52, 1, 8, 100, 2),
     (ELECTROMAG2, 3, 97, 67, 1, 9, 75, 0),
+    (ELECTROMAG2, 4, 301, 203, 1, 12, 260, 0),  # odd sizes: partial float4 groups, ragged last tiles
+    (ELECTROMAG2, 4, 301, 203, 1, 12, 260, 2),
     (SEISMIC2, 0, 45, 37, 1, 5, 160, 0),
     (SEISMIC2, 0, 45, 37, 1, 5, 160, 1),
     (SEISMIC2, 1, 70, 52, 1, 8, 100, 0),
@@ -44,7 +49,7 @@ CASES = [
 
 def _ids(c):
     return f"{KIND_NAMES[c[0]]}-s{c[1]}-{c[2]}x{c[3]}" + (f"x{c[4]}" if c[4] > 1 else "") + \
-        ("-twopass" if c[7] else "")
+        {0: "", 1: "-twopass", 2: "-streaming"}[c[7]]
 
 
 @pytest.mark.parametrize("spec", CASES, ids=[_ids(c) for c in CASES])
