@@ -18,11 +18,12 @@ namespace sfd {
 constexpr int kResMaxTiles1D = 32;
 // Largest number of tiles (CTAs, at most one per SM) of one on-chip run.
 constexpr int kResMaxTiles = 256;
-// Threads of a CTA: up to 31 warps own the cells (four cells of one row per
-// thread), the last warp moves the tile's edges to and from the neighbouring
-// tiles.
-constexpr int kResThreads = 1024;
+// Threads of a CTA: up to 15 warps own the cells (four cells of kResRows rows
+// per thread), the last warp moves the tile's edges to and from the
+// neighbouring tiles.
+constexpr int kResThreads = 512;
 constexpr int kResCellThreads = kResThreads - 32;
+constexpr int kResRows = 2;
 // Receivers a CTA lists in shared memory; a tile holding more scans the
 // whole receiver list every step instead.
 constexpr int kResMaxLocalRec = 256;

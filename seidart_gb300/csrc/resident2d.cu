@@ -151,6 +151,7 @@ enum : unsigned {
 __device__ __forceinline__ bool mbit(unsigned m, unsigned field, int e) { return (m >> (field + e)) & 1u; }
 
 __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __grid_constant__ Em2Resident a) {
+  constexpr int RB = kResRows;
   extern __shared__ __align__(16) float smem[];
   __shared__ int s_abort, s_nrec;
   __shared__ int s_rec[2 * kResMaxLocalRec];  // (receiver, tile cell) pairs
@@ -160,27 +161,29 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
   const int x0 = te.x & 0xffff, z0 = te.y & 0xffff, bz = te.z & 0xffff, bx = te.z >> 16;
   const int nxt = (te.x >> 16) - x0, nzt = (te.y >> 16) - z0;
   const int TW = (nxt + 3) & ~3, TZ = nzt;  // this tile's shared-memory layout
-  const int TXT = TW >> 2, SX = TXT + 1;
+  const int TXT = TW >> 2, TYT = (TZ + RB - 1) / RB, SX = TXT + 1;
   const int nc4 = TXT;
   // row edges are indexed by tile row and global x, column edges by the index
   // in the tile row and global z, so a tile row may be cut unlike its neighbours
   const bool up = bz > 0, down = bz < a.plan.ntz - 1, left = bx > 0, right = bx < te.w - 1;
   const int tid = threadIdx.x;
   const bool xwarp = tid >= kResCellThreads;
-  // Threads take the tile's four-cell groups in class order -- interior
-  // groups, then CPML strip groups, then groups with a boundary plane or the
-  // source -- so each warp runs one update path instead of several in turn.
-  const int ngroups = TXT * nzt;
+  // Threads take the tile's groups (four columns x RB rows) in class order --
+  // interior groups, then CPML strip groups, then groups with a boundary
+  // plane or the source -- so each warp runs one update path instead of
+  // several in turn.
+  const int ngroups = TXT * TYT;
   int g = -1;
   {
-    __shared__ int s_cnt[32][3];
+    __shared__ int s_cnt[kResThreads / 32][3];
     __shared__ unsigned short s_map[kResCellThreads];
     int cls = 3;
     if (!xwarp && tid < ngroups) {
-      const int gi = x0 + 4 * (tid % TXT), gk = z0 + tid / TXT;
-      bool edge = gi < 1 || gi + 3 > NX - 3 || gk < 1 || gk > NZ - 3 ||
-                  (gk == a.io.sk && a.io.si >= gi && a.io.si < gi + 4);
-      bool strp = in_strip(gk, NZ, W) || in_strip(gi, NX, W) || in_strip(gi + 3, NX, W);
+      const int gi = x0 + 4 * (tid % TXT), gk0 = z0 + RB * (tid / TXT);
+      const int gk1 = min(gk0 + RB, z0 + nzt) - 1;
+      const bool edge = gi < 1 || gi + 3 > NX - 3 || gk0 < 1 || gk1 > NZ - 3 ||
+                        (a.io.sk >= gk0 && a.io.sk <= gk1 && a.io.si >= gi && a.io.si < gi + 4);
+      const bool strp = in_strip(gk0, NZ, W) || in_strip(gk1, NZ, W) || in_strip(gi, NX, W) || in_strip(gi + 3, NX, W);
       cls = edge ? 2 : (strp ? 1 : 0);
     }
     const unsigned lane = tid & 31, warp = tid >> 5;
@@ -195,7 +198,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
     if (tid == 0) {
       int run = 0;
       for (int c = 0; c < 3; ++c)
-        for (int w = 0; w < 32; ++w) {
+        for (int w = 0; w < kResThreads / 32; ++w) {  // the warps of this CTA
           const int n = s_cnt[w][c];
           s_cnt[w][c] = run;
           run += n;
@@ -207,25 +210,21 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
     if (!xwarp && tid < ngroups) g = s_map[tid];
   }
   const int tx = g >= 0 ? g % TXT : 0, ty = g >= 0 ? g / TXT : 0;
-  const bool cell = g >= 0;
-  const int i0 = x0 + 4 * tx, k = z0 + ty;
-  const int CS = TZ * TW, so = ty * TW + 4 * tx;
-  float* sCAx = smem;  // update coefficients, [TZ][TW] each
-  float* sCBx = sCAx + CS;
-  float* sCAz = sCBx + CS;
-  float* sCBz = sCAz + CS;
-  float* sMExz = sCBz + CS;  // CPML memory variables of strip cells, [TZ][TW] each
+  const int rbase = RB * ty;
+  const int nrows = g >= 0 ? min(RB, nzt - rbase) : 0;
+  const bool cell = nrows > 0;
+  const int i0 = x0 + 4 * tx;
+  const int CS = TZ * TW;
+  float* sMExz = smem;  // CPML memory variables of strip cells, [TZ][TW] each
   float* sMEzx = sMExz + CS;
   float* sMHyz = sMEzx + CS;
   float* sMHyx = sMHyz + CS;
-  float* sExRow = sMHyx + CS;            // [TZ+1][TW]: Ex of row ty; row TZ = first row of the tile below
-  float* sHyRow = sExRow + (TZ + 1) * TW;  // [TZ+1][TW]: Hy of row ty at row ty+1; row 0 = tile above
-  float* sIkx = sHyRow + (TZ + 1) * TW;    // [TW]: 1/(dx K) at the Ez nodes of the tile's columns
-  float* sIkxh = sIkx + TW;                // [TW]: the same at the half nodes
+  float* sExRow = sMHyx + CS;               // [TYT+1][TW]: first Ex row of thread row ty; row TYT = tile below
+  float* sHyRow = sExRow + (TYT + 1) * TW;  // [TYT+1][TW]: row ty+1 = last Hy row of thread row ty; row 0 = tile above
   // scalar arrays last: every array above starts on a 16-byte boundary (TW is a multiple of 4)
-  float* sEzCol = sIkxh + TW;              // [TZ][SX]: first Ez column of thread tx; column TXT = tile right
-  float* sHyCol = sEzCol + TZ * SX;        // [TZ][SX]: column tx+1 = last Hy column of tx; column 0 = tile left
-  const int nsm = 8 * CS + 2 * (TZ + 1) * TW + 2 * TZ * SX + 2 * TW;
+  float* sEzCol = sHyRow + (TYT + 1) * TW;  // [TZ][SX]: first Ez column of thread column tx; column TXT = tile right
+  float* sHyCol = sEzCol + TZ * SX;         // [TZ][SX]: column tx+1 = last Hy column of tx; column 0 = tile left
+  const int nsm = 4 * CS + 2 * (TYT + 1) * TW + 2 * TZ * SX;
   const int NZp = a.r.NZp;
   // edge words: field 0 = first Ex row / first Ez column, 1 = last Hy row / column
   auto erow = [&](int par, int f, int b) { return a.r.erow + (size_t)((par * 2 + f) * kResMaxTiles1D + b) * P; };
@@ -240,58 +239,78 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
   }
   __syncthreads();
 
-  // ---- load the cells
-  float4 ex = zero4, ez = zero4, hy = zero4;
-  float ikz = 0.0f, ikzh = 0.0f;
-  bool fast = false, xs = false, zs = false;
-  int se = -1;  // element holding the source
-  unsigned m = 0;
-  if (cell && ty == 0) {
-    sts4(sIkx + 4 * tx, ld4(a.X.ik + i0));
-    sts4(sIkxh + 4 * tx, ld4(a.X.ikh + i0));
+  // ---- load the cells into registers
+  float4 ex[RB], ez[RB], hy[RB], cax[RB], cbx[RB], caz[RB], cbz[RB];
+  float ikz[RB], ikzh[RB];
+  unsigned m[RB];  // per-row cell masks
+  bool zs[RB];
+  float4 ikx4 = zero4, ikxh4 = zero4;
+  bool fast = false, plain = false, xs = false;
+  int se = -1;  // 4 * row + element of the source cell
+#pragma unroll
+  for (int j = 0; j < RB; ++j) {
+    ex[j] = ez[j] = hy[j] = cax[j] = cbx[j] = caz[j] = cbz[j] = zero4;
+    ikz[j] = ikzh[j] = 0.0f;
+    m[j] = 0u;
+    zs[j] = false;
   }
   if (cell) {
-    const int g = k * P + i0;
-    ex = ld4(a.Ex + g);
-    ez = ld4(a.Ez + g);
-    hy = ld4(a.Hy + g);
-    sts4(sCAx + so, ld4(a.CAx + g));
-    sts4(sCBx + so, ld4(a.CBx + g));
-    sts4(sCAz + so, ld4(a.CAz + g));
-    sts4(sCBz + so, ld4(a.CBz + g));
-    ikz = __ldg(a.Z.ik + k);
-    ikzh = __ldg(a.Z.ikh + k);
-    zs = in_strip(k, NZ, W);
-    if (zs) {
-      const int zrow = strip_idx(k, NZ, W) * P + i0;
-      sts4(sMExz + so, ld4(a.mExz + zrow));
-      sts4(sMHyz + so, ld4(a.mHyz + zrow));
-    }
+    ikx4 = ld4(a.X.ik + i0);
+    ikxh4 = ld4(a.X.ikh + i0);
+    plain = true;
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const int i = i0 + e;
-      if (i >= NX) continue;
-      m |= 1u << (kMCELL + e);
-      if (in_strip(i, NX, W)) {
-        xs = true;
-        const int mm = k * (2 * W) + strip_idx(i, NX, W);
-        sMEzx[so + e] = a.mEzx[mm];
-        sMHyx[so + e] = a.mHyx[mm];
+    for (int j = 0; j < RB; ++j) {
+      if (j >= nrows) continue;
+      const int row = rbase + j, k = z0 + row;
+      const int gg = k * P + i0, so = row * TW + 4 * tx;
+      ex[j] = ld4(a.Ex + gg);
+      ez[j] = ld4(a.Ez + gg);
+      hy[j] = ld4(a.Hy + gg);
+      cax[j] = ld4(a.CAx + gg);
+      cbx[j] = ld4(a.CBx + gg);
+      caz[j] = ld4(a.CAz + gg);
+      cbz[j] = ld4(a.CBz + gg);
+      ikz[j] = __ldg(a.Z.ik + k);
+      ikzh[j] = __ldg(a.Z.ikh + k);
+      zs[j] = in_strip(k, NZ, W);
+      if (zs[j]) {
+        const int zrow = strip_idx(k, NZ, W) * P + i0;
+        sts4(sMExz + so, ld4(a.mExz + zrow));
+        sts4(sMHyz + so, ld4(a.mHyz + zrow));
       }
-      if (i <= NX - 2 && k <= NZ - 2) m |= 1u << (kMH + e);
-      if (i <= NX - 2 && k >= 1 && k <= NZ - 2) m |= 1u << (kMEX + e);
-      if (k <= NZ - 2 && i >= 1 && i <= NX - 2) m |= 1u << (kMEZ + e);
-      if (i == 0 || i == NX - 2 || k == 0 || k == NZ - 1) m |= 1u << (kMEXZ + e);
-      if (i == 0 || i == NX - 1 || k == 0 || k == NZ - 2) m |= 1u << (kMEZZ + e);
-      if (i <= NX - 2 && k <= NZ - 2 && (i == 0 || i == NX - 2 || k == 0 || k == NZ - 2)) m |= 1u << (kMHYZ + e);
-      if (k == a.io.sk && i == a.io.si) se = e;
+      unsigned mm = 0;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int i = i0 + e;
+        if (i >= NX) continue;
+        mm |= 1u << (kMCELL + e);
+        if (in_strip(i, NX, W)) {
+          xs = true;
+          const int q = k * (2 * W) + strip_idx(i, NX, W);
+          sMEzx[so + e] = a.mEzx[q];
+          sMHyx[so + e] = a.mHyx[q];
+        }
+        if (i <= NX - 2 && k <= NZ - 2) mm |= 1u << (kMH + e);
+        if (i <= NX - 2 && k >= 1 && k <= NZ - 2) mm |= 1u << (kMEX + e);
+        if (k <= NZ - 2 && i >= 1 && i <= NX - 2) mm |= 1u << (kMEZ + e);
+        if (i == 0 || i == NX - 2 || k == 0 || k == NZ - 1) mm |= 1u << (kMEXZ + e);
+        if (i == 0 || i == NX - 1 || k == 0 || k == NZ - 2) mm |= 1u << (kMEZZ + e);
+        if (i <= NX - 2 && k <= NZ - 2 && (i == 0 || i == NX - 2 || k == 0 || k == NZ - 2)) mm |= 1u << (kMHYZ + e);
+        if (k == a.io.sk && i == a.io.si) se = 4 * j + e;
+      }
+      m[j] = mm;
+      // all four cells updated, none on a Dirichlet plane
+      plain = plain && (mm & 0xffffffu) == 0x000fffu;
+      sEzCol[row * SX + tx] = ez[j].x;
+      if (left && tx == 0) ll_put1(ecol(0, 0, bx) + k, ez[j].x, 1u);
     }
-    // all four cells updated, none on a Dirichlet plane, in a strip or the source
-    fast = se < 0 && (m & 0xffffffu) == 0x000fffu && !xs && !zs;
-    sts4(sExRow + so, ex);
-    sEzCol[ty * SX + tx] = ez.x;
-    if (left && tx == 0) ll_put1(ecol(0, 0, bx) + k, ez.x, 1u);
-    if (up && ty == 0) ll_put4(erow(0, 0, bz) + i0, ex, 1u);
+    plain = plain && se < 0;  // ... nor the source
+    bool anyzs = false;
+#pragma unroll
+    for (int j = 0; j < RB; ++j) anyzs |= zs[j];
+    fast = plain && !xs && !anyzs;  // and none in a strip
+    sts4(sExRow + ty * TW + 4 * tx, ex[0]);
+    if (up && rbase == 0) ll_put4(erow(0, 0, bz) + i0, ex[0], 1u);
   }
   // receivers of this tile
   for (int q = tid; q < a.io.nrec; q += blockDim.x) {
@@ -305,7 +324,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
     }
   }
   if (xwarp) {  // edges of the tiles below and to the right for step 0
-    if (!fetch_edges(down ? erow(0, 0, bz + 1) + x0 : nullptr, sExRow + TZ * TW, down ? 4 * nc4 : 0,
+    if (!fetch_edges(down ? erow(0, 0, bz + 1) + x0 : nullptr, sExRow + TYT * TW, down ? 4 * nc4 : 0,
                      right ? ecol(0, 0, bx + 1) + z0 : nullptr, sEzCol + TXT, SX, right ? nzt : 0, 1u, ctl,
                      a.limit_ns) &&
         (tid & 31) == 0)
@@ -313,16 +332,18 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
   }
   __syncthreads();
   const int nloc = s_nrec;
-  unsigned recm = 0;  // own cells that are receivers
+  unsigned recm = 0;  // own cells that are receivers, bit 4 * row + element
   if (cell) {
     for (int q = 0; q < min(nloc, kResMaxLocalRec); ++q) {
-      const int c = s_rec[2 * q + 1];
-      if (c >= so && c < so + 4) recm |= 1u << (c - so);
+      const int c = s_rec[2 * q + 1], row = c / TW, col = c - row * TW;
+      if (row >= rbase && row < rbase + nrows && col >= 4 * tx && col < 4 * tx + 4)
+        recm |= 1u << (4 * (row - rbase) + col - 4 * tx);
     }
     if (nloc > kResMaxLocalRec) {
       for (int q = 0; q < a.io.nrec; ++q) {
-        const int i = a.io.rec[3 * q];
-        if (a.io.rec[3 * q + 2] == k && i >= i0 && i < i0 + 4) recm |= 1u << (i - i0);
+        const int i = a.io.rec[3 * q], kk = a.io.rec[3 * q + 2];
+        if (i >= i0 && i < i0 + 4 && kk >= z0 + rbase && kk < z0 + rbase + nrows)
+          recm |= 1u << (4 * (kk - z0 - rbase) + i - i0);
       }
     }
   }
@@ -337,63 +358,70 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
 
     // ================= H half-step (electromagfdtd.f95:249-262)
     if (cell) {
-      const float4 exn = lds4(sExRow + so + TW);
-      const float ezn = sEzCol[ty * SX + tx + 1];
-      const float4 ikx4 = lds4(sIkx + 4 * tx);
-      float4 hv;
-      if (fast) {
+      const float4 exb = lds4(sExRow + (ty + 1) * TW + 4 * tx);
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const float dEx = el(exn, e) - el(ex, e);
-          const float dEz = (e < 3 ? el(ez, e + 1) : ezn) - el(ez, e);
-          el(hv, e) = el(hy, e) + dbH * (dEz * el(ikx4, e) + dEx * ikz);
-        }
-      } else {  // strip, bound or plane cells: two cells at a time, masks applied as selects
-        const bool hall = ((m >> kMH) & 15u) == 15u;
-        float adz = 0.0f, bzc = 0.0f;
-        if (zs) {
-          adz = __ldg(a.Z.ad + k);
-          bzc = __ldg(a.Z.b + k);
-        }
+      for (int j = 0; j < RB; ++j) {
+        if (j >= nrows) continue;
+        const int row = rbase + j, k = z0 + row, so = row * TW + 4 * tx;
+        float4 exn = exb;
+        if (j + 1 < RB && j + 1 < nrows) exn = ex[j + 1 < RB ? j + 1 : j];
+        const float ezn = sEzCol[row * SX + tx + 1];
+        float4 hv;
+        if (fast) {
 #pragma unroll
-        for (int hh = 0; hh < 2; ++hh) {
-          float2 pz = make_float2(0.f, 0.f), px = pz, adx = pz, bxx = pz;
-          if (zs) pz = lds2(sMExz + so + 2 * hh);
-          if (xs) {
-            px = lds2(sMEzx + so + 2 * hh);
-            adx = ld2(a.X.ad + i0 + 2 * hh);
-            bxx = ld2(a.X.b + i0 + 2 * hh);
+          for (int e = 0; e < 4; ++e) {
+            const float dEx = el(exn, e) - el(ex[j], e);
+            const float dEz = (e < 3 ? el(ez[j], e + 1) : ezn) - el(ez[j], e);
+            el(hv, e) = el(hy[j], e) + dbH * (dEz * el(ikx4, e) + dEx * ikz[j]);
+          }
+        } else {  // strip, bound or plane cells: two cells at a time, masks applied as selects
+          const unsigned mj = m[j];
+          const bool hall = ((mj >> kMH) & 15u) == 15u;
+          float adz = 0.0f, bzc = 0.0f;
+          if (zs[j]) {
+            adz = __ldg(a.Z.ad + k);
+            bzc = __ldg(a.Z.b + k);
           }
 #pragma unroll
-          for (int q = 0; q < 2; ++q) {
-            const int e = 2 * hh + q;
-            const bool on = hall || mbit(m, kMH, e);
-            const float dEx = el(exn, e) - el(ex, e);
-            float vz = dEx * ikz;
-            if (zs) {
-              const float p = bzc * el2(pz, q) + adz * dEx;
-              el2(pz, q) = on ? p : el2(pz, q);
-              vz += el2(pz, q);
-            }
-            const float dEz = (e < 3 ? el(ez, e + 1) : ezn) - el(ez, e);
-            float vx = dEz * el(ikx4, e);
+          for (int hh = 0; hh < 2; ++hh) {
+            float2 pz = make_float2(0.f, 0.f), px = pz, adx = pz, bxx = pz;
+            if (zs[j]) pz = lds2(sMExz + so + 2 * hh);
             if (xs) {
-              const float p = el2(bxx, q) * el2(px, q) + el2(adx, q) * dEz;
-              el2(px, q) = on ? p : el2(px, q);
-              vx += el2(px, q);
+              px = lds2(sMEzx + so + 2 * hh);
+              adx = ld2(a.X.ad + i0 + 2 * hh);
+              bxx = ld2(a.X.b + i0 + 2 * hh);
             }
-            const float h = el(hy, e) + dbH * (vx + vz);
-            el(hv, e) = on ? h : el(hy, e);
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+              const int e = 2 * hh + q;
+              const bool on = hall || mbit(mj, kMH, e);
+              const float dEx = el(exn, e) - el(ex[j], e);
+              float vz = dEx * ikz[j];
+              if (zs[j]) {
+                const float p = bzc * el2(pz, q) + adz * dEx;
+                el2(pz, q) = on ? p : el2(pz, q);
+                vz += el2(pz, q);
+              }
+              const float dEz = (e < 3 ? el(ez[j], e + 1) : ezn) - el(ez[j], e);
+              float vx = dEz * el(ikx4, e);
+              if (xs) {
+                const float p = el2(bxx, q) * el2(px, q) + el2(adx, q) * dEz;
+                el2(px, q) = on ? p : el2(px, q);
+                vx += el2(px, q);
+              }
+              const float h = el(hy[j], e) + dbH * (vx + vz);
+              el(hv, e) = on ? h : el(hy[j], e);
+            }
+            if (zs[j]) sts2(sMExz + so + 2 * hh, pz);
+            if (xs) sts2(sMEzx + so + 2 * hh, px);
           }
-          if (zs) sts2(sMExz + so + 2 * hh, pz);
-          if (xs) sts2(sMEzx + so + 2 * hh, px);
         }
+        hy[j] = hv;
+        sHyCol[row * SX + tx + 1] = hv.w;
+        if (right && tx == TXT - 1) ll_put1(ecol(par, 1, bx) + k, hv.w, tag);
+        if (j == RB - 1) sts4(sHyRow + (ty + 1) * TW + 4 * tx, hv);
+        if (down && row == nzt - 1) ll_put4(erow(par, 1, bz) + i0, hv, tag);
       }
-      hy = hv;
-      sts4(sHyRow + so + TW, hv);
-      sHyCol[ty * SX + tx + 1] = hv.w;
-      if (right && tx == TXT - 1) ll_put1(ecol(par, 1, bx) + k, hv.w, tag);
-      if (down && ty == nzt - 1) ll_put4(erow(par, 1, bz) + i0, hv, tag);
     } else if (xwarp) {  // Hy row above and column on the left for this step's E half
       if (!fetch_edges(up ? erow(par, 1, bz - 1) + x0 : nullptr, sHyRow, up ? 4 * nc4 : 0,
                        left ? ecol(par, 1, bx - 1) + z0 : nullptr, sHyCol, SX, left ? nzt : 0, tag, ctl,
@@ -409,110 +437,118 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
 
     // ================= E half-step, source, Dirichlet planes, norm (:273-321)
     if (cell) {
-      const float4 hm = lds4(sHyRow + so);
-      const float hl = sHyCol[ty * SX + tx];
-      const float4 h = hy;
-      if (fast) {
-        const float4 cax = lds4(sCAx + so), cbx = lds4(sCBx + so), caz = lds4(sCAz + so), cbz = lds4(sCBz + so);
-        const float4 ikxh4 = lds4(sIkxh + 4 * tx);
+      const float4 hmt = lds4(sHyRow + ty * TW + 4 * tx);
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const float dHz = el(h, e) - el(hm, e);
-          const float exv = el(cax, e) * el(ex, e) + el(cbx, e) * (dHz * ikzh);
-          const float dHx = el(h, e) - (e == 0 ? hl : el(h, e - 1));
-          const float ezv = el(caz, e) * el(ez, e) + el(cbz, e) * (dHx * el(ikxh4, e));
-          el(ex, e) = exv;
-          el(ez, e) = ezv;
-          nrm = fmaxf(nrm, norm_monitor(exv, ezv));
-        }
-      } else {  // strip, bound or plane cells: two cells at a time, masks applied as selects
-        const bool plain = se < 0 && (m & 0xffffffu) == 0x000fffu;
-        float adz = 0.0f, bzc = 0.0f;
-        if (zs) {
-          adz = __ldg(a.Z.adh + k);
-          bzc = __ldg(a.Z.bh + k);
-        }
+      for (int j = 0; j < RB; ++j) {
+        if (j >= nrows) continue;
+        const int row = rbase + j, k = z0 + row, so = row * TW + 4 * tx;
+        float4 hm = hmt;
+        if (j > 0) hm = hy[j > 0 ? j - 1 : 0];
+        const float hl = sHyCol[row * SX + tx];
+        const float4 h = hy[j];
+        if (fast) {
 #pragma unroll
-        for (int hh = 0; hh < 2; ++hh) {
-          const float2 cax = lds2(sCAx + so + 2 * hh), cbx = lds2(sCBx + so + 2 * hh);
-          const float2 caz = lds2(sCAz + so + 2 * hh), cbz = lds2(sCBz + so + 2 * hh);
-          const float2 ikxh = lds2(sIkxh + 4 * tx + 2 * hh);
-          float2 pz = make_float2(0.f, 0.f), px = pz, adx = pz, bxx = pz;
-          if (zs) pz = lds2(sMHyz + so + 2 * hh);
-          if (xs) {
-            px = lds2(sMHyx + so + 2 * hh);
-            adx = ld2(a.X.adh + i0 + 2 * hh);
-            bxx = ld2(a.X.bh + i0 + 2 * hh);
-          }
-#pragma unroll
-          for (int q = 0; q < 2; ++q) {
-            const int e = 2 * hh + q;
-            const bool upx = plain || mbit(m, kMEX, e), upz = plain || mbit(m, kMEZ, e);
+          for (int e = 0; e < 4; ++e) {
             const float dHz = el(h, e) - el(hm, e);
-            float d = dHz * ikzh;
-            if (zs) {
-              const float p = bzc * el2(pz, q) + adz * dHz;
-              el2(pz, q) = upx ? p : el2(pz, q);
-              d += el2(pz, q);
-            }
-            float exv = el2(cax, q) * el(ex, e) + el2(cbx, q) * d;
-            exv = upx ? exv : el(ex, e);
+            const float exv = el(cax[j], e) * el(ex[j], e) + el(cbx[j], e) * (dHz * ikzh[j]);
             const float dHx = el(h, e) - (e == 0 ? hl : el(h, e - 1));
-            float d2 = dHx * el2(ikxh, q);
-            if (xs) {
-              const float p = el2(bxx, q) * el2(px, q) + el2(adx, q) * dHx;
-              el2(px, q) = upz ? p : el2(px, q);
-              d2 += el2(px, q);
-            }
-            float ezv = el2(caz, q) * el(ez, e) + el2(cbz, q) * d2;
-            ezv = upz ? ezv : el(ez, e);
-            if (e == se) {  // :300-301
-              exv += a.io.src[t];
-              ezv += a.io.src[a.io.nstep + t];
-            }
-            if (!plain) {  // :304-312
-              if (mbit(m, kMEXZ, e)) exv = 0.0f;
-              if (mbit(m, kMEZZ, e)) ezv = 0.0f;
-            }
-            el(ex, e) = exv;
-            el(ez, e) = ezv;
-            if (plain || mbit(m, kMCELL, e)) nrm = fmaxf(nrm, norm_monitor(exv, ezv));
+            const float ezv = el(caz[j], e) * el(ez[j], e) + el(cbz[j], e) * (dHx * el(ikxh4, e));
+            el(ex[j], e) = exv;
+            el(ez[j], e) = ezv;
+            nrm = fmaxf(nrm, norm_monitor(exv, ezv));
           }
-          if (zs) sts2(sMHyz + so + 2 * hh, pz);
-          if (xs) sts2(sMHyx + so + 2 * hh, px);
+        } else {  // strip, bound or plane cells: two cells at a time, masks applied as selects
+          const unsigned mj = m[j];
+          const bool rowplain = (mj & 0xffffffu) == 0x000fffu;
+          float adz = 0.0f, bzc = 0.0f;
+          if (zs[j]) {
+            adz = __ldg(a.Z.adh + k);
+            bzc = __ldg(a.Z.bh + k);
+          }
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh) {
+            float2 pz = make_float2(0.f, 0.f), px = pz, adx = pz, bxx = pz;
+            if (zs[j]) pz = lds2(sMHyz + so + 2 * hh);
+            if (xs) {
+              px = lds2(sMHyx + so + 2 * hh);
+              adx = ld2(a.X.adh + i0 + 2 * hh);
+              bxx = ld2(a.X.bh + i0 + 2 * hh);
+            }
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+              const int e = 2 * hh + q;
+              const bool upx = rowplain || mbit(mj, kMEX, e), upz = rowplain || mbit(mj, kMEZ, e);
+              const float dHz = el(h, e) - el(hm, e);
+              float d = dHz * ikzh[j];
+              if (zs[j]) {
+                const float p = bzc * el2(pz, q) + adz * dHz;
+                el2(pz, q) = upx ? p : el2(pz, q);
+                d += el2(pz, q);
+              }
+              float exv = el(cax[j], e) * el(ex[j], e) + el(cbx[j], e) * d;
+              exv = upx ? exv : el(ex[j], e);
+              const float dHx = el(h, e) - (e == 0 ? hl : el(h, e - 1));
+              float d2 = dHx * el(ikxh4, e);
+              if (xs) {
+                const float p = el2(bxx, q) * el2(px, q) + el2(adx, q) * dHx;
+                el2(px, q) = upz ? p : el2(px, q);
+                d2 += el2(px, q);
+              }
+              float ezv = el(caz[j], e) * el(ez[j], e) + el(cbz[j], e) * d2;
+              ezv = upz ? ezv : el(ez[j], e);
+              if (4 * j + e == se) {  // :300-301
+                exv += a.io.src[t];
+                ezv += a.io.src[a.io.nstep + t];
+              }
+              if (!rowplain) {  // :304-312
+                if (mbit(mj, kMEXZ, e)) exv = 0.0f;
+                if (mbit(mj, kMEZZ, e)) ezv = 0.0f;
+              }
+              el(ex[j], e) = exv;
+              el(ez[j], e) = ezv;
+              if (rowplain || mbit(mj, kMCELL, e)) nrm = fmaxf(nrm, norm_monitor(exv, ezv));
+            }
+            if (zs[j]) sts2(sMHyz + so + 2 * hh, pz);
+            if (xs) sts2(sMHyx + so + 2 * hh, px);
+          }
         }
-        if (!plain && ((m >> kMHYZ) & 15u)) {  // the stored Hy keeps its Dirichlet planes at zero
+        sEzCol[row * SX + tx] = ez[j].x;
+        if (left && tx == 0) ll_put1(ecol(par ^ 1, 0, bx) + k, ez[j].x, tag + 1u);
+      }
+      sts4(sExRow + ty * TW + 4 * tx, ex[0]);
+      if (up && rbase == 0) ll_put4(erow(par ^ 1, 0, bz) + i0, ex[0], tag + 1u);
+      if (!plain) {  // the stored Hy keeps its Dirichlet planes at zero, after every row's E used it
+#pragma unroll
+        for (int j = 0; j < RB; ++j)
 #pragma unroll
           for (int e = 0; e < 4; ++e)
-            if (mbit(m, kMHYZ, e)) el(hy, e) = 0.0f;
-        }
+            if (mbit(m[j], kMHYZ, e)) el(hy[j], e) = 0.0f;
       }
-      sts4(sExRow + so, ex);
-      sEzCol[ty * SX + tx] = ez.x;
-      if (left && tx == 0) ll_put1(ecol(par ^ 1, 0, bx) + k, ez.x, tag + 1u);
-      if (up && ty == 0) ll_put4(erow(par ^ 1, 0, bz) + i0, ex, tag + 1u);
       if (recm) {  // receivers of step t
         float* tr = a.io.traces + (size_t)t * 2 * a.io.nrec;
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          if (!(recm & (1u << e))) continue;
-          if (nloc <= kResMaxLocalRec) {
-            for (int q = 0; q < nloc; ++q)
-              if (s_rec[2 * q + 1] == so + e) {
-                tr[s_rec[2 * q]] = el(ex, e);
-                tr[a.io.nrec + s_rec[2 * q]] = el(ez, e);
-              }
-          } else {
-            for (int q = 0; q < a.io.nrec; ++q)
-              if (a.io.rec[3 * q] == i0 + e && a.io.rec[3 * q + 2] == k) {
-                tr[q] = el(ex, e);
-                tr[a.io.nrec + q] = el(ez, e);
-              }
+        for (int j = 0; j < RB; ++j)
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            if (!(recm & (1u << (4 * j + e)))) continue;
+            const int c = (rbase + j) * TW + 4 * tx + e;
+            if (nloc <= kResMaxLocalRec) {
+              for (int q = 0; q < nloc; ++q)
+                if (s_rec[2 * q + 1] == c) {
+                  tr[s_rec[2 * q]] = el(ex[j], e);
+                  tr[a.io.nrec + s_rec[2 * q]] = el(ez[j], e);
+                }
+            } else {
+              for (int q = 0; q < a.io.nrec; ++q)
+                if (a.io.rec[3 * q] == i0 + e && a.io.rec[3 * q + 2] == z0 + rbase + j) {
+                  tr[q] = el(ex[j], e);
+                  tr[a.io.nrec + q] = el(ez[j], e);
+                }
+            }
           }
-        }
       }
     } else if (xwarp && s + 1 < a.nsteps) {  // Ex row below and Ez column to the right for step s+1
-      if (!fetch_edges(down ? erow(par ^ 1, 0, bz + 1) + x0 : nullptr, sExRow + TZ * TW, down ? 4 * nc4 : 0,
+      if (!fetch_edges(down ? erow(par ^ 1, 0, bz + 1) + x0 : nullptr, sExRow + TYT * TW, down ? 4 * nc4 : 0,
                        right ? ecol(par ^ 1, 0, bx + 1) + z0 : nullptr, sEzCol + TXT, SX, right ? nzt : 0, tag + 1u,
                        ctl, a.limit_ns) &&
           (tid & 31) == 0)
@@ -525,22 +561,27 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
 
   // ---- write the cells back
   if (cell) {
-    const int g = k * P + i0;
-    st4(a.Ex + g, ex);
-    st4(a.Ez + g, ez);
-    st4(a.Hy + g, hy);
-    if (zs) {
-      const int zrow = strip_idx(k, NZ, W) * P + i0;
-      st4(a.mExz + zrow, lds4(sMExz + so));
-      st4(a.mHyz + zrow, lds4(sMHyz + so));
-    }
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const int i = i0 + e;
-      if (i < NX && in_strip(i, NX, W)) {
-        const int mm = k * (2 * W) + strip_idx(i, NX, W);
-        a.mEzx[mm] = sMEzx[so + e];
-        a.mHyx[mm] = sMHyx[so + e];
+    for (int j = 0; j < RB; ++j) {
+      if (j >= nrows) continue;
+      const int row = rbase + j, k = z0 + row;
+      const int gg = k * P + i0, so = row * TW + 4 * tx;
+      st4(a.Ex + gg, ex[j]);
+      st4(a.Ez + gg, ez[j]);
+      st4(a.Hy + gg, hy[j]);
+      if (zs[j]) {
+        const int zrow = strip_idx(k, NZ, W) * P + i0;
+        st4(a.mExz + zrow, lds4(sMExz + so));
+        st4(a.mHyz + zrow, lds4(sMHyz + so));
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int i = i0 + e;
+        if (i < NX && in_strip(i, NX, W)) {
+          const int q = k * (2 * W) + strip_idx(i, NX, W);
+          a.mEzx[q] = sMEzx[so + e];
+          a.mHyx[q] = sMHyx[so + e];
+        }
       }
     }
   }
@@ -550,8 +591,8 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
 }  // namespace
 
 size_t em2_resident_smem(int TW, int TZ) {
-  const size_t SX = (size_t)TW / 4 + 1;
-  return sizeof(float) * (8 * (size_t)TZ * TW + 2 * ((size_t)TZ + 1) * TW + 2 * (size_t)TZ * SX + 2 * (size_t)TW);
+  const size_t SX = (size_t)TW / 4 + 1, TYT = ((size_t)TZ + kResRows - 1) / kResRows;
+  return sizeof(float) * (4 * (size_t)TZ * TW + 2 * (TYT + 1) * TW + 2 * (size_t)TZ * SX);
 }
 
 namespace {
@@ -605,7 +646,8 @@ bool em2_resident_plan(int NX, int NZ, int npml, int max_ctas, size_t max_smem, 
     for (int g = 0; g < ng; ++g) {
       const double cg = gcol[g] ? kGeneralCost * nr : gr * kGeneralCost + (nr - gr);
       const int ngp = g - g0 + 1;
-      const bool over = cost + cg + 1.0 + nr > C || ngp * nr > kResCellThreads ||
+      const int trows = (nr + kResRows - 1) / kResRows;
+      const bool over = cost + cg + 1.0 + nr > C || ngp * trows > kResCellThreads ||
                         4 * ngp + nr > 32 * kResFetchPerLane || em2_resident_smem(4 * ngp, nr) > max_smem;
       if (over && g > g0) {
         ++count;
@@ -614,7 +656,7 @@ bool em2_resident_plan(int NX, int NZ, int npml, int max_ctas, size_t max_smem, 
         cost = 0.0;
       }
       const int ngp1 = g - g0 + 1;
-      if (ngp1 * nr > kResCellThreads || 4 * ngp1 + nr > 32 * kResFetchPerLane ||
+      if (ngp1 * trows > kResCellThreads || 4 * ngp1 + nr > 32 * kResFetchPerLane ||
           em2_resident_smem(4 * ngp1, nr) > max_smem || cg + 1.0 + nr > C)
         return max_ctas + 1;  // one group alone does not fit
       cost += cg + 1.0;
