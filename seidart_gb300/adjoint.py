@@ -4,8 +4,12 @@
 Its forward pass runs the whole shot, saving the dynamic state every
 ``ckpt_every`` steps.  Its backward pass walks the checkpoints from the last
 to the first.  For each one it recomputes that segment's forward states on the
-device and runs the hand-written discrete adjoint kernels
-(``csrc/adjoint_em2.cu``) backwards over them.  ``sfd_adjoint_gradient`` then
+device and runs the hand-written discrete adjoint backwards over them: when
+the grid runs on chip, one launch recomputes the segment and writes every
+step's state (``csrc/resident2d.cu``) and one launch sweeps the adjoint over
+it with its state on chip (``csrc/resident_adj.cu``); otherwise one launch per
+step does each (``csrc/adjoint_em2.cu``).  ``flags`` are the solver's
+(``FLAG_STREAMING`` selects the per-step form).  ``sfd_adjoint_gradient`` then
 applies the FP64 chain rule from the update coefficients to the model planes.
 
 ``traces = TraceMisfit.apply(eps11, eps33, sigma, model)`` is differentiable
@@ -50,7 +54,7 @@ class TraceModel:
     """
 
     def __init__(self, grid: GridSpec, base_planes, profiles, src_ijk, srcfn, rec_ijk, ckpt_every=200,
-                 device="cuda"):
+                 device="cuda", flags=0):
         import torch
 
         self.grid = grid
@@ -59,7 +63,7 @@ class TraceModel:
         self.srcfn = np.asarray(srcfn, dtype=np.float64)
         self.nstep = self.srcfn.shape[1]
         self.ckpt_every = int(ckpt_every)
-        self.solver = FDTDSolver(grid, self.nstep, len(rec_ijk), device=device)
+        self.solver = FDTDSolver(grid, self.nstep, len(rec_ijk), device=device, flags=flags)
         self.solver.set_model(self.base)
         self.solver.set_cpml(profiles)
         self.solver.set_source(src_ijk, self.srcfn)

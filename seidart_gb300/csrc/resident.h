@@ -55,6 +55,20 @@ inline size_t res_scratch_bytes(int P, int NZ) {
   return sizeof(uint2) * 4 * kResMaxTiles1D * ((size_t)P + (size_t)res_nzp(NZ));
 }
 
+// Per-step copies of the state written by a recompute run for the adjoint:
+// the state after step t0 + s goes to base + (s + 1) * stride, its Ex, Ez,
+// Hy', A (psi dEx_dz, z-strip), B (psi dEz_dx, x-strip), C (psi dHy_dz,
+// z-strip) and D (psi dHy_dx, x-strip) at byte offsets off[0..6], in the
+// layout of the handle's own arrays.  Hy' is Hy after the step's H half,
+// i.e. the stored Hy before its Dirichlet planes are zeroed.  base ==
+// nullptr: no copies, and the final state is written back as usual.  With
+// copies the run leaves its input state untouched.
+struct ResDump {
+  char* base;
+  size_t stride;
+  size_t off[7];
+};
+
 struct Em2Resident {
   int NX, NZ, P, W;
   float *Ex, *Ez, *Hy;               // current copy: read before, written after the run
@@ -67,6 +81,35 @@ struct Em2Resident {
   ResScratch r;
   int t0, nsteps;
   unsigned long long limit_ns;  // longest wait for a neighbour before the run is abandoned
+  ResDump dump;
+};
+
+// On-chip adjoint sweep over one checkpoint segment: the transposed steps
+// t = s0 + nsteps - 1 down to s0, with the adjoint state in registers and
+// shared memory for the whole sweep and the same tiling and edge exchange
+// as the forward run.  The forward state before step s0 + s is read from
+// slots + s * stride (the ResDump layout, slot 0 = the checkpoint).
+struct Em2AdjResident {
+  int NX, NZ, P, W;
+  float *Lx, *Lz, *Lh, *LA, *LB, *LC, *LD;  // adjoint state: read before, written after the sweep
+  const float *CAx, *CBx, *CAz, *CBz;       // staggered-averaged update coefficients
+  AxisTab X, Z;
+  float dbH;
+  float *gCAx, *gCBx, *gCAz, *gCBz;  // dJ/d(coefficient) per cell: the sweep adds its sums
+  float* srcacc;                     // [2]: sum_t lam_E(source) * amplitude(t)
+  const float* srcfn;                // scaled source amplitudes [2][nstep]
+  int nstep, si, sk;
+  const int* rec;                    // [nrec][3]
+  int nrec;
+  const float* resid;                // dJ/d(trace) [nstep][2][nrec]
+  const char* slots;
+  size_t stride;
+  size_t off[7];
+  int s0, nsteps;
+  Ctl* ctl;
+  ResPlan plan;
+  ResScratch r;
+  unsigned long long limit_ns;
 };
 
 // Pick the tiling of an NX x NZ electromag2 grid with npml-cell strips for
@@ -78,5 +121,12 @@ size_t em2_resident_smem(int TW, int TZ);
 // CTAs of `smem` bytes fit on one SM.
 cudaError_t em2_resident_prepare(const ResPlan& plan, int* ctas_per_sm);
 cudaError_t em2_resident_launch(const Em2Resident& a, cudaStream_t s);
+
+// The adjoint sweep's dynamic shared memory for a TW x TZ tile; its set-up
+// for `plan` (the kernel's shared-memory limit, once per device; how many
+// CTAs fit on one SM, 0 when the largest tile does not fit); its launch.
+size_t em2_adj_resident_smem(int TW, int TZ);
+cudaError_t em2_adj_resident_prepare(const ResPlan& plan, int* ctas_per_sm);
+cudaError_t em2_adj_resident_launch(const Em2AdjResident& a, cudaStream_t s);
 
 }  // namespace sfd

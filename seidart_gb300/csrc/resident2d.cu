@@ -38,118 +38,15 @@
 #include <algorithm>
 #include <vector>
 
-#include "fused2d.cuh"
-#include "resident.h"
+#include "resident_common.cuh"
 
 namespace sfd {
 
+using namespace res;
+
 namespace {
 
-__device__ __forceinline__ unsigned long long res_timer_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ void ll_put4(uint2* p, float4 v, unsigned tag) {
-  asm volatile("st.volatile.global.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(p), "r"(__float_as_uint(v.x)), "r"(tag),
-               "r"(__float_as_uint(v.y)), "r"(tag));
-  asm volatile("st.volatile.global.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(p + 2), "r"(__float_as_uint(v.z)),
-               "r"(tag), "r"(__float_as_uint(v.w)), "r"(tag));
-}
-
-__device__ __forceinline__ void ll_put1(uint2* p, float v, unsigned tag) {
-  asm volatile("st.volatile.global.v2.u32 [%0], {%1, %2};" ::"l"(p), "r"(__float_as_uint(v)), "r"(tag));
-}
-
-__device__ __forceinline__ uint4 ld_vol4(const uint2* p) {
-  uint4 r;
-  asm volatile("ld.volatile.global.v4.u32 {%0, %1, %2, %3}, [%4];"
-               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
-               : "l"(p));
-  return r;
-}
-
-__device__ __forceinline__ uint2 ld_vol2(const uint2* p) {
-  uint2 r;
-  asm volatile("ld.volatile.global.v2.u32 {%0, %1}, [%2];" : "=r"(r.x), "=r"(r.y) : "l"(p));
-  return r;
-}
-
-// Called every few unsuccessful polls: false once the limit has passed or
-// any tile has given up.
-__device__ __noinline__ bool keep_polling(Ctl* ctl, unsigned long long limit_ns, unsigned long long& t0) {
-  const unsigned long long now = res_timer_ns();
-  if (t0 == 0) t0 = now;
-  if (*(volatile int*)&ctl->err) return false;
-  if (now - t0 > limit_ns) {
-    atomicExch(&ctl->err, 1);
-    return false;
-  }
-  return true;
-}
-
-// One warp: copy `nrow` row words (rsrc) into rdst[q] and `ncol` column words
-// (csrc) into cdst[c * cstride], each once its tag reads `tag`.  Each lane
-// issues the loads of all its pending words before testing any, so one round
-// trip to L2 serves them all.  At most 32 * kResFetchPerLane words.  False
-// (on every lane) if a wait gave up.
-constexpr int kResFetchPerLane = 8;
-__device__ __noinline__ bool fetch_edges(const uint2* rsrc, float* rdst, int nrow, const uint2* csrc, float* cdst, int cstride,
-                            int ncol, unsigned tag, Ctl* ctl, unsigned long long limit_ns) {
-  const int lane = threadIdx.x & 31;
-  const int n = nrow + ncol;
-  unsigned pending = 0;
-#pragma unroll
-  for (int k = 0; k < kResFetchPerLane; ++k)
-    if (lane + 32 * k < n) pending |= 1u << k;
-  bool ok = true;
-  unsigned long long t0 = 0;
-  uint2 v[kResFetchPerLane];
-  for (int it = 1; pending; ++it) {
-#pragma unroll
-    for (int k = 0; k < kResFetchPerLane; ++k) {
-      const int q = lane + 32 * k;
-      if (pending & (1u << k)) v[k] = ld_vol2(q < nrow ? rsrc + q : csrc + (q - nrow));
-    }
-#pragma unroll
-    for (int k = 0; k < kResFetchPerLane; ++k) {
-      const int q = lane + 32 * k;
-      if ((pending & (1u << k)) && v[k].y == tag) {
-        if (q < nrow) rdst[q] = __uint_as_float(v[k].x);
-        else cdst[(q - nrow) * cstride] = __uint_as_float(v[k].x);
-        pending &= ~(1u << k);
-      }
-    }
-    if (pending && (it & 7) == 0 && !keep_polling(ctl, limit_ns, t0)) {
-      ok = false;
-      break;
-    }
-  }
-  return __all_sync(0xffffffffu, ok);
-}
-
-__device__ __forceinline__ float4 lds4(const float* p) { return *reinterpret_cast<const float4*>(p); }
-__device__ __forceinline__ void sts4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
-__device__ __forceinline__ float2 lds2(const float* p) { return *reinterpret_cast<const float2*>(p); }
-__device__ __forceinline__ void sts2(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
-__device__ __forceinline__ float2 ld2(const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); }
-__device__ __forceinline__ float& el2(float2& v, int q) { return (&v.x)[q]; }
-__device__ __forceinline__ float el2(const float2& v, int q) { return (&v.x)[q]; }
-
-// Per-cell masks of a thread, four bits each (bit e = cell 4tx+e), fixed for
-// the run and packed in one word.
-enum : unsigned {
-  kMH = 0,     // Hy is updated (:249-262: i <= NX-2, k <= NZ-2)
-  kMEX = 4,    // Ex is updated (:273-283: i <= NX-2, 1 <= k <= NZ-2)
-  kMEZ = 8,    // Ez is updated (:285-295: 1 <= i <= NX-2, k <= NZ-2)
-  kMEXZ = 12,  // Ex is a Dirichlet plane (:304-312)
-  kMEZZ = 16,  // Ez is a Dirichlet plane
-  kMHYZ = 20,  // the stored Hy is a Dirichlet plane (:314-317)
-  kMCELL = 24  // i < NX
-};
-__device__ __forceinline__ bool mbit(unsigned m, unsigned field, int e) { return (m >> (field + e)) & 1u; }
-
+template <bool DUMP>
 __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __grid_constant__ Em2Resident a) {
   constexpr int RB = kResRows;
   extern __shared__ __align__(16) float smem[];
@@ -173,42 +70,16 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
   // plane or the source -- so each warp runs one update path instead of
   // several in turn.
   const int ngroups = TXT * TYT;
-  int g = -1;
-  {
-    __shared__ int s_cnt[kResThreads / 32][3];
-    __shared__ unsigned short s_map[kResCellThreads];
-    int cls = 3;
-    if (!xwarp && tid < ngroups) {
-      const int gi = x0 + 4 * (tid % TXT), gk0 = z0 + RB * (tid / TXT);
-      const int gk1 = min(gk0 + RB, z0 + nzt) - 1;
-      const bool edge = gi < 1 || gi + 3 > NX - 3 || gk0 < 1 || gk1 > NZ - 3 ||
-                        (a.io.sk >= gk0 && a.io.sk <= gk1 && a.io.si >= gi && a.io.si < gi + 4);
-      const bool strp = in_strip(gk0, NZ, W) || in_strip(gk1, NZ, W) || in_strip(gi, NX, W) || in_strip(gi + 3, NX, W);
-      cls = edge ? 2 : (strp ? 1 : 0);
-    }
-    const unsigned lane = tid & 31, warp = tid >> 5;
-    unsigned mine = 0;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const unsigned b = __ballot_sync(0xffffffffu, cls == c);
-      if (lane == 0) s_cnt[warp][c] = __popc(b);
-      if (cls == c) mine = __popc(b & ((1u << lane) - 1u));
-    }
-    __syncthreads();
-    if (tid == 0) {
-      int run = 0;
-      for (int c = 0; c < 3; ++c)
-        for (int w = 0; w < kResThreads / 32; ++w) {  // the warps of this CTA
-          const int n = s_cnt[w][c];
-          s_cnt[w][c] = run;
-          run += n;
-        }
-    }
-    __syncthreads();
-    if (cls < 3) s_map[s_cnt[warp][cls] + mine] = (unsigned short)tid;
-    __syncthreads();
-    if (!xwarp && tid < ngroups) g = s_map[tid];
+  int cls = 3;
+  if (!xwarp && tid < ngroups) {
+    const int gi = x0 + 4 * (tid % TXT), gk0 = z0 + RB * (tid / TXT);
+    const int gk1 = min(gk0 + RB, z0 + nzt) - 1;
+    const bool edge = gi < 1 || gi + 3 > NX - 3 || gk0 < 1 || gk1 > NZ - 3 ||
+                      (a.io.sk >= gk0 && a.io.sk <= gk1 && a.io.si >= gi && a.io.si < gi + 4);
+    const bool strp = in_strip(gk0, NZ, W) || in_strip(gk1, NZ, W) || in_strip(gi, NX, W) || in_strip(gi + 3, NX, W);
+    cls = edge ? 2 : (strp ? 1 : 0);
   }
+  const int g = class_ordered_group(cls);
   const int tx = g >= 0 ? g % TXT : 0, ty = g >= 0 ? g / TXT : 0;
   const int rbase = RB * ty;
   const int nrows = g >= 0 ? min(RB, nzt - rbase) : 0;
@@ -517,6 +388,34 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
       }
       sts4(sExRow + ty * TW + 4 * tx, ex[0]);
       if (up && rbase == 0) ll_put4(erow(par ^ 1, 0, bz) + i0, ex[0], tag + 1u);
+      if (DUMP) {  // the state after step t, each thread its own cells; Hy before its planes are zeroed
+        char* d = a.dump.base + (size_t)(s + 1) * a.dump.stride;
+#pragma unroll
+        for (int j = 0; j < RB; ++j) {
+          if (j >= nrows) continue;
+          const int row = rbase + j, k = z0 + row;
+          const int gg = k * P + i0, so = row * TW + 4 * tx;
+          st4((float*)(d + a.dump.off[0]) + gg, ex[j]);
+          st4((float*)(d + a.dump.off[1]) + gg, ez[j]);
+          st4((float*)(d + a.dump.off[2]) + gg, hy[j]);
+          if (zs[j]) {
+            const int zrow = strip_idx(k, NZ, W) * P + i0;
+            st4((float*)(d + a.dump.off[3]) + zrow, lds4(sMExz + so));
+            st4((float*)(d + a.dump.off[5]) + zrow, lds4(sMHyz + so));
+          }
+          if (xs) {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const int i = i0 + e;
+              if (i < NX && in_strip(i, NX, W)) {
+                const int q = k * (2 * W) + strip_idx(i, NX, W);
+                ((float*)(d + a.dump.off[4]))[q] = sMEzx[so + e];
+                ((float*)(d + a.dump.off[6]))[q] = sMHyx[so + e];
+              }
+            }
+          }
+        }
+      }
       if (!plain) {  // the stored Hy keeps its Dirichlet planes at zero, after every row's E used it
 #pragma unroll
         for (int j = 0; j < RB; ++j)
@@ -559,8 +458,8 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
   }
   if (!ok) return;  // the state is left as it was loaded; the host reports the timeout
 
-  // ---- write the cells back
-  if (cell) {
+  // ---- write the cells back (a recompute run for the adjoint keeps its input)
+  if (cell && !DUMP) {
 #pragma unroll
     for (int j = 0; j < RB; ++j) {
       if (j >= nrows) continue;
@@ -711,15 +610,23 @@ bool em2_resident_plan(int NX, int NZ, int npml, int max_ctas, size_t max_smem, 
 }
 
 cudaError_t em2_resident_prepare(const ResPlan& plan, int* ctas_per_sm) {
-  cudaError_t e = cudaFuncSetAttribute(em2_resident_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem);
+  cudaError_t e = cudaFuncSetAttribute(em2_resident_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)plan.smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(em2_resident_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, em2_resident_kernel, kResThreads, plan.smem);
+  int n0 = 0, n1 = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n0, em2_resident_kernel<false>, kResThreads, plan.smem);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, em2_resident_kernel<true>, kResThreads, plan.smem);
+  *ctas_per_sm = std::min(n0, n1);
+  return e;
 }
 
 cudaError_t em2_resident_launch(const Em2Resident& a, cudaStream_t s) {
   void* args[] = {(void*)&a};
-  return cudaLaunchCooperativeKernel((const void*)em2_resident_kernel, dim3(a.plan.ntiles),
-                                     dim3(kResThreads), args, a.plan.smem, s);
+  const void* fn = a.dump.base ? (const void*)em2_resident_kernel<true> : (const void*)em2_resident_kernel<false>;
+  return cudaLaunchCooperativeKernel(fn, dim3(a.plan.ntiles), dim3(kResThreads), args, a.plan.smem, s);
 }
 
 }  // namespace sfd

@@ -258,6 +258,7 @@ struct sfd_handle_s {
   int adj_seg = 0;
   int adj_cur = 0;
   const float* adj_resid = nullptr;
+  int adj_res_state = 0;  // on-chip adjoint sweeps: 0 not yet checked, 1 usable, -1 not usable
   Em2Args em2;
   Seis2Args s2;
   Seis25Args s25;
@@ -504,6 +505,7 @@ Em2Resident resident_args(const sfd_handle* h, int64_t nsteps) {
   r.t0 = (int)h->step;
   r.nsteps = (int)nsteps;
   r.limit_ns = 2000000000ull;
+  r.dump = ResDump{nullptr, 0, {0, 0, 0, 0, 0, 0, 0}};
   return r;
 }
 
@@ -1260,6 +1262,21 @@ AdjState adj_state_at(const AdjLayout& A, char* base) {
   return S;
 }
 
+// Whether the adjoint sweeps of this handle run on chip: its forward runs
+// do, and the sweep's larger per-tile shared memory fits too.
+bool adjoint_on_chip(sfd_handle* h) {
+  if (h->adj_res_state) return h->adj_res_state > 0;
+  h->adj_res_state = -1;
+  if (!resident_usable(h)) return false;
+  int per_sm = 0;
+  if (em2_adj_resident_prepare(h->res_plan, &per_sm) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    return false;
+  }
+  h->adj_res_state = 1;
+  return true;
+}
+
 int adj_check(const sfd_handle* h) {
   if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
   if (h->cfg.kind != SFD_ELECTROMAG2 || !h->single)
@@ -1335,6 +1352,7 @@ int32_t sfd_adjoint_begin(sfd_handle* h, void* dev_work, size_t bytes, int32_t s
   h->adj_cur = 0;
   h->adj_resid = dev_resid;
   CK(cudaMemsetAsync(h->adj, 0, A.slots, h->stream));  // adjoint states, gradients, accumulators
+  CK(cudaMemsetAsync(&((Ctl*)(h->base + h->L.off_ctl))->err, 0, sizeof(int), h->stream));
   return SFD_OK;
 }
 
@@ -1359,6 +1377,49 @@ int32_t sfd_adjoint_segment(sfd_handle* h, int64_t nsteps) {
   CK(cudaMemcpyAsync(S0.B, h->m(1), sizeof(float) * L.mem_sz[1], cudaMemcpyDeviceToDevice, h->stream));
   CK(cudaMemcpyAsync(S0.C, h->m(2), sizeof(float) * L.mem_sz[2], cudaMemcpyDeviceToDevice, h->stream));
   CK(cudaMemcpyAsync(S0.D, h->m(3), sizeof(float) * L.mem_sz[3], cudaMemcpyDeviceToDevice, h->stream));
+  if (adjoint_on_chip(h)) {
+    // forward recompute on chip: slot s + 1 <- the state after step s0 + s
+    Em2Resident fr = resident_args(h, nsteps);
+    fr.Ex = S0.Ex; fr.Ez = S0.Ez; fr.Hy = S0.Hy;
+    fr.mExz = S0.A; fr.mEzx = S0.B; fr.mHyz = S0.C; fr.mHyx = S0.D;
+    fr.t0 = (int)s0;
+    fr.io.nrec = 0;
+    fr.dump.base = h->adj + A.slots;
+    fr.dump.stride = A.state;
+    const size_t F = A.field, ZS = A.zstrip, XS = A.xstrip;
+    const size_t off[7] = {0, F, 2 * F, 3 * F, 3 * F + 2 * ZS, 3 * F + ZS, 3 * F + 2 * ZS + XS};  // Ex Ez Hy A B C D
+    for (int q = 0; q < 7; ++q) fr.dump.off[q] = off[q];
+    const size_t rb = res_scratch_bytes(L.P, L.NZ);
+    CK(cudaMemsetAsync(h->base + L.off_res, 0, rb, h->stream));
+    CK(em2_resident_launch(fr, h->stream));
+    // adjoint sweep on chip, in place on the current adjoint state
+    const AdjState Lc = adj_state_at(A, h->adj + A.lam[h->adj_cur]);
+    const Em2Args& e = h->em2;
+    Em2AdjResident ar;
+    ar.NX = NX; ar.NZ = NZ; ar.P = L.P; ar.W = L.W;
+    ar.Lx = Lc.Ex; ar.Lz = Lc.Ez; ar.Lh = Lc.Hy; ar.LA = Lc.A; ar.LB = Lc.B; ar.LC = Lc.C; ar.LD = Lc.D;
+    ar.CAx = e.CAx; ar.CBx = e.CBx; ar.CAz = e.CAz; ar.CBz = e.CBz;
+    ar.X = e.X; ar.Z = e.Z; ar.dbH = e.dbH;
+    ar.gCAx = (float*)(h->adj + A.g[0]); ar.gCBx = (float*)(h->adj + A.g[1]);
+    ar.gCAz = (float*)(h->adj + A.g[2]); ar.gCBz = (float*)(h->adj + A.g[3]);
+    ar.srcacc = (float*)(h->adj + A.acc);
+    ar.srcfn = (const float*)(h->base + L.off_src);
+    ar.nstep = h->cfg.nstep; ar.si = e.io.si; ar.sk = e.io.sk;
+    ar.rec = (const int*)(h->base + L.off_rec); ar.nrec = h->cfg.nrec; ar.resid = h->adj_resid;
+    ar.slots = h->adj + A.slots;
+    ar.stride = A.state;
+    for (int q = 0; q < 7; ++q) ar.off[q] = off[q];
+    ar.s0 = (int)s0;
+    ar.nsteps = (int)nsteps;
+    ar.ctl = (Ctl*)(h->base + L.off_ctl);
+    ar.plan = h->res_plan;
+    ar.r = fr.r;
+    ar.limit_ns = fr.limit_ns;
+    CK(cudaMemsetAsync(h->base + L.off_res, 0, rb, h->stream));
+    CK(em2_adj_resident_launch(ar, h->stream));
+    CK(cudaGetLastError());
+    return SFD_OK;
+  }
   // forward recompute: slot s -> slot s+1
   k_begin<<<std::min(1024, (L.nslots + 255) / 256 + 1), 256, 0, h->stream>>>((Ctl*)(h->base + L.off_ctl),
                                                                             (float*)(h->base + L.off_slots), L.nslots, (int)s0);
@@ -1411,7 +1472,10 @@ int32_t sfd_adjoint_gradient(sfd_handle* h, double* out, int64_t count) {
   }
   float acc[2];
   CK(cudaMemcpyAsync(acc, h->adj + A.acc, sizeof acc, cudaMemcpyDeviceToHost, h->stream));
+  Ctl ctl;
+  CK(cudaMemcpyAsync(&ctl, h->base + h->L.off_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
+  if (ctl.err) return fail(SFD_ERR_TIMEOUT, "on-chip adjoint sweep: a neighbouring tile did not answer within 2 s");
   const double dt = h->cfg.dt;
   const double *e11 = h->model.data(), *e13 = e11 + N2, *e33 = e11 + 2 * N2;
   const double *s11 = e11 + 3 * N2, *s13 = e11 + 4 * N2, *s33 = e11 + 5 * N2;
