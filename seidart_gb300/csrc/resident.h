@@ -122,11 +122,12 @@ size_t em2_resident_smem(int TW, int TZ);
 cudaError_t em2_resident_prepare(const ResPlan& plan, int* ctas_per_sm);
 cudaError_t em2_resident_launch(const Em2Resident& a, cudaStream_t s);
 
-// The adjoint sweep's dynamic shared memory for a TW x TZ tile; its set-up
-// for `plan` (the kernel's shared-memory limit, once per device; how many
-// CTAs fit on one SM, 0 when the largest tile does not fit); its launch.
-size_t em2_adj_resident_smem(int TW, int TZ);
-cudaError_t em2_adj_resident_prepare(const ResPlan& plan, int* ctas_per_sm);
+// The adjoint sweep's dynamic shared memory for the largest tile of `plan`
+// on an NX x NZ grid with W-cell strips; its set-up for `plan` (the kernel's
+// shared-memory limit, once per device; how many CTAs fit on one SM, 0 when
+// the largest tile does not fit); its launch.
+size_t em2_adj_resident_smem(const ResPlan& plan, int NX, int NZ, int W);
+cudaError_t em2_adj_resident_prepare(const ResPlan& plan, int NX, int NZ, int W, int* ctas_per_sm);
 cudaError_t em2_adj_resident_launch(const Em2AdjResident& a, cudaStream_t s);
 
 }  // namespace sfd

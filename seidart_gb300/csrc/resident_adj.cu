@@ -60,6 +60,22 @@ __device__ __forceinline__ const float* slot_f(const Em2AdjResident& a, int s, i
   return (const float*)(a.slots + (size_t)s * a.stride + a.off[q]);
 }
 
+// Whether the group of four columns from i holds a cell of the x-strip.
+__host__ __device__ inline bool strip_group(int i, int NX, int W) { return i < W || i + 3 >= NX - W; }
+
+// Rows of a tile (columns [x0, x0 + TW), rows [z0, z0 + TZ)) in the z-strip
+// and its groups of four columns holding x-strip cells.
+__host__ __device__ inline void adj_tile_strips(int x0, int TW, int z0, int TZ, int NX, int NZ, int W, int* nzr,
+                                                int* nxg) {
+  auto imax = [](int u, int v) { return u > v ? u : v; };
+  auto imin = [](int u, int v) { return u < v ? u : v; };
+  const int z1 = z0 + TZ, zbot = imax(z0, imax(W, NZ - W));
+  *nzr = imax(0, imin(W, z1) - z0) + imax(0, z1 - zbot);
+  int n = 0;
+  for (int q = 0; 4 * q < TW; ++q) n += strip_group(x0 + 4 * q, NX, W) ? 1 : 0;
+  *nxg = n;
+}
+
 __device__ __forceinline__ bool hy_plane(int i, int k, int NX, int NZ) {
   return i == 0 || i == NX - 2 || k == 0 || k == NZ - 2;
 }
@@ -101,21 +117,33 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
   float* sCBx = sCAx + CS;
   float* sCAz = sCBx + CS;
   float* sCBz = sCAz + CS;
-  float* sLA = sCBz + CS;  // adjoint memory variables (strip cells only)
-  float* sLB = sLA + CS;
-  float* sLC = sLB + CS;
-  float* sLD = sLC + CS;
-  float* sGAx = sLD + CS;  // gradient sums of the sweep
+  float* sGAx = sCBz + CS;  // gradient sums of the sweep
   float* sGBx = sGAx + CS;
   float* sGAz = sGBx + CS;
   float* sGBz = sGAz + CS;
-  float* sGxRow = sGBz + CS;                // [TYT+1][TW]: gx of the first row of thread row ty; row TYT = tile below
+  // adjoint memory variables of the tile's strip cells only: lam_A, lam_C of
+  // its nzr z-strip rows ([nzr][TW]), lam_B, lam_D of its nxg x-strip
+  // groups ([TZ][4 nxg])
+  int nzr, nxg;
+  adj_tile_strips(x0, TW, z0, TZ, NX, NZ, W, &nzr, &nxg);
+  const int XS = 4 * nxg;
+  float* sLA = sGBz + CS;
+  float* sLC = sLA + nzr * TW;
+  float* sLB = sLC + nzr * TW;
+  float* sLD = sLB + TZ * XS;
+  float* sGxRow = sLD + TZ * XS;            // [TYT+1][TW]: gx of the first row of thread row ty; row TYT = tile below
   float* sHaRow = sGxRow + (TYT + 1) * TW;  // [TYT+1][TW]: row ty+1 = hA of the last row of thread row ty; row 0 = tile above
   float* sXt = sHaRow + (TYT + 1) * TW;     // [kNT][TW]
   float* sZt = sXt + kNT * TW;              // [kNT][TZ]
   float* sGzCol = sZt + kNT * TZ;           // [TZ][SX]: gz of the first column of thread column tx; column TXT = tile right
   float* sHbCol = sGzCol + TZ * SX;         // [TZ][SX]: column tx+1 = hB of the last column of tx; column 0 = tile left
-  const int nsm = 12 * CS + 2 * (TYT + 1) * TW + kNT * TW + kNT * TZ + 2 * TZ * SX;
+  const int nsm = 8 * CS + 2 * nzr * TW + 2 * TZ * XS + 2 * (TYT + 1) * TW + kNT * TW + kNT * TZ + 2 * TZ * SX;
+  // offsets of a row of this thread's cells in the z-strip and x-strip arrays
+  const int zbot = max(z0, max(W, NZ - W)), ntop = max(0, min(W, z0 + TZ) - z0);
+  int xgi = 0;  // x-strip groups left of this thread's group
+  for (int q = 0; q < tx; ++q) xgi += strip_group(x0 + 4 * q, NX, W) ? 1 : 0;
+  auto zoff = [&](int row) { return (z0 + row < W ? row : ntop + z0 + row - zbot) * TW + 4 * tx; };
+  auto xoff = [&](int row) { return row * XS + 4 * xgi; };
   const int NZp = a.r.NZp;
   auto erow = [&](int par, int f, int b) { return a.r.erow + (size_t)((par * 2 + f) * kResMaxTiles1D + b) * P; };
   auto ecol = [&](int par, int f, int b) { return a.r.ecol + (size_t)((par * 2 + f) * kResMaxTiles1D + b) * NZp; };
@@ -186,8 +214,8 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
       if (in_strip(k, NZ, W)) {
         zsb |= 1u << j;
         const int zrow = strip_idx(k, NZ, W) * P + i0;
-        sts4(sLA + so, ld4(a.LA + zrow));
-        sts4(sLC + so, ld4(a.LC + zrow));
+        sts4(sLA + zoff(row), ld4(a.LA + zrow));
+        sts4(sLC + zoff(row), ld4(a.LC + zrow));
       }
       unsigned mm = 0;
 #pragma unroll
@@ -199,8 +227,8 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
           xs = true;
           mm |= 1u << (kAXS + e);
           const int q = k * (2 * W) + strip_idx(i, NX, W);
-          sLB[so + e] = a.LB[q];
-          sLD[so + e] = a.LD[q];
+          sLB[xoff(row) + e] = a.LB[q];
+          sLD[xoff(row) + e] = a.LD[q];
         }
         if (i <= NX - 2 && k >= 1 && k <= NZ - 2) mm |= 1u << (kAEX + e);
         if (k <= NZ - 2 && i >= 1 && i <= NX - 2) mm |= 1u << (kAEZ + e);
@@ -289,7 +317,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
     float4 lc = zero4;
     float adh = 0.0f;
     if (zs) {
-      lc = lds4(sLC + so);
+      lc = lds4(sLC + zoff(row));
       adh = sZt[kTADH * TZ + row];
     }
 #pragma unroll
@@ -308,7 +336,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
     const int so = (rbase + j) * TW + 4 * tx;
     const float lez = mbit(m[j], kAZE, e) ? 0.0f : el(lz[j], e);
     float v = sCBz[so + e] * lez * sXt[kTKH * TW + 4 * tx + e];
-    if (mbit(m[j], kAXS, e)) v += sLD[so + e] * sXt[kTADH * TW + 4 * tx + e];
+    if (mbit(m[j], kAXS, e)) v += sLD[xoff(rbase + j) + e] * sXt[kTADH * TW + 4 * tx + e];
     return v;
   };
   // the first row's gx and every row's first gz, to the neighbours inside
@@ -466,7 +494,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
           float4 lc = zero4, s1c = zero4;
           float bhz = 0.0f;
           if (zs) {
-            lc = lds4(sLC + so);
+            lc = lds4(sLC + zoff(row));
             s1c = ld4(slot_f(a, s + 1, 5) + (size_t)strip_idx(k, NZ, W) * P + i0);
             bhz = sZt[kTBH * TZ + row];
           }
@@ -492,7 +520,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
           }
           sts4(sGAx + so, gax);
           sts4(sGBx + so, gbx);
-          if (zs) sts4(sLC + so, lc);
+          if (zs) sts4(sLC + zoff(row), lc);
         }
         // Ez: gradients and lam_D
         {
@@ -501,7 +529,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
           const float4 ikhx = lds4(sXt + kTIKH * TW + 4 * tx);
           float4 ld = zero4, s1d = zero4, bhx = zero4;
           if (xs) {
-            ld = lds4(sLD + so);
+            ld = lds4(sLD + xoff(row));
             bhx = lds4(sXt + kTBH * TW + 4 * tx);
             const float* S1D = slot_f(a, s + 1, 6) + (size_t)k * (2 * W);
 #pragma unroll
@@ -527,7 +555,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
           }
           sts4(sGAz + so, gaz);
           sts4(sGBz + so, gbz);
-          if (xs) sts4(sLD + so, ld);
+          if (xs) sts4(sLD + xoff(row), ld);
         }
         // hA of the last row and hB of the last column, for phase B of the neighbours
         {
@@ -535,7 +563,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
           float4 la = zero4;
           float adz = 0.0f;
           if (zs) {
-            la = lds4(sLA + so);
+            la = lds4(sLA + zoff(row));
             adz = sZt[kTAD * TZ + row];
           }
           if (j == RB - 1 || (down && row == nzt - 1)) {
@@ -550,7 +578,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
           float hb3 = 0.0f;
           if (mbit(mj, kAH, 3)) {
             hb3 = dbH * th.w * sXt[kTK * TW + 4 * tx + 3];
-            if (mbit(mj, kAXS, 3)) hb3 += sLB[so + 3] * sXt[kTAD * TW + 4 * tx + 3];
+            if (mbit(mj, kAXS, 3)) hb3 += sLB[xoff(row) + 3] * sXt[kTAD * TW + 4 * tx + 3];
           }
           sHbCol[row * SX + tx + 1] = hb3;
           if (right && tx == TXT - 1) ll_put1(ecol(par, 1, bx) + k, hb3, tag);
@@ -578,10 +606,16 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
 #pragma unroll
         for (int j = 0; j < RB; ++j) {
           if (j >= nrows) continue;
-          const int gg = (z0 + rbase + j) * P + i0;
+          const int k = z0 + rbase + j, gg = k * P + i0;
           prefetch_l2(nEx + gg);
           prefetch_l2(nEz + gg);
           prefetch_l2(nHy + gg);
+          if ((zsb >> j) & 1u) prefetch_l2(slot_f(a, s, 5) + strip_idx(k, NZ, W) * P + i0);
+          if (xs) {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+              if (mbit(m[j], kAXS, e)) prefetch_l2(slot_f(a, s, 6) + k * (2 * W) + strip_idx(i0 + e, NX, W));
+          }
         }
       }
       float4 hAm = lds4(sHaRow + ty * TW + 4 * tx);
@@ -612,7 +646,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
 #pragma unroll
         for (int j = 0; j < RB; ++j) {
           if (j >= nrows) continue;
-          const int row = rbase + j, so = row * TW + 4 * tx;
+          const int row = rbase + j;
           const unsigned mj = m[j];
           const bool zs = (zsb >> j) & 1u;
           const float4 th = lh[j];
@@ -620,7 +654,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
           float4 la = zero4;
           float adz = 0.0f, bzz = 0.0f;
           if (zs) {
-            la = lds4(sLA + so);
+            la = lds4(sLA + zoff(row));
             adz = sZt[kTAD * TZ + row];
             bzz = sZt[kTB * TZ + row];
           }
@@ -630,7 +664,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
             if (mbit(mj, kAH, e)) el(ha, e) = dbH * el(th, e) * kz + (zs ? el(la, e) * adz : 0.0f);
           float4 lb = zero4, adx = zero4, bxx = zero4;
           if (xs) {
-            lb = lds4(sLB + so);
+            lb = lds4(sLB + xoff(row));
             adx = lds4(sXt + kTAD * TW + 4 * tx);
             bxx = lds4(sXt + kTB * TW + 4 * tx);
           }
@@ -654,8 +688,8 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
             if (hr && mbit(mj, kAXS, e)) el(lb, e) = el(bxx, e) * (dbH * el(th, e) + el(lb, e));
             if (hr && zs) el(la, e) = bzz * (dbH * el(th, e) + el(la, e));
           }
-          if (zs) sts4(sLA + so, la);
-          if (xs) sts4(sLB + so, lb);
+          if (zs) sts4(sLA + zoff(row), la);
+          if (xs) sts4(sLB + xoff(row), lb);
           hAm = ha;
         }
       }
@@ -687,15 +721,15 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
       st4(a.Lh + gg, lh[j]);
       if ((zsb >> j) & 1u) {
         const int zrow = strip_idx(k, NZ, W) * P + i0;
-        st4(a.LA + zrow, lds4(sLA + so));
-        st4(a.LC + zrow, lds4(sLC + so));
+        st4(a.LA + zrow, lds4(sLA + zoff(row)));
+        st4(a.LC + zrow, lds4(sLC + zoff(row)));
       }
 #pragma unroll
       for (int e = 0; e < 4; ++e)
         if (mbit(m[j], kAXS, e)) {
           const int q = k * (2 * W) + strip_idx(i0 + e, NX, W);
-          a.LB[q] = sLB[so + e];
-          a.LD[q] = sLD[so + e];
+          a.LB[q] = sLB[xoff(row) + e];
+          a.LD[q] = sLD[xoff(row) + e];
         }
       float* gp[4] = {a.gCAx, a.gCBx, a.gCAz, a.gCBz};
       const float* gs[4] = {sGAx, sGBx, sGAz, sGBz};
@@ -717,27 +751,39 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
   }
 }
 
-size_t plan_smem(const ResPlan& plan) {
+}  // namespace
+
+size_t em2_adj_resident_smem(const ResPlan& plan, int NX, int NZ, int W) {
   size_t m = 0;
   for (int b = 0; b < plan.ntiles; ++b) {
     const int4 t = plan.tile[b];
-    const int TW = (((t.x >> 16) - (t.x & 0xffff)) + 3) & ~3, TZ = (t.y >> 16) - (t.y & 0xffff);
-    m = std::max(m, em2_adj_resident_smem(TW, TZ));
+    const int x0 = t.x & 0xffff, z0 = t.y & 0xffff;
+    const int TW = (((t.x >> 16) - x0) + 3) & ~3, TZ = (t.y >> 16) - z0;
+    int nzr, nxg;
+    adj_tile_strips(x0, TW, z0, TZ, NX, NZ, W, &nzr, &nxg);
+    const size_t SX = (size_t)TW / 4 + 1, TYT = ((size_t)TZ + kResRows - 1) / kResRows, CS = (size_t)TW * TZ;
+    m = std::max(m, sizeof(float) * (8 * CS + 2 * (size_t)nzr * TW + 8 * (size_t)TZ * nxg + 2 * (TYT + 1) * TW +
+                                     kNT * (size_t)TW + kNT * (size_t)TZ + 2 * (size_t)TZ * SX));
   }
   return m;
 }
 
-}  // namespace
-
-size_t em2_adj_resident_smem(int TW, int TZ) {
-  const size_t SX = (size_t)TW / 4 + 1, TYT = ((size_t)TZ + kResRows - 1) / kResRows, CS = (size_t)TW * TZ;
-  return sizeof(float) * (12 * CS + 2 * (TYT + 1) * TW + kNT * (size_t)TW + kNT * (size_t)TZ + 2 * (size_t)TZ * SX);
-}
-
-cudaError_t em2_adj_resident_prepare(const ResPlan& plan, int* ctas_per_sm) {
+cudaError_t em2_adj_resident_prepare(const ResPlan& plan, int NX, int NZ, int W, int* ctas_per_sm) {
   *ctas_per_sm = 0;
-  const size_t smem = plan_smem(plan);
+  const size_t smem = em2_adj_resident_smem(plan, NX, NZ, W);
   cudaError_t e = cudaFuncSetAttribute(em2_adj_resident_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  // ask for no more shared memory than the largest tile needs, so the rest of
+  // the SM's on-chip memory serves as L1 (it holds the kernel's register spills)
+  int dev = 0, per_sm = 0;
+  cudaFuncAttributes fa;
+  e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, em2_adj_resident_kernel);
+  if (e != cudaSuccess) return e;
+  const size_t need = smem + fa.sharedSizeBytes + 1024;  // the runtime reserves 1 KB per CTA
+  const int pct = (int)std::min<size_t>(100, (100 * need + per_sm - 1) / per_sm);
+  e = cudaFuncSetAttribute(em2_adj_resident_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, em2_adj_resident_kernel, kResThreads, smem);
 }
@@ -745,7 +791,7 @@ cudaError_t em2_adj_resident_prepare(const ResPlan& plan, int* ctas_per_sm) {
 cudaError_t em2_adj_resident_launch(const Em2AdjResident& a, cudaStream_t s) {
   void* args[] = {(void*)&a};
   return cudaLaunchCooperativeKernel((const void*)em2_adj_resident_kernel, dim3(a.plan.ntiles), dim3(kResThreads), args,
-                                     plan_smem(a.plan), s);
+                                     em2_adj_resident_smem(a.plan, a.NX, a.NZ, a.W), s);
 }
 
 }  // namespace sfd

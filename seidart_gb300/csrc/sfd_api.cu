@@ -1269,7 +1269,7 @@ bool adjoint_on_chip(sfd_handle* h) {
   h->adj_res_state = -1;
   if (!resident_usable(h)) return false;
   int per_sm = 0;
-  if (em2_adj_resident_prepare(h->res_plan, &per_sm) != cudaSuccess || per_sm < 1) {
+  if (em2_adj_resident_prepare(h->res_plan, h->cfg.nx, h->cfg.nz, h->L.W, &per_sm) != cudaSuccess || per_sm < 1) {
     cudaGetLastError();
     return false;
   }
