@@ -395,13 +395,14 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
           if (j >= nrows) continue;
           const int row = rbase + j, k = z0 + row;
           const int gg = k * P + i0, so = row * TW + 4 * tx;
-          st4((float*)(d + a.dump.off[0]) + gg, ex[j]);
-          st4((float*)(d + a.dump.off[1]) + gg, ez[j]);
-          st4((float*)(d + a.dump.off[2]) + gg, hy[j]);
+          // streaming stores: the copies are read back only after the run
+          __stcs(reinterpret_cast<float4*>((float*)(d + a.dump.off[0]) + gg), ex[j]);
+          __stcs(reinterpret_cast<float4*>((float*)(d + a.dump.off[1]) + gg), ez[j]);
+          __stcs(reinterpret_cast<float4*>((float*)(d + a.dump.off[2]) + gg), hy[j]);
           if (zs[j]) {
             const int zrow = strip_idx(k, NZ, W) * P + i0;
-            st4((float*)(d + a.dump.off[3]) + zrow, lds4(sMExz + so));
-            st4((float*)(d + a.dump.off[5]) + zrow, lds4(sMHyz + so));
+            __stcs(reinterpret_cast<float4*>((float*)(d + a.dump.off[3]) + zrow), lds4(sMExz + so));
+            __stcs(reinterpret_cast<float4*>((float*)(d + a.dump.off[5]) + zrow), lds4(sMHyz + so));
           }
           if (xs) {
 #pragma unroll

@@ -476,8 +476,24 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
         else gnext = lds4(sGxRow + (ty + 1) * TW + 4 * tx);
         float gz[5];
         gz[0] = sGzCol[row * SX + tx];
+        {
+          const float4 cbz = lds4(sCBz + so), khx = lds4(sXt + kTKH * TW + 4 * tx);
+          float4 ld = zero4, adhx = zero4;
+          if (xs) {
+            ld = lds4(sLD + xoff(row));
+            adhx = lds4(sXt + kTADH * TW + 4 * tx);
+          }
 #pragma unroll
-        for (int e = 1; e < 4; ++e) gz[e] = gz_cell(j, e);
+          for (int e = 1; e < 4; ++e) {
+            float v = 0.0f;
+            if (mbit(mj, kAEZ, e)) {
+              const float lez = mbit(mj, kAZE, e) ? 0.0f : el(lz[j], e);
+              v = el(cbz, e) * lez * el(khx, e);
+              if (mbit(mj, kAXS, e)) v += el(ld, e) * el(adhx, e);
+            }
+            gz[e] = v;
+          }
+        }
         gz[4] = sGzCol[row * SX + tx + 1];
         // Hy' of the row and of the cell on the left
         const float4 h1 = ld4(S1Hy + gg);
