@@ -234,9 +234,12 @@ int32_t sfd_checkpoint_load(sfd_handle* h, const void* dev_src, int64_t step);
  * steps, call sfd_adjoint_begin once, then for each checkpoint from the last
  * to the first: sfd_checkpoint_load(h, ckpt, step), sfd_adjoint_segment(h,
  * steps of that segment).  Each segment recomputes its forward states from
- * the checkpoint and runs the adjoint steps backwards over them.  The
- * workspace (sfd_adjoint_bytes) holds S+1 forward states.  No counterpart in
- * the reference (SeidarT has no adjoint). */
+ * the checkpoint and runs the adjoint steps backwards over them; on a handle
+ * whose runs are on chip (sfd_on_chip) both are one launch per segment.  The
+ * workspace (sfd_adjoint_bytes) holds S+1 forward states.  On chip, a
+ * neighbouring tile that does not answer within 2 s makes
+ * sfd_adjoint_gradient return SFD_ERR_TIMEOUT.  No counterpart in the
+ * reference (SeidarT has no adjoint). */
 int32_t sfd_adjoint_bytes(const sfd_handle* h, int32_t seg_steps, size_t* bytes);
 int32_t sfd_adjoint_begin(sfd_handle* h, void* dev_work, size_t bytes, int32_t seg_steps, const float* dev_resid);
 int32_t sfd_adjoint_segment(sfd_handle* h, int64_t nsteps);
