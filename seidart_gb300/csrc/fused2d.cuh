@@ -120,7 +120,38 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
     }
   };
 
+  // Tiles whose owned cells all lie off the CPML strips, off the Dirichlet
+  // planes and away from the source take a path without per-cell masks (the
+  // same operations the masked path performs on such cells); their halo row
+  // and column still take the general code.
+  const int lo = W > 1 ? W : 1;
+  const bool fast = x0 >= lo && x0 + 127 <= NX - 1 - lo && x0 + 127 <= NX - 3 && z0 >= lo &&
+                    z0 + 8 * ZB - 1 <= NZ - 1 - lo && z0 + 8 * ZB - 1 <= NZ - 3 &&
+                    !(a.io.si >= x0 && a.io.si < x0 + 128 && a.io.sk >= z0 && a.io.sk < z0 + 8 * ZB);
+
   // ---- H half-step on the owned rows
+  if (fast) {
+#pragma unroll
+    for (int r = 0; r < ZB; ++r) {
+      const int k = z0 + ty + 8 * r;
+      const int c0 = k * P + i0;
+      const float4 hy = ld4(a.Hy0 + c0), ex = ld4(a.Ex0 + c0), exn = ld4(a.Ex0 + c0 + P), ez = ld4(a.Ez0 + c0);
+      float ez_next = __shfl_down_sync(0xffffffffu, ez.x, 1);
+      if (tx == 31) ez_next = __ldg(a.Ez0 + c0 + 4);
+      const float ikz = __ldg(a.Z.ik + k);
+      float4 hv;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float dEx = el(exn, e) - el(ex, e);
+        const float vz = dEx * ikz;
+        const float dEz = (e < 3 ? el(ez, e + 1) : ez_next) - el(ez, e);
+        const float vx = dEz * el(ikx4, e);
+        el(hv, e) = el(hy, e) + a.dbH * (vx + vz);
+      }
+      st4(a.Hy1 + c0, hv);
+      *reinterpret_cast<float4*>(&sH[ty + 8 * r + 1][sx]) = hv;
+    }
+  } else {
 #pragma unroll
   for (int r = 0; r < ZB; ++r) {
     const int k = z0 + ty + 8 * r;  // uniform across the warp
@@ -148,6 +179,7 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
       *reinterpret_cast<float4*>(&sH[ty + 8 * r + 1][sx]) = hv;
     }
   }
+  }
   // ---- halo (not stored): warp 0 takes row z0-1, warp 1 column x0-1
   if (ty == 0) {
     if (z0 > 0) {
@@ -168,6 +200,32 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
   __syncthreads();
   // ---- E half-step, source, Dirichlet, norm on the owned rows
   float norm = 0.0f;
+  if (fast) {
+#pragma unroll
+    for (int r = 0; r < ZB; ++r) {
+      const int k = z0 + ty + 8 * r;
+      const int c0 = k * P + i0;
+      const int kk = ty + 8 * r + 1;
+      float4 ex = ld4(a.Ex0 + c0), ez = ld4(a.Ez0 + c0);
+      const float4 cax = ld4(a.CAx + c0), cbx = ld4(a.CBx + c0), caz = ld4(a.CAz + c0), cbz = ld4(a.CBz + c0);
+      const float4 h = *reinterpret_cast<const float4*>(&sH[kk][sx]);
+      const float4 hm = *reinterpret_cast<const float4*>(&sH[kk - 1][sx]);
+      const float hl = sH[kk][sx - 1];
+      const float ikzh = __ldg(a.Z.ikh + k);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float dHz = el(h, e) - el(hm, e);
+        const float exv = el(cax, e) * el(ex, e) + el(cbx, e) * (dHz * ikzh);
+        const float dHx = el(h, e) - (e == 0 ? hl : el(h, e > 0 ? e - 1 : 0));
+        const float ezv = el(caz, e) * el(ez, e) + el(cbz, e) * (dHx * el(ikxh4, e));
+        el(ex, e) = exv;
+        el(ez, e) = ezv;
+        norm = fmaxf(norm, norm_monitor(exv, ezv));
+      }
+      st4(a.Ex1 + c0, ex);
+      st4(a.Ez1 + c0, ez);
+    }
+  } else {
 #pragma unroll
   for (int r = 0; r < ZB; ++r) {
     const int k = z0 + ty + 8 * r;
@@ -223,6 +281,7 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
       st4(a.Ez1 + c0, ez);
       if (zs) st4(a.mHyz + zrow, pc1);
     }
+  }
   }
   block_norm_to_slot(norm, a.io.slots, by * gridx + bx);
 }
@@ -316,7 +375,50 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
   }
   const int x0 = bx * 32, z0 = by * (8 * ZB);
   const int i = x0 + tx;
+  // Tiles whose owned cells all lie off the CPML strips, off the Dirichlet
+  // planes and away from the source take a path without per-cell masks (the
+  // same operations the masked path performs on such cells); the halo ring
+  // still takes the general code.
+  const int lo = W > 1 ? W : 1;
+  const bool fast = x0 >= lo && x0 + 31 <= NX - 1 - lo && x0 + 31 <= NX - 2 && z0 >= lo &&
+                    z0 + 8 * ZB - 1 <= NZ - 1 - lo && z0 + 8 * ZB - 1 <= NZ - 2 &&
+                    !(a.io.si >= x0 && a.io.si < x0 + 32 && a.io.sk >= z0 && a.io.sk < z0 + 8 * ZB);
   // ---- stress half-step on owned cells (stored) ...
+  if (fast) {
+    const float ikx = __ldg(a.X.ik + i), ikxh = __ldg(a.X.ikh + i);
+#pragma unroll
+    for (int r = 0; r < ZB; ++r) {
+      const int k = z0 + ty + 8 * r;
+      const int c = k * P + i;
+      const float ikz = __ldg(a.Z.ik + k), ikzh = __ldg(a.Z.ikh + k);
+      const float vx0 = __ldg(a.vx0 + c), vz0 = __ldg(a.vz0 + c);
+      const float vxl = __ldg(a.vx0 + c - 1), vxr = __ldg(a.vx0 + c + 1);
+      const float vxu = __ldg(a.vx0 + c - P), vxd = __ldg(a.vx0 + c + P);
+      const float vzl = __ldg(a.vz0 + c - 1), vzr = __ldg(a.vz0 + c + 1);
+      const float vzu = __ldg(a.vz0 + c - P), vzd = __ldg(a.vz0 + c + P);
+      float sxx = __ldg(a.sxx0 + c), szz = __ldg(a.szz0 + c), sxz = __ldg(a.sxz0 + c);
+      {  // :247-283
+        const float dvx_dx = (vxr - vx0) * ikxh, dvz_dz = (vz0 - vzu) * ikz;
+        const float dvz_dx = (vzr - vz0) * ikx, dvx_dz = (vx0 - vxu) * ikzh;
+        const float A11 = __ldg(a.A11 + c), A13 = __ldg(a.A13 + c), A15 = __ldg(a.A15 + c);
+        const float A33 = __ldg(a.A33 + c), A35 = __ldg(a.A35 + c);
+        const float shear = dvz_dx + dvx_dz;
+        sxx = sxx + (A11 * dvx_dx + A13 * dvz_dz + A15 * shear);
+        szz = szz + (A13 * dvx_dx + A33 * dvz_dz + A35 * shear);
+      }
+      {  // :285-312
+        const float dvx_dx = (vx0 - vxl) * ikxh, dvz_dz = (vzd - vz0) * ikz;
+        const float dvz_dx = (vz0 - vzl) * ikx, dvx_dz = (vxd - vx0) * ikzh;
+        sxz = sxz + (__ldg(a.B15 + c) * dvx_dx + __ldg(a.B35 + c) * dvz_dz + __ldg(a.B55 + c) * (dvz_dx + dvx_dz));
+      }
+      a.sxx1[c] = sxx;
+      a.szz1[c] = szz;
+      a.sxz1[c] = sxz;
+      sS[0][ty + 8 * r + 1][tx + 1] = sxx;
+      sS[1][ty + 8 * r + 1][tx + 1] = szz;
+      sS[2][ty + 8 * r + 1][tx + 1] = sxz;
+    }
+  } else {
 #pragma unroll
   for (int r = 0; r < ZB; ++r) {
     const int k = z0 + ty + 8 * r;
@@ -341,6 +443,7 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
       sS[2][ty + 8 * r + 1][tx + 1] = s.sxz;
     }
   }
+  }
   // ... and on the halo ring (shared memory only): warps 0-3 take the top
   // row, bottom row, left column and right column, one cell per lane.
   if (ty < 4) {
@@ -361,6 +464,27 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
   __syncthreads();
   // ---- velocity half-step on owned cells (seismicfdtd.f95:317-379)
   float norm = 0.0f;
+  if (fast) {
+    const float ikx = __ldg(a.X.ik + i), ikxh = __ldg(a.X.ikh + i);
+#pragma unroll
+    for (int r = 0; r < ZB; ++r) {
+      const int k = z0 + ty + 8 * r;
+      const int c = k * P + i;
+      const int kk = ty + 8 * r + 1, ii = tx + 1;
+      const float v1 = (sS[0][kk][ii] - sS[0][kk][ii - 1]) * ikx, v2 = (sS[2][kk][ii] - sS[2][kk - 1][ii]) * __ldg(a.Z.ik + k);
+      const float w1 = (sS[2][kk][ii + 1] - sS[2][kk][ii]) * ikxh, w2 = (sS[1][kk + 1][ii] - sS[1][kk][ii]) * __ldg(a.Z.ikh + k);
+      float vx = __ldg(a.vx0 + c), vz = __ldg(a.vz0 + c);
+      if (a.atten) {
+        vx *= __ldg(a.gxp + c);
+        vz *= __ldg(a.gzp + c);
+      }
+      vx = vx + (v1 + v2) * __ldg(a.dtrx + c);
+      vz = vz + (w1 + w2) * __ldg(a.dtrz + c);
+      a.vx1[c] = vx;
+      a.vz1[c] = vz;
+      norm = fmaxf(norm, norm_monitor(vx, vz));
+    }
+  } else {
 #pragma unroll
   for (int r = 0; r < ZB; ++r) {
     const int k = z0 + ty + 8 * r;
@@ -421,6 +545,7 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
       a.vz1[c] = vz;
       norm = fmaxf(norm, norm_monitor(vx, vz));
     }
+  }
   }
   block_norm_to_slot(norm, a.io.slots, by * gridx + bx);
 }
