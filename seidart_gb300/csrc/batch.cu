@@ -60,81 +60,6 @@ __device__ bool grid_barrier(GridBarrier* bar, unsigned nblocks, unsigned long l
   return ok != 0;
 }
 
-__device__ __forceinline__ void prefetch_l1(const float* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
-
-// Rows [k0, k1] of columns [x0, x0 + bytes / 4) of one array into the SM's
-// L1, one 128-byte line per lane of the calling warp.
-__device__ __forceinline__ void prefetch_rows(const float* base, int P, int x0, unsigned bytes, int k0, int k1) {
-  const int lines = (int)(bytes >> 7), n = (k1 - k0 + 1) * lines;
-  for (int q = (int)threadIdx.x; q < n; q += 32) prefetch_l1(base + (size_t)(k0 + q / lines) * P + x0 + 32 * (q % lines));
-}
-
-// Start moving tile `tile` of step s (its fields and coefficients, halo rows
-// included) into the SM's L1 while the block works on the current tile, so
-// the tile's loads find their lines on the SM.  Warp w takes arrays w, w + 8, ...
-// Only addresses inside the arrays are touched: rows are clamped to the grid
-// and columns to the row pitch.
-template <int ZB>
-__device__ void prefetch_tile(const BatchModel* __restrict__ models, const BatchGroup* __restrict__ groups,
-                              int ngroups, int tile, int s) {
-  int g = 0;
-  while (g + 1 < ngroups && tile >= groups[g + 1].tile0) ++g;
-  const BatchGroup& gr = groups[g];
-  const int q = tile - gr.tile0;
-  const BatchModel& md = models[gr.first + q % gr.n];
-  const int lt = q / gr.n;
-  const int bx = lt % md.gx, by = lt / md.gx;
-  const int p = (md.cur + s) & 1;
-  const int w = threadIdx.y;
-  if (md.kind == SFD_BATCH_EM2) {
-    const Em2Step& a = md.em2[p];
-    const int x0 = bx * 128, z0 = by * (8 * ZB);
-    const int k0 = max(z0 - 1, 0), k1 = min(z0 + 8 * ZB, a.NZ - 1);
-    const unsigned bytes = 4u * (unsigned)min(128, a.P - x0);
-    const float* base = nullptr;
-    switch (w) {
-      case 0: base = a.Ex0; break;
-      case 1: base = a.Ez0; break;
-      case 2: base = a.Hy0; break;
-      case 3: base = a.CAx; break;
-      case 4: base = a.CBx; break;
-      case 5: base = a.CAz; break;
-      case 6: base = a.CBz; break;
-      default: break;
-    }
-    if (base) prefetch_rows(base, a.P, x0, bytes, k0, k1);
-  } else {
-    const Seis2Step& a = md.s2[p];
-    const int x0 = bx * 32, z0 = by * (8 * ZB);
-    const int k0 = max(z0 - 1, 0), k1 = min(z0 + 8 * ZB, a.NZ - 1);
-    const unsigned bytes = 4u * (unsigned)min(32, a.P - x0);
-    const int narr = a.atten ? 17 : 15;  // per-cell planes only (q3 is an axis table)
-    for (int v = w; v < narr; v += 8) {
-      const float* base;
-      switch (v) {
-        case 0: base = a.vx0; break;
-        case 1: base = a.vz0; break;
-        case 2: base = a.sxx0; break;
-        case 3: base = a.szz0; break;
-        case 4: base = a.sxz0; break;
-        case 5: base = a.A11; break;
-        case 6: base = a.A13; break;
-        case 7: base = a.A15; break;
-        case 8: base = a.A33; break;
-        case 9: base = a.A35; break;
-        case 10: base = a.B15; break;
-        case 11: base = a.B35; break;
-        case 12: base = a.B55; break;
-        case 13: base = a.dtrx; break;
-        case 14: base = a.dtrz; break;
-        case 15: base = a.gxp; break;
-        default: base = a.gzp; break;
-      }
-      prefetch_rows(base, a.P, x0, bytes, k0, k1);
-    }
-  }
-}
-
 template <int ZB>
 __global__ void __launch_bounds__(256, 3)
     batch_kernel(const BatchModel* __restrict__ models, const BatchGroup* __restrict__ groups, int ngroups,
@@ -146,7 +71,6 @@ __global__ void __launch_bounds__(256, 3)
   for (int s = 0; s < nsteps; ++s) {
     int g = 0;
     for (int tile = blockIdx.x; tile < total_tiles; tile += gridDim.x) {
-      if (tile + (int)gridDim.x < total_tiles) prefetch_tile<ZB>(models, groups, ngroups, tile + gridDim.x, s);
       while (g + 1 < ngroups && tile >= groups[g + 1].tile0) ++g;  // tiles ascend per block
       const BatchGroup& gr = groups[g];
       const int q = tile - gr.tile0;
