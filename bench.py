@@ -182,7 +182,7 @@ def bench_plain(case, device, flush, stream, peak, bytes_fn, steps, warmup):
             "kernel_frac": [round(b[h] / (t / 1e3) / 1e9 / peak, 4) for h, t in zip(("half1", "half2"), kt)]}
 
 
-def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000):
+def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000, tiling=None):
     """The batched survey: 64 electromag2 shots of the layered 1000x500 model (sources every 15
     cells) + 16 seeded seismic2 models of uneven size, 4000 steps, one persistent launch per run."""
     import torch
@@ -204,7 +204,11 @@ def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000):
         s.set_receivers(c.rec_ijk)
         solvers.append(s)
     b = Batch(solvers)
-    tune = autotune(b, steps=8, use_cache=False)
+    if tiling:  # a fixed (rows per thread, blocks per SM), e.g. for a profiler run
+        b.set_tiling(*tiling)
+        tune = {"tiling": tuple(tiling), "timings": {}}
+    else:
+        tune = autotune(b, steps=8, use_cache=False)
     nstep = cases[0].nstep
     b.reset()
     b.run(min(64, nstep))
@@ -241,13 +245,13 @@ def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000):
                    for c in cases)
     value = cells * nstep / (ms / 1e3) / 1e9
     achieved = step_bytes * nstep / (ms / 1e3) / 1e9
-    out = {"workload": "64 electromag2 shots 1040x540 + 16 seismic2 models (nx 200-1200, nz 100-600) x 4000 steps",
+    out = {"workload": f"64 electromag2 shots 1040x540 + 16 seismic2 models (nx 200-1200, nz 100-600) x {nstep} steps",
            "value": round(value, 3), "unit": METRIC, "ms_per_run": round(ms, 2), "cells": cells,
            "bytes_per_cell_update": round(step_bytes / cells, 2),
            "bytes_per_cell_update_unshared": round(unshared / cells, 2),
            "roofline": {"bound": "hbm", "kernel": "batch_kernel", "achieved": round(achieved, 1), "peak": peak,
                         "unit": "GB/s", "frac": round(achieved / peak, 4)},
-           "vs_plain_single_shot": round(value / plain_value, 3),
+           "vs_plain_single_shot": round(value / plain_value, 3) if plain_value else None,
            "tiling": {"rows_per_thread": tune["tiling"][0], "blocks_per_sm": tune["tiling"][1],
                       "candidates_ms_per_step": {k: round(v * 1e3, 4) for k, v in tune["timings"].items()}},
            "launches_per_run": 3}
@@ -257,14 +261,14 @@ def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000):
     return out
 
 
-def bench_adjoint(device, ckpt_every=200):
+def bench_adjoint(device, ckpt_every=200, nstep=6000):
     """Adjoint gradient on the layered electromag2 model (6000 steps, 100 receivers): misfit against
     the unperturbed model's traces, current model with six +-5% Gaussian blobs in eps11 and eps33
     (seed 6), checkpoints every 200 steps with recompute.  Reports backward / forward wall time."""
     import torch
     from seidart_gb300 import synthetic as sy
     from seidart_gb300.adjoint import TraceModel
-    case = sy.electromag2_layers(nstep=6000)
+    case = sy.electromag2_layers(nstep=nstep)
     base = case.planes
     rng = np.random.default_rng(6)
     nz, nx = base.shape[1:]
@@ -300,7 +304,7 @@ def bench_adjoint(device, ckpt_every=200):
     t_plain = time.perf_counter() - t0
     m.close()
     misfit = 0.5 * float((resid.double() ** 2).sum())
-    return {"workload": "electromag2 1040x540 x 6000 steps, gradient wrt eps11, eps33, sigma per cell",
+    return {"workload": f"electromag2 1040x540 x {nstep} steps, gradient wrt eps11, eps33, sigma per cell",
             "forward_s": round(t_plain, 4), "forward_with_checkpoints_s": round(t_fwd, 4),
             "adjoint_s": round(t_bwd, 4), "adjoint_over_forward": round(t_bwd / t_plain, 3),
             "checkpoints_every": ckpt_every, "misfit": misfit,
@@ -475,10 +479,11 @@ def run_ours(args):
             rec = bench_plain(sy.seismic25_ice(nstep=args.time_steps if args.time_steps != 6000 else 3000),
                               device, flush, stream, peak, seis25_bytes, args.steps, args.warmup)
         elif args.only == "batched":
-            rec = bench_batched(device, flush, stream, peak, 1.0, runs=args.steps,
-                                nstep=args.time_steps if args.time_steps != 6000 else 4000)
+            tiling = tuple(int(v) for v in args.batch_tiling.split("x")) if args.batch_tiling else None
+            rec = bench_batched(device, flush, stream, peak, None, runs=args.steps,
+                                nstep=args.time_steps if args.time_steps != 6000 else 4000, tiling=tiling)
         else:
-            rec = bench_adjoint(device)
+            rec = bench_adjoint(device, nstep=args.time_steps)
         print(json.dumps({"only": args.only, **rec}), flush=True)
         return 0
 
@@ -603,6 +608,8 @@ def main(argv=None):
     ap.add_argument("--only", choices=["seismic2", "seismic25", "batched", "adjoint"],
                     help="run one secondary leg alone and print its record (for profiler runs)")
     ap.add_argument("--skip-adjoint", action="store_true")
+    ap.add_argument("--batch-tiling", default=None,
+                    help="with --only batched: fixed rows-per-thread x blocks-per-SM (e.g. 4x3) instead of the autotuner")
     ap.add_argument("--headline-only", action="store_true",
                     help="only the timed headline shots (for profiler runs): no e2e, extras or CPU leg")
     args = ap.parse_args(argv)
