@@ -35,7 +35,10 @@ struct Col {
   }
 };
 
-__global__ void __launch_bounds__(BX * BZ, 5) seis25_stress_kernel(Seis25Args a, int rel) {
+// 8 blocks of 128 threads per SM (64 registers): the y-march's loads wait on
+// HBM, and more resident warps hide more of that latency than the few
+// registers spilled to L1 cost.
+__global__ void __launch_bounds__(BX * BZ, 8) seis25_stress_kernel(Seis25Args a, int rel) {
   const Ctl* ctl = a.io.ctl;
   const int t = ctl->base + rel;
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && t > ctl->run_start) {
@@ -203,7 +206,7 @@ __global__ void __launch_bounds__(BX * BZ, 5) seis25_stress_kernel(Seis25Args a,
   }
 }
 
-__global__ void __launch_bounds__(BX * BZ) seis25_velocity_kernel(Seis25Args a, int rel) {
+__global__ void __launch_bounds__(BX * BZ, 8) seis25_velocity_kernel(Seis25Args a, int rel) {
   const int t = a.io.ctl->base + rel;
   const int i = blockIdx.x * BX + threadIdx.x;
   const int k = blockIdx.y * BZ + threadIdx.y;

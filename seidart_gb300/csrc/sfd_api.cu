@@ -137,10 +137,12 @@ size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 int choose_ysplit(const sfd_config& c) {
   if (!is3(c.kind)) return 1;
-  // enough columns x segments to fill 152 SMs a few times over
+  // enough columns x segments to fill 152 SMs several times over (the
+  // y-march of a segment is latency-bound: more, shorter segments keep more
+  // loads in flight), segments of at least 4 cells
   const long cols = (long)c.nx * c.nz;
   int s = 1;
-  while (cols * s < 152L * 1024 * 2 && s * 8 <= c.ny) s *= 2;
+  while (cols * s < 152L * 1024 * 8 && s * 4 <= c.ny) s *= 2;
   return s;
 }
 
