@@ -2,9 +2,9 @@
 // velocity-stress scheme on (NX, NY, NZ) with y-invariant stiffness C(x, z).
 //
 // Each thread owns one (x, z) column and marches along y, so the 33 averaged
-// stiffness values the four stress loops need at that column (and the three
-// averaged densities of the velocity loops) are formed once per column
-// instead of once per cell.
+// stiffness values the four stress loops need at that column (formed on the
+// host in FP64, y-invariant) and the three averaged densities of the
+// velocity loops are read once per column segment instead of once per cell.
 //   half1: the four stress loops (:616-678 sigmaxx/yy/zz, :681-725 sigmaxy,
 //          :728-771 sigmaxz, :774-815 sigmayz).  The nine velocity-gradient
 //          memory variables are shared by the loops in the Fortran and
@@ -22,18 +22,6 @@ namespace sfd {
 namespace {
 
 constexpr int BX = 32, BZ = 4;
-
-// Plane indices of the 21 stiffness coefficients.
-enum { C11, C12, C13, C14, C15, C16, C22, C23, C24, C25, C26, C33, C34, C35, C36, C44, C45, C46, C55, C56, C66 };
-
-struct Col {
-  const float* C;
-  int P, NZ;
-  __device__ float at(int q, int i, int k) const { return C[((size_t)q * NZ + k) * P + i]; }
-  __device__ float sum4(int q, int i0, int k0, int i1, int k1, int i2, int k2, int i3, int k3) const {
-    return at(q, i0, k0) + at(q, i1, k1) + at(q, i2, k2) + at(q, i3, k3);
-  }
-};
 
 // 8 blocks of 128 threads per SM (64 registers): the y-march's loads wait on
 // HBM, and more resident warps hide more of that latency than the few
@@ -59,42 +47,29 @@ __global__ void __launch_bounds__(BX * BZ, 8) seis25_stress_kernel(Seis25Args a,
   const bool L4 = (k <= NZ - 2) && (i <= NX - 2);
   if (!(L1 || L2 || L3 || L4)) return;
 
-  const Col cc{a.C, P, NZ};
-  // Loop-1 averages over (i+1,k) (i,k) (i,k-1) (i+1,k-1)
+  // The 33 stiffness averages of the four loops at this column, formed once
+  // on the host in FP64 (planes 0-14 loop 1, 15-20 loop 2, 21-26 loop 3,
+  // 27-32 loop 4; zero where the loop does not update the cell).
+  const size_t cpl = (size_t)NZ * P, cpc = (size_t)k * P + i;
+  auto cf = [&](int q) { return __ldg(a.C + q * cpl + cpc); };
   float p11 = 0, p12 = 0, p13 = 0, p14 = 0, p15 = 0, p16 = 0, p22 = 0, p23 = 0, p24 = 0, p25 = 0, p26 = 0;
   float p33 = 0, p34 = 0, p35 = 0, p36 = 0;
-  if (L1) {
-#define S1(q) cc.sum4(q, i + 1, k, i, k, i, k - 1, i + 1, k - 1)
-    p11 = 0.25f * S1(C11); p12 = 0.25f * S1(C12); p13 = 0.25f * S1(C13);
-    p14 = 0.125f * S1(C14); p15 = 0.125f * S1(C15); p16 = 0.125f * S1(C16);
-    p22 = 0.25f * S1(C22); p23 = 0.25f * S1(C23); p24 = 0.125f * S1(C24); p25 = 0.125f * S1(C25);
-    p26 = 0.125f * S1(C26); p33 = 0.25f * S1(C33); p34 = 0.125f * S1(C34); p35 = 0.125f * S1(C35);
-    p36 = 0.125f * S1(C36);
-#undef S1
+  if (L1) {  // over (i+1,k) (i,k) (i,k-1) (i+1,k-1)
+    p11 = cf(0); p12 = cf(1); p13 = cf(2); p14 = cf(3); p15 = cf(4); p16 = cf(5);
+    p22 = cf(6); p23 = cf(7); p24 = cf(8); p25 = cf(9); p26 = cf(10);
+    p33 = cf(11); p34 = cf(12); p35 = cf(13); p36 = cf(14);
   }
-  // Loop-2 averages over (i,k) (i-1,k) (i,k-1) (i-1,k-1)
   float q16 = 0, q26 = 0, q36 = 0, q46 = 0, q56 = 0, q66 = 0;
-  if (L2) {
-#define S2(q) cc.sum4(q, i, k, i - 1, k, i, k - 1, i - 1, k - 1)
-    q16 = 0.25f * S2(C16); q26 = 0.25f * S2(C26); q36 = 0.25f * S2(C36);
-    q46 = 0.125f * S2(C46); q56 = 0.125f * S2(C56); q66 = 0.125f * S2(C66);
-#undef S2
+  if (L2) {  // over (i,k) (i-1,k) (i,k-1) (i-1,k-1)
+    q16 = cf(15); q26 = cf(16); q36 = cf(17); q46 = cf(18); q56 = cf(19); q66 = cf(20);
   }
-  // Loop-3 averages over (i,k+1) (i,k) (i-1,k) (i-1,k+1)
   float r15 = 0, r25 = 0, r35 = 0, r45 = 0, r55 = 0, r56 = 0;
-  if (L3) {
-#define S3(q) cc.sum4(q, i, k + 1, i, k, i - 1, k, i - 1, k + 1)
-    r15 = 0.25f * S3(C15); r25 = 0.25f * S3(C25); r35 = 0.25f * S3(C35);
-    r45 = 0.125f * S3(C45); r55 = 0.125f * S3(C55); r56 = 0.125f * S3(C56);
-#undef S3
+  if (L3) {  // over (i,k+1) (i,k) (i-1,k) (i-1,k+1)
+    r15 = cf(21); r25 = cf(22); r35 = cf(23); r45 = cf(24); r55 = cf(25); r56 = cf(26);
   }
-  // Loop-4 averages over (i+1,k) (i,k) (i,k+1) (i+1,k+1)
   float s14 = 0, s24 = 0, s34 = 0, s44 = 0, s45 = 0, s46 = 0;
-  if (L4) {
-#define S4(q) cc.sum4(q, i + 1, k, i, k, i, k + 1, i + 1, k + 1)
-    s14 = 0.25f * S4(C14); s24 = 0.25f * S4(C24); s34 = 0.25f * S4(C34);
-    s44 = 0.125f * S4(C44); s45 = 0.125f * S4(C45); s46 = 0.125f * S4(C46);
-#undef S4
+  if (L4) {  // over (i+1,k) (i,k) (i,k+1) (i+1,k+1)
+    s14 = cf(27); s24 = cf(28); s34 = cf(29); s44 = cf(30); s45 = cf(31); s46 = cf(32);
   }
 
   const bool xs = in_strip(i, NX, W), zs = in_strip(k, NZ, W);

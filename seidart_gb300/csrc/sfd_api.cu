@@ -126,7 +126,7 @@ const char* mem_axes(int kind) {
 int ncoef(int kind) {
   switch (kind) {
     case SFD_SEISMIC2: return 12;   // A11 A13 A15 A33 A35 B15 B35 B55 (averaged, x dt), dt/rho, dt/rho_avg, 1-gx, 1-gz
-    case SFD_SEISMIC25: return 27;  // 21 C x dt, 3 dt/rho_avg, 3 (1 - gamma)
+    case SFD_SEISMIC25: return 39;  // 33 averaged C x dt (stress loops), 3 dt/rho_avg, 3 (1 - gamma)
     case SFD_ELECTROMAG2: return 4;
     case SFD_ELECTROMAG25: return 6;
   }
@@ -368,7 +368,7 @@ void bind_args(sfd_handle* h) {
       a.m_sxx_x = h->m(9); a.m_syy_y = h->m(10); a.m_szz_z = h->m(11); a.m_sxy_x = h->m(12);
       a.m_sxy_y = h->m(13); a.m_sxz_x = h->m(14); a.m_sxz_z = h->m(15); a.m_syz_y = h->m(16);
       a.m_syz_z = h->m(17);
-      a.C = h->coef(0); a.dtr = h->coef(21); a.gp = h->coef(24);
+      a.C = h->coef(0); a.dtr = h->coef(33); a.gp = h->coef(36);
       a.X = make_axis(h->axis(0), NX); a.Y = make_axis(h->axis(1), NY); a.Z = make_axis(h->axis(2), NZ);
       a.idx = (float)(1.0 / c.dx); a.idz = (float)(1.0 / c.dz);
       a.ysplit = L.ysplit;
@@ -737,8 +737,41 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
     }
     case SFD_SEISMIC25: {
       const double* rho = P(21);
-      for (int q = 0; q < 21; ++q)
-        for (size_t n = 0; n < N2; ++n) out[q][n] = (float)(P(q)[n] * dt);
+      // The y-invariant stiffness averages of the four stress loops, in FP64
+      // (seismicfdtd.f95:616-815): plane q holds factor x (C(a) + C(b) + C(c)
+      // + C(d)) x dt of Voigt entry `cij` over the four cells of its loop,
+      // where that loop updates the cell, else 0.  Factors and stencils as the
+      // stress kernel (seis25.cu) reads them.
+      struct Avg { int loop, cij; double f; };
+      static const Avg avg[33] = {
+          {1, 0, 0.25}, {1, 1, 0.25}, {1, 2, 0.25}, {1, 3, 0.125}, {1, 4, 0.125}, {1, 5, 0.125},     // p11..p16
+          {1, 6, 0.25}, {1, 7, 0.25}, {1, 8, 0.125}, {1, 9, 0.125}, {1, 10, 0.125},                  // p22..p26
+          {1, 11, 0.25}, {1, 12, 0.125}, {1, 13, 0.125}, {1, 14, 0.125},                             // p33..p36
+          {2, 5, 0.25}, {2, 10, 0.25}, {2, 14, 0.25}, {2, 17, 0.125}, {2, 19, 0.125}, {2, 20, 0.125}, // q16 q26 q36 q46 q56 q66
+          {3, 4, 0.25}, {3, 9, 0.25}, {3, 13, 0.25}, {3, 16, 0.125}, {3, 18, 0.125}, {3, 19, 0.125},  // r15 r25 r35 r45 r55 r56
+          {4, 3, 0.25}, {4, 8, 0.25}, {4, 12, 0.25}, {4, 15, 0.125}, {4, 16, 0.125}, {4, 17, 0.125}}; // s14 s24 s34 s44 s45 s46
+      for (int q = 0; q < 33; ++q) {
+        const double* C = P(avg[q].cij);
+        for (int k = 0; k < NZ; ++k)
+          for (int i = 0; i < NX; ++i) {
+            double v = 0.0;
+            switch (avg[q].loop) {
+              case 1:  // (i+1,k) (i,k) (i,k-1) (i+1,k-1), k >= 1, i <= NX-2
+                if (k >= 1 && i <= NX - 2) v = at(C, i + 1, k) + at(C, i, k) + at(C, i, k - 1) + at(C, i + 1, k - 1);
+                break;
+              case 2:  // (i,k) (i-1,k) (i,k-1) (i-1,k-1), k >= 1, i >= 1
+                if (k >= 1 && i >= 1) v = at(C, i, k) + at(C, i - 1, k) + at(C, i, k - 1) + at(C, i - 1, k - 1);
+                break;
+              case 3:  // (i,k+1) (i,k) (i-1,k) (i-1,k+1), k <= NZ-2, i >= 1
+                if (k <= NZ - 2 && i >= 1) v = at(C, i, k + 1) + at(C, i, k) + at(C, i - 1, k) + at(C, i - 1, k + 1);
+                break;
+              default:  // (i+1,k) (i,k) (i,k+1) (i+1,k+1), k <= NZ-2, i <= NX-2
+                if (k <= NZ - 2 && i <= NX - 2) v = at(C, i + 1, k) + at(C, i, k) + at(C, i, k + 1) + at(C, i + 1, k + 1);
+                break;
+            }
+            out[q][(size_t)i + (size_t)NX * k] = (float)(avg[q].f * v * dt);
+          }
+      }
       for (size_t n = 0; n < N2; ++n)
         if (!(rho[n] > 0)) return fail(SFD_ERR_BAD_ARG, "density must be positive (cell %zu)", n);
       for (int k = 0; k < NZ; ++k)
@@ -746,14 +779,14 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
           const size_t n = (size_t)i + (size_t)NX * k;
           const double r = rho[n];
           if (i >= 1 && k >= 1)  // seismicfdtd.f95:826
-            out[21][n] = (float)(dt / ((4 * r + at(rho, i - 1, k) + at(rho, i, k - 1)) / 6));
+            out[33][n] = (float)(dt / ((4 * r + at(rho, i - 1, k) + at(rho, i, k - 1)) / 6));
           if (i <= NX - 2 && k >= 1)  // :851
-            out[22][n] = (float)(dt / ((4 * r + at(rho, i + 1, k) + at(rho, i, k - 1)) / 6));
+            out[34][n] = (float)(dt / ((4 * r + at(rho, i + 1, k) + at(rho, i, k - 1)) / 6));
           if (i <= NX - 2 && k <= NZ - 2)  // :877
-            out[23][n] = (float)(dt / ((at(rho, i + 1, k) + at(rho, i, k + 1) + 4 * r) / 6));
+            out[35][n] = (float)(dt / ((at(rho, i + 1, k) + at(rho, i, k + 1) + 4 * r) / 6));
           for (int d = 0; d < 3; ++d) {
             const double g = P(22 + d)[n];
-            out[24 + d][n] = (float)(1.0 - g);
+            out[36 + d][n] = (float)(1.0 - g);
             if (g != 0.0) atten = 1;
           }
         }

@@ -59,7 +59,7 @@ struct Seis25Args {
   float *m_sxx_x, *m_sxy_x, *m_sxz_x;  // x-strip
   float *m_syy_y, *m_sxy_y, *m_syz_y;  // y-strip
   float *m_szz_z, *m_sxz_z, *m_syz_z;  // z-strip
-  const float* C;     // 21 planes (stiffness * dt), pitch P, NZ rows each
+  const float* C;     // 33 planes: the stress loops' stiffness averages x dt, pitch P, NZ rows each
   const float* dtr;   // 3 planes: dt / rho_avg for vx, vy, vz
   const float* gp;    // 3 planes: 1 - gamma_x, 1 - gamma_y, 1 - gamma_z
   AxisTab X, Y, Z;
