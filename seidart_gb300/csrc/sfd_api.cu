@@ -293,6 +293,16 @@ struct sfd_handle_s {
 
 namespace {
 
+// Rows per thread of the single-pass tiles: two when two-row tiles fill the
+// SMs several times over, else one -- on smaller grids the step waits on
+// L2, and more, smaller blocks keep more loads in flight (measured on the
+// 440 x 240 seismic2 and 1040 x 540 electromag2 grids).
+int single_pass_zb(int kind, int nx, int nz) {
+  const long tw = kind == SFD_ELECTROMAG2 ? 128 : 32;  // tile width
+  const long tiles2 = ((nx + tw - 1) / tw) * (long)((nz + 15) / 16);
+  return tiles2 >= 8L * 152 ? 2 : 1;
+}
+
 void bind_args(sfd_handle* h) {
   const Layout& L = h->L;
   const sfd_config& c = h->cfg;
@@ -321,6 +331,7 @@ void bind_args(sfd_handle* h) {
         b.CAx = a.CAx; b.CBx = a.CBx; b.CAz = a.CAz; b.CBz = a.CBz;
         b.X = a.X; b.Z = a.Z; b.dbH = a.dbH; b.io = io;
       }
+      h->zb = single_pass_zb(c.kind, NX, NZ);
       if (h->single) h->launch1 = em2_step_launch(h->em2s[0], h->zb);
       break;
     }
@@ -352,6 +363,7 @@ void bind_args(sfd_handle* h) {
         b.dtrx = a.dtrx; b.dtrz = a.dtrz; b.gxp = a.gxp; b.gzp = a.gzp; b.q3 = a.q3;
         b.X = a.X; b.Z = a.Z; b.io = io;
       }
+      h->zb = single_pass_zb(c.kind, NX, NZ);
       if (h->single) h->launch1 = seis2_step_launch(h->s2s[0], h->zb);
       break;
     }
