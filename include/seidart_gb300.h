@@ -165,6 +165,14 @@ int32_t sfd_reset(sfd_handle* h);
  * initialcondition*.dat files of classes.py:882-898).  Reads synchronise. */
 int32_t sfd_set_field(sfd_handle* h, int32_t field, const float* host, int64_t count);
 int32_t sfd_get_field(sfd_handle* h, int32_t field, float* host, int64_t count);
+/* The read of sfd_get_field queued on the handle's stream without waiting:
+ * `host` may be read once the stream has passed this point (an event
+ * recorded after the call, or sfd_status).  Into page-locked host memory
+ * the copy overlaps the host's own work; it replaces the per-step snapshot
+ * writes of write_image2/write_image3 (readwrite_routines.f95:473-527,
+ * called each step at seismicfdtd.f95:381-382 and electromagfdtd.f95:323),
+ * whose file output the caller does on its own thread. */
+int32_t sfd_get_field_async(sfd_handle* h, int32_t field, float* host, int64_t count);
 /* One CPML memory variable expanded to the full grid (zero off its strips). */
 int32_t sfd_get_memory(sfd_handle* h, int32_t index, float* host, int64_t count);
 

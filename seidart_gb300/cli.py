@@ -20,7 +20,9 @@ profiles are computed from the project's CPML parameters in FP64
 (``seidart_gb300.cpml``).  Outputs: one FP32 snapshot record per channel and
 per step, named ``{Vx,Vy,Vz|Ex,Ey,Ez}.{step:06d}.{xind}.{[yind.]}{zind}.dat``
 with 1-based steps, which is what ``Array.getrcx`` globs
-(``src/seidart/routines/arraybuild.py:199-240``).  ``--snapshot-every N``
+(``src/seidart/routines/arraybuild.py:199-240``).  Snapshots leave the GPU
+through page-locked buffers and are written on a background thread while
+the GPU steps on.  ``--snapshot-every N``
 thins the snapshots and ``--receivers FILE --traces OUT.npy`` records
 receiver traces on the device instead.  The exit status is 0 on success, 2
 when the run became unstable, and 1 on any input error.
@@ -181,32 +183,54 @@ def read_receivers(path, grid):
 
 
 class SnapshotWriter:
-    """Writes snapshot records on a background thread while the GPU runs on."""
+    """Drains snapshots through page-locked host buffers.  ``put`` queues the
+    device-to-host copy of a field on the solver's stream and returns without
+    waiting; background threads wait for that copy's event, write the record
+    and hand the buffer back.  The GPU keeps stepping meanwhile; with every
+    buffer in flight, ``put`` waits for one to be written."""
 
-    def __init__(self, workdir):
-        self.q = queue.Queue(maxsize=8)
+    def __init__(self, workdir, solver, nbuf=12, nthreads=4):
+        import torch
+
         self.wd = Path(workdir)
+        self.solver = solver
         self.err = None
-        self.t = threading.Thread(target=self._loop, daemon=True)
-        self.t.start()
+        self.free = queue.Queue()
+        for _ in range(nbuf):
+            self.free.put(torch.empty(solver.grid.shape, dtype=torch.float32, pin_memory=True))
+        self.q = queue.Queue()
+        self.ts = [threading.Thread(target=self._loop, daemon=True) for _ in range(nthreads)]
+        for t in self.ts:
+            t.start()
 
     def _loop(self):
         while True:
             item = self.q.get()
             if item is None:
                 return
-            name, arr = item
+            name, buf, ev = item
             try:
-                fio.write_record(self.wd / name, arr, np.float32)
-            except OSError as e:
+                ev.synchronize()
+                fio.write_record(self.wd / name, buf.numpy(), np.float32)
+            except (OSError, RuntimeError) as e:
                 self.err = e
+            finally:
+                self.free.put(buf)
 
-    def put(self, name, arr):
-        self.q.put((name, arr))
+    def put(self, name, ch):
+        import torch
+
+        buf = self.free.get()
+        self.solver.field_async(ch, buf)
+        ev = torch.cuda.Event()
+        ev.record(self.solver.stream)
+        self.q.put((name, buf, ev))
 
     def close(self):
-        self.q.put(None)
-        self.t.join()
+        for _ in self.ts:
+            self.q.put(None)
+        for t in self.ts:
+            t.join()
         if self.err:
             raise self.err
 
@@ -253,7 +277,7 @@ def run(argv=None) -> int:
             for ch, v in p["init"].items():
                 s.set_field(ch, v.astype(np.float32))
             chans = CHANNELS[p["kind"]]
-            writer = SnapshotWriter(a.workdir) if every else None
+            writer = SnapshotWriter(a.workdir, s) if every else None
             done = 0
             while done < p["nstep"]:
                 n = min(every, p["nstep"] - done) if every else p["nstep"]
@@ -261,7 +285,7 @@ def run(argv=None) -> int:
                 done += n
                 if writer:
                     for ch in chans:
-                        writer.put(snapshot_name(ch, done, p), s.field(ch))
+                        writer.put(snapshot_name(ch, done, p), ch)
             if writer:
                 writer.close()
             s.status()

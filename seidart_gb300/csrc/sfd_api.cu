@@ -940,6 +940,17 @@ int32_t sfd_get_field(sfd_handle* h, int32_t field, float* host, int64_t count) 
   return SFD_OK;
 }
 
+int32_t sfd_get_field_async(sfd_handle* h, int32_t field, float* host, int64_t count) {
+  g_err.clear();
+  if (!h || !host) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  const sfd_config& c = h->cfg;
+  if (field < 0 || field >= nfields(c.kind)) return fail(SFD_ERR_BAD_ARG, "field %d out of range", field);
+  if (count != (int64_t)c.nx * c.ny * c.nz) return fail(SFD_ERR_BAD_ARG, "field needs %d*%d*%d values", c.nx, c.ny, c.nz);
+  CK(cudaMemcpy2DAsync(host, sizeof(float) * c.nx, h->f(field), sizeof(float) * h->L.P, sizeof(float) * c.nx,
+                       (size_t)c.ny * c.nz, cudaMemcpyDeviceToHost, h->stream));
+  return SFD_OK;
+}
+
 int32_t sfd_get_memory(sfd_handle* h, int32_t index, float* host, int64_t count) {
   g_err.clear();
   if (!h || !host) return fail(SFD_ERR_BAD_ARG, "NULL argument");

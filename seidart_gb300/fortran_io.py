@@ -35,12 +35,13 @@ def read_record(path, dtype=np.float64) -> np.ndarray:
 
 def write_record(path, array, dtype=np.float32) -> None:
     """Write ``array`` (flattened in C order) as one record of ``dtype``."""
-    data = np.ascontiguousarray(array, dtype=dtype).tobytes()
+    data = np.ascontiguousarray(array, dtype=dtype)
+    n = struct.pack("<i", data.nbytes)
     tmp = f"{path}.tmp"
     with open(tmp, "wb") as f:
-        f.write(struct.pack("<i", len(data)))
-        f.write(data)
-        f.write(struct.pack("<i", len(data)))
+        f.write(n)
+        f.write(memoryview(data.reshape(-1)).cast("B"))
+        f.write(n)
     os.replace(tmp, path)
 
 

@@ -204,6 +204,18 @@ class FDTDSolver:
         check(self._L.sfd_get_field(self._h, q, _fptr(out), out.size))
         return out
 
+    def field_async(self, name, out) -> None:
+        """Queue the copy of field ``name`` into ``out`` (a page-locked CPU
+        float32 torch tensor of the grid's shape) on the solver's stream and
+        return at once; ``out`` holds the field once the stream has passed
+        this point (record a CUDA event on ``self.stream`` after the call)."""
+        import torch
+        q = FIELDS[self.kind].index(name) if isinstance(name, str) else int(name)
+        if out.dtype != torch.float32 or out.device.type != "cpu" or not out.is_contiguous() or \
+                out.numel() != int(np.prod(self.grid.shape)):
+            raise ValueError("out must be a contiguous float32 CPU tensor of the grid's size")
+        check(self._L.sfd_get_field_async(self._h, q, C.c_void_p(out.data_ptr()), out.numel()))
+
     def memory(self, name) -> np.ndarray:
         q = MEMORY[self.kind].index(name) if isinstance(name, str) else int(name)
         out = np.empty(self.grid.shape, dtype=np.float32)
