@@ -173,6 +173,14 @@ int32_t sfd_get_field(sfd_handle* h, int32_t field, float* host, int64_t count);
  * called each step at seismicfdtd.f95:381-382 and electromagfdtd.f95:323),
  * whose file output the caller does on its own thread. */
 int32_t sfd_get_field_async(sfd_handle* h, int32_t field, float* host, int64_t count);
+/* One field as block-floating int16, queued on the handle's stream: device
+ * dev_minmax[0..1] <- the field's min and max (FP32), device dev_out (NX*NY*NZ
+ * int16, x fastest, then y, then z) <- codes with (code + 32767) / 65534 =
+ * (value - min) / (max - min), 0 when max == min.  These are the records of
+ * the SEIDART_EM25B1 block files the reference reads for 2.5-D EM snapshots
+ * (src/seidart/routines/definitions.py:140-212, read_block); the reference
+ * writes them from its Fortran backend, which is not part of its source. */
+int32_t sfd_encode_field_i16(sfd_handle* h, int32_t field, void* dev_out, void* dev_minmax);
 /* One CPML memory variable expanded to the full grid (zero off its strips). */
 int32_t sfd_get_memory(sfd_handle* h, int32_t index, float* host, int64_t count);
 

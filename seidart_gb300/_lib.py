@@ -23,7 +23,7 @@ EXPORTS = (
     "sfd_version", "sfd_last_error", "sfd_model_planes", "sfd_num_fields", "sfd_num_channels",
     "sfd_num_memory", "sfd_state_bytes", "sfd_create", "sfd_set_model", "sfd_set_cpml",
     "sfd_set_source", "sfd_share_model", "sfd_set_receivers", "sfd_reset", "sfd_set_field", "sfd_get_field",
-    "sfd_get_field_async",
+    "sfd_get_field_async", "sfd_encode_field_i16",
     "sfd_get_memory", "sfd_run", "sfd_status", "sfd_get_traces", "sfd_traces_device", "sfd_launch_half",
     "sfd_on_chip",
     "sfd_destroy", "sfd_checkpoint_bytes", "sfd_checkpoint_save", "sfd_checkpoint_load", "sfd_adjoint_bytes",
@@ -80,6 +80,7 @@ def _declare(lib):
         "sfd_set_field": (i32, [P, i32, fp, i64]),
         "sfd_get_field": (i32, [P, i32, fp, i64]),
         "sfd_get_field_async": (i32, [P, i32, P, i64]),
+        "sfd_encode_field_i16": (i32, [P, i32, P, P]),
         "sfd_get_memory": (i32, [P, i32, fp, i64]),
         "sfd_run": (i32, [P, i64]),
         "sfd_status": (i32, [P, C.POINTER(i64), dp]),

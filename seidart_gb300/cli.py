@@ -235,6 +235,80 @@ class SnapshotWriter:
             raise self.err
 
 
+class BlockDrain:
+    """Electromag25 snapshots as SEIDART_EM25B1 block files of ``per_block``
+    consecutive steps (``seidart_gb300.em25block``).  Each field is encoded
+    to int16 on the GPU, copied into page-locked buffers without waiting,
+    and appended to the current block file by one background thread."""
+
+    def __init__(self, workdir, solver, p, per_block, nslots=8):
+        import torch
+
+        self.wd = Path(workdir)
+        self.solver = solver
+        self.p = p
+        self.per_block = int(per_block)
+        self.chans = CHANNELS[p["kind"]]
+        n = int(np.prod(solver.grid.shape))
+        self.free = queue.Queue()
+        for _ in range(nslots):
+            self.free.put({"dev": torch.empty(n, dtype=torch.int16, device=solver.device),
+                           "dmm": torch.empty(2, dtype=torch.float32, device=solver.device),
+                           "pin": torch.empty(n, dtype=torch.int16, pin_memory=True),
+                           "pmm": torch.empty(2, dtype=torch.float32, pin_memory=True)})
+        self.err = None
+        self.q = queue.Queue()
+        self.t = threading.Thread(target=self._loop, daemon=True)
+        self.t.start()
+
+    def put(self, step, ch):
+        import torch
+
+        slot = self.free.get()
+        self.solver.encode_i16(ch, slot["dev"], slot["dmm"])
+        with torch.cuda.stream(self.solver.stream):
+            slot["pin"].copy_(slot["dev"], non_blocking=True)
+            slot["pmm"].copy_(slot["dmm"], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(self.solver.stream)
+        self.q.put((step, ch, slot, ev))
+
+    def _loop(self):
+        from . import em25block
+
+        g = self.solver.grid
+        w = None
+        while True:
+            item = self.q.get()
+            if item is None:
+                break
+            step, ch, slot, ev = item
+            try:
+                ev.synchronize()
+                if self.err is None:
+                    if w is None or (ch == self.chans[0] and w.steps >= self.per_block):
+                        if w is not None:
+                            w.close()
+                        name = em25block.block_name(self.p["xind"], self.p["yind"], self.p["zind"], step)
+                        w = em25block.BlockWriter(self.wd / name, g.nx, g.ny, g.nz, step, self.chans)
+                    w.add(step, ch, float(slot["pmm"][0]), float(slot["pmm"][1]), slot["pin"].numpy())
+            except (OSError, ValueError, RuntimeError) as e:
+                self.err = e
+            finally:
+                self.free.put(slot)
+        if w is not None and self.err is None:
+            try:
+                w.close()
+            except (OSError, ValueError) as e:
+                self.err = e
+
+    def close(self):
+        self.q.put(None)
+        self.t.join()
+        if self.err:
+            raise self.err
+
+
 def snapshot_name(ch, step, p):
     ch = ch[0].upper() + ch[1:]  # Vx Vy Vz / Ex Ey Ez, write_image2/3 (readwrite_routines.f95:486)
     if is_25d(p["kind"]):
@@ -249,6 +323,9 @@ def run(argv=None) -> int:
     ap.add_argument("flags", nargs="*", help="seismic=<true|false> density_method=<none|arithmetic|...>")
     ap.add_argument("--workdir", default=".")
     ap.add_argument("--snapshot-every", type=int, default=1, help="write snapshots every N steps (0 = none)")
+    ap.add_argument("--em25-blocks", type=int, default=0,
+                    help="electromag25: write the snapshots as SEIDART_EM25B1 block files of N steps each "
+                         "(int16 block-floating) instead of one FP32 record per channel and step")
     ap.add_argument("--receivers", help="receiver CSV (X,Y,Z in metres)")
     ap.add_argument("--traces", help="write receiver traces (nstep, channel, receiver) to this .npy")
     ap.add_argument("--device", default="cuda")
@@ -267,6 +344,11 @@ def run(argv=None) -> int:
     grid = p["grid"]
     rec = read_receivers(a.receivers, grid) if a.receivers else np.zeros((0, 3), np.int32)
     every = max(0, int(a.snapshot_every))
+    blocks = max(0, int(a.em25_blocks))
+    if blocks and (p["kind"] != ELECTROMAG25 or every != 1):
+        print("seidartfdtd: --em25-blocks writes consecutive steps of electromag25 runs "
+              "(seismic=false on a 2.5-D project, --snapshot-every 1)", file=sys.stderr)
+        return 1
     try:
         with FDTDSolver(grid, p["nstep"], len(rec), device=a.device) as s:
             s.set_model(p["planes"])
@@ -277,7 +359,10 @@ def run(argv=None) -> int:
             for ch, v in p["init"].items():
                 s.set_field(ch, v.astype(np.float32))
             chans = CHANNELS[p["kind"]]
-            writer = SnapshotWriter(a.workdir, s) if every else None
+            if blocks:
+                writer = BlockDrain(a.workdir, s, p, blocks)
+            else:
+                writer = SnapshotWriter(a.workdir, s) if every else None
             done = 0
             while done < p["nstep"]:
                 n = min(every, p["nstep"] - done) if every else p["nstep"]
@@ -285,7 +370,10 @@ def run(argv=None) -> int:
                 done += n
                 if writer:
                     for ch in chans:
-                        writer.put(snapshot_name(ch, done, p), ch)
+                        if blocks:
+                            writer.put(done, ch)
+                        else:
+                            writer.put(snapshot_name(ch, done, p), ch)
             if writer:
                 writer.close()
             s.status()

@@ -951,6 +951,18 @@ int32_t sfd_get_field_async(sfd_handle* h, int32_t field, float* host, int64_t c
   return SFD_OK;
 }
 
+int32_t sfd_encode_field_i16(sfd_handle* h, int32_t field, void* dev_out, void* dev_minmax) {
+  g_err.clear();
+  if (!h || !dev_out || !dev_minmax) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  const sfd_config& c = h->cfg;
+  if (field < 0 || field >= nfields(c.kind)) return fail(SFD_ERR_BAD_ARG, "field %d out of range", field);
+  if (((uintptr_t)dev_out & 1) || ((uintptr_t)dev_minmax & 3))
+    return fail(SFD_ERR_BAD_ARG, "misaligned output: int16 codes need 2-byte, min/max 4-byte alignment");
+  encode_field_i16(h->f(field), c.nx, h->L.P, (long)c.ny * c.nz, (short*)dev_out, (float*)dev_minmax, h->stream);
+  CK(cudaGetLastError());
+  return SFD_OK;
+}
+
 int32_t sfd_get_memory(sfd_handle* h, int32_t index, float* host, int64_t count) {
   g_err.clear();
   if (!h || !host) return fail(SFD_ERR_BAD_ARG, "NULL argument");

@@ -155,4 +155,9 @@ Launch seis2_step_launch(const Seis2Step& a, int zb);
 void seis2_step(const Seis2Step& a, const Launch& L, int zb, int rel, cudaStream_t s);
 void seis2_step_finalize(const Seis2Step& a, int t_last, cudaStream_t s);
 
+// Block-floating int16 encoding of one field (snapshot.cu): minmax[0..1] <-
+// the field's min and max, out <- the dense x-fastest int16 codes.  rows =
+// NY * NZ rows of NX values at pitch P.  Queued on stream s.
+void encode_field_i16(const float* field, int NX, int P, long rows, short* out, float* minmax, cudaStream_t s);
+
 }  // namespace sfd

@@ -216,6 +216,20 @@ class FDTDSolver:
             raise ValueError("out must be a contiguous float32 CPU tensor of the grid's size")
         check(self._L.sfd_get_field_async(self._h, q, C.c_void_p(out.data_ptr()), out.numel()))
 
+    def encode_i16(self, name, codes, minmax) -> None:
+        """Queue the block-floating int16 encoding of field ``name`` on the
+        solver's stream (``sfd_encode_field_i16``): ``minmax`` (device float32,
+        2 values) gets the field's min and max, ``codes`` (device int16, one per
+        cell, x fastest) the codes of ``seidart_gb300.em25block``."""
+        import torch
+        q = FIELDS[self.kind].index(name) if isinstance(name, str) else int(name)
+        n = int(np.prod(self.grid.shape))
+        if codes.dtype != torch.int16 or codes.numel() != n or codes.device.type != "cuda" or not codes.is_contiguous():
+            raise ValueError("codes must be a contiguous int16 CUDA tensor with one value per cell")
+        if minmax.dtype != torch.float32 or minmax.numel() != 2 or minmax.device.type != "cuda":
+            raise ValueError("minmax must be a float32 CUDA tensor of 2 values")
+        check(self._L.sfd_encode_field_i16(self._h, q, C.c_void_p(codes.data_ptr()), C.c_void_p(minmax.data_ptr())))
+
     def memory(self, name) -> np.ndarray:
         q = MEMORY[self.kind].index(name) if isinstance(name, str) else int(name)
         out = np.empty(self.grid.shape, dtype=np.float32)
