@@ -23,10 +23,10 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "liboracle.so"
-SEISMIC2, SEISMIC25, ELECTROMAG2, ELECTROMAG25 = 1, 2, 3, 4
-NFIELDS = {SEISMIC2: 5, SEISMIC25: 9, ELECTROMAG2: 3, ELECTROMAG25: 6}
-NMEM = {SEISMIC2: 8, SEISMIC25: 18, ELECTROMAG2: 4, ELECTROMAG25: 12}
-NCH = {SEISMIC2: 2, SEISMIC25: 3, ELECTROMAG2: 2, ELECTROMAG25: 3}
+SEISMIC2, SEISMIC25, ELECTROMAG2, ELECTROMAG25, ELECTROMAG2C = 1, 2, 3, 4, 5
+NFIELDS = {SEISMIC2: 5, SEISMIC25: 9, ELECTROMAG2: 3, ELECTROMAG25: 6, ELECTROMAG2C: 6}
+NMEM = {SEISMIC2: 8, SEISMIC25: 18, ELECTROMAG2: 4, ELECTROMAG25: 12, ELECTROMAG2C: 8}
+NCH = {SEISMIC2: 2, SEISMIC25: 3, ELECTROMAG2: 2, ELECTROMAG25: 3, ELECTROMAG2C: 4}
 
 _lock = threading.Lock()
 _lib = None
@@ -50,11 +50,12 @@ def lib():
             i, d = C.c_int, C.c_double
             common_tail = [dp, dp, i, i, dp, i, i, i, dp, dp, i, ip, dp, dp, ip]
             L.orc_electromag2.argtypes = [i, i, d, d, d] + common_tail
+            L.orc_electromag2c.argtypes = [i, i, d, d, d] + common_tail
             L.orc_seismic2.argtypes = [i, i, d, d, d] + common_tail
             tail3 = [dp, dp, i, i, i, dp, i, i, i, dp, dp, i, ip, dp, dp, ip]
             L.orc_seismic25.argtypes = [i, i, i, d, d, d, d] + tail3
             L.orc_electromag25.argtypes = [i, i, i, d, d, d, d] + tail3
-            for f in (L.orc_electromag2, L.orc_seismic2, L.orc_seismic25, L.orc_electromag25):
+            for f in (L.orc_electromag2, L.orc_electromag2c, L.orc_seismic2, L.orc_seismic25, L.orc_electromag25):
                 f.restype = C.c_int
             L.orc_num_threads.restype = C.c_int
             _lib = L
@@ -101,6 +102,10 @@ def run(kind, grid, planes, packed_profiles, src_ijk, srcfn, rec_ijk, nsteps, st
         n = L.orc_electromag2(grid.nx, grid.nz, grid.dx, grid.dz, grid.dt, _d(prof), _d(planes), i, k, _d(srcfn),
                               srcfn.shape[1], state.step, nsteps, _d(state.fields), _d(state.memory), nrec, recp,
                               _d(traces), C.byref(maxnorm), C.byref(blew))
+    elif kind == ELECTROMAG2C:
+        n = L.orc_electromag2c(grid.nx, grid.nz, grid.dx, grid.dz, grid.dt, _d(prof), _d(planes), i, k, _d(srcfn),
+                               srcfn.shape[1], state.step, nsteps, _d(state.fields), _d(state.memory), nrec, recp,
+                               _d(traces), C.byref(maxnorm), C.byref(blew))
     elif kind == SEISMIC2:
         n = L.orc_seismic2(grid.nx, grid.nz, grid.dx, grid.dz, grid.dt, _d(prof), _d(planes), i, k, _d(srcfn),
                            srcfn.shape[1], state.step, nsteps, _d(state.fields), _d(state.memory), nrec, recp,

@@ -29,6 +29,7 @@
 // Every loop below cites the Fortran lines it restates.
 
 #include <cmath>
+#include <complex>
 #include <cstdint>
 #include <cstring>
 #include <vector>
@@ -173,6 +174,133 @@ int orc_electromag2(int NX, int NZ, double dx, double dz, double dt,
   }
   *maxnorm = runmax;
   return nsteps;
+}
+
+// ---------------------------------------------------------------------------
+// electromag2c: legacy/fortran/electromagfdtd.f95:329-616, electromag2 with
+// complex permittivities (material_rwc, readwrite_routines.f95:969-988), so
+// complex update coefficients, fields and memory variables.  Complex arrays
+// travel as (real, imaginary) plane pairs:
+//   mat   = eps11 re, im, eps13 re, im, eps33 re, im, sig11, sig13, sig33  (9 x N)
+//   fld   = Ex re, im, Ez re, im, Hy re, im                                (6 x N)
+//   mem   = dEx_dz re, im, dEz_dx re, im, dHy_dz re, im, dHy_dx re, im     (8 x N)
+//   src   = srcx, srcz (real); chans = Ex re, Ex im, Ez re, Ez im
+// The norm of :598 is |sqrt(Ex^2 + Ez^2)| with complex squares.
+int orc_electromag2c(int NX, int NZ, double dx, double dz, double dt,
+                     const double* prof, const double* mat,
+                     int isrc, int ksrc, const double* src, int nstep_src,
+                     int it0, int nsteps,
+                     double* fld, double* mem,
+                     int nrec, const int* rec, double* traces,
+                     double* maxnorm, int* blew_up) {
+  using cd = std::complex<double>;
+  const size_t N = (size_t)NX * NZ;
+  Axis X, Y, Z;
+  unpack_axes(prof, NX, 1, NZ, false, &X, &Y, &Z);
+  auto cplx = [&](const double* re, const double* im) {
+    std::vector<cd> v(N);
+    for (size_t c = 0; c < N; ++c) v[c] = cd(re[c], im[c]);
+    return v;
+  };
+  const std::vector<cd> eps11 = cplx(mat, mat + N), eps13 = cplx(mat + 2 * N, mat + 3 * N),
+                        eps33 = cplx(mat + 4 * N, mat + 5 * N);
+  const double *sig11 = mat + 6 * N, *sig13 = mat + 7 * N, *sig33 = mat + 8 * N;
+  std::vector<cd> Ex = cplx(fld, fld + N), Ez = cplx(fld + 2 * N, fld + 3 * N), Hy = cplx(fld + 4 * N, fld + 5 * N);
+  std::vector<cd> mExz = cplx(mem, mem + N), mEzx = cplx(mem + 2 * N, mem + 3 * N),
+                  mHyz = cplx(mem + 4 * N, mem + 5 * N), mHyx = cplx(mem + 6 * N, mem + 7 * N);
+  auto I = [NX](int i, int k) { return (size_t)i + (size_t)NX * k; };
+
+  // Coefficients, :439-451.
+  std::vector<cd> caEx(N), cbEx(N), caEz(N), cbEz(N);
+  for (size_t c = 0; c < N; ++c) {
+    const cd ex = (eps11[c] + eps13[c]) * kEps0, ez = (eps13[c] + eps33[c]) * kEps0;
+    const double sx = sig11[c] + sig13[c], sz = sig13[c] + sig33[c];
+    caEx[c] = (1.0 - sx * dt / (2.0 * ex)) / (1.0 + sx * dt / (2.0 * ex));
+    cbEx[c] = (dt / ex) / (1.0 + sx * dt / (2.0 * ex));
+    caEz[c] = (1.0 - sz * dt / (2.0 * ez)) / (1.0 + sz * dt / (2.0 * ez));
+    cbEz[c] = (dt / ez) / (1.0 + sz * dt / (2.0 * ez));
+  }
+  const double daHy = 1.0, dbHy = dt / kMu0;  // :453-455
+  const double* srcx = src;
+  const double* srcz = src + nstep_src;
+  *blew_up = 0;
+  double runmax = 0.0;
+  int done = nsteps;
+
+  for (int s = 0; s < nsteps; ++s) {
+    const int t = it0 + s;
+    // Hy and its memory variables, :530-549.
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k <= NZ - 2; ++k)
+      for (int i = 0; i <= NX - 2; ++i) {
+        const size_t c = I(i, k);
+        cd dEx_dz = (Ex[I(i, k + 1)] - Ex[c]) / dz;
+        mExz[c] = Z.b[k] * mExz[c] + Z.a[k] * dEx_dz;
+        dEx_dz = dEx_dz / Z.K[k] + mExz[c];
+        cd dEz_dx = (Ez[I(i + 1, k)] - Ez[c]) / dx;
+        mEzx[c] = X.b[i] * mEzx[c] + X.a[i] * dEz_dx;
+        dEz_dx = dEz_dx / X.K[i] + mEzx[c];
+        Hy[c] = daHy * Hy[c] + dbHy * (dEz_dx + dEx_dz);
+      }
+    // Ex, :556-565.
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= NZ - 2; ++k)
+      for (int i = 0; i <= NX - 2; ++i) {
+        const size_t c = I(i, k), cm = I(i, k - 1);
+        cd d = (Hy[c] - Hy[cm]) / dz;
+        mHyz[c] = Z.bh[k] * mHyz[c] + Z.ah[k] * d;
+        d = d / Z.Kh[k] + mHyz[c];
+        Ex[c] = ((caEx[c] + caEx[cm]) / 2.0) * Ex[c] + ((cbEx[c] + cbEx[cm]) / 2.0) * d;
+      }
+    // Ez, :567-576.
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k <= NZ - 2; ++k)
+      for (int i = 1; i <= NX - 2; ++i) {
+        const size_t c = I(i, k), cm = I(i - 1, k);
+        cd d = (Hy[c] - Hy[cm]) / dx;
+        mHyx[c] = X.bh[i] * mHyx[c] + X.ah[i] * d;
+        d = d / X.Kh[i] + mHyx[c];
+        Ez[c] = ((caEz[c] + caEz[cm]) / 2.0) * Ez[c] + ((cbEz[c] + cbEz[cm]) / 2.0) * d;
+      }
+    // Source, :581-582: divided by the complex relative permittivity.
+    {
+      const size_t c = I(isrc, ksrc);
+      Ex[c] = Ex[c] + srcx[t] * dt / eps11[c];
+      Ez[c] = Ez[c] + srcz[t] * dt / eps33[c];
+    }
+    // Dirichlet edges, :585-598.
+    for (int k = 0; k < NZ; ++k) {
+      Ex[I(0, k)] = 0.0; Ex[I(NX - 2, k)] = 0.0;
+      Ez[I(0, k)] = 0.0; Ez[I(NX - 1, k)] = 0.0;
+      Hy[I(0, k)] = 0.0; Hy[I(NX - 2, k)] = 0.0;
+    }
+    for (int i = 0; i < NX; ++i) {
+      Ex[I(i, 0)] = 0.0; Ex[I(i, NZ - 1)] = 0.0;
+      Ez[I(i, 0)] = 0.0; Ez[I(i, NZ - 2)] = 0.0;
+      Hy[I(i, 0)] = 0.0; Hy[I(i, NZ - 2)] = 0.0;
+    }
+    // Stability check, :601-602.
+    double mx = 0.0;
+#pragma omp parallel for reduction(max : mx) schedule(static)
+    for (size_t c = 0; c < N; ++c) mx = std::max(mx, std::abs(std::sqrt(Ex[c] * Ex[c] + Ez[c] * Ez[c])));
+    runmax = std::max(runmax, mx);
+    for (int r = 0; r < nrec; ++r) {
+      const size_t c = I(rec[3 * r], rec[3 * r + 2]);
+      traces[((size_t)s * 4 + 0) * nrec + r] = Ex[c].real();
+      traces[((size_t)s * 4 + 1) * nrec + r] = Ex[c].imag();
+      traces[((size_t)s * 4 + 2) * nrec + r] = Ez[c].real();
+      traces[((size_t)s * 4 + 3) * nrec + r] = Ez[c].imag();
+    }
+    if (!(mx <= kStability)) { *blew_up = 1; done = s + 1; break; }
+  }
+  *maxnorm = runmax;
+  auto out = [&](const std::vector<cd>& v, double* re, double* im) {
+    for (size_t c = 0; c < N; ++c) { re[c] = v[c].real(); im[c] = v[c].imag(); }
+  };
+  out(Ex, fld, fld + N); out(Ez, fld + 2 * N, fld + 3 * N); out(Hy, fld + 4 * N, fld + 5 * N);
+  out(mExz, mem, mem + N); out(mEzx, mem + 2 * N, mem + 3 * N);
+  out(mHyz, mem + 4 * N, mem + 5 * N); out(mHyx, mem + 6 * N, mem + 7 * N);
+  return done;
 }
 
 // ---------------------------------------------------------------------------

@@ -1,7 +1,7 @@
-"""Second, independent FP64 restatement of electromag2 and seismic2 in
-vectorised numpy -- TEST INFRASTRUCTURE ONLY.
+"""Second, independent FP64 restatement of electromag2 (real and complex
+permittivities) and seismic2 in vectorised numpy -- TEST INFRASTRUCTURE ONLY.
 
-Written from the Fortran (legacy/fortran/electromagfdtd.f95:244-325,
+Written from the Fortran (legacy/fortran/electromagfdtd.f95:244-325, :519-612,
 legacy/fortran/seismicfdtd.f95:243-384) with whole-array slices instead of
 loops, so that an indexing slip in one restatement shows up as a mismatch
 against the other (fdtd_oracle.cpp).  Arrays are (NZ, NX) = [k, i].
@@ -22,8 +22,23 @@ def _axes(prof, NX, NZ):
 
 
 def electromag2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None):
-    X, Z = _axes(prof, NX, NZ)
     eps11, eps13, eps33, sig11, sig13, sig33 = np.asarray(mat, dtype=np.float64)
+    return _em2(NX, NZ, dx, dz, dt, prof, eps11, eps13, eps33, sig11, sig13, sig33, src_ik, srcfn, nsteps, rec,
+                np.float64)
+
+
+def electromag2c(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None):
+    """electromagfdtd.f95:329-616: electromag2 with complex permittivities.
+    mat = eps11 re, im, eps13 re, im, eps33 re, im, sig11, sig13, sig33;
+    the fields, memory variables and traces come back complex."""
+    m = np.asarray(mat, dtype=np.float64)
+    eps11, eps13, eps33 = m[0] + 1j * m[1], m[2] + 1j * m[3], m[4] + 1j * m[5]
+    return _em2(NX, NZ, dx, dz, dt, prof, eps11, eps13, eps33, m[6], m[7], m[8], src_ik, srcfn, nsteps, rec,
+                np.complex128)
+
+
+def _em2(NX, NZ, dx, dz, dt, prof, eps11, eps13, eps33, sig11, sig13, sig33, src_ik, srcfn, nsteps, rec, dtype):
+    X, Z = _axes(prof, NX, NZ)
     epsx, epsz = (eps11 + eps13) * EPS0, (eps13 + eps33) * EPS0
     sigx, sigz = sig11 + sig13, sig13 + sig33
     caEx = (1 - sigx * dt / (2 * epsx)) / (1 + sigx * dt / (2 * epsx))
@@ -31,8 +46,8 @@ def electromag2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None):
     caEz = (1 - sigz * dt / (2 * epsz)) / (1 + sigz * dt / (2 * epsz))
     cbEz = (dt / epsz) / (1 + sigz * dt / (2 * epsz))
     dbH = dt / MU0
-    Ex, Ez, Hy = (np.zeros((NZ, NX)) for _ in range(3))
-    mExz, mEzx, mHyz, mHyx = (np.zeros((NZ, NX)) for _ in range(4))
+    Ex, Ez, Hy = (np.zeros((NZ, NX), dtype=dtype) for _ in range(3))
+    mExz, mEzx, mHyz, mHyx = (np.zeros((NZ, NX), dtype=dtype) for _ in range(4))
     si, sk = src_ik
     out = []
     Kx, ax, bx, Kxh, axh, bxh = (X[q][None, :] for q in range(6))

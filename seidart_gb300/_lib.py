@@ -12,8 +12,9 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libseidart_gb300.so"
 
-SEISMIC2, SEISMIC25, ELECTROMAG2, ELECTROMAG25 = 1, 2, 3, 4
-KIND_NAMES = {SEISMIC2: "seismic2", SEISMIC25: "seismic25", ELECTROMAG2: "electromag2", ELECTROMAG25: "electromag25"}
+SEISMIC2, SEISMIC25, ELECTROMAG2, ELECTROMAG25, ELECTROMAG2C = 1, 2, 3, 4, 5
+KIND_NAMES = {SEISMIC2: "seismic2", SEISMIC25: "seismic25", ELECTROMAG2: "electromag2", ELECTROMAG25: "electromag25",
+              ELECTROMAG2C: "electromag2c"}
 KIND_BY_NAME = {v: k for k, v in KIND_NAMES.items()}
 
 SFD_OK, SFD_ERR_BAD_ARG, SFD_ERR_STATE, SFD_ERR_CUDA, SFD_ERR_UNSTABLE, SFD_ERR_TIMEOUT = 0, -1, -2, -3, -4, -5

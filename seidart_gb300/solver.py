@@ -20,7 +20,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib
-from ._lib import ELECTROMAG2, ELECTROMAG25, SEISMIC2, SEISMIC25, SfdConfig, check
+from ._lib import ELECTROMAG2, ELECTROMAG25, ELECTROMAG2C, SEISMIC2, SEISMIC25, SfdConfig, check
 
 MODEL_PLANES = {
     SEISMIC2: ["c11", "c13", "c15", "c33", "c35", "c55", "rho", "gamma_x", "gamma_z"],
@@ -29,15 +29,19 @@ MODEL_PLANES = {
     ELECTROMAG2: ["eps11", "eps13", "eps33", "sig11", "sig13", "sig33"],
     ELECTROMAG25: ["eps11", "eps12", "eps13", "eps22", "eps23", "eps33",
                    "sig11", "sig12", "sig13", "sig22", "sig23", "sig33"],
+    # complex permittivities as (real, imaginary) plane pairs
+    ELECTROMAG2C: ["eps11_re", "eps11_im", "eps13_re", "eps13_im", "eps33_re", "eps33_im", "sig11", "sig13", "sig33"],
 }
 FIELDS = {
     SEISMIC2: ["vx", "vz", "sigmaxx", "sigmazz", "sigmaxz"],
     SEISMIC25: ["vx", "vy", "vz", "sigmaxx", "sigmayy", "sigmazz", "sigmaxy", "sigmaxz", "sigmayz"],
     ELECTROMAG2: ["Ex", "Ez", "Hy"],
     ELECTROMAG25: ["Ex", "Ey", "Ez", "Hx", "Hy", "Hz"],
+    ELECTROMAG2C: ["Ex_re", "Ex_im", "Ez_re", "Ez_im", "Hy_re", "Hy_im"],
 }
 CHANNELS = {SEISMIC2: ["vx", "vz"], SEISMIC25: ["vx", "vy", "vz"],
-            ELECTROMAG2: ["Ex", "Ez"], ELECTROMAG25: ["Ex", "Ey", "Ez"]}
+            ELECTROMAG2: ["Ex", "Ez"], ELECTROMAG25: ["Ex", "Ey", "Ez"],
+            ELECTROMAG2C: ["Ex_re", "Ex_im", "Ez_re", "Ez_im"]}
 MEMORY = {
     ELECTROMAG2: ["dEx_dz", "dEz_dx", "dHy_dz", "dHy_dx"],
     SEISMIC2: ["dvx_dx", "dvz_dz", "dvx_dz", "dvz_dx", "dsigmaxx_dx", "dsigmazz_dz", "dsigmaxz_dx", "dsigmaxz_dz"],
@@ -46,6 +50,8 @@ MEMORY = {
                 "dsigmaxz_dz", "dsigmayz_dy", "dsigmayz_dz"],
     ELECTROMAG25: ["dEz_dy", "dEy_dz", "dEx_dz", "dEz_dx", "dEx_dy", "dEy_dx",
                    "dHz_dy", "dHy_dz", "dHz_dx", "dHx_dz", "dHx_dy", "dHy_dx"],
+    ELECTROMAG2C: ["dEx_dz_re", "dEx_dz_im", "dEz_dx_re", "dEz_dx_im", "dHy_dz_re", "dHy_dz_im", "dHy_dx_re",
+                   "dHy_dx_im"],
 }
 
 

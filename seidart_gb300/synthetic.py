@@ -16,7 +16,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import cpml as cp
-from ._lib import ELECTROMAG2, ELECTROMAG25, SEISMIC2, SEISMIC25
+from ._lib import ELECTROMAG2, ELECTROMAG25, ELECTROMAG2C, SEISMIC2, SEISMIC25
 from .solver import GridSpec, is_25d
 
 
@@ -265,6 +265,18 @@ def small_case(kind: int, seed: int = 0, nx: int = 48, nz: int = 40, ny: int = 2
         cfl = 0.4
         seismic = True
         f0 = 300.0
+    elif kind == ELECTROMAG2C:  # complex permittivities with small loss (negative imaginary) parts
+        e11, e33 = 2.0 * noise(0.3), 2.2 * noise(0.3)
+        e13 = 0.03 * rng.uniform(0, 1, shape2)
+        im = lambda e: -0.02 * e * rng.uniform(0, 1, shape2)
+        s11 = 10 ** rng.uniform(-5, -2.5, shape2)
+        s33 = 10 ** rng.uniform(-5, -2.5, shape2)
+        s13 = 1e-4 * rng.uniform(0, 1, shape2)
+        planes = np.stack([e11, im(e11), e13, 0.1 * im(e13), e33, im(e33), s11, s13, s33])
+        vmax = cp.CLIGHT / math.sqrt(min(e11.min(), e33.min()))
+        cfl = 0.6
+        seismic = False
+        f0 = 400e6
     elif kind == ELECTROMAG2:
         e11, e33 = 2.0 * noise(0.3), 2.2 * noise(0.3)
         e13 = 0.03 * rng.uniform(0, 1, shape2)

@@ -8,7 +8,7 @@ import pytest
 import oracle
 from oracle import numpy_ref
 from helpers import rel_l2, run_oracle
-from seidart_gb300 import ELECTROMAG2, ELECTROMAG25, SEISMIC2, SEISMIC25
+from seidart_gb300 import ELECTROMAG2, ELECTROMAG25, ELECTROMAG2C, SEISMIC2, SEISMIC25
 from seidart_gb300 import cpml as cp
 from seidart_gb300 import synthetic as sy
 from seidart_gb300.solver import GridSpec
@@ -30,7 +30,39 @@ def test_loop_and_slice_restatements_agree(kind, fn, seed, nx, nz):
     assert rel_l2(tr, T) < 1e-13
 
 
-@pytest.mark.parametrize("kind", [ELECTROMAG2, SEISMIC2, SEISMIC25, ELECTROMAG25])
+@pytest.mark.parametrize("seed,nx,nz", [(1, 37, 29), (2, 26, 41)])
+def test_complex_em_restatements_agree(seed, nx, nz):
+    """electromag2c (complex permittivities): the C++ loops against the numpy
+    slices; complex values travel as (real, imaginary) plane pairs."""
+    c = sy.small_case(ELECTROMAG2C, seed=seed, nx=nx, nz=nz, npml=5, nstep=120)
+    g = c.grid
+    prof = cp.pack_profiles(c.profiles)
+    st, tr, _, blew = run_oracle(c)
+    assert not blew
+    F, M, T = numpy_ref.electromag2c(g.nx, g.nz, g.dx, g.dz, g.dt, prof, c.planes, (c.src_ijk[0], c.src_ijk[2]),
+                                     c.srcfn, c.nstep, rec=c.rec_ijk)
+    split = lambda a: np.stack([v for z in a for v in (z.real, z.imag)])
+    assert np.abs(F.imag).max() > 1e-3 * np.abs(F.real).max()  # the imaginary parts matter
+    assert rel_l2(st.fields, split(F)) < 1e-13
+    assert rel_l2(st.memory, split(M), floor=1e-300) < 1e-13
+    assert rel_l2(tr, np.stack([T[:, 0].real, T[:, 0].imag, T[:, 1].real, T[:, 1].imag], axis=1)) < 1e-13
+
+
+def test_complex_em_with_real_permittivity_is_electromag2():
+    c = sy.small_case(ELECTROMAG2C, seed=4, nx=30, nz=28, npml=5, nstep=80)
+    c.planes[[1, 3, 5]] = 0.0
+    st, tr, _, _ = run_oracle(c)
+    r = sy.small_case(ELECTROMAG2, seed=4, nx=30, nz=28, npml=5, nstep=80)
+    r.planes = np.ascontiguousarray(c.planes[[0, 2, 4, 6, 7, 8]])
+    g = c.grid
+    r.grid = GridSpec(ELECTROMAG2, g.nx, g.nz, g.dx, g.dz, g.dt, g.npml)
+    r.profiles, r.srcfn, r.src_ijk, r.rec_ijk = c.profiles, c.srcfn, c.src_ijk, c.rec_ijk
+    st_r, tr_r, _, _ = run_oracle(r)
+    assert np.array_equal(st.fields[[0, 2, 4]], st_r.fields) and not st.fields[[1, 3, 5]].any()
+    assert np.array_equal(tr[:, [0, 2]], tr_r)
+
+
+@pytest.mark.parametrize("kind", [ELECTROMAG2, SEISMIC2, SEISMIC25, ELECTROMAG25, ELECTROMAG2C])
 def test_split_runs_equal_one_run(kind):
     c = sy.small_case(kind, seed=3, nx=30, nz=26, ny=18, npml=4, nstep=60)
     st1, tr1, _, _ = run_oracle(c)
