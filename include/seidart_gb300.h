@@ -52,6 +52,7 @@ extern "C" {
 #define SFD_SEISMIC25 2    /* seismicfdtd.f95:388-949   */
 #define SFD_ELECTROMAG2 3  /* electromagfdtd.f95:10-326 */
 #define SFD_ELECTROMAG25 4 /* electromagfdtd.f95:619-1092 */
+#define SFD_ELECTROMAG2C 5 /* electromagfdtd.f95:329-616: electromag2 with complex permittivities */
 
 /* Return codes. */
 #define SFD_OK 0
@@ -102,7 +103,10 @@ const char* sfd_last_error(void);
  *                   (electromagfdtd.f95:146-151)
  *   ELECTROMAG25 12: eps11 eps12 eps13 eps22 eps23 eps33
  *                    sig11 sig12 sig13 sig22 sig23 sig33
- *                    (electromagfdtd.f95:729-740) */
+ *                    (electromagfdtd.f95:729-740)
+ *   ELECTROMAG2C  9: eps11 re, im, eps13 re, im, eps33 re, im, sig11 sig13
+ *                    sig33 (complex eps read by material_rwc,
+ *                    readwrite_routines.f95:969-988; :424-429) */
 int32_t sfd_model_planes(int32_t kind);
 
 /* Number of fields and receiver channels of a kind.
@@ -110,7 +114,9 @@ int32_t sfd_model_planes(int32_t kind);
  *   SEISMIC25:    vx vy vz sigmaxx sigmayy sigmazz sigmaxy sigmaxz sigmayz
  *                                                               channels vx vy vz
  *   ELECTROMAG2:  Ex Ez Hy                                      channels Ex Ez
- *   ELECTROMAG25: Ex Ey Ez Hx Hy Hz                             channels Ex Ey Ez */
+ *   ELECTROMAG25: Ex Ey Ez Hx Hy Hz                             channels Ex Ey Ez
+ *   ELECTROMAG2C: Ex re, im, Ez re, im, Hy re, im  channels Ex re, Ex im, Ez re, Ez im
+ *                 (memory variables likewise in real/imaginary pairs) */
 int32_t sfd_num_fields(int32_t kind);
 int32_t sfd_num_channels(int32_t kind);
 /* Number of CPML memory variables (the Fortran memory_* arrays). */
@@ -140,7 +146,9 @@ int32_t sfd_set_cpml(sfd_handle* h, const double* profiles, int64_t count);
  * functions srcfn, host FP64, ncomp x nstep values, component-major
  * (x, z in 2-D; x, y, z in 2.5-D).  The value added at step t is
  * srcfn[c][t] * dt / rho (seismic) or * dt / eps_ii (EM), as in
- * seismicfdtd.f95:360-361 and electromagfdtd.f95:300-301.  Requires the model. */
+ * seismicfdtd.f95:360-361 and electromagfdtd.f95:300-301.  ELECTROMAG2C
+ * takes 2 real components (x, z) divided by the complex eps11, eps33
+ * (:581-582).  Requires the model. */
 int32_t sfd_set_source(sfd_handle* h, int32_t i, int32_t j, int32_t k, const double* srcfn,
                        int32_t ncomp, int32_t nstep);
 

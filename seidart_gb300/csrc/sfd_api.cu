@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <complex>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -98,16 +99,23 @@ int nfields(int kind) {
     case SFD_SEISMIC25: return 9;
     case SFD_ELECTROMAG2: return 3;
     case SFD_ELECTROMAG25: return 6;
+    case SFD_ELECTROMAG2C: return 6;  // Ex Ez Hy, real and imaginary planes
   }
   return 0;
 }
-int nchan(int kind) { return (kind == SFD_SEISMIC25 || kind == SFD_ELECTROMAG25) ? 3 : 2; }
+int nchan(int kind) {
+  if (kind == SFD_ELECTROMAG2C) return 4;  // Ex re, Ex im, Ez re, Ez im
+  return (kind == SFD_SEISMIC25 || kind == SFD_ELECTROMAG25) ? 3 : 2;
+}
+// Source components the caller gives (real time functions, x [y] z).
+int nsrc(int kind) { return kind == SFD_ELECTROMAG2C ? 2 : nchan(kind); }
 int nplanes(int kind) {
   switch (kind) {
     case SFD_SEISMIC2: return 9;
     case SFD_SEISMIC25: return 25;
     case SFD_ELECTROMAG2: return 6;
     case SFD_ELECTROMAG25: return 12;
+    case SFD_ELECTROMAG2C: return 9;
   }
   return 0;
 }
@@ -120,6 +128,7 @@ const char* mem_axes(int kind) {
     case SFD_SEISMIC2: return "xzzxxzxz";             // dvx_dx dvz_dz dvx_dz dvz_dx dsxx_dx dszz_dz dsxz_dx dsxz_dz
     case SFD_SEISMIC25: return "xyzxyzxyzxyzxyxzyz";  // dv{x,y,z}_d{x,y,z}, dsxx_dx dsyy_dy dszz_dz dsxy_dx dsxy_dy dsxz_dx dsxz_dz dsyz_dy dsyz_dz
     case SFD_ELECTROMAG25: return "yzzxyxyzxzyx";     // dEz_dy dEy_dz dEx_dz dEz_dx dEx_dy dEy_dx dHz_dy dHy_dz dHz_dx dHx_dz dHx_dy dHy_dx
+    case SFD_ELECTROMAG2C: return "zzxxzzxx";         // dEx_dz dEz_dx dHy_dz dHy_dx, each real then imaginary
   }
   return "";
 }
@@ -129,6 +138,7 @@ int ncoef(int kind) {
     case SFD_SEISMIC25: return 39;  // 33 averaged C x dt (stress loops), 3 dt/rho_avg, 3 (1 - gamma)
     case SFD_ELECTROMAG2: return 4;
     case SFD_ELECTROMAG25: return 6;
+    case SFD_ELECTROMAG2C: return 8;  // CAx CBx CAz CBz, each real then imaginary
   }
   return 0;
 }
@@ -172,7 +182,7 @@ int grid_slots(const sfd_config& c, int P, int ysplit) {
 
 int validate_cfg(const sfd_config* c) {
   if (!c) return fail(SFD_ERR_BAD_ARG, "config is NULL");
-  if (c->kind < SFD_SEISMIC2 || c->kind > SFD_ELECTROMAG25) return fail(SFD_ERR_BAD_ARG, "unknown solver kind %d", c->kind);
+  if (c->kind < SFD_SEISMIC2 || c->kind > SFD_ELECTROMAG2C) return fail(SFD_ERR_BAD_ARG, "unknown solver kind %d", c->kind);
   const bool three = is3(c->kind);
   if (c->npml < 1) return fail(SFD_ERR_BAD_ARG, "npml must be >= 1 (got %d)", c->npml);
   if (c->nx < 2 * c->npml + 2 || c->nz < 2 * c->npml + 2)
@@ -253,7 +263,7 @@ struct sfd_handle_s {
   int res_state = 0;    // on-chip runs: 0 not yet checked, 1 usable, -1 not usable
   ResPlan res_plan;
   int64_t step = 0;
-  std::vector<double> src_scale[3];  // planes the source amplitude is divided by
+  std::vector<double> src_scale[4];  // planes the source amplitude is divided by (complex: re, im pairs)
   std::vector<double> model;         // FP64 model planes (kept for the adjoint's chain rule)
   // adjoint workspace (electromag2)
   char* adj = nullptr;
@@ -262,6 +272,7 @@ struct sfd_handle_s {
   const float* adj_resid = nullptr;
   int adj_res_state = 0;  // on-chip adjoint sweeps: 0 not yet checked, 1 usable, -1 not usable
   Em2Args em2;
+  Em2cArgs em2c;
   Seis2Args s2;
   Seis25Args s25;
   Em25Args em25;
@@ -333,6 +344,20 @@ void bind_args(sfd_handle* h) {
       }
       h->zb = single_pass_zb(c.kind, NX, NZ);
       if (h->single) h->launch1 = em2_step_launch(h->em2s[0], h->zb);
+      break;
+    }
+    case SFD_ELECTROMAG2C: {
+      Em2cArgs& a = h->em2c;
+      a.NX = NX; a.NZ = NZ; a.P = L.P; a.W = L.W;
+      for (int q = 0; q < 2; ++q) {
+        a.Ex[q] = h->fc(q, 0); a.Ez[q] = h->fc(2 + q, 0); a.Hy[q] = h->fc(4 + q, 0);
+        a.mExz[q] = h->mc(q, 0); a.mEzx[q] = h->mc(2 + q, 0); a.mHyz[q] = h->mc(4 + q, 0); a.mHyx[q] = h->mc(6 + q, 0);
+        a.CAx[q] = h->coef(q); a.CBx[q] = h->coef(2 + q); a.CAz[q] = h->coef(4 + q); a.CBz[q] = h->coef(6 + q);
+      }
+      a.X = make_axis(h->axis(0), NX); a.Z = make_axis(h->axis(1), NZ);
+      a.dbH = (float)(c.dt / kMu0);
+      a.io = io;
+      h->launch = em2c_launch(a);
       break;
     }
     case SFD_SEISMIC2: {
@@ -408,7 +433,7 @@ void bind_args(sfd_handle* h) {
 }
 
 void set_io_source(sfd_handle* h, int i, int j, int k) {
-  IoArgs* ios[8] = {&h->em2.io, &h->s2.io, &h->s25.io, &h->em25.io,
+  IoArgs* ios[9] = {&h->em2.io, &h->s2.io, &h->s25.io, &h->em25.io, &h->em2c.io,
                     &h->em2s[0].io, &h->em2s[1].io, &h->s2s[0].io, &h->s2s[1].io};
   for (IoArgs* io : ios) { io->si = i; io->sj = j; io->sk = k; }
 }
@@ -431,6 +456,7 @@ void launch_half(sfd_handle* h, int which, int rel, cudaStream_t s) {
     case SFD_SEISMIC2: which == 0 ? seis2_half1(h->s2, L, rel, s) : seis2_half2(h->s2, L, rel, s); break;
     case SFD_SEISMIC25: which == 0 ? seis25_half1(h->s25, L, rel, s) : seis25_half2(h->s25, L, rel, s); break;
     case SFD_ELECTROMAG25: which == 0 ? em25_half1(h->em25, L, rel, s) : em25_half2(h->em25, L, rel, s); break;
+    case SFD_ELECTROMAG2C: which == 0 ? em2c_half1(h->em2c, L, rel, s) : em2c_half2(h->em2c, L, rel, s); break;
   }
 }
 
@@ -445,6 +471,7 @@ void launch_finalize(sfd_handle* h, int t_last, cudaStream_t s) {
     case SFD_SEISMIC2: seis2_finalize(h->s2, t_last, s); break;
     case SFD_SEISMIC25: seis25_finalize(h->s25, t_last, s); break;
     case SFD_ELECTROMAG25: em25_finalize(h->em25, t_last, s); break;
+    case SFD_ELECTROMAG2C: em2c_finalize(h->em2c, t_last, s); break;
   }
 }
 
@@ -692,6 +719,45 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
       h->src_scale[1].assign(e33, e33 + N2);
       break;
     }
+    case SFD_ELECTROMAG2C: {
+      // electromagfdtd.f95:439-451 with complex eps (material_rwc), then the
+      // staggered averages of :563 (Ex points, k >= 1) and :574 (Ez points, i >= 1)
+      using cd = std::complex<double>;
+      std::vector<cd> ca[2], cb[2];
+      for (int d = 0; d < 2; ++d) { ca[d].resize(N2); cb[d].resize(N2); }
+      for (size_t q = 0; q < N2; ++q) {
+        const cd e11(P(0)[q], P(1)[q]), e13(P(2)[q], P(3)[q]), e33(P(4)[q], P(5)[q]);
+        const double s11 = P(6)[q], s13 = P(7)[q], s33 = P(8)[q];
+        const cd ep[2] = {(e11 + e13) * kEps0, (e13 + e33) * kEps0};
+        const double sg[2] = {s11 + s13, s13 + s33};
+        for (int d = 0; d < 2; ++d) {
+          if (!(ep[d].real() > 0)) return fail(SFD_ERR_BAD_ARG, "permittivity must have a positive real part (cell %zu)", q);
+          ca[d][q] = (1.0 - sg[d] * dt / (2.0 * ep[d])) / (1.0 + sg[d] * dt / (2.0 * ep[d]));
+          cb[d][q] = (dt / ep[d]) / (1.0 + sg[d] * dt / (2.0 * ep[d]));
+        }
+        if (std::norm(e11) == 0.0 || std::norm(e33) == 0.0)
+          return fail(SFD_ERR_BAD_ARG, "eps11 and eps33 must be nonzero (cell %zu)", q);
+      }
+      for (int k = 0; k < NZ; ++k)
+        for (int i = 0; i < NX; ++i) {
+          const size_t n = (size_t)i + (size_t)NX * k;
+          if (k >= 1) {
+            const cd a = (ca[0][n] + ca[0][n - NX]) / 2.0, b = (cb[0][n] + cb[0][n - NX]) / 2.0;
+            out[0][n] = (float)a.real(); out[1][n] = (float)a.imag();
+            out[2][n] = (float)b.real(); out[3][n] = (float)b.imag();
+          }
+          if (i >= 1) {
+            const cd a = (ca[1][n] + ca[1][n - 1]) / 2.0, b = (cb[1][n] + cb[1][n - 1]) / 2.0;
+            out[4][n] = (float)a.real(); out[5][n] = (float)a.imag();
+            out[6][n] = (float)b.real(); out[7][n] = (float)b.imag();
+          }
+        }
+      for (int d = 0; d < 2; ++d) {  // the source divides by eps11 (Ex) and eps33 (Ez), :581-582
+        h->src_scale[2 * d].assign(P(4 * d), P(4 * d) + N2);
+        h->src_scale[2 * d + 1].assign(P(4 * d + 1), P(4 * d + 1) + N2);
+      }
+      break;
+    }
     case SFD_ELECTROMAG25: {
       // electromagfdtd.f95:756-789
       const double *e11 = P(0), *e12 = P(1), *e13 = P(2), *e22 = P(3), *e23 = P(4), *e33 = P(5);
@@ -869,17 +935,28 @@ int32_t sfd_set_source(sfd_handle* h, int32_t i, int32_t j, int32_t k, const dou
   if (!h || !srcfn) return fail(SFD_ERR_BAD_ARG, "NULL argument");
   const sfd_config& c = h->cfg;
   if (!h->have_model) return fail(SFD_ERR_STATE, "sfd_set_source needs the model (sfd_set_model) first");
-  if (ncomp != nchan(c.kind)) return fail(SFD_ERR_BAD_ARG, "source needs %d components, got %d", nchan(c.kind), ncomp);
+  if (ncomp != nsrc(c.kind)) return fail(SFD_ERR_BAD_ARG, "source needs %d components, got %d", nsrc(c.kind), ncomp);
   if (nstep < 1 || nstep > c.nstep) return fail(SFD_ERR_BAD_ARG, "source length %d outside [1, %d]", nstep, c.nstep);
   const bool three = is3(c.kind);
   if (i < 1 || i > c.nx - 3 || k < 1 || k > c.nz - 3 || (three && (j < 1 || j > c.ny - 3)) || (!three && j != 0))
     return fail(SFD_ERR_BAD_ARG, "source cell (%d,%d,%d) must lie inside the grid, away from its outer two planes", i, j, k);
   if (!all_finite(srcfn, (size_t)ncomp * nstep)) return fail(SFD_ERR_BAD_ARG, "source contains NaN or Inf");
   const size_t n = (size_t)i + (size_t)c.nx * k;
-  std::vector<float> amp((size_t)ncomp * c.nstep, 0.0f);
-  for (int q = 0; q < ncomp; ++q) {
-    const double s = h->src_scale[q][n];
-    for (int t = 0; t < nstep; ++t) amp[(size_t)q * c.nstep + t] = (float)(srcfn[(size_t)q * nstep + t] * c.dt / s);
+  std::vector<float> amp((size_t)nchan(c.kind) * c.nstep, 0.0f);
+  if (c.kind == SFD_ELECTROMAG2C) {  // a dt / eps with complex eps: rows Ex re, Ex im, Ez re, Ez im
+    for (int q = 0; q < 2; ++q) {
+      const std::complex<double> e(h->src_scale[2 * q][n], h->src_scale[2 * q + 1][n]);
+      for (int t = 0; t < nstep; ++t) {
+        const std::complex<double> v = srcfn[(size_t)q * nstep + t] * c.dt / e;
+        amp[(size_t)(2 * q) * c.nstep + t] = (float)v.real();
+        amp[(size_t)(2 * q + 1) * c.nstep + t] = (float)v.imag();
+      }
+    }
+  } else {
+    for (int q = 0; q < ncomp; ++q) {
+      const double s = h->src_scale[q][n];
+      for (int t = 0; t < nstep; ++t) amp[(size_t)q * c.nstep + t] = (float)(srcfn[(size_t)q * nstep + t] * c.dt / s);
+    }
   }
   CK(cudaMemcpyAsync(h->base + h->L.off_src, amp.data(), sizeof(float) * amp.size(), cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));

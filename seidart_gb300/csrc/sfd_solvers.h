@@ -30,6 +30,18 @@ struct Em2Args {
   IoArgs io;
 };
 
+// electromag2c: complex permittivities (electromagfdtd.f95:329-616).  Every
+// complex array is a pair of planes, [0] real and [1] imaginary.
+struct Em2cArgs {
+  int NX, NZ, P, W;
+  float *Ex[2], *Ez[2], *Hy[2];
+  float *mExz[2], *mEzx[2], *mHyz[2], *mHyx[2];  // z-, x-, z-, x-strip
+  const float *CAx[2], *CBx[2], *CAz[2], *CBz[2];  // staggered averages of the complex coefficients
+  AxisTab X, Z;
+  float dbH;
+  IoArgs io;  // source rows and trace channels: Ex re, Ex im, Ez re, Ez im
+};
+
 struct Seis2Args {
   int NX, NZ, P, W;
   int atten;
@@ -116,6 +128,10 @@ struct Launch {
   int nslots;
 };
 
+Launch em2c_launch(const Em2cArgs& a);
+void em2c_half1(const Em2cArgs& a, const Launch& L, int rel, cudaStream_t s);
+void em2c_half2(const Em2cArgs& a, const Launch& L, int rel, cudaStream_t s);
+void em2c_finalize(const Em2cArgs& a, int t_last, cudaStream_t s);
 Launch em2_launch(const Em2Args& a);
 void em2_half1(const Em2Args& a, const Launch& L, int rel, cudaStream_t s);
 void em2_half2(const Em2Args& a, const Launch& L, int rel, cudaStream_t s);

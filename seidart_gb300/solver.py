@@ -236,6 +236,16 @@ class FDTDSolver:
             raise ValueError("minmax must be a float32 CUDA tensor of 2 values")
         check(self._L.sfd_encode_field_i16(self._h, q, C.c_void_p(codes.data_ptr()), C.c_void_p(minmax.data_ptr())))
 
+    def complex_field(self, name) -> np.ndarray:
+        """Field ``name`` ('Ex', 'Ez', 'Hy') of a complex-permittivity solver
+        (ELECTROMAG2C) as complex64, from its real and imaginary planes."""
+        return (self.field(name + "_re") + 1j * self.field(name + "_im")).astype(np.complex64)
+
+    def complex_traces(self) -> np.ndarray:
+        """Traces (nstep, 2, nrec) of Ex, Ez of an ELECTROMAG2C solver, complex64."""
+        t = self.traces()
+        return (t[:, 0::2] + 1j * t[:, 1::2]).astype(np.complex64)
+
     def memory(self, name) -> np.ndarray:
         q = MEMORY[self.kind].index(name) if isinstance(name, str) else int(name)
         out = np.empty(self.grid.shape, dtype=np.float32)
