@@ -4,16 +4,19 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <complex>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
 
 #include "../../include/seidart_gb300.h"
+#include "host_pool.h"
 #include "adjoint.h"
 #include "batch.h"
 #include "resident.h"
@@ -263,8 +266,14 @@ struct sfd_handle_s {
   int res_state = 0;    // on-chip runs: 0 not yet checked, 1 usable, -1 not usable
   ResPlan res_plan;
   int64_t step = 0;
-  std::vector<double> src_scale[4];  // planes the source amplitude is divided by (complex: re, im pairs)
-  std::vector<double> model;         // FP64 model planes (kept for the adjoint's chain rule)
+  // The FP64 model planes read after sfd_set_model (the source scaling; for
+  // electromag2 also the adjoint's chain rule), copied from its input:
+  // electromag2 all six planes; electromag2c eps11 eps33 (re, im);
+  // electromag25 eps11 eps22 eps33; seismic rho.  Shared, not copied, by
+  // sfd_share_model.
+  std::shared_ptr<double[]> model;
+  int src_plane[4] = {0, 0, 0, 0};  // planes of `model` the source amplitude is divided by (complex: re, im pairs)
+  const double* src_scale(int q) const { return model.get() + (size_t)src_plane[q] * cfg.nx * cfg.nz; }
   // adjoint workspace (electromag2)
   char* adj = nullptr;
   int adj_seg = 0;
@@ -576,10 +585,10 @@ void invalidate_graph(sfd_handle* h) {
     if (h->graph[p]) { cudaGraphExecDestroy(h->graph[p]); h->graph[p] = nullptr; }
 }
 
-// Host FP64 -> device FP32 with row pitch P (rows of NX values).
-int upload_pitched(sfd_handle* h, float* dst, const std::vector<float>& src, int rows) {
-  CK(cudaMemcpy2DAsync(dst, sizeof(float) * h->L.P, src.data(), sizeof(float) * h->cfg.nx,
-                       sizeof(float) * h->cfg.nx, rows, cudaMemcpyHostToDevice, h->stream));
+// Host rows of NX floats -> device rows of pitch P.
+int upload_pitched(sfd_handle* h, float* dst, const float* src, size_t rows) {
+  CK(cudaMemcpy2DAsync(dst, sizeof(float) * h->L.P, src, sizeof(float) * h->cfg.nx, sizeof(float) * h->cfg.nx, rows,
+                       cudaMemcpyHostToDevice, h->stream));
   return SFD_OK;
 }
 
@@ -589,10 +598,59 @@ bool check_strip(const double* v, int n, int W) {
   return true;
 }
 
+// f(begin, end) over [0, n) in contiguous chunks on the host pool, each
+// with at least `grain` items (the calling thread alone for small n).  The
+// model set-up's FP64 loops and copies run this way: a 1040 x 540
+// electromag2 model is 27 MB of input planes.
+template <class F>
+void parallel_for(size_t n, const F& f, size_t grain = 1u << 15) {
+  const size_t want = std::max<size_t>(1, n / std::max<size_t>(1, grain));
+  if (want <= 1) {
+    f((size_t)0, n);
+    return;
+  }
+  HostPool& pool = HostPool::get();
+  const size_t nt = std::min<size_t>(pool.size(), want);
+  const size_t chunk = (n + nt - 1) / nt;
+  pool.run((int)nt, [&](int t) {
+    const size_t b = std::min(n, (size_t)t * chunk), e = std::min(n, b + chunk);
+    if (b < e) f(b, e);
+  });
+}
+
+// rows [0, nrows) of `ncols` values each, split between threads by whole rows
+template <class F>
+void parallel_rows(int nrows, int ncols, const F& row) {
+  parallel_for((size_t)nrows, [&](size_t b, size_t e) {
+    for (size_t k = b; k < e; ++k) row((int)k);
+  }, std::max<size_t>(1, (1u << 15) / (size_t)std::max(1, ncols)));
+}
+
+// The lowest index reported by any thread (`none` if none was).
+struct FirstBad {
+  std::atomic<size_t> v;
+  explicit FirstBad(size_t none) : v(none) {}
+  void note(size_t q) {
+    size_t cur = v.load();
+    while (q < cur && !v.compare_exchange_weak(cur, q)) {
+    }
+  }
+};
+
+void par_copy(double* dst, const double* src, size_t n) {
+  parallel_for(n, [&](size_t b, size_t e) { std::memcpy(dst + b, src + b, sizeof(double) * (e - b)); });
+}
+
 bool all_finite(const double* v, size_t n) {
-  for (size_t i = 0; i < n; ++i)
-    if (!std::isfinite(v[i])) return false;
-  return true;
+  std::atomic<bool> ok{true};
+  parallel_for(n, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i)
+      if (!std::isfinite(v[i])) {
+        ok = false;
+        return;
+      }
+  });
+  return ok;
 }
 
 }  // namespace
@@ -682,28 +740,39 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
                 (long long)np * (long long)N2, (long long)count);
   if (!all_finite(planes, (size_t)count)) return fail(SFD_ERR_BAD_ARG, "model contains NaN or Inf");
   const double dt = c.dt;
+  // Host buffers are left uninitialised and first touched by the worker
+  // threads: zero-filling them on one thread cost more than the arithmetic.
   auto P = [&](int q) { return planes + (size_t)q * N2; };
   auto at = [&](const double* p, int i, int k) { return p[(size_t)i + (size_t)NX * k]; };
-  std::vector<std::vector<float>> out(ncoef(c.kind), std::vector<float>(N2, 0.0f));
+  const int nc = ncoef(c.kind);
+  std::unique_ptr<float[]> coefs(new float[(size_t)nc * N2]);
+  parallel_for((size_t)nc * N2, [&](size_t b, size_t e) { std::memset(coefs.get() + b, 0, sizeof(float) * (e - b)); });
+  std::vector<float*> out(nc);
+  for (int q = 0; q < nc; ++q) out[q] = coefs.get() + (size_t)q * N2;
+  std::vector<int> keep;             // input planes copied into the handle's model
+  int src_plane[4] = {0, 0, 0, 0};  // indices into `keep`
   int atten = 0;
   switch (c.kind) {
     case SFD_ELECTROMAG2: {
-      h->model.assign(planes, planes + (size_t)count);
       // electromagfdtd.f95:164-181
       const double *e11 = P(0), *e13 = P(1), *e33 = P(2), *s11 = P(3), *s13 = P(4), *s33 = P(5);
-      std::vector<double> ca[2], cb[2];
-      for (int d = 0; d < 2; ++d) { ca[d].resize(N2); cb[d].resize(N2); }
-      for (size_t q = 0; q < N2; ++q) {
-        const double ep[2] = {(e11[q] + e13[q]) * kEps0, (e13[q] + e33[q]) * kEps0};
-        const double sg[2] = {s11[q] + s13[q], s13[q] + s33[q]};
-        for (int d = 0; d < 2; ++d) {
-          if (!(ep[d] > 0)) return fail(SFD_ERR_BAD_ARG, "permittivity must be positive (cell %zu)", q);
-          ca[d][q] = (1.0 - sg[d] * dt / (2.0 * ep[d])) / (1.0 + sg[d] * dt / (2.0 * ep[d]));
-          cb[d][q] = (dt / ep[d]) / (1.0 + sg[d] * dt / (2.0 * ep[d]));
+      std::unique_ptr<double[]> ca[2], cb[2];
+      for (int d = 0; d < 2; ++d) { ca[d].reset(new double[N2]); cb[d].reset(new double[N2]); }
+      FirstBad bad(N2);  // first cell with a non-positive permittivity
+      parallel_rows(NZ, NX, [&](int k) {
+        for (size_t q = (size_t)NX * k; q < (size_t)NX * (k + 1); ++q) {
+          const double ep[2] = {(e11[q] + e13[q]) * kEps0, (e13[q] + e33[q]) * kEps0};
+          const double sg[2] = {s11[q] + s13[q], s13[q] + s33[q]};
+          for (int d = 0; d < 2; ++d) {
+            if (!(ep[d] > 0)) return bad.note(q);
+            ca[d][q] = (1.0 - sg[d] * dt / (2.0 * ep[d])) / (1.0 + sg[d] * dt / (2.0 * ep[d]));
+            cb[d][q] = (dt / ep[d]) / (1.0 + sg[d] * dt / (2.0 * ep[d]));
+          }
         }
-      }
+      });
+      if (bad.v < N2) return fail(SFD_ERR_BAD_ARG, "permittivity must be positive (cell %zu)", bad.v.load());
       // staggered averages at the Ex points (k >= 1) and the Ez points (i >= 1), :282, :294
-      for (int k = 0; k < NZ; ++k)
+      parallel_rows(NZ, NX, [&](int k) {
         for (int i = 0; i < NX; ++i) {
           const size_t n = (size_t)i + (size_t)NX * k;
           if (k >= 1) {
@@ -715,30 +784,37 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
             out[3][n] = (float)((cb[1][n] + cb[1][n - 1]) / 2);
           }
         }
-      h->src_scale[0].assign(e11, e11 + N2);
-      h->src_scale[1].assign(e33, e33 + N2);
+      });
+      keep = {0, 1, 2, 3, 4, 5};  // all six: the adjoint's chain rule reads them
+      src_plane[0] = 0;
+      src_plane[1] = 2;
       break;
     }
     case SFD_ELECTROMAG2C: {
       // electromagfdtd.f95:439-451 with complex eps (material_rwc), then the
       // staggered averages of :563 (Ex points, k >= 1) and :574 (Ez points, i >= 1)
       using cd = std::complex<double>;
-      std::vector<cd> ca[2], cb[2];
-      for (int d = 0; d < 2; ++d) { ca[d].resize(N2); cb[d].resize(N2); }
-      for (size_t q = 0; q < N2; ++q) {
-        const cd e11(P(0)[q], P(1)[q]), e13(P(2)[q], P(3)[q]), e33(P(4)[q], P(5)[q]);
-        const double s11 = P(6)[q], s13 = P(7)[q], s33 = P(8)[q];
-        const cd ep[2] = {(e11 + e13) * kEps0, (e13 + e33) * kEps0};
-        const double sg[2] = {s11 + s13, s13 + s33};
-        for (int d = 0; d < 2; ++d) {
-          if (!(ep[d].real() > 0)) return fail(SFD_ERR_BAD_ARG, "permittivity must have a positive real part (cell %zu)", q);
-          ca[d][q] = (1.0 - sg[d] * dt / (2.0 * ep[d])) / (1.0 + sg[d] * dt / (2.0 * ep[d]));
-          cb[d][q] = (dt / ep[d]) / (1.0 + sg[d] * dt / (2.0 * ep[d]));
+      std::unique_ptr<cd[]> ca[2], cb[2];
+      for (int d = 0; d < 2; ++d) { ca[d].reset(new cd[N2]); cb[d].reset(new cd[N2]); }
+      FirstBad bad_re(N2), bad_zero(N2);
+      parallel_rows(NZ, NX, [&](int k) {
+        for (size_t q = (size_t)NX * k; q < (size_t)NX * (k + 1); ++q) {
+          const cd e11(P(0)[q], P(1)[q]), e13(P(2)[q], P(3)[q]), e33(P(4)[q], P(5)[q]);
+          const double s11 = P(6)[q], s13 = P(7)[q], s33 = P(8)[q];
+          const cd ep[2] = {(e11 + e13) * kEps0, (e13 + e33) * kEps0};
+          const double sg[2] = {s11 + s13, s13 + s33};
+          for (int d = 0; d < 2; ++d) {
+            if (!(ep[d].real() > 0)) return bad_re.note(q);
+            ca[d][q] = (1.0 - sg[d] * dt / (2.0 * ep[d])) / (1.0 + sg[d] * dt / (2.0 * ep[d]));
+            cb[d][q] = (dt / ep[d]) / (1.0 + sg[d] * dt / (2.0 * ep[d]));
+          }
+          if (std::norm(e11) == 0.0 || std::norm(e33) == 0.0) return bad_zero.note(q);
         }
-        if (std::norm(e11) == 0.0 || std::norm(e33) == 0.0)
-          return fail(SFD_ERR_BAD_ARG, "eps11 and eps33 must be nonzero (cell %zu)", q);
-      }
-      for (int k = 0; k < NZ; ++k)
+      });
+      if (bad_re.v <= bad_zero.v && bad_re.v < N2)
+        return fail(SFD_ERR_BAD_ARG, "permittivity must have a positive real part (cell %zu)", bad_re.v.load());
+      if (bad_zero.v < N2) return fail(SFD_ERR_BAD_ARG, "eps11 and eps33 must be nonzero (cell %zu)", bad_zero.v.load());
+      parallel_rows(NZ, NX, [&](int k) {
         for (int i = 0; i < NX; ++i) {
           const size_t n = (size_t)i + (size_t)NX * k;
           if (k >= 1) {
@@ -752,29 +828,31 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
             out[6][n] = (float)b.real(); out[7][n] = (float)b.imag();
           }
         }
-      for (int d = 0; d < 2; ++d) {  // the source divides by eps11 (Ex) and eps33 (Ez), :581-582
-        h->src_scale[2 * d].assign(P(4 * d), P(4 * d) + N2);
-        h->src_scale[2 * d + 1].assign(P(4 * d + 1), P(4 * d + 1) + N2);
-      }
+      });
+      keep = {0, 1, 4, 5};  // eps11, eps33 (re, im): :581-582
+      for (int q = 0; q < 4; ++q) src_plane[q] = q;
       break;
     }
     case SFD_ELECTROMAG25: {
       // electromagfdtd.f95:756-789
       const double *e11 = P(0), *e12 = P(1), *e13 = P(2), *e22 = P(3), *e23 = P(4), *e33 = P(5);
       const double *s11 = P(6), *s12 = P(7), *s13 = P(8), *s22 = P(9), *s23 = P(10), *s33 = P(11);
-      for (size_t q = 0; q < N2; ++q) {
-        const double ep[3] = {(e11[q] + e12[q] + e13[q]) * kEps0, (e12[q] + e22[q] + e23[q]) * kEps0,
-                              (e13[q] + e23[q] + e33[q]) * kEps0};
-        const double sg[3] = {s11[q] + s12[q] + s13[q], s12[q] + s22[q] + s23[q], s13[q] + s23[q] + s33[q]};
-        for (int d = 0; d < 3; ++d) {
-          if (!(ep[d] > 0)) return fail(SFD_ERR_BAD_ARG, "permittivity must be positive (cell %zu)", q);
-          out[2 * d][q] = (float)((1.0 - sg[d] * dt / (2.0 * ep[d])) / (1.0 + sg[d] * dt / (2.0 * ep[d])));
-          out[2 * d + 1][q] = (float)((dt / ep[d]) / (1.0 + sg[d] * dt / (2.0 * ep[d])));
+      FirstBad bad(N2);
+      parallel_rows(NZ, NX, [&](int k) {
+        for (size_t q = (size_t)NX * k; q < (size_t)NX * (k + 1); ++q) {
+          const double ep[3] = {(e11[q] + e12[q] + e13[q]) * kEps0, (e12[q] + e22[q] + e23[q]) * kEps0,
+                                (e13[q] + e23[q] + e33[q]) * kEps0};
+          const double sg[3] = {s11[q] + s12[q] + s13[q], s12[q] + s22[q] + s23[q], s13[q] + s23[q] + s33[q]};
+          for (int d = 0; d < 3; ++d) {
+            if (!(ep[d] > 0)) return bad.note(q);
+            out[2 * d][q] = (float)((1.0 - sg[d] * dt / (2.0 * ep[d])) / (1.0 + sg[d] * dt / (2.0 * ep[d])));
+            out[2 * d + 1][q] = (float)((dt / ep[d]) / (1.0 + sg[d] * dt / (2.0 * ep[d])));
+          }
         }
-      }
-      h->src_scale[0].assign(e11, e11 + N2);
-      h->src_scale[1].assign(e22, e22 + N2);
-      h->src_scale[2].assign(e33, e33 + N2);
+      });
+      if (bad.v < N2) return fail(SFD_ERR_BAD_ARG, "permittivity must be positive (cell %zu)", bad.v.load());
+      keep = {0, 3, 5};  // eps11 eps22 eps33
+      for (int q = 0; q < 3; ++q) src_plane[q] = q;
       break;
     }
     case SFD_SEISMIC2: {
@@ -782,7 +860,11 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
       // loop-1 points (i <= NX-2, k >= 1): (c(i+1,k) + 2 c(i,k) + c(i,k-1)) / 4 for c11 c13 c15 c33 c35
       // loop-2 points (k <= NZ-2, i >= 1): (c(i,k+1) + 2 c(i,k) + c(i-1,k)) / 4 for c15 c35 c55
       const int A_src[5] = {0, 1, 2, 3, 4}, B_src[3] = {2, 4, 5};
-      for (int k = 0; k < NZ; ++k)
+      FirstBad bad(N2);
+      std::atomic<int> any_atten{0};
+      parallel_rows(NZ, NX, [&](int k) {
+        for (size_t n = (size_t)NX * k; n < (size_t)NX * (k + 1); ++n)
+          if (!(rho[n] > 0)) return bad.note(n);
         for (int i = 0; i < NX; ++i) {
           const size_t n = (size_t)i + (size_t)NX * k;
           if (i <= NX - 2 && k >= 1)
@@ -796,9 +878,7 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
               out[5 + q][n] = (float)((cc[n + NX] + 2 * cc[n] + cc[n - 1]) / 4 * dt);
             }
         }
-      for (size_t n = 0; n < N2; ++n)
-        if (!(rho[n] > 0)) return fail(SFD_ERR_BAD_ARG, "density must be positive (cell %zu)", n);
-      for (int k = 0; k < NZ; ++k)
+        int a = 0;
         for (int i = 0; i < NX; ++i) {
           const size_t n = (size_t)i + (size_t)NX * k;
           out[8][n] = (float)(dt / rho[n]);  // seismicfdtd.f95:334
@@ -806,10 +886,13 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
             out[9][n] = (float)(dt / ((2 * rho[n] + at(rho, i + 1, k) + at(rho, i, k + 1)) / 4));
           out[10][n] = (float)(1.0 - gx[n]);
           out[11][n] = (float)(1.0 - gz[n]);
-          if (gx[n] != 0.0 || gz[n] != 0.0) atten = 1;
+          if (gx[n] != 0.0 || gz[n] != 0.0) a = 1;
         }
-      h->src_scale[0].assign(rho, rho + N2);
-      h->src_scale[1].assign(rho, rho + N2);
+        if (a) any_atten = 1;
+      });
+      if (bad.v < N2) return fail(SFD_ERR_BAD_ARG, "density must be positive (cell %zu)", bad.v.load());
+      atten = any_atten.load();
+      keep = {6};  // rho
       set_atten(h, atten);
       break;
     }
@@ -828,9 +911,13 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
           {2, 5, 0.25}, {2, 10, 0.25}, {2, 14, 0.25}, {2, 17, 0.125}, {2, 19, 0.125}, {2, 20, 0.125}, // q16 q26 q36 q46 q56 q66
           {3, 4, 0.25}, {3, 9, 0.25}, {3, 13, 0.25}, {3, 16, 0.125}, {3, 18, 0.125}, {3, 19, 0.125},  // r15 r25 r35 r45 r55 r56
           {4, 3, 0.25}, {4, 8, 0.25}, {4, 12, 0.25}, {4, 15, 0.125}, {4, 16, 0.125}, {4, 17, 0.125}}; // s14 s24 s34 s44 s45 s46
-      for (int q = 0; q < 33; ++q) {
-        const double* C = P(avg[q].cij);
-        for (int k = 0; k < NZ; ++k)
+      FirstBad bad(N2);
+      std::atomic<int> any_atten{0};
+      parallel_rows(NZ, NX, [&](int k) {
+        for (size_t n = (size_t)NX * k; n < (size_t)NX * (k + 1); ++n)
+          if (!(rho[n] > 0)) return bad.note(n);
+        for (int q = 0; q < 33; ++q) {
+          const double* C = P(avg[q].cij);
           for (int i = 0; i < NX; ++i) {
             double v = 0.0;
             switch (avg[q].loop) {
@@ -849,10 +936,8 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
             }
             out[q][(size_t)i + (size_t)NX * k] = (float)(avg[q].f * v * dt);
           }
-      }
-      for (size_t n = 0; n < N2; ++n)
-        if (!(rho[n] > 0)) return fail(SFD_ERR_BAD_ARG, "density must be positive (cell %zu)", n);
-      for (int k = 0; k < NZ; ++k)
+        }
+        int a = 0;
         for (int i = 0; i < NX; ++i) {
           const size_t n = (size_t)i + (size_t)NX * k;
           const double r = rho[n];
@@ -865,19 +950,27 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
           for (int d = 0; d < 3; ++d) {
             const double g = P(22 + d)[n];
             out[36 + d][n] = (float)(1.0 - g);
-            if (g != 0.0) atten = 1;
+            if (g != 0.0) a = 1;
           }
         }
-      for (int d = 0; d < 3; ++d) h->src_scale[d].assign(rho, rho + N2);
+        if (a) any_atten = 1;
+      });
+      if (bad.v < N2) return fail(SFD_ERR_BAD_ARG, "density must be positive (cell %zu)", bad.v.load());
+      atten = any_atten.load();
+      keep = {21};  // rho
       set_atten(h, atten);
       break;
     }
   }
-  for (int q = 0; q < ncoef(c.kind); ++q) {
-    int r = upload_pitched(h, h->coef(q), out[q], NZ);
+  {  // the coefficient planes lie back to back on the device, pitch P
+    int r = upload_pitched(h, h->coef(0), coefs.get(), (size_t)nc * NZ);
     if (r) return r;
   }
-  CK(cudaStreamSynchronize(h->stream));  // host vectors go out of scope
+  std::shared_ptr<double[]> model(new double[keep.size() * N2]);
+  for (size_t q = 0; q < keep.size(); ++q) par_copy(model.get() + q * N2, P(keep[q]), N2);
+  CK(cudaStreamSynchronize(h->stream));  // host buffers go out of scope
+  h->model = std::move(model);
+  std::memcpy(h->src_plane, src_plane, sizeof src_plane);
   invalidate_graph(h);                   // kernel arguments (atten) may change
   h->have_model = true;
   return SFD_OK;
@@ -945,7 +1038,7 @@ int32_t sfd_set_source(sfd_handle* h, int32_t i, int32_t j, int32_t k, const dou
   std::vector<float> amp((size_t)nchan(c.kind) * c.nstep, 0.0f);
   if (c.kind == SFD_ELECTROMAG2C) {  // a dt / eps with complex eps: rows Ex re, Ex im, Ez re, Ez im
     for (int q = 0; q < 2; ++q) {
-      const std::complex<double> e(h->src_scale[2 * q][n], h->src_scale[2 * q + 1][n]);
+      const std::complex<double> e(h->src_scale(2 * q)[n], h->src_scale(2 * q + 1)[n]);
       for (int t = 0; t < nstep; ++t) {
         const std::complex<double> v = srcfn[(size_t)q * nstep + t] * c.dt / e;
         amp[(size_t)(2 * q) * c.nstep + t] = (float)v.real();
@@ -954,7 +1047,7 @@ int32_t sfd_set_source(sfd_handle* h, int32_t i, int32_t j, int32_t k, const dou
     }
   } else {
     for (int q = 0; q < ncomp; ++q) {
-      const double s = h->src_scale[q][n];
+      const double s = h->src_scale(q)[n];
       for (int t = 0; t < nstep; ++t) amp[(size_t)q * c.nstep + t] = (float)(srcfn[(size_t)q * nstep + t] * c.dt / s);
     }
   }
@@ -1624,7 +1717,7 @@ int32_t sfd_adjoint_gradient(sfd_handle* h, double* out, int64_t count) {
   CK(cudaStreamSynchronize(h->stream));
   if (ctl.err) return fail(SFD_ERR_TIMEOUT, "on-chip adjoint sweep: a neighbouring tile did not answer within 2 s");
   const double dt = h->cfg.dt;
-  const double *e11 = h->model.data(), *e13 = e11 + N2, *e33 = e11 + 2 * N2;
+  const double *e11 = h->model.get(), *e13 = e11 + N2, *e33 = e11 + 2 * N2;
   const double *s11 = e11 + 3 * N2, *s13 = e11 + 4 * N2, *s33 = e11 + 5 * N2;
   double *g11 = out, *g13 = out + N2, *g33 = out + 2 * N2, *gs11 = out + 3 * N2, *gs13 = out + 4 * N2,
          *gs33 = out + 5 * N2;
@@ -1705,7 +1798,7 @@ int32_t sfd_share_model(sfd_handle* dst, const sfd_handle* src) {
     default:
       return fail(SFD_ERR_BAD_ARG, "model sharing is implemented for electromag2 and seismic2");
   }
-  for (int q = 0; q < 3; ++q) dst->src_scale[q] = src->src_scale[q];
+  std::memcpy(dst->src_plane, src->src_plane, sizeof src->src_plane);
   dst->model = src->model;
   dst->have_model = true;
   invalidate_graph(dst);
