@@ -245,6 +245,26 @@ def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000, 
                    for c in cases)
     value = cells * nstep / (ms / 1e3) / 1e9
     achieved = step_bytes * nstep / (ms / 1e3) / 1e9
+    # The same survey through the plain single-shot path, one model after the
+    # other (each handle's own run: the electromag2 shots on chip, the
+    # seismic2 models one launch per step), against the batched traces.
+    batched_traces = [s.traces() for s in solvers]
+    for s in solvers:
+        s.reset()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for s in solvers:
+        s.run(nstep)
+    ev1.record(stream)
+    for s in solvers:
+        s.status()
+    plain_ms = ev0.elapsed_time(ev1)
+    num = den = 0.0
+    for s, tb in zip(solvers, batched_traces):
+        tp = s.traces().astype(np.float64)
+        num += float(((tp - tb) ** 2).sum())
+        den += float((tp ** 2).sum())
+    plain_agg = cells * nstep / (plain_ms / 1e3) / 1e9
     out = {"workload": f"64 electromag2 shots 1040x540 + 16 seismic2 models (nx 200-1200, nz 100-600) x {nstep} steps",
            "value": round(value, 3), "unit": METRIC, "ms_per_run": round(ms, 2), "cells": cells,
            "bytes_per_cell_update": round(step_bytes / cells, 2),
@@ -252,6 +272,9 @@ def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000, 
            "roofline": {"bound": "hbm", "kernel": "batch_kernel", "achieved": round(achieved, 1), "peak": peak,
                         "unit": "GB/s", "frac": round(achieved / peak, 4)},
            "vs_plain_single_shot": round(value / plain_value, 3) if plain_value else None,
+           "plain_sequential": {"value": round(plain_agg, 3), "unit": METRIC, "ms_per_run": round(plain_ms, 2),
+                                "traces_rel_l2_vs_batched": (num / den) ** 0.5 if den > 0 else None},
+           "vs_plain_aggregate": round(value / plain_agg, 3),
            "tiling": {"rows_per_thread": tune["tiling"][0], "blocks_per_sm": tune["tiling"][1],
                       "candidates_ms_per_step": {k: round(v * 1e3, 4) for k, v in tune["timings"].items()}},
            "launches_per_run": 3}
