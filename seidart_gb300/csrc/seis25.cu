@@ -87,6 +87,25 @@ __global__ void __launch_bounds__(BX * BZ, 8) seis25_stress_kernel(Seis25Args a,
   const float* __restrict__ VX = a.vx;
   const float* __restrict__ VY = a.vy;
   const float* __restrict__ VZ = a.vz;
+  // The stresses and memory variables are distinct arrays: with that stated,
+  // every load of a y step is issued before its first store instead of
+  // after the store of the previous loop (one memory round trip per step
+  // instead of one per loop).
+  float* __restrict__ SXX = a.sxx;
+  float* __restrict__ SYY = a.syy;
+  float* __restrict__ SZZ = a.szz;
+  float* __restrict__ SXY = a.sxy;
+  float* __restrict__ SXZ = a.sxz;
+  float* __restrict__ SYZ = a.syz;
+  float* __restrict__ MVXX = a.m_vx_x;
+  float* __restrict__ MVYX = a.m_vy_x;
+  float* __restrict__ MVZX = a.m_vz_x;
+  float* __restrict__ MVXY = a.m_vx_y;
+  float* __restrict__ MVYY = a.m_vy_y;
+  float* __restrict__ MVZY = a.m_vz_y;
+  float* __restrict__ MVXZ = a.m_vx_z;
+  float* __restrict__ MVYZ = a.m_vy_z;
+  float* __restrict__ MVZZ = a.m_vz_z;
   const bool has_xm = i >= 1, has_xp = i <= NX - 2, has_zm = k >= 1, has_zp = k <= NZ - 2;
   size_t c = ((size_t)k * NY + j0) * P + i;
   float cvx = __ldg(VX + c), cvy = __ldg(VY + c), cvz = __ldg(VZ + c);
@@ -106,14 +125,20 @@ __global__ void __launch_bounds__(BX * BZ, 8) seis25_stress_kernel(Seis25Args a,
     if (has_zm) { zmx = __ldg(VX + c - plane); zmy = __ldg(VY + c - plane); zmz = __ldg(VZ + c - plane); }
     if (has_zp) { zpx = __ldg(VX + c + plane); zpy = __ldg(VY + c + plane); zpz = __ldg(VZ + c + plane); }
     float mvxx = 0, mvyx = 0, mvzx = 0, mvxy = 0, mvyy = 0, mvzy = 0, mvxz = 0, mvyz = 0, mvzz = 0;
-    if (xs) { mvxx = a.m_vx_x[mx]; mvyx = a.m_vy_x[mx]; mvzx = a.m_vz_x[mx]; }
-    if (ys) { mvxy = a.m_vx_y[my]; mvyy = a.m_vy_y[my]; mvzy = a.m_vz_y[my]; }
-    if (zs) { mvxz = a.m_vx_z[mz]; mvyz = a.m_vy_z[mz]; mvzz = a.m_vz_z[mz]; }
+    if (xs) { mvxx = MVXX[mx]; mvyx = MVYX[mx]; mvzx = MVZX[mx]; }
+    if (ys) { mvxy = MVXY[my]; mvyy = MVYY[my]; mvzy = MVZY[my]; }
+    if (zs) { mvxz = MVXZ[mz]; mvyz = MVYZ[mz]; mvzz = MVZZ[mz]; }
+    const bool l1 = L1 && j >= 1, l2 = L2 && j <= NY - 2, l3 = L3 && j >= 1, l4 = L4 && j <= NY - 2;
+    float oxx = 0.f, oyy = 0.f, ozz = 0.f, oxy = 0.f, oxz = 0.f, oyz = 0.f;
+    if (l1) { oxx = SXX[c]; oyy = SYY[c]; ozz = SZZ[c]; }
+    if (l2) oxy = SXY[c];
+    if (l3) oxz = SXZ[c];
+    if (l4) oyz = SYZ[c];
     const float iky = a.Y.ik[j], ikyh = a.Y.ikh[j], ady = a.Y.ad[j], adyh = a.Y.adh[j];
     const float by = a.Y.b[j], byh = a.Y.bh[j];
 
     // ---- Loop 1: sigmaxx, sigmayy, sigmazz (j >= 1): x+, y-, z- differences
-    if (L1 && j >= 1) {
+    if (l1) {
       const float dxx = xpx - cvx, dyx = xpy - cvy, dzx = xpz - cvz;
       const float dyy = cvy - pvy, dxy = cvx - pvx, dzy = cvz - pvz;
       const float dzz = cvz - zmz, dxz = cvx - zmx, dyz = cvy - zmy;
@@ -123,15 +148,15 @@ __global__ void __launch_bounds__(BX * BZ, 8) seis25_stress_kernel(Seis25Args a,
       const float vxx = dxx * ikxh + mvxx, vyx = dyx * ikxh + mvyx, vzx = dzx * ikxh + mvzx;
       const float vyy = dyy * iky + mvyy, vxy = dxy * iky + mvxy, vzy = dzy * iky + mvzy;
       const float vzz = dzz * ikz + mvzz, vxz = dxz * ikz + mvxz, vyz = dyz * ikz + mvyz;
-      a.sxx[c] = a.sxx[c] + (p11 * vxx + p12 * vyy + p13 * vzz + p14 * (vyz + vzy) + p15 * (vxz + vzx) +
-                             p16 * (vxy + vzy));
-      a.syy[c] = a.syy[c] + (p12 * vxx + p22 * vyy + p23 * vzz + p24 * (vyz + vzy) + p25 * (vxz + vzx) +
-                             p26 * (vyx + vxy));
-      a.szz[c] = a.szz[c] + (p13 * vxx + p23 * vyy + p33 * vzz + p34 * (vyz + vzy) + p35 * (vxz + vzx) +
-                             p36 * (vyx + vxy));
+      SXX[c] = oxx + (p11 * vxx + p12 * vyy + p13 * vzz + p14 * (vyz + vzy) + p15 * (vxz + vzx) +
+                      p16 * (vxy + vzy));
+      SYY[c] = oyy + (p12 * vxx + p22 * vyy + p23 * vzz + p24 * (vyz + vzy) + p25 * (vxz + vzx) +
+                      p26 * (vyx + vxy));
+      SZZ[c] = ozz + (p13 * vxx + p23 * vyy + p33 * vzz + p34 * (vyz + vzy) + p35 * (vxz + vzx) +
+                      p36 * (vyx + vxy));
     }
     // ---- Loop 2: sigmaxy (j <= NY-2): x-, y+, z-
-    if (L2 && j <= NY - 2) {
+    if (l2) {
       const float dxx = cvx - xmx, dyx = cvy - xmy, dzx = cvz - xmz;
       const float dyy = nvy - cvy, dxy = nvx - cvx, dzy = nvz - cvz;
       const float dzz = cvz - zmz, dxz = cvx - zmx, dyz = cvy - zmy;
@@ -142,11 +167,11 @@ __global__ void __launch_bounds__(BX * BZ, 8) seis25_stress_kernel(Seis25Args a,
       const float vyy = dyy * ikyh + mvyy, vxy = dxy * ikyh + mvxy, vzy = dzy * ikyh + mvzy;
       const float vzz = dzz * ikzh + mvzz, vyz = dyz * ikzh + mvyz;
       const float vzx = dzx * idx, vxz = dxz * idz;  // left unscaled, :701-707
-      a.sxy[c] = a.sxy[c] + (q16 * vxx + q26 * vyy + q36 * vzz + q46 * (vzy + vyz) + q56 * (vzx + vxz) +
-                             q66 * (vyx + vxy));
+      SXY[c] = oxy + (q16 * vxx + q26 * vyy + q36 * vzz + q46 * (vzy + vyz) + q56 * (vzx + vxz) +
+                      q66 * (vyx + vxy));
     }
     // ---- Loop 3: sigmaxz (j >= 1): x-, y-, z+
-    if (L3 && j >= 1) {
+    if (l3) {
       const float dxx = cvx - xmx, dyx = cvy - xmy, dzx = cvz - xmz;
       const float dyy = cvy - pvy, dzy = cvz - pvz, dxy = cvx - pvx;
       const float dzz = zpz - cvz, dxz = zpx - cvx, dyz = zpy - cvy;
@@ -156,11 +181,11 @@ __global__ void __launch_bounds__(BX * BZ, 8) seis25_stress_kernel(Seis25Args a,
       const float vxx = dxx * ikx + mvxx, vyx = dyx * ikx + mvyx, vzx = dzx * ikx + mvzx;
       const float vyy = dyy * iky + mvyy, vxy = dxy * iky + mvxy;
       const float vzz = dzz * ikzh + mvzz, vxz = dxz * ikzh + mvxz;
-      a.sxz[c] = a.sxz[c] + (r15 * vxx + r25 * vyy + r35 * vzz + r45 * (vxz + vzx) + r55 * (vxz + vzx) +
-                             r56 * (vxy + vyx));
+      SXZ[c] = oxz + (r15 * vxx + r25 * vyy + r35 * vzz + r45 * (vxz + vzx) + r55 * (vxz + vzx) +
+                      r56 * (vxy + vyx));
     }
     // ---- Loop 4: sigmayz (j <= NY-2): x+, y+, z+
-    if (L4 && j <= NY - 2) {
+    if (l4) {
       const float dxx = xpx - cvx, dyx = xpy - cvy, dzx = xpz - cvz;
       const float dyy = nvy - cvy, dxy = nvx - cvx, dzy = nvz - cvz;
       const float dzz = zpz - cvz, dxz = zpx - cvx, dyz = zpy - cvy;
@@ -170,12 +195,12 @@ __global__ void __launch_bounds__(BX * BZ, 8) seis25_stress_kernel(Seis25Args a,
       const float vxx = dxx * ikxh + mvxx, vyx = dyx * ikxh + mvyx, vzx = dzx * ikxh + mvzx;
       const float vyy = dyy * ikyh + mvyy, vxy = dxy * ikyh + mvxy, vzy = dzy * ikyh + mvzy;
       const float vzz = dzz * ikzh + mvzz, vxz = dxz * ikzh + mvxz, vyz = dyz * ikzh + mvyz;
-      a.syz[c] = a.syz[c] + (s14 * vxx + s24 * vyy + s34 * vzz + s44 * (vyz + vzy) + s45 * (vxz + vzx) +
-                             s46 * (vyx + vxy));
+      SYZ[c] = oyz + (s14 * vxx + s24 * vyy + s34 * vzz + s44 * (vyz + vzy) + s45 * (vxz + vzx) +
+                      s46 * (vyx + vxy));
     }
-    if (xs) { a.m_vx_x[mx] = mvxx; a.m_vy_x[mx] = mvyx; a.m_vz_x[mx] = mvzx; }
-    if (ys) { a.m_vx_y[my] = mvxy; a.m_vy_y[my] = mvyy; a.m_vz_y[my] = mvzy; }
-    if (zs) { a.m_vx_z[mz] = mvxz; a.m_vy_z[mz] = mvyz; a.m_vz_z[mz] = mvzz; }
+    if (xs) { MVXX[mx] = mvxx; MVYX[mx] = mvyx; MVZX[mx] = mvzx; }
+    if (ys) { MVXY[my] = mvxy; MVYY[my] = mvyy; MVZY[my] = mvzy; }
+    if (zs) { MVXZ[mz] = mvxz; MVYZ[mz] = mvyz; MVZZ[mz] = mvzz; }
     pvx = cvx; pvy = cvy; pvz = cvz;
     cvx = nvx; cvy = nvy; cvz = nvz;
   }
@@ -215,6 +240,20 @@ __global__ void __launch_bounds__(BX * BZ, 8) seis25_velocity_kernel(Seis25Args 
     const float* __restrict__ SXY = a.sxy;
     const float* __restrict__ SXZ = a.sxz;
     const float* __restrict__ SYZ = a.syz;
+    // velocities and memory variables: distinct arrays, every load of a y
+    // step issued before its first store (as in the stress kernel)
+    float* __restrict__ VX = a.vx;
+    float* __restrict__ VY = a.vy;
+    float* __restrict__ VZ = a.vz;
+    float* __restrict__ MSXXX = a.m_sxx_x;
+    float* __restrict__ MSXYY = a.m_sxy_y;
+    float* __restrict__ MSXZZ = a.m_sxz_z;
+    float* __restrict__ MSXYX = a.m_sxy_x;
+    float* __restrict__ MSYYY = a.m_syy_y;
+    float* __restrict__ MSYZZ = a.m_syz_z;
+    float* __restrict__ MSXZX = a.m_sxz_x;
+    float* __restrict__ MSYZY = a.m_syz_y;
+    float* __restrict__ MSZZZ = a.m_szz_z;
     size_t c = ((size_t)k * NY + j0) * P + i;
     float psxy = 0.f, psyz = 0.f;
     if (j0 >= 1) { psxy = __ldg(SXY + c - P); psyz = __ldg(SYZ + c - P); }
@@ -229,29 +268,47 @@ __global__ void __launch_bounds__(BX * BZ, 8) seis25_velocity_kernel(Seis25Args 
       const float csxx = __ldg(SXX + c), csxy = __ldg(SXY + c), csxz = __ldg(SXZ + c);
       const float csyz = __ldg(SYZ + c), cszz = __ldg(SZZ + c);
       const float nsyy = (j + 1 < NY) ? __ldg(SYY + c + P) : 0.f;
-      float vx = a.vx[c], vy = a.vy[c], vz = a.vz[c];
-      if (Vx && j >= 1) {  // :821-845
+      float vx = VX[c], vy = VY[c], vz = VZ[c];
+      const bool ux = Vx && j >= 1, uy = Vy && j <= NY - 2, uz = Vz && j >= 1;
+      // memory variables of the three loops, loaded up front
+      float m1x = 0.f, m1y = 0.f, m1z = 0.f, m2x = 0.f, m2y = 0.f, m2z = 0.f, m3x = 0.f, m3y = 0.f, m3z = 0.f;
+      if (xs) {
+        if (ux) m1x = MSXXX[mx];
+        if (uy) m2x = MSXYX[mx];
+        if (uz) m3x = MSXZX[mx];
+      }
+      if (ys) {
+        if (ux) m1y = MSXYY[my];
+        if (uy) m2y = MSYYY[my];
+        if (uz) m3y = MSYZY[my];
+      }
+      if (zs) {
+        if (ux) m1z = MSXZZ[mz];
+        if (uy) m2z = MSYZZ[mz];
+        if (uz) m3z = MSZZZ[mz];
+      }
+      if (ux) {  // :821-845
         const float d1 = csxx - __ldg(SXX + c - 1), d2 = csxy - psxy, d3 = csxz - __ldg(SXZ + c - plane);
         float v1 = d1 * ikx, v2 = d2 * iky, v3 = d3 * ikz;
-        if (xs) { const float m = bx * a.m_sxx_x[mx] + adx * d1; a.m_sxx_x[mx] = m; v1 += m; }
-        if (ys) { const float m = by * a.m_sxy_y[my] + ady * d2; a.m_sxy_y[my] = m; v2 += m; }
-        if (zs) { const float m = bz * a.m_sxz_z[mz] + adz * d3; a.m_sxz_z[mz] = m; v3 += m; }
+        if (xs) { const float m = bx * m1x + adx * d1; MSXXX[mx] = m; v1 += m; }
+        if (ys) { const float m = by * m1y + ady * d2; MSXYY[my] = m; v2 += m; }
+        if (zs) { const float m = bz * m1z + adz * d3; MSXZZ[mz] = m; v3 += m; }
         vx = vx * gx + (v1 + v2 + v3) * dtrx;
       }
-      if (Vy && j <= NY - 2) {  // :847-869
+      if (uy) {  // :847-869
         const float d1 = __ldg(SXY + c + 1) - csxy, d2 = nsyy - csyy, d3 = csyz - __ldg(SYZ + c - plane);
         float v1 = d1 * ikxh, v2 = d2 * ikyh, v3 = d3 * ikz;
-        if (xs) { const float m = bxh * a.m_sxy_x[mx] + adxh * d1; a.m_sxy_x[mx] = m; v1 += m; }
-        if (ys) { const float m = byh * a.m_syy_y[my] + adyh * d2; a.m_syy_y[my] = m; v2 += m; }
-        if (zs) { const float m = bz * a.m_syz_z[mz] + adz * d3; a.m_syz_z[mz] = m; v3 += m; }
+        if (xs) { const float m = bxh * m2x + adxh * d1; MSXYX[mx] = m; v1 += m; }
+        if (ys) { const float m = byh * m2y + adyh * d2; MSYYY[my] = m; v2 += m; }
+        if (zs) { const float m = bz * m2z + adz * d3; MSYZZ[mz] = m; v3 += m; }
         vy = vy * gy + (v1 + v2 + v3) * dtry;
       }
-      if (Vz && j >= 1) {  // :872-896
+      if (uz) {  // :872-896
         const float d1 = __ldg(SXZ + c + 1) - csxz, d2 = csyz - psyz, d3 = __ldg(SZZ + c + plane) - cszz;
         float v1 = d1 * ikxh, v2 = d2 * iky, v3 = d3 * ikzh;
-        if (xs) { const float m = bxh * a.m_sxz_x[mx] + adxh * d1; a.m_sxz_x[mx] = m; v1 += m; }
-        if (ys) { const float m = by * a.m_syz_y[my] + ady * d2; a.m_syz_y[my] = m; v2 += m; }
-        if (zs) { const float m = bzh * a.m_szz_z[mz] + adzh * d3; a.m_szz_z[mz] = m; v3 += m; }
+        if (xs) { const float m = bxh * m3x + adxh * d1; MSXZX[mx] = m; v1 += m; }
+        if (ys) { const float m = by * m3y + ady * d2; MSYZY[my] = m; v2 += m; }
+        if (zs) { const float m = bzh * m3z + adzh * d3; MSZZZ[mz] = m; v3 += m; }
         vz = vz * gz + (v1 + v2 + v3) * dtrz;
       }
       if (i == a.io.si && j == a.io.sj && k == a.io.sk) {  // :898-900
@@ -260,9 +317,9 @@ __global__ void __launch_bounds__(BX * BZ, 8) seis25_velocity_kernel(Seis25Args 
         vz += a.io.src[2 * a.io.nstep + t];
       }
       if (xface || j == 0 || j == NY - 1) { vx = 0.f; vy = 0.f; vz = 0.f; }  // :903-925
-      a.vx[c] = vx;
-      a.vy[c] = vy;
-      a.vz[c] = vz;
+      VX[c] = vx;
+      VY[c] = vy;
+      VZ[c] = vz;
       norm = fmaxf(norm, norm_monitor(vx, vy, vz));
       psxy = csxy;
       psyz = csyz;
