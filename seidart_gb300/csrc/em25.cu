@@ -43,6 +43,19 @@ __global__ void __launch_bounds__(BX * BZ) em25_h_kernel(Em25Args a, int rel) {
   const bool fx_x = (i == 0) || (k == 0) || (k == NZ - 2);               // Hx: i=NX-1 is outside the loop
   const bool fy_x = (i == 0) || (i == NX - 2) || (k == 0) || (k == NZ - 2);
   const bool fz_x = (i == 0) || (i == NX - 2) || (k == 0);               // Hz: k=NZ-1 is outside the loop
+  // Distinct arrays: the loads of a y step need not wait behind its stores.
+  const float* __restrict__ Ex_ = a.Ex;
+  const float* __restrict__ Ey_ = a.Ey;
+  const float* __restrict__ Ez_ = a.Ez;
+  float* __restrict__ Hx_ = a.Hx;
+  float* __restrict__ Hy_ = a.Hy;
+  float* __restrict__ Hz_ = a.Hz;
+  float* __restrict__ mEz_y_ = a.mEz_y;
+  float* __restrict__ mEy_z_ = a.mEy_z;
+  float* __restrict__ mEx_z_ = a.mEx_z;
+  float* __restrict__ mEz_x_ = a.mEz_x;
+  float* __restrict__ mEx_y_ = a.mEx_y;
+  float* __restrict__ mEy_x_ = a.mEy_x;
   for (int j = j0; j < j1; ++j) {
     const size_t c = ((size_t)k * NY + j) * P + i;
     const bool ys = in_strip(j, NY, W);
@@ -51,39 +64,39 @@ __global__ void __launch_bounds__(BX * BZ) em25_h_kernel(Em25Args a, int rel) {
     const size_t mz = ((size_t)zsi * NY + j) * P + i;
     const float iky = a.Y.ik[j], ady = a.Y.ad[j], by = a.Y.b[j];
     const float ikyh = a.Y.ikh[j], adyh = a.Y.adh[j], byh = a.Y.bh[j];
-    const float ex = a.Ex[c], ey = a.Ey[c], ez = a.Ez[c];
+    const float ex = Ex_[c], ey = Ey_[c], ez = Ez_[c];
     // Hx, :904-917
     {
-      const float d1 = ez - a.Ez[c + P];  // dEz/dy
+      const float d1 = ez - Ez_[c + P];  // dEz/dy
       float v1 = d1 * ikyh;
-      if (ys) { const float m = byh * a.mEz_y[my] + adyh * d1; a.mEz_y[my] = m; v1 += m; }
-      const float d2 = a.Ey[c + plane] - ey;  // dEy/dz
+      if (ys) { const float m = byh * mEz_y_[my] + adyh * d1; mEz_y_[my] = m; v1 += m; }
+      const float d2 = Ey_[c + plane] - ey;  // dEy/dz
       float v2 = d2 * ikzh;
-      if (zs) { const float m = bzh * a.mEy_z[mz] + adzh * d2; a.mEy_z[mz] = m; v2 += m; }
-      const float h = (fx_x || j == 0 || j == NY - 2) ? 0.f : a.Hx[c];
-      a.Hx[c] = h + dbH * (v2 + v1);
+      if (zs) { const float m = bzh * mEy_z_[mz] + adzh * d2; mEy_z_[mz] = m; v2 += m; }
+      const float h = (fx_x || j == 0 || j == NY - 2) ? 0.f : Hx_[c];
+      Hx_[c] = h + dbH * (v2 + v1);
     }
     // Hy, :925-938
     {
-      const float d1 = ex - a.Ex[c + plane];  // dEx/dz
+      const float d1 = ex - Ex_[c + plane];  // dEx/dz
       float v1 = d1 * ikz;
-      if (zs) { const float m = bz * a.mEx_z[mz] + adz * d1; a.mEx_z[mz] = m; v1 += m; }
-      const float d2 = a.Ez[c + 1] - ez;  // dEz/dx
+      if (zs) { const float m = bz * mEx_z_[mz] + adz * d1; mEx_z_[mz] = m; v1 += m; }
+      const float d2 = Ez_[c + 1] - ez;  // dEz/dx
       float v2 = d2 * ikx;
-      if (xs) { const float m = bx * a.mEz_x[mx] + adx * d2; a.mEz_x[mx] = m; v2 += m; }
-      const float h = (fy_x || j == 0) ? 0.f : a.Hy[c];  // Hy face j=NY-1 is outside the loop
-      a.Hy[c] = h + dbH * (v2 + v1);
+      if (xs) { const float m = bx * mEz_x_[mx] + adx * d2; mEz_x_[mx] = m; v2 += m; }
+      const float h = (fy_x || j == 0) ? 0.f : Hy_[c];  // Hy face j=NY-1 is outside the loop
+      Hy_[c] = h + dbH * (v2 + v1);
     }
     // Hz, :946-960 (k >= 1)
     if (hz_rows) {
-      const float d1 = a.Ex[c + P] - ex;  // dEx/dy
+      const float d1 = Ex_[c + P] - ex;  // dEx/dy
       float v1 = d1 * iky;
-      if (ys) { const float m = by * a.mEx_y[my] + ady * d1; a.mEx_y[my] = m; v1 += m; }
-      const float d2 = ey - a.Ey[c + 1];  // dEy/dx
+      if (ys) { const float m = by * mEx_y_[my] + ady * d1; mEx_y_[my] = m; v1 += m; }
+      const float d2 = ey - Ey_[c + 1];  // dEy/dx
       float v2 = d2 * ikx;
-      if (xs) { const float m = bx * a.mEy_x[mx] + adx * d2; a.mEy_x[mx] = m; v2 += m; }
-      const float h = (fz_x || j == 0 || j == NY - 2) ? 0.f : a.Hz[c];
-      a.Hz[c] = h + dbH * (v2 + v1);
+      if (xs) { const float m = bx * mEy_x_[mx] + adx * d2; mEy_x_[mx] = m; v2 += m; }
+      const float h = (fz_x || j == 0 || j == NY - 2) ? 0.f : Hz_[c];
+      Hz_[c] = h + dbH * (v2 + v1);
     }
   }
 }
@@ -121,6 +134,19 @@ __global__ void __launch_bounds__(BX * BZ) em25_e_kernel(Em25Args a, int rel) {
     const bool fEx = (i == 0) || (i == NX - 2) || (k == 0) || (k == NZ - 1);
     const bool fEy = (i == 0) || (i == NX - 1) || (k == 0) || (k == NZ - 1);
     const bool fEz = (i == 0) || (i == NX - 1) || (k == 0) || (k == NZ - 2);
+  // Distinct arrays: the loads of a y step need not wait behind its stores.
+  const float* __restrict__ Hx_ = a.Hx;
+  const float* __restrict__ Hy_ = a.Hy;
+  const float* __restrict__ Hz_ = a.Hz;
+  float* __restrict__ Ex_ = a.Ex;
+  float* __restrict__ Ey_ = a.Ey;
+  float* __restrict__ Ez_ = a.Ez;
+  float* __restrict__ mHz_y_ = a.mHz_y;
+  float* __restrict__ mHy_z_ = a.mHy_z;
+  float* __restrict__ mHz_x_ = a.mHz_x;
+  float* __restrict__ mHx_z_ = a.mHx_z;
+  float* __restrict__ mHx_y_ = a.mHx_y;
+  float* __restrict__ mHy_x_ = a.mHy_x;
     for (int j = j0; j < j1; ++j) {
       const size_t c = ((size_t)k * NY + j) * P + i;
       const bool ys = in_strip(j, NY, W);
@@ -128,32 +154,32 @@ __global__ void __launch_bounds__(BX * BZ) em25_e_kernel(Em25Args a, int rel) {
       const size_t my = ((size_t)k * (2 * W) + (ys ? strip_idx(j, NY, W) : 0)) * P + i;
       const size_t mz = ((size_t)zsi * NY + j) * P + i;
       const float ikyh = a.Y.ikh[j], adyh = a.Y.adh[j], byh = a.Y.bh[j];
-      float ex = a.Ex[c], ey = a.Ey[c], ez = a.Ez[c];
+      float ex = Ex_[c], ey = Ey_[c], ez = Ez_[c];
       if (XEx && j >= 1 && j <= NY - 2) {  // :971-984
-        const float d1 = a.Hz[c] - a.Hz[c - P];  // dHz/dy
+        const float d1 = Hz_[c] - Hz_[c - P];  // dHz/dy
         float v1 = d1 * ikyh;
-        if (ys) { const float m = byh * a.mHz_y[my] + adyh * d1; a.mHz_y[my] = m; v1 += m; }
-        const float d2 = a.Hy[c - plane] - a.Hy[c];  // dHy/dz
+        if (ys) { const float m = byh * mHz_y_[my] + adyh * d1; mHz_y_[my] = m; v1 += m; }
+        const float d2 = Hy_[c - plane] - Hy_[c];  // dHy/dz
         float v2 = d2 * ikz;
-        if (zs) { const float m = bz * a.mHy_z[mz] + adz * d2; a.mHy_z[mz] = m; v2 += m; }
+        if (zs) { const float m = bz * mHy_z_[mz] + adz * d2; mHy_z_[mz] = m; v2 += m; }
         ex = caX * ex + cbX * (v1 + v2);
       }
       if (XEy && j <= NY - 2) {  // :988-1007
-        const float d1 = a.Hz[c - 1] - a.Hz[c];  // dHz/dx
+        const float d1 = Hz_[c - 1] - Hz_[c];  // dHz/dx
         float v1 = d1 * ikxh;
-        if (xs) { const float m = bxh * a.mHz_x[mx] + adxh * d1; a.mHz_x[mx] = m; v1 += m; }
-        const float d2 = a.Hx[c] - a.Hx[c - plane];  // dHx/dz
+        if (xs) { const float m = bxh * mHz_x_[mx] + adxh * d1; mHz_x_[mx] = m; v1 += m; }
+        const float d2 = Hx_[c] - Hx_[c - plane];  // dHx/dz
         float v2 = d2 * ikzh;
-        if (zs) { const float m = bzh * a.mHx_z[mz] + adzh * d2; a.mHx_z[mz] = m; v2 += m; }
+        if (zs) { const float m = bzh * mHx_z_[mz] + adzh * d2; mHx_z_[mz] = m; v2 += m; }
         ey = caY * ey + cbY * (v1 + v2);
       }
       if (XEz && j >= 1 && j <= NY - 2) {  // :1015-1029
-        const float d1 = a.Hx[c - P] - a.Hx[c];  // dHx/dy
+        const float d1 = Hx_[c - P] - Hx_[c];  // dHx/dy
         float v1 = d1 * ikyh;
-        if (ys) { const float m = byh * a.mHx_y[my] + adyh * d1; a.mHx_y[my] = m; v1 += m; }
-        const float d2 = a.Hy[c] - a.Hy[c - 1];  // dHy/dx
+        if (ys) { const float m = byh * mHx_y_[my] + adyh * d1; mHx_y_[my] = m; v1 += m; }
+        const float d2 = Hy_[c] - Hy_[c - 1];  // dHy/dx
         float v2 = d2 * ikxh;
-        if (xs) { const float m = bxh * a.mHy_x[mx] + adxh * d2; a.mHy_x[mx] = m; v2 += m; }
+        if (xs) { const float m = bxh * mHy_x_[mx] + adxh * d2; mHy_x_[mx] = m; v2 += m; }
         ez = caZ * ez + cbZ * (v1 + v2);
       }
       if (i == a.io.si && j == a.io.sj && k == a.io.sk) {  // :1033-1035
@@ -164,9 +190,9 @@ __global__ void __launch_bounds__(BX * BZ) em25_e_kernel(Em25Args a, int rel) {
       if (fEx || j == 0 || j == NY - 1) ex = 0.f;  // :1038-1043
       if (fEy || j == 0 || j == NY - 2) ey = 0.f;  // :1045-1050
       if (fEz || j == 0 || j == NY - 1) ez = 0.f;  // :1052-1057
-      a.Ex[c] = ex;
-      a.Ey[c] = ey;
-      a.Ez[c] = ez;
+      Ex_[c] = ex;
+      Ey_[c] = ey;
+      Ez_[c] = ez;
       norm = fmaxf(norm, norm_monitor(ex, ey, ez));
     }
   }
