@@ -23,10 +23,14 @@ namespace {
 
 constexpr int BX = 32, BZ = 4;
 
-// 8 blocks of 128 threads per SM (64 registers): the y-march's loads wait on
-// HBM, and more resident warps hide more of that latency than the few
-// registers spilled to L1 cost.
-__global__ void __launch_bounds__(BX * BZ, 8) seis25_stress_kernel(Seis25Args a, int rel) {
+// The stress kernel holds a column's 33 stiffness averages, its axis tables,
+// the carried velocities and nine memory variables: at 4 blocks of 128
+// threads per SM (128 registers) nothing spills, and that beat 8 blocks at
+// 64 registers, whose spills missed L1 (0.345 against 0.412 ms per step on
+// the 630 x 70 x 330 grid).  The velocity kernel needs fewer registers and
+// runs best at 8 blocks, where more resident warps hide the y-march's HBM
+// latency.
+__global__ void __launch_bounds__(BX * BZ, 4) seis25_stress_kernel(Seis25Args a, int rel) {
   const Ctl* ctl = a.io.ctl;
   const int t = ctl->base + rel;
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && t > ctl->run_start) {
