@@ -216,8 +216,10 @@ const float* sfd_traces_device(const sfd_handle* h);
 int32_t sfd_launch_half(sfd_handle* h, int32_t which, int32_t count);
 
 /* Whether sfd_run keeps this handle's whole state on chip (one launch per run,
- * one CTA per tile of the grid): 1 yes, 0 no (one launch per step).  Decided
- * on the current device from its SM count and shared memory.  tiles and
+ * one CTA per tile of the grid): 1 yes, 0 no (one launch per step).  Single-
+ * pass electromag2 and seismic2 handles whose grid fits the SMs' shared
+ * memory (and registers) run on chip; decided on the current device from its
+ * SM count and shared memory.  tiles and
  * tile_rows (may be NULL) receive the number of tiles and of tile rows.  No
  * counterpart in the reference: its time loop has one execution form. */
 int32_t sfd_on_chip(sfd_handle* h, int32_t* tiles, int32_t* tile_rows);

@@ -51,8 +51,10 @@ struct ResScratch {
 };
 
 __host__ __device__ inline int res_nzp(int NZ) { return (NZ + 31) & ~31; }
-inline size_t res_scratch_bytes(int P, int NZ) {
-  return sizeof(uint2) * 4 * kResMaxTiles1D * ((size_t)P + (size_t)res_nzp(NZ));
+// nf edge fields per direction type (two copies each): 2 for electromag2
+// (Ex/Hy rows, Ez/Hy columns), 6 for seismic2.
+inline size_t res_scratch_bytes(int P, int NZ, int nf = 2) {
+  return sizeof(uint2) * 2 * nf * kResMaxTiles1D * ((size_t)P + (size_t)res_nzp(NZ));
 }
 
 // Per-step copies of the state written by a recompute run for the adjoint:
@@ -111,6 +113,35 @@ struct Em2AdjResident {
   ResScratch r;
   unsigned long long limit_ns;
 };
+
+// On-chip seismic2 run: a uniform ntx x ntz grid of tiles, tile (c, r)
+// covering columns [xb[c], xb[c+1]) and rows [zb[r], zb[r+1]).
+struct Seis2ResPlan {
+  int ntx, ntz;
+  int xb[kResMaxTiles1D + 1], zb[kResMaxTiles1D + 1];
+  size_t smem;  // dynamic shared memory of the largest tile
+};
+
+struct Seis2Resident {
+  int NX, NZ, P, W, atten;
+  float *vx, *vz, *sxx, *szz, *sxz;        // current copy: read before, written after the run
+  float *m_vxx, *m_vzz, *m_vxz, *m_vzx;    // velocity-gradient memory (x, z, z, x strips), current copy
+  float *m_sxx_x, *m_szz_z, *m_sxz_x, *m_sxz_z;  // stress-gradient memory (x, z, x, z strips)
+  const float* coef[12];                   // A11 A13 A15 A33 A35 B15 B35 B55 dtrx dtrz gxp gzp
+  const float* q3;
+  AxisTab X, Z;
+  IoArgs io;
+  Seis2ResPlan plan;
+  ResScratch r;  // six edge fields
+  int t0, nsteps;
+  unsigned long long limit_ns;
+};
+
+// Tiling of an NX x NZ seismic2 grid for `max_ctas` CTAs of at most
+// `max_smem` bytes; false when the grid does not fit on chip.
+bool seis2_resident_plan(int NX, int NZ, int max_ctas, size_t max_smem, Seis2ResPlan* out);
+cudaError_t seis2_resident_prepare(const Seis2ResPlan& plan, int* ctas_per_sm);
+cudaError_t seis2_resident_launch(const Seis2Resident& a, cudaStream_t s);
 
 // Pick the tiling of an NX x NZ electromag2 grid with npml-cell strips for
 // `max_ctas` CTAs of at most `max_smem` bytes of shared memory.  Returns

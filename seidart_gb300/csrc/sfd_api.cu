@@ -177,6 +177,9 @@ struct Layout {
       off_q3, off_src, off_rec, off_traces, off_slots, off_res, total;
 };
 
+// Edge fields of an on-chip run (resident.h): electromag2 2, seismic2 6.
+int res_edge_fields(int kind) { return kind == SFD_SEISMIC2 ? 6 : 2; }
+
 int grid_slots(const sfd_config& c, int P, int ysplit) {
   (void)P;
   if (is3(c.kind)) return ((c.nx + 31) / 32) * ((c.nz + 3) / 4) * ysplit;
@@ -240,9 +243,9 @@ void make_layout(const sfd_config& c, Layout* L) {
   L->off_traces = o; o += align256(sizeof(float) * (size_t)c.nstep * nchan(c.kind) * std::max(1, c.nrec));
   L->off_slots = o; o += align256(sizeof(float) * L->nslots);  // ZB = 1 tiles: the largest grid
   L->off_res = 0;
-  if (c.kind == SFD_ELECTROMAG2 && !(c.flags & (SFD_FLAG_TWO_PASS | SFD_FLAG_STREAMING))) {
-    L->off_res = o;  // step counters and edge arrays of on-chip runs
-    o += align256(res_scratch_bytes(L->P, c.nz));
+  if ((c.kind == SFD_ELECTROMAG2 || c.kind == SFD_SEISMIC2) && !(c.flags & (SFD_FLAG_TWO_PASS | SFD_FLAG_STREAMING))) {
+    L->off_res = o;  // edge arrays of on-chip runs
+    o += align256(res_scratch_bytes(L->P, c.nz, res_edge_fields(c.kind)));
   }
   L->total = o;
 }
@@ -264,7 +267,8 @@ struct sfd_handle_s {
   Seis2Step s2s[2];
   Launch launch1;       // single-pass geometry
   int res_state = 0;    // on-chip runs: 0 not yet checked, 1 usable, -1 not usable
-  ResPlan res_plan;
+  ResPlan res_plan;     // electromag2
+  Seis2ResPlan s2_plan;  // seismic2
   int64_t step = 0;
   // The FP64 model planes read after sfd_set_model (the source scaling; for
   // electromag2 also the adjoint's chain rule), copied from its input:
@@ -500,6 +504,19 @@ bool resident_usable(sfd_handle* h) {
   }
   if (!coop) return false;
   const size_t static_smem = 8192;  // receiver list, thread map and reduction buffers of the kernel
+  if (h->cfg.kind == SFD_SEISMIC2) {  // a uniform tiling: searched in microseconds, not cached
+    Seis2ResPlan plan;
+    if (!seis2_resident_plan(h->cfg.nx, h->cfg.nz, std::min(nsm, h->L.nslots), (size_t)optin - static_smem, &plan))
+      return false;
+    int per_sm = 0;
+    if (seis2_resident_prepare(plan, &per_sm) != cudaSuccess || per_sm < 1) {
+      cudaGetLastError();
+      return false;
+    }
+    h->s2_plan = plan;
+    h->res_state = 1;
+    return true;
+  }
   // Plans are searched once per grid shape and device (the search takes
   // tens of milliseconds; a survey creates one handle per shot).
   struct PlanKey {
@@ -556,6 +573,30 @@ Em2Resident resident_args(const sfd_handle* h, int64_t nsteps) {
   r.nsteps = (int)nsteps;
   r.limit_ns = 2000000000ull;
   r.dump = ResDump{nullptr, 0, {0, 0, 0, 0, 0, 0, 0}};
+  return r;
+}
+
+Seis2Resident seis2_resident_args(const sfd_handle* h, int64_t nsteps) {
+  Seis2Resident r;
+  const Seis2Step& b = h->s2s[h->cur];
+  const int p = h->cur;
+  r.NX = b.NX; r.NZ = b.NZ; r.P = b.P; r.W = b.W; r.atten = b.atten;
+  r.vx = h->fc(0, p); r.vz = h->fc(1, p); r.sxx = h->fc(2, p); r.szz = h->fc(3, p); r.sxz = h->fc(4, p);
+  r.m_vxx = h->mc(0, p); r.m_vzz = h->mc(1, p); r.m_vxz = h->mc(2, p); r.m_vzx = h->mc(3, p);
+  r.m_sxx_x = h->mc(4, 0); r.m_szz_z = h->mc(5, 0); r.m_sxz_x = h->mc(6, 0); r.m_sxz_z = h->mc(7, 0);
+  const float* cf[12] = {b.A11, b.A13, b.A15, b.A33, b.A35, b.B15, b.B35, b.B55, b.dtrx, b.dtrz, b.gxp, b.gzp};
+  for (int q = 0; q < 12; ++q) r.coef[q] = cf[q];
+  r.q3 = b.q3;
+  r.X = b.X; r.Z = b.Z;
+  r.io = b.io;
+  r.plan = h->s2_plan;
+  char* base = h->base + h->L.off_res;
+  r.r.erow = (uint2*)base;
+  r.r.NZp = res_nzp(h->cfg.nz);
+  r.r.ecol = r.r.erow + 2 * 6 * kResMaxTiles1D * (size_t)h->L.P;
+  r.t0 = (int)h->step;
+  r.nsteps = (int)nsteps;
+  r.limit_ns = 2000000000ull;
   return r;
 }
 
@@ -1176,8 +1217,9 @@ int32_t sfd_run(sfd_handle* h, int64_t nsteps) {
   k_begin<<<std::min(1024, (L.nslots + 255) / 256 + 1), 256, 0, h->stream>>>(ctl, slots, L.nslots, (int)h->step);
   if (resident_usable(h)) {  // the whole run in one launch, state on chip
     // tags from an earlier run must not match: clear every edge word
-    CK(cudaMemsetAsync(h->base + L.off_res, 0, res_scratch_bytes(L.P, L.NZ), h->stream));
-    CK(em2_resident_launch(resident_args(h, nsteps), h->stream));
+    CK(cudaMemsetAsync(h->base + L.off_res, 0, res_scratch_bytes(L.P, L.NZ, res_edge_fields(h->cfg.kind)), h->stream));
+    if (h->cfg.kind == SFD_SEISMIC2) CK(seis2_resident_launch(seis2_resident_args(h, nsteps), h->stream));
+    else CK(em2_resident_launch(resident_args(h, nsteps), h->stream));
     k_reduce_slots<<<1, 1024, 0, h->stream>>>(ctl, slots, L.nslots);
     CK(cudaGetLastError());
     h->step += nsteps;
@@ -1210,8 +1252,9 @@ int32_t sfd_on_chip(sfd_handle* h, int32_t* tiles_x, int32_t* tiles_z) {  // til
   g_err.clear();
   if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
   const bool on = resident_usable(h);
-  if (tiles_x) *tiles_x = on ? h->res_plan.ntiles : 0;
-  if (tiles_z) *tiles_z = on ? h->res_plan.ntz : 0;
+  const bool s2 = h->cfg.kind == SFD_SEISMIC2;
+  if (tiles_x) *tiles_x = on ? (s2 ? h->s2_plan.ntx * h->s2_plan.ntz : h->res_plan.ntiles) : 0;
+  if (tiles_z) *tiles_z = on ? (s2 ? h->s2_plan.ntz : h->res_plan.ntz) : 0;
   return on ? 1 : 0;
 }
 
