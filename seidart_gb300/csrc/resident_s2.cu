@@ -42,8 +42,12 @@ constexpr int kS2CellThreads = 256;
 constexpr int kS2Threads = 32 * kS2ExchangeWarps + kS2CellThreads;
 constexpr int kS2MaxTile = 128;  // tile width and height: two fields of one side fit one warp's poll
 
+// Fields with their halo ring, coefficients, memory variables and the axis
+// tables of the tile's columns and rows (floats), then the cell order
+// (16-bit (row << 7) | column per cell).
 size_t s2_smem(int TW, int TZ) {
-  return sizeof(float) * (5 * (size_t)(TZ + 2) * (TW + 2) + 20 * (size_t)TZ * TW);
+  return sizeof(float) * (5 * (size_t)(TZ + 2) * (TW + 2) + 20 * (size_t)TZ * TW + 6 * (size_t)TW + 7 * (size_t)TZ) +
+         2 * (((size_t)TZ * TW + 1) & ~(size_t)1);
 }
 
 // One warp: copy n words of src0 into dst0[q * st0] and, when src1 is given,
@@ -108,6 +112,9 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
   float* F = smem;         // vx vz sxx szz sxz, (tz + 2) x (tw + 2) with the halo ring
   float* C = F + 5 * FS;   // A11 A13 A15 A33 A35 B15 B35 B55 dtrx dtrz gxp gzp, tz x tw
   float* M = C + 12 * CS;  // m_vxx m_vzz m_vxz m_vzx m_sxx_x m_szz_z m_sxz_x m_sxz_z, tz x tw
+  float* XT = M + 8 * CS;  // x tables at the tile's columns: ik ad b ikh adh bh, tw each
+  float* ZT = XT + 6 * tw;  // z tables at the tile's rows, then q3, tz each
+  unsigned short* CELL = reinterpret_cast<unsigned short*>(ZT + 7 * tz);  // cell order, see cell_at
   float* VX = F;
   float* VZ = F + FS;
   float* SXX = F + 2 * FS;
@@ -161,6 +168,12 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
       M[7 * CS + q] = a.m_sxz_z[mz];
     }
   }
+  {
+    const float* xs[6] = {a.X.ik, a.X.ad, a.X.b, a.X.ikh, a.X.adh, a.X.bh};
+    const float* zs[7] = {a.Z.ik, a.Z.ad, a.Z.b, a.Z.ikh, a.Z.adh, a.Z.bh, a.q3};
+    for (int q = tid; q < 6 * tw; q += kS2Threads) XT[q] = xs[q / tw][x0 + q % tw];
+    for (int q = tid; q < 7 * tz; q += kS2Threads) ZT[q] = zs[q / tz][z0 + q % tz];
+  }
   for (int q = tid; q < a.io.nrec; q += kS2Threads) {  // receivers of this tile
     const int i = a.io.rec[3 * q], k = a.io.rec[3 * q + 2];
     if (i >= x0 && i < x1 && k >= z0 && k < z1) {
@@ -177,7 +190,8 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
 
   // Cell n of this tile in perimeter-first order: the first and last rows,
   // then the first and last columns, then the interior row by row.
-  auto cell_at = [&](int n, int& lr, int& lc) {
+  // Tabulated once (CELL) so the steps do no division.
+  auto cell_order = [&](int n, int& lr, int& lc) {
     if (tz <= 2 || tw <= 2) {
       lr = n / tw;
       lc = n - lr * tw;
@@ -193,6 +207,17 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
       lr = 1 + m / (tw - 2);
       lc = 1 + m % (tw - 2);
     }
+  };
+  for (int n = tid; n < CS; n += kS2Threads) {
+    int lr, lc;
+    cell_order(n, lr, lc);
+    CELL[n] = (unsigned short)((lr << 7) | lc);
+  }
+  __syncthreads();
+  auto cell_at = [&](int n, int& lr, int& lc) {
+    const unsigned e = CELL[n];
+    lr = (int)(e >> 7);
+    lc = (int)(e & 127u);
   };
   auto record = [&](int t) {  // receivers of step t, by the exchange warps
     float* tr = a.io.traces + (size_t)t * 2 * a.io.nrec;
@@ -248,20 +273,20 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
         const bool loop2 = (k <= NZ - 2) && (i >= 1);
         if (loop1 || loop2) {
           const float vx0 = VX[f], vz0 = VZ[f];
-          const float ikx = __ldg(a.X.ik + i), ikxh = __ldg(a.X.ikh + i);
-          const float ikz = __ldg(a.Z.ik + k), ikzh = __ldg(a.Z.ikh + k);
+          const float ikx = XT[lc], ikxh = XT[3 * tw + lc];
+          const float ikz = ZT[lr], ikzh = ZT[3 * tz + lr];
           if (loop1) {
             const float d_vx_x = VX[f + 1] - vx0;
             const float d_vz_z = vz0 - VZ[f - SW];
             const float d_vz_x = VZ[f + 1] - vz0;
             const float d_vx_z = vx0 - VX[f - SW];
             if (xs) {
-              mvxx = __ldg(a.q3 + k) * mvxx + __ldg(a.X.adh + i) * d_vx_x;  // b_x_half(j), :255
-              mvzx = __ldg(a.X.b + i) * mvzx + __ldg(a.X.ad + i) * d_vz_x;
+              mvxx = ZT[6 * tz + lr] * mvxx + XT[4 * tw + lc] * d_vx_x;  // b_x_half(j), :255
+              mvzx = XT[2 * tw + lc] * mvzx + XT[tw + lc] * d_vz_x;
             }
             if (zs) {
-              mvzz = __ldg(a.Z.b + k) * mvzz + __ldg(a.Z.ad + k) * d_vz_z;
-              mvxz = __ldg(a.Z.bh + k) * mvxz + __ldg(a.Z.adh + k) * d_vx_z;
+              mvzz = ZT[2 * tz + lr] * mvzz + ZT[tz + lr] * d_vz_z;
+              mvxz = ZT[5 * tz + lr] * mvxz + ZT[4 * tz + lr] * d_vx_z;
             }
             const float dvx_dx = d_vx_x * ikxh + mvxx;
             const float dvz_dz = d_vz_z * ikz + mvzz;
@@ -278,12 +303,12 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
             const float d_vz_x = vz0 - VZ[f - 1];
             const float d_vx_z = VX[f + SW] - vx0;
             if (xs) {
-              mvxx = __ldg(a.X.bh + i) * mvxx + __ldg(a.X.adh + i) * d_vx_x;
-              mvzx = __ldg(a.X.b + i) * mvzx + __ldg(a.X.ad + i) * d_vz_x;
+              mvxx = XT[5 * tw + lc] * mvxx + XT[4 * tw + lc] * d_vx_x;
+              mvzx = XT[2 * tw + lc] * mvzx + XT[tw + lc] * d_vz_x;
             }
             if (zs) {
-              mvzz = __ldg(a.Z.b + k) * mvzz + __ldg(a.Z.ad + k) * d_vz_z;
-              mvxz = __ldg(a.Z.bh + k) * mvxz + __ldg(a.Z.adh + k) * d_vx_z;
+              mvzz = ZT[2 * tz + lr] * mvzz + ZT[tz + lr] * d_vz_z;
+              mvxz = ZT[5 * tz + lr] * mvxz + ZT[4 * tz + lr] * d_vx_z;
             }
             const float dvx_dx = d_vx_x * ikxh + mvxx;
             const float dvz_dz = d_vz_z * ikz + mvzz;
@@ -346,14 +371,14 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
         if (k >= 1 && i >= 1) {  // vx loop, :317-336
           const float d1 = SXX[f] - SXX[f - 1];
           const float d2 = SXZ[f] - SXZ[f - SW];
-          float v1 = d1 * __ldg(a.X.ik + i), v2 = d2 * __ldg(a.Z.ik + k);
+          float v1 = d1 * XT[lc], v2 = d2 * ZT[lr];
           if (xs) {
-            const float m = __ldg(a.X.b + i) * M[4 * CS + q] + __ldg(a.X.ad + i) * d1;
+            const float m = XT[2 * tw + lc] * M[4 * CS + q] + XT[tw + lc] * d1;
             M[4 * CS + q] = m;
             v1 += m;
           }
           if (zs) {
-            const float m = __ldg(a.Z.b + k) * M[7 * CS + q] + __ldg(a.Z.ad + k) * d2;
+            const float m = ZT[2 * tz + lr] * M[7 * CS + q] + ZT[tz + lr] * d2;
             M[7 * CS + q] = m;
             v2 += m;
           }
@@ -366,14 +391,14 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
         if (k <= NZ - 2 && i <= NX - 2) {  // vz loop, :338-357
           const float d1 = SXZ[f + 1] - SXZ[f];
           const float d2 = SZZ[f + SW] - SZZ[f];
-          float v1 = d1 * __ldg(a.X.ikh + i), v2 = d2 * __ldg(a.Z.ikh + k);
+          float v1 = d1 * XT[3 * tw + lc], v2 = d2 * ZT[3 * tz + lr];
           if (xs) {
-            const float m = __ldg(a.X.bh + i) * M[6 * CS + q] + __ldg(a.X.adh + i) * d1;
+            const float m = XT[5 * tw + lc] * M[6 * CS + q] + XT[4 * tw + lc] * d1;
             M[6 * CS + q] = m;
             v1 += m;
           }
           if (zs) {
-            const float m = __ldg(a.Z.bh + k) * M[5 * CS + q] + __ldg(a.Z.adh + k) * d2;
+            const float m = ZT[5 * tz + lr] * M[5 * CS + q] + ZT[4 * tz + lr] * d2;
             M[5 * CS + q] = m;
             v2 += m;
           }
