@@ -51,6 +51,21 @@ struct ResScratch {
 };
 
 __host__ __device__ inline int res_nzp(int NZ) { return (NZ + 31) & ~31; }
+
+// Let `fn` take as much dynamic shared memory as the current device allows
+// (its opt-in limit less the kernel's static shared memory).  The limit is a
+// property of the function, shared by every handle: set to one plan's size,
+// a smaller plan prepared later would lower it below a larger plan's launch.
+inline cudaError_t res_allow_max_smem(const void* fn) {
+  int dev = 0, optin = 0;
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, fn);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+  return e;
+}
 // nf edge fields per direction type (two copies each): 2 for electromag2
 // (Ex/Hy rows, Ez/Hy columns), 6 for seismic2.
 inline size_t res_scratch_bytes(int P, int NZ, int nf = 2) {

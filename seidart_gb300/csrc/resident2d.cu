@@ -611,10 +611,8 @@ bool em2_resident_plan(int NX, int NZ, int npml, int max_ctas, size_t max_smem, 
 }
 
 cudaError_t em2_resident_prepare(const ResPlan& plan, int* ctas_per_sm) {
-  cudaError_t e = cudaFuncSetAttribute(em2_resident_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)plan.smem);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(em2_resident_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem);
+  cudaError_t e = res_allow_max_smem((const void*)em2_resident_kernel<false>);
+  if (e == cudaSuccess) e = res_allow_max_smem((const void*)em2_resident_kernel<true>);
   if (e != cudaSuccess) return e;
   int n0 = 0, n1 = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n0, em2_resident_kernel<false>, kResThreads, plan.smem);

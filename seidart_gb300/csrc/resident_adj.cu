@@ -787,7 +787,7 @@ size_t em2_adj_resident_smem(const ResPlan& plan, int NX, int NZ, int W) {
 cudaError_t em2_adj_resident_prepare(const ResPlan& plan, int NX, int NZ, int W, int* ctas_per_sm) {
   *ctas_per_sm = 0;
   const size_t smem = em2_adj_resident_smem(plan, NX, NZ, W);
-  cudaError_t e = cudaFuncSetAttribute(em2_adj_resident_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = res_allow_max_smem((const void*)em2_adj_resident_kernel);
   if (e != cudaSuccess) return e;
   // ask for no more shared memory than the largest tile needs, so the rest of
   // the SM's on-chip memory serves as L1 (it holds the kernel's register spills)

@@ -501,8 +501,7 @@ bool seis2_resident_plan(int NX, int NZ, int max_ctas, size_t max_smem, Seis2Res
 }
 
 cudaError_t seis2_resident_prepare(const Seis2ResPlan& plan, int* ctas_per_sm) {
-  cudaError_t e =
-      cudaFuncSetAttribute(seis2_resident_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem);
+  cudaError_t e = res_allow_max_smem((const void*)seis2_resident_kernel);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, seis2_resident_kernel, kS2Threads, plan.smem);
 }

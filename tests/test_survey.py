@@ -163,6 +163,24 @@ def test_gpu_runner_batches_shots_like_the_oracle(gpu):
 
 
 @pytest.mark.gpu
+def test_gpu_runner_with_a_model_too_large_for_chip(gpu):
+    """A seismic2 grid too large for the on-chip form (700 x 600 cells) in
+    one batched launch with shots and a small model that fit on chip, all
+    against the oracle."""
+    from helpers import make_solver
+    big = sy.small_case(SEISMIC2, seed=13, nx=700, nz=600, npml=10, nstep=40, nrec=6)
+    cases = _survey_cases() + [big]
+    with make_solver(big) as s:
+        assert s.on_chip() is None
+    with make_solver(cases[-2]) as s:
+        assert s.on_chip() is not None
+    got = survey.run_survey(cases)
+    for c, tr in zip(cases, got):
+        e = rel_l2(tr, run_oracle(c)[1])
+        assert e <= 1e-5, f"{c.name}: rel L2 {e:.2e}"
+
+
+@pytest.mark.gpu
 def test_gpu_common_offset_image(gpu):
     base, src, rec = _co_args()
     co = survey.CommonOffset(base.grid, base.planes, base.profiles, base.srcfn, src, rec, "Ex").co_run()
