@@ -1,6 +1,7 @@
 // Single-pass time steps of the 2-D solvers (electromag2, seismic2).
 //
-// One launch per time step.  A block owns a tile of 32 x (8*ZB) cells; it
+// One launch per time step.  A block owns a tile of 8*ZB rows (128 cells wide
+// for electromag2, 32 for seismic2); it
 // first computes the first half-step (Hy, or the three stresses) on its tile
 // plus the one-cell halo the second half-step needs, keeping those values in
 // shared memory, then performs the second half-step (Ex/Ez, or vx/vz) on its

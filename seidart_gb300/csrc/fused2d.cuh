@@ -1,7 +1,9 @@
 // Tile bodies of the single-pass 2-D steps, shared by the per-model kernels
-// (fused2d.cu) and the persistent batched kernel (batch.cu).  A tile is
-// 32 x (8*ZB) cells handled by a 32 x 8 thread block; thread (tx, ty) owns
-// rows z0 + ty + 8 r, r < ZB.  The one-cell halo of the first half-step is
+// (fused2d.cu) and the persistent batched kernel (batch.cu).  A 32 x 8
+// thread block handles a tile of 8*ZB rows: thread (tx, ty) owns rows
+// z0 + ty + 8 r, r < ZB, and in each row four consecutive cells (electromag2,
+// 128-cell-wide tiles) or one (seismic2, 32-cell-wide tiles).  The one-cell
+// halo of the first half-step is
 // computed by whole warps (warp w takes one halo side, one cell per lane), so
 // no warp diverges lane by lane.  Everything read from the "old" copy, the
 // coefficients and the axis tables is read-only during a step and goes
