@@ -7,7 +7,10 @@
 // processes tiles b, b + G, b + 2G, ... with the tile bodies of the per-model
 // kernels, then all blocks meet at a grid barrier before the next step.  A
 // model's step reads the ping-pong copy p = (cur + s) & 1 and writes the
-// other, so the barrier is the only synchronisation.
+// other, so the barrier is the only synchronisation.  The tile bodies read
+// the fields with coherent loads here (RO = false): a field read through the
+// read-only path must not be written during the launch, and this launch
+// writes every field in its earlier steps.
 //
 // The barrier spins on a generation counter with a time limit
 // (%globaltimer); on expiry it records an error that the host reads
@@ -56,7 +59,7 @@ __device__ bool grid_barrier(GridBarrier* bar, unsigned nblocks, unsigned long l
     __threadfence();
   }
   __syncthreads();
-  __threadfence();  // later loads of other blocks' writes go to L2, not stale L1 lines
+  __threadfence();  // orders this block's later (coherent) field loads after the other blocks' writes
   return ok != 0;
 }
 
@@ -80,10 +83,10 @@ __global__ void __launch_bounds__(256, 3)
       const int p = (md.cur + s) & 1;
       if (md.kind == SFD_BATCH_EM2) {
         const Em2Step& a = md.em2[p];
-        em2_tile<ZB>(a, a.io.ctl->base + s, bx, by, md.gx, sm.em2);
+        em2_tile<ZB, false>(a, a.io.ctl->base + s, bx, by, md.gx, sm.em2);
       } else {
         const Seis2Step& a = md.s2[p];
-        seis2_tile<ZB>(a, a.io.ctl->base + s, bx, by, md.gx, sm.s2);
+        seis2_tile<ZB, false>(a, a.io.ctl->base + s, bx, by, md.gx, sm.s2);
       }
       __syncthreads();  // shared tile buffers are reused by the next tile
     }

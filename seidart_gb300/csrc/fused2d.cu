@@ -25,13 +25,13 @@ constexpr int TX = 32, TY = 8;
 template <int ZB>
 __global__ void __launch_bounds__(TX * TY) em2_step_kernel(Em2Step a, int rel) {
   __shared__ __align__(16) float sH[TY * ZB + 1][kEm2Row];
-  em2_tile<ZB>(a, a.io.ctl->base + rel, blockIdx.x, blockIdx.y, gridDim.x, sH);
+  em2_tile<ZB, true>(a, a.io.ctl->base + rel, blockIdx.x, blockIdx.y, gridDim.x, sH);
 }
 
 template <int ZB>
 __global__ void __launch_bounds__(TX * TY) seis2_step_kernel(Seis2Step a, int rel) {
   __shared__ float sS[3][TY * ZB + 2][TX + 2];
-  seis2_tile<ZB>(a, a.io.ctl->base + rel, blockIdx.x, blockIdx.y, gridDim.x, sS);
+  seis2_tile<ZB, true>(a, a.io.ctl->base + rel, blockIdx.x, blockIdx.y, gridDim.x, sS);
 }
 
 __global__ void em2_step_finalize_kernel(Em2Step a, int t_last) {

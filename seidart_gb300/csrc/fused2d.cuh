@@ -5,38 +5,52 @@
 // 128-cell-wide tiles) or one (seismic2, 32-cell-wide tiles).  The one-cell
 // halo of the first half-step is
 // computed by whole warps (warp w takes one halo side, one cell per lane), so
-// no warp diverges lane by lane.  Everything read from the "old" copy, the
-// coefficients and the axis tables is read-only during a step and goes
-// through the non-coherent cache (__ldg).
+// no warp diverges lane by lane.  The coefficients and axis tables go
+// through the non-coherent cache (__ldg).  So do the fields of the "old"
+// copy when the launch writes none of them (RO = true: one launch per step);
+// a persistent launch that writes them in its earlier steps (the batched
+// kernel) reads them with coherent loads (RO = false).
 #pragma once
 #include "sfd_solvers.h"
 
 namespace sfd {
+
+template <bool RO>
+__device__ __forceinline__ float fld(const float* p) {
+  if constexpr (RO) return __ldg(p);
+  else return *p;
+}
+template <bool RO>
+__device__ __forceinline__ float4 fld4(const float* p) {
+  if constexpr (RO) return __ldg(reinterpret_cast<const float4*>(p));
+  else return *reinterpret_cast<const float4*>(p);
+}
 
 // ---------------------------------------------------------------------------
 // electromag2
 
 // Hy at (i, k) after the H half-step, from the old state
 // (electromagfdtd.f95:249-262).  Valid for i <= NX-2, k <= NZ-2.
+template <bool RO>
 __device__ __forceinline__ float em2_h_cell(const Em2Step& a, int i, int k, float& pz, float& px, bool& zs,
                                             bool& xs) {
   const int P = a.P, W = a.W;
   const int c = k * P + i;
-  const float dEx = __ldg(a.Ex0 + c + P) - __ldg(a.Ex0 + c);
+  const float dEx = fld<RO>(a.Ex0 + c + P) - fld<RO>(a.Ex0 + c);
   float vz = dEx * __ldg(a.Z.ik + k);
   zs = in_strip(k, a.NZ, W);
   if (zs) {
-    pz = __ldg(a.Z.b + k) * __ldg(a.mExz0 + strip_idx(k, a.NZ, W) * P + i) + __ldg(a.Z.ad + k) * dEx;
+    pz = __ldg(a.Z.b + k) * fld<RO>(a.mExz0 + strip_idx(k, a.NZ, W) * P + i) + __ldg(a.Z.ad + k) * dEx;
     vz += pz;
   }
-  const float dEz = __ldg(a.Ez0 + c + 1) - __ldg(a.Ez0 + c);
+  const float dEz = fld<RO>(a.Ez0 + c + 1) - fld<RO>(a.Ez0 + c);
   float vx = dEz * __ldg(a.X.ik + i);
   xs = in_strip(i, a.NX, W);
   if (xs) {
-    px = __ldg(a.X.b + i) * __ldg(a.mEzx0 + k * (2 * W) + strip_idx(i, a.NX, W)) + __ldg(a.X.ad + i) * dEz;
+    px = __ldg(a.X.b + i) * fld<RO>(a.mEzx0 + k * (2 * W) + strip_idx(i, a.NX, W)) + __ldg(a.X.ad + i) * dEz;
     vx += px;
   }
-  return __ldg(a.Hy0 + c) + a.dbH * (vx + vz);
+  return fld<RO>(a.Hy0 + c) + a.dbH * (vx + vz);
 }
 
 __device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
@@ -51,7 +65,7 @@ constexpr int kEm2Row = 132;
 // Four consecutive cells per thread along x: the tile is 128 x (8*ZB) cells
 // and every field, coefficient and table access of a row is one 16-byte load
 // or store.
-template <int ZB>
+template <int ZB, bool RO>
 __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by, int gridx,
                                          float (*sH)[kEm2Row]) {
   const int NX = a.NX, NZ = a.NZ, P = a.P, W = a.W;
@@ -76,15 +90,15 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
   // variables of the new copy.
   auto h_row = [&](int k, bool own, float4& hv) {
     const int c0 = k * P + i0;
-    const float4 hy = active ? ld4(a.Hy0 + c0) : zero4;
-    const float4 ex = active ? ld4(a.Ex0 + c0) : zero4;
-    const float4 exn = active ? ld4(a.Ex0 + c0 + P) : zero4;
-    const float4 ez = active ? ld4(a.Ez0 + c0) : zero4;
+    const float4 hy = active ? fld4<RO>(a.Hy0 + c0) : zero4;
+    const float4 ex = active ? fld4<RO>(a.Ex0 + c0) : zero4;
+    const float4 exn = active ? fld4<RO>(a.Ex0 + c0 + P) : zero4;
+    const float4 ez = active ? fld4<RO>(a.Ez0 + c0) : zero4;
     float ez_next = __shfl_down_sync(0xffffffffu, ez.x, 1);
-    if (tx == 31) ez_next = (i0 + 4 < NX) ? __ldg(a.Ez0 + c0 + 4) : 0.f;
+    if (tx == 31) ez_next = (i0 + 4 < NX) ? fld<RO>(a.Ez0 + c0 + 4) : 0.f;
     const bool zs = in_strip(k, NZ, W);
     const int zrow = (zs ? strip_idx(k, NZ, W) : 0) * P + i0;
-    const float4 pz0 = (zs && active) ? ld4(a.mExz0 + zrow) : zero4;
+    const float4 pz0 = (zs && active) ? fld4<RO>(a.mExz0 + zrow) : zero4;
     const float ikz = __ldg(a.Z.ik + k), adz = __ldg(a.Z.ad + k), bz = __ldg(a.Z.b + k);
     float4 pz1 = pz0, hy1 = hy;
 #pragma unroll
@@ -101,7 +115,7 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
         float vx = dEz * el(ikx4, e);
         if (in_strip(i, NX, W)) {
           const int m = k * (2 * W) + strip_idx(i, NX, W);
-          const float px = el(bx4, e) * __ldg(a.mEzx0 + m) + el(adx4, e) * dEz;
+          const float px = el(bx4, e) * fld<RO>(a.mEzx0 + m) + el(adx4, e) * dEz;
           if (own) a.mEzx1[m] = px;
           vx += px;
         }
@@ -112,7 +126,7 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
         el(hv, e) = el(hy, e);
         if (own && i < NX && in_strip(i, NX, W)) {
           const int m = k * (2 * W) + strip_idx(i, NX, W);
-          a.mEzx1[m] = __ldg(a.mEzx0 + m);
+          a.mEzx1[m] = fld<RO>(a.mEzx0 + m);
         }
       }
     }
@@ -137,9 +151,9 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
     for (int r = 0; r < ZB; ++r) {
       const int k = z0 + ty + 8 * r;
       const int c0 = k * P + i0;
-      const float4 hy = ld4(a.Hy0 + c0), ex = ld4(a.Ex0 + c0), exn = ld4(a.Ex0 + c0 + P), ez = ld4(a.Ez0 + c0);
+      const float4 hy = fld4<RO>(a.Hy0 + c0), ex = fld4<RO>(a.Ex0 + c0), exn = fld4<RO>(a.Ex0 + c0 + P), ez = fld4<RO>(a.Ez0 + c0);
       float ez_next = __shfl_down_sync(0xffffffffu, ez.x, 1);
-      if (tx == 31) ez_next = __ldg(a.Ez0 + c0 + 4);
+      if (tx == 31) ez_next = fld<RO>(a.Ez0 + c0 + 4);
       const float ikz = __ldg(a.Z.ik + k);
       float4 hv;
 #pragma unroll
@@ -163,19 +177,19 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
         h_row(k, true, hv);
       } else if (active) {  // row NZ-1 lies outside the H loop: carried over
         const int c0 = k * P + i0;
-        hv = ld4(a.Hy0 + c0);
+        hv = fld4<RO>(a.Hy0 + c0);
         st4(a.Hy1 + c0, hv);
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
           const int i = i0 + e;
           if (i < NX && in_strip(i, NX, W)) {
             const int m = k * (2 * W) + strip_idx(i, NX, W);
-            a.mEzx1[m] = __ldg(a.mEzx0 + m);
+            a.mEzx1[m] = fld<RO>(a.mEzx0 + m);
           }
         }
         if (in_strip(k, NZ, W)) {
           const int zrow = strip_idx(k, NZ, W) * P + i0;
-          st4(a.mExz1 + zrow, ld4(a.mExz0 + zrow));
+          st4(a.mExz1 + zrow, fld4<RO>(a.mExz0 + zrow));
         }
       }
       *reinterpret_cast<float4*>(&sH[ty + 8 * r + 1][sx]) = hv;
@@ -195,7 +209,7 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
       if (x0 > 0 && k <= NZ - 2) {
         float pz, px;
         bool zs, xs;
-        sH[q + 1][3] = em2_h_cell(a, x0 - 1, k, pz, px, zs, xs);
+        sH[q + 1][3] = em2_h_cell<RO>(a, x0 - 1, k, pz, px, zs, xs);
       }
     }
   }
@@ -208,7 +222,7 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
       const int k = z0 + ty + 8 * r;
       const int c0 = k * P + i0;
       const int kk = ty + 8 * r + 1;
-      float4 ex = ld4(a.Ex0 + c0), ez = ld4(a.Ez0 + c0);
+      float4 ex = fld4<RO>(a.Ex0 + c0), ez = fld4<RO>(a.Ez0 + c0);
       const float4 cax = ld4(a.CAx + c0), cbx = ld4(a.CBx + c0), caz = ld4(a.CAz + c0), cbz = ld4(a.CBz + c0);
       const float4 h = *reinterpret_cast<const float4*>(&sH[kk][sx]);
       const float4 hm = *reinterpret_cast<const float4*>(&sH[kk - 1][sx]);
@@ -234,7 +248,7 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
     if (k < NZ && active) {
       const int c0 = k * P + i0;
       const int kk = ty + 8 * r + 1;
-      float4 ex = ld4(a.Ex0 + c0), ez = ld4(a.Ez0 + c0);
+      float4 ex = fld4<RO>(a.Ex0 + c0), ez = fld4<RO>(a.Ez0 + c0);
       const float4 cax = ld4(a.CAx + c0), cbx = ld4(a.CBx + c0), caz = ld4(a.CAz + c0), cbz = ld4(a.CBz + c0);
       const float4 h = *reinterpret_cast<const float4*>(&sH[kk][sx]);
       const float4 hm = *reinterpret_cast<const float4*>(&sH[kk - 1][sx]);
@@ -300,31 +314,32 @@ struct S2Stress {
 // The three stresses at (i, k) after both stress loops of one step, from the
 // old state (seismicfdtd.f95:247-312), with the shared velocity-gradient
 // memory variables advanced once per loop that visits the cell.
+template <bool RO>
 __device__ __forceinline__ S2Stress seis2_stress_cell(const Seis2Step& a, int i, int k) {
   const int NX = a.NX, NZ = a.NZ, P = a.P, W = a.W;
   const int c = k * P + i;
   S2Stress o;
-  o.sxx = __ldg(a.sxx0 + c);
-  o.szz = __ldg(a.szz0 + c);
-  o.sxz = __ldg(a.sxz0 + c);
+  o.sxx = fld<RO>(a.sxx0 + c);
+  o.szz = fld<RO>(a.szz0 + c);
+  o.sxz = fld<RO>(a.sxz0 + c);
   o.xs = in_strip(i, NX, W);
   o.zs = in_strip(k, NZ, W);
   o.mvxx = o.mvzx = o.mvzz = o.mvxz = 0.f;
   const int mx = k * (2 * W) + (o.xs ? strip_idx(i, NX, W) : 0);
   const int mz = (o.zs ? strip_idx(k, NZ, W) : 0) * P + i;
-  if (o.xs) { o.mvxx = __ldg(a.m_vxx0 + mx); o.mvzx = __ldg(a.m_vzx0 + mx); }
-  if (o.zs) { o.mvzz = __ldg(a.m_vzz0 + mz); o.mvxz = __ldg(a.m_vxz0 + mz); }
+  if (o.xs) { o.mvxx = fld<RO>(a.m_vxx0 + mx); o.mvzx = fld<RO>(a.m_vzx0 + mx); }
+  if (o.zs) { o.mvzz = fld<RO>(a.m_vzz0 + mz); o.mvxz = fld<RO>(a.m_vxz0 + mz); }
   const bool loop1 = (k >= 1) && (i <= NX - 2);
   const bool loop2 = (k <= NZ - 2) && (i >= 1);
   if (!loop1 && !loop2) return o;
-  const float vx0 = __ldg(a.vx0 + c), vz0 = __ldg(a.vz0 + c);
+  const float vx0 = fld<RO>(a.vx0 + c), vz0 = fld<RO>(a.vz0 + c);
   const float ikx = __ldg(a.X.ik + i), ikxh = __ldg(a.X.ikh + i);
   const float ikz = __ldg(a.Z.ik + k), ikzh = __ldg(a.Z.ikh + k);
   if (loop1) {
-    const float d_vx_x = __ldg(a.vx0 + c + 1) - vx0;
-    const float d_vz_z = vz0 - __ldg(a.vz0 + c - P);
-    const float d_vz_x = __ldg(a.vz0 + c + 1) - vz0;
-    const float d_vx_z = vx0 - __ldg(a.vx0 + c - P);
+    const float d_vx_x = fld<RO>(a.vx0 + c + 1) - vx0;
+    const float d_vz_z = vz0 - fld<RO>(a.vz0 + c - P);
+    const float d_vz_x = fld<RO>(a.vz0 + c + 1) - vz0;
+    const float d_vx_z = vx0 - fld<RO>(a.vx0 + c - P);
     if (o.xs) {
       o.mvxx = __ldg(a.q3 + k) * o.mvxx + __ldg(a.X.adh + i) * d_vx_x;  // b_x_half(j), :255
       o.mvzx = __ldg(a.X.b + i) * o.mvzx + __ldg(a.X.ad + i) * d_vz_x;
@@ -344,10 +359,10 @@ __device__ __forceinline__ S2Stress seis2_stress_cell(const Seis2Step& a, int i,
     o.szz = o.szz + (A13 * dvx_dx + A33 * dvz_dz + A35 * shear);
   }
   if (loop2) {
-    const float d_vx_x = vx0 - __ldg(a.vx0 + c - 1);
-    const float d_vz_z = __ldg(a.vz0 + c + P) - vz0;
-    const float d_vz_x = vz0 - __ldg(a.vz0 + c - 1);
-    const float d_vx_z = __ldg(a.vx0 + c + P) - vx0;
+    const float d_vx_x = vx0 - fld<RO>(a.vx0 + c - 1);
+    const float d_vz_z = fld<RO>(a.vz0 + c + P) - vz0;
+    const float d_vz_x = vz0 - fld<RO>(a.vz0 + c - 1);
+    const float d_vx_z = fld<RO>(a.vx0 + c + P) - vx0;
     if (o.xs) {
       o.mvxx = __ldg(a.X.bh + i) * o.mvxx + __ldg(a.X.adh + i) * d_vx_x;
       o.mvzx = __ldg(a.X.b + i) * o.mvzx + __ldg(a.X.ad + i) * d_vz_x;
@@ -366,7 +381,7 @@ __device__ __forceinline__ S2Stress seis2_stress_cell(const Seis2Step& a, int i,
   return o;
 }
 
-template <int ZB>
+template <int ZB, bool RO>
 __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, int by, int gridx,
                                            float (*sS)[8 * ZB + 2][34]) {
   const int NX = a.NX, NZ = a.NZ, P = a.P, W = a.W;
@@ -393,12 +408,12 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
       const int k = z0 + ty + 8 * r;
       const int c = k * P + i;
       const float ikz = __ldg(a.Z.ik + k), ikzh = __ldg(a.Z.ikh + k);
-      const float vx0 = __ldg(a.vx0 + c), vz0 = __ldg(a.vz0 + c);
-      const float vxl = __ldg(a.vx0 + c - 1), vxr = __ldg(a.vx0 + c + 1);
-      const float vxu = __ldg(a.vx0 + c - P), vxd = __ldg(a.vx0 + c + P);
-      const float vzl = __ldg(a.vz0 + c - 1), vzr = __ldg(a.vz0 + c + 1);
-      const float vzu = __ldg(a.vz0 + c - P), vzd = __ldg(a.vz0 + c + P);
-      float sxx = __ldg(a.sxx0 + c), szz = __ldg(a.szz0 + c), sxz = __ldg(a.sxz0 + c);
+      const float vx0 = fld<RO>(a.vx0 + c), vz0 = fld<RO>(a.vz0 + c);
+      const float vxl = fld<RO>(a.vx0 + c - 1), vxr = fld<RO>(a.vx0 + c + 1);
+      const float vxu = fld<RO>(a.vx0 + c - P), vxd = fld<RO>(a.vx0 + c + P);
+      const float vzl = fld<RO>(a.vz0 + c - 1), vzr = fld<RO>(a.vz0 + c + 1);
+      const float vzu = fld<RO>(a.vz0 + c - P), vzd = fld<RO>(a.vz0 + c + P);
+      float sxx = fld<RO>(a.sxx0 + c), szz = fld<RO>(a.szz0 + c), sxz = fld<RO>(a.sxz0 + c);
       {  // :247-283
         const float dvx_dx = (vxr - vx0) * ikxh, dvz_dz = (vz0 - vzu) * ikz;
         const float dvz_dx = (vzr - vz0) * ikx, dvx_dz = (vx0 - vxu) * ikzh;
@@ -426,7 +441,7 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
     const int k = z0 + ty + 8 * r;
     if (i < NX && k < NZ) {
       const int c = k * P + i;
-      const S2Stress s = seis2_stress_cell(a, i, k);
+      const S2Stress s = seis2_stress_cell<RO>(a, i, k);
       a.sxx1[c] = s.sxx;
       a.szz1[c] = s.szz;
       a.sxz1[c] = s.sxz;
@@ -456,7 +471,7 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
       else if (ty == 2) { hi = x0 - 1; hk = z0 + q; si = 0; sk = q + 1; }
       else { hi = x0 + 32; hk = z0 + q; si = 33; sk = q + 1; }
       if (hi >= 0 && hi < NX && hk >= 0 && hk < NZ) {
-        const S2Stress s = seis2_stress_cell(a, hi, hk);
+        const S2Stress s = seis2_stress_cell<RO>(a, hi, hk);
         sS[0][sk][si] = s.sxx;
         sS[1][sk][si] = s.szz;
         sS[2][sk][si] = s.sxz;
@@ -475,7 +490,7 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
       const int kk = ty + 8 * r + 1, ii = tx + 1;
       const float v1 = (sS[0][kk][ii] - sS[0][kk][ii - 1]) * ikx, v2 = (sS[2][kk][ii] - sS[2][kk - 1][ii]) * __ldg(a.Z.ik + k);
       const float w1 = (sS[2][kk][ii + 1] - sS[2][kk][ii]) * ikxh, w2 = (sS[1][kk + 1][ii] - sS[1][kk][ii]) * __ldg(a.Z.ikh + k);
-      float vx = __ldg(a.vx0 + c), vz = __ldg(a.vz0 + c);
+      float vx = fld<RO>(a.vx0 + c), vz = fld<RO>(a.vz0 + c);
       if (a.atten) {
         vx *= __ldg(a.gxp + c);
         vz *= __ldg(a.gzp + c);
@@ -513,7 +528,7 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
           v2 += m;
         }
         if (interior) {
-          vx = __ldg(a.vx0 + c);
+          vx = fld<RO>(a.vx0 + c);
           if (a.atten) vx *= __ldg(a.gxp + c);
           vx = vx + (v1 + v2) * __ldg(a.dtrx + c);
         }
@@ -533,7 +548,7 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
           v2 += m;
         }
         if (interior) {
-          vz = __ldg(a.vz0 + c);
+          vz = fld<RO>(a.vz0 + c);
           if (a.atten) vz *= __ldg(a.gzp + c);
           vz = vz + (v1 + v2) * __ldg(a.dtrz + c);
         }
