@@ -1,7 +1,7 @@
 """FP64 CPU oracle of the FDTD path -- TEST INFRASTRUCTURE ONLY.
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg may
-use this package, and only as the checker or the timed CPU baseline.  The
+use this package, and only as the reference results or the timed CPU baseline.  The
 product (seidart_gb300) never imports it.
 
 ``liboracle.so`` (built from fdtd_oracle.cpp by the Makefile here) restates the
