@@ -135,6 +135,19 @@ int32_t sfd_create(const sfd_config* cfg, void* dev_state, size_t state_bytes, v
  * (count = planes*NX*NZ).  Replaces the material_rw reads of the Fortran. */
 int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count);
 
+/* The same model as a material-id map: ids, device int32 [NZ][NX] (x
+ * fastest, the project image's material index per cell, CPML cells
+ * included), values in [0, nmat); table, host FP64 [nmat][planes] in
+ * sfd_set_model's plane order (count = nmat * planes, at most 2048 values).
+ * The update coefficients are formed on the device, in FP64, with the
+ * formulas of sfd_set_model, so both calls store the same coefficients; the
+ * FP64 planes never cross to the GPU.  electromag2 and seismic2 handles.  The
+ * id map must stay allocated while the handle may set a source or take an
+ * adjoint gradient (both read it).  Replaces the driver's expansion of the
+ * material table into per-cell .dat files (src/seidart/routines/
+ * classes.py:608-750) and their reads (readwrite_routines.f95:9-37). */
+int32_t sfd_set_model_ids(sfd_handle* h, const int32_t* ids, int32_t nmat, const double* table, int64_t count);
+
 /* CPML profiles, host FP64: for each axis (x, [y,] z) the arrays
  * K, a, b, K_half, a_half, b_half of the axis length, concatenated
  * (count = 6*(NX + [NY +] NZ)).  Replaces the loadcpml reads

@@ -1,0 +1,127 @@
+// Update coefficients from a material-id map, on the device.
+//
+// A SeidarT model is an image of material ids (one per cell, the PNG colour
+// index) and a table of material properties; the driver expands it into one
+// FP64 file per property (classes.py:608-750) that the Fortran reads back
+// (readwrite_routines.f95:9-37).  Here the id map (caller-owned device
+// int32, x fastest) and the table (passed by value) go to one kernel per
+// solver kind, which forms each cell's FP32 coefficients in FP64 with the
+// formulas of sfd_set_model, operation for operation, so both paths store
+// the same coefficients.  Ids outside [0, nmat) raise a flag in the handle's
+// control block and leave their cells' coefficients zero; the host rejects
+// the call.
+#include "../../include/seidart_gb300.h"
+#include "sfd_solvers.h"
+
+namespace sfd {
+
+namespace {
+
+constexpr double kEps0d = 8.85418782e-12;
+
+__device__ __forceinline__ bool id_ok(int id, int nmat) { return id >= 0 && id < nmat; }
+
+// electromag2 (electromagfdtd.f95:164-181): per cell ca, cb on the x and z
+// staggered points, averaged over the cell and its neighbour below (Ex
+// points, k >= 1) or to the left (Ez points, i >= 1), :282, :294.
+__device__ __forceinline__ void em2_cacb(const MatTable& m, int id, int d, double dt, double& ca, double& cb) {
+  const double* t = m.v + id * 6;  // eps11 eps13 eps33 sig11 sig13 sig33
+  const double ep = (d == 0 ? t[0] + t[1] : t[1] + t[2]) * kEps0d;
+  const double sg = d == 0 ? t[3] + t[4] : t[4] + t[5];
+  ca = (1.0 - sg * dt / (2.0 * ep)) / (1.0 + sg * dt / (2.0 * ep));
+  cb = (dt / ep) / (1.0 + sg * dt / (2.0 * ep));
+}
+
+__global__ void em2_coef_from_ids(const int* __restrict__ ids, MatTable m, int NX, int NZ, int P, double dt,
+                                  float* CAx, float* CBx, float* CAz, float* CBz, int* bad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= NX || k >= NZ) return;
+  const size_t n = (size_t)k * NX + i, c = (size_t)k * P + i;
+  const int id = ids[n];
+  float ax = 0.f, bx = 0.f, az = 0.f, bz = 0.f;
+  if (!id_ok(id, m.nmat)) {
+    atomicExch(bad, 1);
+  } else {
+    double ca, cb;
+    if (k >= 1) {
+      const int up = ids[n - NX];
+      if (id_ok(up, m.nmat)) {
+        double ca2, cb2;
+        em2_cacb(m, id, 0, dt, ca, cb);
+        em2_cacb(m, up, 0, dt, ca2, cb2);
+        ax = (float)((ca + ca2) / 2);
+        bx = (float)((cb + cb2) / 2);
+      }
+    }
+    if (i >= 1) {
+      const int lf = ids[n - 1];
+      if (id_ok(lf, m.nmat)) {
+        double ca2, cb2;
+        em2_cacb(m, id, 1, dt, ca, cb);
+        em2_cacb(m, lf, 1, dt, ca2, cb2);
+        az = (float)((ca + ca2) / 2);
+        bz = (float)((cb + cb2) / 2);
+      }
+    }
+  }
+  CAx[c] = ax;
+  CBx[c] = bx;
+  CAz[c] = az;
+  CBz[c] = bz;
+}
+
+// seismic2 (seismicfdtd.f95:247-357): planes c11 c13 c15 c33 c35 c55 rho
+// gamma_x gamma_z.  Stress-loop averages (c(i+1,k) + 2 c(i,k) + c(i,k-1))/4
+// and (c(i,k+1) + 2 c(i,k) + c(i-1,k))/4 times dt, dt/rho, the averaged
+// dt/rho of the vz points (:341, :355) and 1 - gamma.
+__global__ void seis2_coef_from_ids(const int* __restrict__ ids, MatTable m, int NX, int NZ, int P, double dt,
+                                    float* coef, size_t plane, int* bad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= NX || k >= NZ) return;
+  const size_t n = (size_t)k * NX + i, c = (size_t)k * P + i;
+  const int id = ids[n];
+  float out[12];
+#pragma unroll
+  for (int q = 0; q < 12; ++q) out[q] = 0.f;
+  auto val = [&](int cell_id, int q) { return m.v[cell_id * 9 + q]; };
+  auto okat = [&](int ii, int kk) { return id_ok(ids[(size_t)kk * NX + ii], m.nmat); };
+  if (!id_ok(id, m.nmat)) {
+    atomicExch(bad, 1);
+  } else {
+    const int A_src[5] = {0, 1, 2, 3, 4}, B_src[3] = {2, 4, 5};
+    if (i <= NX - 2 && k >= 1 && okat(i + 1, k) && okat(i, k - 1)) {
+      const int r = ids[n + 1], u = ids[n - NX];
+#pragma unroll
+      for (int q = 0; q < 5; ++q)
+        out[q] = (float)((val(r, A_src[q]) + 2 * val(id, A_src[q]) + val(u, A_src[q])) / 4 * dt);
+    }
+    if (k <= NZ - 2 && i >= 1 && okat(i, k + 1) && okat(i - 1, k)) {
+      const int d = ids[n + NX], l = ids[n - 1];
+#pragma unroll
+      for (int q = 0; q < 3; ++q)
+        out[5 + q] = (float)((val(d, B_src[q]) + 2 * val(id, B_src[q]) + val(l, B_src[q])) / 4 * dt);
+    }
+    const double rho = val(id, 6);
+    out[8] = (float)(dt / rho);  // seismicfdtd.f95:334
+    if (i <= NX - 2 && k <= NZ - 2 && okat(i + 1, k) && okat(i, k + 1))  // :341, :355
+      out[9] = (float)(dt / ((2 * rho + val(ids[n + 1], 6) + val(ids[n + NX], 6)) / 4));
+    out[10] = (float)(1.0 - val(id, 7));
+    out[11] = (float)(1.0 - val(id, 8));
+  }
+#pragma unroll
+  for (int q = 0; q < 12; ++q) coef[q * plane + c] = out[q];
+}
+
+}  // namespace
+
+void coef_from_ids(int kind, const int* ids, const MatTable& m, int NX, int NZ, int P, double dt, float* coef,
+                   size_t plane, int* bad, cudaStream_t s) {
+  const dim3 b(32, 8), g((NX + 31) / 32, (NZ + 7) / 8);
+  if (kind == SFD_ELECTROMAG2)
+    em2_coef_from_ids<<<g, b, 0, s>>>(ids, m, NX, NZ, P, dt, coef, coef + plane, coef + 2 * plane, coef + 3 * plane,
+                                      bad);
+  else
+    seis2_coef_from_ids<<<g, b, 0, s>>>(ids, m, NX, NZ, P, dt, coef, plane, bad);
+}
+
+}  // namespace sfd

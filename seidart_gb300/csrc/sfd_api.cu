@@ -278,6 +278,11 @@ struct sfd_handle_s {
   std::shared_ptr<double[]> model;
   int src_plane[4] = {0, 0, 0, 0};  // planes of `model` the source amplitude is divided by (complex: re, im pairs)
   const double* src_scale(int q) const { return model.get() + (size_t)src_plane[q] * cfg.nx * cfg.nz; }
+  // sfd_set_model_ids: the caller's device id map and the material table
+  // (rows of the kind's model planes); `model` is then expanded from them
+  // only when the adjoint needs it
+  const int32_t* mat_ids = nullptr;
+  std::shared_ptr<std::vector<double>> mat_table;
   // adjoint workspace (electromag2)
   char* adj = nullptr;
   int adj_seg = 0;
@@ -765,9 +770,101 @@ int32_t create_handle(const sfd_config* cfg, void* dev_state, size_t state_bytes
   return SFD_OK;
 }
 
+// Model plane (sfd_set_model's order) the source amplitude q is divided by,
+// for the kinds sfd_set_model_ids takes: electromag2 eps11, eps33; seismic2 rho.
+int src_full_plane(int kind, int q) {
+  if (kind == SFD_ELECTROMAG2) return q == 0 ? 0 : 2;
+  return 6;
+}
+
+// Divisor of source component q at cell n (host FP64 value of the model).
+int source_divisor(sfd_handle* h, int q, size_t n, double* out) {
+  if (!h->mat_ids) {
+    *out = h->src_scale(q)[n];
+    return SFD_OK;
+  }
+  int32_t id = 0;
+  CK(cudaMemcpyAsync(&id, h->mat_ids + n, sizeof id, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  const int np = nplanes(h->cfg.kind);
+  *out = (*h->mat_table)[(size_t)id * np + src_full_plane(h->cfg.kind, q)];
+  return SFD_OK;
+}
+
+// The FP64 model planes of an id-map model, expanded on the host when first
+// needed (the electromag2 adjoint's chain rule reads all six).
+int ensure_model_planes(sfd_handle* h) {
+  if (!h->mat_ids || h->model) return SFD_OK;
+  const size_t N2 = (size_t)h->cfg.nx * h->cfg.nz;
+  const int np = nplanes(h->cfg.kind);
+  std::vector<int32_t> ids(N2);
+  CK(cudaMemcpyAsync(ids.data(), h->mat_ids, sizeof(int32_t) * N2, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  std::shared_ptr<double[]> model(new double[(size_t)np * N2]);
+  const std::vector<double>& t = *h->mat_table;
+  parallel_for(N2, [&](size_t b, size_t e) {
+    for (size_t n = b; n < e; ++n)
+      for (int q = 0; q < np; ++q) model[(size_t)q * N2 + n] = t[(size_t)ids[n] * np + q];
+  });
+  h->model = std::move(model);
+  for (int q = 0; q < 4; ++q) h->src_plane[q] = src_full_plane(h->cfg.kind, q);  // all planes kept
+  return SFD_OK;
+}
+
 }  // namespace sfd
 
 extern "C" {
+
+int32_t sfd_set_model_ids(sfd_handle* h, const int32_t* dev_ids, int32_t nmat, const double* table, int64_t count) {
+  g_err.clear();
+  if (!h || !dev_ids || !table) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  const sfd_config& c = h->cfg;
+  if (c.kind != SFD_ELECTROMAG2 && c.kind != SFD_SEISMIC2)
+    return fail(SFD_ERR_BAD_ARG, "material-id models are implemented for electromag2 and seismic2");
+  const int np = nplanes(c.kind);
+  if (nmat < 1 || count != (int64_t)nmat * np)
+    return fail(SFD_ERR_BAD_ARG, "table needs nmat >= 1 rows of %d values (count = nmat * %d), got nmat %d, count %lld", np,
+                np, nmat, (long long)count);
+  if (count > kMatTableMax) return fail(SFD_ERR_BAD_ARG, "table holds at most %d values", kMatTableMax);
+  if (!all_finite(table, (size_t)count)) return fail(SFD_ERR_BAD_ARG, "table contains NaN or Inf");
+  cudaPointerAttributes attr;
+  cudaError_t pe = cudaPointerGetAttributes(&attr, dev_ids);
+  if (pe != cudaSuccess || attr.type != cudaMemoryTypeDevice) {
+    cudaGetLastError();
+    return fail(SFD_ERR_BAD_ARG, "ids must be device memory");
+  }
+  int atten = 0;
+  for (int m = 0; m < nmat; ++m) {  // the checks of sfd_set_model, per material
+    const double* t = table + (size_t)m * np;
+    if (c.kind == SFD_ELECTROMAG2) {
+      if (!((t[0] + t[1]) * kEps0 > 0) || !((t[1] + t[2]) * kEps0 > 0))
+        return fail(SFD_ERR_BAD_ARG, "permittivity must be positive (material %d)", m);
+    } else {
+      if (!(t[6] > 0)) return fail(SFD_ERR_BAD_ARG, "density must be positive (material %d)", m);
+      if (t[7] != 0.0 || t[8] != 0.0) atten = 1;
+    }
+  }
+  MatTable mt;
+  mt.nmat = nmat;
+  std::memcpy(mt.v, table, sizeof(double) * (size_t)count);
+  Ctl* ctl = (Ctl*)(h->base + h->L.off_ctl);
+  int* bad = &ctl->pad2;
+  CK(cudaMemsetAsync(bad, 0, sizeof(int), h->stream));
+  coef_from_ids(c.kind, dev_ids, mt, c.nx, c.nz, h->L.P, c.dt, h->coef(0), h->L.coef_plane, bad, h->stream);
+  CK(cudaGetLastError());
+  int flag = 0;
+  CK(cudaMemcpyAsync(&flag, bad, sizeof flag, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (flag) return fail(SFD_ERR_BAD_ARG, "material id outside [0, %d)", nmat);
+  if (c.kind == SFD_SEISMIC2) set_atten(h, atten);  // any material with attenuation (gamma = 0 cells multiply by 1)
+  h->mat_ids = dev_ids;
+  h->mat_table = std::make_shared<std::vector<double>>(table, table + count);
+  h->model.reset();
+  for (int q = 0; q < 4; ++q) h->src_plane[q] = src_full_plane(c.kind, q);
+  invalidate_graph(h);
+  h->have_model = true;
+  return SFD_OK;
+}
 
 int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
   g_err.clear();
@@ -1012,6 +1109,8 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
   CK(cudaStreamSynchronize(h->stream));  // host buffers go out of scope
   h->model = std::move(model);
   std::memcpy(h->src_plane, src_plane, sizeof src_plane);
+  h->mat_ids = nullptr;
+  h->mat_table.reset();
   invalidate_graph(h);                   // kernel arguments (atten) may change
   h->have_model = true;
   return SFD_OK;
@@ -1088,7 +1187,9 @@ int32_t sfd_set_source(sfd_handle* h, int32_t i, int32_t j, int32_t k, const dou
     }
   } else {
     for (int q = 0; q < ncomp; ++q) {
-      const double s = h->src_scale(q)[n];
+      double s = 0.0;
+      int r = source_divisor(h, q, n, &s);
+      if (r) return r;
       for (int t = 0; t < nstep; ++t) amp[(size_t)q * c.nstep + t] = (float)(srcfn[(size_t)q * nstep + t] * c.dt / s);
     }
   }
@@ -1760,6 +1861,8 @@ int32_t sfd_adjoint_gradient(sfd_handle* h, double* out, int64_t count) {
   CK(cudaStreamSynchronize(h->stream));
   if (ctl.err) return fail(SFD_ERR_TIMEOUT, "on-chip adjoint sweep: a neighbouring tile did not answer within 2 s");
   const double dt = h->cfg.dt;
+  r = ensure_model_planes(h);
+  if (r) return r;
   const double *e11 = h->model.get(), *e13 = e11 + N2, *e33 = e11 + 2 * N2;
   const double *s11 = e11 + 3 * N2, *s13 = e11 + 4 * N2, *s33 = e11 + 5 * N2;
   double *g11 = out, *g13 = out + N2, *g33 = out + 2 * N2, *gs11 = out + 3 * N2, *gs13 = out + 4 * N2,
@@ -1843,6 +1946,8 @@ int32_t sfd_share_model(sfd_handle* dst, const sfd_handle* src) {
   }
   std::memcpy(dst->src_plane, src->src_plane, sizeof src->src_plane);
   dst->model = src->model;
+  dst->mat_ids = src->mat_ids;
+  dst->mat_table = src->mat_table;
   dst->have_model = true;
   invalidate_graph(dst);
   return SFD_OK;

@@ -122,6 +122,19 @@ struct Seis2Step {
   IoArgs io;
 };
 
+// A material table passed by value to the coefficient kernels of
+// sfd_set_model_ids: nmat rows of the kind's model planes, FP64.
+constexpr int kMatTableMax = 2048;
+struct MatTable {
+  int nmat;
+  double v[kMatTableMax];
+};
+// FP32 coefficient planes (plane stride `plane`, row pitch P) of an
+// electromag2 or seismic2 handle from a device material-id map; *bad is set
+// to 1 if an id is outside [0, nmat).
+void coef_from_ids(int kind, const int* ids, const MatTable& m, int NX, int NZ, int P, double dt, float* coef,
+                   size_t plane, int* bad, cudaStream_t s);
+
 // Launch geometry of a solver's two half-step kernels.
 struct Launch {
   dim3 grid, block;

@@ -144,6 +144,25 @@ class FDTDSolver:
         arr = np.ascontiguousarray(arr)
         check(self._L.sfd_set_model(self._h, _dptr(arr), arr.size))
 
+    def set_model_ids(self, ids, table) -> None:
+        """The model as a material-id map: ids (NZ, NX) integers in [0, nmat)
+        (numpy, or a torch tensor on this solver's device) and table (nmat,
+        planes) in ``MODEL_PLANES`` order.  The coefficients are formed on the
+        GPU; the id map is kept on the device with the solver."""
+        import torch
+        names = MODEL_PLANES[self.kind]
+        tab = np.ascontiguousarray(np.asarray(table, dtype=np.float64))
+        if tab.ndim != 2 or tab.shape[1] != len(names):
+            raise ValueError(f"table must be (nmat, {len(names)}) in the order {names}")
+        if isinstance(ids, torch.Tensor):
+            dev = ids.to(device=self.device, dtype=torch.int32).contiguous()
+        else:
+            dev = torch.as_tensor(np.ascontiguousarray(np.asarray(ids, dtype=np.int32))).to(self.device)
+        if tuple(dev.shape) != (self.grid.nz, self.grid.nx):
+            raise ValueError(f"ids must be ({self.grid.nz}, {self.grid.nx}), got {tuple(dev.shape)}")
+        check(self._L.sfd_set_model_ids(self._h, C.c_void_p(dev.data_ptr()), tab.shape[0], _dptr(tab), tab.size))
+        self._ids = dev  # read again by set_source and the adjoint
+
     def set_cpml(self, profiles) -> None:
         """Per-axis CPML profiles: list of cpml.AxisProfile or the packed FP64 vector."""
         if isinstance(profiles, (list, tuple)):

@@ -1,0 +1,107 @@
+"""GPU: models given as a material-id map and a table (sfd_set_model_ids),
+with the update coefficients formed on the device, against the same models
+given as full FP64 planes (sfd_set_model).
+
+Both paths evaluate the same FP64 formulas and round once to FP32, so the
+runs are compared bit for bit; the adjoint gradient of an id-map model
+(whose FP64 planes the host expands from the ids on demand) is compared
+likewise.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from helpers import make_solver
+from seidart_gb300 import ELECTROMAG2, SEISMIC2
+from seidart_gb300 import synthetic as sy
+from seidart_gb300._lib import SfdError
+
+pytestmark = pytest.mark.gpu
+
+
+def _id_model(kind, nx, nz, nmat, seed):
+    """A random block-structured id map and a table of plausible materials."""
+    rng = np.random.default_rng(seed)
+    coarse = rng.integers(0, nmat, size=(nz // 6 + 1, nx // 6 + 1))
+    ids = np.kron(coarse, np.ones((6, 6), dtype=np.int64))[:nz, :nx].astype(np.int32)
+    if kind == ELECTROMAG2:  # eps11 eps13 eps33 sig11 sig13 sig33
+        table = np.column_stack([rng.uniform(1.5, 3.2, nmat), rng.uniform(0, 0.05, nmat), rng.uniform(1.5, 3.2, nmat),
+                                 10 ** rng.uniform(-6, -3, nmat), np.zeros(nmat), 10 ** rng.uniform(-6, -3, nmat)])
+    else:  # c11 c13 c15 c33 c35 c55 rho gamma_x gamma_z (wave speeds within small_case's time step)
+        c11 = rng.uniform(8e9, 12e9, nmat)
+        table = np.column_stack([c11, 0.4 * c11, rng.uniform(0, 1e8, nmat), rng.uniform(8e9, 12e9, nmat),
+                                 rng.uniform(0, 1e8, nmat), rng.uniform(1.5e9, 3e9, nmat), rng.uniform(850, 950, nmat),
+                                 rng.uniform(0, 0.002, nmat) * (np.arange(nmat) % 2), np.zeros(nmat)])
+    planes = np.ascontiguousarray(np.transpose(table[ids], (2, 0, 1)))
+    return ids, table, planes
+
+
+def _pair(kind, seed, nx=70, nz=56, nmat=4, nstep=120):
+    case = sy.small_case(kind, seed=seed, nx=nx, nz=nz, npml=6, nstep=nstep)
+    ids, table, planes = _id_model(kind, nx, nz, nmat, seed)
+    case.planes = planes
+    a = make_solver(case)
+    b = make_solver(case)
+    b.set_model_ids(ids, table)
+    b.set_source(case.src_ijk, case.srcfn)  # the amplitude divides by the model at the source cell
+    return case, a, b, ids, table
+
+
+@pytest.mark.parametrize("kind,seed", [(ELECTROMAG2, 1), (ELECTROMAG2, 2), (SEISMIC2, 3), (SEISMIC2, 4)])
+def test_id_map_matches_planes(gpu, kind, seed):
+    case, a, b, _, _ = _pair(kind, seed)
+    with a, b:
+        for s in (a, b):
+            s.run(47)
+            s.run(case.nstep - 47)
+            s.status()
+        assert np.array_equal(a.traces(), b.traces())
+        names = ("Ex", "Ez", "Hy") if kind == ELECTROMAG2 else ("vx", "vz", "sigmaxx", "sigmazz", "sigmaxz")
+        for name in names:
+            assert np.array_equal(a.field(name), b.field(name)), name
+
+
+def test_bad_ids_and_tables_are_rejected(gpu):
+    case, a, b, ids, table = _pair(SEISMIC2, 5, nstep=10)
+    with a, b:
+        bad = ids.copy()
+        bad[3, 4] = table.shape[0]
+        with pytest.raises(SfdError):
+            b.set_model_ids(bad, table)
+        neg = table.copy()
+        neg[1, 6] = -1.0  # density
+        with pytest.raises(SfdError):
+            b.set_model_ids(ids, neg)
+        with pytest.raises(ValueError):
+            b.set_model_ids(ids, table[:, :5])
+
+
+def test_adjoint_gradient_of_an_id_map_model(gpu):
+    """The chain rule reads the FP64 planes, expanded from the ids on demand."""
+    import torch
+    from seidart_gb300 import adjoint as adj
+    nx, nz = 64, 52
+    case = sy.small_case(ELECTROMAG2, seed=8, nx=nx, nz=nz, npml=6, nstep=90)
+    ids, table, planes = _id_model(ELECTROMAG2, nx, nz, 3, 8)
+    table[:, 5] = table[:, 3]  # TraceModel's sigma is sig11 = sig33
+    planes[5] = planes[3]
+    tm = adj.TraceModel(case.grid, planes, case.profiles, case.src_ijk, case.srcfn, case.rec_ijk, ckpt_every=30)
+    try:
+        tr = tm.forward(planes[0], planes[2], planes[3])
+        resid = torch.randn_like(tr)
+        want = tm.backward(resid)[3]
+        # the same model as ids: forward with checkpoints and the adjoint, as TraceModel does
+        s, L, h = tm.solver, tm._L, tm.solver._h
+        s.set_model_ids(ids, table)
+        s.set_source(case.src_ijk, case.srcfn)
+        s.reset()
+        for q in range(tm.nseg):
+            L.sfd_checkpoint_save(h, C.c_void_p(tm.ckpt[q].data_ptr()))
+            s.run(min(tm.ckpt_every, tm.nstep - q * tm.ckpt_every))
+        s.status()
+        assert torch.equal(s.traces_tensor(), tr)
+        got = tm.backward(resid)[3]
+        assert np.array_equal(got, want)
+    finally:
+        tm.close()
