@@ -597,6 +597,26 @@ def run_ours(args):
                        "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                        "ms_per_step": round(el * 1e3, 2),
                        "path": "seidart_gb300.solver.run_shot (host arrays in, host traces out)"}
+        # the same shots with the model as its material-id map and table
+        # (sfd_set_model_ids: coefficients formed on the GPU)
+        ids, table = case.meta["ids"], case.meta["table"]
+        sync_all()
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            tr_ids = run_shot(g, None, case.profiles, case.src_ijk, case.srcfn, case.rec_ijk, device=device, ids=ids,
+                              table=table)
+        torch.cuda.synchronize()
+        el_ids = (time.perf_counter() - t0) / n_e2e
+        if dist is not None:
+            t = torch.tensor([el_ids], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            el_ids = float(t.item())
+        h2d_ids = h2d - 4 * 4 * g.nx * g.nz + ids.nbytes + table.nbytes
+        line["e2e_material_ids"] = {"value": round(world * cells * case.nstep / el_ids / 1e9, 3), "unit": METRIC,
+                                    "h2d_bytes_per_step": int(h2d_ids), "d2h_bytes_per_step": int(d2h),
+                                    "ms_per_step": round(el_ids * 1e3, 2),
+                                    "traces_equal_to_planes_path": bool(np.array_equal(tr_ids, tr)),
+                                    "path": "run_shot(ids=, table=): sfd_set_model_ids"}
 
     # ---- extra lines: the other plain configurations ------------------------
     if not args.skip_extras:

@@ -302,14 +302,21 @@ class FDTDSolver:
         self.close()
 
 
-def run_shot(grid: GridSpec, planes, profiles, src_ijk, srcfn, rec_ijk, nsteps=None, device="cuda"):
+def run_shot(grid: GridSpec, planes, profiles, src_ijk, srcfn, rec_ijk, nsteps=None, device="cuda", ids=None,
+             table=None):
     """One complete shot: model + CPML + source + receivers in, traces out
-    (host arrays both ways).  Raises UnstableError like the Fortran stop."""
+    (host arrays both ways).  The model is ``planes``, or, with ``ids`` and
+    ``table`` (``planes`` may then be None), a material-id map whose
+    coefficients are formed on the GPU.  Raises UnstableError like the
+    Fortran stop."""
     srcfn = np.asarray(srcfn, dtype=np.float64)
     nstep = srcfn.shape[1]
     rec = np.asarray(rec_ijk, dtype=np.int32).reshape(-1, 3)
     with FDTDSolver(grid, nstep, rec.shape[0], device=device) as s:
-        s.set_model(planes)
+        if ids is not None:
+            s.set_model_ids(ids, table)
+        else:
+            s.set_model(planes)
         s.set_cpml(profiles)
         s.set_source(src_ijk, srcfn)
         s.set_receivers(rec)

@@ -190,8 +190,11 @@ def electromag2_layers(nstep: int = 6000, src_x: int = 500, nx: int = 1000, nz: 
     srcfn[0] = ricker(nstep, dt, f0)
     nrec = 100
     rec = np.array([[min(nx - 1, 10 * q + 5) + c, 0, 25 + c] for q in range(nrec)], dtype=np.int32)
+    # the same model as a material-id map (CPML cells take their edge's id) and its table
+    ids = extend_cpml(layer, c).astype(np.int32)
+    table = np.column_stack([mats[k] for k in ["eps11", "eps13", "eps33", "sig11", "sig13", "sig33"]])
     return Case(f"electromag2 layers {nx}x{nz}", grid, planes, profiles, (src_x + c, 0, 25 + c), srcfn, rec, f0,
-                dict(vmax=vmax, layers=layer))
+                dict(vmax=vmax, layers=layer, ids=ids, table=table))
 
 
 def seismic25_ice(nstep: int = 3000, nx: int = 600, ny: int = 40, nz: int = 300, c: int = 15) -> Case:

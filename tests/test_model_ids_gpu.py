@@ -105,3 +105,16 @@ def test_adjoint_gradient_of_an_id_map_model(gpu):
         assert np.array_equal(got, want)
     finally:
         tm.close()
+
+
+def test_run_shot_of_the_layered_model_by_ids(gpu):
+    """The 1040 x 540 layered model (three materials) through run_shot, as
+    planes and as its id map: the same traces."""
+    from seidart_gb300.solver import run_shot
+    case = sy.electromag2_layers(nstep=60)
+    g, m = case.grid, case.meta
+    assert m["ids"].shape == (g.nz, g.nx) and m["table"].shape == (3, 6)
+    assert np.array_equal(np.transpose(m["table"][m["ids"]], (2, 0, 1)), case.planes)
+    a = run_shot(g, case.planes, case.profiles, case.src_ijk, case.srcfn, case.rec_ijk)
+    b = run_shot(g, None, case.profiles, case.src_ijk, case.srcfn, case.rec_ijk, ids=m["ids"], table=m["table"])
+    assert np.array_equal(a, b)
