@@ -141,7 +141,8 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count);
  * sfd_set_model's plane order (count = nmat * planes, at most 2048 values).
  * The update coefficients are formed on the device, in FP64, with the
  * formulas of sfd_set_model, so both calls store the same coefficients; the
- * FP64 planes never cross to the GPU.  electromag2 and seismic2 handles.  The
+ * FP64 planes never cross to the GPU.  All kinds but electromag2c; for the
+ * 2.5-D kinds the map is the (x, z) image of the y-invariant model.  The
  * id map must stay allocated while the handle may set a source or take an
  * adjoint gradient (both read it).  Replaces the driver's expansion of the
  * material table into per-cell .dat files (src/seidart/routines/

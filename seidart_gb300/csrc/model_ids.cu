@@ -1,4 +1,6 @@
-// Update coefficients from a material-id map, on the device.
+// Update coefficients from a material-id map, on the device (electromag2,
+// seismic2, electromag25, seismic25; the 2.5-D models are y-invariant, so
+// their id map is the (x, z) image).
 //
 // A SeidarT model is an image of material ids (one per cell, the PNG colour
 // index) and a table of material properties; the driver expands it into one
@@ -112,16 +114,118 @@ __global__ void seis2_coef_from_ids(const int* __restrict__ ids, MatTable m, int
   for (int q = 0; q < 12; ++q) coef[q * plane + c] = out[q];
 }
 
+// electromag25 (electromagfdtd.f95:756-789): ca, cb of Ex, Ey, Ez per (x, z)
+// column from the row sums of the permittivity and conductivity tensors.
+__global__ void em25_coef_from_ids(const int* __restrict__ ids, MatTable m, int NX, int NZ, int P, double dt,
+                                   float* coef, size_t plane, int* bad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= NX || k >= NZ) return;
+  const size_t n = (size_t)k * NX + i, c = (size_t)k * P + i;
+  const int id = ids[n];
+  float out[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (!id_ok(id, m.nmat)) {
+    atomicExch(bad, 1);
+  } else {
+    const double* t = m.v + id * 12;  // eps11 eps12 eps13 eps22 eps23 eps33, sig11 .. sig33
+    const double ep[3] = {(t[0] + t[1] + t[2]) * kEps0d, (t[1] + t[3] + t[4]) * kEps0d, (t[2] + t[4] + t[5]) * kEps0d};
+    const double sg[3] = {t[6] + t[7] + t[8], t[7] + t[9] + t[10], t[8] + t[10] + t[11]};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      out[2 * d] = (float)((1.0 - sg[d] * dt / (2.0 * ep[d])) / (1.0 + sg[d] * dt / (2.0 * ep[d])));
+      out[2 * d + 1] = (float)((dt / ep[d]) / (1.0 + sg[d] * dt / (2.0 * ep[d])));
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 6; ++q) coef[q * plane + c] = out[q];
+}
+
+// seismic25 (seismicfdtd.f95:616-877): the 33 y-invariant stiffness averages
+// of the four stress loops (loop, Voigt entry, factor; the table of
+// sfd_set_model), the three averaged dt/rho of the velocity loops and
+// 1 - gamma per axis.
+struct S25Avg {
+  int loop, cij;
+  double f;
+};
+__constant__ S25Avg kS25Avg[33] = {
+    {1, 0, 0.25}, {1, 1, 0.25}, {1, 2, 0.25}, {1, 3, 0.125}, {1, 4, 0.125}, {1, 5, 0.125},
+    {1, 6, 0.25}, {1, 7, 0.25}, {1, 8, 0.125}, {1, 9, 0.125}, {1, 10, 0.125},
+    {1, 11, 0.25}, {1, 12, 0.125}, {1, 13, 0.125}, {1, 14, 0.125},
+    {2, 5, 0.25}, {2, 10, 0.25}, {2, 14, 0.25}, {2, 17, 0.125}, {2, 19, 0.125}, {2, 20, 0.125},
+    {3, 4, 0.25}, {3, 9, 0.25}, {3, 13, 0.25}, {3, 16, 0.125}, {3, 18, 0.125}, {3, 19, 0.125},
+    {4, 3, 0.25}, {4, 8, 0.25}, {4, 12, 0.25}, {4, 15, 0.125}, {4, 16, 0.125}, {4, 17, 0.125}};
+
+__global__ void seis25_coef_from_ids(const int* __restrict__ ids, MatTable m, int NX, int NZ, int P, double dt,
+                                     float* coef, size_t plane, int* bad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= NX || k >= NZ) return;
+  const size_t n = (size_t)k * NX + i, c = (size_t)k * P + i;
+  const int id = ids[n];
+  // the material of cell (ii, kk), or -1 (out of the grid or a bad id)
+  auto mat = [&](int ii, int kk) {
+    if (ii < 0 || ii >= NX || kk < 0 || kk >= NZ) return -1;
+    const int v = ids[(size_t)kk * NX + ii];
+    return id_ok(v, m.nmat) ? v : -1;
+  };
+  auto val = [&](int cell_id, int q) { return m.v[cell_id * 25 + q]; };
+  if (!id_ok(id, m.nmat)) {
+    atomicExch(bad, 1);
+    for (int q = 0; q < 39; ++q) coef[q * plane + c] = 0.f;
+    return;
+  }
+  const int mr = mat(i + 1, k), ml = mat(i - 1, k), mu = mat(i, k - 1), md = mat(i, k + 1);
+  const int mru = mat(i + 1, k - 1), mlu = mat(i - 1, k - 1), mld = mat(i - 1, k + 1), mrd = mat(i + 1, k + 1);
+  for (int q = 0; q < 33; ++q) {
+    const S25Avg av = kS25Avg[q];
+    double v = 0.0;
+    switch (av.loop) {
+      case 1:  // (i+1,k) (i,k) (i,k-1) (i+1,k-1), k >= 1, i <= NX-2
+        if (k >= 1 && i <= NX - 2 && mr >= 0 && mu >= 0 && mru >= 0)
+          v = val(mr, av.cij) + val(id, av.cij) + val(mu, av.cij) + val(mru, av.cij);
+        break;
+      case 2:  // (i,k) (i-1,k) (i,k-1) (i-1,k-1), k >= 1, i >= 1
+        if (k >= 1 && i >= 1 && ml >= 0 && mu >= 0 && mlu >= 0)
+          v = val(id, av.cij) + val(ml, av.cij) + val(mu, av.cij) + val(mlu, av.cij);
+        break;
+      case 3:  // (i,k+1) (i,k) (i-1,k) (i-1,k+1), k <= NZ-2, i >= 1
+        if (k <= NZ - 2 && i >= 1 && md >= 0 && ml >= 0 && mld >= 0)
+          v = val(md, av.cij) + val(id, av.cij) + val(ml, av.cij) + val(mld, av.cij);
+        break;
+      default:  // (i+1,k) (i,k) (i,k+1) (i+1,k+1), k <= NZ-2, i <= NX-2
+        if (k <= NZ - 2 && i <= NX - 2 && mr >= 0 && md >= 0 && mrd >= 0)
+          v = val(mr, av.cij) + val(id, av.cij) + val(md, av.cij) + val(mrd, av.cij);
+        break;
+    }
+    coef[q * plane + c] = (float)(av.f * v * dt);
+  }
+  const double r = val(id, 21);
+  float o33 = 0.f, o34 = 0.f, o35 = 0.f;
+  if (i >= 1 && k >= 1 && ml >= 0 && mu >= 0)  // seismicfdtd.f95:826
+    o33 = (float)(dt / ((4 * r + val(ml, 21) + val(mu, 21)) / 6));
+  if (i <= NX - 2 && k >= 1 && mr >= 0 && mu >= 0)  // :851
+    o34 = (float)(dt / ((4 * r + val(mr, 21) + val(mu, 21)) / 6));
+  if (i <= NX - 2 && k <= NZ - 2 && mr >= 0 && md >= 0)  // :877
+    o35 = (float)(dt / ((val(mr, 21) + val(md, 21) + 4 * r) / 6));
+  coef[33 * plane + c] = o33;
+  coef[34 * plane + c] = o34;
+  coef[35 * plane + c] = o35;
+  for (int d = 0; d < 3; ++d) coef[(36 + d) * plane + c] = (float)(1.0 - val(id, 22 + d));
+}
+
 }  // namespace
 
 void coef_from_ids(int kind, const int* ids, const MatTable& m, int NX, int NZ, int P, double dt, float* coef,
                    size_t plane, int* bad, cudaStream_t s) {
   const dim3 b(32, 8), g((NX + 31) / 32, (NZ + 7) / 8);
-  if (kind == SFD_ELECTROMAG2)
-    em2_coef_from_ids<<<g, b, 0, s>>>(ids, m, NX, NZ, P, dt, coef, coef + plane, coef + 2 * plane, coef + 3 * plane,
-                                      bad);
-  else
-    seis2_coef_from_ids<<<g, b, 0, s>>>(ids, m, NX, NZ, P, dt, coef, plane, bad);
+  switch (kind) {
+    case SFD_ELECTROMAG2:
+      em2_coef_from_ids<<<g, b, 0, s>>>(ids, m, NX, NZ, P, dt, coef, coef + plane, coef + 2 * plane, coef + 3 * plane,
+                                        bad);
+      break;
+    case SFD_SEISMIC2: seis2_coef_from_ids<<<g, b, 0, s>>>(ids, m, NX, NZ, P, dt, coef, plane, bad); break;
+    case SFD_ELECTROMAG25: em25_coef_from_ids<<<g, b, 0, s>>>(ids, m, NX, NZ, P, dt, coef, plane, bad); break;
+    default: seis25_coef_from_ids<<<g, b, 0, s>>>(ids, m, NX, NZ, P, dt, coef, plane, bad); break;
+  }
 }
 
 }  // namespace sfd

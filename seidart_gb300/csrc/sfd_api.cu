@@ -771,9 +771,14 @@ int32_t create_handle(const sfd_config* cfg, void* dev_state, size_t state_bytes
 }
 
 // Model plane (sfd_set_model's order) the source amplitude q is divided by,
-// for the kinds sfd_set_model_ids takes: electromag2 eps11, eps33; seismic2 rho.
+// for the kinds sfd_set_model_ids takes: electromag2 eps11, eps33;
+// electromag25 eps11, eps22, eps33; seismic2 and seismic25 rho.
 int src_full_plane(int kind, int q) {
-  if (kind == SFD_ELECTROMAG2) return q == 0 ? 0 : 2;
+  switch (kind) {
+    case SFD_ELECTROMAG2: return q == 0 ? 0 : 2;
+    case SFD_ELECTROMAG25: return q == 0 ? 0 : (q == 1 ? 3 : 5);
+    case SFD_SEISMIC25: return 21;
+  }
   return 6;
 }
 
@@ -819,8 +824,8 @@ int32_t sfd_set_model_ids(sfd_handle* h, const int32_t* dev_ids, int32_t nmat, c
   g_err.clear();
   if (!h || !dev_ids || !table) return fail(SFD_ERR_BAD_ARG, "NULL argument");
   const sfd_config& c = h->cfg;
-  if (c.kind != SFD_ELECTROMAG2 && c.kind != SFD_SEISMIC2)
-    return fail(SFD_ERR_BAD_ARG, "material-id models are implemented for electromag2 and seismic2");
+  if (c.kind == SFD_ELECTROMAG2C)
+    return fail(SFD_ERR_BAD_ARG, "material-id models are implemented for the real-valued kinds");
   const int np = nplanes(c.kind);
   if (nmat < 1 || count != (int64_t)nmat * np)
     return fail(SFD_ERR_BAD_ARG, "table needs nmat >= 1 rows of %d values (count = nmat * %d), got nmat %d, count %lld", np,
@@ -839,9 +844,16 @@ int32_t sfd_set_model_ids(sfd_handle* h, const int32_t* dev_ids, int32_t nmat, c
     if (c.kind == SFD_ELECTROMAG2) {
       if (!((t[0] + t[1]) * kEps0 > 0) || !((t[1] + t[2]) * kEps0 > 0))
         return fail(SFD_ERR_BAD_ARG, "permittivity must be positive (material %d)", m);
-    } else {
+    } else if (c.kind == SFD_ELECTROMAG25) {
+      if (!((t[0] + t[1] + t[2]) * kEps0 > 0) || !((t[1] + t[3] + t[4]) * kEps0 > 0) ||
+          !((t[2] + t[4] + t[5]) * kEps0 > 0))
+        return fail(SFD_ERR_BAD_ARG, "permittivity must be positive (material %d)", m);
+    } else if (c.kind == SFD_SEISMIC2) {
       if (!(t[6] > 0)) return fail(SFD_ERR_BAD_ARG, "density must be positive (material %d)", m);
       if (t[7] != 0.0 || t[8] != 0.0) atten = 1;
+    } else {
+      if (!(t[21] > 0)) return fail(SFD_ERR_BAD_ARG, "density must be positive (material %d)", m);
+      if (t[22] != 0.0 || t[23] != 0.0 || t[24] != 0.0) atten = 1;
     }
   }
   MatTable mt;
@@ -856,7 +868,8 @@ int32_t sfd_set_model_ids(sfd_handle* h, const int32_t* dev_ids, int32_t nmat, c
   CK(cudaMemcpyAsync(&flag, bad, sizeof flag, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   if (flag) return fail(SFD_ERR_BAD_ARG, "material id outside [0, %d)", nmat);
-  if (c.kind == SFD_SEISMIC2) set_atten(h, atten);  // any material with attenuation (gamma = 0 cells multiply by 1)
+  if (c.kind == SFD_SEISMIC2 || c.kind == SFD_SEISMIC25)
+    set_atten(h, atten);  // any material with attenuation (gamma = 0 cells multiply by 1)
   h->mat_ids = dev_ids;
   h->mat_table = std::make_shared<std::vector<double>>(table, table + count);
   h->model.reset();
