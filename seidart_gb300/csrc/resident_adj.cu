@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
     const bool strp = in_strip(gk0, NZ, W) || in_strip(gk1, NZ, W) || in_strip(gi, NX, W) || in_strip(gi + 3, NX, W);
     cls = edge ? 2 : (strp ? 1 : 0);
   }
-  const int g = class_ordered_group(cls);
+  const int g = class_ordered_group<3>(cls);
   const int tx = g >= 0 ? g % TXT : 0, ty = g >= 0 ? g / TXT : 0;
   const int rbase = RB * ty;
   const int nrows = g >= 0 ? min(RB, nzt - rbase) : 0;

@@ -115,20 +115,20 @@ enum : unsigned {
 };
 __device__ __forceinline__ bool mbit(unsigned m, unsigned field, int e) { return (m >> (field + e)) & 1u; }
 
-// Threads take the tile's groups (four columns x kResRows rows) in class
-// order -- cls 0 (interior groups), then 1 (CPML strip groups), then 2
-// (groups with a boundary plane or the source) -- so each warp runs one
-// update path instead of several in turn.  Every thread of the CTA calls
-// this with the class of group tid (3 when tid has no group) and gets the
-// group it owns (-1: none).  Contains barriers.
+// Threads take the tile's groups (four columns x kResRows rows) in the order
+// of their class, 0 .. NC - 1 (the kernels order the groups by update path,
+// so each warp runs one path instead of several in turn).  Every thread of
+// the CTA calls this with the class of group tid (NC when tid has no group)
+// and gets the group it owns (-1: none).  Contains barriers.
+template <int NC>
 __device__ __noinline__ int class_ordered_group(int cls) {
-  __shared__ int s_cnt[kResThreads / 32][3];
+  __shared__ int s_cnt[kResThreads / 32][NC];
   __shared__ unsigned short s_map[kResCellThreads];
   const int tid = threadIdx.x;
   const unsigned lane = tid & 31, warp = tid >> 5;
   unsigned mine = 0;
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
+  for (int c = 0; c < NC; ++c) {
     const unsigned b = __ballot_sync(0xffffffffu, cls == c);
     if (lane == 0) s_cnt[warp][c] = __popc(b);
     if (cls == c) mine = __popc(b & ((1u << lane) - 1u));
@@ -136,7 +136,7 @@ __device__ __noinline__ int class_ordered_group(int cls) {
   __syncthreads();
   if (tid == 0) {
     int run = 0;
-    for (int c = 0; c < 3; ++c)
+    for (int c = 0; c < NC; ++c)
       for (int w = 0; w < kResThreads / 32; ++w) {  // the warps of this CTA
         const int n = s_cnt[w][c];
         s_cnt[w][c] = run;
@@ -144,9 +144,9 @@ __device__ __noinline__ int class_ordered_group(int cls) {
       }
   }
   __syncthreads();
-  if (cls < 3) s_map[s_cnt[warp][cls] + mine] = (unsigned short)tid;
+  if (cls < NC) s_map[s_cnt[warp][cls] + mine] = (unsigned short)tid;
   __syncthreads();
-  return (tid < kResCellThreads && cls < 3) ? s_map[tid] : -1;
+  return (tid < kResCellThreads && cls < NC) ? s_map[tid] : -1;
 }
 
 }  // namespace
