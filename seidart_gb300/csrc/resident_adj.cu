@@ -96,16 +96,18 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
   const bool up = bz > 0, down = bz < a.plan.ntz - 1, left = bx > 0, right = bx < te.w - 1;
   const int tid = threadIdx.x;
   const bool xwarp = tid >= kResCellThreads;
-  int cls = 3;
+  int cls = 4;
   if (!xwarp && tid < TXT * TYT) {
     const int gi = x0 + 4 * (tid % TXT), gk0 = z0 + RB * (tid / TXT);
     const int gk1 = min(gk0 + RB, z0 + nzt) - 1;
     const bool edge = gi < 1 || gi + 3 > NX - 3 || gk0 < 1 || gk1 > NZ - 3 ||
                       (a.sk >= gk0 && a.sk <= gk1 && a.si >= gi && a.si < gi + 4);
     const bool strp = in_strip(gk0, NZ, W) || in_strip(gk1, NZ, W) || in_strip(gi, NX, W) || in_strip(gi + 3, NX, W);
-    cls = edge ? 2 : (strp ? 1 : 0);
+    const int tx0 = tid % TXT, ty0 = tid / TXT;
+    const bool perim = (up && ty0 == 0) || (down && ty0 == TYT - 1) || (left && tx0 == 0) || (right && tx0 == TXT - 1);
+    cls = edge ? 3 : (strp ? 2 : (perim ? 0 : 1));  // the forward run's order (resident2d.cu)
   }
-  const int g = class_ordered_group<3>(cls);
+  const int g = class_ordered_group<4>(cls);
   const int tx = g >= 0 ? g % TXT : 0, ty = g >= 0 ? g / TXT : 0;
   const int rbase = RB * ty;
   const int nrows = g >= 0 ? min(RB, nzt - rbase) : 0;
