@@ -90,12 +90,15 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
   const int nrows = g >= 0 ? min(RB, nzt - rbase) : 0;
   const bool cell = nrows > 0;
   const int i0 = x0 + 4 * tx;
-  const int CS = TZ * TW;
-  float* sMExz = smem;  // CPML memory variables of strip cells, [TZ][TW] each
+  // Arrays only the owning thread reads are indexed by thread: row j of
+  // thread tid is the float4 at so = 4 (j * kResCellThreads + tid), so a warp's
+  // accesses are conflict-free whichever groups its threads own.
+  const int CS = 4 * RB * kResCellThreads;
+  float* sMExz = smem;  // CPML memory variables of strip cells
   float* sMEzx = sMExz + CS;
   float* sMHyz = sMEzx + CS;
   float* sMHyx = sMHyz + CS;
-  float* sCAx = sMHyx + CS;  // update coefficients, [TZ][TW] each
+  float* sCAx = sMHyx + CS;  // update coefficients
   float* sCBx = sCAx + CS;
   float* sCAz = sCBx + CS;
   float* sCBz = sCAz + CS;
@@ -142,7 +145,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
     for (int j = 0; j < RB; ++j) {
       if (j >= nrows) continue;
       const int row = rbase + j, k = z0 + row;
-      const int gg = k * P + i0, so = row * TW + 4 * tx;
+      const int gg = k * P + i0, so = 4 * (j * kResCellThreads + tid);
       ex[j] = ld4(a.Ex + gg);
       ez[j] = ld4(a.Ez + gg);
       hy[j] = ld4(a.Hy + gg);
@@ -242,7 +245,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
 #pragma unroll
       for (int j = 0; j < RB; ++j) {
         if (j >= nrows) continue;
-        const int row = rbase + j, k = z0 + row, so = row * TW + 4 * tx;
+        const int row = rbase + j, k = z0 + row, so = 4 * (j * kResCellThreads + tid);
         float4 exn = exb;
         if (j + 1 < RB && j + 1 < nrows) exn = ex[j + 1 < RB ? j + 1 : j];
         const float ezn = sEzCol[row * SX + tx + 1];
@@ -321,7 +324,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
 #pragma unroll
       for (int j = 0; j < RB; ++j) {
         if (j >= nrows) continue;
-        const int row = rbase + j, k = z0 + row, so = row * TW + 4 * tx;
+        const int row = rbase + j, k = z0 + row, so = 4 * (j * kResCellThreads + tid);
         float4 hm = hmt;
         if (j > 0) hm = hy[j > 0 ? j - 1 : 0];
         const float hl = sHyCol[row * SX + tx];
@@ -404,7 +407,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
         for (int j = 0; j < RB; ++j) {
           if (j >= nrows) continue;
           const int row = rbase + j, k = z0 + row;
-          const int gg = k * P + i0, so = row * TW + 4 * tx;
+          const int gg = k * P + i0, so = 4 * (j * kResCellThreads + tid);
           // streaming stores: the copies are read back only after the run
           __stcs(reinterpret_cast<float4*>((float*)(d + a.dump.off[0]) + gg), ex[j]);
           __stcs(reinterpret_cast<float4*>((float*)(d + a.dump.off[1]) + gg), ez[j]);
@@ -475,7 +478,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
     for (int j = 0; j < RB; ++j) {
       if (j >= nrows) continue;
       const int row = rbase + j, k = z0 + row;
-      const int gg = k * P + i0, so = row * TW + 4 * tx;
+      const int gg = k * P + i0, so = 4 * (j * kResCellThreads + tid);
       st4(a.Ex + gg, ex[j]);
       st4(a.Ez + gg, ez[j]);
       st4(a.Hy + gg, hy[j]);
@@ -502,7 +505,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
 
 size_t em2_resident_smem(int TW, int TZ) {
   const size_t SX = (size_t)TW / 4 + 1, TYT = ((size_t)TZ + kResRows - 1) / kResRows;
-  return sizeof(float) * (8 * (size_t)TZ * TW + 2 * (TYT + 1) * TW + 2 * (size_t)TZ * SX);
+  return sizeof(float) * (32 * (size_t)kResRows * kResCellThreads + 2 * (TYT + 1) * TW + 2 * (size_t)TZ * SX);
 }
 
 namespace {
