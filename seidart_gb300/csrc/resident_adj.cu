@@ -96,25 +96,27 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
   const bool up = bz > 0, down = bz < a.plan.ntz - 1, left = bx > 0, right = bx < te.w - 1;
   const int tid = threadIdx.x;
   const bool xwarp = tid >= kResCellThreads;
-  int cls = 4;
+  int cls = 3;
   if (!xwarp && tid < TXT * TYT) {
     const int gi = x0 + 4 * (tid % TXT), gk0 = z0 + RB * (tid / TXT);
     const int gk1 = min(gk0 + RB, z0 + nzt) - 1;
     const bool edge = gi < 1 || gi + 3 > NX - 3 || gk0 < 1 || gk1 > NZ - 3 ||
                       (a.sk >= gk0 && a.sk <= gk1 && a.si >= gi && a.si < gi + 4);
     const bool strp = in_strip(gk0, NZ, W) || in_strip(gk1, NZ, W) || in_strip(gi, NX, W) || in_strip(gi + 3, NX, W);
-    const int tx0 = tid % TXT, ty0 = tid / TXT;
-    const bool perim = (up && ty0 == 0) || (down && ty0 == TYT - 1) || (left && tx0 == 0) || (right && tx0 == TXT - 1);
-    cls = edge ? 3 : (strp ? 2 : (perim ? 0 : 1));  // the forward run's order (resident2d.cu)
+    cls = edge ? 2 : (strp ? 1 : 0);
   }
-  const int g = class_ordered_group<4>(cls);
+  const int g = class_ordered_group<3>(cls);
   const int tx = g >= 0 ? g % TXT : 0, ty = g >= 0 ? g / TXT : 0;
   const int rbase = RB * ty;
   const int nrows = g >= 0 ? min(RB, nzt - rbase) : 0;
   const bool cell = nrows > 0;
   const int i0 = x0 + 4 * tx;
-  const int CS = TZ * TW;
-  // float4-accessed arrays first (CS and TW are multiples of 4)
+  // float4-accessed arrays first (CS and TW are multiples of 4).  The
+  // coefficients and gradient sums are read only by the owning thread and
+  // indexed by thread: row j of thread tid is the float4 at
+  // so = 4 (j * kResCellThreads + tid), conflict-free whichever groups a
+  // warp's threads own.
+  const int CS = 4 * RB * kResCellThreads;
   float* sCAx = smem;
   float* sCBx = sCAx + CS;
   float* sCAz = sCBx + CS;
@@ -205,7 +207,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
     for (int j = 0; j < RB; ++j) {
       if (j >= nrows) continue;
       const int row = rbase + j, k = z0 + row;
-      const int gg = k * P + i0, so = row * TW + 4 * tx;
+      const int gg = k * P + i0, so = 4 * (j * kResCellThreads + tid);
       lx[j] = ld4(a.Lx + gg);
       lz[j] = ld4(a.Lz + gg);
       lh[j] = ld4(a.Lh + gg);
@@ -312,7 +314,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
   // gx of the thread's row j (zero outside the Ex range)
   auto gx_row = [&](int j) {
     float4 gx = zero4;
-    const int row = rbase + j, so = row * TW + 4 * tx;
+    const int row = rbase + j, so = 4 * (j * kResCellThreads + tid);
     const float4 cb = lds4(sCBx + so);
     const float kz = sZt[kTKH * TZ + row];
     const bool zs = (zsb >> j) & 1u;
@@ -335,7 +337,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
   // gz of cell e of the thread's row j (zero outside the Ez range)
   auto gz_cell = [&](int j, int e) {
     if (!mbit(m[j], kAEZ, e)) return 0.0f;
-    const int so = (rbase + j) * TW + 4 * tx;
+    const int so = 4 * (j * kResCellThreads + tid);
     const float lez = mbit(m[j], kAZE, e) ? 0.0f : el(lz[j], e);
     float v = sCBz[so + e] * lez * sXt[kTKH * TW + 4 * tx + e];
     if (mbit(m[j], kAXS, e)) v += sLD[xoff(rbase + j) + e] * sXt[kTADH * TW + 4 * tx + e];
@@ -411,11 +413,11 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
 #pragma unroll
       for (int j = 0; j < RB; ++j) {
         if (j >= nrows) continue;
-        const int row = rbase + j, k = z0 + row, so = row * TW + 4 * tx;
+        const int row = rbase + j, k = z0 + row, so = 4 * (j * kResCellThreads + tid);
         float4 gnext;
         if (j + 1 < RB && j + 1 < nrows) {
           const int jn = j + 1 < RB ? j + 1 : j;
-          const float4 cb = lds4(sCBx + so + TW);
+          const float4 cb = lds4(sCBx + so + 4 * kResCellThreads);
           const float kz = sZt[kTKH * TZ + row + 1];
 #pragma unroll
           for (int e = 0; e < 4; ++e) el(gnext, e) = el(cb, e) * el(lx[jn], e) * kz;
@@ -470,7 +472,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
       for (int j = 0; j < RB; ++j) {
         if (j >= nrows) continue;
         const int row = rbase + j, k = z0 + row;
-        const int gg = k * P + i0, so = row * TW + 4 * tx;
+        const int gg = k * P + i0, so = 4 * (j * kResCellThreads + tid);
         const unsigned mj = m[j];
         const bool zs = (zsb >> j) & 1u;
         float4 gnext;
@@ -733,7 +735,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
     for (int j = 0; j < RB; ++j) {
       if (j >= nrows) continue;
       const int row = rbase + j, k = z0 + row;
-      const int gg = k * P + i0, so = row * TW + 4 * tx;
+      const int gg = k * P + i0, so = 4 * (j * kResCellThreads + tid);
       st4(a.Lx + gg, lx[j]);
       st4(a.Lz + gg, lz[j]);
       st4(a.Lh + gg, lh[j]);
@@ -779,7 +781,7 @@ size_t em2_adj_resident_smem(const ResPlan& plan, int NX, int NZ, int W) {
     const int TW = (((t.x >> 16) - x0) + 3) & ~3, TZ = (t.y >> 16) - z0;
     int nzr, nxg;
     adj_tile_strips(x0, TW, z0, TZ, NX, NZ, W, &nzr, &nxg);
-    const size_t SX = (size_t)TW / 4 + 1, TYT = ((size_t)TZ + kResRows - 1) / kResRows, CS = (size_t)TW * TZ;
+    const size_t SX = (size_t)TW / 4 + 1, TYT = ((size_t)TZ + kResRows - 1) / kResRows, CS = 4 * (size_t)kResRows * kResCellThreads;
     m = std::max(m, sizeof(float) * (8 * CS + 2 * (size_t)nzr * TW + 8 * (size_t)TZ * nxg + 2 * (TYT + 1) * TW +
                                      kNT * (size_t)TW + kNT * (size_t)TZ + 2 * (size_t)TZ * SX));
   }
