@@ -56,6 +56,16 @@ enum : unsigned {
 enum { kTKH, kTADH, kTBH, kTIKH, kTK, kTAD, kTB, kNT };
 
 // Array q (0..6: Ex Ez Hy A B C D) of forward slot s.
+// 16-byte copy from global to shared memory that completes asynchronously
+// (cp.async, through L2); cp_async_wait_all makes the thread's own copies
+// visible to it.
+__device__ __forceinline__ void cp_async16(float* sdst, const float* gsrc) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(sdst)),
+               "l"(gsrc)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 __device__ __forceinline__ const float* slot_f(const Em2AdjResident& a, int s, int q) {
   return (const float*)(a.slots + (size_t)s * a.stride + a.off[q]);
 }
@@ -131,7 +141,12 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
   int nzr, nxg;
   adj_tile_strips(x0, TW, z0, TZ, NX, NZ, W, &nzr, &nxg);
   const int XS = 4 * nxg;
-  float* sLA = sGBz + CS;
+  // the forward Ex, Ez and Hy' of the thread's cells for the next transposed
+  // step, copied in one step ahead (cp.async) and indexed like the above
+  float* sSEx = sGBz + CS;
+  float* sSEz = sSEx + CS;
+  float* sSHy = sSEz + CS;
+  float* sLA = sSHy + CS;
   float* sLC = sLA + nzr * TW;
   float* sLB = sLC + nzr * TW;
   float* sLD = sLB + TZ * XS;
@@ -141,7 +156,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
   float* sZt = sXt + kNT * TW;              // [kNT][TZ]
   float* sGzCol = sZt + kNT * TZ;           // [TZ][SX]: gz of the first column of thread column tx; column TXT = tile right
   float* sHbCol = sGzCol + TZ * SX;         // [TZ][SX]: column tx+1 = hB of the last column of tx; column 0 = tile left
-  const int nsm = 8 * CS + 2 * nzr * TW + 2 * TZ * XS + 2 * (TYT + 1) * TW + kNT * TW + kNT * TZ + 2 * TZ * SX;
+  const int nsm = 11 * CS + 2 * nzr * TW + 2 * TZ * XS + 2 * (TYT + 1) * TW + kNT * TW + kNT * TZ + 2 * TZ * SX;
   // offsets of a row of this thread's cells in the z-strip and x-strip arrays
   const int zbot = max(z0, max(W, NZ - W)), ntop = max(0, min(W, z0 + TZ) - z0);
   int xgi = 0;  // x-strip groups left of this thread's group
@@ -370,7 +385,22 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
     return h;
   };
 
+  // the forward state phase A of slot s reads, into this thread's staging slots
+  auto stage = [&](int s) {
+    const float *SEx = slot_f(a, s, 0), *SEz = slot_f(a, s, 1), *S1Hy = slot_f(a, s + 1, 2);
+#pragma unroll
+    for (int j = 0; j < RB; ++j) {
+      if (j >= nrows) continue;
+      const size_t gg = (size_t)(z0 + rbase + j) * P + i0;
+      const int so = 4 * (j * kResCellThreads + tid);
+      cp_async16(sSEx + so, SEx + gg);
+      cp_async16(sSEz + so, SEz + gg);
+      cp_async16(sSHy + so, S1Hy + gg);
+    }
+  };
+
   if (cell) {
+    stage(a.nsteps - 1);
     inject(a.s0 + a.nsteps - 1);
     publish_g(0, 1u);
   } else if (xwarp) {  // gx row below and gz column to the right for the first transposed step
@@ -391,8 +421,9 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
     const unsigned tag = (unsigned)it + 1u;
 
     // ================= phase A: E half transposed, gradients, source
+    if (cell) cp_async_wait_all();  // this step's staged forward state
     if (cell && fast) {  // interior cells: no masks, no strips
-      const float *SEx = slot_f(a, s, 0), *SEz = slot_f(a, s, 1), *S1Hy = slot_f(a, s + 1, 2);
+      const float* S1Hy = slot_f(a, s + 1, 2);
       float4 sx[RB], sz[RB], h1[RB];
       float hl[RB];
 #pragma unroll
@@ -401,9 +432,10 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
         hl[j] = 0.0f;
         if (j >= nrows) continue;
         const int gg = (z0 + rbase + j) * P + i0;
-        sx[j] = ld4(SEx + gg);
-        sz[j] = ld4(SEz + gg);
-        h1[j] = ld4(S1Hy + gg);
+        const int so = 4 * (j * kResCellThreads + tid);
+        sx[j] = lds4(sSEx + so);
+        sz[j] = lds4(sSEz + so);
+        h1[j] = lds4(sSHy + so);
         hl[j] = __ldg(S1Hy + gg - 1);
       }
       float4 hpm = hy_above(s);
@@ -465,7 +497,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
         hpm = hp;
       }
     } else if (cell) {  // strip, plane, source or partial groups: per-cell masks
-      const float *SEx = slot_f(a, s, 0), *SEz = slot_f(a, s, 1), *S1Hy = slot_f(a, s + 1, 2);
+      const float* S1Hy = slot_f(a, s + 1, 2);
       float4 gcur = lds4(sGxRow + ty * TW + 4 * tx);
       float4 hpm = hy_above(s);
 #pragma unroll
@@ -500,7 +532,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
         }
         gz[4] = sGzCol[row * SX + tx + 1];
         // Hy' of the row and of the cell on the left
-        const float4 h1 = ld4(S1Hy + gg);
+        const float4 h1 = lds4(sSHy + so);
         float4 hp;
 #pragma unroll
         for (int e = 0; e < 4; ++e)
@@ -508,7 +540,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
         const float hpl = (i0 >= 1 && k <= NZ - 2) ? __ldg(S1Hy + gg - 1) : 0.0f;
         // Ex: gradients and lam_C
         {
-          const float4 sx = ld4(SEx + gg), cax = lds4(sCAx + so), cbx = lds4(sCBx + so);
+          const float4 sx = lds4(sSEx + so), cax = lds4(sCAx + so), cbx = lds4(sCBx + so);
           float4 gax = lds4(sGAx + so), gbx = lds4(sGBx + so);
           const float ikhz = sZt[kTIKH * TZ + row];
           float4 lc = zero4, s1c = zero4;
@@ -544,7 +576,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
         }
         // Ez: gradients and lam_D
         {
-          const float4 sz = ld4(SEz + gg), caz = lds4(sCAz + so), cbz = lds4(sCBz + so);
+          const float4 sz = lds4(sSEz + so), caz = lds4(sCAz + so), cbz = lds4(sCBz + so);
           float4 gaz = lds4(sGAz + so), gbz = lds4(sGBz + so);
           const float4 ikhx = lds4(sXt + kTIKH * TW + 4 * tx);
           float4 ld = zero4, s1d = zero4, bhx = zero4;
@@ -621,15 +653,12 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
 
     // ================= phase B: H half transposed
     if (cell) {
-      if (it + 1 < a.nsteps) {  // the forward state of the next transposed step, into L2
-        const float *nEx = slot_f(a, s - 1, 0), *nEz = slot_f(a, s - 1, 1), *nHy = slot_f(a, s, 2);
+      if (it + 1 < a.nsteps) {  // the forward state of the next transposed step: staged, strips into L2
+        stage(s - 1);
 #pragma unroll
         for (int j = 0; j < RB; ++j) {
           if (j >= nrows) continue;
-          const int k = z0 + rbase + j, gg = k * P + i0;
-          prefetch_l2(nEx + gg);
-          prefetch_l2(nEz + gg);
-          prefetch_l2(nHy + gg);
+          const int k = z0 + rbase + j;
           if ((zsb >> j) & 1u) prefetch_l2(slot_f(a, s, 5) + strip_idx(k, NZ, W) * P + i0);
           if (xs) {
 #pragma unroll
@@ -727,6 +756,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
     __syncthreads();
     if (s_abort) ok = false;
   }
+  cp_async_wait_all();  // no copy left in flight
   if (!ok) return;  // the adjoint state is left as it was loaded; the host reports the timeout
 
   // ---- write the adjoint state back, add the gradient sums
@@ -782,7 +812,7 @@ size_t em2_adj_resident_smem(const ResPlan& plan, int NX, int NZ, int W) {
     int nzr, nxg;
     adj_tile_strips(x0, TW, z0, TZ, NX, NZ, W, &nzr, &nxg);
     const size_t SX = (size_t)TW / 4 + 1, TYT = ((size_t)TZ + kResRows - 1) / kResRows, CS = 4 * (size_t)kResRows * kResCellThreads;
-    m = std::max(m, sizeof(float) * (8 * CS + 2 * (size_t)nzr * TW + 8 * (size_t)TZ * nxg + 2 * (TYT + 1) * TW +
+    m = std::max(m, sizeof(float) * (11 * CS + 2 * (size_t)nzr * TW + 8 * (size_t)TZ * nxg + 2 * (TYT + 1) * TW +
                                      kNT * (size_t)TW + kNT * (size_t)TZ + 2 * (size_t)TZ * SX));
   }
   return m;
