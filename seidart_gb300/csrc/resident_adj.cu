@@ -28,8 +28,11 @@
 // coefficients, the adjoint memory variables, the gradient sums and the axis
 // tables stay in shared memory.  The forward state of each step (Ex, Ez,
 // Hy' -- Hy after the H half, before its Dirichlet planes are zeroed -- and
-// psi' on the strips) is read from the per-step copies a recompute run
-// (resident2d.cu with a ResDump) wrote just before.
+// psi' on the strips) comes from the per-step copies a recompute run
+// (resident2d.cu with a ResDump) wrote just before: each thread copies the
+// Ex, Ez, Hy' of its cells for the next transposed step into shared memory
+// with cp.async while it runs phase B, and prefetches the strips' psi' into
+// L2.
 #include <algorithm>
 
 #include "resident_common.cuh"
