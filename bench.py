@@ -33,6 +33,26 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Gcell-updates/s"
 WORKLOAD = "electromag2 plain 1040x540 cells (1000x500 + 20-cell CPML) x 6000 steps, 100 receivers"
+DATA = "synthetic (seeded layered permittivity/conductivity model)"
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu), for the CPU baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+    except (OSError, subprocess.SubprocessError):
+        return "unknown"
+    for line in out.splitlines():
+        if line.strip().lower().startswith("model name"):
+            return line.split(":", 1)[1].strip()
+    return "unknown"
+
+
+def bench_config(nstep, cells, world):
+    """The workload description both arms print (the reference arm times a
+    bounded sample of it, described in its cpu_baseline.sample)."""
+    return {"workload": WORKLOAD, "time_steps_per_bench_step": nstep, "cells": cells,
+            "l2": "256 MiB buffer written between shots (flush)", "parallelism": f"replicas x{world}"}
 
 
 def _peaks():
@@ -188,9 +208,11 @@ def bench_plain(case, device, flush, stream, peak, bytes_fn, steps, warmup):
             "kernel_frac": [round(b[h] / (t / 1e3) / 1e9 / peak, 4) for h, t in zip(("half1", "half2"), kt)]}
 
 
-def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000, tiling=None):
+def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000, tiling=None, parity_models=()):
     """The batched survey: 64 electromag2 shots of the layered 1000x500 model (sources every 15
-    cells) + 16 seeded seismic2 models of uneven size, 4000 steps, one persistent launch per run."""
+    cells) + 16 seeded seismic2 models of uneven size, 4000 steps, one persistent launch per run.
+    ``parity_models``: indices of the models (shots first) whose batched traces and fields are
+    compared with the FP64 oracle."""
     import torch
     from seidart_gb300 import ELECTROMAG2, synthetic as sy
     from seidart_gb300.batch import Batch, autotune
@@ -255,6 +277,24 @@ def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000, 
     # other (each handle's own run: the electromag2 shots on chip, the
     # seismic2 models one launch per step), against the batched traces.
     batched_traces = [s.traces() for s in solvers]
+    parity = None
+    if parity_models:
+        # a few shots and models of the batch against the FP64 oracle (traces
+        # and final fields of the batched run)
+        from oracle import parity as par
+        from seidart_gb300.solver import FIELDS
+        picks = [q for q in parity_models if q < len(cases)]
+        fields = {q: [solvers[q].field(nm) for nm in FIELDS[cases[q].grid.kind]] for q in picks}
+        parity = {}
+        t0 = time.perf_counter()
+        for q in picks:
+            st, ref = par.oracle_case(cases[q])
+            r = par.compare_run(batched_traces[q], fields[q], st, ref, FIELDS[cases[q].grid.kind])
+            parity[cases[q].name] = {"rel_l2_traces": r["rel_l2_traces"], "rel_l2_fields_max": r["rel_l2_fields_max"]}
+        parity = {"models": parity, "steps": nstep,
+                  "rel_l2_traces_max": max(v["rel_l2_traces"] for v in parity.values()),
+                  "rel_l2_fields_max": max(v["rel_l2_fields_max"] for v in parity.values()),
+                  "oracle_s": round(time.perf_counter() - t0, 1)}
     for s in solvers:
         s.reset()
     torch.cuda.synchronize()
@@ -284,13 +324,15 @@ def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000, 
            "tiling": {"rows_per_thread": tune["tiling"][0], "blocks_per_sm": tune["tiling"][1],
                       "candidates_ms_per_step": {k: round(v * 1e3, 4) for k, v in tune["timings"].items()}},
            "launches_per_run": 3}
+    if parity is not None:
+        out["parity"] = parity
     b.close()
     for s in solvers:
         s.close()
     return out
 
 
-def bench_adjoint(device, ckpt_every=200, nstep=6000):
+def bench_adjoint(device, ckpt_every=200, nstep=6000, fd_cells=0):
     """Adjoint gradient on the layered electromag2 model (6000 steps, 100 receivers): misfit against
     the unperturbed model's traces, current model with six +-5% Gaussian blobs in eps11 and eps33
     (seed 6), checkpoints every 200 steps with recompute.  Reports backward / forward wall time."""
@@ -333,11 +375,82 @@ def bench_adjoint(device, ckpt_every=200, nstep=6000):
     t_plain = time.perf_counter() - t0
     m.close()
     misfit = 0.5 * float((resid.double() ** 2).sum())
-    return {"workload": f"electromag2 1040x540 x {nstep} steps, gradient wrt eps11, eps33, sigma per cell",
-            "forward_s": round(t_plain, 4), "forward_with_checkpoints_s": round(t_fwd, 4),
-            "adjoint_s": round(t_bwd, 4), "adjoint_over_forward": round(t_bwd / t_plain, 3),
-            "checkpoints_every": ckpt_every, "misfit": misfit,
-            "grad_abs_max": [float(np.abs(g).max()) for g in (g11, g33, gs)]}
+    out = {"workload": f"electromag2 1040x540 x {nstep} steps, gradient wrt eps11, eps33, sigma per cell",
+           "forward_s": round(t_plain, 4), "forward_with_checkpoints_s": round(t_fwd, 4),
+           "adjoint_s": round(t_bwd, 4), "adjoint_over_forward": round(t_bwd / t_plain, 3),
+           "whole_gradient_over_forward": round((t_fwd + t_bwd) / t_plain, 3),
+           "checkpoints_every": ckpt_every, "misfit": misfit,
+           "grad_abs_max": [float(np.abs(g).max()) for g in (g11, g33, gs)]}
+    if fd_cells:
+        out["parity_fd"] = adjoint_fd_check(case, base, cur, (g11, g33, gs), fd_cells)
+    return out
+
+
+def adjoint_fd_check(case, base, cur, grads, ncells, seed=7, h_rel=1e-4):
+    """Central finite differences of the FP64 oracle's misfit at ``ncells``
+    seeded interior cells (seed 7), relative step h = 1e-4 of the cell's value,
+    against the GPU adjoint gradient.  The parameter cycles through eps11,
+    eps33 and sigma (= sig11 = sig33) from cell to cell.  d_obs = the oracle's
+    traces of the unperturbed model; the misfit is evaluated at ``cur``."""
+    from oracle import parity as par
+    from seidart_gb300 import cpml as cp
+    prof = cp.pack_profiles(case.profiles)
+    t0 = time.perf_counter()
+    import oracle
+
+    def J(planes):
+        _, tr, _, blew = oracle.run(case.grid.kind, case.grid, planes, prof, case.src_ijk, case.srcfn,
+                                    case.rec_ijk, case.nstep)
+        assert not blew
+        return tr
+
+    d_obs = J(base)
+    cells = par.fd_cells(base.shape[1:], case.grid.npml, ncells, seed)
+    names = ("eps11", "eps33", "sigma")
+    planes_of = ((0,), (2,), (3, 5))
+    ad, fd, rows = [], [], []
+    for n, (k, i) in enumerate(cells):
+        q = n % 3
+        h = h_rel * cur[planes_of[q][0]][k, i]
+        p, m_ = cur.copy(), cur.copy()
+        for pl in planes_of[q]:
+            p[pl][k, i] += h
+            m_[pl][k, i] -= h
+        d = (par.misfit(J(p), d_obs) - par.misfit(J(m_), d_obs)) / (2 * h)
+        g = float(grads[q][k, i])
+        ad.append(g)
+        fd.append(d)
+        rows.append({"cell": [k, i], "param": names[q], "adjoint": g, "fd": d,
+                     "rel_err": abs(g - d) / abs(d) if d != 0 else None})
+    ad, fd = np.array(ad), np.array(fd)
+    rel = [r["rel_err"] for r in rows if r["rel_err"] is not None]
+    return {"cells": len(cells), "seed": seed, "h_rel": h_rel, "steps": case.nstep,
+            "rel_l2": float(np.linalg.norm(ad - fd) / np.linalg.norm(fd)),
+            "rel_err_max": max(rel) if rel else None, "rel_err_median": float(np.median(rel)) if rel else None,
+            "per_cell": rows, "oracle_s": round(time.perf_counter() - t0, 1)}
+
+
+def parity_plain(case, device, nsteps=None):
+    """The default GPU path of ``case`` (the form the bench times) against the
+    FP64 oracle over ``nsteps`` steps from rest: traces and final fields."""
+    from oracle import parity as par
+    from seidart_gb300.solver import FIELDS
+    n = case.nstep if nsteps is None else int(nsteps)
+    s = make_solver(case, device)
+    tiles = s.on_chip()
+    s.run(n)
+    s.status()
+    tr = s.traces()[:n]
+    names = FIELDS[case.grid.kind]
+    fields = [s.field(nm) for nm in names]
+    s.close()
+    t0 = time.perf_counter()
+    st, ref = par.oracle_case(case, n)
+    out = {"workload": f"{case.name}: {case.grid.cells} cells", "steps": n, "of_steps": case.nstep,
+           "form": "on chip" if tiles else "one launch per step"}
+    out.update(par.compare_run(tr, fields, st, ref, names))
+    out["oracle_s"] = round(time.perf_counter() - t0, 1)
+    return out
 
 
 def time_shots(solver, nstep, K, W, flush, stream, sync_all=None):
@@ -416,7 +529,8 @@ def profile_traffic(name):
 
 
 def cpu_baseline(case, seconds=10.0, chunk=100):
-    """FP64 oracle (restated legacy Fortran loops) on all host threads, time-bounded sample."""
+    """FP64 oracle (restated legacy Fortran loops) on all host threads, time-bounded sample, built
+    for the host CPU (oracle.NATIVE_FLAGS)."""
     import oracle
     from seidart_gb300 import cpml as cp
     prof = cp.pack_profiles(case.profiles)
@@ -425,11 +539,12 @@ def cpu_baseline(case, seconds=10.0, chunk=100):
     t0 = time.perf_counter()
     while time.perf_counter() - t0 < seconds and done + chunk <= case.nstep:
         st, _, _, _ = oracle.run(case.grid.kind, case.grid, case.planes, prof, case.src_ijk, case.srcfn,
-                                 case.rec_ijk, chunk, state=st)
+                                 case.rec_ijk, chunk, state=st, native=True)
         done += chunk
     el = time.perf_counter() - t0
     value = case.grid.cells * done / el / 1e9
     return {"value": round(value, 4), "unit": METRIC, "cores": oracle.num_threads(), "kind": "port",
+            "cpu": cpu_model(), "build": oracle.NATIVE_FLAGS,
             "sample": f"{done} of {case.nstep} steps of the same workload, FP64, OpenMP ({el:.1f} s)"}
 
 
@@ -451,7 +566,7 @@ def run_reference(args):
         if st is not None and st.step + chunk > case.nstep:
             st = None
         st, _, _, _ = oracle.run(case.grid.kind, case.grid, case.planes, prof, case.src_ijk, case.srcfn,
-                                 case.rec_ijk, chunk, state=st)
+                                 case.rec_ijk, chunk, state=st, native=True)
 
     for _ in range(args.warmup):
         step()
@@ -460,14 +575,15 @@ def run_reference(args):
         step()
     el = time.perf_counter() - t0
     value = case.grid.cells * chunk * args.steps / el / 1e9
-    sample = f"{chunk} consecutive time steps of the workload per bench step, FP64 restatement of the legacy loops"
+    sample = (f"{chunk} consecutive time steps of the workload per bench step (the shot restarts after its "
+              f"{case.nstep} steps), FP64 restatement of the legacy loops")
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": METRIC, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * el / args.steps, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_steps": chunk},
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
+        "config": bench_config(case.nstep, case.grid.cells, args.gpus),
         "cpu_baseline": {"value": round(value, 4), "unit": METRIC, "cores": oracle.num_threads(), "kind": "port",
-                         "sample": sample},
+                         "cpu": cpu_model(), "build": oracle.NATIVE_FLAGS, "sample": sample},
         "e2e": {"value": round(value, 4), "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -565,9 +681,8 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded layered permittivity/conductivity model)",
-        "config": {"workload": WORKLOAD, "time_steps_per_bench_step": case.nstep, "cells": cells,
-                   "l2": "256 MiB buffer written between shots (flush)", "parallelism": f"replicas x{world}"},
+        "vs_baseline": None, "dtype": "f32", "data": DATA,
+        "config": bench_config(case.nstep, cells, world),
         "gpu_launches": args.steps * launches,
         "roofline": roofline, "roofline_step": roofline_step,
     }
@@ -626,10 +741,29 @@ def run_ours(args):
         extras["seismic25_plain"] = bench_plain(sy.seismic25_ice(nstep=3000), device, flush, stream, peak,
                                                 seis25_bytes, 2, 1)
         line["extras"] = extras
+    par_on = rank == 0 and not args.skip_parity
     if not args.skip_batched:
-        line.setdefault("extras", {})["batched"] = bench_batched(device, flush, stream, peak, value / world)
+        picks = (0, 31, 63, 64, 69, 74, 79) if par_on else ()
+        line.setdefault("extras", {})["batched"] = bench_batched(device, flush, stream, peak, value / world,
+                                                                 parity_models=picks)
     if not args.skip_adjoint:
-        line.setdefault("extras", {})["adjoint"] = bench_adjoint(device)
+        line.setdefault("extras", {})["adjoint"] = bench_adjoint(device, fd_cells=args.parity_fd_cells if par_on else 0)
+
+    # ---- parity: each workload's timed GPU form against the FP64 oracle ------
+    if par_on:
+        par = {"tolerance_rel_l2": 1e-5,
+               "config0_seismic2": parity_plain(sy.seismic2_firn_ice(nstep=2000), device),
+               "config1_electromag2": parity_plain(case, device),
+               "config2_seismic25": parity_plain(sy.seismic25_ice(nstep=3000), device, nsteps=args.parity_s25_steps)}
+        if par["config2_seismic25"]["steps"] < 3000:
+            par["config2_seismic25"]["note"] = ("first steps of the 3000-step shot only: the FP64 oracle of the "
+                                                "14.6 M-cell grid takes minutes per thousand steps on the host")
+        ex = line.get("extras", {})
+        if "parity" in ex.get("batched", {}):
+            par["config3_batched"] = ex["batched"]["parity"]
+        if "parity_fd" in ex.get("adjoint", {}):
+            par["config4_adjoint_fd"] = {k: v for k, v in ex["adjoint"]["parity_fd"].items() if k != "per_cell"}
+        line["parity"] = par
 
     if rank == 0 and not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline(case, seconds=args.cpu_seconds)
@@ -657,13 +791,19 @@ def main(argv=None):
     ap.add_argument("--only", choices=["seismic2", "seismic25", "batched", "adjoint"],
                     help="run one secondary leg alone and print its record (for profiler runs)")
     ap.add_argument("--skip-adjoint", action="store_true")
+    ap.add_argument("--skip-parity", action="store_true",
+                    help="skip the comparison of each workload's GPU form with the FP64 oracle (untimed)")
+    ap.add_argument("--parity-s25-steps", type=int, default=1000,
+                    help="time steps of the seismic25 workload compared with the oracle")
+    ap.add_argument("--parity-fd-cells", type=int, default=20,
+                    help="cells of the adjoint's finite-difference check (0 = none)")
     ap.add_argument("--batch-tiling", default=None,
                     help="with --only batched: fixed rows-per-thread x blocks-per-SM (e.g. 4x3) instead of the autotuner")
     ap.add_argument("--headline-only", action="store_true",
                     help="only the timed headline shots (for profiler runs): no e2e, extras or CPU leg")
     args = ap.parse_args(argv)
     if args.headline_only:
-        args.skip_extras = args.skip_cpu = args.skip_batched = args.skip_adjoint = True
+        args.skip_extras = args.skip_cpu = args.skip_batched = args.skip_adjoint = args.skip_parity = True
         args.e2e_steps = 0
     if args.warmup < 3:
         print("note: fewer than 3 warm-up steps", file=sys.stderr)

@@ -238,16 +238,35 @@ int32_t sfd_launch_half(sfd_handle* h, int32_t which, int32_t count);
  * counterpart in the reference: its time loop has one execution form. */
 int32_t sfd_on_chip(sfd_handle* h, int32_t* tiles, int32_t* tile_rows);
 
+/* Longest wait, in ns, of this handle's on-chip runs (sfd_run, and the
+ * adjoint's on-chip recompute and sweep) for a neighbouring tile's edge
+ * values; 0 restores the default, 2 s.  A wait that runs out makes every
+ * tile leave the run and sfd_status (sfd_adjoint_gradient) return
+ * SFD_ERR_TIMEOUT; the context stays usable and sfd_reset starts over.  A
+ * correct run never waits near the default: a short limit is how a caller
+ * (or a test) checks the timeout path.  No counterpart in the reference. */
+int32_t sfd_set_wait_limit(sfd_handle* h, int64_t ns);
+/* Test aid for that timeout path: with `on` != 0, the on-chip runs of this
+ * handle await edge values under tags no tile ever writes, so every wait runs
+ * out after the limit and the run ends with SFD_ERR_TIMEOUT (a flag that
+ * nothing sets; no fault, no unbounded wait).  0 restores normal runs. */
+int32_t sfd_test_stall_waits(sfd_handle* h, int32_t on);
+
 /* Release the handle (the caller frees its device buffer afterwards). */
 int32_t sfd_destroy(sfd_handle* h);
 
 /* ---- One shot without device allocation --------------------------------------
  * For callers that cannot call cudaMalloc (a host application that owns every
  * device allocation and exposes no allocator, a plugin whose process forbids
- * new device allocations, a fixed memory budget).  Runs one electromag2 shot
- * with the whole device state in a file-scope device array of 32 MiB that
- * every GPU loading this library holds until exit; larger configurations are
- * rejected with SFD_ERR_BAD_ARG.  Inputs and outputs are host arrays: model
+ * new device allocations, a fixed memory budget).  Runs one electromag2 shot,
+ * in the two-pass form (cfg->flags must be 0 or SFD_FLAG_TWO_PASS), with the
+ * whole device state in a file-scope device array of 32 MiB that every GPU
+ * loading this library holds until exit; larger configurations are rejected
+ * with SFD_ERR_BAD_ARG.  The array is taken from a device's memory when the
+ * first call there loads its module (lazy module loading; at library load
+ * with CUDA_MODULE_LOADING=EAGER), so that first call can fail with
+ * SFD_ERR_CUDA on a full device: make it early, before the caller's own
+ * memory budget is spent.  Inputs and outputs are host arrays: model
  * (6 planes as sfd_set_model), profiles (as sfd_set_cpml), source cell and
  * time functions (2 x nstep, as sfd_set_source), receivers (nrec (i,j,k)
  * triples) and traces out (nstep x 2 x nrec FP32).  Each call clears the
@@ -302,6 +321,14 @@ int32_t sfd_batch_create(sfd_handle* const* handles, int32_t nmodels, void* dev_
 int32_t sfd_batch_set_tiling(sfd_batch* b, int32_t zb, int32_t blocks_per_sm);
 /* Advance every model nsteps steps (asynchronous). */
 int32_t sfd_batch_run(sfd_batch* b, int64_t nsteps);
+/* Longest wait, in ns, of a block at the batch kernel's grid barrier; 0
+ * restores the default, 2 s.  A wait that runs out makes every block leave
+ * the kernel and sfd_batch_status return SFD_ERR_TIMEOUT. */
+int32_t sfd_batch_set_wait_limit(sfd_batch* b, int64_t ns);
+/* Test aid: with `on` != 0 the grid barrier waits for one block more than the
+ * launch has, so every block's wait runs out after the limit and the run ends
+ * with SFD_ERR_TIMEOUT.  0 restores normal runs. */
+int32_t sfd_batch_test_stall_waits(sfd_batch* b, int32_t on);
 /* Synchronise; SFD_ERR_TIMEOUT if the grid barrier gave up, SFD_ERR_UNSTABLE
  * (with *failed_model) if a model blew up. */
 int32_t sfd_batch_status(sfd_batch* b, int32_t* failed_model);

@@ -23,29 +23,32 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "liboracle.so"
+LIB_NATIVE = HERE / "liboracle_native.so"
+# compiler flags of liboracle_native.so (the timed CPU baseline's build)
+NATIVE_FLAGS = "g++ -O3 -fopenmp " + ("-mcpu=native" if os.uname().machine == "aarch64" else "-march=native")
 SEISMIC2, SEISMIC25, ELECTROMAG2, ELECTROMAG25, ELECTROMAG2C = 1, 2, 3, 4, 5
 NFIELDS = {SEISMIC2: 5, SEISMIC25: 9, ELECTROMAG2: 3, ELECTROMAG25: 6, ELECTROMAG2C: 6}
 NMEM = {SEISMIC2: 8, SEISMIC25: 18, ELECTROMAG2: 4, ELECTROMAG25: 12, ELECTROMAG2C: 8}
 NCH = {SEISMIC2: 2, SEISMIC25: 3, ELECTROMAG2: 2, ELECTROMAG25: 3, ELECTROMAG2C: 4}
 
 _lock = threading.Lock()
-_lib = None
+_libs = {}
 
 
-def build(force: bool = False) -> Path:
-    """Compile liboracle.so with the Makefile in this directory."""
+def build(force: bool = False, native: bool = False) -> Path:
+    """Compile liboracle.so (or the host-tuned liboracle_native.so) with the
+    Makefile in this directory."""
     src = HERE / "fdtd_oracle.cpp"
-    if force or not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
-        subprocess.run(["make", "-s", "-C", str(HERE), "liboracle.so"] + (["-B"] if force else []), check=True)
-    return LIB
+    out = LIB_NATIVE if native else LIB
+    if force or not out.exists() or out.stat().st_mtime < src.stat().st_mtime:
+        subprocess.run(["make", "-s", "-C", str(HERE), out.name] + (["-B"] if force else []), check=True)
+    return out
 
 
-def lib():
-    global _lib
+def lib(native: bool = False):
     with _lock:
-        if _lib is None:
-            build()
-            L = C.CDLL(str(LIB))
+        if native not in _libs:
+            L = C.CDLL(str(build(native=native)))
             dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
             i, d = C.c_int, C.c_double
             common_tail = [dp, dp, i, i, dp, i, i, i, dp, dp, i, ip, dp, dp, ip]
@@ -58,8 +61,8 @@ def lib():
             for f in (L.orc_electromag2, L.orc_electromag2c, L.orc_seismic2, L.orc_seismic25, L.orc_electromag25):
                 f.restype = C.c_int
             L.orc_num_threads.restype = C.c_int
-            _lib = L
-        return _lib
+            _libs[native] = L
+        return _libs[native]
 
 
 @dataclass
@@ -80,10 +83,12 @@ def _d(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
-def run(kind, grid, planes, packed_profiles, src_ijk, srcfn, rec_ijk, nsteps, state: OracleState = None):
+def run(kind, grid, planes, packed_profiles, src_ijk, srcfn, rec_ijk, nsteps, state: OracleState = None,
+        native: bool = False):
     """Advance ``nsteps`` steps of the FP64 oracle.  Returns (state, traces,
-    maxnorm, blew_up); traces is (nsteps, nch, nrec)."""
-    L = lib()
+    maxnorm, blew_up); traces is (nsteps, nch, nrec).  ``native`` runs the
+    host-tuned build (timing only)."""
+    L = lib(native)
     three = kind in (SEISMIC25, ELECTROMAG25)
     shape = (grid.nz, grid.ny, grid.nx) if three else (grid.nz, grid.nx)
     if state is None:

@@ -26,10 +26,10 @@ EXPORTS = (
     "sfd_set_source", "sfd_share_model", "sfd_set_receivers", "sfd_reset", "sfd_set_field", "sfd_get_field",
     "sfd_get_field_async", "sfd_encode_field_i16",
     "sfd_get_memory", "sfd_run", "sfd_status", "sfd_get_traces", "sfd_traces_device", "sfd_launch_half",
-    "sfd_on_chip",
+    "sfd_on_chip", "sfd_set_wait_limit", "sfd_test_stall_waits",
     "sfd_destroy", "sfd_checkpoint_bytes", "sfd_checkpoint_save", "sfd_checkpoint_load", "sfd_adjoint_bytes",
     "sfd_adjoint_begin", "sfd_adjoint_segment", "sfd_adjoint_gradient", "sfd_batch_scratch_bytes", "sfd_batch_create", "sfd_batch_set_tiling", "sfd_batch_run",
-    "sfd_batch_status", "sfd_batch_destroy", "sfd_electromag2_run_static",
+    "sfd_batch_status", "sfd_batch_set_wait_limit", "sfd_batch_test_stall_waits", "sfd_batch_destroy", "sfd_electromag2_run_static",
 )
 
 
@@ -90,6 +90,8 @@ def _declare(lib):
         "sfd_traces_device": (P, [P]),
         "sfd_launch_half": (i32, [P, i32, i32]),
         "sfd_on_chip": (i32, [P, ip, ip]),
+        "sfd_set_wait_limit": (i32, [P, i64]),
+        "sfd_test_stall_waits": (i32, [P, i32]),
         "sfd_destroy": (i32, [P]),
         "sfd_electromag2_run_static": (i32, [C.POINTER(SfdConfig), dp, dp, i32, i32, dp, ip, fp, P]),
     }

@@ -35,6 +35,8 @@ def _declare(L):
         ("sfd_batch_set_tiling", i32, [P, i32, i32]),
         ("sfd_batch_run", i32, [P, i64]),
         ("sfd_batch_status", i32, [P, C.POINTER(i32)]),
+        ("sfd_batch_set_wait_limit", i32, [P, i64]),
+        ("sfd_batch_test_stall_waits", i32, [P, i32]),
         ("sfd_batch_destroy", i32, [P]),
     ]:
         f = getattr(L, name)
@@ -75,6 +77,10 @@ class Batch:
 
     def run(self, nsteps: int) -> None:
         check(self._L.sfd_batch_run(self._b, int(nsteps)))
+
+    def set_wait_limit(self, ns: int) -> None:
+        """Longest wait (ns) at the kernel's grid barrier; 0 = the default 2 s."""
+        check(self._L.sfd_batch_set_wait_limit(self._b, int(ns)))
 
     def status(self) -> None:
         """Synchronise; raise on a barrier timeout or a blown-up model."""

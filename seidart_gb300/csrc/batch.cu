@@ -66,7 +66,7 @@ __device__ bool grid_barrier(GridBarrier* bar, unsigned nblocks, unsigned long l
 template <int ZB>
 __global__ void __launch_bounds__(256, 3)
     batch_kernel(const BatchModel* __restrict__ models, const BatchGroup* __restrict__ groups, int ngroups,
-                 int total_tiles, int nsteps, GridBarrier* bar, unsigned long long limit_ns) {
+                 int total_tiles, int nsteps, GridBarrier* bar, unsigned long long limit_ns, int extra) {
   __shared__ __align__(16) union {
     float em2[8 * ZB + 1][kEm2Row];
     float s2[3][8 * ZB + 2][34];
@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(256, 3)
       }
       __syncthreads();  // shared tile buffers are reused by the next tile
     }
-    if (!grid_barrier(bar, gridDim.x, limit_ns)) return;
+    if (!grid_barrier(bar, gridDim.x + extra, limit_ns)) return;
   }
 }
 
@@ -162,9 +162,10 @@ void batch_end(const BatchModel* models, int nmodels, int nsteps, cudaStream_t s
 }
 
 cudaError_t batch_launch(int zb, int grid, const BatchModel* models, const BatchGroup* groups, int ngroups,
-                         int total_tiles, int nsteps, GridBarrier* bar, unsigned long long limit_ns, cudaStream_t s) {
+                         int total_tiles, int nsteps, GridBarrier* bar, unsigned long long limit_ns, int extra,
+                         cudaStream_t s) {
   void* args[] = {(void*)&models, (void*)&groups, (void*)&ngroups, (void*)&total_tiles, (void*)&nsteps,
-                  (void*)&bar, (void*)&limit_ns};
+                  (void*)&bar, (void*)&limit_ns, (void*)&extra};
   return cudaLaunchCooperativeKernel(batch_kernel_ptr(zb), dim3(grid), dim3(32, 8), args, 0, s);
 }
 

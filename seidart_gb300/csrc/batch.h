@@ -41,6 +41,7 @@ const void* batch_kernel_ptr(int zb);
 void batch_begin(const BatchModel* models, int nmodels, const int* steps, GridBarrier* bar, cudaStream_t s);
 void batch_end(const BatchModel* models, int nmodels, int nsteps, cudaStream_t s);
 cudaError_t batch_launch(int zb, int grid, const BatchModel* models, const BatchGroup* groups, int ngroups,
-                         int total_tiles, int nsteps, GridBarrier* bar, unsigned long long limit_ns, cudaStream_t s);
+                         int total_tiles, int nsteps, GridBarrier* bar, unsigned long long limit_ns, int extra,
+                         cudaStream_t s);
 
 }  // namespace sfd

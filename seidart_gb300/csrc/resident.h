@@ -98,6 +98,7 @@ struct Em2Resident {
   ResScratch r;
   int t0, nsteps;
   unsigned long long limit_ns;  // longest wait for a neighbour before the run is abandoned
+  unsigned tag_bias;            // added to every awaited edge tag; 0 except in the timeout test aid
   ResDump dump;
 };
 
@@ -150,6 +151,7 @@ struct Seis2Resident {
   ResScratch r;  // six edge fields
   int t0, nsteps;
   unsigned long long limit_ns;
+  unsigned tag_bias;  // added to every awaited edge tag; 0 except in the timeout test aid
 };
 
 // Tiling of an NX x NZ seismic2 grid for `max_ctas` CTAs of at most

@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
   }
   if (xwarp) {  // edges of the tiles below and to the right for step 0
     if (!fetch_edges(down ? erow(0, 0, bz + 1) + x0 : nullptr, sExRow + TYT * TW, down ? 4 * nc4 : 0,
-                     right ? ecol(0, 0, bx + 1) + z0 : nullptr, sEzCol + TXT, SX, right ? nzt : 0, 1u, ctl,
+                     right ? ecol(0, 0, bx + 1) + z0 : nullptr, sEzCol + TXT, SX, right ? nzt : 0, 1u + a.tag_bias, ctl,
                      a.limit_ns) &&
         (tid & 31) == 0)
       s_abort = 1;
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
       }
     } else if (xwarp) {  // Hy row above and column on the left for this step's E half
       if (!fetch_edges(up ? erow(par, 1, bz - 1) + x0 : nullptr, sHyRow, up ? 4 * nc4 : 0,
-                       left ? ecol(par, 1, bx - 1) + z0 : nullptr, sHyCol, SX, left ? nzt : 0, tag, ctl,
+                       left ? ecol(par, 1, bx - 1) + z0 : nullptr, sHyCol, SX, left ? nzt : 0, tag + a.tag_bias, ctl,
                        a.limit_ns) &&
           (tid & 31) == 0)
         s_abort = 1;
@@ -462,7 +462,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
       }
     } else if (xwarp && s + 1 < a.nsteps) {  // Ex row below and Ez column to the right for step s+1
       if (!fetch_edges(down ? erow(par ^ 1, 0, bz + 1) + x0 : nullptr, sExRow + TYT * TW, down ? 4 * nc4 : 0,
-                       right ? ecol(par ^ 1, 0, bx + 1) + z0 : nullptr, sEzCol + TXT, SX, right ? nzt : 0, tag + 1u,
+                       right ? ecol(par ^ 1, 0, bx + 1) + z0 : nullptr, sEzCol + TXT, SX, right ? nzt : 0, tag + 1u + a.tag_bias,
                        ctl, a.limit_ns) &&
           (tid & 31) == 0)
         s_abort = 1;

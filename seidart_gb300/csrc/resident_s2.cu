@@ -253,13 +253,13 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
       if (s > 0) record(t - 1);
       bool good = true;
       if (warp == 0 && left)
-        good = fetch2(ecol(ps, kESLast, bx - 1) + z0, SXX + fi(0, -1), SW, nullptr, nullptr, 0, tz, ts, ctl, a.limit_ns);
+        good = fetch2(ecol(ps, kESLast, bx - 1) + z0, SXX + fi(0, -1), SW, nullptr, nullptr, 0, tz, ts + a.tag_bias, ctl, a.limit_ns);
       else if (warp == 1 && right)
-        good = fetch2(ecol(ps, kESFirst, bx + 1) + z0, SXZ + fi(0, tw), SW, nullptr, nullptr, 0, tz, ts, ctl, a.limit_ns);
+        good = fetch2(ecol(ps, kESFirst, bx + 1) + z0, SXZ + fi(0, tw), SW, nullptr, nullptr, 0, tz, ts + a.tag_bias, ctl, a.limit_ns);
       else if (warp == 2 && up)
-        good = fetch2(erow(ps, kESLast, bz - 1) + x0, SXZ + fi(-1, 0), 1, nullptr, nullptr, 0, tw, ts, ctl, a.limit_ns);
+        good = fetch2(erow(ps, kESLast, bz - 1) + x0, SXZ + fi(-1, 0), 1, nullptr, nullptr, 0, tw, ts + a.tag_bias, ctl, a.limit_ns);
       else if (warp == 3 && down)
-        good = fetch2(erow(ps, kESFirst, bz + 1) + x0, SZZ + fi(tz, 0), 1, nullptr, nullptr, 0, tw, ts, ctl, a.limit_ns);
+        good = fetch2(erow(ps, kESFirst, bz + 1) + x0, SZZ + fi(tz, 0), 1, nullptr, nullptr, 0, tw, ts + a.tag_bias, ctl, a.limit_ns);
       if (!good && (tid & 31) == 0) s_abort = 1;
     } else {
       for (int n = tid - 32 * kS2ExchangeWarps; n < CS; n += kS2CellThreads) {
@@ -348,16 +348,16 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
       if (s + 1 < a.nsteps) {
         if (warp == 0 && left)
           good = fetch2(ecol(pv, kEVxLast, bx - 1) + z0, VX + fi(0, -1), SW, ecol(pv, kEVzLast, bx - 1) + z0,
-                        VZ + fi(0, -1), SW, tz, tv, ctl, a.limit_ns);
+                        VZ + fi(0, -1), SW, tz, tv + a.tag_bias, ctl, a.limit_ns);
         else if (warp == 1 && right)
           good = fetch2(ecol(pv, kEVxFirst, bx + 1) + z0, VX + fi(0, tw), SW, ecol(pv, kEVzFirst, bx + 1) + z0,
-                        VZ + fi(0, tw), SW, tz, tv, ctl, a.limit_ns);
+                        VZ + fi(0, tw), SW, tz, tv + a.tag_bias, ctl, a.limit_ns);
         else if (warp == 2 && up)
           good = fetch2(erow(pv, kEVxLast, bz - 1) + x0, VX + fi(-1, 0), 1, erow(pv, kEVzLast, bz - 1) + x0,
-                        VZ + fi(-1, 0), 1, tw, tv, ctl, a.limit_ns);
+                        VZ + fi(-1, 0), 1, tw, tv + a.tag_bias, ctl, a.limit_ns);
         else if (warp == 3 && down)
           good = fetch2(erow(pv, kEVxFirst, bz + 1) + x0, VX + fi(tz, 0), 1, erow(pv, kEVzFirst, bz + 1) + x0,
-                        VZ + fi(tz, 0), 1, tw, tv, ctl, a.limit_ns);
+                        VZ + fi(tz, 0), 1, tw, tv + a.tag_bias, ctl, a.limit_ns);
       }
       if (!good && (tid & 31) == 0) s_abort = 1;
     } else {

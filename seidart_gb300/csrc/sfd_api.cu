@@ -64,6 +64,10 @@ constexpr double kPI = 3.141592653589793238462643;
 constexpr double kMu0 = 4.0 * kPI * 1.0e-7;
 constexpr double kEps0 = 8.85418782e-12;
 constexpr int kGraphSteps = 32;
+constexpr unsigned long long kDefaultWaitNs = 2000000000ull;  // bounded device waits: 2 s
+// Added to the awaited edge tags by the timeout test aid: tags are step
+// numbers + 1 or 2, so no tile ever writes a biased one.
+constexpr unsigned kStallTagBias = 0x40000000u;
 
 thread_local std::string g_err;
 
@@ -270,6 +274,8 @@ struct sfd_handle_s {
   ResPlan res_plan;     // electromag2
   Seis2ResPlan s2_plan;  // seismic2
   int64_t step = 0;
+  unsigned long long wait_ns = kDefaultWaitNs;  // longest wait of an on-chip run for a neighbouring tile
+  bool stall_waits = false;                     // timeout test aid: waits expect tags no tile writes
   // The FP64 model planes read after sfd_set_model (the source scaling; for
   // electromag2 also the adjoint's chain rule), copied from its input:
   // electromag2 all six planes; electromag2c eps11 eps33 (re, im);
@@ -576,7 +582,8 @@ Em2Resident resident_args(const sfd_handle* h, int64_t nsteps) {
   r.r.ecol = r.r.erow + 4 * kResMaxTiles1D * (size_t)h->L.P;
   r.t0 = (int)h->step;
   r.nsteps = (int)nsteps;
-  r.limit_ns = 2000000000ull;
+  r.limit_ns = h->wait_ns;
+  r.tag_bias = h->stall_waits ? kStallTagBias : 0u;
   r.dump = ResDump{nullptr, 0, {0, 0, 0, 0, 0, 0, 0}};
   return r;
 }
@@ -601,7 +608,8 @@ Seis2Resident seis2_resident_args(const sfd_handle* h, int64_t nsteps) {
   r.r.ecol = r.r.erow + 2 * 6 * kResMaxTiles1D * (size_t)h->L.P;
   r.t0 = (int)h->step;
   r.nsteps = (int)nsteps;
-  r.limit_ns = 2000000000ull;
+  r.limit_ns = h->wait_ns;
+  r.tag_bias = h->stall_waits ? kStallTagBias : 0u;
   return r;
 }
 
@@ -1380,9 +1388,26 @@ int32_t sfd_status(sfd_handle* h, int64_t* step, double* maxnorm) {
   CK(cudaStreamSynchronize(h->stream));
   if (step) *step = h->step;
   if (maxnorm) *maxnorm = (double)ctl.maxnorm;
-  if (ctl.err) return fail(SFD_ERR_TIMEOUT, "on-chip run: a neighbouring tile did not answer within 2 s");
+  if (ctl.err)
+    return fail(SFD_ERR_TIMEOUT, "on-chip run: a neighbouring tile did not answer within %.3g s",
+                (double)h->wait_ns * 1e-9);
   if (!(ctl.maxnorm <= 1.0e25f))
     return fail(SFD_ERR_UNSTABLE, "field norm %g exceeded 1e25 (code became unstable and blew up)", (double)ctl.maxnorm);
+  return SFD_OK;
+}
+
+int32_t sfd_set_wait_limit(sfd_handle* h, int64_t ns) {
+  g_err.clear();
+  if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
+  if (ns < 0) return fail(SFD_ERR_BAD_ARG, "wait limit must be >= 0 ns (0 = the default 2 s)");
+  h->wait_ns = ns == 0 ? kDefaultWaitNs : (unsigned long long)ns;
+  return SFD_OK;
+}
+
+int32_t sfd_test_stall_waits(sfd_handle* h, int32_t on) {
+  g_err.clear();
+  if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
+  h->stall_waits = on != 0;
   return SFD_OK;
 }
 
@@ -1443,7 +1468,8 @@ struct sfd_batch_s {
   char* scratch = nullptr;
   cudaStream_t stream = nullptr;
   int zb = 2, bps = 4, nsm = 0;
-  unsigned long long limit_ns = 2000000000ull;  // barrier wait limit: 2 s
+  unsigned long long limit_ns = kDefaultWaitNs;  // barrier wait limit
+  int stall = 0;  // timeout test aid: the barrier waits for one block more than the launch has
   std::vector<BatchModel> models;
   std::vector<int> steps;
   GridBarrier* bar() const { return (GridBarrier*)scratch; }
@@ -1571,13 +1597,28 @@ int32_t sfd_batch_run(sfd_batch* b, int64_t nsteps) {
                      b->stream));
   batch_begin(b->dmodels(), n, b->dsteps(), b->bar(), b->stream);
   CK(batch_launch(b->zb, grid, b->dmodels(), b->dgroups(), (int)b->groups.size(), total, (int)nsteps, b->bar(),
-                  b->limit_ns, b->stream));
+                  b->limit_ns, b->stall, b->stream));
   batch_end(b->dmodels(), n, (int)nsteps, b->stream);
   CK(cudaGetLastError());
   for (sfd_handle* h : b->h) {
     h->step += nsteps;
     h->cur ^= (int)(nsteps & 1);
   }
+  return SFD_OK;
+}
+
+int32_t sfd_batch_set_wait_limit(sfd_batch* b, int64_t ns) {
+  g_err.clear();
+  if (!b) return fail(SFD_ERR_BAD_ARG, "NULL batch");
+  if (ns < 0) return fail(SFD_ERR_BAD_ARG, "wait limit must be >= 0 ns (0 = the default 2 s)");
+  b->limit_ns = ns == 0 ? kDefaultWaitNs : (unsigned long long)ns;
+  return SFD_OK;
+}
+
+int32_t sfd_batch_test_stall_waits(sfd_batch* b, int32_t on) {
+  g_err.clear();
+  if (!b) return fail(SFD_ERR_BAD_ARG, "NULL batch");
+  b->stall = on ? 1 : 0;
   return SFD_OK;
 }
 

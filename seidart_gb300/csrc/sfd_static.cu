@@ -10,8 +10,19 @@
 // array of fixed size, so the call allocates nothing.  The caller passes its
 // inputs and receives its outputs in host memory.
 //
+// The shot runs the two-pass electromag2 form (one kernel per half-step,
+// fields updated in place), the one that needs a single copy of the state:
+// config flags other than 0 or SFD_FLAG_TWO_PASS are rejected.
+//
 // The array is 32 MiB.  Every GPU that loads this library holds it until the
-// process exits.  A configuration whose state does not fit is rejected with
+// process exits.  The library is built without relocatable device code, so
+// this file is its own CUDA module; under the runtime's default lazy module
+// loading the module, and with it the 32 MiB, is loaded on a device at the
+// first call there (at library load only with CUDA_MODULE_LOADING=EAGER).
+// That first call can therefore fail with SFD_ERR_CUDA when the device has no
+// 32 MiB left: a caller with a fixed device-memory budget should make one
+// early call (a tiny shot) before it commits the rest of its memory.  A
+// configuration whose state does not fit is rejected with
 // SFD_ERR_BAD_ARG.  Every call shares the one array and keeps whatever the
 // previous call left in it, so each call clears the whole state first;
 // calls whose GPU work overlaps (several host threads, or streams that are
@@ -71,6 +82,9 @@ extern "C" int32_t sfd_electromag2_run_static(const sfd_config* cfg, const doubl
     return fail_static(SFD_ERR_BAD_ARG, "NULL argument");
   if (cfg->kind != SFD_ELECTROMAG2)
     return fail_static(SFD_ERR_BAD_ARG, "sfd_electromag2_run_static runs electromag2 only");
+  if (cfg->flags != 0 && cfg->flags != SFD_FLAG_TWO_PASS)
+    return fail_static(SFD_ERR_BAD_ARG,
+                       "sfd_electromag2_run_static runs the two-pass form: flags must be 0 or SFD_FLAG_TWO_PASS");
   sfd_config c = *cfg;
   c.flags = SFD_FLAG_TWO_PASS;  // two kernels per step: one copy of the state
   size_t need = 0;

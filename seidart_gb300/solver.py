@@ -213,6 +213,12 @@ class FDTDSolver:
         invalid afterwards; reset before the next run)."""
         check(self._L.sfd_launch_half(self._h, int(which), int(count)))
 
+    def set_wait_limit(self, ns: int) -> None:
+        """Longest wait (ns) of an on-chip run for a neighbouring tile; 0 = the
+        default 2 s.  A wait that runs out makes ``status`` raise SfdError
+        with code SFD_ERR_TIMEOUT."""
+        check(self._L.sfd_set_wait_limit(self._h, int(ns)))
+
     def on_chip(self):
         """(tiles, tile rows) when ``run`` keeps the whole state on chip (one
         launch per run, one CTA per tile), else None (one launch per step)."""

@@ -110,13 +110,26 @@ def _cost(case) -> float:
     return float(case.grid.cells) * float(case.nstep)
 
 
-def gpu_runner(cases, device="cuda") -> List[np.ndarray]:
+def default_device(group=None) -> str:
+    """The GPU of this process: ``cuda:{LOCAL_RANK}`` when torch.distributed
+    is initialised with more than one rank (one process per GPU, as torchrun
+    starts them), else ``cuda`` (the current device)."""
+    import os
+    _, world, _ = _dist(group)
+    if world > 1 and "LOCAL_RANK" in os.environ:
+        return f"cuda:{int(os.environ['LOCAL_RANK'])}"
+    return "cuda"
+
+
+def gpu_runner(cases, device=None) -> List[np.ndarray]:
     """Receiver traces (nstep, nch, nrec) of each case.  The 2-D single-pass
     kinds advance together in one batched launch per run, cases that hold
     the same model planes (the same array object) sharing one copy of the
-    coefficients; 2.5-D cases run one after another."""
+    coefficients; 2.5-D cases run one after another.  ``device`` defaults to
+    :func:`default_device`."""
     from .batch import Batch, autotune
     from .solver import FDTDSolver, run_shot
+    device = default_device() if device is None else device
 
     out: List[Optional[np.ndarray]] = [None] * len(cases)
     two_d = [q for q, c in enumerate(cases) if c.grid.kind in (SEISMIC2, ELECTROMAG2)]
@@ -157,14 +170,16 @@ def gpu_runner(cases, device="cuda") -> List[np.ndarray]:
     return out
 
 
-def run_survey(cases, runner: Optional[Callable] = None, group=None, device="cuda") -> Optional[List[np.ndarray]]:
+def run_survey(cases, runner: Optional[Callable] = None, group=None, device=None) -> Optional[List[np.ndarray]]:
     """Traces of every case of a survey (a list of
     :class:`seidart_gb300.synthetic.Case`-like objects: grid, planes, profiles,
     src_ijk, srcfn, rec_ijk).  Under ``torch.distributed`` each rank runs
     the cases :func:`partition` gives it.  ``runner(cases)`` returns their
-    traces; the default is :func:`gpu_runner`.  Returns the traces in case
-    order on rank 0, None on the other ranks."""
+    traces; the default is :func:`gpu_runner` on ``device`` (by default
+    :func:`default_device`: each rank its own GPU).  Returns the traces in
+    case order on rank 0, None on the other ranks."""
     rank, world, _ = _dist(group)
+    device = default_device(group) if device is None else device
     mine = partition([_cost(c) for c in cases], world)[rank]
     run = runner or (lambda cs: gpu_runner(cs, device=device))
     traces = run([cases[q] for q in mine]) if mine else []
@@ -197,7 +212,7 @@ class CommonOffset:
     shots share the model's coefficient planes and run in one batched launch
     per rank."""
 
-    def __init__(self, grid, planes, profiles, srcfn, source_ijk, receiver_ijk, channel: str, device="cuda",
+    def __init__(self, grid, planes, profiles, srcfn, source_ijk, receiver_ijk, channel: str, device=None,
                  runner: Optional[Callable] = None, group=None):
         self.grid = grid
         self.planes = np.ascontiguousarray(planes, dtype=np.float64)
@@ -236,7 +251,7 @@ class CommonOffset:
 
 
 def survey_gradient(cases, residual_fn: Callable, grad_fn: Optional[Callable] = None, group=None,
-                    ckpt_every: int = 200, device="cuda") -> np.ndarray:
+                    ckpt_every: int = 200, device=None) -> np.ndarray:
     """Gradient of a misfit summed over the shots of one model with respect
     to its six planes: the sum over shots of the per-shot gradients, on every
     rank.  ``residual_fn(index, traces)`` gives dJ/d(traces) of shot
@@ -244,8 +259,9 @@ def survey_gradient(cases, residual_fn: Callable, grad_fn: Optional[Callable] = 
     that shot's (6, NZ, NX) gradient -- the default runs the forward and the
     checkpointed adjoint of :class:`seidart_gb300.adjoint.TraceModel`
     (electromag2).  Each rank adds up its own shots; one all-reduce adds the
-    ranks' sums."""
+    ranks' sums.  ``device`` defaults to :func:`default_device`."""
     rank, world, _ = _dist(group)
+    device = default_device(group) if device is None else device
     mine = partition([_cost(c) for c in cases], world)[rank]
     g = None
     for q in mine:

@@ -73,3 +73,16 @@ def test_create_rejects_null_buffer(L):
     h = C.c_void_p()
     rc = L.sfd_create(C.byref(_cfg()), None, 0, None, C.byref(h))
     assert rc == _lib.SFD_ERR_BAD_ARG and not h.value
+
+
+def test_library_sources_never_allocate_device_memory():
+    """The library allocates no device memory (callers pass every buffer; the
+    allocation-free entry point relies on it): no CUDA allocation or free call
+    appears in its sources outside comments."""
+    import re
+    csrc = Path(__file__).resolve().parent.parent / "seidart_gb300" / "csrc"
+    pat = re.compile(r"\b(cudaMalloc\w*|cudaFree\w*|cuMemAlloc\w*|cuMemFree\w*)\s*\(")
+    for f in sorted(csrc.glob("*.c*")) + sorted(csrc.glob("*.h")):
+        code = re.sub(r"//[^\n]*|/\*.*?\*/", "", f.read_text(), flags=re.S)
+        hits = pat.findall(code)
+        assert not hits, f"{f.name} calls {hits}"

@@ -79,6 +79,13 @@ def _worker(rank, world, port, outdir, what):
             base, src, rec = _co_args()
             res = survey.CommonOffset(base.grid, base.planes, base.profiles, base.srcfn, src, rec, "Ez",
                                       runner=oracle_runner).co_run()
+        elif what == "device":
+            # one process per GPU: each rank's default shot runner gets cuda:{LOCAL_RANK}
+            os.environ["LOCAL_RANK"] = str(rank)
+            seen = []
+            survey.gpu_runner = lambda cases, device=None: (seen.append(device), oracle_runner(cases))[1]
+            survey.run_survey(_survey_cases())
+            res = (survey.default_device(), seen)
         else:
             res = survey.survey_gradient(_shots(3), _residual, grad_fn=_numpy_grad)
         with open(os.path.join(outdir, f"{what}_{rank}.pkl"), "wb") as f:
@@ -142,6 +149,18 @@ def test_two_rank_common_offset_image(tmp_path):
                      [1][:, 1, 0] for s, r in zip(src, rec)], axis=1)
     assert res[0].shape == (base.nstep, len(src))
     assert np.array_equal(res[0], want)
+
+
+def test_two_rank_default_device_follows_local_rank(tmp_path):
+    res = _spawn("device", tmp_path)
+    for rank, (dev, seen) in enumerate(res):
+        assert dev == f"cuda:{rank}"
+        assert seen == [f"cuda:{rank}"]
+
+
+def test_single_process_default_device_is_the_current_one(monkeypatch):
+    monkeypatch.setenv("LOCAL_RANK", "3")  # no process group: the current device
+    assert survey.default_device() == "cuda"
 
 
 def test_two_rank_gradient_is_the_sum_over_shots(tmp_path):

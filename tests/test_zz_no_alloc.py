@@ -15,17 +15,17 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from helpers import make_solver, rel_l2
+from helpers import make_solver, rel_l2, run_oracle
 from seidart_gb300 import ELECTROMAG2, _lib, cpml as cp, synthetic as sy
 from seidart_gb300._lib import SfdConfig
 
 pytestmark = pytest.mark.gpu
 
 
-def _static_run(L, case):
+def _static_run(L, case, flags=0):
     g = case.grid
     cfg = SfdConfig(kind=ELECTROMAG2, nx=g.nx, ny=1, nz=g.nz, npml=g.npml, nstep=case.nstep,
-                    nrec=len(case.rec_ijk), flags=0, dx=g.dx, dy=g.dy, dz=g.dz, dt=g.dt)
+                    nrec=len(case.rec_ijk), flags=flags, dx=g.dx, dy=g.dy, dz=g.dz, dt=g.dt)
     model = np.ascontiguousarray(case.planes, dtype=np.float64)
     prof = cp.pack_profiles(case.profiles)
     src = np.ascontiguousarray(case.srcfn, dtype=np.float64)
@@ -53,6 +53,36 @@ def test_static_entry_point_matches_handle_entry_point(gpu):
             ref = s.traces()
         assert np.all(np.isfinite(tr))
         assert rel_l2(tr, ref) <= 1e-5
+        assert rel_l2(tr, run_oracle(case)[1]) <= 1e-5
+
+
+def test_static_entry_point_takes_no_device_memory(gpu):
+    """After a first call (which loads the library's module and its array),
+    a call leaves the device's free memory unchanged: it allocates nothing."""
+    import torch
+    L = _lib.lib()
+    case = sy.small_case(ELECTROMAG2, seed=63, nx=50, nz=42, npml=6, nstep=80, nrec=5)
+    rc, _ = _static_run(L, case)
+    assert rc == 0, L.sfd_last_error().decode()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    rc, tr = _static_run(L, case)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert rc == 0, L.sfd_last_error().decode()
+    assert free1 == free0
+    assert rel_l2(tr, run_oracle(case)[1]) <= 1e-5
+
+
+def test_static_entry_point_rejects_other_forms(gpu):
+    L = _lib.lib()
+    case = sy.small_case(ELECTROMAG2, seed=64, nx=40, nz=36, npml=5, nstep=20, nrec=3)
+    for flags in (2, 4, 1 << 20):
+        rc, _ = _static_run(L, case, flags=flags)
+        assert rc == _lib.SFD_ERR_BAD_ARG
+        assert "two-pass" in L.sfd_last_error().decode()
+    rc, _ = _static_run(L, case, flags=1)  # the form it runs, named explicitly
+    assert rc == 0, L.sfd_last_error().decode()
 
 
 def test_static_entry_point_rejects_oversized_state(gpu):
