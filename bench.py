@@ -172,10 +172,12 @@ def seis25_bytes(grid, atten=True):
 
 def make_solver(case, device):
     from seidart_gb300.solver import FDTDSolver
-    s = FDTDSolver(case.grid, case.nstep, len(case.rec_ijk), device=device)
+    s = FDTDSolver(case.grid, case.nstep, len(case.rec_ijk), device=device, **case.solver_options())
     s.set_model(case.planes)
     s.set_cpml(case.profiles)
     s.set_source(case.src_ijk, case.srcfn)
+    if case.stress_srcfn is not None:
+        s.set_stress_source(case.src_ijk, case.stress_srcfn)
     s.set_receivers(case.rec_ijk)
     return s
 
@@ -288,12 +290,14 @@ def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000, 
         parity = {}
         t0 = time.perf_counter()
         for q in picks:
-            st, ref = par.oracle_case(cases[q])
-            r = par.compare_run(batched_traces[q], fields[q], st, ref, FIELDS[cases[q].grid.kind])
-            parity[cases[q].name] = {"rel_l2_traces": r["rel_l2_traces"], "rel_l2_fields_max": r["rel_l2_fields_max"]}
+            st, ref, peaks = par.oracle_case_peaks(cases[q])
+            r = par.compare_run(batched_traces[q], fields[q], st, ref, FIELDS[cases[q].grid.kind], peaks)
+            parity[cases[q].name] = {k: r[k] for k in ("rel_l2_traces", "rel_l2_fields_max",
+                                                        "fields_err_vs_peak_norm_max")}
         parity = {"models": parity, "steps": nstep,
                   "rel_l2_traces_max": max(v["rel_l2_traces"] for v in parity.values()),
                   "rel_l2_fields_max": max(v["rel_l2_fields_max"] for v in parity.values()),
+                  "fields_err_vs_peak_norm_max": max(v["fields_err_vs_peak_norm_max"] for v in parity.values()),
                   "oracle_s": round(time.perf_counter() - t0, 1)}
     for s in solvers:
         s.reset()
@@ -433,6 +437,7 @@ def adjoint_fd_check(case, base, cur, grads, ncells, seed=7, h_rel=1e-4):
 def parity_plain(case, device, nsteps=None):
     """The default GPU path of ``case`` (the form the bench times) against the
     FP64 oracle over ``nsteps`` steps from rest: traces and final fields."""
+    from seidart_gb300 import SEISMIC2, SEISMIC25
     from oracle import parity as par
     from seidart_gb300.solver import FIELDS
     n = case.nstep if nsteps is None else int(nsteps)
@@ -445,10 +450,13 @@ def parity_plain(case, device, nsteps=None):
     fields = [s.field(nm) for nm in names]
     s.close()
     t0 = time.perf_counter()
-    st, ref = par.oracle_case(case, n)
+    st, ref, peaks = par.oracle_case_peaks(case, n)
     out = {"workload": f"{case.name}: {case.grid.cells} cells", "steps": n, "of_steps": case.nstep,
-           "form": "on chip" if tiles else "one launch per step"}
-    out.update(par.compare_run(tr, fields, st, ref, names))
+           "form": "on chip" if tiles else "one launch per step",
+           "physics": {"legacy_quirks": case.legacy, "density": case.density,
+                       "source": "stress (explosive)" if case.stress_srcfn is not None else "force"}
+           if case.grid.kind in (SEISMIC2, SEISMIC25) else None}
+    out.update(par.compare_run(tr, fields, st, ref, names, peaks))
     out["oracle_s"] = round(time.perf_counter() - t0, 1)
     return out
 

@@ -70,6 +70,29 @@ extern "C" {
                                when the grid fits on chip (by default a run of
                                a grid that fits in the SMs' shared memory is
                                one launch with the state held on chip) */
+/* Seismic kinds: reproduce the legacy Fortran loops' quirks instead of the
+ * default corrected physics.
+ *   seismic2: the two stress loops share their four velocity-gradient CPML
+ *     memory variables, which so advance twice per step where both loops
+ *     visit a cell (seismicfdtd.f95:255-262, 291-298); loop 1 reads
+ *     b_x_half at the z index (:255); vx divides by the cell's own rho (:334)
+ *     although :320 forms the averaged density.  Corrected: the sigmaxz loop
+ *     keeps its own four memory variables, b_x_half(i), and vx divides by
+ *     the average of :320.
+ *   seismic25: the coefficient pairs c16 (dvx_dy + dvz_dy) (:657) and
+ *     c45 (dvx_dz + dvz_dx) (:766).  Corrected: the Voigt pairs c16 (dvx_dy +
+ *     dvy_dx) and c45 (dvy_dz + dvz_dy). */
+#define SFD_FLAG_LEGACY_QUIRKS 4
+/* Seismic kinds: averaging of the density at the staggered velocity points
+ * (the driver's density_method argument, src/seidart/routines/classes.py:311,
+ * 910-924), a two-bit field.  0 (no flag) = arithmetic, the Fortran's
+ * averages (seismicfdtd.f95:320, 342, 825, 850, 876); NONE = the cell's own
+ * density; GEOMETRIC and HARMONIC = the weighted geometric and harmonic means
+ * over the same stencil (weights 2,1,1 in 2-D, 4,1,1 in 2.5-D). */
+#define SFD_FLAG_DENSITY_NONE 8
+#define SFD_FLAG_DENSITY_GEOMETRIC 16
+#define SFD_FLAG_DENSITY_HARMONIC 24
+#define SFD_FLAG_DENSITY_MASK 24
 
 
 typedef struct sfd_config {
@@ -119,7 +142,10 @@ int32_t sfd_model_planes(int32_t kind);
  *                 (memory variables likewise in real/imaginary pairs) */
 int32_t sfd_num_fields(int32_t kind);
 int32_t sfd_num_channels(int32_t kind);
-/* Number of CPML memory variables (the Fortran memory_* arrays). */
+/* Number of CPML memory variables (the Fortran memory_* arrays).  SEISMIC2
+ * has 12: dvx_dx dvz_dz dvx_dz dvz_dx dsigmaxx_dx dsigmazz_dz dsigmaxz_dx
+ * dsigmaxz_dz, then the sigmaxz loop's own dvx_dx dvz_dz dvx_dz dvz_dx
+ * (corrected physics; zero with SFD_FLAG_LEGACY_QUIRKS). */
 int32_t sfd_num_memory(int32_t kind);
 
 /* Bytes of device memory a handle of this configuration needs. */
@@ -165,6 +191,18 @@ int32_t sfd_set_cpml(sfd_handle* h, const double* profiles, int64_t count);
  * (:581-582).  Requires the model. */
 int32_t sfd_set_source(sfd_handle* h, int32_t i, int32_t j, int32_t k, const double* srcfn,
                        int32_t ncomp, int32_t nstep);
+
+/* Seismic kinds: a moment-tensor (stress) source at full-grid cell (i, j, k),
+ * the same cell as the force source when both are set.  srcfn, host FP64,
+ * ncomp x nstep values, component-major: sigma xx, zz, xz in 2-D (ncomp 3);
+ * xx, yy, zz, xy, xz, yz in 2.5-D (ncomp 6).  After the stress half-step of
+ * step t, sigma_ij(i, j, k) += srcfn[ij][t] * dt; an explosive source is equal
+ * normal components and zero shear.  ncomp = 0 removes the stress source.
+ * Replaces the seismicsource{xx,yy,zz,xy,xz,yz}.dat files the driver writes
+ * (src/seidart/routines/sourcefunction.py:354-372), which the legacy Fortran
+ * never reads. */
+int32_t sfd_set_stress_source(sfd_handle* h, int32_t i, int32_t j, int32_t k, const double* srcfn, int32_t ncomp,
+                              int32_t nstep);
 
 /* Make dst read src's update coefficients instead of its own (no copy): the
  * shots of one survey share one model.  Same kind, grid, dt and flags

@@ -28,7 +28,10 @@ LIB_NATIVE = HERE / "liboracle_native.so"
 NATIVE_FLAGS = "g++ -O3 -fopenmp " + ("-mcpu=native" if os.uname().machine == "aarch64" else "-march=native")
 SEISMIC2, SEISMIC25, ELECTROMAG2, ELECTROMAG25, ELECTROMAG2C = 1, 2, 3, 4, 5
 NFIELDS = {SEISMIC2: 5, SEISMIC25: 9, ELECTROMAG2: 3, ELECTROMAG25: 6, ELECTROMAG2C: 6}
-NMEM = {SEISMIC2: 8, SEISMIC25: 18, ELECTROMAG2: 4, ELECTROMAG25: 12, ELECTROMAG2C: 8}
+NMEM = {SEISMIC2: 12, SEISMIC25: 18, ELECTROMAG2: 4, ELECTROMAG25: 12, ELECTROMAG2C: 8}
+# density_method values of the driver (src/seidart/routines/classes.py:311) -> oracle option bits
+DENSITY = {"arithmetic": 0, "none": 1, "geometric": 2, "harmonic": 3}
+NSTRESS = {SEISMIC2: 3, SEISMIC25: 6}  # stress source components (xx zz xz | xx yy zz xy xz yz)
 NCH = {SEISMIC2: 2, SEISMIC25: 3, ELECTROMAG2: 2, ELECTROMAG25: 3, ELECTROMAG2C: 4}
 
 _lock = threading.Lock()
@@ -54,9 +57,9 @@ def lib(native: bool = False):
             common_tail = [dp, dp, i, i, dp, i, i, i, dp, dp, i, ip, dp, dp, ip]
             L.orc_electromag2.argtypes = [i, i, d, d, d] + common_tail
             L.orc_electromag2c.argtypes = [i, i, d, d, d] + common_tail
-            L.orc_seismic2.argtypes = [i, i, d, d, d] + common_tail
+            L.orc_seismic2.argtypes = [i, i, d, d, d] + common_tail + [i, dp]
             tail3 = [dp, dp, i, i, i, dp, i, i, i, dp, dp, i, ip, dp, dp, ip]
-            L.orc_seismic25.argtypes = [i, i, i, d, d, d, d] + tail3
+            L.orc_seismic25.argtypes = [i, i, i, d, d, d, d] + tail3 + [i, dp]
             L.orc_electromag25.argtypes = [i, i, i, d, d, d, d] + tail3
             for f in (L.orc_electromag2, L.orc_electromag2c, L.orc_seismic2, L.orc_seismic25, L.orc_electromag25):
                 f.restype = C.c_int
@@ -84,11 +87,21 @@ def _d(a):
 
 
 def run(kind, grid, planes, packed_profiles, src_ijk, srcfn, rec_ijk, nsteps, state: OracleState = None,
-        native: bool = False):
+        native: bool = False, legacy: bool = False, density: str = "arithmetic", stress_src=None):
     """Advance ``nsteps`` steps of the FP64 oracle.  Returns (state, traces,
     maxnorm, blew_up); traces is (nsteps, nch, nrec).  ``native`` runs the
-    host-tuned build (timing only)."""
+    host-tuned build (timing only).  Seismic kinds: ``legacy`` keeps the
+    legacy Fortran's quirks (default: corrected physics), ``density`` is the
+    density method ('arithmetic', 'none', 'geometric', 'harmonic') and
+    ``stress_src`` the stress source time functions (NSTRESS[kind] x nstep,
+    same cell as the force source) or None."""
     L = lib(native)
+    opts = (1 if legacy else 0) | (DENSITY[density] << 1)
+    ssrc = None
+    if stress_src is not None:
+        ssrc = np.ascontiguousarray(stress_src, dtype=np.float64)
+        if kind not in NSTRESS or ssrc.shape != (NSTRESS[kind], np.asarray(srcfn).shape[1]):
+            raise ValueError("stress_src must be (3 | 6, nstep) for seismic2 | seismic25")
     three = kind in (SEISMIC25, ELECTROMAG25)
     shape = (grid.nz, grid.ny, grid.nx) if three else (grid.nz, grid.nx)
     if state is None:
@@ -114,11 +127,13 @@ def run(kind, grid, planes, packed_profiles, src_ijk, srcfn, rec_ijk, nsteps, st
     elif kind == SEISMIC2:
         n = L.orc_seismic2(grid.nx, grid.nz, grid.dx, grid.dz, grid.dt, _d(prof), _d(planes), i, k, _d(srcfn),
                            srcfn.shape[1], state.step, nsteps, _d(state.fields), _d(state.memory), nrec, recp,
-                           _d(traces), C.byref(maxnorm), C.byref(blew))
+                           _d(traces), C.byref(maxnorm), C.byref(blew), opts,
+                           _d(ssrc) if ssrc is not None else None)
     elif kind == SEISMIC25:
         n = L.orc_seismic25(grid.nx, grid.ny, grid.nz, grid.dx, grid.dy, grid.dz, grid.dt, _d(prof), _d(planes),
                             i, j, k, _d(srcfn), srcfn.shape[1], state.step, nsteps, _d(state.fields),
-                            _d(state.memory), nrec, recp, _d(traces), C.byref(maxnorm), C.byref(blew))
+                            _d(state.memory), nrec, recp, _d(traces), C.byref(maxnorm), C.byref(blew), opts,
+                            _d(ssrc) if ssrc is not None else None)
     elif kind == ELECTROMAG25:
         n = L.orc_electromag25(grid.nx, grid.ny, grid.nz, grid.dx, grid.dy, grid.dz, grid.dt, _d(prof), _d(planes),
                                i, j, k, _d(srcfn), srcfn.shape[1], state.step, nsteps, _d(state.fields),

@@ -63,6 +63,21 @@ static void unpack_axes(const double* prof, int nx, int ny, int nz, bool three, 
   take(z, nz);
 }
 
+// Density at a staggered velocity point, from the cell's own value r and the
+// two neighbours a, b of the Fortran's deltarho stencil, weights (w, 1, 1):
+// w = 2 in seismic2 (seismicfdtd.f95:342), w = 4 in seismic25 (:825, :850,
+// :876).  method: 0 arithmetic (the Fortran's average), 1 none (r itself),
+// 2 geometric, 3 harmonic (the density_method values the driver passes,
+// src/seidart/routines/classes.py:311, 910-924).
+static double rho_avg(int method, double w, double r, double a, double b) {
+  switch (method) {
+    case 1: return r;
+    case 2: return w == 2.0 ? std::sqrt(std::sqrt(r * r * a * b)) : std::cbrt(std::sqrt(r * r * r * r * a * b));
+    case 3: return (w + 2.0) / (w / r + 1.0 / a + 1.0 / b);
+  }
+  return (w * r + a + b) / (w + 2.0);
+}
+
 }  // namespace
 
 extern "C" {
@@ -308,21 +323,32 @@ int orc_electromag2c(int NX, int NZ, double dx, double dz, double dt,
 //   mat   = c11, c13, c15, c33, c35, c55, rho, gamma_x, gamma_z  (9 x NX*NZ)
 //   fld   = vx, vz, sigmaxx, sigmazz, sigmaxz                     (5 x NX*NZ)
 //   mem   = dvx_dx, dvz_dz, dvx_dz, dvz_dx,
-//           dsigmaxx_dx, dsigmazz_dz, dsigmaxz_dx, dsigmaxz_dz    (8 x NX*NZ)
+//           dsigmaxx_dx, dsigmazz_dz, dsigmaxz_dx, dsigmaxz_dz,
+//           dvx_dx, dvz_dz, dvx_dz, dvz_dx of the sigmaxz loop     (12 x NX*NZ)
 //   src   = srcx, srcz; chans = vx, vz
-// The four velocity-gradient memory variables are shared by both stress loops
-// and so advance twice per step where the loops overlap (:255-262, :291-298),
-// and the first stress loop indexes b_x_half by the z index (:255); where
-// that index runs past the x axis (NZ > NX) the interior value 0 of the
-// profile writer is used.  gamma_x and gamma_z are taken as given (the legacy
-// file-loading slip of :158-159 belongs to the file reader, not the stencil).
+//   ssrc  = stress source sxx, szz, sxz (3 x nstep_src) or NULL
+//   opts  = bit 0: legacy quirks; bits 1-2: density method (rho_avg)
+// With the legacy quirks (opts bit 0) the loops are the Fortran's as written:
+//   Q2  the four velocity-gradient memory variables are shared by both stress
+//       loops, so they advance twice per step where the loops overlap
+//       (:255-262, :291-298); the last four memory arrays stay unused;
+//   Q3  the first stress loop indexes b_x_half by the z index (:255); where
+//       that index runs past the x axis (NZ > NX) the interior value 0 of the
+//       profile writer is used;
+//   vx divides by the cell's own rho (:334) although :320 forms the average.
+// Without (the default, corrected physics): the sigmaxz loop keeps its own
+// four memory variables (each advances once per step), b_x_half(i), and vx
+// divides by the average of :320.  The density method applies to the vz
+// average (:342) in both modes and to the vx average when it is used.
+// gamma_x and gamma_z are taken as given (the legacy file-loading slip of
+// :158-159 belongs to the file reader, not the stencil).
 int orc_seismic2(int NX, int NZ, double dx, double dz, double dt,
                  const double* prof, const double* mat,
                  int isrc, int ksrc, const double* src, int nstep_src,
                  int it0, int nsteps,
                  double* fld, double* mem,
                  int nrec, const int* rec, double* traces,
-                 double* maxnorm, int* blew_up) {
+                 double* maxnorm, int* blew_up, int opts, const double* ssrc) {
   const size_t N = (size_t)NX * NZ;
   Axis X, Y, Z;
   unpack_axes(prof, NX, 1, NZ, false, &X, &Y, &Z);
@@ -332,6 +358,12 @@ int orc_seismic2(int NX, int NZ, double dx, double dz, double dt,
   double *vx = fld, *vz = fld + N, *sxx = fld + 2 * N, *szz = fld + 3 * N, *sxz = fld + 4 * N;
   double *m_vxx = mem, *m_vzz = mem + N, *m_vxz = mem + 2 * N, *m_vzx = mem + 3 * N;
   double *m_sxx_x = mem + 4 * N, *m_szz_z = mem + 5 * N, *m_sxz_x = mem + 6 * N, *m_sxz_z = mem + 7 * N;
+  const bool legacy = opts & 1;
+  const int dens = (opts >> 1) & 3;
+  // the sigmaxz loop's own velocity-gradient memory (corrected physics); the
+  // legacy loops share the first four arrays
+  double *m2_vxx = legacy ? m_vxx : mem + 8 * N, *m2_vzz = legacy ? m_vzz : mem + 9 * N;
+  double *m2_vxz = legacy ? m_vxz : mem + 10 * N, *m2_vzx = legacy ? m_vzx : mem + 11 * N;
   auto I = [NX](int i, int k) { return (size_t)i + (size_t)NX * k; };
   const double* srcx = src;
   const double* srcz = src + nstep_src;
@@ -349,8 +381,9 @@ int orc_seismic2(int NX, int NZ, double dx, double dz, double dt,
         double dvz_dz = (vz[c] - vz[czm]) / dz;
         double dvz_dx = (vz[cxp] - vz[c]) / dx;
         double dvx_dz = (vx[c] - vx[czm]) / dz;
-        const double bxh_k = (k < NX) ? X.bh[k] : 0.0;  // b_x_half(j), :255
-        m_vxx[c] = bxh_k * m_vxx[c] + X.ah[i] * dvx_dx;
+        // legacy: b_x_half(j), :255 (0 past the x axis); corrected: b_x_half(i)
+        const double bxh = legacy ? ((k < NX) ? X.bh[k] : 0.0) : X.bh[i];
+        m_vxx[c] = bxh * m_vxx[c] + X.ah[i] * dvx_dx;
         m_vzz[c] = Z.b[k] * m_vzz[c] + Z.a[k] * dvz_dz;
         m_vxz[c] = Z.bh[k] * m_vxz[c] + Z.ah[k] * dvx_dz;
         m_vzx[c] = X.b[i] * m_vzx[c] + X.a[i] * dvz_dx;
@@ -365,7 +398,8 @@ int orc_seismic2(int NX, int NZ, double dx, double dz, double dt,
                            ((c33[cxp] + 2 * c33[c] + c33[czm]) / 4) * dvz_dz +
                            ((c35[cxp] + 2 * c35[c] + c35[czm]) / 4) * (dvz_dx + dvx_dz)) * dt;
       }
-    // sigmaxz, :283-312 (same memory arrays again).
+    // sigmaxz, :283-312: legacy, the same memory arrays again (each advances
+    // twice where both loops visit a cell); corrected, its own arrays.
 #pragma omp parallel for schedule(static)
     for (int k = 0; k <= NZ - 2; ++k)
       for (int i = 1; i <= NX - 1; ++i) {
@@ -374,18 +408,26 @@ int orc_seismic2(int NX, int NZ, double dx, double dz, double dt,
         double dvz_dz = (vz[czp] - vz[c]) / dz;
         double dvz_dx = (vz[c] - vz[cxm]) / dx;
         double dvx_dz = (vx[czp] - vx[c]) / dz;
-        m_vxx[c] = X.bh[i] * m_vxx[c] + X.ah[i] * dvx_dx;
-        m_vzz[c] = Z.b[k] * m_vzz[c] + Z.a[k] * dvz_dz;
-        m_vxz[c] = Z.bh[k] * m_vxz[c] + Z.ah[k] * dvx_dz;
-        m_vzx[c] = X.b[i] * m_vzx[c] + X.a[i] * dvz_dx;
-        dvx_dx = dvx_dx / X.Kh[i] + m_vxx[c];
-        dvz_dz = dvz_dz / Z.K[k] + m_vzz[c];
-        dvz_dx = dvz_dx / X.K[i] + m_vzx[c];
-        dvx_dz = dvx_dz / Z.Kh[k] + m_vxz[c];
+        m2_vxx[c] = X.bh[i] * m2_vxx[c] + X.ah[i] * dvx_dx;
+        m2_vzz[c] = Z.b[k] * m2_vzz[c] + Z.a[k] * dvz_dz;
+        m2_vxz[c] = Z.bh[k] * m2_vxz[c] + Z.ah[k] * dvx_dz;
+        m2_vzx[c] = X.b[i] * m2_vzx[c] + X.a[i] * dvz_dx;
+        dvx_dx = dvx_dx / X.Kh[i] + m2_vxx[c];
+        dvz_dz = dvz_dz / Z.K[k] + m2_vzz[c];
+        dvz_dx = dvz_dx / X.K[i] + m2_vzx[c];
+        dvx_dz = dvx_dz / Z.Kh[k] + m2_vxz[c];
         sxz[c] = sxz[c] + (((c15[czp] + 2 * c15[c] + c15[cxm]) / 4) * dvx_dx +
                            ((c35[czp] + 2 * c35[c] + c35[cxm]) / 4) * dvz_dz +
                            ((c55[czp] + 2 * c55[c] + c55[cxm]) / 4) * (dvz_dx + dvx_dz)) * dt;
       }
+    // Stress source (moment tensor; explosive = equal normal components):
+    // sigma_ij += f_ij(t) dt at the source cell, after both stress loops.
+    if (ssrc) {
+      const size_t c = I(isrc, ksrc);
+      sxx[c] += ssrc[t] * dt;
+      szz[c] += ssrc[nstep_src + t] * dt;
+      sxz[c] += ssrc[2 * (size_t)nstep_src + t] * dt;
+    }
     // vx, :317-336.
 #pragma omp parallel for schedule(static)
     for (int k = 1; k <= NZ - 1; ++k)
@@ -397,14 +439,17 @@ int orc_seismic2(int NX, int NZ, double dx, double dz, double dt,
         m_sxz_z[c] = Z.b[k] * m_sxz_z[c] + Z.a[k] * dsxz_dz;
         dsxx_dx = dsxx_dx / X.K[i] + m_sxx_x[c];
         dsxz_dz = dsxz_dz / Z.K[k] + m_sxz_z[c];
-        vx[c] = vx[c] * (1 - gx[c]) + (dsxx_dx + dsxz_dz) * dt / rho[c];
+        // legacy: the cell's own rho (:334; the average of :320 is unused);
+        // corrected: the average of :320 by the density method
+        const double rx = legacy ? rho[c] : rho_avg(dens, 2.0, rho[c], rho[I(i - 1, k)], rho[I(i, k - 1)]);
+        vx[c] = vx[c] * (1 - gx[c]) + (dsxx_dx + dsxz_dz) * dt / rx;
       }
     // vz, :338-357.
 #pragma omp parallel for schedule(static)
     for (int k = 0; k <= NZ - 2; ++k)
       for (int i = 0; i <= NX - 2; ++i) {
         const size_t c = I(i, k);
-        const double deltarho = (2 * rho[c] + rho[I(i + 1, k)] + rho[I(i, k + 1)]) / 4;
+        const double deltarho = rho_avg(dens, 2.0, rho[c], rho[I(i + 1, k)], rho[I(i, k + 1)]);  // :342
         double dsxz_dx = (sxz[I(i + 1, k)] - sxz[c]) / dx;
         double dszz_dz = (szz[I(i, k + 1)] - szz[c]) / dz;
         m_sxz_x[c] = X.bh[i] * m_sxz_x[c] + X.ah[i] * dsxz_dx;
@@ -447,10 +492,15 @@ int orc_seismic2(int NX, int NZ, double dx, double dz, double dt,
 //         dsxx_dx dsyy_dy dszz_dz dsxy_dx dsxy_dy dsxz_dx dsxz_dz
 //         dsyz_dy dsyz_dz                                        (18 x NX*NY*NZ)
 //   src = srcx srcy srcz; chans = vx vy vz
+//   ssrc = stress source sxx syy szz sxy sxz syz (6 x nstep_src) or NULL
+//   opts = bit 0: legacy quirks; bits 1-2: density method (rho_avg)
 // The nine velocity-gradient memory variables are shared by the four stress
-// loops and advance once per loop (:630-638, :691-699, :750-758, :795-803).
-// The coefficient pairs of :657 (c16) and :766 (c45) and the two derivatives
-// that :701-707 leave unscaled are kept as written.  Attenuation: the legacy
+// loops and advance once per loop (:630-638, :691-699, :750-758, :795-803),
+// and the two derivatives that :701-707 leave unscaled stay so, in both
+// modes.  Q4: with the legacy quirks the coefficient pairs of :657
+// (c16 (dvx_dy + dvz_dy)) and :766 (c45 (dvx_dz + dvz_dx)) are kept as
+// written; without (the default) they are the Voigt pairs c16 (dvx_dy +
+// dvy_dx) and c45 (dvy_dz + dvz_dy).  Attenuation: the legacy
 // routine has none; v <- v (1 - gamma) + ... with y-invariant gamma, as in
 // seismic2 (:334, :355), is applied here and reduces to the legacy update
 // when gamma = 0.
@@ -460,9 +510,11 @@ int orc_seismic25(int NX, int NY, int NZ, double dx, double dy, double dz, doubl
                   int it0, int nsteps,
                   double* fld, double* mem,
                   int nrec, const int* rec, double* traces,
-                  double* maxnorm, int* blew_up) {
+                  double* maxnorm, int* blew_up, int opts, const double* ssrc) {
   const size_t N2 = (size_t)NX * NZ;
   const size_t N = (size_t)NX * NY * NZ;
+  const bool legacy = opts & 1;
+  const int dens = (opts >> 1) & 3;
   Axis X, Y, Z;
   unpack_axes(prof, NX, NY, NZ, true, &X, &Y, &Z);
   const double* C[21];
@@ -529,7 +581,7 @@ int orc_seismic25(int NX, int NY, int NZ, double dx, double dy, double dz, doubl
           auto A = [&](const double* cc) { return av4(cc, i + 1, k, i, k, i, k - 1, i + 1, k - 1); };
           sxx[c] = sxx[c] + ((A(c11) / 4) * dvx_dx + (A(c12) / 4) * dvy_dy + (A(c13) / 4) * dvz_dz +
                              (A(c14) / 8) * (dvy_dz + dvz_dy) + (A(c15) / 8) * (dvx_dz + dvz_dx) +
-                             (A(c16) / 8) * (dvx_dy + dvz_dy)) * dt;
+                             (A(c16) / 8) * (legacy ? dvx_dy + dvz_dy : dvx_dy + dvy_dx)) * dt;  // Q4, :657
           syy[c] = syy[c] + ((A(c12) / 4) * dvx_dx + (A(c22) / 4) * dvy_dy + (A(c23) / 4) * dvz_dz +
                              (A(c24) / 8) * (dvy_dz + dvz_dy) + (A(c25) / 8) * (dvx_dz + dvz_dx) +
                              (A(c26) / 8) * (dvy_dx + dvx_dy)) * dt;
@@ -608,8 +660,8 @@ int orc_seismic25(int NX, int NY, int NZ, double dx, double dy, double dz, doubl
           dvy_dz = dvy_dz / Z.Kh[k] + m_vy_z[c];
           auto A = [&](const double* cc) { return av4(cc, i, k + 1, i, k, i - 1, k, i - 1, k + 1); };
           sxz[c] = sxz[c] + ((A(c15) / 4) * dvx_dx + (A(c25) / 4) * dvy_dy + (A(c35) / 4) * dvz_dz +
-                             (A(c45) / 8) * (dvx_dz + dvz_dx) + (A(c55) / 8) * (dvx_dz + dvz_dx) +
-                             (A(c56) / 8) * (dvx_dy + dvy_dx)) * dt;
+                             (A(c45) / 8) * (legacy ? dvx_dz + dvz_dx : dvy_dz + dvz_dy) +  // Q4, :766
+                             (A(c55) / 8) * (dvx_dz + dvz_dx) + (A(c56) / 8) * (dvx_dy + dvy_dx)) * dt;
         }
       for (int j = 0; j <= NY - 2; ++j)
         for (int i = 0; i <= NX - 2; ++i) {
@@ -647,13 +699,20 @@ int orc_seismic25(int NX, int NY, int NZ, double dx, double dy, double dz, doubl
                              (A(c46) / 8) * (dvy_dx + dvx_dy)) * dt;
         }
     }
+    // Stress source (moment tensor; explosive = equal normal components):
+    // sigma_ij += f_ij(t) dt at the source cell, after the four stress loops.
+    if (ssrc) {
+      const size_t c = I(isrc, jsrc, ksrc);
+      double* S[6] = {sxx, syy, szz, sxy, sxz, syz};
+      for (int q = 0; q < 6; ++q) S[q][c] += ssrc[(size_t)q * nstep_src + t] * dt;
+    }
     // vx and vy, :821-870.
 #pragma omp parallel for schedule(static)
     for (int k = 1; k <= NZ - 1; ++k) {
       for (int j = 1; j <= NY - 1; ++j)
         for (int i = 1; i <= NX - 1; ++i) {
           const size_t c = I(i, j, k);
-          const double deltarho = (4 * rho[P(i, k)] + rho[P(i - 1, k)] + rho[P(i, k - 1)]) / 6;
+          const double deltarho = rho_avg(dens, 4.0, rho[P(i, k)], rho[P(i - 1, k)], rho[P(i, k - 1)]);  // :825
           double d1 = (sxx[c] - sxx[I(i - 1, j, k)]) / dx;
           double d2 = (sxy[c] - sxy[I(i, j - 1, k)]) / dy;
           double d3 = (sxz[c] - sxz[I(i, j, k - 1)]) / dz;
@@ -668,7 +727,7 @@ int orc_seismic25(int NX, int NY, int NZ, double dx, double dy, double dz, doubl
       for (int j = 0; j <= NY - 2; ++j)
         for (int i = 0; i <= NX - 2; ++i) {
           const size_t c = I(i, j, k);
-          const double deltarho = (4 * rho[P(i, k)] + rho[P(i + 1, k)] + rho[P(i, k - 1)]) / 6;
+          const double deltarho = rho_avg(dens, 4.0, rho[P(i, k)], rho[P(i + 1, k)], rho[P(i, k - 1)]);  // :850
           double d1 = (sxy[I(i + 1, j, k)] - sxy[c]) / dx;
           double d2 = (syy[I(i, j + 1, k)] - syy[c]) / dy;
           double d3 = (syz[c] - syz[I(i, j, k - 1)]) / dz;
@@ -687,7 +746,7 @@ int orc_seismic25(int NX, int NY, int NZ, double dx, double dy, double dz, doubl
       for (int j = 1; j <= NY - 1; ++j)
         for (int i = 0; i <= NX - 2; ++i) {
           const size_t c = I(i, j, k);
-          const double deltarho = (rho[P(i + 1, k)] + rho[P(i, k + 1)] + 4 * rho[P(i, k)]) / 6;
+          const double deltarho = rho_avg(dens, 4.0, rho[P(i, k)], rho[P(i + 1, k)], rho[P(i, k + 1)]);  // :876
           double d1 = (sxz[I(i + 1, j, k)] - sxz[c]) / dx;
           double d2 = (syz[c] - syz[I(i, j - 1, k)]) / dy;
           double d3 = (szz[I(i, j, k + 1)] - szz[c]) / dz;

@@ -83,19 +83,39 @@ def _em2(NX, NZ, dx, dz, dt, prof, eps11, eps13, eps33, sig11, sig13, sig33, src
     return np.stack([Ex, Ez, Hy]), np.stack([mExz, mEzx, mHyz, mHyx]), (np.stack(out) if out else None)
 
 
-def seismic2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None):
+def _rho_avg(method, w, r, a, b):
+    """Density at a staggered point, weights (w, 1, 1) (as rho_avg of fdtd_oracle.cpp)."""
+    if method == "none":
+        return r
+    if method == "geometric":
+        return np.sqrt(np.sqrt(r * r * a * b)) if w == 2 else np.cbrt(np.sqrt(r * r * r * r * a * b))
+    if method == "harmonic":
+        return (w + 2.0) / (w / r + 1.0 / a + 1.0 / b)
+    return (w * r + a + b) / (w + 2.0)
+
+
+def seismic2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None, legacy=False, density="arithmetic",
+             stress_src=None):
+    """legacy: the legacy quirks (shared velocity-gradient memory of the two
+    stress loops, b_x_half(j), vx over the cell's own rho); otherwise
+    corrected physics.  stress_src: (3, nstep) sxx, szz, sxz or None."""
     X, Z = _axes(prof, NX, NZ)
     c11, c13, c15, c33, c35, c55, rho, gx, gz = np.asarray(mat, dtype=np.float64)
     vx, vz, sxx, szz, sxz = (np.zeros((NZ, NX)) for _ in range(5))
     m_vxx, m_vzz, m_vxz, m_vzx, m_sxx, m_szz, m_sxzx, m_sxzz = (np.zeros((NZ, NX)) for _ in range(8))
+    n_vxx, n_vzz, n_vxz, n_vzx = (np.zeros((NZ, NX)) for _ in range(4))  # the sigmaxz loop's own
+    if legacy:
+        n_vxx, n_vzz, n_vxz, n_vzx = m_vxx, m_vzz, m_vxz, m_vzx
     si, sk = src_ik
     Kx, ax, bx, Kxh, axh, bxh = (X[q][None, :] for q in range(6))
     Kz, az, bz, Kzh, azh, bzh = (Z[q][:, None] for q in range(6))
-    # b_x_half read with the z index (seismicfdtd.f95:255); 0 past the x axis
-    q3 = np.zeros(NZ)
-    n = min(NX, NZ)
-    q3[:n] = X[5][:n]
-    q3 = q3[:, None]
+    if legacy:  # b_x_half read with the z index (seismicfdtd.f95:255); 0 past the x axis
+        q3 = np.zeros(NZ)
+        n = min(NX, NZ)
+        q3[:n] = X[5][:n]
+        q3 = q3[:, None]
+    else:
+        q3 = np.broadcast_to(bxh, (NZ, NX))
     out = []
     for t in range(nsteps):
         # loop 1: k in [1, NZ-1], i in [0, NX-2]
@@ -104,7 +124,7 @@ def seismic2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None):
         dvz_dz = (vz[1:, :-1] - vz[:-1, :-1]) / dz
         dvz_dx = (vz[1:, 1:] - vz[1:, :-1]) / dx
         dvx_dz = (vx[1:, :-1] - vx[:-1, :-1]) / dz
-        m_vxx[s1] = q3[1:] * m_vxx[s1] + axh[:, :-1] * dvx_dx
+        m_vxx[s1] = (q3[1:] if legacy else q3[1:, :-1]) * m_vxx[s1] + axh[:, :-1] * dvx_dx
         m_vzz[s1] = bz[1:] * m_vzz[s1] + az[1:] * dvz_dz
         m_vxz[s1] = bzh[1:] * m_vxz[s1] + azh[1:] * dvx_dz
         m_vzx[s1] = bx[:, :-1] * m_vzx[s1] + ax[:, :-1] * dvz_dx
@@ -121,16 +141,20 @@ def seismic2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None):
         dvz_dz = (vz[1:, 1:] - vz[:-1, 1:]) / dz
         dvz_dx = (vz[:-1, 1:] - vz[:-1, :-1]) / dx
         dvx_dz = (vx[1:, 1:] - vx[:-1, 1:]) / dz
-        m_vxx[s2] = bxh[:, 1:] * m_vxx[s2] + axh[:, 1:] * dvx_dx
-        m_vzz[s2] = bz[:-1] * m_vzz[s2] + az[:-1] * dvz_dz
-        m_vxz[s2] = bzh[:-1] * m_vxz[s2] + azh[:-1] * dvx_dz
-        m_vzx[s2] = bx[:, 1:] * m_vzx[s2] + ax[:, 1:] * dvz_dx
-        dvx_dx = dvx_dx / Kxh[:, 1:] + m_vxx[s2]
-        dvz_dz = dvz_dz / Kz[:-1] + m_vzz[s2]
-        dvz_dx = dvz_dx / Kx[:, 1:] + m_vzx[s2]
-        dvx_dz = dvx_dz / Kzh[:-1] + m_vxz[s2]
+        n_vxx[s2] = bxh[:, 1:] * n_vxx[s2] + axh[:, 1:] * dvx_dx
+        n_vzz[s2] = bz[:-1] * n_vzz[s2] + az[:-1] * dvz_dz
+        n_vxz[s2] = bzh[:-1] * n_vxz[s2] + azh[:-1] * dvx_dz
+        n_vzx[s2] = bx[:, 1:] * n_vzx[s2] + ax[:, 1:] * dvz_dx
+        dvx_dx = dvx_dx / Kxh[:, 1:] + n_vxx[s2]
+        dvz_dz = dvz_dz / Kz[:-1] + n_vzz[s2]
+        dvz_dx = dvz_dx / Kx[:, 1:] + n_vzx[s2]
+        dvx_dz = dvx_dz / Kzh[:-1] + n_vxz[s2]
         bv = lambda c: (c[1:, 1:] + 2 * c[:-1, 1:] + c[:-1, :-1]) / 4
         sxz[s2] = sxz[s2] + (bv(c15) * dvx_dx + bv(c35) * dvz_dz + bv(c55) * (dvz_dx + dvx_dz)) * dt
+        if stress_src is not None:
+            sxx[sk, si] += stress_src[0][t] * dt
+            szz[sk, si] += stress_src[1][t] * dt
+            sxz[sk, si] += stress_src[2][t] * dt
         # vx: k in [1, NZ-1], i in [1, NX-1]
         s3 = (slice(1, NZ), slice(1, NX))
         d1 = (sxx[1:, 1:] - sxx[1:, :-1]) / dx
@@ -139,10 +163,11 @@ def seismic2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None):
         m_sxzz[s3] = bz[1:] * m_sxzz[s3] + az[1:] * d2
         d1 = d1 / Kx[:, 1:] + m_sxx[s3]
         d2 = d2 / Kz[1:] + m_sxzz[s3]
-        vx[s3] = vx[s3] * (1 - gx[s3]) + (d1 + d2) * dt / rho[s3]
+        rx = rho[s3] if legacy else _rho_avg(density, 2, rho[s3], rho[1:, :-1], rho[:-1, 1:])
+        vx[s3] = vx[s3] * (1 - gx[s3]) + (d1 + d2) * dt / rx
         # vz: k in [0, NZ-2], i in [0, NX-2]
         s4 = (slice(0, NZ - 1), slice(0, NX - 1))
-        rbar = (2 * rho[s4] + rho[:-1, 1:] + rho[1:, :-1]) / 4
+        rbar = _rho_avg(density, 2, rho[s4], rho[:-1, 1:], rho[1:, :-1])
         d1 = (sxz[:-1, 1:] - sxz[:-1, :-1]) / dx
         d2 = (szz[1:, :-1] - szz[:-1, :-1]) / dz
         m_sxzx[s4] = bxh[:, :-1] * m_sxzx[s4] + axh[:, :-1] * d1
@@ -156,5 +181,7 @@ def seismic2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None):
             f[:, 0] = 0; f[:, NX - 1] = 0; f[0, :] = 0; f[NZ - 1, :] = 0
         if rec is not None:
             out.append(np.stack([vx[rec[:, 2], rec[:, 0]], vz[rec[:, 2], rec[:, 0]]]))
-    mem = np.stack([m_vxx, m_vzz, m_vxz, m_vzx, m_sxx, m_szz, m_sxzx, m_sxzz])
+    zero = np.zeros((NZ, NX))
+    second = [zero] * 4 if legacy else [n_vxx, n_vzz, n_vxz, n_vzx]
+    mem = np.stack([m_vxx, m_vzz, m_vxz, m_vzx, m_sxx, m_szz, m_sxzx, m_sxzz] + second)
     return np.stack([vx, vz, sxx, szz, sxz]), mem, (np.stack(out) if out else None)

@@ -307,15 +307,20 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
 
 struct S2Stress {
   float sxx, szz, sxz;
-  float mvxx, mvzx, mvzz, mvxz;
+  float mvxx, mvzx, mvzz, mvxz;  // velocity-gradient memory of the first stress loop (legacy: of both)
+  float nvxx, nvzx, nvzz, nvxz;  // the sigmaxz loop's own (corrected physics)
   bool xs, zs;
 };
 
-// The three stresses at (i, k) after both stress loops of one step, from the
-// old state (seismicfdtd.f95:247-312), with the shared velocity-gradient
-// memory variables advanced once per loop that visits the cell.
+// The three stresses at (i, k) after both stress loops of step t, from the
+// old state (seismicfdtd.f95:247-312).  Legacy quirks (a.legacy): the
+// velocity-gradient memory variables are shared by the two loops and so
+// advance once per loop that visits the cell, and loop 1 reads b_x_half at
+// the z index (:255, the q3 table).  Corrected physics: the sigmaxz loop has
+// its own four memory variables and loop 1 reads b_x_half(i).  A stress
+// source is added after both loops at the source cell.
 template <bool RO>
-__device__ __forceinline__ S2Stress seis2_stress_cell(const Seis2Step& a, int i, int k) {
+__device__ __forceinline__ S2Stress seis2_stress_cell(const Seis2Step& a, int i, int k, int t) {
   const int NX = a.NX, NZ = a.NZ, P = a.P, W = a.W;
   const int c = k * P + i;
   S2Stress o;
@@ -325,10 +330,20 @@ __device__ __forceinline__ S2Stress seis2_stress_cell(const Seis2Step& a, int i,
   o.xs = in_strip(i, NX, W);
   o.zs = in_strip(k, NZ, W);
   o.mvxx = o.mvzx = o.mvzz = o.mvxz = 0.f;
+  o.nvxx = o.nvzx = o.nvzz = o.nvxz = 0.f;
+  const bool own2 = !a.legacy;
   const int mx = k * (2 * W) + (o.xs ? strip_idx(i, NX, W) : 0);
   const int mz = (o.zs ? strip_idx(k, NZ, W) : 0) * P + i;
-  if (o.xs) { o.mvxx = fld<RO>(a.m_vxx0 + mx); o.mvzx = fld<RO>(a.m_vzx0 + mx); }
-  if (o.zs) { o.mvzz = fld<RO>(a.m_vzz0 + mz); o.mvxz = fld<RO>(a.m_vxz0 + mz); }
+  if (o.xs) {
+    o.mvxx = fld<RO>(a.m_vxx0 + mx);
+    o.mvzx = fld<RO>(a.m_vzx0 + mx);
+    if (own2) { o.nvxx = fld<RO>(a.m2_vxx0 + mx); o.nvzx = fld<RO>(a.m2_vzx0 + mx); }
+  }
+  if (o.zs) {
+    o.mvzz = fld<RO>(a.m_vzz0 + mz);
+    o.mvxz = fld<RO>(a.m_vxz0 + mz);
+    if (own2) { o.nvzz = fld<RO>(a.m2_vzz0 + mz); o.nvxz = fld<RO>(a.m2_vxz0 + mz); }
+  }
   const bool loop1 = (k >= 1) && (i <= NX - 2);
   const bool loop2 = (k <= NZ - 2) && (i >= 1);
   if (!loop1 && !loop2) return o;
@@ -341,7 +356,8 @@ __device__ __forceinline__ S2Stress seis2_stress_cell(const Seis2Step& a, int i,
     const float d_vz_x = fld<RO>(a.vz0 + c + 1) - vz0;
     const float d_vx_z = vx0 - fld<RO>(a.vx0 + c - P);
     if (o.xs) {
-      o.mvxx = __ldg(a.q3 + k) * o.mvxx + __ldg(a.X.adh + i) * d_vx_x;  // b_x_half(j), :255
+      const float bq = a.legacy ? __ldg(a.q3 + k) : __ldg(a.X.bh + i);  // b_x_half(j) as :255, or (i)
+      o.mvxx = bq * o.mvxx + __ldg(a.X.adh + i) * d_vx_x;
       o.mvzx = __ldg(a.X.b + i) * o.mvzx + __ldg(a.X.ad + i) * d_vz_x;
     }
     if (o.zs) {
@@ -363,20 +379,29 @@ __device__ __forceinline__ S2Stress seis2_stress_cell(const Seis2Step& a, int i,
     const float d_vz_z = fld<RO>(a.vz0 + c + P) - vz0;
     const float d_vz_x = vz0 - fld<RO>(a.vz0 + c - 1);
     const float d_vx_z = fld<RO>(a.vx0 + c + P) - vx0;
+    float mxx = own2 ? o.nvxx : o.mvxx, mzx = own2 ? o.nvzx : o.mvzx;
+    float mzz = own2 ? o.nvzz : o.mvzz, mxz = own2 ? o.nvxz : o.mvxz;
     if (o.xs) {
-      o.mvxx = __ldg(a.X.bh + i) * o.mvxx + __ldg(a.X.adh + i) * d_vx_x;
-      o.mvzx = __ldg(a.X.b + i) * o.mvzx + __ldg(a.X.ad + i) * d_vz_x;
+      mxx = __ldg(a.X.bh + i) * mxx + __ldg(a.X.adh + i) * d_vx_x;
+      mzx = __ldg(a.X.b + i) * mzx + __ldg(a.X.ad + i) * d_vz_x;
     }
     if (o.zs) {
-      o.mvzz = __ldg(a.Z.b + k) * o.mvzz + __ldg(a.Z.ad + k) * d_vz_z;
-      o.mvxz = __ldg(a.Z.bh + k) * o.mvxz + __ldg(a.Z.adh + k) * d_vx_z;
+      mzz = __ldg(a.Z.b + k) * mzz + __ldg(a.Z.ad + k) * d_vz_z;
+      mxz = __ldg(a.Z.bh + k) * mxz + __ldg(a.Z.adh + k) * d_vx_z;
     }
-    const float dvx_dx = d_vx_x * ikxh + o.mvxx;
-    const float dvz_dz = d_vz_z * ikz + o.mvzz;
-    const float dvz_dx = d_vz_x * ikx + o.mvzx;
-    const float dvx_dz = d_vx_z * ikzh + o.mvxz;
+    const float dvx_dx = d_vx_x * ikxh + mxx;
+    const float dvz_dz = d_vz_z * ikz + mzz;
+    const float dvz_dx = d_vz_x * ikx + mzx;
+    const float dvx_dz = d_vx_z * ikzh + mxz;
     o.sxz = o.sxz + (__ldg(a.B15 + c) * dvx_dx + __ldg(a.B35 + c) * dvz_dz +
                      __ldg(a.B55 + c) * (dvz_dx + dvx_dz));
+    if (own2) { o.nvxx = mxx; o.nvzx = mzx; o.nvzz = mzz; o.nvxz = mxz; }
+    else { o.mvxx = mxx; o.mvzx = mzx; o.mvzz = mzz; o.mvxz = mxz; }
+  }
+  if (a.io.ssrc && i == a.io.si && k == a.io.sk) {  // stress source: sigma_ij += f_ij(t) dt
+    o.sxx += __ldg(a.io.ssrc + t);
+    o.szz += __ldg(a.io.ssrc + a.io.nstep + t);
+    o.sxz += __ldg(a.io.ssrc + 2 * a.io.nstep + t);
   }
   return o;
 }
@@ -441,7 +466,7 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
     const int k = z0 + ty + 8 * r;
     if (i < NX && k < NZ) {
       const int c = k * P + i;
-      const S2Stress s = seis2_stress_cell<RO>(a, i, k);
+      const S2Stress s = seis2_stress_cell<RO>(a, i, k, t);
       a.sxx1[c] = s.sxx;
       a.szz1[c] = s.szz;
       a.sxz1[c] = s.sxz;
@@ -449,11 +474,13 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
         const int m = k * (2 * W) + strip_idx(i, NX, W);
         a.m_vxx1[m] = s.mvxx;
         a.m_vzx1[m] = s.mvzx;
+        if (!a.legacy) { a.m2_vxx1[m] = s.nvxx; a.m2_vzx1[m] = s.nvzx; }
       }
       if (s.zs) {
         const int m = strip_idx(k, NZ, W) * P + i;
         a.m_vzz1[m] = s.mvzz;
         a.m_vxz1[m] = s.mvxz;
+        if (!a.legacy) { a.m2_vzz1[m] = s.nvzz; a.m2_vxz1[m] = s.nvxz; }
       }
       sS[0][ty + 8 * r + 1][tx + 1] = s.sxx;
       sS[1][ty + 8 * r + 1][tx + 1] = s.szz;
@@ -471,7 +498,7 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
       else if (ty == 2) { hi = x0 - 1; hk = z0 + q; si = 0; sk = q + 1; }
       else { hi = x0 + 32; hk = z0 + q; si = 33; sk = q + 1; }
       if (hi >= 0 && hi < NX && hk >= 0 && hk < NZ) {
-        const S2Stress s = seis2_stress_cell<RO>(a, hi, hk);
+        const S2Stress s = seis2_stress_cell<RO>(a, hi, hk, t);
         sS[0][sk][si] = s.sxx;
         sS[1][sk][si] = s.szz;
         sS[2][sk][si] = s.sxz;

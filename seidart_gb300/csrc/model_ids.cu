@@ -77,7 +77,7 @@ __global__ void em2_coef_from_ids(const int* __restrict__ ids, MatTable m, int N
 // and (c(i,k+1) + 2 c(i,k) + c(i-1,k))/4 times dt, dt/rho, the averaged
 // dt/rho of the vz points (:341, :355) and 1 - gamma.
 __global__ void seis2_coef_from_ids(const int* __restrict__ ids, MatTable m, int NX, int NZ, int P, double dt,
-                                    float* coef, size_t plane, int* bad) {
+                                    float* coef, size_t plane, int* bad, int dens, int legacy) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= NX || k >= NZ) return;
   const size_t n = (size_t)k * NX + i, c = (size_t)k * P + i;
@@ -104,9 +104,13 @@ __global__ void seis2_coef_from_ids(const int* __restrict__ ids, MatTable m, int
         out[5 + q] = (float)((val(d, B_src[q]) + 2 * val(id, B_src[q]) + val(l, B_src[q])) / 4 * dt);
     }
     const double rho = val(id, 6);
-    out[8] = (float)(dt / rho);  // seismicfdtd.f95:334
-    if (i <= NX - 2 && k <= NZ - 2 && okat(i + 1, k) && okat(i, k + 1))  // :341, :355
-      out[9] = (float)(dt / ((2 * rho + val(ids[n + 1], 6) + val(ids[n + NX], 6)) / 4));
+    // vx: the cell's own rho with the legacy quirks (:334), else the average of :320
+    if (legacy || i < 1 || k < 1 || !okat(i - 1, k) || !okat(i, k - 1))
+      out[8] = (float)(dt / rho);
+    else
+      out[8] = (float)(dt / rho_avg(dens, 2, rho, val(ids[n - 1], 6), val(ids[n - NX], 6)));
+    if (i <= NX - 2 && k <= NZ - 2 && okat(i + 1, k) && okat(i, k + 1))  // :342, :355
+      out[9] = (float)(dt / rho_avg(dens, 2, rho, val(ids[n + 1], 6), val(ids[n + NX], 6)));
     out[10] = (float)(1.0 - val(id, 7));
     out[11] = (float)(1.0 - val(id, 8));
   }
@@ -156,7 +160,7 @@ __constant__ S25Avg kS25Avg[33] = {
     {4, 3, 0.25}, {4, 8, 0.25}, {4, 12, 0.25}, {4, 15, 0.125}, {4, 16, 0.125}, {4, 17, 0.125}};
 
 __global__ void seis25_coef_from_ids(const int* __restrict__ ids, MatTable m, int NX, int NZ, int P, double dt,
-                                     float* coef, size_t plane, int* bad) {
+                                     float* coef, size_t plane, int* bad, int dens) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= NX || k >= NZ) return;
   const size_t n = (size_t)k * NX + i, c = (size_t)k * P + i;
@@ -200,12 +204,12 @@ __global__ void seis25_coef_from_ids(const int* __restrict__ ids, MatTable m, in
   }
   const double r = val(id, 21);
   float o33 = 0.f, o34 = 0.f, o35 = 0.f;
-  if (i >= 1 && k >= 1 && ml >= 0 && mu >= 0)  // seismicfdtd.f95:826
-    o33 = (float)(dt / ((4 * r + val(ml, 21) + val(mu, 21)) / 6));
-  if (i <= NX - 2 && k >= 1 && mr >= 0 && mu >= 0)  // :851
-    o34 = (float)(dt / ((4 * r + val(mr, 21) + val(mu, 21)) / 6));
-  if (i <= NX - 2 && k <= NZ - 2 && mr >= 0 && md >= 0)  // :877
-    o35 = (float)(dt / ((val(mr, 21) + val(md, 21) + 4 * r) / 6));
+  if (i >= 1 && k >= 1 && ml >= 0 && mu >= 0)  // seismicfdtd.f95:825
+    o33 = (float)(dt / rho_avg(dens, 4, r, val(ml, 21), val(mu, 21)));
+  if (i <= NX - 2 && k >= 1 && mr >= 0 && mu >= 0)  // :850
+    o34 = (float)(dt / rho_avg(dens, 4, r, val(mr, 21), val(mu, 21)));
+  if (i <= NX - 2 && k <= NZ - 2 && mr >= 0 && md >= 0)  // :876
+    o35 = (float)(dt / rho_avg(dens, 4, r, val(mr, 21), val(md, 21)));
   coef[33 * plane + c] = o33;
   coef[34 * plane + c] = o34;
   coef[35 * plane + c] = o35;
@@ -215,16 +219,20 @@ __global__ void seis25_coef_from_ids(const int* __restrict__ ids, MatTable m, in
 }  // namespace
 
 void coef_from_ids(int kind, const int* ids, const MatTable& m, int NX, int NZ, int P, double dt, float* coef,
-                   size_t plane, int* bad, cudaStream_t s) {
+                   size_t plane, int* bad, int flags, cudaStream_t s) {
+  const int dens = (flags & SFD_FLAG_DENSITY_MASK) / SFD_FLAG_DENSITY_NONE;
+  const int legacy = (flags & SFD_FLAG_LEGACY_QUIRKS) ? 1 : 0;
   const dim3 b(32, 8), g((NX + 31) / 32, (NZ + 7) / 8);
   switch (kind) {
     case SFD_ELECTROMAG2:
       em2_coef_from_ids<<<g, b, 0, s>>>(ids, m, NX, NZ, P, dt, coef, coef + plane, coef + 2 * plane, coef + 3 * plane,
                                         bad);
       break;
-    case SFD_SEISMIC2: seis2_coef_from_ids<<<g, b, 0, s>>>(ids, m, NX, NZ, P, dt, coef, plane, bad); break;
+    case SFD_SEISMIC2:
+      seis2_coef_from_ids<<<g, b, 0, s>>>(ids, m, NX, NZ, P, dt, coef, plane, bad, dens, legacy);
+      break;
     case SFD_ELECTROMAG25: em25_coef_from_ids<<<g, b, 0, s>>>(ids, m, NX, NZ, P, dt, coef, plane, bad); break;
-    default: seis25_coef_from_ids<<<g, b, 0, s>>>(ids, m, NX, NZ, P, dt, coef, plane, bad); break;
+    default: seis25_coef_from_ids<<<g, b, 0, s>>>(ids, m, NX, NZ, P, dt, coef, plane, bad, dens); break;
   }
 }
 

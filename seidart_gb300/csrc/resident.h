@@ -139,9 +139,10 @@ struct Seis2ResPlan {
 };
 
 struct Seis2Resident {
-  int NX, NZ, P, W, atten;
+  int NX, NZ, P, W, atten, legacy;
   float *vx, *vz, *sxx, *szz, *sxz;        // current copy: read before, written after the run
   float *m_vxx, *m_vzz, *m_vxz, *m_vzx;    // velocity-gradient memory (x, z, z, x strips), current copy
+  float *m2_vxx, *m2_vzz, *m2_vxz, *m2_vzx;  // the sigmaxz loop's own (corrected physics), current copy
   float *m_sxx_x, *m_szz_z, *m_sxz_x, *m_sxz_z;  // stress-gradient memory (x, z, x, z strips)
   const float* coef[12];                   // A11 A13 A15 A33 A35 B15 B35 B55 dtrx dtrz gxp gzp
   const float* q3;

@@ -4,7 +4,8 @@
 // The grid is cut into a uniform ntx x ntz grid of tiles (Seis2ResPlan), one
 // CTA per tile for the whole run.  A tile keeps, in shared memory, its five
 // fields with a one-cell halo ring, its twelve coefficient planes and its
-// eight CPML memory variables.  The per-cell arithmetic is that of the
+// twelve CPML memory variables (eight with the legacy quirks, where the two
+// stress loops share four).  The per-cell arithmetic is that of the
 // single-pass tile (fused2d.cuh: seis2_stress_cell and the per-cell velocity
 // code), i.e. the loops of legacy/fortran/seismicfdtd.f95:247-379, so the
 // streaming and on-chip forms give the same fields.
@@ -46,7 +47,7 @@ constexpr int kS2MaxTile = 128;  // tile width and height: two fields of one sid
 // tables of the tile's columns and rows (floats), then the cell order
 // (16-bit (row << 7) | column per cell).
 size_t s2_smem(int TW, int TZ) {
-  return sizeof(float) * (5 * (size_t)(TZ + 2) * (TW + 2) + 20 * (size_t)TZ * TW + 6 * (size_t)TW + 7 * (size_t)TZ) +
+  return sizeof(float) * (5 * (size_t)(TZ + 2) * (TW + 2) + 24 * (size_t)TZ * TW + 6 * (size_t)TW + 7 * (size_t)TZ) +
          2 * (((size_t)TZ * TW + 1) & ~(size_t)1);
 }
 
@@ -111,8 +112,10 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
   const bool up = bz > 0, down = bz < ntz - 1, left = bx > 0, right = bx < ntx - 1;
   float* F = smem;         // vx vz sxx szz sxz, (tz + 2) x (tw + 2) with the halo ring
   float* C = F + 5 * FS;   // A11 A13 A15 A33 A35 B15 B35 B55 dtrx dtrz gxp gzp, tz x tw
-  float* M = C + 12 * CS;  // m_vxx m_vzz m_vxz m_vzx m_sxx_x m_szz_z m_sxz_x m_sxz_z, tz x tw
-  float* XT = M + 8 * CS;  // x tables at the tile's columns: ik ad b ikh adh bh, tw each
+  // m_vxx m_vzz m_vxz m_vzx m_sxx_x m_szz_z m_sxz_x m_sxz_z, then the sigmaxz
+  // loop's own m2_vxx m2_vzz m2_vxz m2_vzx (corrected physics), tz x tw each
+  float* M = C + 12 * CS;
+  float* XT = M + 12 * CS;  // x tables at the tile's columns: ik ad b ikh adh bh, tw each
   float* ZT = XT + 6 * tw;  // z tables at the tile's rows, then q3, tz each
   unsigned short* CELL = reinterpret_cast<unsigned short*>(ZT + 7 * tz);  // cell order, see cell_at
   float* VX = F;
@@ -129,7 +132,7 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
 
   // ---- load the tile: fields, the velocities of the halo ring (the
   // stresses of the ring are exchanged every step), coefficients, memory
-  for (int q = tid; q < 5 * FS + 20 * CS; q += kS2Threads) smem[q] = 0.0f;
+  for (int q = tid; q < 5 * FS + 24 * CS; q += kS2Threads) smem[q] = 0.0f;
   if (tid == 0) {
     s_nrec = 0;
     s_abort = 0;
@@ -159,6 +162,10 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
       M[3 * CS + q] = a.m_vzx[mx];
       M[4 * CS + q] = a.m_sxx_x[mx];
       M[6 * CS + q] = a.m_sxz_x[mx];
+      if (!a.legacy) {
+        M[8 * CS + q] = a.m2_vxx[mx];
+        M[11 * CS + q] = a.m2_vzx[mx];
+      }
     }
     if (in_strip(k, NZ, W)) {
       const size_t mz = (size_t)strip_idx(k, NZ, W) * P + i;
@@ -166,6 +173,10 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
       M[2 * CS + q] = a.m_vxz[mz];
       M[5 * CS + q] = a.m_szz_z[mz];
       M[7 * CS + q] = a.m_sxz_z[mz];
+      if (!a.legacy) {
+        M[9 * CS + q] = a.m2_vzz[mz];
+        M[10 * CS + q] = a.m2_vxz[mz];
+      }
     }
   }
   {
@@ -269,6 +280,8 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
         float sxx = SXX[f], szz = SZZ[f], sxz = SXZ[f];
         const bool xs = in_strip(i, NX, W), zs = in_strip(k, NZ, W);
         float mvxx = M[q], mvzz = M[CS + q], mvxz = M[2 * CS + q], mvzx = M[3 * CS + q];
+        // the sigmaxz loop's memory: its own (corrected physics) or loop 1's (legacy)
+        const bool own2 = !a.legacy;
         const bool loop1 = (k >= 1) && (i <= NX - 2);
         const bool loop2 = (k <= NZ - 2) && (i >= 1);
         if (loop1 || loop2) {
@@ -280,8 +293,8 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
             const float d_vz_z = vz0 - VZ[f - SW];
             const float d_vz_x = VZ[f + 1] - vz0;
             const float d_vx_z = vx0 - VX[f - SW];
-            if (xs) {
-              mvxx = ZT[6 * tz + lr] * mvxx + XT[4 * tw + lc] * d_vx_x;  // b_x_half(j), :255
+            if (xs) {  // legacy: b_x_half(j), :255 (the q3 row table); corrected: b_x_half(i)
+              mvxx = (a.legacy ? ZT[6 * tz + lr] : XT[5 * tw + lc]) * mvxx + XT[4 * tw + lc] * d_vx_x;
               mvzx = XT[2 * tw + lc] * mvzx + XT[tw + lc] * d_vz_x;
             }
             if (zs) {
@@ -302,19 +315,32 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
             const float d_vz_z = VZ[f + SW] - vz0;
             const float d_vz_x = vz0 - VZ[f - 1];
             const float d_vx_z = VX[f + SW] - vx0;
+            float mxx = own2 ? M[8 * CS + q] : mvxx, mzz = own2 ? M[9 * CS + q] : mvzz;
+            float mxz = own2 ? M[10 * CS + q] : mvxz, mzx = own2 ? M[11 * CS + q] : mvzx;
             if (xs) {
-              mvxx = XT[5 * tw + lc] * mvxx + XT[4 * tw + lc] * d_vx_x;
-              mvzx = XT[2 * tw + lc] * mvzx + XT[tw + lc] * d_vz_x;
+              mxx = XT[5 * tw + lc] * mxx + XT[4 * tw + lc] * d_vx_x;
+              mzx = XT[2 * tw + lc] * mzx + XT[tw + lc] * d_vz_x;
             }
             if (zs) {
-              mvzz = ZT[2 * tz + lr] * mvzz + ZT[tz + lr] * d_vz_z;
-              mvxz = ZT[5 * tz + lr] * mvxz + ZT[4 * tz + lr] * d_vx_z;
+              mzz = ZT[2 * tz + lr] * mzz + ZT[tz + lr] * d_vz_z;
+              mxz = ZT[5 * tz + lr] * mxz + ZT[4 * tz + lr] * d_vx_z;
             }
-            const float dvx_dx = d_vx_x * ikxh + mvxx;
-            const float dvz_dz = d_vz_z * ikz + mvzz;
-            const float dvz_dx = d_vz_x * ikx + mvzx;
-            const float dvx_dz = d_vx_z * ikzh + mvxz;
+            const float dvx_dx = d_vx_x * ikxh + mxx;
+            const float dvz_dz = d_vz_z * ikz + mzz;
+            const float dvz_dx = d_vz_x * ikx + mzx;
+            const float dvx_dz = d_vx_z * ikzh + mxz;
             sxz = sxz + (C[5 * CS + q] * dvx_dx + C[6 * CS + q] * dvz_dz + C[7 * CS + q] * (dvz_dx + dvx_dz));
+            if (own2) {
+              if (xs) { M[8 * CS + q] = mxx; M[11 * CS + q] = mzx; }
+              if (zs) { M[9 * CS + q] = mzz; M[10 * CS + q] = mxz; }
+            } else {
+              mvxx = mxx; mvzz = mzz; mvxz = mxz; mvzx = mzx;
+            }
+          }
+          if (a.io.ssrc && i == si && k == sk) {  // stress source: sigma_ij += f_ij(t) dt
+            sxx += a.io.ssrc[t];
+            szz += a.io.ssrc[a.io.nstep + t];
+            sxz += a.io.ssrc[2 * a.io.nstep + t];
           }
           SXX[f] = sxx;
           SZZ[f] = szz;
@@ -461,6 +487,10 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
       a.m_vzx[mx] = M[3 * CS + q];
       a.m_sxx_x[mx] = M[4 * CS + q];
       a.m_sxz_x[mx] = M[6 * CS + q];
+      if (!a.legacy) {
+        a.m2_vxx[mx] = M[8 * CS + q];
+        a.m2_vzx[mx] = M[11 * CS + q];
+      }
     }
     if (in_strip(k, NZ, W)) {
       const size_t mz = (size_t)strip_idx(k, NZ, W) * P + i;
@@ -468,6 +498,10 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
       a.m_vxz[mz] = M[2 * CS + q];
       a.m_szz_z[mz] = M[5 * CS + q];
       a.m_sxz_z[mz] = M[7 * CS + q];
+      if (!a.legacy) {
+        a.m2_vzz[mz] = M[9 * CS + q];
+        a.m2_vxz[mz] = M[10 * CS + q];
+      }
     }
   }
   block_norm_to_slot(nrm, a.io.slots, blockIdx.x);

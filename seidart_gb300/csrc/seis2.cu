@@ -1,12 +1,14 @@
 // seismic2 (legacy/fortran/seismicfdtd.f95:12-385): 2-D anisotropic
 // velocity-stress scheme.  Two fused kernels per step:
 //   half1: both stress loops (:247-281 sigmaxx/sigmazz, :283-312 sigmaxz) for
-//          one cell per thread.  The four velocity-gradient memory variables
-//          are shared by the two loops in the Fortran, so at a cell that both
+//          one cell per thread, then the stress source at its cell.  With the
+//          legacy quirks the four velocity-gradient memory variables are
+//          shared by the two loops, as in the Fortran, so at a cell that both
 //          loops visit they advance twice, first with the loop-1 stencil and
-//          then with the loop-2 stencil; each thread does the same in
-//          registers.  Loop 1 uses b_x_half at the z index (:255), read here
-//          from a table q3[k] that the host fills from b_x_half.
+//          then with the loop-2 stencil, and loop 1 uses b_x_half at the z
+//          index (:255), read from a table q3[k] that the host fills from
+//          b_x_half.  With corrected physics (the default) the sigmaxz loop
+//          has its own four memory variables and loop 1 uses b_x_half(i).
 //          Block (0,0) first records the receivers of the previous step.
 //   half2: vx (:317-336) and vz (:338-357) with the stress-gradient memory
 //          variables, attenuation, the source (:360-361), the Dirichlet edges
@@ -37,9 +39,17 @@ __global__ void __launch_bounds__(BX * BY) seis2_stress_kernel(Seis2Args a, int 
   const bool xs = in_strip(i, NX, W), zs = in_strip(k, NZ, W);
   const size_t mx = (size_t)k * (2 * W) + (xs ? strip_idx(i, NX, W) : 0);
   const size_t mz = (size_t)(zs ? strip_idx(k, NZ, W) : 0) * P + i;
+  const bool own2 = !a.legacy;
   float m_vxx = 0.f, m_vzx = 0.f, m_vzz = 0.f, m_vxz = 0.f;
-  if (xs) { m_vxx = a.m_vxx[mx]; m_vzx = a.m_vzx[mx]; }
-  if (zs) { m_vzz = a.m_vzz[mz]; m_vxz = a.m_vxz[mz]; }
+  float n_vxx = 0.f, n_vzx = 0.f, n_vzz = 0.f, n_vxz = 0.f;  // the sigmaxz loop's own
+  if (xs) {
+    m_vxx = a.m_vxx[mx]; m_vzx = a.m_vzx[mx];
+    if (own2) { n_vxx = a.m2_vxx[mx]; n_vzx = a.m2_vzx[mx]; }
+  }
+  if (zs) {
+    m_vzz = a.m_vzz[mz]; m_vxz = a.m_vxz[mz];
+    if (own2) { n_vzz = a.m2_vzz[mz]; n_vxz = a.m2_vxz[mz]; }
+  }
   const float vx0 = a.vx[c], vz0 = a.vz[c];
   const float ikx = a.X.ik[i], ikxh = a.X.ikh[i], ikz = a.Z.ik[k], ikzh = a.Z.ikh[k];
 
@@ -49,7 +59,7 @@ __global__ void __launch_bounds__(BX * BY) seis2_stress_kernel(Seis2Args a, int 
     const float d_vz_x = a.vz[c + 1] - vz0;
     const float d_vx_z = vx0 - a.vx[c - P];
     if (xs) {
-      m_vxx = a.q3[k] * m_vxx + a.X.adh[i] * d_vx_x;
+      m_vxx = (a.legacy ? a.q3[k] : a.X.bh[i]) * m_vxx + a.X.adh[i] * d_vx_x;
       m_vzx = a.X.b[i] * m_vzx + a.X.ad[i] * d_vz_x;
     }
     if (zs) {
@@ -70,23 +80,38 @@ __global__ void __launch_bounds__(BX * BY) seis2_stress_kernel(Seis2Args a, int 
     const float d_vz_z = a.vz[c + P] - vz0;
     const float d_vz_x = vz0 - a.vz[c - 1];
     const float d_vx_z = a.vx[c + P] - vx0;
+    float mxx = own2 ? n_vxx : m_vxx, mzx = own2 ? n_vzx : m_vzx;
+    float mzz = own2 ? n_vzz : m_vzz, mxz = own2 ? n_vxz : m_vxz;
     if (xs) {
-      m_vxx = a.X.bh[i] * m_vxx + a.X.adh[i] * d_vx_x;
-      m_vzx = a.X.b[i] * m_vzx + a.X.ad[i] * d_vz_x;
+      mxx = a.X.bh[i] * mxx + a.X.adh[i] * d_vx_x;
+      mzx = a.X.b[i] * mzx + a.X.ad[i] * d_vz_x;
     }
     if (zs) {
-      m_vzz = a.Z.b[k] * m_vzz + a.Z.ad[k] * d_vz_z;
-      m_vxz = a.Z.bh[k] * m_vxz + a.Z.adh[k] * d_vx_z;
+      mzz = a.Z.b[k] * mzz + a.Z.ad[k] * d_vz_z;
+      mxz = a.Z.bh[k] * mxz + a.Z.adh[k] * d_vx_z;
     }
-    const float dvx_dx = d_vx_x * ikxh + m_vxx;
-    const float dvz_dz = d_vz_z * ikz + m_vzz;
-    const float dvz_dx = d_vz_x * ikx + m_vzx;
-    const float dvx_dz = d_vx_z * ikzh + m_vxz;
+    const float dvx_dx = d_vx_x * ikxh + mxx;
+    const float dvz_dz = d_vz_z * ikz + mzz;
+    const float dvz_dx = d_vz_x * ikx + mzx;
+    const float dvx_dz = d_vx_z * ikzh + mxz;
     const float B15 = a.B15[c], B35 = a.B35[c], B55 = a.B55[c];
     a.sxz[c] = a.sxz[c] + (B15 * dvx_dx + B35 * dvz_dz + B55 * (dvz_dx + dvx_dz));
+    if (own2) { n_vxx = mxx; n_vzx = mzx; n_vzz = mzz; n_vxz = mxz; }
+    else { m_vxx = mxx; m_vzx = mzx; m_vzz = mzz; m_vxz = mxz; }
   }
-  if (xs) { a.m_vxx[mx] = m_vxx; a.m_vzx[mx] = m_vzx; }
-  if (zs) { a.m_vzz[mz] = m_vzz; a.m_vxz[mz] = m_vxz; }
+  if (xs) {
+    a.m_vxx[mx] = m_vxx; a.m_vzx[mx] = m_vzx;
+    if (own2) { a.m2_vxx[mx] = n_vxx; a.m2_vzx[mx] = n_vzx; }
+  }
+  if (zs) {
+    a.m_vzz[mz] = m_vzz; a.m_vxz[mz] = m_vxz;
+    if (own2) { a.m2_vzz[mz] = n_vzz; a.m2_vxz[mz] = n_vxz; }
+  }
+  if (a.io.ssrc && i == a.io.si && k == a.io.sk) {  // stress source: sigma_ij += f_ij(t) dt
+    a.sxx[c] += a.io.ssrc[t];
+    a.szz[c] += a.io.ssrc[a.io.nstep + t];
+    a.sxz[c] += a.io.ssrc[2 * a.io.nstep + t];
+  }
 }
 
 __global__ void __launch_bounds__(BX * BY) seis2_velocity_kernel(Seis2Args a, int rel) {

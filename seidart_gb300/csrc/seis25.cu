@@ -9,9 +9,13 @@
 //          :728-771 sigmaxz, :774-815 sigmayz).  The nine velocity-gradient
 //          memory variables are shared by the loops in the Fortran and
 //          advance once per loop that visits a cell, in loop order; each
-//          thread applies the same sequence in registers.  The coefficient
-//          pairs written at :657 (c16) and :766 (c45) and the two derivatives
-//          :701-707 leave unscaled are kept as written.
+//          thread applies the same sequence in registers.  The two
+//          derivatives :701-707 leave unscaled are kept as written.  The
+//          coefficient pairs of :657 (c16 (dvx_dy + dvz_dy)) and :766 (c45
+//          (dvx_dz + dvz_dx)) are kept with the legacy quirks (a.legacy);
+//          corrected physics (the default) uses the Voigt pairs c16 (dvx_dy +
+//          dvy_dx) and c45 (dvy_dz + dvz_dy).  A stress source is added at its
+//          cell after the four loops.
 //   half2: vx, vy (:821-870) and vz (:872-896) with the stress-gradient
 //          memory variables, optional attenuation v <- v (1 - gamma), the
 //          source (:898-900), the six Dirichlet faces (:903-925) and the norm.
@@ -153,7 +157,7 @@ __global__ void __launch_bounds__(BX * BZ, 4) seis25_stress_kernel(Seis25Args a,
       const float vyy = dyy * iky + mvyy, vxy = dxy * iky + mvxy, vzy = dzy * iky + mvzy;
       const float vzz = dzz * ikz + mvzz, vxz = dxz * ikz + mvxz, vyz = dyz * ikz + mvyz;
       SXX[c] = oxx + (p11 * vxx + p12 * vyy + p13 * vzz + p14 * (vyz + vzy) + p15 * (vxz + vzx) +
-                      p16 * (vxy + vzy));
+                      p16 * (a.legacy ? vxy + vzy : vxy + vyx));  // Q4, :657
       SYY[c] = oyy + (p12 * vxx + p22 * vyy + p23 * vzz + p24 * (vyz + vzy) + p25 * (vxz + vzx) +
                       p26 * (vyx + vxy));
       SZZ[c] = ozz + (p13 * vxx + p23 * vyy + p33 * vzz + p34 * (vyz + vzy) + p35 * (vxz + vzx) +
@@ -183,10 +187,10 @@ __global__ void __launch_bounds__(BX * BZ, 4) seis25_stress_kernel(Seis25Args a,
       if (ys) { mvyy = by * mvyy + ady * dyy; mvxy = by * mvxy + ady * dxy; mvzy = by * mvzy + ady * dzy; }
       if (zs) { mvzz = bzh * mvzz + adzh * dzz; mvxz = bzh * mvxz + adzh * dxz; mvyz = bzh * mvyz + adzh * dyz; }
       const float vxx = dxx * ikx + mvxx, vyx = dyx * ikx + mvyx, vzx = dzx * ikx + mvzx;
-      const float vyy = dyy * iky + mvyy, vxy = dxy * iky + mvxy;
-      const float vzz = dzz * ikzh + mvzz, vxz = dxz * ikzh + mvxz;
-      SXZ[c] = oxz + (r15 * vxx + r25 * vyy + r35 * vzz + r45 * (vxz + vzx) + r55 * (vxz + vzx) +
-                      r56 * (vxy + vyx));
+      const float vyy = dyy * iky + mvyy, vxy = dxy * iky + mvxy, vzy = dzy * iky + mvzy;
+      const float vzz = dzz * ikzh + mvzz, vxz = dxz * ikzh + mvxz, vyz = dyz * ikzh + mvyz;
+      SXZ[c] = oxz + (r15 * vxx + r25 * vyy + r35 * vzz + r45 * (a.legacy ? vxz + vzx : vyz + vzy) +  // Q4, :766
+                      r55 * (vxz + vzx) + r56 * (vxy + vyx));
     }
     // ---- Loop 4: sigmayz (j <= NY-2): x+, y+, z+
     if (l4) {
@@ -205,6 +209,16 @@ __global__ void __launch_bounds__(BX * BZ, 4) seis25_stress_kernel(Seis25Args a,
     if (xs) { MVXX[mx] = mvxx; MVYX[mx] = mvyx; MVZX[mx] = mvzx; }
     if (ys) { MVXY[my] = mvxy; MVYY[my] = mvyy; MVZY[my] = mvzy; }
     if (zs) { MVXZ[mz] = mvxz; MVYZ[mz] = mvyz; MVZZ[mz] = mvzz; }
+    if (a.io.ssrc && i == a.io.si && j == a.io.sj && k == a.io.sk) {  // stress source: sigma_ij += f_ij(t) dt
+      const float* f = a.io.ssrc + t;
+      const int n = a.io.nstep;
+      SXX[c] += f[0];
+      SYY[c] += f[n];
+      SZZ[c] += f[2 * n];
+      SXY[c] += f[3 * n];
+      SXZ[c] += f[4 * n];
+      SYZ[c] += f[5 * n];
+    }
     pvx = cvx; pvy = cvy; pvz = cvz;
     cvx = nvx; cvy = nvy; cvz = nvz;
   }

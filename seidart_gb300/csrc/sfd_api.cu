@@ -116,6 +116,10 @@ int nchan(int kind) {
 }
 // Source components the caller gives (real time functions, x [y] z).
 int nsrc(int kind) { return kind == SFD_ELECTROMAG2C ? 2 : nchan(kind); }
+// Stress source components (sfd_set_stress_source): xx zz xz in 2-D, xx yy zz xy xz yz in 2.5-D.
+int nstress(int kind) { return kind == SFD_SEISMIC2 ? 3 : (kind == SFD_SEISMIC25 ? 6 : 0); }
+// Density method of the flags: 0 arithmetic, 1 none, 2 geometric, 3 harmonic.
+int density_method(int flags) { return (flags & SFD_FLAG_DENSITY_MASK) / SFD_FLAG_DENSITY_NONE; }
 int nplanes(int kind) {
   switch (kind) {
     case SFD_SEISMIC2: return 9;
@@ -132,7 +136,8 @@ bool is3(int kind) { return kind == SFD_SEISMIC25 || kind == SFD_ELECTROMAG25; }
 const char* mem_axes(int kind) {
   switch (kind) {
     case SFD_ELECTROMAG2: return "zxzx";              // dEx_dz dEz_dx dHy_dz dHy_dx
-    case SFD_SEISMIC2: return "xzzxxzxz";             // dvx_dx dvz_dz dvx_dz dvz_dx dsxx_dx dszz_dz dsxz_dx dsxz_dz
+    case SFD_SEISMIC2: return "xzzxxzxzxzzx";  // dvx_dx dvz_dz dvx_dz dvz_dx dsxx_dx dszz_dz dsxz_dx dsxz_dz,
+                                                // then the sigmaxz loop's own dvx_dx dvz_dz dvx_dz dvz_dx
     case SFD_SEISMIC25: return "xyzxyzxyzxyzxyxzyz";  // dv{x,y,z}_d{x,y,z}, dsxx_dx dsyy_dy dszz_dz dsxy_dx dsxy_dy dsxz_dx dsxz_dz dsyz_dy dsyz_dz
     case SFD_ELECTROMAG25: return "yzzxyxyzxzyx";     // dEz_dy dEy_dz dEx_dz dEz_dx dEx_dy dEy_dx dHz_dy dHy_dz dHz_dx dHx_dz dHx_dy dHy_dx
     case SFD_ELECTROMAG2C: return "zzxxzzxx";         // dEx_dz dEz_dx dHy_dz dHy_dx, each real then imaginary
@@ -163,21 +168,21 @@ int choose_ysplit(const sfd_config& c) {
   return s;
 }
 
-// Number of memory variables that the single-pass 2-D steps keep in two
-// copies (those of the first half-step, re-derived on tile halos).
-int npingpong_mem(int kind) {
+// Whether the single-pass 2-D steps keep memory variable q in two copies
+// (those of the first half-step, re-derived on tile halos).
+bool pingpong_mem(int kind, int q) {
   switch (kind) {
-    case SFD_ELECTROMAG2: return 2;  // dEx_dz dEz_dx
-    case SFD_SEISMIC2: return 4;     // dvx_dx dvz_dz dvx_dz dvz_dx
+    case SFD_ELECTROMAG2: return q < 2;                // dEx_dz dEz_dx
+    case SFD_SEISMIC2: return q < 4 || (q >= 8 && q < 12);  // the velocity-gradient ones of both stress loops
   }
-  return 0;
+  return false;
 }
 bool has_single_pass(int kind) { return kind == SFD_ELECTROMAG2 || kind == SFD_SEISMIC2; }
 
 struct Layout {
   int P, NX, NY, NZ, W, ysplit, nslots;
   size_t fsz;                // floats per field
-  size_t off_ctl, off_fields, off_mem[18], mem_sz[18], off_fieldsB, off_memB[4], off_coef, coef_plane, off_axis[3],
+  size_t off_ctl, off_fields, off_mem[18], mem_sz[18], off_fieldsB, off_memB[18], off_coef, coef_plane, off_axis[3],
       off_q3, off_src, off_rec, off_traces, off_slots, off_res, total;
 };
 
@@ -201,7 +206,10 @@ int validate_cfg(const sfd_config* c) {
   if (!three && c->ny != 1) return fail(SFD_ERR_BAD_ARG, "2-D solvers need ny = 1 (got %d)", c->ny);
   if (c->nstep < 1) return fail(SFD_ERR_BAD_ARG, "nstep must be >= 1");
   if (c->nrec < 0) return fail(SFD_ERR_BAD_ARG, "nrec must be >= 0");
-  if ((c->flags & ~(SFD_FLAG_TWO_PASS | SFD_FLAG_STREAMING)) != 0) return fail(SFD_ERR_BAD_ARG, "unknown flags 0x%x", c->flags);
+  if ((c->flags & ~(SFD_FLAG_TWO_PASS | SFD_FLAG_STREAMING | SFD_FLAG_LEGACY_QUIRKS | SFD_FLAG_DENSITY_MASK)) != 0)
+    return fail(SFD_ERR_BAD_ARG, "unknown flags 0x%x", c->flags);
+  if ((c->flags & (SFD_FLAG_LEGACY_QUIRKS | SFD_FLAG_DENSITY_MASK)) && c->kind != SFD_SEISMIC2 && c->kind != SFD_SEISMIC25)
+    return fail(SFD_ERR_BAD_ARG, "SFD_FLAG_LEGACY_QUIRKS and the density flags apply to the seismic kinds only");
   if (!(c->dt > 0) || !(c->dx > 0) || !(c->dz > 0) || (three && !(c->dy > 0)))
     return fail(SFD_ERR_BAD_ARG, "dt and grid steps must be positive");
   const double cells = (double)c->nx * c->ny * c->nz;
@@ -230,10 +238,11 @@ void make_layout(const sfd_config& c, Layout* L) {
     o += align256(sizeof(float) * n);
   }
   L->off_fieldsB = 0;
-  for (int m = 0; m < 4; ++m) L->off_memB[m] = 0;
+  for (int m = 0; m < 18; ++m) L->off_memB[m] = 0;
   if (has_single_pass(c.kind) && !(c.flags & SFD_FLAG_TWO_PASS)) {
     L->off_fieldsB = o; o += align256(sizeof(float) * L->fsz * nfields(c.kind));
-    for (int m = 0; m < npingpong_mem(c.kind); ++m) { L->off_memB[m] = o; o += align256(sizeof(float) * L->mem_sz[m]); }
+    for (int m = 0; m < nm; ++m)
+      if (pingpong_mem(c.kind, m)) { L->off_memB[m] = o; o += align256(sizeof(float) * L->mem_sz[m]); }
   }
   L->coef_plane = (size_t)L->P * c.nz;
   L->off_coef = o; o += align256(sizeof(float) * L->coef_plane * ncoef(c.kind));
@@ -242,7 +251,7 @@ void make_layout(const sfd_config& c, Layout* L) {
   for (int a = 0; a < 3; ++a) L->off_axis[a] = 0;
   for (int a = 0; a < nax; ++a) { L->off_axis[a] = o; o += align256(sizeof(float) * 6 * axis_stride(lens[a])); }
   L->off_q3 = o; o += align256(sizeof(float) * c.nz);
-  L->off_src = o; o += align256(sizeof(float) * (size_t)nchan(c.kind) * c.nstep);
+  L->off_src = o; o += align256(sizeof(float) * (size_t)(nchan(c.kind) + nstress(c.kind)) * c.nstep);
   L->off_rec = o; o += align256(sizeof(int) * 3 * (size_t)std::max(1, c.nrec));
   L->off_traces = o; o += align256(sizeof(float) * (size_t)c.nstep * nchan(c.kind) * std::max(1, c.nrec));
   L->off_slots = o; o += align256(sizeof(float) * L->nslots);  // ZB = 1 tiles: the largest grid
@@ -264,6 +273,8 @@ struct sfd_handle_s {
   cudaStream_t cap_stream;   // private stream used only to capture graphs
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // indexed by the parity the graph starts from
   bool have_model = false, have_cpml = false;
+  bool have_ssrc = false;       // a stress source was set (seismic kinds)
+  bool have_force_src = false;  // a force (or E) source was set
   bool single = false;  // single-pass 2-D steps (ping-pong state)
   int cur = 0;          // copy holding the current state (single-pass only)
   int zb = 2;           // rows per thread of the single-pass tiles
@@ -306,7 +317,7 @@ struct sfd_handle_s {
     return (float*)(base + (copy ? L.off_fieldsB : L.off_fields)) + (size_t)q * L.fsz;
   }
   float* mc(int q, int copy) const {
-    return (float*)(base + ((copy && q < 4 && L.off_memB[q]) ? L.off_memB[q] : L.off_mem[q]));
+    return (float*)(base + ((copy && L.off_memB[q]) ? L.off_memB[q] : L.off_mem[q]));
   }
   float* f(int q) const { return fc(q, single ? cur : 0); }
   float* m(int q) const { return mc(q, single ? cur : 0); }
@@ -318,6 +329,7 @@ struct sfd_handle_s {
     io.slots = (float*)(base + L.off_slots);
     io.src = (const float*)(base + L.off_src);
     io.nstep = cfg.nstep;
+    io.ssrc = have_ssrc ? (const float*)(base + L.off_src) + (size_t)nchan(cfg.kind) * cfg.nstep : nullptr;
     io.si = io.sj = io.sk = -1;
     io.rec = (const int*)(base + L.off_rec);
     io.nrec = cfg.nrec;
@@ -387,8 +399,10 @@ void bind_args(sfd_handle* h) {
     case SFD_SEISMIC2: {
       Seis2Args& a = h->s2;
       a.NX = NX; a.NZ = NZ; a.P = L.P; a.W = L.W; a.atten = 0;
+      a.legacy = (c.flags & SFD_FLAG_LEGACY_QUIRKS) ? 1 : 0;
       a.vx = h->fc(0, 0); a.vz = h->fc(1, 0); a.sxx = h->fc(2, 0); a.szz = h->fc(3, 0); a.sxz = h->fc(4, 0);
       a.m_vxx = h->mc(0, 0); a.m_vzz = h->mc(1, 0); a.m_vxz = h->mc(2, 0); a.m_vzx = h->mc(3, 0);
+      a.m2_vxx = h->mc(8, 0); a.m2_vzz = h->mc(9, 0); a.m2_vxz = h->mc(10, 0); a.m2_vzx = h->mc(11, 0);
       a.m_sxx_x = h->mc(4, 0); a.m_szz_z = h->mc(5, 0); a.m_sxz_x = h->mc(6, 0); a.m_sxz_z = h->mc(7, 0);
       a.A11 = h->coef(0); a.A13 = h->coef(1); a.A15 = h->coef(2); a.A33 = h->coef(3); a.A35 = h->coef(4);
       a.B15 = h->coef(5); a.B35 = h->coef(6); a.B55 = h->coef(7);
@@ -399,7 +413,10 @@ void bind_args(sfd_handle* h) {
       h->launch = seis2_launch(a);
       for (int p = 0; p < 2 && h->single; ++p) {
         Seis2Step& b = h->s2s[p];
-        b.NX = NX; b.NZ = NZ; b.P = L.P; b.W = L.W; b.atten = a.atten;
+        b.NX = NX; b.NZ = NZ; b.P = L.P; b.W = L.W; b.atten = a.atten; b.legacy = a.legacy;
+        b.m2_vxx0 = h->mc(8, p); b.m2_vzz0 = h->mc(9, p); b.m2_vxz0 = h->mc(10, p); b.m2_vzx0 = h->mc(11, p);
+        b.m2_vxx1 = h->mc(8, 1 - p); b.m2_vzz1 = h->mc(9, 1 - p); b.m2_vxz1 = h->mc(10, 1 - p);
+        b.m2_vzx1 = h->mc(11, 1 - p);
         b.vx0 = h->fc(0, p); b.vz0 = h->fc(1, p); b.sxx0 = h->fc(2, p); b.szz0 = h->fc(3, p); b.sxz0 = h->fc(4, p);
         b.vx1 = h->fc(0, 1 - p); b.vz1 = h->fc(1, 1 - p); b.sxx1 = h->fc(2, 1 - p); b.szz1 = h->fc(3, 1 - p);
         b.sxz1 = h->fc(4, 1 - p);
@@ -419,6 +436,7 @@ void bind_args(sfd_handle* h) {
     case SFD_SEISMIC25: {
       Seis25Args& a = h->s25;
       a.NX = NX; a.NY = NY; a.NZ = NZ; a.P = L.P; a.W = L.W; a.atten = 0;
+      a.legacy = (c.flags & SFD_FLAG_LEGACY_QUIRKS) ? 1 : 0;
       float** F[9] = {&a.vx, &a.vy, &a.vz, &a.sxx, &a.syy, &a.szz, &a.sxy, &a.sxz, &a.syz};
       for (int q = 0; q < 9; ++q) *F[q] = h->f(q);
       // oracle order: dvx_dx dvx_dy dvx_dz dvy_dx dvy_dy dvy_dz dvz_dx dvz_dy dvz_dz
@@ -460,6 +478,20 @@ void set_io_source(sfd_handle* h, int i, int j, int k) {
   IoArgs* ios[9] = {&h->em2.io, &h->s2.io, &h->s25.io, &h->em25.io, &h->em2c.io,
                     &h->em2s[0].io, &h->em2s[1].io, &h->s2s[0].io, &h->s2s[1].io};
   for (IoArgs* io : ios) { io->si = i; io->sj = j; io->sk = k; }
+}
+
+// Whether (i, j, k) is the source cell already set on the handle.
+bool same_source_cell(const sfd_handle* h, int i, int j, int k) {
+  const IoArgs& io = h->s2.io;  // every argument block holds the same cell
+  return io.si == i && io.sj == j && io.sk == k;
+}
+
+// Point every argument block at the stress source amplitudes (or at none).
+void set_io_ssrc(sfd_handle* h) {
+  const IoArgs ref = h->io();
+  IoArgs* ios[9] = {&h->em2.io, &h->s2.io, &h->s25.io, &h->em25.io, &h->em2c.io,
+                    &h->em2s[0].io, &h->em2s[1].io, &h->s2s[0].io, &h->s2s[1].io};
+  for (IoArgs* io : ios) io->ssrc = ref.ssrc;
 }
 
 void set_atten(sfd_handle* h, int atten) {
@@ -592,9 +624,10 @@ Seis2Resident seis2_resident_args(const sfd_handle* h, int64_t nsteps) {
   Seis2Resident r;
   const Seis2Step& b = h->s2s[h->cur];
   const int p = h->cur;
-  r.NX = b.NX; r.NZ = b.NZ; r.P = b.P; r.W = b.W; r.atten = b.atten;
+  r.NX = b.NX; r.NZ = b.NZ; r.P = b.P; r.W = b.W; r.atten = b.atten; r.legacy = b.legacy;
   r.vx = h->fc(0, p); r.vz = h->fc(1, p); r.sxx = h->fc(2, p); r.szz = h->fc(3, p); r.sxz = h->fc(4, p);
   r.m_vxx = h->mc(0, p); r.m_vzz = h->mc(1, p); r.m_vxz = h->mc(2, p); r.m_vzx = h->mc(3, p);
+  r.m2_vxx = h->mc(8, p); r.m2_vzz = h->mc(9, p); r.m2_vxz = h->mc(10, p); r.m2_vzx = h->mc(11, p);
   r.m_sxx_x = h->mc(4, 0); r.m_szz_z = h->mc(5, 0); r.m_sxz_x = h->mc(6, 0); r.m_sxz_z = h->mc(7, 0);
   const float* cf[12] = {b.A11, b.A13, b.A15, b.A33, b.A35, b.B15, b.B35, b.B55, b.dtrx, b.dtrz, b.gxp, b.gzp};
   for (int q = 0; q < 12; ++q) r.coef[q] = cf[q];
@@ -870,7 +903,7 @@ int32_t sfd_set_model_ids(sfd_handle* h, const int32_t* dev_ids, int32_t nmat, c
   Ctl* ctl = (Ctl*)(h->base + h->L.off_ctl);
   int* bad = &ctl->pad2;
   CK(cudaMemsetAsync(bad, 0, sizeof(int), h->stream));
-  coef_from_ids(c.kind, dev_ids, mt, c.nx, c.nz, h->L.P, c.dt, h->coef(0), h->L.coef_plane, bad, h->stream);
+  coef_from_ids(c.kind, dev_ids, mt, c.nx, c.nz, h->L.P, c.dt, h->coef(0), h->L.coef_plane, bad, c.flags, h->stream);
   CK(cudaGetLastError());
   int flag = 0;
   CK(cudaMemcpyAsync(&flag, bad, sizeof flag, cudaMemcpyDeviceToHost, h->stream));
@@ -1016,6 +1049,8 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
     }
     case SFD_SEISMIC2: {
       const double *rho = P(6), *gx = P(7), *gz = P(8);
+      const int dm = density_method(c.flags);
+      const bool legacy = (c.flags & SFD_FLAG_LEGACY_QUIRKS) != 0;
       // loop-1 points (i <= NX-2, k >= 1): (c(i+1,k) + 2 c(i,k) + c(i,k-1)) / 4 for c11 c13 c15 c33 c35
       // loop-2 points (k <= NZ-2, i >= 1): (c(i,k+1) + 2 c(i,k) + c(i-1,k)) / 4 for c15 c35 c55
       const int A_src[5] = {0, 1, 2, 3, 4}, B_src[3] = {2, 4, 5};
@@ -1040,9 +1075,14 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
         int a = 0;
         for (int i = 0; i < NX; ++i) {
           const size_t n = (size_t)i + (size_t)NX * k;
-          out[8][n] = (float)(dt / rho[n]);  // seismicfdtd.f95:334
-          if (i <= NX - 2 && k <= NZ - 2)    // seismicfdtd.f95:341, 355
-            out[9][n] = (float)(dt / ((2 * rho[n] + at(rho, i + 1, k) + at(rho, i, k + 1)) / 4));
+          // vx: the cell's own rho with the legacy quirks (seismicfdtd.f95:334),
+          // else the average the Fortran forms at :320, by the density method
+          if (legacy || i < 1 || k < 1)
+            out[8][n] = (float)(dt / rho[n]);
+          else
+            out[8][n] = (float)(dt / rho_avg(dm, 2, rho[n], at(rho, i - 1, k), at(rho, i, k - 1)));
+          if (i <= NX - 2 && k <= NZ - 2)  // vz: the average of :342, by the density method (:355)
+            out[9][n] = (float)(dt / rho_avg(dm, 2, rho[n], at(rho, i + 1, k), at(rho, i, k + 1)));
           out[10][n] = (float)(1.0 - gx[n]);
           out[11][n] = (float)(1.0 - gz[n]);
           if (gx[n] != 0.0 || gz[n] != 0.0) a = 1;
@@ -1100,12 +1140,13 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
         for (int i = 0; i < NX; ++i) {
           const size_t n = (size_t)i + (size_t)NX * k;
           const double r = rho[n];
-          if (i >= 1 && k >= 1)  // seismicfdtd.f95:826
-            out[33][n] = (float)(dt / ((4 * r + at(rho, i - 1, k) + at(rho, i, k - 1)) / 6));
-          if (i <= NX - 2 && k >= 1)  // :851
-            out[34][n] = (float)(dt / ((4 * r + at(rho, i + 1, k) + at(rho, i, k - 1)) / 6));
-          if (i <= NX - 2 && k <= NZ - 2)  // :877
-            out[35][n] = (float)(dt / ((at(rho, i + 1, k) + at(rho, i, k + 1) + 4 * r) / 6));
+          const int dm = density_method(c.flags);
+          if (i >= 1 && k >= 1)  // seismicfdtd.f95:825
+            out[33][n] = (float)(dt / rho_avg(dm, 4, r, at(rho, i - 1, k), at(rho, i, k - 1)));
+          if (i <= NX - 2 && k >= 1)  // :850
+            out[34][n] = (float)(dt / rho_avg(dm, 4, r, at(rho, i + 1, k), at(rho, i, k - 1)));
+          if (i <= NX - 2 && k <= NZ - 2)  // :876
+            out[35][n] = (float)(dt / rho_avg(dm, 4, r, at(rho, i + 1, k), at(rho, i, k + 1)));
           for (int d = 0; d < 3; ++d) {
             const double g = P(22 + d)[n];
             out[36 + d][n] = (float)(1.0 - g);
@@ -1214,8 +1255,48 @@ int32_t sfd_set_source(sfd_handle* h, int32_t i, int32_t j, int32_t k, const dou
       for (int t = 0; t < nstep; ++t) amp[(size_t)q * c.nstep + t] = (float)(srcfn[(size_t)q * nstep + t] * c.dt / s);
     }
   }
+  if (h->have_ssrc && !same_source_cell(h, i, j, k))
+    return fail(SFD_ERR_BAD_ARG, "the force source must lie at the stress source's cell (%d,%d,%d)", h->s2.io.si,
+                h->s2.io.sj, h->s2.io.sk);
   CK(cudaMemcpyAsync(h->base + h->L.off_src, amp.data(), sizeof(float) * amp.size(), cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
+  set_io_source(h, i, j, k);
+  h->have_force_src = true;
+  invalidate_graph(h);
+  return SFD_OK;
+}
+
+int32_t sfd_set_stress_source(sfd_handle* h, int32_t i, int32_t j, int32_t k, const double* srcfn, int32_t ncomp,
+                              int32_t nstep) {
+  g_err.clear();
+  if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
+  const sfd_config& c = h->cfg;
+  const int ns = nstress(c.kind);
+  if (!ns) return fail(SFD_ERR_BAD_ARG, "stress sources apply to the seismic kinds only");
+  if (ncomp == 0) {  // remove the stress source
+    h->have_ssrc = false;
+    set_io_ssrc(h);
+    invalidate_graph(h);
+    return SFD_OK;
+  }
+  if (!srcfn) return fail(SFD_ERR_BAD_ARG, "NULL source");
+  if (ncomp != ns) return fail(SFD_ERR_BAD_ARG, "stress source needs %d components, got %d", ns, ncomp);
+  if (nstep < 1 || nstep > c.nstep) return fail(SFD_ERR_BAD_ARG, "source length %d outside [1, %d]", nstep, c.nstep);
+  const bool three = is3(c.kind);
+  if (i < 1 || i > c.nx - 3 || k < 1 || k > c.nz - 3 || (three && (j < 1 || j > c.ny - 3)) || (!three && j != 0))
+    return fail(SFD_ERR_BAD_ARG, "source cell (%d,%d,%d) must lie inside the grid, away from its outer two planes", i, j, k);
+  if (h->have_force_src && !same_source_cell(h, i, j, k))
+    return fail(SFD_ERR_BAD_ARG, "the stress source must lie at the force source's cell (%d,%d,%d)", h->s2.io.si,
+                h->s2.io.sj, h->s2.io.sk);
+  if (!all_finite(srcfn, (size_t)ncomp * nstep)) return fail(SFD_ERR_BAD_ARG, "source contains NaN or Inf");
+  std::vector<float> amp((size_t)ns * c.nstep, 0.0f);
+  for (int q = 0; q < ns; ++q)
+    for (int t = 0; t < nstep; ++t) amp[(size_t)q * c.nstep + t] = (float)(srcfn[(size_t)q * nstep + t] * c.dt);
+  CK(cudaMemcpyAsync(h->base + h->L.off_src + sizeof(float) * (size_t)nchan(c.kind) * c.nstep, amp.data(),
+                     sizeof(float) * amp.size(), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->have_ssrc = true;
+  set_io_ssrc(h);
   set_io_source(h, i, j, k);
   invalidate_graph(h);
   return SFD_OK;

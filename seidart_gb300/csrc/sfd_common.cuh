@@ -14,6 +14,7 @@
 //   axis tables  per axis 6 x n floats: 1/(delta K), a/delta, b, and the same
 //               for the half-node offset.
 #pragma once
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -66,6 +67,23 @@ __device__ __forceinline__ float nan_to_inf(float v) { return (v != v) ? __int_a
 // sqrt(2) (sqrt(3)); above 1e24 the exact 2-norm is returned, so the 1e25
 // threshold is tested exactly.  NaN propagates through the sum and comes back
 // as +inf.
+// Density at a staggered velocity point, from the cell's own value r and the
+// two neighbours a, b of the Fortran's averaging stencil, weights (w, 1, 1):
+// w = 2 in seismic2 (legacy/fortran/seismicfdtd.f95:320, 342), w = 4 in
+// seismic25 (:825, 850, 876).  method (sfd_config flags / SFD_FLAG_DENSITY_NONE):
+// 0 arithmetic (the Fortran's average), 1 none (r itself), 2 geometric,
+// 3 harmonic -- the density_method values the driver passes
+// (src/seidart/routines/classes.py:311, 910-924).  The host (sfd_set_model)
+// and the device (sfd_set_model_ids) evaluate the same FP64 expression.
+__host__ __device__ inline double rho_avg(int method, int w, double r, double a, double b) {
+  switch (method) {
+    case 1: return r;
+    case 2: return w == 2 ? sqrt(sqrt(r * r * a * b)) : cbrt(sqrt(r * r * r * r * a * b));
+    case 3: return (w + 2.0) / (w / r + 1.0 / a + 1.0 / b);
+  }
+  return (w * r + a + b) / (w + 2.0);
+}
+
 __device__ __forceinline__ float norm_monitor(float a, float b) {
   const float m = fabsf(a) + fabsf(b);
   return (m <= 1e24f) ? m : nan_to_inf(hypotf(a, b));

@@ -11,6 +11,10 @@ struct IoArgs {
   Ctl* ctl;
   float* slots;       // one norm slot per block of the second half-step kernel
   const float* src;   // [ncomp][nstep] amplitudes already scaled by dt/rho or dt/eps
+  // seismic stress source at the same cell, [ncomp][nstep] amplitudes scaled
+  // by dt (xx zz xz in 2-D; xx yy zz xy xz yz in 2.5-D), added to the
+  // stresses after the stress half-step; NULL when the handle has none
+  const float* ssrc;
   int nstep;
   int si, sj, sk;     // source cell
   const int* rec;     // [nrec][3]
@@ -45,8 +49,10 @@ struct Em2cArgs {
 struct Seis2Args {
   int NX, NZ, P, W;
   int atten;
+  int legacy;  // 1: the legacy loops' quirks (shared memory variables, b_x_half(j)); 0: corrected physics
   float *vx, *vz, *sxx, *szz, *sxz;
   float *m_vxx, *m_vzz, *m_vxz, *m_vzx;      // x, z, z, x strips
+  float *m2_vxx, *m2_vzz, *m2_vxz, *m2_vzx;  // the sigmaxz loop's own (corrected physics), same strips
   float *m_sxx_x, *m_szz_z, *m_sxz_x, *m_sxz_z;  // x, z, x, z strips
   // dt * averaged stiffness, formed in FP64: (c(i+1,j) + 2c(i,j) + c(i,j-1))/4
   // at the normal-stress points (seismicfdtd.f95:270-280) and
@@ -54,7 +60,7 @@ struct Seis2Args {
   const float *A11, *A13, *A15, *A33, *A35, *B15, *B35, *B55;
   const float *dtrx, *dtrz;                      // dt / rho, dt / rho_avg
   const float *gxp, *gzp;                        // 1 - gamma
-  const float* q3;                               // b_x_half indexed by the z index
+  const float* q3;                               // b_x_half indexed by the z index (legacy loop 1)
   AxisTab X, Z;
   IoArgs io;
 };
@@ -62,6 +68,7 @@ struct Seis2Args {
 struct Seis25Args {
   int NX, NY, NZ, P, W;
   int atten;
+  int legacy;  // 1: the legacy coefficient pairs of c16 and c45 (seismicfdtd.f95:657, 766); 0: Voigt pairs
   float *vx, *vy, *vz, *sxx, *syy, *szz, *sxy, *sxz, *syz;
   // velocity-gradient memory (shared by the four stress loops)
   float *m_vx_x, *m_vy_x, *m_vz_x;  // x-strip
@@ -112,10 +119,13 @@ struct Em2Step {
 struct Seis2Step {
   int NX, NZ, P, W;
   int atten;
+  int legacy;  // as Seis2Args
   const float *vx0, *vz0, *sxx0, *szz0, *sxz0;
   float *vx1, *vz1, *sxx1, *szz1, *sxz1;
   const float *m_vxx0, *m_vzz0, *m_vxz0, *m_vzx0;  // velocity-gradient memory, old
   float *m_vxx1, *m_vzz1, *m_vxz1, *m_vzx1;        // new
+  const float *m2_vxx0, *m2_vzz0, *m2_vxz0, *m2_vzx0;  // the sigmaxz loop's own (corrected physics), old
+  float *m2_vxx1, *m2_vzz1, *m2_vxz1, *m2_vzx1;        // new
   float *m_sxx_x, *m_szz_z, *m_sxz_x, *m_sxz_z;    // in place
   const float *A11, *A13, *A15, *A33, *A35, *B15, *B35, *B55, *dtrx, *dtrz, *gxp, *gzp, *q3;
   AxisTab X, Z;
@@ -133,7 +143,7 @@ struct MatTable {
 // electromag2 or seismic2 handle from a device material-id map; *bad is set
 // to 1 if an id is outside [0, nmat).
 void coef_from_ids(int kind, const int* ids, const MatTable& m, int NX, int NZ, int P, double dt, float* coef,
-                   size_t plane, int* bad, cudaStream_t s);
+                   size_t plane, int* bad, int flags, cudaStream_t s);
 
 // Launch geometry of a solver's two half-step kernels.
 struct Launch {

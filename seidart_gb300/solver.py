@@ -44,7 +44,9 @@ CHANNELS = {SEISMIC2: ["vx", "vz"], SEISMIC25: ["vx", "vy", "vz"],
             ELECTROMAG2C: ["Ex_re", "Ex_im", "Ez_re", "Ez_im"]}
 MEMORY = {
     ELECTROMAG2: ["dEx_dz", "dEz_dx", "dHy_dz", "dHy_dx"],
-    SEISMIC2: ["dvx_dx", "dvz_dz", "dvx_dz", "dvz_dx", "dsigmaxx_dx", "dsigmazz_dz", "dsigmaxz_dx", "dsigmaxz_dz"],
+    # the last four: the sigmaxz loop's own velocity-gradient memory (corrected physics)
+    SEISMIC2: ["dvx_dx", "dvz_dz", "dvx_dz", "dvz_dx", "dsigmaxx_dx", "dsigmazz_dz", "dsigmaxz_dx", "dsigmaxz_dz",
+               "dvx_dx_sxz", "dvz_dz_sxz", "dvx_dz_sxz", "dvz_dx_sxz"],
     SEISMIC25: ["dvx_dx", "dvx_dy", "dvx_dz", "dvy_dx", "dvy_dy", "dvy_dz", "dvz_dx", "dvz_dy", "dvz_dz",
                 "dsigmaxx_dx", "dsigmayy_dy", "dsigmazz_dz", "dsigmaxy_dx", "dsigmaxy_dy", "dsigmaxz_dx",
                 "dsigmaxz_dz", "dsigmayz_dy", "dsigmayz_dz"],
@@ -57,6 +59,18 @@ MEMORY = {
 
 FLAG_TWO_PASS = 1
 FLAG_STREAMING = 2
+FLAG_LEGACY_QUIRKS = 4
+# density_method (the driver's argument, src/seidart/routines/classes.py:311) -> flag bits
+DENSITY_FLAGS = {"arithmetic": 0, "none": 8, "geometric": 16, "harmonic": 24}
+
+
+def physics_flags(legacy: bool = False, density: str = "arithmetic") -> int:
+    """sfd_config flag bits of the seismic physics options: ``legacy`` keeps
+    the legacy Fortran loops' quirks (default: corrected physics), ``density``
+    is the density averaging method."""
+    if density not in DENSITY_FLAGS:
+        raise ValueError(f"density must be one of {sorted(DENSITY_FLAGS)}, got {density!r}")
+    return (FLAG_LEGACY_QUIRKS if legacy else 0) | DENSITY_FLAGS[density]
 
 
 def is_25d(kind: int) -> bool:
@@ -105,10 +119,21 @@ class FDTDSolver:
     ``nstep`` is the number of source samples (the run length); ``nrec`` the
     number of receivers.  The device state is allocated with torch on
     ``device`` and bound to the current torch stream of that device.
+
+    Seismic kinds: ``legacy`` reproduces the legacy Fortran loops' quirks
+    (shared CPML memory of the two seismic2 stress loops, b_x_half(j), vx
+    over the cell's own density; the seismic25 c16/c45 pairs) instead of the
+    default corrected physics; ``density`` is the density averaging method
+    ('arithmetic', 'none', 'geometric', 'harmonic').
     """
 
-    def __init__(self, grid: GridSpec, nstep: int, nrec: int, device="cuda", stream=None, flags: int = 0):
+    def __init__(self, grid: GridSpec, nstep: int, nrec: int, device="cuda", stream=None, flags: int = 0,
+                 legacy: bool = False, density: str = "arithmetic"):
         import torch
+        if grid.kind in (SEISMIC2, SEISMIC25):
+            flags = int(flags) | physics_flags(legacy, density)
+        elif legacy or density != "arithmetic":
+            raise ValueError("legacy and density apply to the seismic kinds only")
 
         self.grid = grid
         self.kind = grid.kind
@@ -184,6 +209,20 @@ class FDTDSolver:
             raise ValueError("srcfn must be (ncomp, nstep)")
         i, j, k = (int(v) for v in ijk)
         check(self._L.sfd_set_source(self._h, i, j, k, _dptr(s), s.shape[0], s.shape[1]))
+
+    def set_stress_source(self, ijk, srcfn) -> None:
+        """Seismic kinds: moment-tensor source at cell (i, j, k) (the force
+        source's cell) with time functions (ncomp, nstep): sigma xx, zz, xz in
+        2-D, xx, yy, zz, xy, xz, yz in 2.5-D; sigma_ij += srcfn[ij][t] dt
+        after each stress half-step.  None removes it."""
+        i, j, k = (int(v) for v in ijk)
+        if srcfn is None:
+            check(self._L.sfd_set_stress_source(self._h, i, j, k, None, 0, 0))
+            return
+        s = np.ascontiguousarray(srcfn, dtype=np.float64)
+        if s.ndim != 2:
+            raise ValueError("srcfn must be (ncomp, nstep)")
+        check(self._L.sfd_set_stress_source(self._h, i, j, k, _dptr(s), s.shape[0], s.shape[1]))
 
     def set_receivers(self, ijk) -> None:
         r = np.ascontiguousarray(np.asarray(ijk, dtype=np.int32).reshape(-1, 3))
@@ -309,22 +348,27 @@ class FDTDSolver:
 
 
 def run_shot(grid: GridSpec, planes, profiles, src_ijk, srcfn, rec_ijk, nsteps=None, device="cuda", ids=None,
-             table=None):
+             table=None, stress_srcfn=None, legacy: bool = False, density: str = "arithmetic"):
     """One complete shot: model + CPML + source + receivers in, traces out
     (host arrays both ways).  The model is ``planes``, or, with ``ids`` and
     ``table`` (``planes`` may then be None), a material-id map whose
-    coefficients are formed on the GPU.  Raises UnstableError like the
-    Fortran stop."""
+    coefficients are formed on the GPU.  Seismic kinds also take a stress
+    source (``stress_srcfn``, at the force source's cell) and the physics
+    options of :class:`FDTDSolver`.  Raises UnstableError like the Fortran
+    stop."""
     srcfn = np.asarray(srcfn, dtype=np.float64)
     nstep = srcfn.shape[1]
     rec = np.asarray(rec_ijk, dtype=np.int32).reshape(-1, 3)
-    with FDTDSolver(grid, nstep, rec.shape[0], device=device) as s:
+    opts = {"legacy": legacy, "density": density} if grid.kind in (SEISMIC2, SEISMIC25) else {}
+    with FDTDSolver(grid, nstep, rec.shape[0], device=device, **opts) as s:
         if ids is not None:
             s.set_model_ids(ids, table)
         else:
             s.set_model(planes)
         s.set_cpml(profiles)
         s.set_source(src_ijk, srcfn)
+        if stress_srcfn is not None:
+            s.set_stress_source(src_ijk, stress_srcfn)
         s.set_receivers(rec)
         s.run(nstep if nsteps is None else nsteps)
         s.status()

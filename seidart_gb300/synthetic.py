@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import math
 from dataclasses import dataclass, field
+from typing import Optional
 
 import numpy as np
 
@@ -31,10 +32,20 @@ class Case:
     rec_ijk: np.ndarray         # (nrec, 3) int32
     f0: float
     meta: dict = field(default_factory=dict)
+    # seismic kinds: stress source (3 | 6, nstep) at src_ijk, legacy quirks, density method
+    stress_srcfn: Optional[np.ndarray] = None
+    legacy: bool = False
+    density: str = "arithmetic"
 
     @property
     def nstep(self) -> int:
         return self.srcfn.shape[1]
+
+    def solver_options(self) -> dict:
+        """FDTDSolver keywords of the case's physics options."""
+        if self.grid.kind in (SEISMIC2, SEISMIC25):
+            return {"legacy": self.legacy, "density": self.density}
+        return {}
 
 
 def ricker(nstep: int, dt: float, f0: float, amp: float = 1.0) -> np.ndarray:
@@ -197,12 +208,16 @@ def electromag2_layers(nstep: int = 6000, src_x: int = 500, nx: int = 1000, nz: 
                 dict(vmax=vmax, layers=layer, ids=ids, table=table))
 
 
-def seismic25_ice(nstep: int = 3000, nx: int = 600, ny: int = 40, nz: int = 300, c: int = 15) -> Case:
+def seismic25_ice(nstep: int = 3000, nx: int = 600, ny: int = 40, nz: int = 300, c: int = 15,
+                  explosive: bool = True) -> Case:
     """2.5-D anisotropic elastic, 600x40x300, 1 m cells, 15-cell CPML, per-(x,z)
     hexagonal ice rotated by tilt U[0,30] deg / azimuth U[0,360) (seed 3),
-    gamma U[0,0.02] per axis (seed 4), 150 Hz Ricker at (300,20,150), CFL 1/sqrt(3),
-    100 receivers on the surface line y=20.  The legacy seismic25 injects forces
-    only, so the explosive source is applied as equal x, y, z force components."""
+    gamma U[0,0.02] per axis (seed 4), 150 Hz Ricker explosive source at
+    (300,20,150) (equal normal stress components, the driver's 'tnt' source,
+    src/seidart/routines/sourcefunction.py:305-311), CFL 1/sqrt(3), 100
+    receivers on the surface line y=20.  ``explosive=False`` applies the
+    wavelet as equal x, y, z forces instead (the legacy seismic25 injects
+    forces only)."""
     d = 1.0
     rng = np.random.default_rng(3)
     tilt = np.deg2rad(rng.uniform(0, 30, (nz, nx)))
@@ -223,11 +238,16 @@ def seismic25_ice(nstep: int = 3000, nx: int = 600, ny: int = 40, nz: int = 300,
     f0 = 150.0
     grid = GridSpec(SEISMIC25, NX, NZ, d, d, dt, c, ny=NY, dy=d)
     profiles = cp.build_profiles((NX, NY, NZ), (d, d, d), c, dt, f0, vmax, seismic=True)
-    w = ricker(nstep, dt, f0) / math.sqrt(3.0)
-    srcfn = np.stack([w, w, w])
     rec = np.array([[min(nx - 1, 6 * q) + c, 20 + c, c] for q in range(100)], dtype=np.int32)
-    return Case(f"seismic25 ice {nx}x{ny}x{nz}", grid, planes, profiles, (nx // 2 + c, 20 + c, nz // 2 + c),
-                srcfn, rec, f0, dict(vmax=vmax))
+    src = (nx // 2 + c, 20 + c, nz // 2 + c)
+    if explosive:
+        w = ricker(nstep, dt, f0)
+        z = np.zeros(nstep)
+        return Case(f"seismic25 ice {nx}x{ny}x{nz}", grid, planes, profiles, src, np.zeros((3, nstep)), rec, f0,
+                    dict(vmax=vmax), stress_srcfn=np.stack([w, w, w, z, z, z]))
+    w = ricker(nstep, dt, f0) / math.sqrt(3.0)
+    return Case(f"seismic25 ice {nx}x{ny}x{nz}", grid, planes, profiles, src, np.stack([w, w, w]), rec, f0,
+                dict(vmax=vmax))
 
 
 # ---------------------------------------------------------------------------

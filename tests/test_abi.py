@@ -33,7 +33,7 @@ def test_counts(L):
     assert L.sfd_model_planes(_lib.ELECTROMAG2) == 6
     assert L.sfd_model_planes(_lib.ELECTROMAG25) == 12
     assert L.sfd_num_fields(_lib.SEISMIC25) == 9 and L.sfd_num_channels(_lib.SEISMIC25) == 3
-    assert L.sfd_num_memory(_lib.SEISMIC2) == 8 and L.sfd_num_memory(_lib.ELECTROMAG25) == 12
+    assert L.sfd_num_memory(_lib.SEISMIC2) == 12 and L.sfd_num_memory(_lib.ELECTROMAG25) == 12
     assert L.sfd_version() >= 100
 
 

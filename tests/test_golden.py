@@ -4,11 +4,11 @@ parity tolerance (GPU)."""
 import numpy as np
 import pytest
 
-from golden.make_golden import SPECS, case_of, path_of
+from golden.make_golden import SPECS, VARIANTS, case_of, path_of
 from helpers import make_solver, rel_l2, run_oracle
 from seidart_gb300 import KIND_NAMES
 
-IDS = [f"{KIND_NAMES[s[0]]}_s{s[1]}" for s in SPECS]
+IDS = [f"{KIND_NAMES[s[0]]}_s{s[1]}{VARIANTS[s[7]][0]}" for s in SPECS]
 
 
 @pytest.mark.parametrize("spec", SPECS, ids=IDS)

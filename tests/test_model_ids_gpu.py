@@ -71,6 +71,42 @@ def test_id_map_matches_planes(gpu, kind, seed):
             assert np.array_equal(a.field(name), b.field(name)), name
 
 
+@pytest.mark.parametrize("kind,density,legacy", [(SEISMIC2, "geometric", False), (SEISMIC2, "harmonic", True),
+                                                  (SEISMIC2, "none", False), (SEISMIC25, "harmonic", False),
+                                                  (SEISMIC25, "geometric", True)])
+def test_id_map_matches_planes_with_physics_options(gpu, kind, density, legacy):
+    """The density methods and the legacy/corrected density of vx, formed on
+    the device from the ids and on the host from the planes.  Both evaluate
+    the same FP64 expression; the 2.5-D geometric mean goes through cbrt,
+    whose host and device results may differ in the last bit, so that case
+    is compared to 1e-6 instead of bit for bit."""
+    from helpers import rel_l2
+    from seidart_gb300.solver import FIELDS
+    three = kind == SEISMIC25
+    case, a, b, ids, table = _pair(kind, 7, nx=40 if three else 64, nz=34 if three else 52, nstep=60 if three else 100)
+    a.close()
+    b.close()
+    case.density, case.legacy = density, legacy
+    a = make_solver(case)
+    b = make_solver(case)
+    b.set_model_ids(ids, table)
+    b.set_source(case.src_ijk, case.srcfn)
+    exact = not (three and density == "geometric")
+    with a, b:
+        for s in (a, b):
+            s.run(case.nstep)
+            s.status()
+        if exact:
+            assert np.array_equal(a.traces(), b.traces())
+        else:
+            assert rel_l2(b.traces(), a.traces()) <= 1e-6
+        for name in FIELDS[kind]:
+            if exact:
+                assert np.array_equal(a.field(name), b.field(name)), name
+            else:
+                assert rel_l2(b.field(name), a.field(name)) <= 1e-6, name
+
+
 def test_bad_ids_and_tables_are_rejected(gpu):
     case, a, b, ids, table = _pair(SEISMIC2, 5, nstep=10)
     with a, b:

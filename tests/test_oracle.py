@@ -30,6 +30,45 @@ def test_loop_and_slice_restatements_agree(kind, fn, seed, nx, nz):
     assert rel_l2(tr, T) < 1e-13
 
 
+@pytest.mark.parametrize("legacy,density,stress", [(True, "arithmetic", False), (False, "geometric", True),
+                                                    (False, "harmonic", False), (False, "none", True)])
+@pytest.mark.parametrize("seed,nx,nz", [(3, 33, 28), (4, 24, 39)])
+def test_seismic2_physics_options_agree(legacy, density, stress, seed, nx, nz):
+    """The seismic2 physics options (legacy quirks or corrected physics,
+    density method, moment-tensor source) in the C++ loops and the numpy
+    slices."""
+    c = sy.small_case(SEISMIC2, seed=seed, nx=nx, nz=nz, npml=5, nstep=110)
+    c.legacy, c.density = legacy, density
+    if stress:
+        w = 1e6 * c.srcfn[0]
+        c.stress_srcfn = np.stack([w, 0.7 * w, -0.4 * w])
+    g = c.grid
+    st, tr, _, blew = run_oracle(c)
+    assert not blew
+    F, M, T = numpy_ref.seismic2(g.nx, g.nz, g.dx, g.dz, g.dt, cp.pack_profiles(c.profiles), c.planes,
+                                 (c.src_ijk[0], c.src_ijk[2]), c.srcfn, c.nstep, rec=c.rec_ijk, legacy=legacy,
+                                 density=density, stress_src=c.stress_srcfn)
+    assert rel_l2(st.fields, F) < 1e-12
+    assert rel_l2(st.memory, M, floor=1e-300) < 1e-12
+    assert rel_l2(tr, T) < 1e-12
+
+
+def test_seismic_physics_options_change_the_result():
+    """Each option changes the traces (so the tests above compare something):
+    the corrected physics against the legacy loops, each density method
+    against the others, and the stress source against none."""
+    base = sy.small_case(SEISMIC2, seed=5, nx=36, nz=30, npml=5, nstep=120)
+    _, ref, _, _ = run_oracle(base)
+    for legacy, density in [(True, "arithmetic"), (False, "none"), (False, "geometric"), (False, "harmonic")]:
+        c = sy.small_case(SEISMIC2, seed=5, nx=36, nz=30, npml=5, nstep=120)
+        c.legacy, c.density = legacy, density
+        assert rel_l2(run_oracle(c)[1], ref) > 1e-6, (legacy, density)
+    c = sy.small_case(SEISMIC2, seed=5, nx=36, nz=30, npml=5, nstep=120)
+    w = 1e6 * c.srcfn[0]
+    c.stress_srcfn = np.stack([w, w, 0 * w])
+    assert rel_l2(run_oracle(c)[1], ref) > 1e-3
+
+
 @pytest.mark.parametrize("seed,nx,nz", [(1, 37, 29), (2, 26, 41)])
 def test_complex_em_restatements_agree(seed, nx, nz):
     """electromag2c (complex permittivities): the C++ loops against the numpy
