@@ -12,8 +12,20 @@ Same argv and the same working-directory files as the backend that
 * material planes ``c11.dat ... c66.dat rho.dat`` (+ ``gamma_x/y/z.dat``) or
   ``e11.dat ... e33.dat s11.dat ... s33.dat`` (``classes.py:608-750``);
 * source time functions ``seismicsource{x,y,z}.dat`` /
-  ``electromagneticsource{x,y,z}.dat`` (``sourcefunction.py:354-372``);
+  ``electromagneticsource{x,y,z}.dat`` and the moment-tensor (stress) source
+  ``seismicsource{xx,yy,zz,xy,xz,yz}.dat`` (``sourcefunction.py:354-372``);
+  a 2-D model takes the in-plane xx, zz, xz components (yy, xy and yz do not
+  enter the x-z equations);
+* ``density_gradient.dat`` (``definitions.py:475-557``, the air-surface
+  density taper the driver writes, ``classes.py:525-533``): the interior
+  (nx, nz) factors, extended into the CPML by edge replication, multiply the
+  density of a seismic model;
 * initial conditions ``initialcondition{V|E}{x,y,z}.dat`` (``classes.py:882-898``).
+
+``density_method`` (``classes.py:311, 910-924``) selects the density
+averaging at the staggered velocity points (none, arithmetic, geometric,
+harmonic); ``--legacy-quirks`` reproduces the legacy Fortran loops' quirks
+instead of the default corrected physics (``SFD_FLAG_LEGACY_QUIRKS``).
 
 All are Fortran records, x fastest, full grid (CPML included).  The CPML
 profiles are computed from the project's CPML parameters in FP64
@@ -64,7 +76,7 @@ def parse_flag(args, name, default=None):
     return default
 
 
-def load_project(json_path, seismic: bool, workdir="."):
+def load_project(json_path, seismic: bool, workdir=".", density_gradient: bool = True):
     """Everything one run needs, read from the project JSON and the .dat files."""
     with open(json_path) as f:
         prj = json.load(f)
@@ -110,6 +122,32 @@ def load_project(json_path, seismic: bool, workdir="."):
         else:
             srcfn.append(np.zeros(nstep))
     srcfn = np.stack(srcfn)
+    stress = None
+    if seismic:  # moment-tensor source: the components the solver carries
+        names = ["xx", "yy", "zz", "xy", "xz", "yz"] if is_25d(kind) else ["xx", "zz", "xz"]
+        comps_s = []
+        for q in names:
+            fn = wd / f"seismicsource{q}.dat"
+            s = np.zeros(nstep)
+            if fn.exists():
+                v = fio.read_record(fn, np.float64)
+                if v.size < nstep:
+                    raise ProjectError(f"{fn}: {v.size} samples, need {nstep}")
+                s = v[:nstep]
+            comps_s.append(s)
+        if any(np.any(s) for s in comps_s):
+            stress = np.stack(comps_s)
+        gfile = wd / "density_gradient.dat"
+        if density_gradient and gfile.exists():
+            g = fio.read_record(gfile, np.float64)
+            ni, nk = nx - 2 * c, nz - 2 * c
+            if g.size != ni * nk:
+                raise ProjectError(f"{gfile}: {g.size} values, need {ni} x {nk}")
+            if not np.all(np.isfinite(g)) or np.any(g <= 0):
+                raise ProjectError(f"{gfile}: density factors must be positive")
+            # the driver's (nx, nz) array (written without a transpose) -> (nz, nx), then the CPML
+            fac = np.pad(g.reshape(ni, nk).T, c, mode="edge")
+            planes[MODEL_PLANES[kind].index("rho")] *= fac
     xind, yind, zind = int(src.get("xind", 0)), int(src.get("yind", 0)), int(src.get("zind", 0))
     src_ijk = (xind + c, (yind + c) if is_25d(kind) else 0, zind + c)
     init = {}
@@ -123,19 +161,25 @@ def load_project(json_path, seismic: bool, workdir="."):
                 init[ch] = a.reshape(fshape)
     f0 = float(src.get("source_frequency", 1.0))
     params = {k: float(dom[k]) for k in ("alpha_max_scalar", "kappa_max", "NP", "NPA", "Rcoef") if k in dom}
-    vmax = max_speed(kind, planes)
+    vmax, axis_v = max_speed(kind, planes, per_axis=True)
     deltas = (dx, dy, dz) if is_25d(kind) else (dx, dz)
     shape = (nx, ny, nz) if is_25d(kind) else (nx, nz)
-    profiles = cp.build_profiles(shape, deltas, c, dt, f0, vmax, seismic=seismic, params=params)
+    # the driver's seismic sigma_max of an axis takes the largest speed along it (definitions.py:613-661)
+    profiles = cp.build_profiles(shape, deltas, c, dt, f0, vmax, seismic=seismic, params=params,
+                                 axis_vmax=axis_v if seismic else None)
     return dict(kind=kind, grid=grid, planes=planes, profiles=profiles, srcfn=srcfn, src_ijk=src_ijk,
-                init=init, nstep=nstep, xind=xind, yind=yind, zind=zind, seismic=seismic, vmax=vmax)
+                init=init, nstep=nstep, xind=xind, yind=yind, zind=zind, seismic=seismic, vmax=vmax,
+                stress_srcfn=stress)
 
 
-def max_speed(kind, planes):
-    """Largest wave speed of the model (the driver's global CPML velocity)."""
+def max_speed(kind, planes, per_axis=False):
+    """Largest wave speed of the model over the driver's direction set, and
+    with ``per_axis`` also the largest speed along each axis (x, [y,] z), the
+    velocities the driver's seismic CPML takes (definitions.py:613-661)."""
     if kind in (ELECTROMAG2, ELECTROMAG25):
         eps = planes[[0, 2]] if kind == ELECTROMAG2 else planes[[0, 3, 5]]
-        return cp.CLIGHT / math.sqrt(max(float(eps.min()), 1e-30))
+        v = cp.CLIGHT / math.sqrt(max(float(eps.min()), 1e-30))
+        return (v, None) if per_axis else v
     names = MODEL_PLANES[kind]
     idx = {n: q for q, n in enumerate(names)}
     rho = planes[idx["rho"]].ravel()
@@ -149,7 +193,8 @@ def max_speed(kind, planes):
     if len(uniq) > 4096:  # per-cell random media: a strided sample bounds the cost
         uniq = uniq[:: max(1, len(uniq) // 4096)]
     dim = 2.5 if kind == SEISMIC25 else 2
-    best = 0.0
+    axes = ("x", "y", "z") if kind == SEISMIC25 else ("x", "z")
+    best, along = 0.0, [0.0] * len(axes)
     for row in uniq:
         C6 = np.zeros((6, 6))
         for v, n in zip(row[:-1], cols):
@@ -160,7 +205,9 @@ def max_speed(kind, planes):
             C6[1, 2], C6[2, 1], C6[3, 3], C6[5, 5] = C6[0, 2], C6[0, 2], C6[4, 4], C6[4, 4]
         if row[-1] > 0:
             best = max(best, cp.max_velocity(C6, row[-1], dim))
-    return best
+            for q, ax in enumerate(axes):
+                along[q] = max(along[q], cp.axis_velocity(C6, row[-1], ax))
+    return (best, tuple(along)) if per_axis else best
 
 
 def read_receivers(path, grid):
@@ -329,18 +376,24 @@ def run(argv=None) -> int:
     ap.add_argument("--receivers", help="receiver CSV (X,Y,Z in metres)")
     ap.add_argument("--traces", help="write receiver traces (nstep, channel, receiver) to this .npy")
     ap.add_argument("--device", default="cuda")
+    ap.add_argument("--legacy-quirks", action="store_true",
+                    help="seismic: reproduce the legacy Fortran loops' quirks instead of the corrected physics")
+    ap.add_argument("--no-density-gradient", action="store_true",
+                    help="seismic: ignore density_gradient.dat")
     a = ap.parse_args(argv)
     seismic = str(parse_flag(a.flags, "seismic", "true")).lower() in ("true", "1", "yes")
     density = str(parse_flag(a.flags, "density_method", "arithmetic")).lower()
+    from .solver import DENSITY_FLAGS, FDTDSolver
+    if density not in DENSITY_FLAGS:
+        print(f"seidartfdtd: density_method={density}: expected one of {', '.join(sorted(DENSITY_FLAGS))}",
+              file=sys.stderr)
+        return 1
     try:
-        p = load_project(a.project, seismic, a.workdir)
+        p = load_project(a.project, seismic, a.workdir, density_gradient=not a.no_density_gradient)
     except (ProjectError, ValueError, KeyError, OSError) as e:
         print(f"seidartfdtd: {e}", file=sys.stderr)
         return 1
-    if density not in ("none", "arithmetic"):
-        print(f"seidartfdtd: density_method={density}: the solver uses the staggered arithmetic density "
-              "averages of the reference loops (seismicfdtd.f95:341, 826-877)", file=sys.stderr)
-    from .solver import FDTDSolver
+    opts = {"legacy": a.legacy_quirks, "density": density} if seismic else {}
     grid = p["grid"]
     rec = read_receivers(a.receivers, grid) if a.receivers else np.zeros((0, 3), np.int32)
     every = max(0, int(a.snapshot_every))
@@ -350,10 +403,12 @@ def run(argv=None) -> int:
               "(seismic=false on a 2.5-D project, --snapshot-every 1)", file=sys.stderr)
         return 1
     try:
-        with FDTDSolver(grid, p["nstep"], len(rec), device=a.device) as s:
+        with FDTDSolver(grid, p["nstep"], len(rec), device=a.device, **opts) as s:
             s.set_model(p["planes"])
             s.set_cpml(p["profiles"])
             s.set_source(p["src_ijk"], p["srcfn"])
+            if p["stress_srcfn"] is not None:
+                s.set_stress_source(p["src_ijk"], p["stress_srcfn"])
             if len(rec):
                 s.set_receivers(rec)
             for ch, v in p["init"].items():

@@ -56,6 +56,27 @@ def ricker(nstep: int, dt: float, f0: float, amp: float = 1.0) -> np.ndarray:
     return amp * x / np.max(np.abs(x))
 
 
+def wavelet(t: np.ndarray, f: float, stype: str = "gaus1") -> np.ndarray:
+    """The driver's Gaussian source wavelets at times t, peak-normalised
+    (sourcefunction.py:25-57): 'gaus0' a Gaussian of width 0.2/(pi f),
+    'gaus1' the Ricker wavelet, 'gaus2' the second derivative form; each
+    centred on t0 = 1/f."""
+    t0 = 1.0 / f
+    if stype == "gaus0":
+        a = (t - t0) / (0.2 / (math.pi * f))
+        x = np.exp(-a * a)
+    elif stype == "gaus1":
+        a = math.pi * f * (t - t0)
+        x = (1.0 - 2.0 * a * a) * np.exp(-a * a)
+    elif stype == "gaus2":
+        k = math.pi * math.pi * f * f
+        d = t - t0
+        x = 2.0 * k * d * (2.0 * k * d * d - 3.0) * np.exp(-k * d * d)
+    else:
+        raise ValueError(f"unknown wavelet {stype!r}")
+    return x / np.max(np.abs(x))
+
+
 def extend_cpml(interior: np.ndarray, npml: int) -> np.ndarray:
     """(nz, nx) interior -> (nz+2c, nx+2c) by edge replication (classes.py:660-674)."""
     return np.pad(interior, npml, mode="edge")

@@ -13,7 +13,10 @@ FILE_OF = {"eps11": "e11", "eps12": "e12", "eps13": "e13", "eps22": "e22", "eps2
            "sig11": "s11", "sig12": "s12", "sig13": "s13", "sig22": "s22", "sig23": "s23", "sig33": "s33"}
 
 
-def write_project(case, workdir, receivers_m=None):
+def write_project(case, workdir, receivers_m=None, stress=None, density_gradient=None):
+    """``stress``: dict of seismicsource{xx,yy,zz,xy,xz,yz}.dat time series to
+    write; ``density_gradient``: the interior (nx, nz) factors the driver's
+    airsurf writes (definitions.py:475-557), saved the way it saves them."""
     g = case.grid
     c = g.npml
     seismic = g.kind in (SEISMIC2, SEISMIC25)
@@ -35,6 +38,13 @@ def write_project(case, workdir, receivers_m=None):
     comps = ["x", "y", "z"] if three else ["x", "z"]
     for q, s in zip(comps, case.srcfn):
         fio.write_record(f"{workdir}/{stem}{q}.dat", s, np.float64)
+    for name, series in (stress or {}).items():
+        fio.write_record(f"{workdir}/seismicsource{name}.dat", np.asarray(series), np.float64)
+    if density_gradient is not None:  # a C-order (nx, nz) record, no transpose (definitions.py:554-556)
+        g = np.ascontiguousarray(density_gradient, dtype=np.float64)
+        with open(f"{workdir}/density_gradient.dat", "wb") as f:
+            n = np.array([g.nbytes], dtype=np.int32).tobytes()
+            f.write(n + g.tobytes() + n)
     if receivers_m is not None:
         with open(f"{workdir}/receivers.csv", "w") as f:
             f.write("X,Y,Z\n")

@@ -70,3 +70,56 @@ def test_cli_run_matches_oracle(gpu, tmp_path, kind):
     assert [os.path.basename(f).split(".")[1] for f in files] == ["000020", "000040", "000060"]
     last = fio.read_record(files[-1], np.float32).reshape(g.nz, g.nx)
     assert rel_l2(last, st.fields[0]) <= 1e-5
+
+
+def _gradient(case):
+    """An air-surface style taper: 0.15 and 0.575 in the top two interior rows."""
+    c = case.grid.npml
+    ni, nk = case.grid.nx - 2 * c, case.grid.nz - 2 * c
+    g = np.ones((ni, nk))
+    g[:, 0], g[:, 1] = 0.15, 0.575
+    return g
+
+
+def test_load_project_density_gradient_and_stress(tmp_path):
+    case = sy.small_case(SEISMIC2, seed=4, nx=40, nz=34, npml=5, nstep=60)
+    w = case.srcfn[1]
+    path, _ = write_project(case, tmp_path, stress={"xx": w, "yy": 2 * w, "zz": 3 * w, "xz": 0.5 * w},
+                            density_gradient=_gradient(case))
+    p = cli.load_project(path, seismic=True, workdir=tmp_path)
+    rho = case.planes[6].copy()
+    rho[:6, :] *= 0.15  # CPML rows take the edge row's factor
+    rho[6, :] *= 0.575
+    assert np.allclose(p["planes"][6], rho, rtol=0, atol=0)
+    assert np.array_equal(p["stress_srcfn"], np.stack([w, 3 * w, 0.5 * w]))  # xx zz xz in 2-D
+    q = cli.load_project(path, seismic=True, workdir=tmp_path, density_gradient=False)
+    assert np.array_equal(q["planes"][6], case.planes[6])
+
+
+def test_unknown_density_method_is_an_input_error(tmp_path):
+    case = sy.small_case(SEISMIC2, seed=2, nx=40, nz=34, npml=5, nstep=60)
+    path, _ = write_project(case, tmp_path)
+    assert cli.run([path, "seismic=true", "density_method=cubic", "--workdir", str(tmp_path)]) == 1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("density,legacy", [("geometric", False), ("harmonic", True), ("none", False),
+                                            ("arithmetic", False)])
+def test_cli_seismic_options_match_oracle(gpu, tmp_path, density, legacy):
+    """A default SeidarT seismic project: density_method, density_gradient.dat
+    and a moment-tensor source, with and without --legacy-quirks."""
+    case = sy.small_case(SEISMIC2, seed=5, nx=44, nz=38, npml=5, nstep=80)
+    g = case.grid
+    w = 1e6 * case.srcfn[1]
+    rec_m = [((i - g.npml + 0.25) * g.dx, 0.0, (k - g.npml + 0.25) * g.dz) for i, k in ((10, 12), (30, 20), (18, 9))]
+    path, _ = write_project(case, tmp_path, receivers_m=rec_m, stress={"xx": w, "zz": w, "yy": w},
+                            density_gradient=_gradient(case))
+    args = [path, "seismic=true", f"density_method={density}", "--workdir", str(tmp_path), "--snapshot-every", "0",
+            "--receivers", str(tmp_path / "receivers.csv"), "--traces", str(tmp_path / "traces.npy")]
+    assert cli.run(args + (["--legacy-quirks"] if legacy else [])) == 0
+    p = cli.load_project(path, True, tmp_path)
+    rec = cli.read_receivers(tmp_path / "receivers.csv", g)
+    from oracle import run as orun
+    _, tr, _, _ = orun(SEISMIC2, g, p["planes"], cp.pack_profiles(p["profiles"]), p["src_ijk"], p["srcfn"], rec,
+                       case.nstep, legacy=legacy, density=density, stress_src=p["stress_srcfn"])
+    assert rel_l2(np.load(tmp_path / "traces.npy"), tr) <= 1e-5
