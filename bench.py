@@ -556,6 +556,36 @@ def cpu_baseline(case, seconds=10.0, chunk=100):
             "sample": f"{done} of {case.nstep} steps of the same workload, FP64, OpenMP ({el:.1f} s)"}
 
 
+def cpu_baseline_snapshots(case, steps=100):
+    """The FP64 oracle with the reference's per-step output: after every step
+    one full-field FP32 record per channel (write_image2,
+    readwrite_routines.f95:473-499, called each step at
+    electromagfdtd.f95:323).  The two parts run one after the other in the
+    reference, so each is timed on its own over ``steps`` steps of the
+    workload and the times are added: the oracle advancing the steps in one
+    call, and the records of every step written to a scratch directory."""
+    import oracle
+    from seidart_gb300 import cpml as cp, fortran_io as fio
+    prof = cp.pack_profiles(case.profiles)
+    oracle.lib(native=True)  # built before the timed region
+    t0 = time.perf_counter()
+    st, _, _, _ = oracle.run(case.grid.kind, case.grid, case.planes, prof, case.src_ijk, case.srcfn, case.rec_ijk,
+                             steps, native=True)
+    t_comp = time.perf_counter() - t0
+    with tempfile.TemporaryDirectory() as td:
+        t0 = time.perf_counter()
+        for t in range(steps):
+            for q, ch in enumerate(("Ex", "Ez")):
+                fio.write_record(Path(td) / f"{ch}.{t + 1:06d}.500.25.dat", st.fields[q].astype(np.float32),
+                                 np.float32)
+        t_write = time.perf_counter() - t0
+    value = case.grid.cells * steps / (t_comp + t_write) / 1e9
+    return {"value": round(value, 4), "unit": METRIC, "cores": oracle.num_threads(), "kind": "port",
+            "cpu": cpu_model(), "build": oracle.NATIVE_FLAGS,
+            "sample": f"{steps} of {case.nstep} steps: compute {t_comp:.2f} s plus a full-field FP32 record of Ex "
+                      f"and Ez per step, {t_write:.2f} s (timed apart, added)"}
+
+
 def run_reference(args):
     """--impl reference: the reference algorithm (FP64 oracle port) on the host cores."""
     rank = int(os.environ.get("RANK", "0"))
@@ -775,6 +805,7 @@ def run_ours(args):
 
     if rank == 0 and not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline(case, seconds=args.cpu_seconds)
+        line["cpu_baseline"]["with_snapshot_writes"] = cpu_baseline_snapshots(case)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

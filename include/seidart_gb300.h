@@ -259,6 +259,13 @@ int32_t sfd_status(sfd_handle* h, int64_t* step, double* maxnorm);
  * (count = nstep*nchan*nrec) or the device pointer. */
 int32_t sfd_get_traces(sfd_handle* h, float* host, int64_t count);
 const float* sfd_traces_device(const sfd_handle* h);
+/* Device address of field `field` of the handle's current state and its row
+ * pitch in floats (x fastest; row (k) of a 2-D field, row (k, j) of a 2.5-D
+ * field at ptr + (k*NY + j) * pitch; the NX cells of a row are valid, the
+ * rest of the pitch is padding).  For a zero-copy view; single-pass 2-D
+ * handles swap between two copies, so the address holds until the next
+ * sfd_run, sfd_reset or sfd_checkpoint_load. */
+int32_t sfd_field_device(const sfd_handle* h, int32_t field, float** ptr, int64_t* pitch);
 
 /* Profiling aid: launch half-step kernel `which` (0 = first half-step of the
  * Fortran time loop: H or stress; 1 = second: E or velocity) `count` times

@@ -25,7 +25,7 @@ EXPORTS = (
     "sfd_num_memory", "sfd_state_bytes", "sfd_create", "sfd_set_model", "sfd_set_model_ids", "sfd_set_cpml",
     "sfd_set_source", "sfd_set_stress_source", "sfd_share_model", "sfd_set_receivers", "sfd_reset", "sfd_set_field", "sfd_get_field",
     "sfd_get_field_async", "sfd_encode_field_i16",
-    "sfd_get_memory", "sfd_run", "sfd_status", "sfd_get_traces", "sfd_traces_device", "sfd_launch_half",
+    "sfd_get_memory", "sfd_run", "sfd_status", "sfd_get_traces", "sfd_traces_device", "sfd_field_device", "sfd_launch_half",
     "sfd_on_chip", "sfd_set_wait_limit", "sfd_test_stall_waits",
     "sfd_destroy", "sfd_checkpoint_bytes", "sfd_checkpoint_save", "sfd_checkpoint_load", "sfd_adjoint_bytes",
     "sfd_adjoint_begin", "sfd_adjoint_segment", "sfd_adjoint_gradient", "sfd_batch_scratch_bytes", "sfd_batch_create", "sfd_batch_set_tiling", "sfd_batch_run",
@@ -89,6 +89,7 @@ def _declare(lib):
         "sfd_status": (i32, [P, C.POINTER(i64), dp]),
         "sfd_get_traces": (i32, [P, fp, i64]),
         "sfd_traces_device": (P, [P]),
+        "sfd_field_device": (i32, [P, i32, C.POINTER(P), C.POINTER(i64)]),
         "sfd_launch_half": (i32, [P, i32, i32]),
         "sfd_on_chip": (i32, [P, ip, ip]),
         "sfd_set_wait_limit": (i32, [P, i64]),

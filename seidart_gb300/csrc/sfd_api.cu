@@ -1529,6 +1529,15 @@ const float* sfd_traces_device(const sfd_handle* h) {
   return h ? (const float*)(h->base + h->L.off_traces) : nullptr;
 }
 
+int32_t sfd_field_device(const sfd_handle* h, int32_t field, float** ptr, int64_t* pitch) {
+  g_err.clear();
+  if (!h || !ptr) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  if (field < 0 || field >= nfields(h->cfg.kind)) return fail(SFD_ERR_BAD_ARG, "field %d out of range", field);
+  *ptr = h->f(field);
+  if (pitch) *pitch = h->L.P;
+  return SFD_OK;
+}
+
 int32_t sfd_destroy(sfd_handle* h) {
   g_err.clear();
   if (!h) return SFD_OK;

@@ -321,6 +321,22 @@ class FDTDSolver:
         check(self._L.sfd_get_traces(self._h, _fptr(out), out.size))
         return out
 
+    def field_tensor(self, name):
+        """Device view (no copy) of field ``name`` of the current state:
+        (NZ, NX) in 2-D, (NZ, NY, NX) in 2.5-D, a strided view into the state
+        buffer (rows padded to the library's pitch).  The view holds until the
+        next ``run``, ``reset`` or checkpoint load: single-pass 2-D solvers
+        alternate between two copies of their fields."""
+        import torch
+        q = FIELDS[self.kind].index(name) if isinstance(name, str) else int(name)
+        ptr, pitch = C.c_void_p(), C.c_int64()
+        check(self._L.sfd_field_device(self._h, q, C.byref(ptr), C.byref(pitch)))
+        off = (int(ptr.value) - self.state.data_ptr()) // 4
+        g = self.grid
+        rows = g.nz * (g.ny if is_25d(self.kind) else 1)
+        flat = self.state.view(torch.float32)[off: off + rows * pitch.value].view(rows, pitch.value)[:, :g.nx]
+        return flat.view(g.nz, g.ny, g.nx) if is_25d(self.kind) else flat
+
     def traces_tensor(self):
         """Device view (nstep, nch, nrec) of the trace buffer (no copy)."""
         import torch
