@@ -93,6 +93,12 @@ extern "C" {
 #define SFD_FLAG_DENSITY_GEOMETRIC 16
 #define SFD_FLAG_DENSITY_HARMONIC 24
 #define SFD_FLAG_DENSITY_MASK 24
+/* electromag2 and seismic2: CPML coefficients from the driver's 2-D fields
+ * (sfd_set_cpml2d) instead of per-axis profiles (sfd_set_cpml): every
+ * derivative direction takes the field's value at the cell.  The run uses
+ * two kernels per step with every CPML memory variable on the full grid;
+ * not with SFD_FLAG_LEGACY_QUIRKS (whose loops read 1-D profiles). */
+#define SFD_FLAG_CPML_2D 32
 
 
 typedef struct sfd_config {
@@ -181,6 +187,15 @@ int32_t sfd_set_model_ids(sfd_handle* h, const int32_t* ids, int32_t nmat, const
  * (seismicfdtd.f95:202-220).  a and a_half must vanish outside the npml-cell
  * strips at both ends of each axis. */
 int32_t sfd_set_cpml(sfd_handle* h, const double* profiles, int64_t count);
+
+/* SFD_FLAG_CPML_2D handles: the driver's 2-D CPML fields, host FP64, six
+ * planes of NX*NZ values (x fastest): K, a, b, K_half, a_half, b_half
+ * (count = 6*NX*NZ) -- the kappa, acoef, bcoef{,_half}_cpml.dat files the
+ * current driver writes (src/seidart/routines/definitions.py:560-998; their
+ * records hold the (NX, NZ) arrays x fastest).  The full-offset field is
+ * used where the Fortran loops read a full-offset profile, the half-offset
+ * field where they read a half-offset one.  K must be positive. */
+int32_t sfd_set_cpml2d(sfd_handle* h, const double* fields, int64_t count);
 
 /* Point source at full-grid cell (i, j, k) (j = 0 in 2-D) with time
  * functions srcfn, host FP64, ncomp x nstep values, component-major

@@ -55,9 +55,9 @@ def lib(native: bool = False):
             dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
             i, d = C.c_int, C.c_double
             common_tail = [dp, dp, i, i, dp, i, i, i, dp, dp, i, ip, dp, dp, ip]
-            L.orc_electromag2.argtypes = [i, i, d, d, d] + common_tail
+            L.orc_electromag2.argtypes = [i, i, d, d, d] + common_tail + [dp]
             L.orc_electromag2c.argtypes = [i, i, d, d, d] + common_tail
-            L.orc_seismic2.argtypes = [i, i, d, d, d] + common_tail + [i, dp]
+            L.orc_seismic2.argtypes = [i, i, d, d, d] + common_tail + [i, dp, dp]
             tail3 = [dp, dp, i, i, i, dp, i, i, i, dp, dp, i, ip, dp, dp, ip]
             L.orc_seismic25.argtypes = [i, i, i, d, d, d, d] + tail3 + [i, dp]
             L.orc_electromag25.argtypes = [i, i, i, d, d, d, d] + tail3
@@ -87,16 +87,28 @@ def _d(a):
 
 
 def run(kind, grid, planes, packed_profiles, src_ijk, srcfn, rec_ijk, nsteps, state: OracleState = None,
-        native: bool = False, legacy: bool = False, density: str = "arithmetic", stress_src=None):
+        native: bool = False, legacy: bool = False, density: str = "arithmetic", stress_src=None, cpml2d=None):
     """Advance ``nsteps`` steps of the FP64 oracle.  Returns (state, traces,
     maxnorm, blew_up); traces is (nsteps, nch, nrec).  ``native`` runs the
     host-tuned build (timing only).  Seismic kinds: ``legacy`` keeps the
     legacy Fortran's quirks (default: corrected physics), ``density`` is the
     density method ('arithmetic', 'none', 'geometric', 'harmonic') and
     ``stress_src`` the stress source time functions (NSTRESS[kind] x nstep,
-    same cell as the force source) or None."""
+    same cell as the force source) or None.  ``cpml2d``: electromag2 and
+    seismic2 only, the driver's 2-D CPML fields (6, NZ, NX): K, a, b,
+    K_half, a_half, b_half, used for every derivative direction in place of
+    the per-axis profiles (which are then ignored)."""
     L = lib(native)
     opts = (1 if legacy else 0) | (DENSITY[density] << 1)
+    f2 = None
+    if cpml2d is not None:
+        if kind not in (ELECTROMAG2, SEISMIC2):
+            raise ValueError("2-D CPML fields apply to electromag2 and seismic2")
+        if legacy:
+            raise ValueError("the legacy loops read 1-D CPML profiles")
+        f2 = np.ascontiguousarray(cpml2d, dtype=np.float64)
+        if f2.shape != (6, grid.nz, grid.nx):
+            raise ValueError("cpml2d must be (6, NZ, NX)")
     ssrc = None
     if stress_src is not None:
         ssrc = np.ascontiguousarray(stress_src, dtype=np.float64)
@@ -119,7 +131,7 @@ def run(kind, grid, planes, packed_profiles, src_ijk, srcfn, rec_ijk, nsteps, st
     if kind == ELECTROMAG2:
         n = L.orc_electromag2(grid.nx, grid.nz, grid.dx, grid.dz, grid.dt, _d(prof), _d(planes), i, k, _d(srcfn),
                               srcfn.shape[1], state.step, nsteps, _d(state.fields), _d(state.memory), nrec, recp,
-                              _d(traces), C.byref(maxnorm), C.byref(blew))
+                              _d(traces), C.byref(maxnorm), C.byref(blew), _d(f2) if f2 is not None else None)
     elif kind == ELECTROMAG2C:
         n = L.orc_electromag2c(grid.nx, grid.nz, grid.dx, grid.dz, grid.dt, _d(prof), _d(planes), i, k, _d(srcfn),
                                srcfn.shape[1], state.step, nsteps, _d(state.fields), _d(state.memory), nrec, recp,
@@ -128,7 +140,7 @@ def run(kind, grid, planes, packed_profiles, src_ijk, srcfn, rec_ijk, nsteps, st
         n = L.orc_seismic2(grid.nx, grid.nz, grid.dx, grid.dz, grid.dt, _d(prof), _d(planes), i, k, _d(srcfn),
                            srcfn.shape[1], state.step, nsteps, _d(state.fields), _d(state.memory), nrec, recp,
                            _d(traces), C.byref(maxnorm), C.byref(blew), opts,
-                           _d(ssrc) if ssrc is not None else None)
+                           _d(ssrc) if ssrc is not None else None, _d(f2) if f2 is not None else None)
     elif kind == SEISMIC25:
         n = L.orc_seismic25(grid.nx, grid.ny, grid.nz, grid.dx, grid.dy, grid.dz, grid.dt, _d(prof), _d(planes),
                             i, j, k, _d(srcfn), srcfn.shape[1], state.step, nsteps, _d(state.fields),

@@ -80,25 +80,28 @@ static double rho_avg(int method, double w, double r, double a, double b) {
 
 }  // namespace
 
-extern "C" {
-
-// ---------------------------------------------------------------------------
-// electromag2: legacy/fortran/electromagfdtd.f95:10-326.
-//   mat   = eps11, eps13, eps33, sig11, sig13, sig33   (6 x NX*NZ)
-//   fld   = Ex, Ez, Hy                                  (3 x NX*NZ)
-//   mem   = dEx_dz, dEz_dx, dHy_dz, dHy_dx              (4 x NX*NZ)
-//   src   = srcx, srcz                                  (2 x nstep_src)
-//   chans = Ex, Ez
-// Returns the number of steps completed; *blew_up = 1 if the norm check of
-// electromagfdtd.f95:320-321 fired (the run stops there, as the Fortran does).
-int orc_electromag2(int NX, int NZ, double dx, double dz, double dt,
+template <bool TWO_D>
+static int electromag2_impl(int NX, int NZ, double dx, double dz, double dt,
                     const double* prof, const double* mat,
                     int isrc, int ksrc, const double* src, int nstep_src,
                     int it0, int nsteps,
                     double* fld, double* mem,
                     int nrec, const int* rec, double* traces,
-                    double* maxnorm, int* blew_up) {
+                    double* maxnorm, int* blew_up, const double* cpml2d) {
   const size_t N = (size_t)NX * NZ;
+
+  // CPML coefficient q (K a b K_half a_half b_half) of the x (z) axis at cell
+  // (i, k): the axis profile at i (k), or, with the driver's 2-D fields
+  // (TWO_D), the field's value at the cell -- the same field for every
+  // derivative direction
+  auto XP = [&](const double* ax, int q, int i, int k) -> double {
+    if constexpr (TWO_D) return cpml2d[(size_t)q * N + (size_t)i + (size_t)NX * k];
+    else return ax[i];
+  };
+  auto ZP = [&](const double* ax, int q, int i, int k) -> double {
+    if constexpr (TWO_D) return cpml2d[(size_t)q * N + (size_t)i + (size_t)NX * k];
+    else return ax[k];
+  };
   Axis X, Y, Z;
   unpack_axes(prof, NX, 1, NZ, false, &X, &Y, &Z);
   const double *eps11 = mat, *eps13 = mat + N, *eps33 = mat + 2 * N;
@@ -131,11 +134,11 @@ int orc_electromag2(int NX, int NZ, double dx, double dz, double dt,
       for (int i = 0; i <= NX - 2; ++i) {
         const size_t c = I(i, k);
         double dEx_dz = (Ex[I(i, k + 1)] - Ex[c]) / dz;
-        mExz[c] = Z.b[k] * mExz[c] + Z.a[k] * dEx_dz;
-        dEx_dz = dEx_dz / Z.K[k] + mExz[c];
+        mExz[c] = ZP(Z.b, 2, i, k) * mExz[c] + ZP(Z.a, 1, i, k) * dEx_dz;
+        dEx_dz = dEx_dz / ZP(Z.K, 0, i, k) + mExz[c];
         double dEz_dx = (Ez[I(i + 1, k)] - Ez[c]) / dx;
-        mEzx[c] = X.b[i] * mEzx[c] + X.a[i] * dEz_dx;
-        dEz_dx = dEz_dx / X.K[i] + mEzx[c];
+        mEzx[c] = XP(X.b, 2, i, k) * mEzx[c] + XP(X.a, 1, i, k) * dEz_dx;
+        dEz_dx = dEz_dx / XP(X.K, 0, i, k) + mEzx[c];
         Hy[c] = daHy * Hy[c] + dbHy * (dEz_dx + dEx_dz);
       }
     // Ex, :273-283.
@@ -144,8 +147,8 @@ int orc_electromag2(int NX, int NZ, double dx, double dz, double dt,
       for (int i = 0; i <= NX - 2; ++i) {
         const size_t c = I(i, k), cm = I(i, k - 1);
         double d = (Hy[c] - Hy[cm]) / dz;
-        mHyz[c] = Z.bh[k] * mHyz[c] + Z.ah[k] * d;
-        d = d / Z.Kh[k] + mHyz[c];
+        mHyz[c] = ZP(Z.bh, 5, i, k) * mHyz[c] + ZP(Z.ah, 4, i, k) * d;
+        d = d / ZP(Z.Kh, 3, i, k) + mHyz[c];
         Ex[c] = ((caEx[c] + caEx[cm]) / 2) * Ex[c] + ((cbEx[c] + cbEx[cm]) / 2) * d;
       }
     // Ez, :285-295.
@@ -154,8 +157,8 @@ int orc_electromag2(int NX, int NZ, double dx, double dz, double dt,
       for (int i = 1; i <= NX - 2; ++i) {
         const size_t c = I(i, k), cm = I(i - 1, k);
         double d = (Hy[c] - Hy[cm]) / dx;
-        mHyx[c] = X.bh[i] * mHyx[c] + X.ah[i] * d;
-        d = d / X.Kh[i] + mHyx[c];
+        mHyx[c] = XP(X.bh, 5, i, k) * mHyx[c] + XP(X.ah, 4, i, k) * d;
+        d = d / XP(X.Kh, 3, i, k) + mHyx[c];
         Ez[c] = ((caEz[c] + caEz[cm]) / 2) * Ez[c] + ((cbEz[c] + cbEz[cm]) / 2) * d;
       }
     // Source, :300-301 (divided by the relative permittivity, as written).
@@ -189,6 +192,182 @@ int orc_electromag2(int NX, int NZ, double dx, double dz, double dt,
   }
   *maxnorm = runmax;
   return nsteps;
+}
+
+template <bool TWO_D>
+static int seismic2_impl(int NX, int NZ, double dx, double dz, double dt,
+                 const double* prof, const double* mat,
+                 int isrc, int ksrc, const double* src, int nstep_src,
+                 int it0, int nsteps,
+                 double* fld, double* mem,
+                 int nrec, const int* rec, double* traces,
+                 double* maxnorm, int* blew_up, int opts, const double* ssrc, const double* cpml2d) {
+  const size_t N = (size_t)NX * NZ;
+
+  // CPML coefficient q (K a b K_half a_half b_half) of the x (z) axis at cell
+  // (i, k): the axis profile at i (k), or, with the driver's 2-D fields
+  // (TWO_D), the field's value at the cell -- the same field for every
+  // derivative direction
+  auto XP = [&](const double* ax, int q, int i, int k) -> double {
+    if constexpr (TWO_D) return cpml2d[(size_t)q * N + (size_t)i + (size_t)NX * k];
+    else return ax[i];
+  };
+  auto ZP = [&](const double* ax, int q, int i, int k) -> double {
+    if constexpr (TWO_D) return cpml2d[(size_t)q * N + (size_t)i + (size_t)NX * k];
+    else return ax[k];
+  };
+  Axis X, Y, Z;
+  unpack_axes(prof, NX, 1, NZ, false, &X, &Y, &Z);
+  const double *c11 = mat, *c13 = mat + N, *c15 = mat + 2 * N, *c33 = mat + 3 * N;
+  const double *c35 = mat + 4 * N, *c55 = mat + 5 * N, *rho = mat + 6 * N;
+  const double *gx = mat + 7 * N, *gz = mat + 8 * N;
+  double *vx = fld, *vz = fld + N, *sxx = fld + 2 * N, *szz = fld + 3 * N, *sxz = fld + 4 * N;
+  double *m_vxx = mem, *m_vzz = mem + N, *m_vxz = mem + 2 * N, *m_vzx = mem + 3 * N;
+  double *m_sxx_x = mem + 4 * N, *m_szz_z = mem + 5 * N, *m_sxz_x = mem + 6 * N, *m_sxz_z = mem + 7 * N;
+  const bool legacy = opts & 1;
+  const int dens = (opts >> 1) & 3;
+  // the sigmaxz loop's own velocity-gradient memory (corrected physics); the
+  // legacy loops share the first four arrays
+  double *m2_vxx = legacy ? m_vxx : mem + 8 * N, *m2_vzz = legacy ? m_vzz : mem + 9 * N;
+  double *m2_vxz = legacy ? m_vxz : mem + 10 * N, *m2_vzx = legacy ? m_vzx : mem + 11 * N;
+  auto I = [NX](int i, int k) { return (size_t)i + (size_t)NX * k; };
+  const double* srcx = src;
+  const double* srcz = src + nstep_src;
+  *blew_up = 0;
+  double runmax = 0.0;
+
+  for (int s = 0; s < nsteps; ++s) {
+    const int t = it0 + s;
+    // sigmaxx, sigmazz, :247-281.
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= NZ - 1; ++k)
+      for (int i = 0; i <= NX - 2; ++i) {
+        const size_t c = I(i, k), cxp = I(i + 1, k), czm = I(i, k - 1);
+        double dvx_dx = (vx[cxp] - vx[c]) / dx;
+        double dvz_dz = (vz[c] - vz[czm]) / dz;
+        double dvz_dx = (vz[cxp] - vz[c]) / dx;
+        double dvx_dz = (vx[c] - vx[czm]) / dz;
+        // legacy: b_x_half(j), :255 (0 past the x axis); corrected: b_x_half(i)
+        const double bxh = legacy ? ((k < NX) ? X.bh[k] : 0.0) : XP(X.bh, 5, i, k);
+        m_vxx[c] = bxh * m_vxx[c] + XP(X.ah, 4, i, k) * dvx_dx;
+        m_vzz[c] = ZP(Z.b, 2, i, k) * m_vzz[c] + ZP(Z.a, 1, i, k) * dvz_dz;
+        m_vxz[c] = ZP(Z.bh, 5, i, k) * m_vxz[c] + ZP(Z.ah, 4, i, k) * dvx_dz;
+        m_vzx[c] = XP(X.b, 2, i, k) * m_vzx[c] + XP(X.a, 1, i, k) * dvz_dx;
+        dvx_dx = dvx_dx / XP(X.Kh, 3, i, k) + m_vxx[c];
+        dvz_dz = dvz_dz / ZP(Z.K, 0, i, k) + m_vzz[c];
+        dvz_dx = dvz_dx / XP(X.K, 0, i, k) + m_vzx[c];
+        dvx_dz = dvx_dz / ZP(Z.Kh, 3, i, k) + m_vxz[c];
+        sxx[c] = sxx[c] + (((c11[cxp] + 2 * c11[c] + c11[czm]) / 4) * dvx_dx +
+                           ((c13[cxp] + 2 * c13[c] + c13[czm]) / 4) * dvz_dz +
+                           ((c15[cxp] + 2 * c15[c] + c15[czm]) / 4) * (dvz_dx + dvx_dz)) * dt;
+        szz[c] = szz[c] + (((c13[cxp] + 2 * c13[c] + c13[czm]) / 4) * dvx_dx +
+                           ((c33[cxp] + 2 * c33[c] + c33[czm]) / 4) * dvz_dz +
+                           ((c35[cxp] + 2 * c35[c] + c35[czm]) / 4) * (dvz_dx + dvx_dz)) * dt;
+      }
+    // sigmaxz, :283-312: legacy, the same memory arrays again (each advances
+    // twice where both loops visit a cell); corrected, its own arrays.
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k <= NZ - 2; ++k)
+      for (int i = 1; i <= NX - 1; ++i) {
+        const size_t c = I(i, k), cxm = I(i - 1, k), czp = I(i, k + 1);
+        double dvx_dx = (vx[c] - vx[cxm]) / dx;
+        double dvz_dz = (vz[czp] - vz[c]) / dz;
+        double dvz_dx = (vz[c] - vz[cxm]) / dx;
+        double dvx_dz = (vx[czp] - vx[c]) / dz;
+        m2_vxx[c] = XP(X.bh, 5, i, k) * m2_vxx[c] + XP(X.ah, 4, i, k) * dvx_dx;
+        m2_vzz[c] = ZP(Z.b, 2, i, k) * m2_vzz[c] + ZP(Z.a, 1, i, k) * dvz_dz;
+        m2_vxz[c] = ZP(Z.bh, 5, i, k) * m2_vxz[c] + ZP(Z.ah, 4, i, k) * dvx_dz;
+        m2_vzx[c] = XP(X.b, 2, i, k) * m2_vzx[c] + XP(X.a, 1, i, k) * dvz_dx;
+        dvx_dx = dvx_dx / XP(X.Kh, 3, i, k) + m2_vxx[c];
+        dvz_dz = dvz_dz / ZP(Z.K, 0, i, k) + m2_vzz[c];
+        dvz_dx = dvz_dx / XP(X.K, 0, i, k) + m2_vzx[c];
+        dvx_dz = dvx_dz / ZP(Z.Kh, 3, i, k) + m2_vxz[c];
+        sxz[c] = sxz[c] + (((c15[czp] + 2 * c15[c] + c15[cxm]) / 4) * dvx_dx +
+                           ((c35[czp] + 2 * c35[c] + c35[cxm]) / 4) * dvz_dz +
+                           ((c55[czp] + 2 * c55[c] + c55[cxm]) / 4) * (dvz_dx + dvx_dz)) * dt;
+      }
+    // Stress source (moment tensor; explosive = equal normal components):
+    // sigma_ij += f_ij(t) dt at the source cell, after both stress loops.
+    if (ssrc) {
+      const size_t c = I(isrc, ksrc);
+      sxx[c] += ssrc[t] * dt;
+      szz[c] += ssrc[nstep_src + t] * dt;
+      sxz[c] += ssrc[2 * (size_t)nstep_src + t] * dt;
+    }
+    // vx, :317-336.
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= NZ - 1; ++k)
+      for (int i = 1; i <= NX - 1; ++i) {
+        const size_t c = I(i, k);
+        double dsxx_dx = (sxx[c] - sxx[I(i - 1, k)]) / dx;
+        double dsxz_dz = (sxz[c] - sxz[I(i, k - 1)]) / dz;
+        m_sxx_x[c] = XP(X.b, 2, i, k) * m_sxx_x[c] + XP(X.a, 1, i, k) * dsxx_dx;
+        m_sxz_z[c] = ZP(Z.b, 2, i, k) * m_sxz_z[c] + ZP(Z.a, 1, i, k) * dsxz_dz;
+        dsxx_dx = dsxx_dx / XP(X.K, 0, i, k) + m_sxx_x[c];
+        dsxz_dz = dsxz_dz / ZP(Z.K, 0, i, k) + m_sxz_z[c];
+        // legacy: the cell's own rho (:334; the average of :320 is unused);
+        // corrected: the average of :320 by the density method
+        const double rx = legacy ? rho[c] : rho_avg(dens, 2.0, rho[c], rho[I(i - 1, k)], rho[I(i, k - 1)]);
+        vx[c] = vx[c] * (1 - gx[c]) + (dsxx_dx + dsxz_dz) * dt / rx;
+      }
+    // vz, :338-357.
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k <= NZ - 2; ++k)
+      for (int i = 0; i <= NX - 2; ++i) {
+        const size_t c = I(i, k);
+        const double deltarho = rho_avg(dens, 2.0, rho[c], rho[I(i + 1, k)], rho[I(i, k + 1)]);  // :342
+        double dsxz_dx = (sxz[I(i + 1, k)] - sxz[c]) / dx;
+        double dszz_dz = (szz[I(i, k + 1)] - szz[c]) / dz;
+        m_sxz_x[c] = XP(X.bh, 5, i, k) * m_sxz_x[c] + XP(X.ah, 4, i, k) * dsxz_dx;
+        m_szz_z[c] = ZP(Z.bh, 5, i, k) * m_szz_z[c] + ZP(Z.ah, 4, i, k) * dszz_dz;
+        dsxz_dx = dsxz_dx / XP(X.Kh, 3, i, k) + m_sxz_x[c];
+        dszz_dz = dszz_dz / ZP(Z.Kh, 3, i, k) + m_szz_z[c];
+        vz[c] = vz[c] * (1 - gz[c]) + (dsxz_dx + dszz_dz) * dt / deltarho;
+      }
+    // Source, :360-361.
+    {
+      const size_t c = I(isrc, ksrc);
+      vx[c] = vx[c] + srcx[t] * dt / rho[c];
+      vz[c] = vz[c] + srcz[t] * dt / rho[c];
+    }
+    // Dirichlet edges, :365-375.
+    for (int k = 0; k < NZ; ++k) { vx[I(0, k)] = vx[I(NX - 1, k)] = 0; vz[I(0, k)] = vz[I(NX - 1, k)] = 0; }
+    for (int i = 0; i < NX; ++i) { vx[I(i, 0)] = vx[I(i, NZ - 1)] = 0; vz[I(i, 0)] = vz[I(i, NZ - 1)] = 0; }
+    // Stability check, :378-379.
+    double mx = 0.0;
+#pragma omp parallel for reduction(max : mx) schedule(static)
+    for (size_t c = 0; c < N; ++c) mx = std::max(mx, std::sqrt(vx[c] * vx[c] + vz[c] * vz[c]));
+    runmax = std::max(runmax, mx);
+    for (int r = 0; r < nrec; ++r) {
+      const size_t c = I(rec[3 * r], rec[3 * r + 2]);
+      traces[((size_t)s * 2 + 0) * nrec + r] = vx[c];
+      traces[((size_t)s * 2 + 1) * nrec + r] = vz[c];
+    }
+    if (!(mx <= kStability)) { *blew_up = 1; *maxnorm = runmax; return s + 1; }
+  }
+  *maxnorm = runmax;
+  return nsteps;
+}
+
+extern "C" {
+
+// ---------------------------------------------------------------------------
+// electromag2: legacy/fortran/electromagfdtd.f95:10-326.
+//   mat   = eps11, eps13, eps33, sig11, sig13, sig33   (6 x NX*NZ)
+//   fld   = Ex, Ez, Hy                                  (3 x NX*NZ)
+//   mem   = dEx_dz, dEz_dx, dHy_dz, dHy_dx              (4 x NX*NZ)
+//   src   = srcx, srcz                                  (2 x nstep_src)
+//   chans = Ex, Ez
+// Returns the number of steps completed; *blew_up = 1 if the norm check of
+// electromagfdtd.f95:320-321 fired (the run stops there, as the Fortran does).
+int orc_electromag2(int NX, int NZ, double dx, double dz, double dt,
+                    const double* prof, const double* mat,
+                    int isrc, int ksrc, const double* src, int nstep_src,
+                    int it0, int nsteps,
+                    double* fld, double* mem,
+                    int nrec, const int* rec, double* traces,
+                    double* maxnorm, int* blew_up, const double* cpml2d) {
+  return cpml2d ? electromag2_impl<true>(NX, NZ, dx, dz, dt, prof, mat, isrc, ksrc, src, nstep_src, it0, nsteps, fld, mem, nrec, rec, traces, maxnorm, blew_up, cpml2d) : electromag2_impl<false>(NX, NZ, dx, dz, dt, prof, mat, isrc, ksrc, src, nstep_src, it0, nsteps, fld, mem, nrec, rec, traces, maxnorm, blew_up, cpml2d);
 }
 
 // ---------------------------------------------------------------------------
@@ -348,139 +527,8 @@ int orc_seismic2(int NX, int NZ, double dx, double dz, double dt,
                  int it0, int nsteps,
                  double* fld, double* mem,
                  int nrec, const int* rec, double* traces,
-                 double* maxnorm, int* blew_up, int opts, const double* ssrc) {
-  const size_t N = (size_t)NX * NZ;
-  Axis X, Y, Z;
-  unpack_axes(prof, NX, 1, NZ, false, &X, &Y, &Z);
-  const double *c11 = mat, *c13 = mat + N, *c15 = mat + 2 * N, *c33 = mat + 3 * N;
-  const double *c35 = mat + 4 * N, *c55 = mat + 5 * N, *rho = mat + 6 * N;
-  const double *gx = mat + 7 * N, *gz = mat + 8 * N;
-  double *vx = fld, *vz = fld + N, *sxx = fld + 2 * N, *szz = fld + 3 * N, *sxz = fld + 4 * N;
-  double *m_vxx = mem, *m_vzz = mem + N, *m_vxz = mem + 2 * N, *m_vzx = mem + 3 * N;
-  double *m_sxx_x = mem + 4 * N, *m_szz_z = mem + 5 * N, *m_sxz_x = mem + 6 * N, *m_sxz_z = mem + 7 * N;
-  const bool legacy = opts & 1;
-  const int dens = (opts >> 1) & 3;
-  // the sigmaxz loop's own velocity-gradient memory (corrected physics); the
-  // legacy loops share the first four arrays
-  double *m2_vxx = legacy ? m_vxx : mem + 8 * N, *m2_vzz = legacy ? m_vzz : mem + 9 * N;
-  double *m2_vxz = legacy ? m_vxz : mem + 10 * N, *m2_vzx = legacy ? m_vzx : mem + 11 * N;
-  auto I = [NX](int i, int k) { return (size_t)i + (size_t)NX * k; };
-  const double* srcx = src;
-  const double* srcz = src + nstep_src;
-  *blew_up = 0;
-  double runmax = 0.0;
-
-  for (int s = 0; s < nsteps; ++s) {
-    const int t = it0 + s;
-    // sigmaxx, sigmazz, :247-281.
-#pragma omp parallel for schedule(static)
-    for (int k = 1; k <= NZ - 1; ++k)
-      for (int i = 0; i <= NX - 2; ++i) {
-        const size_t c = I(i, k), cxp = I(i + 1, k), czm = I(i, k - 1);
-        double dvx_dx = (vx[cxp] - vx[c]) / dx;
-        double dvz_dz = (vz[c] - vz[czm]) / dz;
-        double dvz_dx = (vz[cxp] - vz[c]) / dx;
-        double dvx_dz = (vx[c] - vx[czm]) / dz;
-        // legacy: b_x_half(j), :255 (0 past the x axis); corrected: b_x_half(i)
-        const double bxh = legacy ? ((k < NX) ? X.bh[k] : 0.0) : X.bh[i];
-        m_vxx[c] = bxh * m_vxx[c] + X.ah[i] * dvx_dx;
-        m_vzz[c] = Z.b[k] * m_vzz[c] + Z.a[k] * dvz_dz;
-        m_vxz[c] = Z.bh[k] * m_vxz[c] + Z.ah[k] * dvx_dz;
-        m_vzx[c] = X.b[i] * m_vzx[c] + X.a[i] * dvz_dx;
-        dvx_dx = dvx_dx / X.Kh[i] + m_vxx[c];
-        dvz_dz = dvz_dz / Z.K[k] + m_vzz[c];
-        dvz_dx = dvz_dx / X.K[i] + m_vzx[c];
-        dvx_dz = dvx_dz / Z.Kh[k] + m_vxz[c];
-        sxx[c] = sxx[c] + (((c11[cxp] + 2 * c11[c] + c11[czm]) / 4) * dvx_dx +
-                           ((c13[cxp] + 2 * c13[c] + c13[czm]) / 4) * dvz_dz +
-                           ((c15[cxp] + 2 * c15[c] + c15[czm]) / 4) * (dvz_dx + dvx_dz)) * dt;
-        szz[c] = szz[c] + (((c13[cxp] + 2 * c13[c] + c13[czm]) / 4) * dvx_dx +
-                           ((c33[cxp] + 2 * c33[c] + c33[czm]) / 4) * dvz_dz +
-                           ((c35[cxp] + 2 * c35[c] + c35[czm]) / 4) * (dvz_dx + dvx_dz)) * dt;
-      }
-    // sigmaxz, :283-312: legacy, the same memory arrays again (each advances
-    // twice where both loops visit a cell); corrected, its own arrays.
-#pragma omp parallel for schedule(static)
-    for (int k = 0; k <= NZ - 2; ++k)
-      for (int i = 1; i <= NX - 1; ++i) {
-        const size_t c = I(i, k), cxm = I(i - 1, k), czp = I(i, k + 1);
-        double dvx_dx = (vx[c] - vx[cxm]) / dx;
-        double dvz_dz = (vz[czp] - vz[c]) / dz;
-        double dvz_dx = (vz[c] - vz[cxm]) / dx;
-        double dvx_dz = (vx[czp] - vx[c]) / dz;
-        m2_vxx[c] = X.bh[i] * m2_vxx[c] + X.ah[i] * dvx_dx;
-        m2_vzz[c] = Z.b[k] * m2_vzz[c] + Z.a[k] * dvz_dz;
-        m2_vxz[c] = Z.bh[k] * m2_vxz[c] + Z.ah[k] * dvx_dz;
-        m2_vzx[c] = X.b[i] * m2_vzx[c] + X.a[i] * dvz_dx;
-        dvx_dx = dvx_dx / X.Kh[i] + m2_vxx[c];
-        dvz_dz = dvz_dz / Z.K[k] + m2_vzz[c];
-        dvz_dx = dvz_dx / X.K[i] + m2_vzx[c];
-        dvx_dz = dvx_dz / Z.Kh[k] + m2_vxz[c];
-        sxz[c] = sxz[c] + (((c15[czp] + 2 * c15[c] + c15[cxm]) / 4) * dvx_dx +
-                           ((c35[czp] + 2 * c35[c] + c35[cxm]) / 4) * dvz_dz +
-                           ((c55[czp] + 2 * c55[c] + c55[cxm]) / 4) * (dvz_dx + dvx_dz)) * dt;
-      }
-    // Stress source (moment tensor; explosive = equal normal components):
-    // sigma_ij += f_ij(t) dt at the source cell, after both stress loops.
-    if (ssrc) {
-      const size_t c = I(isrc, ksrc);
-      sxx[c] += ssrc[t] * dt;
-      szz[c] += ssrc[nstep_src + t] * dt;
-      sxz[c] += ssrc[2 * (size_t)nstep_src + t] * dt;
-    }
-    // vx, :317-336.
-#pragma omp parallel for schedule(static)
-    for (int k = 1; k <= NZ - 1; ++k)
-      for (int i = 1; i <= NX - 1; ++i) {
-        const size_t c = I(i, k);
-        double dsxx_dx = (sxx[c] - sxx[I(i - 1, k)]) / dx;
-        double dsxz_dz = (sxz[c] - sxz[I(i, k - 1)]) / dz;
-        m_sxx_x[c] = X.b[i] * m_sxx_x[c] + X.a[i] * dsxx_dx;
-        m_sxz_z[c] = Z.b[k] * m_sxz_z[c] + Z.a[k] * dsxz_dz;
-        dsxx_dx = dsxx_dx / X.K[i] + m_sxx_x[c];
-        dsxz_dz = dsxz_dz / Z.K[k] + m_sxz_z[c];
-        // legacy: the cell's own rho (:334; the average of :320 is unused);
-        // corrected: the average of :320 by the density method
-        const double rx = legacy ? rho[c] : rho_avg(dens, 2.0, rho[c], rho[I(i - 1, k)], rho[I(i, k - 1)]);
-        vx[c] = vx[c] * (1 - gx[c]) + (dsxx_dx + dsxz_dz) * dt / rx;
-      }
-    // vz, :338-357.
-#pragma omp parallel for schedule(static)
-    for (int k = 0; k <= NZ - 2; ++k)
-      for (int i = 0; i <= NX - 2; ++i) {
-        const size_t c = I(i, k);
-        const double deltarho = rho_avg(dens, 2.0, rho[c], rho[I(i + 1, k)], rho[I(i, k + 1)]);  // :342
-        double dsxz_dx = (sxz[I(i + 1, k)] - sxz[c]) / dx;
-        double dszz_dz = (szz[I(i, k + 1)] - szz[c]) / dz;
-        m_sxz_x[c] = X.bh[i] * m_sxz_x[c] + X.ah[i] * dsxz_dx;
-        m_szz_z[c] = Z.bh[k] * m_szz_z[c] + Z.ah[k] * dszz_dz;
-        dsxz_dx = dsxz_dx / X.Kh[i] + m_sxz_x[c];
-        dszz_dz = dszz_dz / Z.Kh[k] + m_szz_z[c];
-        vz[c] = vz[c] * (1 - gz[c]) + (dsxz_dx + dszz_dz) * dt / deltarho;
-      }
-    // Source, :360-361.
-    {
-      const size_t c = I(isrc, ksrc);
-      vx[c] = vx[c] + srcx[t] * dt / rho[c];
-      vz[c] = vz[c] + srcz[t] * dt / rho[c];
-    }
-    // Dirichlet edges, :365-375.
-    for (int k = 0; k < NZ; ++k) { vx[I(0, k)] = vx[I(NX - 1, k)] = 0; vz[I(0, k)] = vz[I(NX - 1, k)] = 0; }
-    for (int i = 0; i < NX; ++i) { vx[I(i, 0)] = vx[I(i, NZ - 1)] = 0; vz[I(i, 0)] = vz[I(i, NZ - 1)] = 0; }
-    // Stability check, :378-379.
-    double mx = 0.0;
-#pragma omp parallel for reduction(max : mx) schedule(static)
-    for (size_t c = 0; c < N; ++c) mx = std::max(mx, std::sqrt(vx[c] * vx[c] + vz[c] * vz[c]));
-    runmax = std::max(runmax, mx);
-    for (int r = 0; r < nrec; ++r) {
-      const size_t c = I(rec[3 * r], rec[3 * r + 2]);
-      traces[((size_t)s * 2 + 0) * nrec + r] = vx[c];
-      traces[((size_t)s * 2 + 1) * nrec + r] = vz[c];
-    }
-    if (!(mx <= kStability)) { *blew_up = 1; *maxnorm = runmax; return s + 1; }
-  }
-  *maxnorm = runmax;
-  return nsteps;
+                 double* maxnorm, int* blew_up, int opts, const double* ssrc, const double* cpml2d) {
+  return cpml2d ? seismic2_impl<true>(NX, NZ, dx, dz, dt, prof, mat, isrc, ksrc, src, nstep_src, it0, nsteps, fld, mem, nrec, rec, traces, maxnorm, blew_up, opts, ssrc, cpml2d) : seismic2_impl<false>(NX, NZ, dx, dz, dt, prof, mat, isrc, ksrc, src, nstep_src, it0, nsteps, fld, mem, nrec, rec, traces, maxnorm, blew_up, opts, ssrc, cpml2d);
 }
 
 // ---------------------------------------------------------------------------

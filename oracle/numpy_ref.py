@@ -21,10 +21,12 @@ def _axes(prof, NX, NZ):
     return x, z  # rows: K, a, b, Kh, ah, bh
 
 
-def electromag2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None):
+def electromag2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None, cpml2d=None):
+    """cpml2d: the driver's 2-D CPML fields (6, NZ, NX), K a b K_half a_half
+    b_half, for every derivative direction in place of the axis profiles."""
     eps11, eps13, eps33, sig11, sig13, sig33 = np.asarray(mat, dtype=np.float64)
     return _em2(NX, NZ, dx, dz, dt, prof, eps11, eps13, eps33, sig11, sig13, sig33, src_ik, srcfn, nsteps, rec,
-                np.float64)
+                np.float64, cpml2d)
 
 
 def electromag2c(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None):
@@ -37,7 +39,21 @@ def electromag2c(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None)
                 np.complex128)
 
 
-def _em2(NX, NZ, dx, dz, dt, prof, eps11, eps13, eps33, sig11, sig13, sig33, src_ik, srcfn, nsteps, rec, dtype):
+def _coef_fields(X, Z, NX, NZ, cpml2d):
+    """Every CPML coefficient as an (NZ, NX) array: the x profile spread over
+    the rows and the z profile over the columns, or, with the driver's 2-D
+    fields, the same field for both axes.  Returns (x tuple, z tuple), each
+    K, a, b, K_half, a_half, b_half."""
+    if cpml2d is not None:
+        F = tuple(np.asarray(cpml2d, dtype=np.float64))
+        return F, F
+    xs = tuple(np.broadcast_to(X[q][None, :], (NZ, NX)) for q in range(6))
+    zs = tuple(np.broadcast_to(Z[q][:, None], (NZ, NX)) for q in range(6))
+    return xs, zs
+
+
+def _em2(NX, NZ, dx, dz, dt, prof, eps11, eps13, eps33, sig11, sig13, sig33, src_ik, srcfn, nsteps, rec, dtype,
+         cpml2d=None):
     X, Z = _axes(prof, NX, NZ)
     epsx, epsz = (eps11 + eps13) * EPS0, (eps13 + eps33) * EPS0
     sigx, sigz = sig11 + sig13, sig13 + sig33
@@ -50,29 +66,27 @@ def _em2(NX, NZ, dx, dz, dt, prof, eps11, eps13, eps33, sig11, sig13, sig33, src
     mExz, mEzx, mHyz, mHyx = (np.zeros((NZ, NX), dtype=dtype) for _ in range(4))
     si, sk = src_ik
     out = []
-    Kx, ax, bx, Kxh, axh, bxh = (X[q][None, :] for q in range(6))
-    Kz, az, bz, Kzh, azh, bzh = (Z[q][:, None] for q in range(6))
+    (Kx, ax, bx, Kxh, axh, bxh), (Kz, az, bz, Kzh, azh, bzh) = _coef_fields(X, Z, NX, NZ, cpml2d)
+    H, EX, EZ = np.s_[:-1, :-1], np.s_[1:-1, :-1], np.s_[:-1, 1:-1]
     for t in range(nsteps):
         # H: k in [0,NZ-2], i in [0,NX-2]
         dEx = (Ex[1:, :-1] - Ex[:-1, :-1]) / dz
-        mExz[:-1, :-1] = bz[:-1] * mExz[:-1, :-1] + az[:-1] * dEx
-        vz = dEx / Kz[:-1] + mExz[:-1, :-1]
+        mExz[H] = bz[H] * mExz[H] + az[H] * dEx
+        vz = dEx / Kz[H] + mExz[H]
         dEz = (Ez[:-1, 1:] - Ez[:-1, :-1]) / dx
-        mEzx[:-1, :-1] = bx[:, :-1] * mEzx[:-1, :-1] + ax[:, :-1] * dEz
-        vx = dEz / Kx[:, :-1] + mEzx[:-1, :-1]
-        Hy[:-1, :-1] = Hy[:-1, :-1] + dbH * (vx + vz)
+        mEzx[H] = bx[H] * mEzx[H] + ax[H] * dEz
+        vx = dEz / Kx[H] + mEzx[H]
+        Hy[H] = Hy[H] + dbH * (vx + vz)
         # Ex: k in [1,NZ-2], i in [0,NX-2]
         d = (Hy[1:-1, :-1] - Hy[:-2, :-1]) / dz
-        mHyz[1:-1, :-1] = bzh[1:-1] * mHyz[1:-1, :-1] + azh[1:-1] * d
-        d = d / Kzh[1:-1] + mHyz[1:-1, :-1]
-        Ex[1:-1, :-1] = ((caEx[1:-1, :-1] + caEx[:-2, :-1]) / 2) * Ex[1:-1, :-1] + \
-            ((cbEx[1:-1, :-1] + cbEx[:-2, :-1]) / 2) * d
+        mHyz[EX] = bzh[EX] * mHyz[EX] + azh[EX] * d
+        d = d / Kzh[EX] + mHyz[EX]
+        Ex[EX] = ((caEx[1:-1, :-1] + caEx[:-2, :-1]) / 2) * Ex[EX] + ((cbEx[1:-1, :-1] + cbEx[:-2, :-1]) / 2) * d
         # Ez: k in [0,NZ-2], i in [1,NX-2]
         d = (Hy[:-1, 1:-1] - Hy[:-1, :-2]) / dx
-        mHyx[:-1, 1:-1] = bxh[:, 1:-1] * mHyx[:-1, 1:-1] + axh[:, 1:-1] * d
-        d = d / Kxh[:, 1:-1] + mHyx[:-1, 1:-1]
-        Ez[:-1, 1:-1] = ((caEz[:-1, 1:-1] + caEz[:-1, :-2]) / 2) * Ez[:-1, 1:-1] + \
-            ((cbEz[:-1, 1:-1] + cbEz[:-1, :-2]) / 2) * d
+        mHyx[EZ] = bxh[EZ] * mHyx[EZ] + axh[EZ] * d
+        d = d / Kxh[EZ] + mHyx[EZ]
+        Ez[EZ] = ((caEz[:-1, 1:-1] + caEz[:-1, :-2]) / 2) * Ez[EZ] + ((cbEz[:-1, 1:-1] + cbEz[:-1, :-2]) / 2) * d
         Ex[sk, si] += srcfn[0][t] * dt / eps11[sk, si]
         Ez[sk, si] += srcfn[1][t] * dt / eps33[sk, si]
         Ex[:, 0] = 0; Ex[:, NX - 2] = 0; Ex[0, :] = 0; Ex[NZ - 1, :] = 0
@@ -95,7 +109,7 @@ def _rho_avg(method, w, r, a, b):
 
 
 def seismic2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None, legacy=False, density="arithmetic",
-             stress_src=None):
+             stress_src=None, cpml2d=None):
     """legacy: the legacy quirks (shared velocity-gradient memory of the two
     stress loops, b_x_half(j), vx over the cell's own rho); otherwise
     corrected physics.  stress_src: (3, nstep) sxx, szz, sxz or None."""
@@ -107,15 +121,14 @@ def seismic2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None, leg
     if legacy:
         n_vxx, n_vzz, n_vxz, n_vzx = m_vxx, m_vzz, m_vxz, m_vzx
     si, sk = src_ik
-    Kx, ax, bx, Kxh, axh, bxh = (X[q][None, :] for q in range(6))
-    Kz, az, bz, Kzh, azh, bzh = (Z[q][:, None] for q in range(6))
+    (Kx, ax, bx, Kxh, axh, bxh), (Kz, az, bz, Kzh, azh, bzh) = _coef_fields(X, Z, NX, NZ, cpml2d)
     if legacy:  # b_x_half read with the z index (seismicfdtd.f95:255); 0 past the x axis
         q3 = np.zeros(NZ)
         n = min(NX, NZ)
         q3[:n] = X[5][:n]
-        q3 = q3[:, None]
+        q3 = np.broadcast_to(q3[:, None], (NZ, NX))
     else:
-        q3 = np.broadcast_to(bxh, (NZ, NX))
+        q3 = bxh
     out = []
     for t in range(nsteps):
         # loop 1: k in [1, NZ-1], i in [0, NX-2]
@@ -124,14 +137,14 @@ def seismic2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None, leg
         dvz_dz = (vz[1:, :-1] - vz[:-1, :-1]) / dz
         dvz_dx = (vz[1:, 1:] - vz[1:, :-1]) / dx
         dvx_dz = (vx[1:, :-1] - vx[:-1, :-1]) / dz
-        m_vxx[s1] = (q3[1:] if legacy else q3[1:, :-1]) * m_vxx[s1] + axh[:, :-1] * dvx_dx
-        m_vzz[s1] = bz[1:] * m_vzz[s1] + az[1:] * dvz_dz
-        m_vxz[s1] = bzh[1:] * m_vxz[s1] + azh[1:] * dvx_dz
-        m_vzx[s1] = bx[:, :-1] * m_vzx[s1] + ax[:, :-1] * dvz_dx
-        dvx_dx = dvx_dx / Kxh[:, :-1] + m_vxx[s1]
-        dvz_dz = dvz_dz / Kz[1:] + m_vzz[s1]
-        dvz_dx = dvz_dx / Kx[:, :-1] + m_vzx[s1]
-        dvx_dz = dvx_dz / Kzh[1:] + m_vxz[s1]
+        m_vxx[s1] = q3[s1] * m_vxx[s1] + axh[s1] * dvx_dx
+        m_vzz[s1] = bz[s1] * m_vzz[s1] + az[s1] * dvz_dz
+        m_vxz[s1] = bzh[s1] * m_vxz[s1] + azh[s1] * dvx_dz
+        m_vzx[s1] = bx[s1] * m_vzx[s1] + ax[s1] * dvz_dx
+        dvx_dx = dvx_dx / Kxh[s1] + m_vxx[s1]
+        dvz_dz = dvz_dz / Kz[s1] + m_vzz[s1]
+        dvz_dx = dvz_dx / Kx[s1] + m_vzx[s1]
+        dvx_dz = dvx_dz / Kzh[s1] + m_vxz[s1]
         av = lambda c: (c[1:, 1:] + 2 * c[1:, :-1] + c[:-1, :-1]) / 4
         sxx[s1] = sxx[s1] + (av(c11) * dvx_dx + av(c13) * dvz_dz + av(c15) * (dvz_dx + dvx_dz)) * dt
         szz[s1] = szz[s1] + (av(c13) * dvx_dx + av(c33) * dvz_dz + av(c35) * (dvz_dx + dvx_dz)) * dt
@@ -141,14 +154,14 @@ def seismic2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None, leg
         dvz_dz = (vz[1:, 1:] - vz[:-1, 1:]) / dz
         dvz_dx = (vz[:-1, 1:] - vz[:-1, :-1]) / dx
         dvx_dz = (vx[1:, 1:] - vx[:-1, 1:]) / dz
-        n_vxx[s2] = bxh[:, 1:] * n_vxx[s2] + axh[:, 1:] * dvx_dx
-        n_vzz[s2] = bz[:-1] * n_vzz[s2] + az[:-1] * dvz_dz
-        n_vxz[s2] = bzh[:-1] * n_vxz[s2] + azh[:-1] * dvx_dz
-        n_vzx[s2] = bx[:, 1:] * n_vzx[s2] + ax[:, 1:] * dvz_dx
-        dvx_dx = dvx_dx / Kxh[:, 1:] + n_vxx[s2]
-        dvz_dz = dvz_dz / Kz[:-1] + n_vzz[s2]
-        dvz_dx = dvz_dx / Kx[:, 1:] + n_vzx[s2]
-        dvx_dz = dvx_dz / Kzh[:-1] + n_vxz[s2]
+        n_vxx[s2] = bxh[s2] * n_vxx[s2] + axh[s2] * dvx_dx
+        n_vzz[s2] = bz[s2] * n_vzz[s2] + az[s2] * dvz_dz
+        n_vxz[s2] = bzh[s2] * n_vxz[s2] + azh[s2] * dvx_dz
+        n_vzx[s2] = bx[s2] * n_vzx[s2] + ax[s2] * dvz_dx
+        dvx_dx = dvx_dx / Kxh[s2] + n_vxx[s2]
+        dvz_dz = dvz_dz / Kz[s2] + n_vzz[s2]
+        dvz_dx = dvz_dx / Kx[s2] + n_vzx[s2]
+        dvx_dz = dvx_dz / Kzh[s2] + n_vxz[s2]
         bv = lambda c: (c[1:, 1:] + 2 * c[:-1, 1:] + c[:-1, :-1]) / 4
         sxz[s2] = sxz[s2] + (bv(c15) * dvx_dx + bv(c35) * dvz_dz + bv(c55) * (dvz_dx + dvx_dz)) * dt
         if stress_src is not None:
@@ -159,10 +172,10 @@ def seismic2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None, leg
         s3 = (slice(1, NZ), slice(1, NX))
         d1 = (sxx[1:, 1:] - sxx[1:, :-1]) / dx
         d2 = (sxz[1:, 1:] - sxz[:-1, 1:]) / dz
-        m_sxx[s3] = bx[:, 1:] * m_sxx[s3] + ax[:, 1:] * d1
-        m_sxzz[s3] = bz[1:] * m_sxzz[s3] + az[1:] * d2
-        d1 = d1 / Kx[:, 1:] + m_sxx[s3]
-        d2 = d2 / Kz[1:] + m_sxzz[s3]
+        m_sxx[s3] = bx[s3] * m_sxx[s3] + ax[s3] * d1
+        m_sxzz[s3] = bz[s3] * m_sxzz[s3] + az[s3] * d2
+        d1 = d1 / Kx[s3] + m_sxx[s3]
+        d2 = d2 / Kz[s3] + m_sxzz[s3]
         rx = rho[s3] if legacy else _rho_avg(density, 2, rho[s3], rho[1:, :-1], rho[:-1, 1:])
         vx[s3] = vx[s3] * (1 - gx[s3]) + (d1 + d2) * dt / rx
         # vz: k in [0, NZ-2], i in [0, NX-2]
@@ -170,10 +183,10 @@ def seismic2(NX, NZ, dx, dz, dt, prof, mat, src_ik, srcfn, nsteps, rec=None, leg
         rbar = _rho_avg(density, 2, rho[s4], rho[:-1, 1:], rho[1:, :-1])
         d1 = (sxz[:-1, 1:] - sxz[:-1, :-1]) / dx
         d2 = (szz[1:, :-1] - szz[:-1, :-1]) / dz
-        m_sxzx[s4] = bxh[:, :-1] * m_sxzx[s4] + axh[:, :-1] * d1
-        m_szz[s4] = bzh[:-1] * m_szz[s4] + azh[:-1] * d2
-        d1 = d1 / Kxh[:, :-1] + m_sxzx[s4]
-        d2 = d2 / Kzh[:-1] + m_szz[s4]
+        m_sxzx[s4] = bxh[s4] * m_sxzx[s4] + axh[s4] * d1
+        m_szz[s4] = bzh[s4] * m_szz[s4] + azh[s4] * d2
+        d1 = d1 / Kxh[s4] + m_sxzx[s4]
+        d2 = d2 / Kzh[s4] + m_szz[s4]
         vz[s4] = vz[s4] * (1 - gz[s4]) + (d1 + d2) * dt / rbar
         vx[sk, si] += srcfn[0][t] * dt / rho[sk, si]
         vz[sk, si] += srcfn[1][t] * dt / rho[sk, si]

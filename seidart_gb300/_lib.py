@@ -22,7 +22,7 @@ SFD_OK, SFD_ERR_BAD_ARG, SFD_ERR_STATE, SFD_ERR_CUDA, SFD_ERR_UNSTABLE, SFD_ERR_
 # Every exported symbol of include/seidart_gb300.h
 EXPORTS = (
     "sfd_version", "sfd_last_error", "sfd_model_planes", "sfd_num_fields", "sfd_num_channels",
-    "sfd_num_memory", "sfd_state_bytes", "sfd_create", "sfd_set_model", "sfd_set_model_ids", "sfd_set_cpml",
+    "sfd_num_memory", "sfd_state_bytes", "sfd_create", "sfd_set_model", "sfd_set_model_ids", "sfd_set_cpml", "sfd_set_cpml2d",
     "sfd_set_source", "sfd_set_stress_source", "sfd_share_model", "sfd_set_receivers", "sfd_reset", "sfd_set_field", "sfd_get_field",
     "sfd_get_field_async", "sfd_encode_field_i16",
     "sfd_get_memory", "sfd_run", "sfd_status", "sfd_get_traces", "sfd_traces_device", "sfd_field_device", "sfd_launch_half",
@@ -75,6 +75,7 @@ def _declare(lib):
         "sfd_set_model": (i32, [P, dp, i64]),
         "sfd_set_model_ids": (i32, [P, P, i32, dp, i64]),
         "sfd_set_cpml": (i32, [P, dp, i64]),
+        "sfd_set_cpml2d": (i32, [P, dp, i64]),
         "sfd_set_source": (i32, [P, i32, i32, i32, dp, i32, i32]),
         "sfd_set_stress_source": (i32, [P, i32, i32, i32, dp, i32, i32]),
         "sfd_set_receivers": (i32, [P, ip, i32]),

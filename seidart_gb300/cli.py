@@ -26,6 +26,9 @@ Same argv and the same working-directory files as the backend that
 averaging at the staggered velocity points (none, arithmetic, geometric,
 harmonic); ``--legacy-quirks`` reproduces the legacy Fortran loops' quirks
 instead of the default corrected physics (``SFD_FLAG_LEGACY_QUIRKS``).
+``--cpml-mode 2d`` (2-D models) takes the driver's 2-D CPML fields
+``{kappa,acoef,bcoef}{,_half}_cpml.dat`` for every derivative direction
+instead of per-axis profiles built from the project's CPML parameters.
 
 All are Fortran records, x fastest, full grid (CPML included).  The CPML
 profiles are computed from the project's CPML parameters in FP64
@@ -170,6 +173,21 @@ def load_project(json_path, seismic: bool, workdir=".", density_gradient: bool =
     return dict(kind=kind, grid=grid, planes=planes, profiles=profiles, srcfn=srcfn, src_ijk=src_ijk,
                 init=init, nstep=nstep, xind=xind, yind=yind, zind=zind, seismic=seismic, vmax=vmax,
                 stress_srcfn=stress)
+
+
+def read_cpml2d(workdir, grid):
+    """The driver's 2-D CPML fields (definitions.py:560-998): the records of
+    {kappa,acoef,bcoef}{,_half}_cpml.dat, (NX, NZ) arrays x fastest, as
+    (6, NZ, NX) K, a, b, K_half, a_half, b_half."""
+    wd = Path(workdir)
+    out = []
+    for suffix in ("_cpml.dat", "_half_cpml.dat"):
+        for name in ("kappa", "acoef", "bcoef"):
+            fn = wd / f"{name}{suffix}"
+            if not fn.exists():
+                raise ProjectError(f"missing CPML file {fn} (--cpml-mode 2d)")
+            out.append(fio.read_plane(fn, (grid.nz, grid.nx)))
+    return np.stack(out)
 
 
 def max_speed(kind, planes, per_axis=False):
@@ -380,6 +398,10 @@ def run(argv=None) -> int:
                     help="seismic: reproduce the legacy Fortran loops' quirks instead of the corrected physics")
     ap.add_argument("--no-density-gradient", action="store_true",
                     help="seismic: ignore density_gradient.dat")
+    ap.add_argument("--cpml-mode", choices=["1d", "2d"], default="1d",
+                    help="1d: per-axis CPML profiles from the project's CPML parameters (default); 2d: the driver's "
+                         "2-D fields {kappa,acoef,bcoef}{,_half}_cpml.dat for every derivative direction "
+                         "(2-D models)")
     a = ap.parse_args(argv)
     seismic = str(parse_flag(a.flags, "seismic", "true")).lower() in ("true", "1", "yes")
     density = str(parse_flag(a.flags, "density_method", "arithmetic")).lower()
@@ -394,6 +416,20 @@ def run(argv=None) -> int:
         print(f"seidartfdtd: {e}", file=sys.stderr)
         return 1
     opts = {"legacy": a.legacy_quirks, "density": density} if seismic else {}
+    fields2d = None
+    if a.cpml_mode == "2d":
+        if p["kind"] not in (ELECTROMAG2, SEISMIC2):
+            print("seidartfdtd: --cpml-mode 2d applies to 2-D models (electromag2, seismic2)", file=sys.stderr)
+            return 1
+        if a.legacy_quirks:
+            print("seidartfdtd: --cpml-mode 2d excludes --legacy-quirks (the legacy loops read 1-D profiles)",
+                  file=sys.stderr)
+            return 1
+        try:
+            fields2d = read_cpml2d(a.workdir, p["grid"])
+        except (ProjectError, ValueError, OSError) as e:
+            print(f"seidartfdtd: {e}", file=sys.stderr)
+            return 1
     grid = p["grid"]
     rec = read_receivers(a.receivers, grid) if a.receivers else np.zeros((0, 3), np.int32)
     every = max(0, int(a.snapshot_every))
@@ -403,9 +439,14 @@ def run(argv=None) -> int:
               "(seismic=false on a 2.5-D project, --snapshot-every 1)", file=sys.stderr)
         return 1
     try:
-        with FDTDSolver(grid, p["nstep"], len(rec), device=a.device, **opts) as s:
+        from .solver import FLAG_CPML_2D
+        with FDTDSolver(grid, p["nstep"], len(rec), device=a.device, flags=FLAG_CPML_2D if fields2d is not None else 0,
+                        **opts) as s:
             s.set_model(p["planes"])
-            s.set_cpml(p["profiles"])
+            if fields2d is not None:
+                s.set_cpml2d(fields2d)
+            else:
+                s.set_cpml(p["profiles"])
             s.set_source(p["src_ijk"], p["srcfn"])
             if p["stress_srcfn"] is not None:
                 s.set_stress_source(p["src_ijk"], p["stress_srcfn"])

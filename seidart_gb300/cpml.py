@@ -215,6 +215,18 @@ def driver_fields_2d(nx, nz, npml, dx, dz, dt, f0, vmax, seismic, params=None, h
     return {"sigma": sigma, "kappa": kappa, "alpha": alpha, "acoef": acoef, "bcoef": bcoef}
 
 
+def driver_cpml_planes(nx, nz, npml, dx, dz, dt, f0, vmax_x, seismic, params=None, vmax_z=None, deltamin=None):
+    """The (6, NZ, NX) planes K, a, b, K_half, a_half, b_half of the driver's
+    2-D CPML fields (driver_fields_2d at both offsets), the input of
+    FDTDSolver.set_cpml2d."""
+    out = []
+    for half in (False, True):
+        f = driver_fields_2d(nx, nz, npml, dx, dz, dt, f0, vmax_x, seismic, params, half=half, deltamin=deltamin,
+                             vmax_z=vmax_z)
+        out += [f["kappa"], f["acoef"], f["bcoef"]]
+    return np.ascontiguousarray(np.stack(out))
+
+
 def pack_profiles(profiles) -> np.ndarray:
     """Concatenate K, a, b, K_half, a_half, b_half of every axis (x, [y,] z)."""
     return np.ascontiguousarray(np.concatenate([pr.packed().ravel() for pr in profiles]), dtype=np.float64)

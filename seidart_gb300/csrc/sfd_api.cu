@@ -178,6 +178,11 @@ bool pingpong_mem(int kind, int q) {
   return false;
 }
 bool has_single_pass(int kind) { return kind == SFD_ELECTROMAG2 || kind == SFD_SEISMIC2; }
+bool cpml2d(const sfd_config& c) { return (c.flags & SFD_FLAG_CPML_2D) != 0; }
+// Whether a handle steps in the single-pass form (the others: two kernels per step).
+bool single_pass(const sfd_config& c) {
+  return has_single_pass(c.kind) && !(c.flags & (SFD_FLAG_TWO_PASS | SFD_FLAG_CPML_2D));
+}
 
 struct Layout {
   int P, NX, NY, NZ, W, ysplit, nslots;
@@ -206,8 +211,13 @@ int validate_cfg(const sfd_config* c) {
   if (!three && c->ny != 1) return fail(SFD_ERR_BAD_ARG, "2-D solvers need ny = 1 (got %d)", c->ny);
   if (c->nstep < 1) return fail(SFD_ERR_BAD_ARG, "nstep must be >= 1");
   if (c->nrec < 0) return fail(SFD_ERR_BAD_ARG, "nrec must be >= 0");
-  if ((c->flags & ~(SFD_FLAG_TWO_PASS | SFD_FLAG_STREAMING | SFD_FLAG_LEGACY_QUIRKS | SFD_FLAG_DENSITY_MASK)) != 0)
+  if ((c->flags & ~(SFD_FLAG_TWO_PASS | SFD_FLAG_STREAMING | SFD_FLAG_LEGACY_QUIRKS | SFD_FLAG_DENSITY_MASK |
+                    SFD_FLAG_CPML_2D)) != 0)
     return fail(SFD_ERR_BAD_ARG, "unknown flags 0x%x", c->flags);
+  if ((c->flags & SFD_FLAG_CPML_2D) && c->kind != SFD_ELECTROMAG2 && c->kind != SFD_SEISMIC2)
+    return fail(SFD_ERR_BAD_ARG, "SFD_FLAG_CPML_2D applies to electromag2 and seismic2");
+  if ((c->flags & SFD_FLAG_CPML_2D) && (c->flags & SFD_FLAG_LEGACY_QUIRKS))
+    return fail(SFD_ERR_BAD_ARG, "SFD_FLAG_CPML_2D excludes SFD_FLAG_LEGACY_QUIRKS (the legacy loops read 1-D profiles)");
   if ((c->flags & (SFD_FLAG_LEGACY_QUIRKS | SFD_FLAG_DENSITY_MASK)) && c->kind != SFD_SEISMIC2 && c->kind != SFD_SEISMIC25)
     return fail(SFD_ERR_BAD_ARG, "SFD_FLAG_LEGACY_QUIRKS and the density flags apply to the seismic kinds only");
   if (!(c->dt > 0) || !(c->dx > 0) || !(c->dz > 0) || (three && !(c->dy > 0)))
@@ -231,7 +241,8 @@ void make_layout(const sfd_config& c, Layout* L) {
   for (int m = 0; m < 18; ++m) { L->off_mem[m] = 0; L->mem_sz[m] = 0; }
   for (int m = 0; m < nm; ++m) {
     size_t n = 0;
-    if (ax[m] == 'x') n = (size_t)c.ny * c.nz * 2 * c.npml;
+    if (cpml2d(c)) n = (size_t)L->P * c.nz;  // 2-D CPML fields: every memory variable on the full grid
+    else if (ax[m] == 'x') n = (size_t)c.ny * c.nz * 2 * c.npml;
     else if (ax[m] == 'y') n = (size_t)c.nz * 2 * c.npml * L->P;
     else n = (size_t)2 * c.npml * c.ny * L->P;
     L->off_mem[m] = o; L->mem_sz[m] = n;
@@ -239,13 +250,14 @@ void make_layout(const sfd_config& c, Layout* L) {
   }
   L->off_fieldsB = 0;
   for (int m = 0; m < 18; ++m) L->off_memB[m] = 0;
-  if (has_single_pass(c.kind) && !(c.flags & SFD_FLAG_TWO_PASS)) {
+  if (single_pass(c)) {
     L->off_fieldsB = o; o += align256(sizeof(float) * L->fsz * nfields(c.kind));
     for (int m = 0; m < nm; ++m)
       if (pingpong_mem(c.kind, m)) { L->off_memB[m] = o; o += align256(sizeof(float) * L->mem_sz[m]); }
   }
   L->coef_plane = (size_t)L->P * c.nz;
-  L->off_coef = o; o += align256(sizeof(float) * L->coef_plane * ncoef(c.kind));
+  // the update coefficients, then (2-D CPML fields) 1/K, a, b of the full and half offsets
+  L->off_coef = o; o += align256(sizeof(float) * L->coef_plane * (ncoef(c.kind) + (cpml2d(c) ? 6 : 0)));
   const int nax = is3(c.kind) ? 3 : 2;
   const int lens[3] = {c.nx, is3(c.kind) ? c.ny : c.nz, c.nz};
   for (int a = 0; a < 3; ++a) L->off_axis[a] = 0;
@@ -256,7 +268,7 @@ void make_layout(const sfd_config& c, Layout* L) {
   L->off_traces = o; o += align256(sizeof(float) * (size_t)c.nstep * nchan(c.kind) * std::max(1, c.nrec));
   L->off_slots = o; o += align256(sizeof(float) * L->nslots);  // ZB = 1 tiles: the largest grid
   L->off_res = 0;
-  if ((c.kind == SFD_ELECTROMAG2 || c.kind == SFD_SEISMIC2) && !(c.flags & (SFD_FLAG_TWO_PASS | SFD_FLAG_STREAMING))) {
+  if (single_pass(c) && !(c.flags & SFD_FLAG_STREAMING)) {
     L->off_res = o;  // edge arrays of on-chip runs
     o += align256(res_scratch_bytes(L->P, c.nz, res_edge_fields(c.kind)));
   }
@@ -350,6 +362,22 @@ int single_pass_zb(int kind, int nx, int nz) {
   return tiles2 >= 8L * 152 ? 2 : 1;
 }
 
+// The 2-D CPML planes of a SFD_FLAG_CPML_2D handle (after the update
+// coefficients), empty otherwise.
+Cpml2d cpml2d_args(const sfd_handle* h) {
+  Cpml2d f;
+  const bool on = cpml2d(h->cfg);
+  const int nc = ncoef(h->cfg.kind);
+  for (int o = 0; o < 2; ++o) {
+    f.ik[o] = on ? h->coef(nc + 3 * o) : nullptr;
+    f.a[o] = on ? h->coef(nc + 3 * o + 1) : nullptr;
+    f.b[o] = on ? h->coef(nc + 3 * o + 2) : nullptr;
+  }
+  f.idx = (float)(1.0 / h->cfg.dx);
+  f.idz = (float)(1.0 / h->cfg.dz);
+  return f;
+}
+
 void bind_args(sfd_handle* h) {
   const Layout& L = h->L;
   const sfd_config& c = h->cfg;
@@ -364,6 +392,7 @@ void bind_args(sfd_handle* h) {
       a.CAx = h->coef(0); a.CBx = h->coef(1); a.CAz = h->coef(2); a.CBz = h->coef(3);
       a.X = make_axis(h->axis(0), NX); a.Z = make_axis(h->axis(1), NZ);
       a.dbH = (float)(c.dt / kMu0);
+      a.c2d = cpml2d_args(h);
       a.io = io;
       h->launch = em2_launch(a);
       for (int p = 0; p < 2 && h->single; ++p) {
@@ -409,6 +438,7 @@ void bind_args(sfd_handle* h) {
       a.dtrx = h->coef(8); a.dtrz = h->coef(9); a.gxp = h->coef(10); a.gzp = h->coef(11);
       a.q3 = (const float*)(h->base + L.off_q3);
       a.X = make_axis(h->axis(0), NX); a.Z = make_axis(h->axis(1), NZ);
+      a.c2d = cpml2d_args(h);
       a.io = io;
       h->launch = seis2_launch(a);
       for (int p = 0; p < 2 && h->single; ++p) {
@@ -508,8 +538,14 @@ void launch_step(sfd_handle* h, int p, int rel, cudaStream_t s) {
 void launch_half(sfd_handle* h, int which, int rel, cudaStream_t s) {
   const Launch& L = h->launch;
   switch (h->cfg.kind) {
-    case SFD_ELECTROMAG2: which == 0 ? em2_half1(h->em2, L, rel, s) : em2_half2(h->em2, L, rel, s); break;
-    case SFD_SEISMIC2: which == 0 ? seis2_half1(h->s2, L, rel, s) : seis2_half2(h->s2, L, rel, s); break;
+    case SFD_ELECTROMAG2:
+      if (cpml2d(h->cfg)) which == 0 ? em2_c2d_half1(h->em2, L, rel, s) : em2_c2d_half2(h->em2, L, rel, s);
+      else which == 0 ? em2_half1(h->em2, L, rel, s) : em2_half2(h->em2, L, rel, s);
+      break;
+    case SFD_SEISMIC2:
+      if (cpml2d(h->cfg)) which == 0 ? seis2_c2d_half1(h->s2, L, rel, s) : seis2_c2d_half2(h->s2, L, rel, s);
+      else which == 0 ? seis2_half1(h->s2, L, rel, s) : seis2_half2(h->s2, L, rel, s);
+      break;
     case SFD_SEISMIC25: which == 0 ? seis25_half1(h->s25, L, rel, s) : seis25_half2(h->s25, L, rel, s); break;
     case SFD_ELECTROMAG25: which == 0 ? em25_half1(h->em25, L, rel, s) : em25_half2(h->em25, L, rel, s); break;
     case SFD_ELECTROMAG2C: which == 0 ? em2c_half1(h->em2c, L, rel, s) : em2c_half2(h->em2c, L, rel, s); break;
@@ -798,7 +834,7 @@ int32_t create_handle(const sfd_config* cfg, void* dev_state, size_t state_bytes
   h->L = L;
   h->base = (char*)dev_state;
   h->stream = (cudaStream_t)stream;
-  h->single = has_single_pass(cfg->kind) && !(cfg->flags & SFD_FLAG_TWO_PASS);
+  h->single = single_pass(*cfg);
   h->cap_stream = nullptr;
   if (graphs) {
     e = cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking);
@@ -1178,10 +1214,38 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
   return SFD_OK;
 }
 
+int32_t sfd_set_cpml2d(sfd_handle* h, const double* fields, int64_t count) {
+  g_err.clear();
+  if (!h || !fields) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  const sfd_config& c = h->cfg;
+  if (!cpml2d(c)) return fail(SFD_ERR_STATE, "sfd_set_cpml2d needs a handle created with SFD_FLAG_CPML_2D");
+  const size_t N2 = (size_t)c.nx * c.nz;
+  if (count != (int64_t)(6 * N2))
+    return fail(SFD_ERR_BAD_ARG, "2-D CPML fields need 6 planes of %dx%d values, got %lld", c.nx, c.nz, (long long)count);
+  if (!all_finite(fields, (size_t)count)) return fail(SFD_ERR_BAD_ARG, "2-D CPML fields contain NaN or Inf");
+  std::vector<float> planes(6 * N2);
+  for (int o = 0; o < 2; ++o) {
+    const double *K = fields + (size_t)(3 * o) * N2, *A = K + N2, *B = A + N2;
+    float *ik = planes.data() + (size_t)(3 * o) * N2, *a = ik + N2, *b = a + N2;
+    for (size_t n = 0; n < N2; ++n) {
+      if (!(K[n] > 0)) return fail(SFD_ERR_BAD_ARG, "2-D CPML kappa must be positive (cell %zu)", n);
+      ik[n] = (float)(1.0 / K[n]);
+      a[n] = (float)A[n];
+      b[n] = (float)B[n];
+    }
+  }
+  int r = upload_pitched(h, h->coef(ncoef(c.kind)), planes.data(), 6 * (size_t)c.nz);
+  if (r) return r;
+  CK(cudaStreamSynchronize(h->stream));
+  h->have_cpml = true;
+  return SFD_OK;
+}
+
 int32_t sfd_set_cpml(sfd_handle* h, const double* prof, int64_t count) {
   g_err.clear();
   if (!h || !prof) return fail(SFD_ERR_BAD_ARG, "NULL argument");
   const sfd_config& c = h->cfg;
+  if (cpml2d(c)) return fail(SFD_ERR_STATE, "a SFD_FLAG_CPML_2D handle takes its CPML from sfd_set_cpml2d");
   const bool three = is3(c.kind);
   const int lens[3] = {c.nx, three ? c.ny : c.nz, c.nz};
   const double deltas[3] = {c.dx, three ? c.dy : c.dz, c.dz};
@@ -1385,6 +1449,12 @@ int32_t sfd_get_memory(sfd_handle* h, int32_t index, float* host, int64_t count)
   if (index < 0 || index >= (int)strlen(ax)) return fail(SFD_ERR_BAD_ARG, "memory variable %d out of range", index);
   const int NX = c.nx, NY = c.ny, NZ = c.nz, W = c.npml, P = h->L.P;
   if (count != (int64_t)NX * NY * NZ) return fail(SFD_ERR_BAD_ARG, "memory variable needs %d*%d*%d values", NX, NY, NZ);
+  if (cpml2d(c)) {  // stored on the full grid, rows of pitch P
+    CK(cudaMemcpy2DAsync(host, sizeof(float) * NX, h->m(index), sizeof(float) * P, sizeof(float) * NX, NZ,
+                         cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return SFD_OK;
+  }
   std::vector<float> s(h->L.mem_sz[index]);
   CK(cudaMemcpyAsync(s.data(), h->m(index), sizeof(float) * s.size(), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));

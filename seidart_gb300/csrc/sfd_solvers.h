@@ -22,6 +22,14 @@ struct IoArgs {
   float* traces;      // [nstep][nch][nrec]
 };
 
+// The driver's 2-D CPML coefficients (SFD_FLAG_CPML_2D): FP32 planes of
+// pitch P, [0] of the full offset, [1] of the half offset: 1/K, a, b; and
+// 1/dx, 1/dz.  Empty (null planes) otherwise.
+struct Cpml2d {
+  const float *ik[2], *a[2], *b[2];
+  float idx, idz;
+};
+
 struct Em2Args {
   int NX, NZ, P, W;
   float *Ex, *Ez, *Hy;
@@ -31,6 +39,7 @@ struct Em2Args {
   const float *CAx, *CBx, *CAz, *CBz;
   AxisTab X, Z;
   float dbH;
+  Cpml2d c2d;
   IoArgs io;
 };
 
@@ -62,6 +71,7 @@ struct Seis2Args {
   const float *gxp, *gzp;                        // 1 - gamma
   const float* q3;                               // b_x_half indexed by the z index (legacy loop 1)
   AxisTab X, Z;
+  Cpml2d c2d;
   IoArgs io;
 };
 
@@ -159,6 +169,12 @@ Launch em2_launch(const Em2Args& a);
 void em2_half1(const Em2Args& a, const Launch& L, int rel, cudaStream_t s);
 void em2_half2(const Em2Args& a, const Launch& L, int rel, cudaStream_t s);
 void em2_finalize(const Em2Args& a, int t_last, cudaStream_t s);
+
+// Two-pass steps with the driver's 2-D CPML fields (cpml2d.cu).
+void em2_c2d_half1(const Em2Args& a, const Launch& L, int rel, cudaStream_t s);
+void em2_c2d_half2(const Em2Args& a, const Launch& L, int rel, cudaStream_t s);
+void seis2_c2d_half1(const Seis2Args& a, const Launch& L, int rel, cudaStream_t s);
+void seis2_c2d_half2(const Seis2Args& a, const Launch& L, int rel, cudaStream_t s);
 
 Launch seis2_launch(const Seis2Args& a);
 void seis2_half1(const Seis2Args& a, const Launch& L, int rel, cudaStream_t s);

@@ -60,6 +60,7 @@ MEMORY = {
 FLAG_TWO_PASS = 1
 FLAG_STREAMING = 2
 FLAG_LEGACY_QUIRKS = 4
+FLAG_CPML_2D = 32  # electromag2, seismic2: CPML from the driver's 2-D fields (set_cpml2d)
 # density_method (the driver's argument, src/seidart/routines/classes.py:311) -> flag bits
 DENSITY_FLAGS = {"arithmetic": 0, "none": 8, "geometric": 16, "harmonic": 24}
 
@@ -196,6 +197,18 @@ class FDTDSolver:
         else:
             arr = np.ascontiguousarray(profiles, dtype=np.float64)
         check(self._L.sfd_set_cpml(self._h, _dptr(arr), arr.size))
+
+    def set_cpml2d(self, fields) -> None:
+        """The driver's 2-D CPML fields (solver created with ``FLAG_CPML_2D``):
+        array (6, NZ, NX) of K, a, b, K_half, a_half, b_half, or a dict of
+        those names."""
+        names = ("K", "a", "b", "K_half", "a_half", "b_half")
+        if isinstance(fields, dict):
+            fields = np.stack([np.asarray(fields[n], dtype=np.float64) for n in names])
+        arr = np.ascontiguousarray(fields, dtype=np.float64)
+        if arr.shape != (6, self.grid.nz, self.grid.nx):
+            raise ValueError(f"2-D CPML fields must be (6, {self.grid.nz}, {self.grid.nx})")
+        check(self._L.sfd_set_cpml2d(self._h, _dptr(arr), arr.size))
 
     def share_model(self, other: "FDTDSolver") -> None:
         """Read ``other``'s update coefficients instead of a copy (shots of one model)."""

@@ -123,3 +123,17 @@ def test_cli_seismic_options_match_oracle(gpu, tmp_path, density, legacy):
     _, tr, _, _ = orun(SEISMIC2, g, p["planes"], cp.pack_profiles(p["profiles"]), p["src_ijk"], p["srcfn"], rec,
                        case.nstep, legacy=legacy, density=density, stress_src=p["stress_srcfn"])
     assert rel_l2(np.load(tmp_path / "traces.npy"), tr) <= 1e-5
+
+
+def test_cpml_mode_2d_refused_where_it_cannot_be_honoured(tmp_path):
+    """--cpml-mode 2d: a 2.5-D model (the driver writes no y fields) and a
+    project without the CPML files end with exit status 1."""
+    case = sy.small_case(SEISMIC2, seed=2, nx=40, nz=34, npml=5, nstep=20)
+    path, _ = write_project(case, tmp_path)
+    assert cli.run([path, "seismic=true", "--workdir", str(tmp_path), "--cpml-mode", "2d"]) == 1
+    from seidart_gb300 import SEISMIC25
+    d = tmp_path / "three"
+    d.mkdir()
+    case3 = sy.small_case(SEISMIC25, seed=3, nx=30, nz=28, ny=20, npml=5, nstep=20)
+    path3, _ = write_project(case3, d)
+    assert cli.run([path3, "seismic=true", "--workdir", str(d), "--cpml-mode", "2d"]) == 1

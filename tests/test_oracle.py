@@ -187,3 +187,30 @@ def test_blow_up_detected():
     c.grid.dt *= 4.0
     _, _, norm, blew = run_oracle(c)
     assert blew and norm > 1e25
+
+
+def _planes2d(c):
+    g = c.grid
+    seismic = g.kind == SEISMIC2
+    return cp.driver_cpml_planes(g.nx, g.nz, g.npml, g.dx, g.dz, g.dt, c.f0, c.meta["vmax"], seismic)
+
+
+@pytest.mark.parametrize("kind", [ELECTROMAG2, SEISMIC2])
+@pytest.mark.parametrize("seed,nx,nz", [(7, 38, 31), (8, 27, 40)])
+def test_cpml2d_restatements_agree(kind, seed, nx, nz):
+    """The driver's 2-D CPML fields in place of the axis profiles: C++ loops
+    against the numpy slices, and different from the 1-D run."""
+    c = sy.small_case(kind, seed=seed, nx=nx, nz=nz, npml=6, nstep=110)
+    g = c.grid
+    F = _planes2d(c)
+    prof = cp.pack_profiles(c.profiles)
+    st, tr, _, blew = oracle.run(kind, g, c.planes, prof, c.src_ijk, c.srcfn, c.rec_ijk, c.nstep, cpml2d=F)
+    assert not blew
+    fn = numpy_ref.electromag2 if kind == ELECTROMAG2 else numpy_ref.seismic2
+    Fn, Mn, Tn = fn(g.nx, g.nz, g.dx, g.dz, g.dt, prof, c.planes, (c.src_ijk[0], c.src_ijk[2]), c.srcfn, c.nstep,
+                    rec=c.rec_ijk, cpml2d=F)
+    assert rel_l2(st.fields, Fn) < 1e-12
+    assert rel_l2(st.memory, Mn, floor=1e-300) < 1e-12
+    assert rel_l2(tr, Tn) < 1e-12
+    _, tr1, _, _ = run_oracle(c)
+    assert rel_l2(tr, tr1) > 1e-6
