@@ -154,6 +154,25 @@ def seis2_bytes(grid, atten=False):
     return {"half1": h1, "half2": h2, "step": step, "per_cell_step": step / cells}
 
 
+def em25_bytes(grid):
+    """electromag25 with y-marching: H kernel reads Hx Hy Hz and Ex Ey Ez, writes H; E kernel reads all six,
+    writes E; 6 coefficients per (x,z) column amortised over NY; psi: 12 on strips (2 per axis per kernel)."""
+    fx, fy, fz = strip_fractions(grid)
+    cells = grid.nx * grid.ny * grid.nz
+    col = grid.nx * grid.nz
+    psi = 2 * 8 * (fx + fy + fz)
+    h1 = (6 * 4 + 3 * 4 + psi) * cells
+    h2 = (6 * 4 + 3 * 4 + psi) * cells + 6 * 4 * col
+    step = (6 * 8 + 2 * psi) * cells + 6 * 4 * col
+    return {"half1": h1, "half2": h2, "step": step, "per_cell_step": step / cells}
+
+
+def em2c_bytes(grid):
+    """electromag2c: electromag2 with every field, coefficient and memory variable a (real, imaginary) pair."""
+    b = em2_bytes(grid)
+    return {k: 2 * v for k, v in b.items()}
+
+
 def seis25_bytes(grid, atten=True):
     """seismic25 with y-marching: coefficients (21 stiffness, 3 dt/rho, 3 gamma) are read once per (x,z)
     column and amortised over NY.  Stress kernel: read 9 fields, write 6 stresses; velocity kernel: read
@@ -170,9 +189,9 @@ def seis25_bytes(grid, atten=True):
 
 # ---------------------------------------------------------------------------
 
-def make_solver(case, device):
+def make_solver(case, device, flags=0):
     from seidart_gb300.solver import FDTDSolver
-    s = FDTDSolver(case.grid, case.nstep, len(case.rec_ijk), device=device, **case.solver_options())
+    s = FDTDSolver(case.grid, case.nstep, len(case.rec_ijk), device=device, flags=flags, **case.solver_options())
     s.set_model(case.planes)
     s.set_cpml(case.profiles)
     s.set_source(case.src_ijk, case.srcfn)
@@ -190,9 +209,9 @@ def launches_per_shot(kind, nstep, single_pass=True):
     return per * nstep + nstep // 32 + 3 + (1 if kind == ELECTROMAG25 else 0)
 
 
-def bench_plain(case, device, flush, stream, peak, bytes_fn, steps, warmup):
+def bench_plain(case, device, flush, stream, peak, bytes_fn, steps, warmup, flags=0):
     """One plain configuration: shots of `case`, kernel times, roofline fractions."""
-    s = make_solver(case, device)
+    s = make_solver(case, device, flags)
     ms = time_shots(s, case.nstep, max(1, steps), warmup, flush, stream)
     kt = kernel_times(s, stream, n=20)
     b = bytes_fn(case.grid)
@@ -661,6 +680,22 @@ def run_ours(args):
         elif args.only == "seismic25":
             rec = bench_plain(sy.seismic25_ice(nstep=args.time_steps if args.time_steps != 6000 else 3000),
                               device, flush, stream, peak, seis25_bytes, args.steps, args.warmup)
+        elif args.only == "electromag2_step":  # the workload with one launch per step (em2_step_kernel)
+            from seidart_gb300.solver import FLAG_STREAMING
+            rec = bench_plain(sy.electromag2_layers(nstep=args.time_steps), device, flush, stream, peak, em2_bytes,
+                              args.steps, args.warmup, flags=FLAG_STREAMING)
+        elif args.only == "electromag25":  # a 2.5-D EM model of the seismic25 workload's grid
+            from seidart_gb300 import ELECTROMAG25
+            c = sy.small_case(ELECTROMAG25, seed=3, nx=630, nz=330, ny=70, npml=15,
+                              nstep=args.time_steps if args.time_steps != 6000 else 300)
+            c.name = "electromag25 random 600x40x300"
+            rec = bench_plain(c, device, flush, stream, peak, em25_bytes, args.steps, args.warmup)
+        elif args.only == "electromag2c":  # complex permittivities, 2000 x 1500 cells
+            from seidart_gb300 import ELECTROMAG2C
+            c = sy.small_case(ELECTROMAG2C, seed=3, nx=2000, nz=1500, npml=20,
+                              nstep=args.time_steps if args.time_steps != 6000 else 300)
+            c.name = "electromag2c random 1960x1460"
+            rec = bench_plain(c, device, flush, stream, peak, em2c_bytes, args.steps, args.warmup)
         elif args.only == "batched":
             tiling = tuple(int(v) for v in args.batch_tiling.split("x")) if args.batch_tiling else None
             rec = bench_batched(device, flush, stream, peak, None, runs=args.steps,
@@ -827,7 +862,8 @@ def main(argv=None):
     ap.add_argument("--time-steps", type=int, default=6000,
                     help="time steps per headline shot (6000 = the workload; smaller only for profiler runs)")
     ap.add_argument("--skip-batched", action="store_true")
-    ap.add_argument("--only", choices=["seismic2", "seismic25", "batched", "adjoint"],
+    ap.add_argument("--only", choices=["seismic2", "seismic25", "batched", "adjoint", "electromag2_step",
+                                       "electromag25", "electromag2c"],
                     help="run one secondary leg alone and print its record (for profiler runs)")
     ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--skip-parity", action="store_true",

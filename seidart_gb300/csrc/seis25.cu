@@ -27,6 +27,16 @@ namespace {
 
 constexpr int BX = 32, BZ = 4;
 
+// Resident blocks per SM the two kernels are compiled for (registers per
+// thread = 65536 / (128 x blocks)); build-time tunables, the defaults the
+// measured best on the 630 x 70 x 330 grid.
+#ifndef SEIS25_STRESS_BLOCKS
+#define SEIS25_STRESS_BLOCKS 5
+#endif
+#ifndef SEIS25_VELOCITY_BLOCKS
+#define SEIS25_VELOCITY_BLOCKS 8
+#endif
+
 // The stress kernel holds a column's 33 stiffness averages, its axis tables,
 // the carried velocities and nine memory variables: at 4 blocks of 128
 // threads per SM (128 registers) nothing spills, and that beat 8 blocks at
@@ -34,7 +44,7 @@ constexpr int BX = 32, BZ = 4;
 // the 630 x 70 x 330 grid).  The velocity kernel needs fewer registers and
 // runs best at 8 blocks, where more resident warps hide the y-march's HBM
 // latency.
-__global__ void __launch_bounds__(BX * BZ, 4) seis25_stress_kernel(Seis25Args a, int rel) {
+__global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS) seis25_stress_kernel(Seis25Args a, int rel) {
   const Ctl* ctl = a.io.ctl;
   const int t = ctl->base + rel;
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && t > ctl->run_start) {
@@ -57,28 +67,27 @@ __global__ void __launch_bounds__(BX * BZ, 4) seis25_stress_kernel(Seis25Args a,
 
   // The 33 stiffness averages of the four loops at this column, formed once
   // on the host in FP64 (planes 0-14 loop 1, 15-20 loop 2, 21-26 loop 3,
-  // 27-32 loop 4; zero where the loop does not update the cell).
-  const size_t cpl = (size_t)NZ * P, cpc = (size_t)k * P + i;
-  auto cf = [&](int q) { return __ldg(a.C + q * cpl + cpc); };
-  float p11 = 0, p12 = 0, p13 = 0, p14 = 0, p15 = 0, p16 = 0, p22 = 0, p23 = 0, p24 = 0, p25 = 0, p26 = 0;
-  float p33 = 0, p34 = 0, p35 = 0, p36 = 0;
-  if (L1) {  // over (i+1,k) (i,k) (i,k-1) (i+1,k-1)
-    p11 = cf(0); p12 = cf(1); p13 = cf(2); p14 = cf(3); p15 = cf(4); p16 = cf(5);
-    p22 = cf(6); p23 = cf(7); p24 = cf(8); p25 = cf(9); p26 = cf(10);
-    p33 = cf(11); p34 = cf(12); p35 = cf(13); p36 = cf(14);
+  // 27-32 loop 4; zero where the loop does not update the cell).  Each thread
+  // keeps its column's values in its own shared-memory slots and reads them at
+  // every y step: held in registers they capped the kernel at 4 blocks of 128
+  // threads per SM, too few loads in flight to cover the y-march's latency.
+  __shared__ float sC[33 * BX * BZ];
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  {
+    const size_t cpl = (size_t)NZ * P, cpc = (size_t)k * P + i;
+    auto cf = [&](int q, bool on) { return on ? __ldg(a.C + q * cpl + cpc) : 0.0f; };
+#pragma unroll
+    for (int q = 0; q < 15; ++q) sC[q * BX * BZ + tid] = cf(q, L1);   // over (i+1,k) (i,k) (i,k-1) (i+1,k-1)
+#pragma unroll
+    for (int q = 15; q < 21; ++q) sC[q * BX * BZ + tid] = cf(q, L2);  // over (i,k) (i-1,k) (i,k-1) (i-1,k-1)
+#pragma unroll
+    for (int q = 21; q < 27; ++q) sC[q * BX * BZ + tid] = cf(q, L3);  // over (i,k+1) (i,k) (i-1,k) (i-1,k+1)
+#pragma unroll
+    for (int q = 27; q < 33; ++q) sC[q * BX * BZ + tid] = cf(q, L4);  // over (i+1,k) (i,k) (i,k+1) (i+1,k+1)
   }
-  float q16 = 0, q26 = 0, q36 = 0, q46 = 0, q56 = 0, q66 = 0;
-  if (L2) {  // over (i,k) (i-1,k) (i,k-1) (i-1,k-1)
-    q16 = cf(15); q26 = cf(16); q36 = cf(17); q46 = cf(18); q56 = cf(19); q66 = cf(20);
-  }
-  float r15 = 0, r25 = 0, r35 = 0, r45 = 0, r55 = 0, r56 = 0;
-  if (L3) {  // over (i,k+1) (i,k) (i-1,k) (i-1,k+1)
-    r15 = cf(21); r25 = cf(22); r35 = cf(23); r45 = cf(24); r55 = cf(25); r56 = cf(26);
-  }
-  float s14 = 0, s24 = 0, s34 = 0, s44 = 0, s45 = 0, s46 = 0;
-  if (L4) {  // over (i+1,k) (i,k) (i,k+1) (i+1,k+1)
-    s14 = cf(27); s24 = cf(28); s34 = cf(29); s44 = cf(30); s45 = cf(31); s46 = cf(32);
-  }
+  // volatile: read at each use, not hoisted back into registers
+  const volatile float* cc = sC + tid;
+  auto C = [&](int q) -> float { return cc[q * BX * BZ]; };
 
   const bool xs = in_strip(i, NX, W), zs = in_strip(k, NZ, W);
   const int xsi = xs ? strip_idx(i, NX, W) : 0;
@@ -156,12 +165,12 @@ __global__ void __launch_bounds__(BX * BZ, 4) seis25_stress_kernel(Seis25Args a,
       const float vxx = dxx * ikxh + mvxx, vyx = dyx * ikxh + mvyx, vzx = dzx * ikxh + mvzx;
       const float vyy = dyy * iky + mvyy, vxy = dxy * iky + mvxy, vzy = dzy * iky + mvzy;
       const float vzz = dzz * ikz + mvzz, vxz = dxz * ikz + mvxz, vyz = dyz * ikz + mvyz;
-      SXX[c] = oxx + (p11 * vxx + p12 * vyy + p13 * vzz + p14 * (vyz + vzy) + p15 * (vxz + vzx) +
-                      p16 * (a.legacy ? vxy + vzy : vxy + vyx));  // Q4, :657
-      SYY[c] = oyy + (p12 * vxx + p22 * vyy + p23 * vzz + p24 * (vyz + vzy) + p25 * (vxz + vzx) +
-                      p26 * (vyx + vxy));
-      SZZ[c] = ozz + (p13 * vxx + p23 * vyy + p33 * vzz + p34 * (vyz + vzy) + p35 * (vxz + vzx) +
-                      p36 * (vyx + vxy));
+      SXX[c] = oxx + (C(0) * vxx + C(1) * vyy + C(2) * vzz + C(3) * (vyz + vzy) + C(4) * (vxz + vzx) +
+                      C(5) * (a.legacy ? vxy + vzy : vxy + vyx));  // Q4, :657
+      SYY[c] = oyy + (C(1) * vxx + C(6) * vyy + C(7) * vzz + C(8) * (vyz + vzy) + C(9) * (vxz + vzx) +
+                      C(10) * (vyx + vxy));
+      SZZ[c] = ozz + (C(2) * vxx + C(7) * vyy + C(11) * vzz + C(12) * (vyz + vzy) + C(13) * (vxz + vzx) +
+                      C(14) * (vyx + vxy));
     }
     // ---- Loop 2: sigmaxy (j <= NY-2): x-, y+, z-
     if (l2) {
@@ -175,8 +184,8 @@ __global__ void __launch_bounds__(BX * BZ, 4) seis25_stress_kernel(Seis25Args a,
       const float vyy = dyy * ikyh + mvyy, vxy = dxy * ikyh + mvxy, vzy = dzy * ikyh + mvzy;
       const float vzz = dzz * ikzh + mvzz, vyz = dyz * ikzh + mvyz;
       const float vzx = dzx * idx, vxz = dxz * idz;  // left unscaled, :701-707
-      SXY[c] = oxy + (q16 * vxx + q26 * vyy + q36 * vzz + q46 * (vzy + vyz) + q56 * (vzx + vxz) +
-                      q66 * (vyx + vxy));
+      SXY[c] = oxy + (C(15) * vxx + C(16) * vyy + C(17) * vzz + C(18) * (vzy + vyz) + C(19) * (vzx + vxz) +
+                      C(20) * (vyx + vxy));
     }
     // ---- Loop 3: sigmaxz (j >= 1): x-, y-, z+
     if (l3) {
@@ -189,8 +198,8 @@ __global__ void __launch_bounds__(BX * BZ, 4) seis25_stress_kernel(Seis25Args a,
       const float vxx = dxx * ikx + mvxx, vyx = dyx * ikx + mvyx, vzx = dzx * ikx + mvzx;
       const float vyy = dyy * iky + mvyy, vxy = dxy * iky + mvxy, vzy = dzy * iky + mvzy;
       const float vzz = dzz * ikzh + mvzz, vxz = dxz * ikzh + mvxz, vyz = dyz * ikzh + mvyz;
-      SXZ[c] = oxz + (r15 * vxx + r25 * vyy + r35 * vzz + r45 * (a.legacy ? vxz + vzx : vyz + vzy) +  // Q4, :766
-                      r55 * (vxz + vzx) + r56 * (vxy + vyx));
+      SXZ[c] = oxz + (C(21) * vxx + C(22) * vyy + C(23) * vzz + C(24) * (a.legacy ? vxz + vzx : vyz + vzy) +  // Q4, :766
+                      C(25) * (vxz + vzx) + C(26) * (vxy + vyx));
     }
     // ---- Loop 4: sigmayz (j <= NY-2): x+, y+, z+
     if (l4) {
@@ -203,8 +212,8 @@ __global__ void __launch_bounds__(BX * BZ, 4) seis25_stress_kernel(Seis25Args a,
       const float vxx = dxx * ikxh + mvxx, vyx = dyx * ikxh + mvyx, vzx = dzx * ikxh + mvzx;
       const float vyy = dyy * ikyh + mvyy, vxy = dxy * ikyh + mvxy, vzy = dzy * ikyh + mvzy;
       const float vzz = dzz * ikzh + mvzz, vxz = dxz * ikzh + mvxz, vyz = dyz * ikzh + mvyz;
-      SYZ[c] = oyz + (s14 * vxx + s24 * vyy + s34 * vzz + s44 * (vyz + vzy) + s45 * (vxz + vzx) +
-                      s46 * (vyx + vxy));
+      SYZ[c] = oyz + (C(27) * vxx + C(28) * vyy + C(29) * vzz + C(30) * (vyz + vzy) + C(31) * (vxz + vzx) +
+                      C(32) * (vyx + vxy));
     }
     if (xs) { MVXX[mx] = mvxx; MVYX[mx] = mvyx; MVZX[mx] = mvzx; }
     if (ys) { MVXY[my] = mvxy; MVYY[my] = mvyy; MVZY[my] = mvzy; }
@@ -224,7 +233,7 @@ __global__ void __launch_bounds__(BX * BZ, 4) seis25_stress_kernel(Seis25Args a,
   }
 }
 
-__global__ void __launch_bounds__(BX * BZ, 8) seis25_velocity_kernel(Seis25Args a, int rel) {
+__global__ void __launch_bounds__(BX * BZ, SEIS25_VELOCITY_BLOCKS) seis25_velocity_kernel(Seis25Args a, int rel) {
   const int t = a.io.ctl->base + rel;
   const int i = blockIdx.x * BX + threadIdx.x;
   const int k = blockIdx.y * BZ + threadIdx.y;
