@@ -1,4 +1,5 @@
-"""Gradients of a receiver-trace misfit with respect to the electromag2 model.
+"""Gradients of a receiver-trace misfit with respect to the electromag2 and
+seismic2 models.
 
 ``TraceModel`` owns one single-pass electromag2 solver and its checkpoints.
 Its forward pass runs the whole shot, saving the dynamic state every
@@ -15,6 +16,14 @@ applies the FP64 chain rule from the update coefficients to the model planes.
 ``traces = TraceMisfit.apply(eps11, eps33, sigma, model)`` is differentiable
 in torch: ``eps11``, ``eps33``, ``sigma`` (sig11 = sig33) are per-cell
 (NZ, NX) FP64 tensors, and the traces are (nstep, 2, nrec) FP32 on the GPU.
+
+``SeismicTraceModel`` does the same for a seismic2 shot (any of the solver's
+step forms, the corrected physics with 1-D CPML profiles, any density
+method): the backward pass recomputes each segment by the solver's own steps
+and runs the transposed step (``csrc/adjoint_s2.cu``) over it, and the
+gradient covers all nine model planes (c11 c13 c15 c33 c35 c55 rho gamma_x
+gamma_z).  ``traces = SeismicTraceMisfit.apply(planes, model)`` is its torch
+function for a (9, NZ, NX) FP64 tensor.
 """
 from __future__ import annotations
 
@@ -46,15 +55,16 @@ def _declare(L):
     L._adj_declared = True
 
 
-class TraceModel:
-    """An electromag2 shot whose eps11, eps33 and sigma can be differentiated.
+class _Checkpointed:
+    """One solver, its checkpoints and the adjoint workspace; ``_run(planes)``
+    runs the shot saving a checkpoint per segment, ``_gradient(resid)`` runs
+    the adjoint over the segments, last first, and returns the FP64 gradient
+    planes of ``sfd_adjoint_gradient``."""
 
-    ``base_planes``: (6, NZ, NX) FP64 model (eps11 eps13 eps33 sig11 sig13 sig33);
-    eps13 and sig13 stay fixed, the other planes are replaced by the inputs.
-    """
+    nplanes = 0
 
-    def __init__(self, grid: GridSpec, base_planes, profiles, src_ijk, srcfn, rec_ijk, ckpt_every=200,
-                 device="cuda", flags=0):
+    def __init__(self, grid: GridSpec, base_planes, profiles, src_ijk, srcfn, rec_ijk, ckpt_every, device, flags,
+                 **solver_kw):
         import torch
 
         self.grid = grid
@@ -63,7 +73,7 @@ class TraceModel:
         self.srcfn = np.asarray(srcfn, dtype=np.float64)
         self.nstep = self.srcfn.shape[1]
         self.ckpt_every = int(ckpt_every)
-        self.solver = FDTDSolver(grid, self.nstep, len(rec_ijk), device=device, flags=flags)
+        self.solver = FDTDSolver(grid, self.nstep, len(rec_ijk), device=device, flags=flags, **solver_kw)
         self.solver.set_model(self.base)
         self.solver.set_cpml(profiles)
         self.solver.set_source(src_ijk, self.srcfn)
@@ -80,19 +90,10 @@ class TraceModel:
         check(L.sfd_adjoint_bytes(h, self.ckpt_every, C.byref(nb2)))
         self.work = torch.empty(int(nb2.value), dtype=torch.uint8, device=self.solver.device)
 
-    def planes_for(self, eps11, eps33, sigma):
-        p = self.base.copy()
-        p[0] = np.asarray(eps11, dtype=np.float64)
-        p[2] = np.asarray(eps33, dtype=np.float64)
-        p[3] = np.asarray(sigma, dtype=np.float64)
-        p[5] = np.asarray(sigma, dtype=np.float64)
-        return p
-
-    def forward(self, eps11, eps33, sigma):
-        """Run the shot; returns the device trace tensor (nstep, 2, nrec)."""
+    def _run(self, planes):
         s = self.solver
-        s.set_model(self.planes_for(eps11, eps33, sigma))
-        s.set_source(self.src_ijk, self.srcfn)  # the amplitude is divided by eps11 at the source
+        s.set_model(planes)
+        s.set_source(self.src_ijk, self.srcfn)  # the amplitude is divided by the model at the source
         s.reset()
         h = s._h
         for q in range(self.nseg):
@@ -101,8 +102,7 @@ class TraceModel:
         s.status()
         return s.traces_tensor().clone()
 
-    def backward(self, resid):
-        """dJ/d(eps11, eps33, sigma) for dJ/d(traces) = resid (device FP32)."""
+    def _gradient(self, resid):
         import torch
 
         r = resid.detach().to(device=self.solver.device, dtype=torch.float32).contiguous()
@@ -114,13 +114,74 @@ class TraceModel:
             n = min(self.ckpt_every, self.nstep - start)
             check(self._L.sfd_checkpoint_load(h, C.c_void_p(self.ckpt[q].data_ptr()), start))
             check(self._L.sfd_adjoint_segment(h, n))
-        g = np.empty((6, self.grid.nz, self.grid.nx))
+        g = np.empty((self.nplanes, self.grid.nz, self.grid.nx))
         check(self._L.sfd_adjoint_gradient(h, g.ctypes.data_as(C.POINTER(C.c_double)), g.size))
         torch.cuda.synchronize(self.solver.device)
-        return g[0], g[2], g[3] + g[5], g
+        return g
 
     def close(self):
         self.solver.close()
+
+
+class TraceModel(_Checkpointed):
+    """An electromag2 shot whose eps11, eps33 and sigma can be differentiated.
+
+    ``base_planes``: (6, NZ, NX) FP64 model (eps11 eps13 eps33 sig11 sig13 sig33);
+    eps13 and sig13 stay fixed, the other planes are replaced by the inputs.
+    ``flags`` are the solver's; the handle must be single-pass.
+    """
+
+    nplanes = 6
+
+    def __init__(self, grid: GridSpec, base_planes, profiles, src_ijk, srcfn, rec_ijk, ckpt_every=200,
+                 device="cuda", flags=0):
+        super().__init__(grid, base_planes, profiles, src_ijk, srcfn, rec_ijk, ckpt_every, device, flags)
+
+    def planes_for(self, eps11, eps33, sigma):
+        p = self.base.copy()
+        p[0] = np.asarray(eps11, dtype=np.float64)
+        p[2] = np.asarray(eps33, dtype=np.float64)
+        p[3] = np.asarray(sigma, dtype=np.float64)
+        p[5] = np.asarray(sigma, dtype=np.float64)
+        return p
+
+    def forward(self, eps11, eps33, sigma):
+        """Run the shot; returns the device trace tensor (nstep, 2, nrec)."""
+        return self._run(self.planes_for(eps11, eps33, sigma))
+
+    def backward(self, resid):
+        """dJ/d(eps11, eps33, sigma) for dJ/d(traces) = resid (device FP32)."""
+        g = self._gradient(resid)
+        return g[0], g[2], g[3] + g[5], g
+
+
+class SeismicTraceModel(_Checkpointed):
+    """A seismic2 shot whose nine model planes (c11 c13 c15 c33 c35 c55 rho
+    gamma_x gamma_z) can be differentiated.
+
+    ``base_planes``: (9, NZ, NX) FP64, the model before the first ``forward``.
+    ``density`` is the density averaging method; ``stress_srcfn`` (3, nstep)
+    adds the moment-tensor source at the force source's cell.  ``flags`` are
+    the solver's (any step form).
+    """
+
+    nplanes = 9
+
+    def __init__(self, grid: GridSpec, base_planes, profiles, src_ijk, srcfn, rec_ijk, ckpt_every=200,
+                 device="cuda", flags=0, density="arithmetic", stress_srcfn=None):
+        super().__init__(grid, base_planes, profiles, src_ijk, srcfn, rec_ijk, ckpt_every, device, flags,
+                         density=density)
+        if stress_srcfn is not None:
+            self.solver.set_stress_source(src_ijk, stress_srcfn)
+
+    def forward(self, planes):
+        """Run the shot with the (9, NZ, NX) model; returns the device trace
+        tensor (nstep, 2, nrec)."""
+        return self._run(np.ascontiguousarray(planes, dtype=np.float64))
+
+    def backward(self, resid):
+        """dJ/d(planes) (9, NZ, NX) FP64 for dJ/d(traces) = resid (device FP32)."""
+        return self._gradient(resid)
 
 
 def _make_function():
@@ -147,13 +208,38 @@ def _make_function():
     return TraceMisfit
 
 
+def _make_seismic_function():
+    import torch
+
+    class SeismicTraceMisfit(torch.autograd.Function):
+        """traces = SeismicTraceMisfit.apply(planes, model), planes (9, NZ, NX)."""
+
+        @staticmethod
+        def forward(ctx, planes, model):
+            ctx.model = model
+            ctx.like = planes
+            return model.forward(planes.detach().cpu().numpy())
+
+        @staticmethod
+        def backward(ctx, grad):
+            g = ctx.model.backward(grad)
+            return torch.as_tensor(g, dtype=ctx.like.dtype, device=ctx.like.device), None
+
+    return SeismicTraceMisfit
+
+
 class _Lazy:
-    _fn = None
+    """The torch function, made on first use (torch is imported then)."""
+
+    def __init__(self, make):
+        self._make = make
+        self._fn = None
 
     def __getattr__(self, name):
-        if _Lazy._fn is None:
-            _Lazy._fn = _make_function()
-        return getattr(_Lazy._fn, name)
+        if self._fn is None:
+            self._fn = self._make()
+        return getattr(self._fn, name)
 
 
-TraceMisfit = _Lazy()
+TraceMisfit = _Lazy(_make_function)
+SeismicTraceMisfit = _Lazy(_make_seismic_function)

@@ -20,6 +20,10 @@
 //          memory variables, optional attenuation v <- v (1 - gamma), the
 //          source (:898-900), the six Dirichlet faces (:903-925) and the norm.
 #include "sfd_solvers.h"
+#include "tma.cuh"
+
+#include <mutex>
+#include <cudaTypedefs.h>
 
 namespace sfd {
 
@@ -356,6 +360,402 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_VELOCITY_BLOCKS) seis25_veloci
   block_norm_to_slot(norm, a.io.slots, (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
 }
 
+// ---------------------------------------------------------------------------
+// The TMA-staged form.  Each block (32 x BZ columns, one y segment) streams
+// its y planes through a ring of RING shared-memory stages, each filled by
+// cp.async.bulk.tensor copies that one thread issues RING - 2 planes ahead
+// and every thread waits for on the stage's mbarrier:
+//   stress kernel:   the three velocities of the plane with a one-cell halo
+//                    (x from i0 - 4, so the box starts on a 16-byte boundary;
+//                    rows k0 - 1 .. k0 + BZ), and the six stresses of the
+//                    block's own cells;
+//   velocity kernel: the six stresses with the halo, the three velocities of
+//                    the own cells.
+// The plane after the segment is staged too (its velocities or stresses only)
+// for the y+ differences; the y- values are carried in registers.  A step
+// needs its plane and the next, so RING - 2 planes stay in flight while it
+// computes; the memory variables (strips only) and the results go through
+// plain loads and stores.  Boxes reaching past the grid read zeros, the
+// values the plain form substitutes there.
+#ifndef SEIS25_TMA
+#define SEIS25_TMA 1
+#endif
+
+constexpr int HX = 4;                  // x halo of the staged tiles (16 bytes)
+constexpr int VW = BX + 2 * HX;        // 40 floats per staged row
+constexpr int VH = BZ + 2;             // rows k0 - 1 .. k0 + BZ
+constexpr int RING = 4;                // staged planes per block
+constexpr int HALO3 = 3 * VH * VW;     // velocities with the halo
+constexpr int HALO6 = 6 * VH * VW;     // stresses with the halo
+constexpr int OWN3 = 3 * BZ * BX;
+constexpr int OWN6 = 6 * BZ * BX;
+constexpr int S_OWN = 736;             // stress stage: own stresses after the velocity halo, 128-byte aligned
+constexpr int S_STAGE = S_OWN + OWN6;  // 6016 bytes
+constexpr int V_OWN = HALO6;           // velocity stage: own velocities after the stress halo
+constexpr int V_STAGE = V_OWN + OWN3;  // 7296 bytes
+static_assert(S_OWN >= HALO3 && (S_OWN * 4) % 128 == 0 && (S_STAGE * 4) % 128 == 0, "stage alignment");
+static_assert((V_OWN * 4) % 128 == 0 && (V_STAGE * 4) % 128 == 0, "stage alignment");
+
+// Records a wait that ran out and lets the copies this block already issued
+// land (each again within the limit) before its shared memory is released.
+__device__ void staged_wait_failed(const Seis25Args& a, uint64_t* full, int n, int np) {
+  atomicExch(const_cast<int*>(&a.io.ctl->err), 1);
+  const int issued = min(np, n + RING);
+  for (int m = n; m < issued; ++m) tma::bar_wait(full + m % RING, (m / RING) & 1, a.wait_ns);
+}
+
+__global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS)
+    seis25_stress_tma_kernel(const __grid_constant__ Seis25Args a, int rel) {
+  extern __shared__ __align__(128) float stage[];
+  __shared__ __align__(8) uint64_t full[RING];
+  __shared__ float sC[33 * BX * BZ];
+  const Ctl* ctl = a.io.ctl;
+  const int t = ctl->base + rel;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && t > ctl->run_start) {
+    const float* ch[3] = {a.vx, a.vy, a.vz};
+    gather_receivers<3>(a.io.rec, a.io.nrec, a.io.traces, t - 1, ch, a.P, a.NY, true);
+  }
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
+  const int i0 = blockIdx.x * BX, k0 = blockIdx.y * BZ;
+  const int NX = a.NX, NY = a.NY, NZ = a.NZ, P = a.P, W = a.W;
+  const int seg = (NY + a.ysplit - 1) / a.ysplit;
+  const int j0 = blockIdx.z * seg, j1 = min(NY, j0 + seg);
+  if (j0 >= j1) return;  // the whole block
+  const int np = min(NY, j1 + 1) - j0;
+  if (tid == 0) {
+    for (int q = 0; q < RING; ++q) tma::bar_init(full + q, 1);
+    tma::fence_bar_init();
+  }
+  __syncthreads();
+  auto issue = [&](int n) {  // plane j0 + n into its stage (one thread)
+    float* st = stage + (n % RING) * S_STAGE;
+    uint64_t* bar = full + n % RING;
+    const int j = j0 + n;
+    const bool own = j < j1;
+    tma::bar_arrive_expect(bar, (own ? (HALO3 + OWN6) * 4u : HALO3 * 4u) + a.stall_tx);
+    tma::load_4d(st, &a.tm_vhalo, bar, i0 - HX, j, k0 - 1, 0);
+    if (own) tma::load_4d(st + S_OWN, &a.tm_sown, bar, i0, j, k0, 3);
+  };
+  if (tid == 0)
+    for (int n = 0; n < min(RING, np); ++n) issue(n);
+
+  const int i = i0 + tx, k = k0 + ty;
+  const bool inside = i < NX && k < NZ;
+  const bool L1 = inside && (k >= 1) && (i <= NX - 2);
+  const bool L2 = inside && (k >= 1) && (i >= 1);
+  const bool L3 = inside && (k <= NZ - 2) && (i >= 1);
+  const bool L4 = inside && (k <= NZ - 2) && (i <= NX - 2);
+  const bool active = L1 || L2 || L3 || L4;
+  const int ic = inside ? i : 0, kc = inside ? k : 0;
+  {
+    const size_t cpl = (size_t)NZ * P, cpc = (size_t)kc * P + ic;
+    auto cf = [&](int q, bool on) { return on ? __ldg(a.C + q * cpl + cpc) : 0.0f; };
+#pragma unroll
+    for (int q = 0; q < 15; ++q) sC[q * BX * BZ + tid] = cf(q, L1);
+#pragma unroll
+    for (int q = 15; q < 21; ++q) sC[q * BX * BZ + tid] = cf(q, L2);
+#pragma unroll
+    for (int q = 21; q < 27; ++q) sC[q * BX * BZ + tid] = cf(q, L3);
+#pragma unroll
+    for (int q = 27; q < 33; ++q) sC[q * BX * BZ + tid] = cf(q, L4);
+  }
+  const volatile float* cc = sC + tid;
+  auto C = [&](int q) -> float { return cc[q * BX * BZ]; };
+
+  const bool xs = inside && in_strip(i, NX, W), zs = inside && in_strip(k, NZ, W);
+  const int xsi = xs ? strip_idx(i, NX, W) : 0;
+  const int zsi = zs ? strip_idx(k, NZ, W) : 0;
+  const float ikx = a.X.ik[ic], ikxh = a.X.ikh[ic], adx = a.X.ad[ic], adxh = a.X.adh[ic];
+  const float bx = a.X.b[ic], bxh = a.X.bh[ic];
+  const float ikz = a.Z.ik[kc], ikzh = a.Z.ikh[kc], adz = a.Z.ad[kc], adzh = a.Z.adh[kc];
+  const float bz = a.Z.b[kc], bzh = a.Z.bh[kc];
+  float* __restrict__ SXX = a.sxx;
+  float* __restrict__ SYY = a.syy;
+  float* __restrict__ SZZ = a.szz;
+  float* __restrict__ SXY = a.sxy;
+  float* __restrict__ SXZ = a.sxz;
+  float* __restrict__ SYZ = a.syz;
+  float* __restrict__ MVXX = a.m_vx_x;
+  float* __restrict__ MVYX = a.m_vy_x;
+  float* __restrict__ MVZX = a.m_vz_x;
+  float* __restrict__ MVXY = a.m_vx_y;
+  float* __restrict__ MVYY = a.m_vy_y;
+  float* __restrict__ MVZY = a.m_vz_y;
+  float* __restrict__ MVXZ = a.m_vx_z;
+  float* __restrict__ MVYZ = a.m_vy_z;
+  float* __restrict__ MVZZ = a.m_vz_z;
+  size_t c = ((size_t)kc * NY + j0) * P + ic;
+  float pvx = 0.f, pvy = 0.f, pvz = 0.f;
+  if (active && j0 >= 1) { pvx = __ldg(a.vx + c - P); pvy = __ldg(a.vy + c - P); pvz = __ldg(a.vz + c - P); }
+  const int hc = (ty + 1) * VW + tx + HX;  // own cell in a halo tile
+  const int oc = ty * BX + tx;             // own cell in an own-cells tile
+  for (int n = 0; n < j1 - j0; ++n, c += P) {
+    const int j = j0 + n;
+    const bool more = n + 1 < np;
+    bool ok = tma::bar_wait(full + n % RING, (n / RING) & 1, a.wait_ns);
+    if (more && ok) ok = tma::bar_wait(full + (n + 1) % RING, ((n + 1) / RING) & 1, a.wait_ns);
+    if (ok && active) {
+      const float* V = stage + (n % RING) * S_STAGE;
+      const float* Vn = stage + ((n + 1) % RING) * S_STAGE;
+      const float* S = V + S_OWN;
+      constexpr int F = VH * VW;
+      const float cvx = V[hc], cvy = V[F + hc], cvz = V[2 * F + hc];
+      const float nvx = more ? Vn[hc] : 0.f, nvy = more ? Vn[F + hc] : 0.f, nvz = more ? Vn[2 * F + hc] : 0.f;
+      const float xmx = V[hc - 1], xmy = V[F + hc - 1], xmz = V[2 * F + hc - 1];
+      const float xpx = V[hc + 1], xpy = V[F + hc + 1], xpz = V[2 * F + hc + 1];
+      const float zmx = V[hc - VW], zmy = V[F + hc - VW], zmz = V[2 * F + hc - VW];
+      const float zpx = V[hc + VW], zpy = V[F + hc + VW], zpz = V[2 * F + hc + VW];
+      const bool ys = in_strip(j, NY, W);
+      const size_t mx = ((size_t)k * NY + j) * (2 * W) + xsi;
+      const size_t my = ((size_t)k * (2 * W) + (ys ? strip_idx(j, NY, W) : 0)) * P + i;
+      const size_t mz = ((size_t)zsi * NY + j) * P + i;
+      float mvxx = 0, mvyx = 0, mvzx = 0, mvxy = 0, mvyy = 0, mvzy = 0, mvxz = 0, mvyz = 0, mvzz = 0;
+      if (xs) { mvxx = MVXX[mx]; mvyx = MVYX[mx]; mvzx = MVZX[mx]; }
+      if (ys) { mvxy = MVXY[my]; mvyy = MVYY[my]; mvzy = MVZY[my]; }
+      if (zs) { mvxz = MVXZ[mz]; mvyz = MVYZ[mz]; mvzz = MVZZ[mz]; }
+      const bool l1 = L1 && j >= 1, l2 = L2 && j <= NY - 2, l3 = L3 && j >= 1, l4 = L4 && j <= NY - 2;
+      const float iky = a.Y.ik[j], ikyh = a.Y.ikh[j], ady = a.Y.ad[j], adyh = a.Y.adh[j];
+      const float by = a.Y.b[j], byh = a.Y.bh[j];
+      if (l1) {  // sigmaxx, sigmayy, sigmazz: x+, y-, z- differences (:616-678)
+        const float dxx = xpx - cvx, dyx = xpy - cvy, dzx = xpz - cvz;
+        const float dyy = cvy - pvy, dxy = cvx - pvx, dzy = cvz - pvz;
+        const float dzz = cvz - zmz, dxz = cvx - zmx, dyz = cvy - zmy;
+        if (xs) { mvxx = bxh * mvxx + adxh * dxx; mvyx = bxh * mvyx + adxh * dyx; mvzx = bxh * mvzx + adxh * dzx; }
+        if (ys) { mvyy = by * mvyy + ady * dyy; mvxy = by * mvxy + ady * dxy; mvzy = by * mvzy + ady * dzy; }
+        if (zs) { mvzz = bz * mvzz + adz * dzz; mvxz = bz * mvxz + adz * dxz; mvyz = bz * mvyz + adz * dyz; }
+        const float vxx = dxx * ikxh + mvxx, vyx = dyx * ikxh + mvyx, vzx = dzx * ikxh + mvzx;
+        const float vyy = dyy * iky + mvyy, vxy = dxy * iky + mvxy, vzy = dzy * iky + mvzy;
+        const float vzz = dzz * ikz + mvzz, vxz = dxz * ikz + mvxz, vyz = dyz * ikz + mvyz;
+        SXX[c] = S[oc] + (C(0) * vxx + C(1) * vyy + C(2) * vzz + C(3) * (vyz + vzy) + C(4) * (vxz + vzx) +
+                          C(5) * (a.legacy ? vxy + vzy : vxy + vyx));  // Q4, :657
+        SYY[c] = S[OWN6 / 6 + oc] + (C(1) * vxx + C(6) * vyy + C(7) * vzz + C(8) * (vyz + vzy) +
+                                     C(9) * (vxz + vzx) + C(10) * (vyx + vxy));
+        SZZ[c] = S[2 * (OWN6 / 6) + oc] + (C(2) * vxx + C(7) * vyy + C(11) * vzz + C(12) * (vyz + vzy) +
+                                           C(13) * (vxz + vzx) + C(14) * (vyx + vxy));
+      }
+      if (l2) {  // sigmaxy: x-, y+, z- (:681-725)
+        const float dxx = cvx - xmx, dyx = cvy - xmy, dzx = cvz - xmz;
+        const float dyy = nvy - cvy, dxy = nvx - cvx, dzy = nvz - cvz;
+        const float dzz = cvz - zmz, dxz = cvx - zmx, dyz = cvy - zmy;
+        if (xs) { mvxx = bx * mvxx + adx * dxx; mvyx = bx * mvyx + adx * dyx; mvzx = bx * mvzx + adx * dzx; }
+        if (ys) { mvyy = byh * mvyy + adyh * dyy; mvxy = byh * mvxy + adyh * dxy; mvzy = byh * mvzy + adyh * dzy; }
+        if (zs) { mvzz = bzh * mvzz + adzh * dzz; mvxz = bzh * mvxz + adzh * dxz; mvyz = bzh * mvyz + adzh * dyz; }
+        const float vxx = dxx * ikx + mvxx, vyx = dyx * ikx + mvyx;
+        const float vyy = dyy * ikyh + mvyy, vxy = dxy * ikyh + mvxy, vzy = dzy * ikyh + mvzy;
+        const float vzz = dzz * ikzh + mvzz, vyz = dyz * ikzh + mvyz;
+        const float vzx = dzx * a.idx, vxz = dxz * a.idz;  // left unscaled, :701-707
+        SXY[c] = S[3 * (OWN6 / 6) + oc] + (C(15) * vxx + C(16) * vyy + C(17) * vzz + C(18) * (vzy + vyz) +
+                                           C(19) * (vzx + vxz) + C(20) * (vyx + vxy));
+      }
+      if (l3) {  // sigmaxz: x-, y-, z+ (:728-771)
+        const float dxx = cvx - xmx, dyx = cvy - xmy, dzx = cvz - xmz;
+        const float dyy = cvy - pvy, dzy = cvz - pvz, dxy = cvx - pvx;
+        const float dzz = zpz - cvz, dxz = zpx - cvx, dyz = zpy - cvy;
+        if (xs) { mvxx = bx * mvxx + adx * dxx; mvyx = bx * mvyx + adx * dyx; mvzx = bx * mvzx + adx * dzx; }
+        if (ys) { mvyy = by * mvyy + ady * dyy; mvxy = by * mvxy + ady * dxy; mvzy = by * mvzy + ady * dzy; }
+        if (zs) { mvzz = bzh * mvzz + adzh * dzz; mvxz = bzh * mvxz + adzh * dxz; mvyz = bzh * mvyz + adzh * dyz; }
+        const float vxx = dxx * ikx + mvxx, vyx = dyx * ikx + mvyx, vzx = dzx * ikx + mvzx;
+        const float vyy = dyy * iky + mvyy, vxy = dxy * iky + mvxy, vzy = dzy * iky + mvzy;
+        const float vzz = dzz * ikzh + mvzz, vxz = dxz * ikzh + mvxz, vyz = dyz * ikzh + mvyz;
+        SXZ[c] = S[4 * (OWN6 / 6) + oc] + (C(21) * vxx + C(22) * vyy + C(23) * vzz +
+                                           C(24) * (a.legacy ? vxz + vzx : vyz + vzy) +  // Q4, :766
+                                           C(25) * (vxz + vzx) + C(26) * (vxy + vyx));
+      }
+      if (l4) {  // sigmayz: x+, y+, z+ (:774-815)
+        const float dxx = xpx - cvx, dyx = xpy - cvy, dzx = xpz - cvz;
+        const float dyy = nvy - cvy, dxy = nvx - cvx, dzy = nvz - cvz;
+        const float dzz = zpz - cvz, dxz = zpx - cvx, dyz = zpy - cvy;
+        if (xs) { mvxx = bxh * mvxx + adxh * dxx; mvyx = bxh * mvyx + adxh * dyx; mvzx = bxh * mvzx + adxh * dzx; }
+        if (ys) { mvyy = byh * mvyy + adyh * dyy; mvxy = byh * mvxy + adyh * dxy; mvzy = byh * mvzy + adyh * dzy; }
+        if (zs) { mvzz = bzh * mvzz + adzh * dzz; mvxz = bzh * mvxz + adzh * dxz; mvyz = bzh * mvyz + adzh * dyz; }
+        const float vxx = dxx * ikxh + mvxx, vyx = dyx * ikxh + mvyx, vzx = dzx * ikxh + mvzx;
+        const float vyy = dyy * ikyh + mvyy, vxy = dxy * ikyh + mvxy, vzy = dzy * ikyh + mvzy;
+        const float vzz = dzz * ikzh + mvzz, vxz = dxz * ikzh + mvxz, vyz = dyz * ikzh + mvyz;
+        SYZ[c] = S[5 * (OWN6 / 6) + oc] + (C(27) * vxx + C(28) * vyy + C(29) * vzz + C(30) * (vyz + vzy) +
+                                           C(31) * (vxz + vzx) + C(32) * (vyx + vxy));
+      }
+      if (xs) { MVXX[mx] = mvxx; MVYX[mx] = mvyx; MVZX[mx] = mvzx; }
+      if (ys) { MVXY[my] = mvxy; MVYY[my] = mvyy; MVZY[my] = mvzy; }
+      if (zs) { MVXZ[mz] = mvxz; MVYZ[mz] = mvyz; MVZZ[mz] = mvzz; }
+      if (a.io.ssrc && i == a.io.si && j == a.io.sj && k == a.io.sk) {  // stress source: sigma_ij += f_ij(t) dt
+        const float* f = a.io.ssrc + t;
+        const int ns = a.io.nstep;
+        SXX[c] += f[0];
+        SYY[c] += f[ns];
+        SZZ[c] += f[2 * ns];
+        SXY[c] += f[3 * ns];
+        SXZ[c] += f[4 * ns];
+        SYZ[c] += f[5 * ns];
+      }
+      pvx = cvx; pvy = cvy; pvz = cvz;
+    }
+    if (!__syncthreads_and(ok)) {  // every thread is done with plane n (or a wait ran out)
+      if (tid == 0) staged_wait_failed(a, full, n, np);
+      break;
+    }
+    if (tid == 0 && n + RING < np) {
+      tma::fence_async_smem();
+      issue(n + RING);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(BX * BZ, SEIS25_VELOCITY_BLOCKS)
+    seis25_velocity_tma_kernel(const __grid_constant__ Seis25Args a, int rel) {
+  extern __shared__ __align__(128) float stage[];
+  __shared__ __align__(8) uint64_t full[RING];
+  const int t = a.io.ctl->base + rel;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
+  const int i0 = blockIdx.x * BX, k0 = blockIdx.y * BZ;
+  const int NX = a.NX, NY = a.NY, NZ = a.NZ, P = a.P, W = a.W;
+  const int seg = (NY + a.ysplit - 1) / a.ysplit;
+  const int j0 = blockIdx.z * seg, j1 = min(NY, j0 + seg);
+  float norm = 0.0f;
+  const int slot = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+  if (j0 >= j1) {  // the whole block
+    block_norm_to_slot(norm, a.io.slots, slot);
+    return;
+  }
+  const int np = min(NY, j1 + 1) - j0;
+  if (tid == 0) {
+    for (int q = 0; q < RING; ++q) tma::bar_init(full + q, 1);
+    tma::fence_bar_init();
+  }
+  __syncthreads();
+  auto issue = [&](int n) {
+    float* st = stage + (n % RING) * V_STAGE;
+    uint64_t* bar = full + n % RING;
+    const int j = j0 + n;
+    const bool own = j < j1;
+    tma::bar_arrive_expect(bar, (own ? (HALO6 + OWN3) * 4u : HALO6 * 4u) + a.stall_tx);
+    tma::load_4d(st, &a.tm_shalo, bar, i0 - HX, j, k0 - 1, 3);
+    if (own) tma::load_4d(st + V_OWN, &a.tm_vown, bar, i0, j, k0, 0);
+  };
+  if (tid == 0)
+    for (int n = 0; n < min(RING, np); ++n) issue(n);
+
+  const int i = i0 + tx, k = k0 + ty;
+  const bool inside = i < NX && k < NZ;
+  const int ic = inside ? i : 0, kc = inside ? k : 0;
+  const bool Vx = inside && (k >= 1) && (i >= 1);
+  const bool Vy = inside && (k >= 1) && (i <= NX - 2);
+  const bool Vz = inside && (k <= NZ - 2) && (i <= NX - 2);
+  const size_t pc = (size_t)kc * P + ic;
+  const size_t p2 = (size_t)NZ * P;
+  const float dtrx = Vx ? a.dtr[pc] : 0.f, dtry = Vy ? a.dtr[p2 + pc] : 0.f, dtrz = Vz ? a.dtr[2 * p2 + pc] : 0.f;
+  float gx = 1.f, gy = 1.f, gz = 1.f;
+  if (a.atten && inside) { gx = a.gp[pc]; gy = a.gp[p2 + pc]; gz = a.gp[2 * p2 + pc]; }
+  const bool xs = inside && in_strip(i, NX, W), zs = inside && in_strip(k, NZ, W);
+  const int xsi = xs ? strip_idx(i, NX, W) : 0;
+  const int zsi = zs ? strip_idx(k, NZ, W) : 0;
+  const float ikx = a.X.ik[ic], ikxh = a.X.ikh[ic], adx = a.X.ad[ic], adxh = a.X.adh[ic];
+  const float bx = a.X.b[ic], bxh = a.X.bh[ic];
+  const float ikz = a.Z.ik[kc], ikzh = a.Z.ikh[kc], adz = a.Z.ad[kc], adzh = a.Z.adh[kc];
+  const float bz = a.Z.b[kc], bzh = a.Z.bh[kc];
+  const bool xface = (i == 0) || (i == NX - 1) || (k == 0) || (k == NZ - 1);
+  float* __restrict__ VX = a.vx;
+  float* __restrict__ VY = a.vy;
+  float* __restrict__ VZ = a.vz;
+  float* __restrict__ MSXXX = a.m_sxx_x;
+  float* __restrict__ MSXYY = a.m_sxy_y;
+  float* __restrict__ MSXZZ = a.m_sxz_z;
+  float* __restrict__ MSXYX = a.m_sxy_x;
+  float* __restrict__ MSYYY = a.m_syy_y;
+  float* __restrict__ MSYZZ = a.m_syz_z;
+  float* __restrict__ MSXZX = a.m_sxz_x;
+  float* __restrict__ MSYZY = a.m_syz_y;
+  float* __restrict__ MSZZZ = a.m_szz_z;
+  size_t c = ((size_t)kc * NY + j0) * P + ic;
+  float psxy = 0.f, psyz = 0.f;
+  if (inside && j0 >= 1) { psxy = __ldg(a.sxy + c - P); psyz = __ldg(a.syz + c - P); }
+  const int hc = (ty + 1) * VW + tx + HX;
+  const int oc = ty * BX + tx;
+  constexpr int F = VH * VW;  // one field of a halo tile
+  for (int n = 0; n < j1 - j0; ++n, c += P) {
+    const int j = j0 + n;
+    const bool more = n + 1 < np;
+    bool ok = tma::bar_wait(full + n % RING, (n / RING) & 1, a.wait_ns);
+    if (more && ok) ok = tma::bar_wait(full + (n + 1) % RING, ((n + 1) / RING) & 1, a.wait_ns);
+    if (ok && inside) {
+      const float* S = stage + (n % RING) * V_STAGE;  // sxx syy szz sxy sxz syz with the halo
+      const float* Sn = stage + ((n + 1) % RING) * V_STAGE;
+      const float* V = S + V_OWN;
+      const float csxx = S[hc], csyy = S[F + hc], cszz = S[2 * F + hc];
+      const float csxy = S[3 * F + hc], csxz = S[4 * F + hc], csyz = S[5 * F + hc];
+      const float nsyy = more ? Sn[F + hc] : 0.f;
+      const bool ys = in_strip(j, NY, W);
+      const size_t mx = ((size_t)k * NY + j) * (2 * W) + xsi;
+      const size_t my = ((size_t)k * (2 * W) + (ys ? strip_idx(j, NY, W) : 0)) * P + i;
+      const size_t mz = ((size_t)zsi * NY + j) * P + i;
+      const float iky = a.Y.ik[j], ikyh = a.Y.ikh[j], ady = a.Y.ad[j], adyh = a.Y.adh[j];
+      const float by = a.Y.b[j], byh = a.Y.bh[j];
+      float vx = V[oc], vy = V[OWN3 / 3 + oc], vz = V[2 * (OWN3 / 3) + oc];
+      const bool ux = Vx && j >= 1, uy = Vy && j <= NY - 2, uz = Vz && j >= 1;
+      float m1x = 0.f, m1y = 0.f, m1z = 0.f, m2x = 0.f, m2y = 0.f, m2z = 0.f, m3x = 0.f, m3y = 0.f, m3z = 0.f;
+      if (xs) {
+        if (ux) m1x = MSXXX[mx];
+        if (uy) m2x = MSXYX[mx];
+        if (uz) m3x = MSXZX[mx];
+      }
+      if (ys) {
+        if (ux) m1y = MSXYY[my];
+        if (uy) m2y = MSYYY[my];
+        if (uz) m3y = MSYZY[my];
+      }
+      if (zs) {
+        if (ux) m1z = MSXZZ[mz];
+        if (uy) m2z = MSYZZ[mz];
+        if (uz) m3z = MSZZZ[mz];
+      }
+      if (ux) {  // :821-845
+        const float d1 = csxx - S[hc - 1], d2 = csxy - psxy, d3 = csxz - S[4 * F + hc - VW];
+        float v1 = d1 * ikx, v2 = d2 * iky, v3 = d3 * ikz;
+        if (xs) { const float m = bx * m1x + adx * d1; MSXXX[mx] = m; v1 += m; }
+        if (ys) { const float m = by * m1y + ady * d2; MSXYY[my] = m; v2 += m; }
+        if (zs) { const float m = bz * m1z + adz * d3; MSXZZ[mz] = m; v3 += m; }
+        vx = vx * gx + (v1 + v2 + v3) * dtrx;
+      }
+      if (uy) {  // :847-869
+        const float d1 = S[3 * F + hc + 1] - csxy, d2 = nsyy - csyy, d3 = csyz - S[5 * F + hc - VW];
+        float v1 = d1 * ikxh, v2 = d2 * ikyh, v3 = d3 * ikz;
+        if (xs) { const float m = bxh * m2x + adxh * d1; MSXYX[mx] = m; v1 += m; }
+        if (ys) { const float m = byh * m2y + adyh * d2; MSYYY[my] = m; v2 += m; }
+        if (zs) { const float m = bz * m2z + adz * d3; MSYZZ[mz] = m; v3 += m; }
+        vy = vy * gy + (v1 + v2 + v3) * dtry;
+      }
+      if (uz) {  // :872-896
+        const float d1 = S[4 * F + hc + 1] - csxz, d2 = csyz - psyz, d3 = S[2 * F + hc + VW] - cszz;
+        float v1 = d1 * ikxh, v2 = d2 * iky, v3 = d3 * ikzh;
+        if (xs) { const float m = bxh * m3x + adxh * d1; MSXZX[mx] = m; v1 += m; }
+        if (ys) { const float m = by * m3y + ady * d2; MSYZY[my] = m; v2 += m; }
+        if (zs) { const float m = bzh * m3z + adzh * d3; MSZZZ[mz] = m; v3 += m; }
+        vz = vz * gz + (v1 + v2 + v3) * dtrz;
+      }
+      if (i == a.io.si && j == a.io.sj && k == a.io.sk) {  // :898-900
+        vx += a.io.src[t];
+        vy += a.io.src[a.io.nstep + t];
+        vz += a.io.src[2 * a.io.nstep + t];
+      }
+      if (xface || j == 0 || j == NY - 1) { vx = 0.f; vy = 0.f; vz = 0.f; }  // :903-925
+      VX[c] = vx;
+      VY[c] = vy;
+      VZ[c] = vz;
+      norm = fmaxf(norm, norm_monitor(vx, vy, vz));
+      psxy = csxy;
+      psyz = csyz;
+    }
+    if (!__syncthreads_and(ok)) {
+      if (tid == 0) staged_wait_failed(a, full, n, np);
+      break;
+    }
+    if (tid == 0 && n + RING < np) {
+      tma::fence_async_smem();
+      issue(n + RING);
+    }
+  }
+  block_norm_to_slot(norm, a.io.slots, slot);
+}
+
 __global__ void seis25_finalize_kernel(Seis25Args a, int t_last) {
   const float* ch[3] = {a.vx, a.vy, a.vz};
   gather_receivers<3>(a.io.rec, a.io.nrec, a.io.traces, t_last, ch, a.P, a.NY, true);
@@ -372,11 +772,42 @@ Launch seis25_launch(const Seis25Args& a) {
 }
 
 void seis25_half1(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s) {
-  seis25_stress_kernel<<<L.grid, L.block, 0, s>>>(a, rel);
+  if (SEIS25_TMA)
+    seis25_stress_tma_kernel<<<L.grid, L.block, RING * S_STAGE * sizeof(float), s>>>(a, rel);
+  else
+    seis25_stress_kernel<<<L.grid, L.block, 0, s>>>(a, rel);
 }
 
 void seis25_half2(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s) {
-  seis25_velocity_kernel<<<L.grid, L.block, 0, s>>>(a, rel);
+  if (SEIS25_TMA)
+    seis25_velocity_tma_kernel<<<L.grid, L.block, RING * V_STAGE * sizeof(float), s>>>(a, rel);
+  else
+    seis25_velocity_kernel<<<L.grid, L.block, 0, s>>>(a, rel);
+}
+
+bool seis25_make_maps(Seis25Args& a, size_t field_stride) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", (void**)&encode, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      encode = nullptr;
+  });
+  if (!encode) return false;
+  // (x, y, z, field): x extent NX, so the halo past the last column reads zeros
+  const cuuint64_t dims[4] = {(cuuint64_t)a.NX, (cuuint64_t)a.NY, (cuuint64_t)a.NZ, 9};
+  const cuuint64_t strides[3] = {(cuuint64_t)a.P * 4, (cuuint64_t)a.NY * a.P * 4, (cuuint64_t)field_stride * 4};
+  const cuuint32_t ones[4] = {1, 1, 1, 1};
+  auto make = [&](CUtensorMap* m, int bx, int bz, int nf) {
+    const cuuint32_t box[4] = {(cuuint32_t)bx, 1, (cuuint32_t)bz, (cuuint32_t)nf};
+    return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a.vx, dims, strides, box, ones, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  };
+  return make(&a.tm_vhalo, VW, VH, 3) && make(&a.tm_sown, BX, BZ, 6) && make(&a.tm_shalo, VW, VH, 6) &&
+         make(&a.tm_vown, BX, BZ, 3);
 }
 
 void seis25_finalize(const Seis25Args& a, int t_last, cudaStream_t s) {

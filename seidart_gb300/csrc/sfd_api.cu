@@ -18,6 +18,7 @@
 #include "../../include/seidart_gb300.h"
 #include "host_pool.h"
 #include "adjoint.h"
+#include "adjoint_s2.h"
 #include "batch.h"
 #include "resident.h"
 #include "sfd_solvers.h"
@@ -378,7 +379,8 @@ Cpml2d cpml2d_args(const sfd_handle* h) {
   return f;
 }
 
-void bind_args(sfd_handle* h) {
+// false when the driver refuses a TMA descriptor (seismic25)
+bool bind_args(sfd_handle* h) {
   const Layout& L = h->L;
   const sfd_config& c = h->cfg;
   const int NX = c.nx, NY = c.ny, NZ = c.nz;
@@ -482,6 +484,9 @@ void bind_args(sfd_handle* h) {
       a.idx = (float)(1.0 / c.dx); a.idz = (float)(1.0 / c.dz);
       a.ysplit = L.ysplit;
       a.io = io;
+      a.wait_ns = h->wait_ns;
+      a.stall_tx = h->stall_waits ? 16u : 0u;
+      if (!seis25_make_maps(a, L.fsz)) return false;
       h->launch = seis25_launch(a);
       break;
     }
@@ -502,6 +507,7 @@ void bind_args(sfd_handle* h) {
       break;
     }
   }
+  return true;
 }
 
 void set_io_source(sfd_handle* h, int i, int j, int k) {
@@ -840,7 +846,11 @@ int32_t create_handle(const sfd_config* cfg, void* dev_state, size_t state_bytes
     e = cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaStreamCreateWithFlags"); }
   }
-  bind_args(h);
+  if (!bind_args(h)) {
+    if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+    delete h;
+    return fail(SFD_ERR_CUDA, "cuTensorMapEncodeTiled refused the seismic25 field tiles");
+  }
   e = cudaMemsetAsync(h->base, 0, L.total, h->stream);
   if (e != cudaSuccess) { cudaStreamDestroy(h->cap_stream); delete h; return cuda_fail(e, "cudaMemsetAsync"); }
   *out = h;
@@ -1540,7 +1550,9 @@ int32_t sfd_status(sfd_handle* h, int64_t* step, double* maxnorm) {
   if (step) *step = h->step;
   if (maxnorm) *maxnorm = (double)ctl.maxnorm;
   if (ctl.err)
-    return fail(SFD_ERR_TIMEOUT, "on-chip run: a neighbouring tile did not answer within %.3g s",
+    return fail(SFD_ERR_TIMEOUT,
+                h->cfg.kind == SFD_SEISMIC25 ? "seismic25 step: a staged tile did not arrive within %.3g s"
+                                             : "on-chip run: a neighbouring tile did not answer within %.3g s",
                 (double)h->wait_ns * 1e-9);
   if (!(ctl.maxnorm <= 1.0e25f))
     return fail(SFD_ERR_UNSTABLE, "field norm %g exceeded 1e25 (code became unstable and blew up)", (double)ctl.maxnorm);
@@ -1552,6 +1564,8 @@ int32_t sfd_set_wait_limit(sfd_handle* h, int64_t ns) {
   if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
   if (ns < 0) return fail(SFD_ERR_BAD_ARG, "wait limit must be >= 0 ns (0 = the default 2 s)");
   h->wait_ns = ns == 0 ? kDefaultWaitNs : (unsigned long long)ns;
+  h->s25.wait_ns = h->wait_ns;
+  invalidate_graph(h);
   return SFD_OK;
 }
 
@@ -1559,6 +1573,8 @@ int32_t sfd_test_stall_waits(sfd_handle* h, int32_t on) {
   g_err.clear();
   if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
   h->stall_waits = on != 0;
+  h->s25.stall_tx = h->stall_waits ? 16u : 0u;
+  invalidate_graph(h);
   return SFD_OK;
 }
 
@@ -1877,8 +1893,186 @@ bool adjoint_on_chip(sfd_handle* h) {
 
 int adj_check(const sfd_handle* h) {
   if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
+  if (h->cfg.kind == SFD_SEISMIC2) {
+    if (h->cfg.flags & (SFD_FLAG_LEGACY_QUIRKS | SFD_FLAG_CPML_2D))
+      return fail(SFD_ERR_BAD_ARG,
+                  "the seismic2 adjoint follows the corrected physics with 1-D CPML profiles "
+                  "(no SFD_FLAG_LEGACY_QUIRKS, no SFD_FLAG_CPML_2D)");
+    return SFD_OK;
+  }
   if (h->cfg.kind != SFD_ELECTROMAG2 || !h->single)
-    return fail(SFD_ERR_BAD_ARG, "the adjoint is implemented for single-pass electromag2 handles");
+    return fail(SFD_ERR_BAD_ARG, "the adjoint is implemented for single-pass electromag2 handles and seismic2 handles");
+  return SFD_OK;
+}
+
+// seismic2 adjoint workspace: two adjoint states, twelve scratch planes,
+// twelve gradient planes, the source accumulator, then seg+1 forward state
+// slots.  A state holds vx vz sxx szz sxz (full grid) and the twelve memory
+// variables (their strips), each array 256-byte aligned.
+struct S2AdjLayout {
+  size_t field, mem[12], state, lam[2], tmp, g, acc, slots, total;
+};
+
+S2AdjLayout s2_adj_layout(const sfd_handle* h, int seg) {
+  S2AdjLayout A;
+  const Layout& L = h->L;
+  A.field = align256(sizeof(float) * L.fsz);
+  size_t o = 5 * A.field;
+  for (int m = 0; m < 12; ++m) { A.mem[m] = o; o += align256(sizeof(float) * L.mem_sz[m]); }
+  A.state = o;
+  o = 0;
+  A.lam[0] = o; o += A.state;
+  A.lam[1] = o; o += A.state;
+  A.tmp = o; o += 12 * A.field;
+  A.g = o; o += 12 * A.field;
+  A.acc = o; o += 256;
+  A.slots = o; o += A.state * (size_t)(seg + 1);
+  A.total = o;
+  return A;
+}
+
+S2State s2_state_at(const S2AdjLayout& A, char* base) {
+  S2State S;
+  float** f[5] = {&S.vx, &S.vz, &S.sxx, &S.szz, &S.sxz};
+  for (int q = 0; q < 5; ++q) *f[q] = (float*)(base + q * A.field);
+  for (int m = 0; m < 12; ++m) S.m[m] = (float*)(base + A.mem[m]);
+  return S;
+}
+
+// The handle's current state -> a state slot.
+int s2_save_state(sfd_handle* h, const S2AdjLayout& A, char* dst) {
+  const size_t fb = sizeof(float) * h->L.fsz;
+  for (int q = 0; q < 5; ++q) CK(cudaMemcpyAsync(dst + q * A.field, h->f(q), fb, cudaMemcpyDeviceToDevice, h->stream));
+  for (int m = 0; m < 12; ++m)
+    CK(cudaMemcpyAsync(dst + A.mem[m], h->m(m), sizeof(float) * h->L.mem_sz[m], cudaMemcpyDeviceToDevice, h->stream));
+  return SFD_OK;
+}
+
+size_t adj_total(const sfd_handle* h, int seg) {
+  return h->cfg.kind == SFD_SEISMIC2 ? s2_adj_layout(h, seg).total : adj_layout(h, seg).total;
+}
+size_t adj_slots(const sfd_handle* h, int seg) {
+  return h->cfg.kind == SFD_SEISMIC2 ? s2_adj_layout(h, seg).slots : adj_layout(h, seg).slots;
+}
+
+// One seismic2 segment: the forward states recomputed by the handle's own
+// steps into the slots, then the adjoint steps over them, last step first.
+int s2_adjoint_segment(sfd_handle* h, int64_t nsteps) {
+  const int64_t s0 = h->step;
+  const S2AdjLayout A = s2_adj_layout(h, h->adj_seg);
+  const Layout& L = h->L;
+  char* slots = h->adj + A.slots;
+  int r = s2_save_state(h, A, slots);
+  if (r) return r;
+  for (int64_t s = 0; s < nsteps; ++s) {
+    r = sfd_run(h, 1);
+    if (r) return r;
+    r = s2_save_state(h, A, slots + A.state * (size_t)(s + 1));
+    if (r) return r;
+  }
+  const Seis2Args& e = h->s2;
+  S2Adj a;
+  a.NX = h->cfg.nx; a.NZ = h->cfg.nz; a.P = L.P; a.W = L.W;
+  const float** co[12] = {&a.A11, &a.A13, &a.A15, &a.A33, &a.A35, &a.B15, &a.B35, &a.B55, &a.dtrx, &a.dtrz, &a.gxp, &a.gzp};
+  const float* src_co[12] = {e.A11, e.A13, e.A15, e.A33, e.A35, e.B15, e.B35, e.B55, e.dtrx, e.dtrz, e.gxp, e.gzp};
+  for (int q = 0; q < 12; ++q) *co[q] = src_co[q];
+  a.X = e.X; a.Z = e.Z;
+  for (int q = 0; q < 12; ++q) a.tmp[q] = (float*)(h->adj + A.tmp + q * A.field);
+  float** g[12] = {&a.gA11, &a.gA13, &a.gA15, &a.gA33, &a.gA35, &a.gB15, &a.gB35, &a.gB55, &a.gdtrx, &a.gdtrz, &a.ggxp, &a.ggzp};
+  for (int q = 0; q < 12; ++q) *g[q] = (float*)(h->adj + A.g + q * A.field);
+  a.srcacc = (float*)(h->adj + A.acc);
+  a.srcfn = (const float*)(h->base + L.off_src);
+  a.nstep = h->cfg.nstep; a.si = h->have_force_src ? e.io.si : -1; a.sk = e.io.sk;
+  a.rec = (const int*)(h->base + L.off_rec); a.nrec = h->cfg.nrec; a.resid = h->adj_resid;
+  for (int64_t s = nsteps - 1; s >= 0; --s) {
+    const S2State S = s2_state_at(A, slots + A.state * (size_t)s);
+    const S2State S1 = s2_state_at(A, slots + A.state * (size_t)(s + 1));
+    const S2State Ln = s2_state_at(A, h->adj + A.lam[h->adj_cur]);
+    const S2State Lc = s2_state_at(A, h->adj + A.lam[1 - h->adj_cur]);
+    s2_adj_step(a, S, S1, Ln, Lc, (int)(s0 + s), h->stream);
+    h->adj_cur ^= 1;
+  }
+  CK(cudaGetLastError());
+  return SFD_OK;
+}
+
+// dJ/d(c11 c13 c15 c33 c35 c55 rho gamma_x gamma_z) from the gradient planes
+// of the update coefficients, in FP64 (the coefficients of sfd_set_model:
+// stiffness averages (c(i+1,k) + 2 c(i,k) + c(i,k-1)) dt / 4 on loop-1
+// points and (c(i,k+1) + 2 c(i,k) + c(i-1,k)) dt / 4 on loop-2 points,
+// dt over the density average of the velocity loops, 1 - gamma, and the
+// source amplitude f dt / rho).
+int s2_adjoint_gradient(sfd_handle* h, double* out, int64_t count) {
+  const int NX = h->cfg.nx, NZ = h->cfg.nz, P = h->L.P;
+  const size_t N2 = (size_t)NX * NZ;
+  if (!out || count != (int64_t)(9 * N2)) return fail(SFD_ERR_BAD_ARG, "gradient needs 9 planes of %dx%d", NX, NZ);
+  const S2AdjLayout A = s2_adj_layout(h, h->adj_seg);
+  std::vector<float> g((size_t)12 * P * NZ);
+  for (int q = 0; q < 12; ++q)
+    CK(cudaMemcpyAsync(g.data() + (size_t)q * P * NZ, h->adj + A.g + q * A.field, sizeof(float) * P * NZ,
+                       cudaMemcpyDeviceToHost, h->stream));
+  float acc = 0.f;
+  CK(cudaMemcpyAsync(&acc, h->adj + A.acc, sizeof acc, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  int r = ensure_model_planes(h);
+  if (r) return r;
+  const double* rho = h->src_scale(0);
+  const double dt = h->cfg.dt, w = dt / 4;
+  const int dm = density_method(h->cfg.flags);
+  std::fill(out, out + 9 * N2, 0.0);
+  auto G = [&](int q, int i, int k) -> double {
+    if (i < 0 || i >= NX || k < 0 || k >= NZ) return 0.0;
+    return g[(size_t)q * P * NZ + (size_t)k * P + i];
+  };
+  auto fromA = [&](int q, int i, int k) { return w * (2 * G(q, i, k) + G(q, i - 1, k) + G(q, i, k + 1)); };
+  auto fromB = [&](int q, int i, int k) { return w * (2 * G(q, i, k) + G(q, i, k - 1) + G(q, i + 1, k)); };
+  // rho_avg(method, 2, r, a, b) and its partial derivatives
+  auto parts = [&](double r0, double a0, double b0, double* d) {
+    const double m = rho_avg(dm, 2, r0, a0, b0);
+    switch (dm) {
+      case 1: d[0] = 1; d[1] = 0; d[2] = 0; break;
+      case 2: d[0] = m / (2 * r0); d[1] = m / (4 * a0); d[2] = m / (4 * b0); break;
+      case 3: d[0] = m * m / (2 * r0 * r0); d[1] = m * m / (4 * a0 * a0); d[2] = m * m / (4 * b0 * b0); break;
+      default: d[0] = 0.5; d[1] = 0.25; d[2] = 0.25;
+    }
+    return m;
+  };
+  double* grho = out + 6 * N2;
+  for (int k = 0; k < NZ; ++k)
+    for (int i = 0; i < NX; ++i) {
+      const size_t n = (size_t)i + (size_t)NX * k;
+      out[n] = fromA(0, i, k);
+      out[N2 + n] = fromA(1, i, k);
+      out[2 * N2 + n] = fromA(2, i, k) + fromB(5, i, k);
+      out[3 * N2 + n] = fromA(3, i, k);
+      out[4 * N2 + n] = fromA(4, i, k) + fromB(6, i, k);
+      out[5 * N2 + n] = fromB(7, i, k);
+      out[7 * N2 + n] = -G(10, i, k);
+      out[8 * N2 + n] = -G(11, i, k);
+      double d[3];
+      const double gx = G(8, i, k), gz = G(9, i, k);
+      if (gx != 0.0) {
+        if (i >= 1 && k >= 1) {  // dtrx = dt / rho_avg(rho(i,k), rho(i-1,k), rho(i,k-1))
+          const double m = parts(rho[n], rho[n - 1], rho[n - NX], d), u = gx * (-dt / (m * m));
+          grho[n] += u * d[0];
+          grho[n - 1] += u * d[1];
+          grho[n - NX] += u * d[2];
+        } else {
+          grho[n] += gx * (-dt / (rho[n] * rho[n]));
+        }
+      }
+      if (gz != 0.0 && i <= NX - 2 && k <= NZ - 2) {  // dtrz = dt / rho_avg(rho(i,k), rho(i+1,k), rho(i,k+1))
+        const double m = parts(rho[n], rho[n + 1], rho[n + NX], d), u = gz * (-dt / (m * m));
+        grho[n] += u * d[0];
+        grho[n + 1] += u * d[1];
+        grho[n + NX] += u * d[2];
+      }
+    }
+  const int si = h->s2.io.si, sk = h->s2.io.sk;
+  if (h->have_force_src && si >= 0) {  // vx, vz += f dt / rho at the source cell
+    const size_t n = (size_t)si + (size_t)NX * sk;
+    grho[n] += -(double)acc / rho[n];
+  }
   return SFD_OK;
 }
 
@@ -1932,7 +2126,7 @@ int32_t sfd_adjoint_bytes(const sfd_handle* h, int32_t seg_steps, size_t* bytes)
   int r = adj_check(h);
   if (r) return r;
   if (seg_steps < 1 || !bytes) return fail(SFD_ERR_BAD_ARG, "need seg_steps >= 1 and bytes");
-  *bytes = adj_layout(h, seg_steps).total;
+  *bytes = adj_total(h, seg_steps);
   return SFD_OK;
 }
 
@@ -1942,14 +2136,14 @@ int32_t sfd_adjoint_begin(sfd_handle* h, void* dev_work, size_t bytes, int32_t s
   if (r) return r;
   if (!dev_work || ((uintptr_t)dev_work & 255)) return fail(SFD_ERR_BAD_ARG, "workspace must be 256-byte aligned device memory");
   if (seg_steps < 1) return fail(SFD_ERR_BAD_ARG, "seg_steps must be >= 1");
-  const AdjLayout A = adj_layout(h, seg_steps);
-  if (bytes < A.total) return fail(SFD_ERR_BAD_ARG, "adjoint workspace has %zu bytes, needs %zu", bytes, A.total);
+  const size_t total = adj_total(h, seg_steps);
+  if (bytes < total) return fail(SFD_ERR_BAD_ARG, "adjoint workspace has %zu bytes, needs %zu", bytes, total);
   if (h->cfg.nrec > 0 && !dev_resid) return fail(SFD_ERR_BAD_ARG, "residual traces are NULL");
   h->adj = (char*)dev_work;
   h->adj_seg = seg_steps;
   h->adj_cur = 0;
   h->adj_resid = dev_resid;
-  CK(cudaMemsetAsync(h->adj, 0, A.slots, h->stream));  // adjoint states, gradients, accumulators
+  CK(cudaMemsetAsync(h->adj, 0, adj_slots(h, seg_steps), h->stream));  // adjoint states, gradients, accumulators
   CK(cudaMemsetAsync(&((Ctl*)(h->base + h->L.off_ctl))->err, 0, sizeof(int), h->stream));
   return SFD_OK;
 }
@@ -1962,6 +2156,7 @@ int32_t sfd_adjoint_segment(sfd_handle* h, int64_t nsteps) {
   if (nsteps < 1 || nsteps > h->adj_seg) return fail(SFD_ERR_BAD_ARG, "segment of %lld steps outside [1, %d]", (long long)nsteps, h->adj_seg);
   const int64_t s0 = h->step;
   if (s0 + nsteps > h->cfg.nstep) return fail(SFD_ERR_BAD_ARG, "segment runs past the source length");
+  if (h->cfg.kind == SFD_SEISMIC2) return s2_adjoint_segment(h, nsteps);
   const AdjLayout A = adj_layout(h, h->adj_seg);
   const Layout& L = h->L;
   const int NX = h->cfg.nx, NZ = h->cfg.nz;
@@ -2059,6 +2254,7 @@ int32_t sfd_adjoint_gradient(sfd_handle* h, double* out, int64_t count) {
   int r = adj_check(h);
   if (r) return r;
   if (!h->adj) return fail(SFD_ERR_STATE, "call sfd_adjoint_begin first");
+  if (h->cfg.kind == SFD_SEISMIC2) return s2_adjoint_gradient(h, out, count);
   const int NX = h->cfg.nx, NZ = h->cfg.nz, P = h->L.P;
   const size_t N2 = (size_t)NX * NZ;
   if (!out || count != (int64_t)(6 * N2)) return fail(SFD_ERR_BAD_ARG, "gradient needs 6 planes of %dx%d", NX, NZ);

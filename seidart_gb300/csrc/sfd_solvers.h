@@ -1,6 +1,7 @@
 // Host-side argument blocks and launchers of the four solvers.  One struct per
 // solver holds the device pointers of a handle; kernels take it by value.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include "sfd_common.cuh"
 
@@ -95,6 +96,13 @@ struct Seis25Args {
   float idx, idz;     // 1/dx, 1/dz for the derivatives :701-707 leaves unscaled
   int ysplit;         // y segments per column (work split of the y march)
   IoArgs io;
+  // TMA descriptors of the nine fields as one (NX, NY, NZ, 9) FP32 tensor
+  // (seis25_make_maps): velocities with a halo and the stresses of the own
+  // cells (stress kernel), stresses with a halo and the velocities of the own
+  // cells (velocity kernel)
+  CUtensorMap tm_vhalo, tm_sown, tm_shalo, tm_vown;
+  unsigned long long wait_ns;  // bound of each wait for a staged tile
+  unsigned stall_tx;           // test aid: extra bytes each stage expects (0; > 0 makes the waits run out)
 };
 
 struct Em25Args {
@@ -181,6 +189,9 @@ void seis2_half1(const Seis2Args& a, const Launch& L, int rel, cudaStream_t s);
 void seis2_half2(const Seis2Args& a, const Launch& L, int rel, cudaStream_t s);
 void seis2_finalize(const Seis2Args& a, int t_last, cudaStream_t s);
 
+// Encodes a's four tensor maps over its field array (fields contiguous,
+// `field_stride` floats apart); false when the driver refuses one.
+bool seis25_make_maps(Seis25Args& a, size_t field_stride);
 Launch seis25_launch(const Seis25Args& a);
 void seis25_half1(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s);
 void seis25_half2(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s);
