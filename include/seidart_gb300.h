@@ -346,23 +346,30 @@ int32_t sfd_checkpoint_bytes(const sfd_handle* h, size_t* bytes);
 int32_t sfd_checkpoint_save(sfd_handle* h, void* dev_dst);
 int32_t sfd_checkpoint_load(sfd_handle* h, const void* dev_src, int64_t step);
 
-/* ---- Discrete adjoint (electromag2, single-pass handles) --------------------
- * Gradient of J with respect to the six model planes, given dJ/d(trace)
+/* ---- Discrete adjoint (electromag2 single-pass handles; seismic2) ----------
+ * Gradient of J with respect to the model planes, given dJ/d(trace)
  * (device FP32 [nstep][2][nrec]; for J = 1/2 sum (d - d_obs)^2 this is the
  * residual).  Usage: after a forward run that saved checkpoints every S
  * steps, call sfd_adjoint_begin once, then for each checkpoint from the last
  * to the first: sfd_checkpoint_load(h, ckpt, step), sfd_adjoint_segment(h,
  * steps of that segment).  Each segment recomputes its forward states from
- * the checkpoint and runs the adjoint steps backwards over them; on a handle
- * whose runs are on chip (sfd_on_chip) both are one launch per segment.  The
- * workspace (sfd_adjoint_bytes) holds S+1 forward states.  On chip, a
- * neighbouring tile that does not answer within 2 s makes
- * sfd_adjoint_gradient return SFD_ERR_TIMEOUT.  No counterpart in the
- * reference (SeidarT has no adjoint). */
+ * the checkpoint and runs the adjoint steps backwards over them; on an
+ * electromag2 handle whose runs are on chip (sfd_on_chip) both are one
+ * launch per segment.  The workspace (sfd_adjoint_bytes) holds S+1 forward
+ * states.  On chip, a neighbouring tile that does not answer within the
+ * wait limit makes sfd_adjoint_gradient return SFD_ERR_TIMEOUT.
+ * seismic2: any step form; the corrected physics with 1-D CPML profiles
+ * (SFD_FLAG_LEGACY_QUIRKS and SFD_FLAG_CPML_2D are refused), any density
+ * method, attenuation and stress sources.  Set the force source after the
+ * model (its amplitude is divided by rho there) for the rho gradient to
+ * include the source term.  No counterpart in the reference (SeidarT has no
+ * adjoint). */
 int32_t sfd_adjoint_bytes(const sfd_handle* h, int32_t seg_steps, size_t* bytes);
 int32_t sfd_adjoint_begin(sfd_handle* h, void* dev_work, size_t bytes, int32_t seg_steps, const float* dev_resid);
 int32_t sfd_adjoint_segment(sfd_handle* h, int64_t nsteps);
-/* dJ/d(eps11 eps13 eps33 sig11 sig13 sig33), host FP64, 6*NX*NZ values. */
+/* Host FP64 planes: electromag2 dJ/d(eps11 eps13 eps33 sig11 sig13 sig33),
+ * 6*NX*NZ values; seismic2 dJ/d(c11 c13 c15 c33 c35 c55 rho gamma_x
+ * gamma_z), 9*NX*NZ values. */
 int32_t sfd_adjoint_gradient(sfd_handle* h, double* planes, int64_t count);
 
 /* ---- Batched runs ----------------------------------------------------------

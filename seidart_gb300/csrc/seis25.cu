@@ -35,10 +35,10 @@ constexpr int BX = 32, BZ = 4;
 // thread = 65536 / (128 x blocks)); build-time tunables, the defaults the
 // measured best on the 630 x 70 x 330 grid.
 #ifndef SEIS25_STRESS_BLOCKS
-#define SEIS25_STRESS_BLOCKS 5
+#define SEIS25_STRESS_BLOCKS 4
 #endif
 #ifndef SEIS25_VELOCITY_BLOCKS
-#define SEIS25_VELOCITY_BLOCKS 8
+#define SEIS25_VELOCITY_BLOCKS 6
 #endif
 
 // The stress kernel holds a column's 33 stiffness averages, its axis tables,
