@@ -409,6 +409,92 @@ def bench_adjoint(device, ckpt_every=200, nstep=6000, fd_cells=0):
     return out
 
 
+def bench_seismic2_adjoint(device, ckpt_every=200, fd_cells=0):
+    """Adjoint gradient of all nine seismic2 planes on the firn/ice model (400 x 200 + CPML, 2000 steps,
+    force source): misfit against the oracle's traces of the model, current model with +-4% Gaussian
+    blobs in c11, c33, c55 and rho (seed 6), checkpoints every 200 steps with recompute.  Reports the
+    wall times and, with ``fd_cells``, central differences of the FP64 oracle's misfit at seeded cells."""
+    import torch
+    import oracle
+    from oracle import parity as par
+    from seidart_gb300 import cpml as cp, synthetic as sy
+    from seidart_gb300.adjoint import SeismicTraceModel
+    case = sy.seismic2_firn_ice(nstep=2000)
+    base = case.planes
+    rng = np.random.default_rng(6)
+    nz, nx = base.shape[1:]
+    zz, xx = np.meshgrid(np.arange(nz), np.arange(nx), indexing="ij")
+    cur = base.copy()
+    for q in (0, 3, 5, 6):
+        cz, cx = rng.uniform(0.3, 0.7) * nz, rng.uniform(0.3, 0.7) * nx
+        cur[q] = base[q] * (1 + rng.choice([-1, 1]) * 0.04 * np.exp(-((zz - cz) ** 2 + (xx - cx) ** 2) / (2 * 12.0 ** 2)))
+    prof = cp.pack_profiles(case.profiles)
+
+    def traces(planes):
+        _, tr, _, blew = oracle.run(case.grid.kind, case.grid, planes, prof, case.src_ijk, case.srcfn, case.rec_ijk,
+                                    case.nstep)
+        assert not blew
+        return tr
+
+    d_obs_np = traces(base)
+    m = SeismicTraceModel(case.grid, cur, case.profiles, case.src_ijk, case.srcfn, case.rec_ijk,
+                          ckpt_every=ckpt_every, device=device)
+    d_obs = torch.as_tensor(d_obs_np, dtype=torch.float32, device=device)
+    m.forward(cur)  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tr = m.forward(cur)
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    resid = tr - d_obs
+    m.backward(resid)  # warm
+    t0 = time.perf_counter()
+    g = m.backward(resid)
+    t_bwd = time.perf_counter() - t0
+    s = m.solver
+    s.reset()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.run(case.nstep)
+    s.status()
+    t_plain = time.perf_counter() - t0
+    on_chip = s.on_chip() is not None
+    m.close()
+    out = {"workload": "seismic2 firn/ice 400x200 x 2000 steps, gradient wrt c11 c13 c15 c33 c35 c55 rho gamma_x "
+                       "gamma_z per cell",
+           "forward_form": "on chip" if on_chip else "one launch per step",
+           "forward_s": round(t_plain, 4), "forward_with_checkpoints_s": round(t_fwd, 4),
+           "adjoint_s": round(t_bwd, 4), "adjoint_over_forward": round(t_bwd / t_plain, 2),
+           "whole_gradient_over_forward": round((t_fwd + t_bwd) / t_plain, 2), "checkpoints_every": ckpt_every,
+           "misfit": 0.5 * float((resid.double() ** 2).sum())}
+    if fd_cells:
+        t0 = time.perf_counter()
+        names = ("c11", "c13", "c15", "c33", "c35", "c55", "rho", "gamma_x", "gamma_z")
+        floor = [1e-4 * float(np.abs(cur[0]).mean())] * 6 + [0.0, 1e-3, 1e-3]
+        cells = par.fd_cells(base.shape[1:], case.grid.npml, fd_cells, 7)
+        rows, ad, fd = [], [], []
+        for n, (k, i) in enumerate(cells):
+            q = n % 9
+            h = 1e-4 * max(abs(float(cur[q][k, i])), floor[q])
+            p_, m_ = cur.copy(), cur.copy()
+            p_[q][k, i] += h
+            m_[q][k, i] -= h
+            d = (par.misfit(traces(p_), d_obs_np) - par.misfit(traces(m_), d_obs_np)) / (2 * h)
+            a = float(g[q][k, i])
+            ad.append(a)
+            fd.append(d)
+            rows.append({"cell": [k, i], "param": names[q], "adjoint": a, "fd": d,
+                         "rel_err": abs(a - d) / abs(d) if d != 0 else None})
+        ad, fd = np.array(ad), np.array(fd)
+        rel = [r["rel_err"] for r in rows if r["rel_err"] is not None]
+        out["parity_fd"] = {"cells": len(cells), "seed": 7, "h_rel": 1e-4, "steps": case.nstep,
+                            "rel_l2": float(np.linalg.norm(ad - fd) / np.linalg.norm(fd)),
+                            "rel_err_max": max(rel) if rel else None,
+                            "rel_err_median": float(np.median(rel)) if rel else None,
+                            "per_cell": rows, "oracle_s": round(time.perf_counter() - t0, 1)}
+    return out
+
+
 def adjoint_fd_check(case, base, cur, grads, ncells, seed=7, h_rel=1e-4):
     """Central finite differences of the FP64 oracle's misfit at ``ncells``
     seeded interior cells (seed 7), relative step h = 1e-4 of the cell's value,
@@ -700,6 +786,8 @@ def run_ours(args):
             tiling = tuple(int(v) for v in args.batch_tiling.split("x")) if args.batch_tiling else None
             rec = bench_batched(device, flush, stream, peak, None, runs=args.steps,
                                 nstep=args.time_steps if args.time_steps != 6000 else 4000, tiling=tiling)
+        elif args.only == "seismic2_adjoint":
+            rec = bench_seismic2_adjoint(device, fd_cells=9)
         else:
             rec = bench_adjoint(device, nstep=args.time_steps)
         print(json.dumps({"only": args.only, **rec}), flush=True)
@@ -821,6 +909,7 @@ def run_ours(args):
                                                                  parity_models=picks)
     if not args.skip_adjoint:
         line.setdefault("extras", {})["adjoint"] = bench_adjoint(device, fd_cells=args.parity_fd_cells if par_on else 0)
+        line["extras"]["seismic2_adjoint"] = bench_seismic2_adjoint(device, fd_cells=9 if par_on else 0)
 
     # ---- parity: each workload's timed GPU form against the FP64 oracle ------
     if par_on:
@@ -836,6 +925,9 @@ def run_ours(args):
             par["config3_batched"] = ex["batched"]["parity"]
         if "parity_fd" in ex.get("adjoint", {}):
             par["config4_adjoint_fd"] = {k: v for k, v in ex["adjoint"]["parity_fd"].items() if k != "per_cell"}
+        if "parity_fd" in ex.get("seismic2_adjoint", {}):
+            par["seismic2_adjoint_fd"] = {k: v for k, v in ex["seismic2_adjoint"]["parity_fd"].items()
+                                          if k != "per_cell"}
         line["parity"] = par
 
     if rank == 0 and not args.skip_cpu:
@@ -862,8 +954,8 @@ def main(argv=None):
     ap.add_argument("--time-steps", type=int, default=6000,
                     help="time steps per headline shot (6000 = the workload; smaller only for profiler runs)")
     ap.add_argument("--skip-batched", action="store_true")
-    ap.add_argument("--only", choices=["seismic2", "seismic25", "batched", "adjoint", "electromag2_step",
-                                       "electromag25", "electromag2c"],
+    ap.add_argument("--only", choices=["seismic2", "seismic25", "batched", "adjoint", "seismic2_adjoint",
+                                       "electromag2_step", "electromag25", "electromag2c"],
                     help="run one secondary leg alone and print its record (for profiler runs)")
     ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--skip-parity", action="store_true",

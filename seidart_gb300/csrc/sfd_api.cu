@@ -160,6 +160,9 @@ size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 int choose_ysplit(const sfd_config& c) {
   if (!is3(c.kind)) return 1;
+#ifdef SFD_YSPLIT
+  return std::max(1, std::min(SFD_YSPLIT, c.ny));  // build-time override for tuning sweeps
+#endif
   // enough columns x segments to fill 152 SMs several times over (the
   // y-march of a segment is latency-bound: more, shorter segments keep more
   // loads in flight), segments of at least 4 cells
