@@ -9,6 +9,7 @@
 // E update has read them; half1 treats the previous H on those faces as zero
 // and the finalize kernels zero them in memory at the end of each run.
 #include "sfd_solvers.h"
+#include "tma.cuh"
 
 namespace sfd {
 
@@ -199,6 +200,296 @@ __global__ void __launch_bounds__(BX * BZ) em25_e_kernel(Em25Args a, int rel) {
   block_norm_to_slot(norm, a.io.slots, (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
 }
 
+// ---------------------------------------------------------------------------
+// The TMA-staged form (the default).  As the seismic25 kernels: each block
+// (32 x BZ columns, one y segment) streams its y planes through a ring of
+// RING shared-memory stages filled by cp.async.bulk.tensor boxes that one
+// thread issues RING - 2 planes ahead, completion on the stage's mbarrier:
+//   H kernel: the three E fields with a one-cell halo (x from i0 - 4, rows
+//             k0 - 1 .. k0 + BZ) and the three H fields of the own cells; the
+//             plane after the segment is staged too (its E only) for the y+
+//             differences;
+//   E kernel: the three H fields with the halo and the three E fields of the
+//             own cells; the y- values are carried in registers.
+// The memory variables (strips only) and the results go through plain loads
+// and stores.  Every wait is bounded (Em25Args::wait_ns): one that runs out
+// sets the control block's error word and the block leaves the kernel.
+#ifndef EM25_TMA
+#define EM25_TMA 1
+#endif
+
+constexpr int HX = 4;                // x halo of the staged tiles (16 bytes)
+constexpr int VW = BX + 2 * HX;      // 40 floats per staged row
+constexpr int VH = BZ + 2;           // rows k0 - 1 .. k0 + BZ
+constexpr int RING = 4;              // staged planes per block
+constexpr int HALO3 = 3 * VH * VW;   // three fields with the halo
+constexpr int OWN3 = 3 * BZ * BX;    // three fields of the own cells
+constexpr int OWN = 736;             // own cells after the halo, 128-byte aligned
+constexpr int STAGE = OWN + OWN3;    // 4480 bytes
+constexpr int FH = VH * VW;          // one field of a halo tile
+static_assert(OWN >= HALO3 && (OWN * 4) % 128 == 0 && (STAGE * 4) % 128 == 0, "stage alignment");
+
+__device__ void em25_wait_failed(const Em25Args& a, uint64_t* full, int n, int np) {
+  atomicExch(const_cast<int*>(&a.io.ctl->err), 1);
+  const int issued = min(np, n + RING);
+  for (int m = n; m < issued; ++m) tma::bar_wait(full + m % RING, (m / RING) & 1, a.wait_ns);
+}
+
+__global__ void __launch_bounds__(BX * BZ) em25_h_tma_kernel(const __grid_constant__ Em25Args a, int rel) {
+  extern __shared__ __align__(128) float stage[];
+  __shared__ __align__(8) uint64_t full[RING];
+  const Ctl* ctl = a.io.ctl;
+  const int t = ctl->base + rel;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && t > ctl->run_start) {
+    const float* ch[3] = {a.Ex, a.Ey, a.Ez};
+    gather_receivers<3>(a.io.rec, a.io.nrec, a.io.traces, t - 1, ch, a.P, a.NY, true);
+  }
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
+  const int i0 = blockIdx.x * BX, k0 = blockIdx.y * BZ;
+  const int NX = a.NX, NY = a.NY, NZ = a.NZ, P = a.P, W = a.W;
+  const int seg = (NY + a.ysplit - 1) / a.ysplit;
+  const int j0 = blockIdx.z * seg, j1 = min(NY - 1, j0 + seg);  // every H loop runs over j <= NY-2
+  if (j0 >= j1) return;  // the whole block
+  const int np = j1 - j0 + 1;  // the segment's planes and the next one (its E only)
+  if (tid == 0) {
+    for (int q = 0; q < RING; ++q) tma::bar_init(full + q, 1);
+    tma::fence_bar_init();
+  }
+  __syncthreads();
+  auto issue = [&](int n) {
+    float* st = stage + (n % RING) * STAGE;
+    uint64_t* bar = full + n % RING;
+    const int j = j0 + n;
+    const bool own = j < j1;
+    tma::bar_arrive_expect(bar, (own ? (HALO3 + OWN3) * 4u : HALO3 * 4u) + a.stall_tx);
+    tma::load_4d(st, &a.tm_halo, bar, i0 - HX, j, k0 - 1, 0);       // Ex Ey Ez
+    if (own) tma::load_4d(st + OWN, &a.tm_own, bar, i0, j, k0, 3);  // Hx Hy Hz
+  };
+  if (tid == 0)
+    for (int n = 0; n < min(RING, np); ++n) issue(n);
+
+  const int i = i0 + tx, k = k0 + ty;
+  const bool active = i <= NX - 2 && k <= NZ - 2;
+  const int ic = active ? i : 0, kc = active ? k : 0;
+  const bool xs = active && in_strip(i, NX, W), zs = active && in_strip(k, NZ, W);
+  const int xsi = xs ? strip_idx(i, NX, W) : 0;
+  const int zsi = zs ? strip_idx(k, NZ, W) : 0;
+  const float ikx = a.X.ik[ic], adx = a.X.ad[ic], bx = a.X.b[ic];
+  const float ikz = a.Z.ik[kc], adz = a.Z.ad[kc], bz = a.Z.b[kc];
+  const float ikzh = a.Z.ikh[kc], adzh = a.Z.adh[kc], bzh = a.Z.bh[kc];
+  const float dbH = a.dbH;
+  const bool hz_rows = (k >= 1);
+  const bool fx_x = (i == 0) || (k == 0) || (k == NZ - 2);
+  const bool fy_x = (i == 0) || (i == NX - 2) || (k == 0) || (k == NZ - 2);
+  const bool fz_x = (i == 0) || (i == NX - 2) || (k == 0);
+  float* __restrict__ Hx_ = a.Hx;
+  float* __restrict__ Hy_ = a.Hy;
+  float* __restrict__ Hz_ = a.Hz;
+  float* __restrict__ mEz_y_ = a.mEz_y;
+  float* __restrict__ mEy_z_ = a.mEy_z;
+  float* __restrict__ mEx_z_ = a.mEx_z;
+  float* __restrict__ mEz_x_ = a.mEz_x;
+  float* __restrict__ mEx_y_ = a.mEx_y;
+  float* __restrict__ mEy_x_ = a.mEy_x;
+  const int hc = (ty + 1) * VW + tx + HX;  // own cell in a halo tile
+  const int oc = ty * BX + tx;             // own cell in an own-cells tile
+  size_t c = ((size_t)kc * NY + j0) * P + ic;
+  for (int n = 0; n < j1 - j0; ++n, c += P) {
+    const int j = j0 + n;
+    bool ok = tma::bar_wait(full + n % RING, (n / RING) & 1, a.wait_ns);
+    if (ok) ok = tma::bar_wait(full + (n + 1) % RING, ((n + 1) / RING) & 1, a.wait_ns);
+    if (ok && active) {
+      const float* E = stage + (n % RING) * STAGE;         // Ex Ey Ez of plane j, with the halo
+      const float* En = stage + ((n + 1) % RING) * STAGE;  // plane j + 1
+      const float* H = E + OWN;                            // Hx Hy Hz of the own cells
+      const bool ys = in_strip(j, NY, W);
+      const size_t mx = ((size_t)k * NY + j) * (2 * W) + xsi;
+      const size_t my = ((size_t)k * (2 * W) + (ys ? strip_idx(j, NY, W) : 0)) * P + i;
+      const size_t mz = ((size_t)zsi * NY + j) * P + i;
+      const float iky = a.Y.ik[j], ady = a.Y.ad[j], by = a.Y.b[j];
+      const float ikyh = a.Y.ikh[j], adyh = a.Y.adh[j], byh = a.Y.bh[j];
+      const float ex = E[hc], ey = E[FH + hc], ez = E[2 * FH + hc];
+      {  // Hx, :904-917
+        const float d1 = ez - En[2 * FH + hc];  // dEz/dy
+        float v1 = d1 * ikyh;
+        if (ys) { const float m = byh * mEz_y_[my] + adyh * d1; mEz_y_[my] = m; v1 += m; }
+        const float d2 = E[FH + hc + VW] - ey;  // dEy/dz
+        float v2 = d2 * ikzh;
+        if (zs) { const float m = bzh * mEy_z_[mz] + adzh * d2; mEy_z_[mz] = m; v2 += m; }
+        const float h = (fx_x || j == 0 || j == NY - 2) ? 0.f : H[oc];
+        Hx_[c] = h + dbH * (v2 + v1);
+      }
+      {  // Hy, :925-938
+        const float d1 = ex - E[hc + VW];  // dEx/dz
+        float v1 = d1 * ikz;
+        if (zs) { const float m = bz * mEx_z_[mz] + adz * d1; mEx_z_[mz] = m; v1 += m; }
+        const float d2 = E[2 * FH + hc + 1] - ez;  // dEz/dx
+        float v2 = d2 * ikx;
+        if (xs) { const float m = bx * mEz_x_[mx] + adx * d2; mEz_x_[mx] = m; v2 += m; }
+        const float h = (fy_x || j == 0) ? 0.f : H[OWN3 / 3 + oc];  // Hy face j=NY-1 is outside the loop
+        Hy_[c] = h + dbH * (v2 + v1);
+      }
+      if (hz_rows) {  // Hz, :946-960 (k >= 1)
+        const float d1 = En[hc] - ex;  // dEx/dy
+        float v1 = d1 * iky;
+        if (ys) { const float m = by * mEx_y_[my] + ady * d1; mEx_y_[my] = m; v1 += m; }
+        const float d2 = ey - E[FH + hc + 1];  // dEy/dx
+        float v2 = d2 * ikx;
+        if (xs) { const float m = bx * mEy_x_[mx] + adx * d2; mEy_x_[mx] = m; v2 += m; }
+        const float h = (fz_x || j == 0 || j == NY - 2) ? 0.f : H[2 * (OWN3 / 3) + oc];
+        Hz_[c] = h + dbH * (v2 + v1);
+      }
+    }
+    if (!__syncthreads_and(ok)) {  // every thread is done with plane n (or a wait ran out)
+      if (tid == 0) em25_wait_failed(a, full, n, np);
+      break;
+    }
+    if (tid == 0 && n + RING < np) {
+      tma::fence_async_smem();
+      issue(n + RING);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(BX * BZ) em25_e_tma_kernel(const __grid_constant__ Em25Args a, int rel) {
+  extern __shared__ __align__(128) float stage[];
+  __shared__ __align__(8) uint64_t full[RING];
+  const int t = a.io.ctl->base + rel;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
+  const int i0 = blockIdx.x * BX, k0 = blockIdx.y * BZ;
+  const int NX = a.NX, NY = a.NY, NZ = a.NZ, P = a.P, W = a.W;
+  const int seg = (NY + a.ysplit - 1) / a.ysplit;
+  const int j0 = blockIdx.z * seg, j1 = min(NY, j0 + seg);
+  const int slot = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+  float norm = 0.0f;
+  if (j0 >= j1) {  // the whole block
+    block_norm_to_slot(norm, a.io.slots, slot);
+    return;
+  }
+  const int np = j1 - j0;
+  if (tid == 0) {
+    for (int q = 0; q < RING; ++q) tma::bar_init(full + q, 1);
+    tma::fence_bar_init();
+  }
+  __syncthreads();
+  auto issue = [&](int n) {
+    float* st = stage + (n % RING) * STAGE;
+    uint64_t* bar = full + n % RING;
+    const int j = j0 + n;
+    tma::bar_arrive_expect(bar, (HALO3 + OWN3) * 4u + a.stall_tx);
+    tma::load_4d(st, &a.tm_halo, bar, i0 - HX, j, k0 - 1, 3);  // Hx Hy Hz
+    tma::load_4d(st + OWN, &a.tm_own, bar, i0, j, k0, 0);     // Ex Ey Ez
+  };
+  if (tid == 0)
+    for (int n = 0; n < min(RING, np); ++n) issue(n);
+
+  const int i = i0 + tx, k = k0 + ty;
+  const bool inside = i < NX && k < NZ;
+  const int ic = inside ? i : 0, kc = inside ? k : 0;
+  const bool XEx = inside && (k >= 1) && (k <= NZ - 2) && (i <= NX - 2);
+  const bool XEy = inside && (k >= 1) && (k <= NZ - 2) && (i >= 1) && (i <= NX - 2);
+  const bool XEz = inside && (k <= NZ - 2) && (i >= 1) && (i <= NX - 2);
+  const size_t pc = (size_t)kc * P + ic;
+  float caX = 0, cbX = 0, caY = 0, cbY = 0, caZ = 0, cbZ = 0;
+  if (XEx) { caX = a.caEx[pc]; cbX = a.cbEx[pc]; }
+  if (XEy) {  // (4 c(i,k) + c(i-1,k) + c(i,k-1)) / 6, :1004-1006
+    caY = (4.f * a.caEy[pc] + a.caEy[pc - 1] + a.caEy[pc - P]) / 6.f;
+    cbY = (4.f * a.cbEy[pc] + a.cbEy[pc - 1] + a.cbEy[pc - P]) / 6.f;
+  }
+  if (XEz) {  // (4 c(i,k) + c(i-1,k) + c(i,k+1)) / 6, :1026-1028
+    caZ = (4.f * a.caEz[pc] + a.caEz[pc - 1] + a.caEz[pc + P]) / 6.f;
+    cbZ = (4.f * a.cbEz[pc] + a.cbEz[pc - 1] + a.cbEz[pc + P]) / 6.f;
+  }
+  const bool xs = inside && in_strip(i, NX, W), zs = inside && in_strip(k, NZ, W);
+  const int xsi = xs ? strip_idx(i, NX, W) : 0;
+  const int zsi = zs ? strip_idx(k, NZ, W) : 0;
+  const float ikxh = a.X.ikh[ic], adxh = a.X.adh[ic], bxh = a.X.bh[ic];
+  const float ikz = a.Z.ik[kc], adz = a.Z.ad[kc], bz = a.Z.b[kc];
+  const float ikzh = a.Z.ikh[kc], adzh = a.Z.adh[kc], bzh = a.Z.bh[kc];
+  const bool fEx = (i == 0) || (i == NX - 2) || (k == 0) || (k == NZ - 1);
+  const bool fEy = (i == 0) || (i == NX - 1) || (k == 0) || (k == NZ - 1);
+  const bool fEz = (i == 0) || (i == NX - 1) || (k == 0) || (k == NZ - 2);
+  float* __restrict__ Ex_ = a.Ex;
+  float* __restrict__ Ey_ = a.Ey;
+  float* __restrict__ Ez_ = a.Ez;
+  float* __restrict__ mHz_y_ = a.mHz_y;
+  float* __restrict__ mHy_z_ = a.mHy_z;
+  float* __restrict__ mHz_x_ = a.mHz_x;
+  float* __restrict__ mHx_z_ = a.mHx_z;
+  float* __restrict__ mHx_y_ = a.mHx_y;
+  float* __restrict__ mHy_x_ = a.mHy_x;
+  const int hc = (ty + 1) * VW + tx + HX;
+  const int oc = ty * BX + tx;
+  size_t c = ((size_t)kc * NY + j0) * P + ic;
+  float phx = 0.f, phz = 0.f;  // Hx, Hz of the plane before
+  if (inside && j0 >= 1) { phx = __ldg(a.Hx + c - P); phz = __ldg(a.Hz + c - P); }
+  for (int n = 0; n < np; ++n, c += P) {
+    const int j = j0 + n;
+    const bool ok = tma::bar_wait(full + n % RING, (n / RING) & 1, a.wait_ns);
+    if (ok && inside) {
+      const float* H = stage + (n % RING) * STAGE;  // Hx Hy Hz of plane j, with the halo
+      const float* E = H + OWN;                     // Ex Ey Ez of the own cells
+      const bool ys = in_strip(j, NY, W);
+      const size_t mx = ((size_t)k * NY + j) * (2 * W) + xsi;
+      const size_t my = ((size_t)k * (2 * W) + (ys ? strip_idx(j, NY, W) : 0)) * P + i;
+      const size_t mz = ((size_t)zsi * NY + j) * P + i;
+      const float ikyh = a.Y.ikh[j], adyh = a.Y.adh[j], byh = a.Y.bh[j];
+      const float hx = H[hc], hy = H[FH + hc], hz = H[2 * FH + hc];
+      float ex = E[oc], ey = E[OWN3 / 3 + oc], ez = E[2 * (OWN3 / 3) + oc];
+      if (XEx && j >= 1 && j <= NY - 2) {  // :971-984
+        const float d1 = hz - phz;  // dHz/dy
+        float v1 = d1 * ikyh;
+        if (ys) { const float m = byh * mHz_y_[my] + adyh * d1; mHz_y_[my] = m; v1 += m; }
+        const float d2 = H[FH + hc - VW] - hy;  // dHy/dz
+        float v2 = d2 * ikz;
+        if (zs) { const float m = bz * mHy_z_[mz] + adz * d2; mHy_z_[mz] = m; v2 += m; }
+        ex = caX * ex + cbX * (v1 + v2);
+      }
+      if (XEy && j <= NY - 2) {  // :988-1007
+        const float d1 = H[2 * FH + hc - 1] - hz;  // dHz/dx
+        float v1 = d1 * ikxh;
+        if (xs) { const float m = bxh * mHz_x_[mx] + adxh * d1; mHz_x_[mx] = m; v1 += m; }
+        const float d2 = hx - H[hc - VW];  // dHx/dz
+        float v2 = d2 * ikzh;
+        if (zs) { const float m = bzh * mHx_z_[mz] + adzh * d2; mHx_z_[mz] = m; v2 += m; }
+        ey = caY * ey + cbY * (v1 + v2);
+      }
+      if (XEz && j >= 1 && j <= NY - 2) {  // :1015-1029
+        const float d1 = phx - hx;  // dHx/dy
+        float v1 = d1 * ikyh;
+        if (ys) { const float m = byh * mHx_y_[my] + adyh * d1; mHx_y_[my] = m; v1 += m; }
+        const float d2 = hy - H[FH + hc - 1];  // dHy/dx
+        float v2 = d2 * ikxh;
+        if (xs) { const float m = bxh * mHy_x_[mx] + adxh * d2; mHy_x_[mx] = m; v2 += m; }
+        ez = caZ * ez + cbZ * (v1 + v2);
+      }
+      if (i == a.io.si && j == a.io.sj && k == a.io.sk) {  // :1033-1035
+        ex += a.io.src[t];
+        ey += a.io.src[a.io.nstep + t];
+        ez += a.io.src[2 * a.io.nstep + t];
+      }
+      if (fEx || j == 0 || j == NY - 1) ex = 0.f;  // :1038-1043
+      if (fEy || j == 0 || j == NY - 2) ey = 0.f;  // :1045-1050
+      if (fEz || j == 0 || j == NY - 1) ez = 0.f;  // :1052-1057
+      Ex_[c] = ex;
+      Ey_[c] = ey;
+      Ez_[c] = ez;
+      norm = fmaxf(norm, norm_monitor(ex, ey, ez));
+      phx = hx;
+      phz = hz;
+    }
+    if (!__syncthreads_and(ok)) {
+      if (tid == 0) em25_wait_failed(a, full, n, np);
+      break;
+    }
+    if (tid == 0 && n + RING < np) {
+      tma::fence_async_smem();
+      issue(n + RING);
+    }
+  }
+  block_norm_to_slot(norm, a.io.slots, slot);
+}
+
 // Zero the H Dirichlet faces (:1059-1078) in memory.
 __global__ void em25_hfaces_kernel(Em25Args a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -232,11 +523,22 @@ Launch em25_launch(const Em25Args& a) {
 }
 
 void em25_half1(const Em25Args& a, const Launch& L, int rel, cudaStream_t s) {
-  em25_h_kernel<<<L.grid, L.block, 0, s>>>(a, rel);
+  if (EM25_TMA)
+    em25_h_tma_kernel<<<L.grid, L.block, RING * STAGE * sizeof(float), s>>>(a, rel);
+  else
+    em25_h_kernel<<<L.grid, L.block, 0, s>>>(a, rel);
 }
 
 void em25_half2(const Em25Args& a, const Launch& L, int rel, cudaStream_t s) {
-  em25_e_kernel<<<L.grid, L.block, 0, s>>>(a, rel);
+  if (EM25_TMA)
+    em25_e_tma_kernel<<<L.grid, L.block, RING * STAGE * sizeof(float), s>>>(a, rel);
+  else
+    em25_e_kernel<<<L.grid, L.block, 0, s>>>(a, rel);
+}
+
+bool em25_make_maps(Em25Args& a, size_t field_stride) {
+  return encode_field_map(&a.tm_halo, a.Ex, a.NX, a.NY, a.NZ, a.P, field_stride, 6, VW, VH, 3) &&
+         encode_field_map(&a.tm_own, a.Ex, a.NX, a.NY, a.NZ, a.P, field_stride, 6, BX, BZ, 3);
 }
 
 void em25_finalize(const Em25Args& a, int t_last, cudaStream_t s) {

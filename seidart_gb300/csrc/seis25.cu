@@ -22,9 +22,6 @@
 #include "sfd_solvers.h"
 #include "tma.cuh"
 
-#include <mutex>
-#include <cudaTypedefs.h>
-
 namespace sfd {
 
 namespace {
@@ -786,25 +783,8 @@ void seis25_half2(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s)
 }
 
 bool seis25_make_maps(Seis25Args& a, size_t field_stride) {
-  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", (void**)&encode, 12000, cudaEnableDefault, &q) !=
-            cudaSuccess ||
-        q != cudaDriverEntryPointSuccess)
-      encode = nullptr;
-  });
-  if (!encode) return false;
-  // (x, y, z, field): x extent NX, so the halo past the last column reads zeros
-  const cuuint64_t dims[4] = {(cuuint64_t)a.NX, (cuuint64_t)a.NY, (cuuint64_t)a.NZ, 9};
-  const cuuint64_t strides[3] = {(cuuint64_t)a.P * 4, (cuuint64_t)a.NY * a.P * 4, (cuuint64_t)field_stride * 4};
-  const cuuint32_t ones[4] = {1, 1, 1, 1};
   auto make = [&](CUtensorMap* m, int bx, int bz, int nf) {
-    const cuuint32_t box[4] = {(cuuint32_t)bx, 1, (cuuint32_t)bz, (cuuint32_t)nf};
-    return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a.vx, dims, strides, box, ones, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    return encode_field_map(m, a.vx, a.NX, a.NY, a.NZ, a.P, field_stride, 9, bx, bz, nf);
   };
   return make(&a.tm_vhalo, VW, VH, 3) && make(&a.tm_sown, BX, BZ, 6) && make(&a.tm_shalo, VW, VH, 6) &&
          make(&a.tm_vown, BX, BZ, 3);

@@ -163,12 +163,14 @@ int choose_ysplit(const sfd_config& c) {
 #ifdef SFD_YSPLIT
   return std::max(1, std::min(SFD_YSPLIT, c.ny));  // build-time override for tuning sweeps
 #endif
-  // enough columns x segments to fill 152 SMs several times over (the
-  // y-march of a segment is latency-bound: more, shorter segments keep more
-  // loads in flight), segments of at least 4 cells
+  // enough columns x segments to fill 152 SMs a few times over, segments of
+  // at least 4 cells: each segment pays its staging ring's fill once, so the
+  // TMA-staged march favours longer segments than the plain one did (on the
+  // 630 x 70 x 330 seismic25 grid 4 segments of 18 planes ran at 26.2
+  // Gcell-updates/s, 8 of 9 planes at 24.8, 2 at 25.3, 1 at 23.7)
   const long cols = (long)c.nx * c.nz;
   int s = 1;
-  while (cols * s < 152L * 1024 * 8 && s * 4 <= c.ny) s *= 2;
+  while (cols * s < 152L * 1024 * 4 && s * 4 <= c.ny) s *= 2;
   return s;
 }
 
@@ -506,6 +508,9 @@ bool bind_args(sfd_handle* h) {
       a.dbH = (float)(c.dt / kMu0);
       a.ysplit = L.ysplit;
       a.io = io;
+      a.wait_ns = h->wait_ns;
+      a.stall_tx = h->stall_waits ? 16u : 0u;
+      if (!em25_make_maps(a, L.fsz)) return false;
       h->launch = em25_launch(a);
       break;
     }
@@ -852,7 +857,7 @@ int32_t create_handle(const sfd_config* cfg, void* dev_state, size_t state_bytes
   if (!bind_args(h)) {
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
     delete h;
-    return fail(SFD_ERR_CUDA, "cuTensorMapEncodeTiled refused the seismic25 field tiles");
+    return fail(SFD_ERR_CUDA, "cuTensorMapEncodeTiled refused the 2.5-D field tiles");
   }
   e = cudaMemsetAsync(h->base, 0, L.total, h->stream);
   if (e != cudaSuccess) { cudaStreamDestroy(h->cap_stream); delete h; return cuda_fail(e, "cudaMemsetAsync"); }
@@ -1554,7 +1559,8 @@ int32_t sfd_status(sfd_handle* h, int64_t* step, double* maxnorm) {
   if (maxnorm) *maxnorm = (double)ctl.maxnorm;
   if (ctl.err)
     return fail(SFD_ERR_TIMEOUT,
-                h->cfg.kind == SFD_SEISMIC25 ? "seismic25 step: a staged tile did not arrive within %.3g s"
+                (h->cfg.kind == SFD_SEISMIC25 || h->cfg.kind == SFD_ELECTROMAG25)
+                    ? "2.5-D step: a staged tile did not arrive within %.3g s"
                                              : "on-chip run: a neighbouring tile did not answer within %.3g s",
                 (double)h->wait_ns * 1e-9);
   if (!(ctl.maxnorm <= 1.0e25f))
@@ -1568,6 +1574,7 @@ int32_t sfd_set_wait_limit(sfd_handle* h, int64_t ns) {
   if (ns < 0) return fail(SFD_ERR_BAD_ARG, "wait limit must be >= 0 ns (0 = the default 2 s)");
   h->wait_ns = ns == 0 ? kDefaultWaitNs : (unsigned long long)ns;
   h->s25.wait_ns = h->wait_ns;
+  h->em25.wait_ns = h->wait_ns;
   invalidate_graph(h);
   return SFD_OK;
 }
@@ -1577,6 +1584,7 @@ int32_t sfd_test_stall_waits(sfd_handle* h, int32_t on) {
   if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
   h->stall_waits = on != 0;
   h->s25.stall_tx = h->stall_waits ? 16u : 0u;
+  h->em25.stall_tx = h->stall_waits ? 16u : 0u;
   invalidate_graph(h);
   return SFD_OK;
 }
@@ -1967,11 +1975,40 @@ int s2_adjoint_segment(sfd_handle* h, int64_t nsteps) {
   char* slots = h->adj + A.slots;
   int r = s2_save_state(h, A, slots);
   if (r) return r;
-  for (int64_t s = 0; s < nsteps; ++s) {
-    r = sfd_run(h, 1);
-    if (r) return r;
-    r = s2_save_state(h, A, slots + A.state * (size_t)(s + 1));
-    if (r) return r;
+  // forward recompute, slot s -> slot s + 1, no receivers; the kernels read
+  // the step index from the control block (base = s0)
+  k_begin<<<std::min(1024, (L.nslots + 255) / 256 + 1), 256, 0, h->stream>>>((Ctl*)(h->base + L.off_ctl),
+                                                                            (float*)(h->base + L.off_slots), L.nslots, (int)s0);
+  if (h->single) {  // the single-pass step kernel between slots; its in-place memory variables copied ahead
+    Seis2Step st = h->s2s[0];
+    st.io.nrec = 0;
+    for (int64_t s = 0; s < nsteps; ++s) {
+      const S2State a0 = s2_state_at(A, slots + A.state * (size_t)s);
+      const S2State a1 = s2_state_at(A, slots + A.state * (size_t)(s + 1));
+      st.vx0 = a0.vx; st.vz0 = a0.vz; st.sxx0 = a0.sxx; st.szz0 = a0.szz; st.sxz0 = a0.sxz;
+      st.vx1 = a1.vx; st.vz1 = a1.vz; st.sxx1 = a1.sxx; st.szz1 = a1.szz; st.sxz1 = a1.sxz;
+      st.m_vxx0 = a0.m[0]; st.m_vzz0 = a0.m[1]; st.m_vxz0 = a0.m[2]; st.m_vzx0 = a0.m[3];
+      st.m_vxx1 = a1.m[0]; st.m_vzz1 = a1.m[1]; st.m_vxz1 = a1.m[2]; st.m_vzx1 = a1.m[3];
+      st.m2_vxx0 = a0.m[8]; st.m2_vzz0 = a0.m[9]; st.m2_vxz0 = a0.m[10]; st.m2_vzx0 = a0.m[11];
+      st.m2_vxx1 = a1.m[8]; st.m2_vzz1 = a1.m[9]; st.m2_vxz1 = a1.m[10]; st.m2_vzx1 = a1.m[11];
+      CK(cudaMemcpyAsync(a1.m[4], a0.m[4], A.mem[8] - A.mem[4], cudaMemcpyDeviceToDevice, h->stream));
+      st.m_sxx_x = a1.m[4]; st.m_szz_z = a1.m[5]; st.m_sxz_x = a1.m[6]; st.m_sxz_z = a1.m[7];
+      seis2_step(st, h->launch1, h->zb, (int)s, h->stream);
+    }
+  } else {  // the two half-step kernels in place on a copy of the previous slot
+    Seis2Args ar = h->s2;
+    ar.io.nrec = 0;
+    for (int64_t s = 0; s < nsteps; ++s) {
+      char* dst = slots + A.state * (size_t)(s + 1);
+      CK(cudaMemcpyAsync(dst, slots + A.state * (size_t)s, A.state, cudaMemcpyDeviceToDevice, h->stream));
+      const S2State a1 = s2_state_at(A, dst);
+      ar.vx = a1.vx; ar.vz = a1.vz; ar.sxx = a1.sxx; ar.szz = a1.szz; ar.sxz = a1.sxz;
+      ar.m_vxx = a1.m[0]; ar.m_vzz = a1.m[1]; ar.m_vxz = a1.m[2]; ar.m_vzx = a1.m[3];
+      ar.m_sxx_x = a1.m[4]; ar.m_szz_z = a1.m[5]; ar.m_sxz_x = a1.m[6]; ar.m_sxz_z = a1.m[7];
+      ar.m2_vxx = a1.m[8]; ar.m2_vzz = a1.m[9]; ar.m2_vxz = a1.m[10]; ar.m2_vzx = a1.m[11];
+      seis2_half1(ar, h->launch, (int)s, h->stream);
+      seis2_half2(ar, h->launch, (int)s, h->stream);
+    }
   }
   const Seis2Args& e = h->s2;
   S2Adj a;

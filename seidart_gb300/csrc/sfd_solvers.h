@@ -115,6 +115,11 @@ struct Em25Args {
   float dbH;
   int ysplit;
   IoArgs io;
+  // TMA descriptors of the six fields as one (NX, NY, NZ, 6) FP32 tensor
+  // (em25_make_maps): three fields with a halo, three of the own cells
+  CUtensorMap tm_halo, tm_own;
+  unsigned long long wait_ns;  // bound of each wait for a staged tile
+  unsigned stall_tx;           // test aid: extra bytes each stage expects (0; > 0 makes the waits run out)
 };
 
 // Single-pass (fused) 2-D steps.  Each launch reads the "old" copy of every
@@ -197,6 +202,12 @@ void seis25_half1(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s)
 void seis25_half2(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s);
 void seis25_finalize(const Seis25Args& a, int t_last, cudaStream_t s);
 
+// A 4-D (x, y, z, field) FP32 tensor map over `nfields` fields of (NX, NY,
+// NZ) cells at `base` (row pitch P floats, fields `field_stride` floats
+// apart) with boxes of box_x x 1 x box_z x box_f (tma_maps.cu).
+bool encode_field_map(CUtensorMap* map, void* base, int NX, int NY, int NZ, int P, size_t field_stride, int nfields,
+                      int box_x, int box_z, int box_f);
+bool em25_make_maps(Em25Args& a, size_t field_stride);
 Launch em25_launch(const Em25Args& a);
 void em25_half1(const Em25Args& a, const Launch& L, int rel, cudaStream_t s);
 void em25_half2(const Em25Args& a, const Launch& L, int rel, cudaStream_t s);

@@ -1,7 +1,7 @@
 """Bounded device waits on the GPU.
 
 The on-chip runs poll neighbouring tiles' edge values, the batched kernel
-meets at a grid barrier every step, and the seismic25 kernels wait for their
+meets at a grid barrier every step, and the 2.5-D kernels wait for their
 TMA-staged planes.  Each wait gives up after a limit
 (sfd_set_wait_limit / sfd_batch_set_wait_limit, 2 s by default), records the
 failure, and every tile or block leaves the kernel; the host reads
@@ -14,7 +14,7 @@ No kernel faults or hangs here: every wait is bounded by the limit.
 import pytest
 
 from helpers import make_solver, rel_l2, run_oracle
-from seidart_gb300 import ELECTROMAG2, SEISMIC2, SEISMIC25, _lib
+from seidart_gb300 import ELECTROMAG2, ELECTROMAG25, SEISMIC2, SEISMIC25, _lib
 from seidart_gb300 import synthetic as sy
 from seidart_gb300._lib import SFD_ERR_TIMEOUT, SfdError
 from seidart_gb300.batch import Batch
@@ -81,11 +81,12 @@ def test_batch_grid_barrier_times_out(gpu):
             s.close()
 
 
-def test_seismic25_staged_tiles_time_out(gpu):
-    """The seismic25 kernels wait on mbarriers for their TMA-staged planes;
-    with the test aid each stage expects 16 bytes that never arrive."""
+@pytest.mark.parametrize("kind", [SEISMIC25, ELECTROMAG25], ids=["seismic25", "electromag25"])
+def test_2p5d_staged_tiles_time_out(gpu, kind):
+    """The 2.5-D kernels wait on mbarriers for their TMA-staged planes; with
+    the test aid each stage expects 16 bytes that never arrive."""
     L = _lib.lib()
-    case = sy.small_case(SEISMIC25, seed=5, nx=70, nz=36, ny=30, npml=5, nstep=40)
+    case = sy.small_case(kind, seed=5, nx=70, nz=36, ny=30, npml=5, nstep=40)
     with make_solver(case) as s:
         s.set_wait_limit(LIMIT_NS)
         assert L.sfd_test_stall_waits(s._h, 1) == 0
