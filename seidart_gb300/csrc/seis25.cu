@@ -19,349 +19,11 @@
 //   half2: vx, vy (:821-870) and vz (:872-896) with the stress-gradient
 //          memory variables, optional attenuation v <- v (1 - gamma), the
 //          source (:898-900), the six Dirichlet faces (:903-925) and the norm.
-#include "sfd_solvers.h"
-#include "tma.cuh"
-
-namespace sfd {
-
-namespace {
-
-constexpr int BX = 32, BZ = 4;
-
-// Resident blocks per SM the two kernels are compiled for (registers per
-// thread = 65536 / (128 x blocks)); build-time tunables, the defaults the
-// measured best on the 630 x 70 x 330 grid.
-#ifndef SEIS25_STRESS_BLOCKS
-#define SEIS25_STRESS_BLOCKS 4
-#endif
-#ifndef SEIS25_VELOCITY_BLOCKS
-#define SEIS25_VELOCITY_BLOCKS 6
-#endif
-
-// The stress kernel holds a column's 33 stiffness averages, its axis tables,
-// the carried velocities and nine memory variables: at 4 blocks of 128
-// threads per SM (128 registers) nothing spills, and that beat 8 blocks at
-// 64 registers, whose spills missed L1 (0.345 against 0.412 ms per step on
-// the 630 x 70 x 330 grid).  The velocity kernel needs fewer registers and
-// runs best at 8 blocks, where more resident warps hide the y-march's HBM
-// latency.
-__global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS) seis25_stress_kernel(Seis25Args a, int rel) {
-  const Ctl* ctl = a.io.ctl;
-  const int t = ctl->base + rel;
-  if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && t > ctl->run_start) {
-    const float* ch[3] = {a.vx, a.vy, a.vz};
-    gather_receivers<3>(a.io.rec, a.io.nrec, a.io.traces, t - 1, ch, a.P, a.NY, true);
-  }
-  const int i = blockIdx.x * BX + threadIdx.x;
-  const int k = blockIdx.y * BZ + threadIdx.y;
-  const int NX = a.NX, NY = a.NY, NZ = a.NZ, P = a.P, W = a.W;
-  if (i >= NX || k >= NZ) return;
-  const int seg = (NY + a.ysplit - 1) / a.ysplit;
-  const int j0 = blockIdx.z * seg, j1 = min(NY, j0 + seg);
-  if (j0 >= j1) return;
-
-  const bool L1 = (k >= 1) && (i <= NX - 2);
-  const bool L2 = (k >= 1) && (i >= 1);
-  const bool L3 = (k <= NZ - 2) && (i >= 1);
-  const bool L4 = (k <= NZ - 2) && (i <= NX - 2);
-  if (!(L1 || L2 || L3 || L4)) return;
-
-  // The 33 stiffness averages of the four loops at this column, formed once
-  // on the host in FP64 (planes 0-14 loop 1, 15-20 loop 2, 21-26 loop 3,
-  // 27-32 loop 4; zero where the loop does not update the cell).  Each thread
-  // keeps its column's values in its own shared-memory slots and reads them at
-  // every y step: held in registers they capped the kernel at 4 blocks of 128
-  // threads per SM, too few loads in flight to cover the y-march's latency.
-  __shared__ float sC[33 * BX * BZ];
-  const int tid = threadIdx.y * BX + threadIdx.x;
-  {
-    const size_t cpl = (size_t)NZ * P, cpc = (size_t)k * P + i;
-    auto cf = [&](int q, bool on) { return on ? __ldg(a.C + q * cpl + cpc) : 0.0f; };
-#pragma unroll
-    for (int q = 0; q < 15; ++q) sC[q * BX * BZ + tid] = cf(q, L1);   // over (i+1,k) (i,k) (i,k-1) (i+1,k-1)
-#pragma unroll
-    for (int q = 15; q < 21; ++q) sC[q * BX * BZ + tid] = cf(q, L2);  // over (i,k) (i-1,k) (i,k-1) (i-1,k-1)
-#pragma unroll
-    for (int q = 21; q < 27; ++q) sC[q * BX * BZ + tid] = cf(q, L3);  // over (i,k+1) (i,k) (i-1,k) (i-1,k+1)
-#pragma unroll
-    for (int q = 27; q < 33; ++q) sC[q * BX * BZ + tid] = cf(q, L4);  // over (i+1,k) (i,k) (i,k+1) (i+1,k+1)
-  }
-  // volatile: read at each use, not hoisted back into registers
-  const volatile float* cc = sC + tid;
-  auto C = [&](int q) -> float { return cc[q * BX * BZ]; };
-
-  const bool xs = in_strip(i, NX, W), zs = in_strip(k, NZ, W);
-  const int xsi = xs ? strip_idx(i, NX, W) : 0;
-  const int zsi = zs ? strip_idx(k, NZ, W) : 0;
-  const float ikx = a.X.ik[i], ikxh = a.X.ikh[i], adx = a.X.ad[i], adxh = a.X.adh[i];
-  const float bx = a.X.b[i], bxh = a.X.bh[i];
-  const float ikz = a.Z.ik[k], ikzh = a.Z.ikh[k], adz = a.Z.ad[k], adzh = a.Z.adh[k];
-  const float bz = a.Z.b[k], bzh = a.Z.bh[k];
-  const float idx = a.idx, idz = a.idz;
-  const size_t plane = (size_t)NY * P;      // one z-plane of a field
-
-  // Velocities are read-only in this kernel: read them through the
-  // non-coherent path, once per cell, and carry the y-neighbours in registers.
-  const float* __restrict__ VX = a.vx;
-  const float* __restrict__ VY = a.vy;
-  const float* __restrict__ VZ = a.vz;
-  // The stresses and memory variables are distinct arrays: with that stated,
-  // every load of a y step is issued before its first store instead of
-  // after the store of the previous loop (one memory round trip per step
-  // instead of one per loop).
-  float* __restrict__ SXX = a.sxx;
-  float* __restrict__ SYY = a.syy;
-  float* __restrict__ SZZ = a.szz;
-  float* __restrict__ SXY = a.sxy;
-  float* __restrict__ SXZ = a.sxz;
-  float* __restrict__ SYZ = a.syz;
-  float* __restrict__ MVXX = a.m_vx_x;
-  float* __restrict__ MVYX = a.m_vy_x;
-  float* __restrict__ MVZX = a.m_vz_x;
-  float* __restrict__ MVXY = a.m_vx_y;
-  float* __restrict__ MVYY = a.m_vy_y;
-  float* __restrict__ MVZY = a.m_vz_y;
-  float* __restrict__ MVXZ = a.m_vx_z;
-  float* __restrict__ MVYZ = a.m_vy_z;
-  float* __restrict__ MVZZ = a.m_vz_z;
-  const bool has_xm = i >= 1, has_xp = i <= NX - 2, has_zm = k >= 1, has_zp = k <= NZ - 2;
-  size_t c = ((size_t)k * NY + j0) * P + i;
-  float cvx = __ldg(VX + c), cvy = __ldg(VY + c), cvz = __ldg(VZ + c);
-  float pvx = 0.f, pvy = 0.f, pvz = 0.f;
-  if (j0 >= 1) { pvx = __ldg(VX + c - P); pvy = __ldg(VY + c - P); pvz = __ldg(VZ + c - P); }
-  for (int j = j0; j < j1; ++j, c += P) {
-    const bool ys = in_strip(j, NY, W);
-    const size_t mx = ((size_t)k * NY + j) * (2 * W) + xsi;
-    const size_t my = ((size_t)k * (2 * W) + (ys ? strip_idx(j, NY, W) : 0)) * P + i;
-    const size_t mz = ((size_t)zsi * NY + j) * P + i;
-    float nvx = 0.f, nvy = 0.f, nvz = 0.f;
-    if (j + 1 < NY) { nvx = __ldg(VX + c + P); nvy = __ldg(VY + c + P); nvz = __ldg(VZ + c + P); }
-    float xmx = 0.f, xmy = 0.f, xmz = 0.f, xpx = 0.f, xpy = 0.f, xpz = 0.f;
-    float zmx = 0.f, zmy = 0.f, zmz = 0.f, zpx = 0.f, zpy = 0.f, zpz = 0.f;
-    if (has_xm) { xmx = __ldg(VX + c - 1); xmy = __ldg(VY + c - 1); xmz = __ldg(VZ + c - 1); }
-    if (has_xp) { xpx = __ldg(VX + c + 1); xpy = __ldg(VY + c + 1); xpz = __ldg(VZ + c + 1); }
-    if (has_zm) { zmx = __ldg(VX + c - plane); zmy = __ldg(VY + c - plane); zmz = __ldg(VZ + c - plane); }
-    if (has_zp) { zpx = __ldg(VX + c + plane); zpy = __ldg(VY + c + plane); zpz = __ldg(VZ + c + plane); }
-    float mvxx = 0, mvyx = 0, mvzx = 0, mvxy = 0, mvyy = 0, mvzy = 0, mvxz = 0, mvyz = 0, mvzz = 0;
-    if (xs) { mvxx = MVXX[mx]; mvyx = MVYX[mx]; mvzx = MVZX[mx]; }
-    if (ys) { mvxy = MVXY[my]; mvyy = MVYY[my]; mvzy = MVZY[my]; }
-    if (zs) { mvxz = MVXZ[mz]; mvyz = MVYZ[mz]; mvzz = MVZZ[mz]; }
-    const bool l1 = L1 && j >= 1, l2 = L2 && j <= NY - 2, l3 = L3 && j >= 1, l4 = L4 && j <= NY - 2;
-    float oxx = 0.f, oyy = 0.f, ozz = 0.f, oxy = 0.f, oxz = 0.f, oyz = 0.f;
-    if (l1) { oxx = SXX[c]; oyy = SYY[c]; ozz = SZZ[c]; }
-    if (l2) oxy = SXY[c];
-    if (l3) oxz = SXZ[c];
-    if (l4) oyz = SYZ[c];
-    const float iky = a.Y.ik[j], ikyh = a.Y.ikh[j], ady = a.Y.ad[j], adyh = a.Y.adh[j];
-    const float by = a.Y.b[j], byh = a.Y.bh[j];
-
-    // ---- Loop 1: sigmaxx, sigmayy, sigmazz (j >= 1): x+, y-, z- differences
-    if (l1) {
-      const float dxx = xpx - cvx, dyx = xpy - cvy, dzx = xpz - cvz;
-      const float dyy = cvy - pvy, dxy = cvx - pvx, dzy = cvz - pvz;
-      const float dzz = cvz - zmz, dxz = cvx - zmx, dyz = cvy - zmy;
-      if (xs) { mvxx = bxh * mvxx + adxh * dxx; mvyx = bxh * mvyx + adxh * dyx; mvzx = bxh * mvzx + adxh * dzx; }
-      if (ys) { mvyy = by * mvyy + ady * dyy; mvxy = by * mvxy + ady * dxy; mvzy = by * mvzy + ady * dzy; }
-      if (zs) { mvzz = bz * mvzz + adz * dzz; mvxz = bz * mvxz + adz * dxz; mvyz = bz * mvyz + adz * dyz; }
-      const float vxx = dxx * ikxh + mvxx, vyx = dyx * ikxh + mvyx, vzx = dzx * ikxh + mvzx;
-      const float vyy = dyy * iky + mvyy, vxy = dxy * iky + mvxy, vzy = dzy * iky + mvzy;
-      const float vzz = dzz * ikz + mvzz, vxz = dxz * ikz + mvxz, vyz = dyz * ikz + mvyz;
-      SXX[c] = oxx + (C(0) * vxx + C(1) * vyy + C(2) * vzz + C(3) * (vyz + vzy) + C(4) * (vxz + vzx) +
-                      C(5) * (a.legacy ? vxy + vzy : vxy + vyx));  // Q4, :657
-      SYY[c] = oyy + (C(1) * vxx + C(6) * vyy + C(7) * vzz + C(8) * (vyz + vzy) + C(9) * (vxz + vzx) +
-                      C(10) * (vyx + vxy));
-      SZZ[c] = ozz + (C(2) * vxx + C(7) * vyy + C(11) * vzz + C(12) * (vyz + vzy) + C(13) * (vxz + vzx) +
-                      C(14) * (vyx + vxy));
-    }
-    // ---- Loop 2: sigmaxy (j <= NY-2): x-, y+, z-
-    if (l2) {
-      const float dxx = cvx - xmx, dyx = cvy - xmy, dzx = cvz - xmz;
-      const float dyy = nvy - cvy, dxy = nvx - cvx, dzy = nvz - cvz;
-      const float dzz = cvz - zmz, dxz = cvx - zmx, dyz = cvy - zmy;
-      if (xs) { mvxx = bx * mvxx + adx * dxx; mvyx = bx * mvyx + adx * dyx; mvzx = bx * mvzx + adx * dzx; }
-      if (ys) { mvyy = byh * mvyy + adyh * dyy; mvxy = byh * mvxy + adyh * dxy; mvzy = byh * mvzy + adyh * dzy; }
-      if (zs) { mvzz = bzh * mvzz + adzh * dzz; mvxz = bzh * mvxz + adzh * dxz; mvyz = bzh * mvyz + adzh * dyz; }
-      const float vxx = dxx * ikx + mvxx, vyx = dyx * ikx + mvyx;
-      const float vyy = dyy * ikyh + mvyy, vxy = dxy * ikyh + mvxy, vzy = dzy * ikyh + mvzy;
-      const float vzz = dzz * ikzh + mvzz, vyz = dyz * ikzh + mvyz;
-      const float vzx = dzx * idx, vxz = dxz * idz;  // left unscaled, :701-707
-      SXY[c] = oxy + (C(15) * vxx + C(16) * vyy + C(17) * vzz + C(18) * (vzy + vyz) + C(19) * (vzx + vxz) +
-                      C(20) * (vyx + vxy));
-    }
-    // ---- Loop 3: sigmaxz (j >= 1): x-, y-, z+
-    if (l3) {
-      const float dxx = cvx - xmx, dyx = cvy - xmy, dzx = cvz - xmz;
-      const float dyy = cvy - pvy, dzy = cvz - pvz, dxy = cvx - pvx;
-      const float dzz = zpz - cvz, dxz = zpx - cvx, dyz = zpy - cvy;
-      if (xs) { mvxx = bx * mvxx + adx * dxx; mvyx = bx * mvyx + adx * dyx; mvzx = bx * mvzx + adx * dzx; }
-      if (ys) { mvyy = by * mvyy + ady * dyy; mvxy = by * mvxy + ady * dxy; mvzy = by * mvzy + ady * dzy; }
-      if (zs) { mvzz = bzh * mvzz + adzh * dzz; mvxz = bzh * mvxz + adzh * dxz; mvyz = bzh * mvyz + adzh * dyz; }
-      const float vxx = dxx * ikx + mvxx, vyx = dyx * ikx + mvyx, vzx = dzx * ikx + mvzx;
-      const float vyy = dyy * iky + mvyy, vxy = dxy * iky + mvxy, vzy = dzy * iky + mvzy;
-      const float vzz = dzz * ikzh + mvzz, vxz = dxz * ikzh + mvxz, vyz = dyz * ikzh + mvyz;
-      SXZ[c] = oxz + (C(21) * vxx + C(22) * vyy + C(23) * vzz + C(24) * (a.legacy ? vxz + vzx : vyz + vzy) +  // Q4, :766
-                      C(25) * (vxz + vzx) + C(26) * (vxy + vyx));
-    }
-    // ---- Loop 4: sigmayz (j <= NY-2): x+, y+, z+
-    if (l4) {
-      const float dxx = xpx - cvx, dyx = xpy - cvy, dzx = xpz - cvz;
-      const float dyy = nvy - cvy, dxy = nvx - cvx, dzy = nvz - cvz;
-      const float dzz = zpz - cvz, dxz = zpx - cvx, dyz = zpy - cvy;
-      if (xs) { mvxx = bxh * mvxx + adxh * dxx; mvyx = bxh * mvyx + adxh * dyx; mvzx = bxh * mvzx + adxh * dzx; }
-      if (ys) { mvyy = byh * mvyy + adyh * dyy; mvxy = byh * mvxy + adyh * dxy; mvzy = byh * mvzy + adyh * dzy; }
-      if (zs) { mvzz = bzh * mvzz + adzh * dzz; mvxz = bzh * mvxz + adzh * dxz; mvyz = bzh * mvyz + adzh * dyz; }
-      const float vxx = dxx * ikxh + mvxx, vyx = dyx * ikxh + mvyx, vzx = dzx * ikxh + mvzx;
-      const float vyy = dyy * ikyh + mvyy, vxy = dxy * ikyh + mvxy, vzy = dzy * ikyh + mvzy;
-      const float vzz = dzz * ikzh + mvzz, vxz = dxz * ikzh + mvxz, vyz = dyz * ikzh + mvyz;
-      SYZ[c] = oyz + (C(27) * vxx + C(28) * vyy + C(29) * vzz + C(30) * (vyz + vzy) + C(31) * (vxz + vzx) +
-                      C(32) * (vyx + vxy));
-    }
-    if (xs) { MVXX[mx] = mvxx; MVYX[mx] = mvyx; MVZX[mx] = mvzx; }
-    if (ys) { MVXY[my] = mvxy; MVYY[my] = mvyy; MVZY[my] = mvzy; }
-    if (zs) { MVXZ[mz] = mvxz; MVYZ[mz] = mvyz; MVZZ[mz] = mvzz; }
-    if (a.io.ssrc && i == a.io.si && j == a.io.sj && k == a.io.sk) {  // stress source: sigma_ij += f_ij(t) dt
-      const float* f = a.io.ssrc + t;
-      const int n = a.io.nstep;
-      SXX[c] += f[0];
-      SYY[c] += f[n];
-      SZZ[c] += f[2 * n];
-      SXY[c] += f[3 * n];
-      SXZ[c] += f[4 * n];
-      SYZ[c] += f[5 * n];
-    }
-    pvx = cvx; pvy = cvy; pvz = cvz;
-    cvx = nvx; cvy = nvy; cvz = nvz;
-  }
-}
-
-__global__ void __launch_bounds__(BX * BZ, SEIS25_VELOCITY_BLOCKS) seis25_velocity_kernel(Seis25Args a, int rel) {
-  const int t = a.io.ctl->base + rel;
-  const int i = blockIdx.x * BX + threadIdx.x;
-  const int k = blockIdx.y * BZ + threadIdx.y;
-  const int NX = a.NX, NY = a.NY, NZ = a.NZ, P = a.P, W = a.W;
-  const int seg = (NY + a.ysplit - 1) / a.ysplit;
-  const int j0 = blockIdx.z * seg, j1 = min(NY, j0 + seg);
-  float norm = 0.0f;
-  if (i < NX && k < NZ && j0 < j1) {
-    const bool Vx = (k >= 1) && (i >= 1);
-    const bool Vy = (k >= 1) && (i <= NX - 2);
-    const bool Vz = (k <= NZ - 2) && (i <= NX - 2);
-    const size_t pc = (size_t)k * P + i;
-    const size_t p2 = (size_t)NZ * P;
-    const float dtrx = Vx ? a.dtr[pc] : 0.f, dtry = Vy ? a.dtr[p2 + pc] : 0.f, dtrz = Vz ? a.dtr[2 * p2 + pc] : 0.f;
-    float gx = 1.f, gy = 1.f, gz = 1.f;
-    if (a.atten) { gx = a.gp[pc]; gy = a.gp[p2 + pc]; gz = a.gp[2 * p2 + pc]; }
-    const bool xs = in_strip(i, NX, W), zs = in_strip(k, NZ, W);
-    const int xsi = xs ? strip_idx(i, NX, W) : 0;
-    const int zsi = zs ? strip_idx(k, NZ, W) : 0;
-    const float ikx = a.X.ik[i], ikxh = a.X.ikh[i], adx = a.X.ad[i], adxh = a.X.adh[i];
-    const float bx = a.X.b[i], bxh = a.X.bh[i];
-    const float ikz = a.Z.ik[k], ikzh = a.Z.ikh[k], adz = a.Z.ad[k], adzh = a.Z.adh[k];
-    const float bz = a.Z.b[k], bzh = a.Z.bh[k];
-    const size_t plane = (size_t)NY * P;
-    const bool xface = (i == 0) || (i == NX - 1) || (k == 0) || (k == NZ - 1);
-    // Stresses are read-only here: one non-coherent load per value, sxy/syz at
-    // j-1 and syy at j+1 carried along the y march.
-    const float* __restrict__ SXX = a.sxx;
-    const float* __restrict__ SYY = a.syy;
-    const float* __restrict__ SZZ = a.szz;
-    const float* __restrict__ SXY = a.sxy;
-    const float* __restrict__ SXZ = a.sxz;
-    const float* __restrict__ SYZ = a.syz;
-    // velocities and memory variables: distinct arrays, every load of a y
-    // step issued before its first store (as in the stress kernel)
-    float* __restrict__ VX = a.vx;
-    float* __restrict__ VY = a.vy;
-    float* __restrict__ VZ = a.vz;
-    float* __restrict__ MSXXX = a.m_sxx_x;
-    float* __restrict__ MSXYY = a.m_sxy_y;
-    float* __restrict__ MSXZZ = a.m_sxz_z;
-    float* __restrict__ MSXYX = a.m_sxy_x;
-    float* __restrict__ MSYYY = a.m_syy_y;
-    float* __restrict__ MSYZZ = a.m_syz_z;
-    float* __restrict__ MSXZX = a.m_sxz_x;
-    float* __restrict__ MSYZY = a.m_syz_y;
-    float* __restrict__ MSZZZ = a.m_szz_z;
-    size_t c = ((size_t)k * NY + j0) * P + i;
-    float psxy = 0.f, psyz = 0.f;
-    if (j0 >= 1) { psxy = __ldg(SXY + c - P); psyz = __ldg(SYZ + c - P); }
-    float csyy = __ldg(SYY + c);
-    for (int j = j0; j < j1; ++j, c += P) {
-      const bool ys = in_strip(j, NY, W);
-      const size_t mx = ((size_t)k * NY + j) * (2 * W) + xsi;
-      const size_t my = ((size_t)k * (2 * W) + (ys ? strip_idx(j, NY, W) : 0)) * P + i;
-      const size_t mz = ((size_t)zsi * NY + j) * P + i;
-      const float iky = a.Y.ik[j], ikyh = a.Y.ikh[j], ady = a.Y.ad[j], adyh = a.Y.adh[j];
-      const float by = a.Y.b[j], byh = a.Y.bh[j];
-      const float csxx = __ldg(SXX + c), csxy = __ldg(SXY + c), csxz = __ldg(SXZ + c);
-      const float csyz = __ldg(SYZ + c), cszz = __ldg(SZZ + c);
-      const float nsyy = (j + 1 < NY) ? __ldg(SYY + c + P) : 0.f;
-      float vx = VX[c], vy = VY[c], vz = VZ[c];
-      const bool ux = Vx && j >= 1, uy = Vy && j <= NY - 2, uz = Vz && j >= 1;
-      // memory variables of the three loops, loaded up front
-      float m1x = 0.f, m1y = 0.f, m1z = 0.f, m2x = 0.f, m2y = 0.f, m2z = 0.f, m3x = 0.f, m3y = 0.f, m3z = 0.f;
-      if (xs) {
-        if (ux) m1x = MSXXX[mx];
-        if (uy) m2x = MSXYX[mx];
-        if (uz) m3x = MSXZX[mx];
-      }
-      if (ys) {
-        if (ux) m1y = MSXYY[my];
-        if (uy) m2y = MSYYY[my];
-        if (uz) m3y = MSYZY[my];
-      }
-      if (zs) {
-        if (ux) m1z = MSXZZ[mz];
-        if (uy) m2z = MSYZZ[mz];
-        if (uz) m3z = MSZZZ[mz];
-      }
-      if (ux) {  // :821-845
-        const float d1 = csxx - __ldg(SXX + c - 1), d2 = csxy - psxy, d3 = csxz - __ldg(SXZ + c - plane);
-        float v1 = d1 * ikx, v2 = d2 * iky, v3 = d3 * ikz;
-        if (xs) { const float m = bx * m1x + adx * d1; MSXXX[mx] = m; v1 += m; }
-        if (ys) { const float m = by * m1y + ady * d2; MSXYY[my] = m; v2 += m; }
-        if (zs) { const float m = bz * m1z + adz * d3; MSXZZ[mz] = m; v3 += m; }
-        vx = vx * gx + (v1 + v2 + v3) * dtrx;
-      }
-      if (uy) {  // :847-869
-        const float d1 = __ldg(SXY + c + 1) - csxy, d2 = nsyy - csyy, d3 = csyz - __ldg(SYZ + c - plane);
-        float v1 = d1 * ikxh, v2 = d2 * ikyh, v3 = d3 * ikz;
-        if (xs) { const float m = bxh * m2x + adxh * d1; MSXYX[mx] = m; v1 += m; }
-        if (ys) { const float m = byh * m2y + adyh * d2; MSYYY[my] = m; v2 += m; }
-        if (zs) { const float m = bz * m2z + adz * d3; MSYZZ[mz] = m; v3 += m; }
-        vy = vy * gy + (v1 + v2 + v3) * dtry;
-      }
-      if (uz) {  // :872-896
-        const float d1 = __ldg(SXZ + c + 1) - csxz, d2 = csyz - psyz, d3 = __ldg(SZZ + c + plane) - cszz;
-        float v1 = d1 * ikxh, v2 = d2 * iky, v3 = d3 * ikzh;
-        if (xs) { const float m = bxh * m3x + adxh * d1; MSXZX[mx] = m; v1 += m; }
-        if (ys) { const float m = by * m3y + ady * d2; MSYZY[my] = m; v2 += m; }
-        if (zs) { const float m = bzh * m3z + adzh * d3; MSZZZ[mz] = m; v3 += m; }
-        vz = vz * gz + (v1 + v2 + v3) * dtrz;
-      }
-      if (i == a.io.si && j == a.io.sj && k == a.io.sk) {  // :898-900
-        vx += a.io.src[t];
-        vy += a.io.src[a.io.nstep + t];
-        vz += a.io.src[2 * a.io.nstep + t];
-      }
-      if (xface || j == 0 || j == NY - 1) { vx = 0.f; vy = 0.f; vz = 0.f; }  // :903-925
-      VX[c] = vx;
-      VY[c] = vy;
-      VZ[c] = vz;
-      norm = fmaxf(norm, norm_monitor(vx, vy, vz));
-      psxy = csxy;
-      psyz = csyz;
-      csyy = nsyy;
-    }
-  }
-  block_norm_to_slot(norm, a.io.slots, (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
-}
-
-// ---------------------------------------------------------------------------
-// The TMA-staged form.  Each block (32 x BZ columns, one y segment) streams
-// its y planes through a ring of RING shared-memory stages, each filled by
-// cp.async.bulk.tensor copies that one thread issues RING - 2 planes ahead
-// and every thread waits for on the stage's mbarrier:
+//
+// Each block (32 x BZ columns, one y segment) streams its y planes through a
+// ring of RING shared-memory stages, each filled by cp.async.bulk.tensor
+// copies that one thread issues RING - 2 planes ahead and every thread waits
+// for on the stage's mbarrier:
 //   stress kernel:   the three velocities of the plane with a one-cell halo
 //                    (x from i0 - 4, so the box starts on a 16-byte boundary;
 //                    rows k0 - 1 .. k0 + BZ), and the six stresses of the
@@ -373,9 +35,26 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_VELOCITY_BLOCKS) seis25_veloci
 // needs its plane and the next, so RING - 2 planes stay in flight while it
 // computes; the memory variables (strips only) and the results go through
 // plain loads and stores.  Boxes reaching past the grid read zeros, the
-// values the plain form substitutes there.
-#ifndef SEIS25_TMA
-#define SEIS25_TMA 1
+// values the Fortran's loop bounds leave there.  Staging replaced a plain
+// y-march whose every step waited a memory round trip (0.682 against 0.587
+// ms per step on the 630 x 70 x 330 grid).
+#include "sfd_solvers.h"
+#include "tma.cuh"
+
+namespace sfd {
+
+namespace {
+
+constexpr int BX = 32, BZ = 4;
+
+// Resident blocks per SM the two kernels are compiled for (registers per
+// thread = 65536 / (128 x blocks)); build-time tunables, the defaults the
+// measured best on the 630 x 70 x 330 grid (the stress kernel spills at 5).
+#ifndef SEIS25_STRESS_BLOCKS
+#define SEIS25_STRESS_BLOCKS 4
+#endif
+#ifndef SEIS25_VELOCITY_BLOCKS
+#define SEIS25_VELOCITY_BLOCKS 6
 #endif
 
 constexpr int HX = 4;                  // x halo of the staged tiles (16 bytes)
@@ -769,17 +448,11 @@ Launch seis25_launch(const Seis25Args& a) {
 }
 
 void seis25_half1(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s) {
-  if (SEIS25_TMA)
-    seis25_stress_tma_kernel<<<L.grid, L.block, RING * S_STAGE * sizeof(float), s>>>(a, rel);
-  else
-    seis25_stress_kernel<<<L.grid, L.block, 0, s>>>(a, rel);
+  seis25_stress_tma_kernel<<<L.grid, L.block, RING * S_STAGE * sizeof(float), s>>>(a, rel);
 }
 
 void seis25_half2(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s) {
-  if (SEIS25_TMA)
-    seis25_velocity_tma_kernel<<<L.grid, L.block, RING * V_STAGE * sizeof(float), s>>>(a, rel);
-  else
-    seis25_velocity_kernel<<<L.grid, L.block, 0, s>>>(a, rel);
+  seis25_velocity_tma_kernel<<<L.grid, L.block, RING * V_STAGE * sizeof(float), s>>>(a, rel);
 }
 
 bool seis25_make_maps(Seis25Args& a, size_t field_stride) {
