@@ -334,6 +334,40 @@ def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000, 
         num += float(((tp - tb) ** 2).sum())
         den += float((tp ** 2).sum())
     plain_agg = cells * nstep / (plain_ms / 1e3) / 1e9
+    # ... and through the one-launch-per-step kernels whose tile bodies the
+    # batch runs (SFD_FLAG_STREAMING: no model runs on chip)
+    from seidart_gb300.solver import FLAG_STREAMING
+    step_solvers, owner2 = [], {}
+    for c in cases:
+        s = FDTDSolver(c.grid, c.nstep, len(c.rec_ijk), device=device, flags=FLAG_STREAMING)
+        if id(c.planes) in owner2:
+            s.share_model(owner2[id(c.planes)])
+        else:
+            s.set_model(c.planes)
+            owner2[id(c.planes)] = s
+        s.set_cpml(c.profiles)
+        s.set_source(c.src_ijk, c.srcfn)
+        s.set_receivers(c.rec_ijk)
+        step_solvers.append(s)
+    for s in step_solvers:
+        s.run(8)
+        s.reset()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for s in step_solvers:
+        s.run(nstep)
+    ev1.record(stream)
+    for s in step_solvers:
+        s.status()
+    step_ms = ev0.elapsed_time(ev1)
+    num2 = den2 = 0.0
+    for s, tb in zip(step_solvers, batched_traces):
+        tp = s.traces().astype(np.float64)
+        num2 += float(((tp - tb) ** 2).sum())
+        den2 += float((tp ** 2).sum())
+    for s in step_solvers:
+        s.close()
+    step_agg = cells * nstep / (step_ms / 1e3) / 1e9
     out = {"workload": f"64 electromag2 shots 1040x540 + 16 seismic2 models (nx 200-1200, nz 100-600) x {nstep} steps",
            "value": round(value, 3), "unit": METRIC, "ms_per_run": round(ms, 2), "cells": cells,
            "bytes_per_cell_update": round(step_bytes / cells, 2),
@@ -344,6 +378,10 @@ def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000, 
            "plain_sequential": {"value": round(plain_agg, 3), "unit": METRIC, "ms_per_run": round(plain_ms, 2),
                                 "traces_rel_l2_vs_batched": (num / den) ** 0.5 if den > 0 else None},
            "vs_plain_aggregate": round(value / plain_agg, 3),
+           "per_step_sequential": {"value": round(step_agg, 3), "unit": METRIC, "ms_per_run": round(step_ms, 2),
+                                   "form": "each model alone, one launch per step (SFD_FLAG_STREAMING)",
+                                   "traces_rel_l2_vs_batched": (num2 / den2) ** 0.5 if den2 > 0 else None},
+           "vs_per_step_aggregate": round(value / step_agg, 3),
            "tiling": {"rows_per_thread": tune["tiling"][0], "blocks_per_sm": tune["tiling"][1],
                       "candidates_ms_per_step": {k: round(v * 1e3, 4) for k, v in tune["timings"].items()}},
            "launches_per_run": 3}

@@ -345,6 +345,13 @@ int32_t sfd_electromag2_run_static(const sfd_config* cfg, const double* model, c
 int32_t sfd_checkpoint_bytes(const sfd_handle* h, size_t* bytes);
 int32_t sfd_checkpoint_save(sfd_handle* h, void* dev_dst);
 int32_t sfd_checkpoint_load(sfd_handle* h, const void* dev_src, int64_t step);
+/* sfd_run(h, nsteps) that also saves a checkpoint before every `every`
+ * steps: checkpoint q, the state at step (current + q * every), goes to
+ * dev_ckpt + q * stride (stride >= sfd_checkpoint_bytes, 4-byte aligned),
+ * for q = 0 .. ceil(nsteps / every) - 1.  An electromag2 handle whose runs
+ * are on chip writes them from the one launch of the run, without stopping
+ * it; the other handles stop every `every` steps to copy the state. */
+int32_t sfd_run_checkpointed(sfd_handle* h, int64_t nsteps, void* dev_ckpt, size_t stride, int32_t every);
 
 /* ---- Discrete adjoint (electromag2 single-pass handles; seismic2) ----------
  * Gradient of J with respect to the model planes, given dJ/d(trace)

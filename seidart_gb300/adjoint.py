@@ -44,6 +44,7 @@ def _declare(L):
         ("sfd_checkpoint_bytes", i32, [P, C.POINTER(sz)]),
         ("sfd_checkpoint_save", i32, [P, P]),
         ("sfd_checkpoint_load", i32, [P, P, i64]),
+        ("sfd_run_checkpointed", i32, [P, i64, P, sz, i32]),
         ("sfd_adjoint_bytes", i32, [P, i32, C.POINTER(sz)]),
         ("sfd_adjoint_begin", i32, [P, P, sz, i32, P]),
         ("sfd_adjoint_segment", i32, [P, i64]),
@@ -95,10 +96,8 @@ class _Checkpointed:
         s.set_model(planes)
         s.set_source(self.src_ijk, self.srcfn)  # the amplitude is divided by the model at the source
         s.reset()
-        h = s._h
-        for q in range(self.nseg):
-            check(self._L.sfd_checkpoint_save(h, C.c_void_p(self.ckpt[q].data_ptr())))
-            s.run(min(self.ckpt_every, self.nstep - q * self.ckpt_every))
+        check(self._L.sfd_run_checkpointed(s._h, self.nstep, C.c_void_p(self.ckpt.data_ptr()),
+                                           C.c_size_t(self.ckpt.stride(0)), self.ckpt_every))
         s.status()
         return s.traces_tensor().clone()
 

@@ -100,6 +100,10 @@ struct Em2Resident {
   unsigned long long limit_ns;  // longest wait for a neighbour before the run is abandoned
   unsigned tag_bias;            // added to every awaited edge tag; 0 except in the timeout test aid
   ResDump dump;
+  // checkpoints: after every ckpt_every-th step of the run (not its last),
+  // the state in the sfd_checkpoint_save layout at ckpt.base + (s / every) * stride
+  ResDump ckpt;
+  int ckpt_every;
 };
 
 // On-chip adjoint sweep over one checkpoint segment: the transposed steps

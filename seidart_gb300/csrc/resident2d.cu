@@ -46,8 +46,11 @@ using namespace res;
 
 namespace {
 
-template <bool DUMP>
+// MODE 0: a run; 1: a recompute for the adjoint (every step's state dumped,
+// the handle's state kept); 2: a run that also saves checkpoints.
+template <int MODE>
 __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __grid_constant__ Em2Resident a) {
+  constexpr bool DUMP = MODE == 1, CKPT = MODE == 2;
   constexpr int RB = kResRows;
   extern __shared__ __align__(16) float smem[];
   __shared__ int s_abort, s_nrec;
@@ -437,6 +440,36 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
           for (int e = 0; e < 4; ++e)
             if (mbit(m[j], kMHYZ, e)) el(hy[j], e) = 0.0f;
       }
+      if (CKPT && (s + 1) % a.ckpt_every == 0 && s + 1 < a.nsteps) {
+        // a checkpoint: the state the handle would hold after step t, in the
+        // sfd_checkpoint_save layout (scalar stores: the caller's rows need
+        // only 4-byte alignment)
+        char* d = a.ckpt.base + (size_t)((s + 1) / a.ckpt_every) * a.ckpt.stride;
+#pragma unroll
+        for (int j = 0; j < RB; ++j) {
+          if (j >= nrows) continue;
+          const int row = rbase + j, k = z0 + row;
+          const int gg = k * P + i0, so = 4 * (j * kResCellThreads + tid);
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int i = i0 + e;
+            if (i >= NX) continue;
+            __stcs((float*)(d + a.ckpt.off[0]) + gg + e, el(ex[j], e));
+            __stcs((float*)(d + a.ckpt.off[1]) + gg + e, el(ez[j], e));
+            __stcs((float*)(d + a.ckpt.off[2]) + gg + e, el(hy[j], e));
+            if (zs[j]) {
+              const int zrow = strip_idx(k, NZ, W) * P + i;
+              __stcs((float*)(d + a.ckpt.off[3]) + zrow, sMExz[so + e]);
+              __stcs((float*)(d + a.ckpt.off[5]) + zrow, sMHyz[so + e]);
+            }
+            if (in_strip(i, NX, W)) {
+              const int q = k * (2 * W) + strip_idx(i, NX, W);
+              __stcs((float*)(d + a.ckpt.off[4]) + q, sMEzx[so + e]);
+              __stcs((float*)(d + a.ckpt.off[6]) + q, sMHyx[so + e]);
+            }
+          }
+        }
+      }
       if (recm) {  // receivers of step t
         float* tr = a.io.traces + (size_t)t * 2 * a.io.nrec;
 #pragma unroll
@@ -624,20 +657,25 @@ bool em2_resident_plan(int NX, int NZ, int npml, int max_ctas, size_t max_smem, 
 }
 
 cudaError_t em2_resident_prepare(const ResPlan& plan, int* ctas_per_sm) {
-  cudaError_t e = res_allow_max_smem((const void*)em2_resident_kernel<false>);
-  if (e == cudaSuccess) e = res_allow_max_smem((const void*)em2_resident_kernel<true>);
-  if (e != cudaSuccess) return e;
-  int n0 = 0, n1 = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n0, em2_resident_kernel<false>, kResThreads, plan.smem);
-  if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, em2_resident_kernel<true>, kResThreads, plan.smem);
-  *ctas_per_sm = std::min(n0, n1);
-  return e;
+  const void* fns[3] = {(const void*)em2_resident_kernel<0>, (const void*)em2_resident_kernel<1>,
+                        (const void*)em2_resident_kernel<2>};
+  int n = 1 << 30;
+  for (const void* fn : fns) {
+    cudaError_t e = res_allow_max_smem(fn);
+    int q = 0;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, fn, kResThreads, plan.smem);
+    if (e != cudaSuccess) return e;
+    n = std::min(n, q);
+  }
+  *ctas_per_sm = n;
+  return cudaSuccess;
 }
 
 cudaError_t em2_resident_launch(const Em2Resident& a, cudaStream_t s) {
   void* args[] = {(void*)&a};
-  const void* fn = a.dump.base ? (const void*)em2_resident_kernel<true> : (const void*)em2_resident_kernel<false>;
+  const void* fn = a.dump.base   ? (const void*)em2_resident_kernel<1>
+                   : a.ckpt.base ? (const void*)em2_resident_kernel<2>
+                                 : (const void*)em2_resident_kernel<0>;
   return cudaLaunchCooperativeKernel(fn, dim3(a.plan.ntiles), dim3(kResThreads), args, a.plan.smem, s);
 }
 

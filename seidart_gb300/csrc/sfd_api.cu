@@ -667,6 +667,8 @@ Em2Resident resident_args(const sfd_handle* h, int64_t nsteps) {
   r.limit_ns = h->wait_ns;
   r.tag_bias = h->stall_waits ? kStallTagBias : 0u;
   r.dump = ResDump{nullptr, 0, {0, 0, 0, 0, 0, 0, 0}};
+  r.ckpt = ResDump{nullptr, 0, {0, 0, 0, 0, 0, 0, 0}};
+  r.ckpt_every = 0;
   return r;
 }
 
@@ -2158,6 +2160,57 @@ int32_t sfd_checkpoint_load(sfd_handle* h, const void* dev_src, int64_t step) {
     d += mb;
   }
   h->step = step;
+  return SFD_OK;
+}
+
+int32_t sfd_run_checkpointed(sfd_handle* h, int64_t nsteps, void* dev_ckpt, size_t stride, int32_t every) {
+  g_err.clear();
+  if (!h || !dev_ckpt) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  if (!h->have_model || !h->have_cpml) return fail(SFD_ERR_STATE, "sfd_run needs sfd_set_model and sfd_set_cpml first");
+  if (nsteps < 0 || every < 1) return fail(SFD_ERR_BAD_ARG, "need nsteps >= 0 and every >= 1");
+  if (h->step + nsteps > h->cfg.nstep)
+    return fail(SFD_ERR_BAD_ARG, "run to step %lld exceeds the %d source samples", (long long)(h->step + nsteps), h->cfg.nstep);
+  const size_t nb = ckpt_bytes(h);
+  if (stride < nb) return fail(SFD_ERR_BAD_ARG, "checkpoint stride %zu is below the %zu bytes of a checkpoint", stride, nb);
+  if (((uintptr_t)dev_ckpt | stride) & 3) return fail(SFD_ERR_BAD_ARG, "checkpoints must be 4-byte aligned");
+  char* base = (char*)dev_ckpt;
+  int r = sfd_checkpoint_save(h, base);
+  if (r) return r;
+  if (nsteps == 0) return SFD_OK;
+  if (h->cfg.kind == SFD_ELECTROMAG2 && resident_usable(h)) {
+    // one launch for the whole run, the checkpoints written from chip
+    const Layout& L = h->L;
+    Ctl* ctl = (Ctl*)(h->base + L.off_ctl);
+    float* slots = (float*)(h->base + L.off_slots);
+    k_begin<<<std::min(1024, (L.nslots + 255) / 256 + 1), 256, 0, h->stream>>>(ctl, slots, L.nslots, (int)h->step);
+    CK(cudaMemsetAsync(h->base + L.off_res, 0, res_scratch_bytes(L.P, L.NZ, res_edge_fields(h->cfg.kind)), h->stream));
+    Em2Resident ra = resident_args(h, nsteps);
+    ra.ckpt.base = base;
+    ra.ckpt.stride = stride;
+    const size_t F = sizeof(float) * L.fsz;
+    size_t o = 3 * F;
+    for (int q = 0; q < 3; ++q) ra.ckpt.off[q] = q * F;
+    for (int m = 0; m < 4; ++m) {  // dEx_dz dEz_dx dHy_dz dHy_dx: A B C D
+      ra.ckpt.off[3 + m] = o;
+      o += sizeof(float) * L.mem_sz[m];
+    }
+    ra.ckpt_every = every;
+    CK(em2_resident_launch(ra, h->stream));
+    k_reduce_slots<<<1, 1024, 0, h->stream>>>(ctl, slots, L.nslots);
+    CK(cudaGetLastError());
+    h->step += nsteps;
+    return SFD_OK;
+  }
+  for (int64_t done = 0; done < nsteps;) {
+    const int64_t m = std::min<int64_t>(every, nsteps - done);
+    r = sfd_run(h, m);
+    if (r) return r;
+    done += m;
+    if (done < nsteps) {
+      r = sfd_checkpoint_save(h, base + (size_t)(done / every) * stride);
+      if (r) return r;
+    }
+  }
   return SFD_OK;
 }
 

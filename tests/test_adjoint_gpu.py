@@ -154,3 +154,44 @@ def test_on_chip_adjoint_matches_per_step_adjoint(gpu, grid):
     for q in (0, 2, 3, 5):
         err = np.linalg.norm(ga[q] - gb[q]) / np.linalg.norm(gb[q])
         assert err <= 1e-4, f"plane {q}: relative L2 {err:.3e}"
+
+
+@pytest.mark.parametrize("flags", [0, "streaming"])
+def test_run_checkpointed_matches_save_and_run(gpu, flags):
+    """sfd_run_checkpointed (on chip: checkpoints written from the one launch
+    of the run) saves the same states as a save / run loop, and leaves the
+    same final state and traces."""
+    import ctypes as C
+    import torch
+    from seidart_gb300 import _lib
+    from seidart_gb300.adjoint import _declare
+    from seidart_gb300.solver import FLAG_STREAMING
+    from helpers import make_solver
+    case = sy.electromag2_layers(nstep=230)
+    fl = FLAG_STREAMING if flags == "streaming" else 0
+    L = _lib.lib()
+    _declare(L)
+    out = []
+    for mode in ("checkpointed", "loop"):
+        s = make_solver(case, gpu, fl)
+        try:
+            assert (s.on_chip() is not None) == (fl == 0)
+            nb = C.c_size_t()
+            assert L.sfd_checkpoint_bytes(s._h, C.byref(nb)) == 0
+            every = 50
+            nseg = (case.nstep + every - 1) // every
+            ck = torch.zeros((nseg, nb.value + 12), dtype=torch.uint8, device=gpu)  # padded rows: stride > size
+            if mode == "checkpointed":
+                assert L.sfd_run_checkpointed(s._h, case.nstep, C.c_void_p(ck.data_ptr()), C.c_size_t(ck.stride(0)),
+                                              every) == 0, L.sfd_last_error()
+            else:
+                for q in range(nseg):
+                    assert L.sfd_checkpoint_save(s._h, C.c_void_p(ck[q].data_ptr())) == 0
+                    s.run(min(every, case.nstep - q * every))
+            s.status()
+            out.append((ck.cpu().numpy()[:, :nb.value], s.traces(), s.field("Ex")))
+        finally:
+            s.close()
+    (ca, ta, ea), (cb, tb, eb) = out
+    assert np.array_equal(ca, cb)
+    assert np.array_equal(ta, tb) and np.array_equal(ea, eb)
