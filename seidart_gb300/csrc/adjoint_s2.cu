@@ -48,7 +48,8 @@ __device__ __forceinline__ int mz_idx(int i, int k, int NZ, int P, int W) { retu
 // 11 dvz_dx (x), the last four of the sigmaxz loop.
 enum { P1 = 0, P2 = 1, P4 = 2, P3 = 3, R1 = 4, R4 = 5, R3 = 6, R2 = 7, Q1 = 8, Q2 = 9, Q4 = 10, Q3 = 11 };
 
-__global__ void s2adj_inject(S2Adj a, S2State Ln, int t) {
+__global__ void s2adj_inject(S2Adj a, S2State Ln, int rel) {
+  const int t = a.ctl->base + rel;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= a.nrec) return;
   const size_t c = (size_t)a.rec[3 * r + 2] * a.P + a.rec[3 * r];
@@ -56,7 +57,8 @@ __global__ void s2adj_inject(S2Adj a, S2State Ln, int t) {
   atomicAdd(Ln.vz + c, a.resid[((size_t)t * 2 + 1) * a.nrec + r]);
 }
 
-__global__ void __launch_bounds__(BX * BY) s2adj_v(S2Adj a, S2State S, S2State S1, S2State Ln, S2State Lc, int t) {
+__global__ void __launch_bounds__(BX * BY) s2adj_v(S2Adj a, S2State S, S2State S1, S2State Ln, S2State Lc, int rel) {
+  const int t = a.ctl->base + rel;
   const int i = blockIdx.x * BX + threadIdx.x, k = blockIdx.y * BY + threadIdx.y;
   const int NX = a.NX, NZ = a.NZ, P = a.P, W = a.W;
   if (i >= NX || k >= NZ) return;
@@ -239,11 +241,11 @@ __global__ void __launch_bounds__(BX * BY) s2adj_g(S2Adj a, S2State Lc) {
 
 }  // namespace
 
-void s2_adj_step(const S2Adj& a, const S2State& S, const S2State& S1, const S2State& Ln, const S2State& Lc, int t,
+void s2_adj_step(const S2Adj& a, const S2State& S, const S2State& S1, const S2State& Ln, const S2State& Lc, int rel,
                  cudaStream_t s) {
-  if (a.nrec > 0) s2adj_inject<<<(a.nrec + 127) / 128, 128, 0, s>>>(a, Ln, t);
+  if (a.nrec > 0) s2adj_inject<<<(a.nrec + 127) / 128, 128, 0, s>>>(a, Ln, rel);
   const dim3 b(BX, BY), g((a.NX + BX - 1) / BX, (a.NZ + BY - 1) / BY);
-  s2adj_v<<<g, b, 0, s>>>(a, S, S1, Ln, Lc, t);
+  s2adj_v<<<g, b, 0, s>>>(a, S, S1, Ln, Lc, rel);
   s2adj_s<<<g, b, 0, s>>>(a, S, S1, Ln, Lc);
   s2adj_g<<<g, b, 0, s>>>(a, Lc);
 }

@@ -27,12 +27,13 @@ struct S2Adj {
   const int* rec;
   int nrec;
   const float* resid;  // dJ/d(trace) [nstep][2][nrec]
+  const Ctl* ctl;      // its base + a step's relative index = the step
 };
 
-// One reverse step t: S is the forward state before step t, S1 the state
-// after it; Ln the adjoint of S1 (receives this step's residual), Lc the
-// adjoint of S written in full.
-void s2_adj_step(const S2Adj& a, const S2State& S, const S2State& S1, const S2State& Ln, const S2State& Lc, int t,
+// One reverse step t = a.ctl->base + rel: S is the forward state before step
+// t, S1 the state after it; Ln the adjoint of S1 (receives this step's
+// residual), Lc the adjoint of S written in full.
+void s2_adj_step(const S2Adj& a, const S2State& S, const S2State& S1, const S2State& Ln, const S2State& Lc, int rel,
                  cudaStream_t s);
 
 }  // namespace sfd

@@ -290,6 +290,12 @@ struct sfd_handle_s {
   cudaStream_t stream;       // caller's stream
   cudaStream_t cap_stream;   // private stream used only to capture graphs
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // indexed by the parity the graph starts from
+  // a seismic2 adjoint segment's work (s2_adjoint_segment) and what it was captured for
+  cudaGraphExec_t adj_graph = nullptr;
+  int64_t adj_graph_n = 0;
+  int adj_graph_cur = 0, adj_graph_seg = 0;
+  const char* adj_graph_work = nullptr;
+  const float* adj_graph_resid = nullptr;
   bool have_model = false, have_cpml = false;
   bool have_ssrc = false;       // a stress source was set (seismic kinds)
   bool have_force_src = false;  // a force (or E) source was set
@@ -722,6 +728,7 @@ int ensure_graph(sfd_handle* h, int p) {
 void invalidate_graph(sfd_handle* h) {
   for (int p = 0; p < 2; ++p)
     if (h->graph[p]) { cudaGraphExecDestroy(h->graph[p]); h->graph[p] = nullptr; }
+  if (h->adj_graph) { cudaGraphExecDestroy(h->adj_graph); h->adj_graph = nullptr; }
 }
 
 // Host rows of NX floats -> device rows of pitch P.
@@ -1970,21 +1977,21 @@ size_t adj_slots(const sfd_handle* h, int seg) {
 
 // One seismic2 segment: the forward states recomputed by the handle's own
 // steps into the slots, then the adjoint steps over them, last step first.
-int s2_adjoint_segment(sfd_handle* h, int64_t nsteps) {
-  const int64_t s0 = h->step;
-  const S2AdjLayout A = s2_adj_layout(h, h->adj_seg);
+// The work of one seismic2 segment after its slot 0 is filled and the
+// control block's base set to the segment's first step: the forward
+// recompute, slot s -> slot s + 1 (no receivers), then the adjoint steps,
+// last first, starting from adjoint state `cur`.  Every address it names is
+// the handle's or its adjoint workspace's and every step index is relative
+// to the control block's base, so a capture of it replays for any segment of
+// the same length.
+cudaError_t s2_segment_work(sfd_handle* h, const S2AdjLayout& A, int64_t nsteps, int cur, cudaStream_t stream) {
   const Layout& L = h->L;
   char* slots = h->adj + A.slots;
-  int r = s2_save_state(h, A, slots);
-  if (r) return r;
-  // forward recompute, slot s -> slot s + 1, no receivers; the kernels read
-  // the step index from the control block (base = s0)
-  k_begin<<<std::min(1024, (L.nslots + 255) / 256 + 1), 256, 0, h->stream>>>((Ctl*)(h->base + L.off_ctl),
-                                                                            (float*)(h->base + L.off_slots), L.nslots, (int)s0);
+  cudaError_t e = cudaSuccess;
   if (h->single) {  // the single-pass step kernel between slots; its in-place memory variables copied ahead
     Seis2Step st = h->s2s[0];
     st.io.nrec = 0;
-    for (int64_t s = 0; s < nsteps; ++s) {
+    for (int64_t s = 0; s < nsteps && e == cudaSuccess; ++s) {
       const S2State a0 = s2_state_at(A, slots + A.state * (size_t)s);
       const S2State a1 = s2_state_at(A, slots + A.state * (size_t)(s + 1));
       st.vx0 = a0.vx; st.vz0 = a0.vz; st.sxx0 = a0.sxx; st.szz0 = a0.szz; st.sxz0 = a0.sxz;
@@ -1993,48 +2000,87 @@ int s2_adjoint_segment(sfd_handle* h, int64_t nsteps) {
       st.m_vxx1 = a1.m[0]; st.m_vzz1 = a1.m[1]; st.m_vxz1 = a1.m[2]; st.m_vzx1 = a1.m[3];
       st.m2_vxx0 = a0.m[8]; st.m2_vzz0 = a0.m[9]; st.m2_vxz0 = a0.m[10]; st.m2_vzx0 = a0.m[11];
       st.m2_vxx1 = a1.m[8]; st.m2_vzz1 = a1.m[9]; st.m2_vxz1 = a1.m[10]; st.m2_vzx1 = a1.m[11];
-      CK(cudaMemcpyAsync(a1.m[4], a0.m[4], A.mem[8] - A.mem[4], cudaMemcpyDeviceToDevice, h->stream));
+      e = cudaMemcpyAsync(a1.m[4], a0.m[4], A.mem[8] - A.mem[4], cudaMemcpyDeviceToDevice, stream);
       st.m_sxx_x = a1.m[4]; st.m_szz_z = a1.m[5]; st.m_sxz_x = a1.m[6]; st.m_sxz_z = a1.m[7];
-      seis2_step(st, h->launch1, h->zb, (int)s, h->stream);
+      seis2_step(st, h->launch1, h->zb, (int)s, stream);
     }
   } else {  // the two half-step kernels in place on a copy of the previous slot
     Seis2Args ar = h->s2;
     ar.io.nrec = 0;
-    for (int64_t s = 0; s < nsteps; ++s) {
+    for (int64_t s = 0; s < nsteps && e == cudaSuccess; ++s) {
       char* dst = slots + A.state * (size_t)(s + 1);
-      CK(cudaMemcpyAsync(dst, slots + A.state * (size_t)s, A.state, cudaMemcpyDeviceToDevice, h->stream));
+      e = cudaMemcpyAsync(dst, slots + A.state * (size_t)s, A.state, cudaMemcpyDeviceToDevice, stream);
       const S2State a1 = s2_state_at(A, dst);
       ar.vx = a1.vx; ar.vz = a1.vz; ar.sxx = a1.sxx; ar.szz = a1.szz; ar.sxz = a1.sxz;
       ar.m_vxx = a1.m[0]; ar.m_vzz = a1.m[1]; ar.m_vxz = a1.m[2]; ar.m_vzx = a1.m[3];
       ar.m_sxx_x = a1.m[4]; ar.m_szz_z = a1.m[5]; ar.m_sxz_x = a1.m[6]; ar.m_sxz_z = a1.m[7];
       ar.m2_vxx = a1.m[8]; ar.m2_vzz = a1.m[9]; ar.m2_vxz = a1.m[10]; ar.m2_vzx = a1.m[11];
-      seis2_half1(ar, h->launch, (int)s, h->stream);
-      seis2_half2(ar, h->launch, (int)s, h->stream);
+      seis2_half1(ar, h->launch, (int)s, stream);
+      seis2_half2(ar, h->launch, (int)s, stream);
     }
   }
-  const Seis2Args& e = h->s2;
+  if (e != cudaSuccess) return e;
+  const Seis2Args& c = h->s2;
   S2Adj a;
   a.NX = h->cfg.nx; a.NZ = h->cfg.nz; a.P = L.P; a.W = L.W;
   const float** co[12] = {&a.A11, &a.A13, &a.A15, &a.A33, &a.A35, &a.B15, &a.B35, &a.B55, &a.dtrx, &a.dtrz, &a.gxp, &a.gzp};
-  const float* src_co[12] = {e.A11, e.A13, e.A15, e.A33, e.A35, e.B15, e.B35, e.B55, e.dtrx, e.dtrz, e.gxp, e.gzp};
+  const float* src_co[12] = {c.A11, c.A13, c.A15, c.A33, c.A35, c.B15, c.B35, c.B55, c.dtrx, c.dtrz, c.gxp, c.gzp};
   for (int q = 0; q < 12; ++q) *co[q] = src_co[q];
-  a.X = e.X; a.Z = e.Z;
+  a.X = c.X; a.Z = c.Z;
   for (int q = 0; q < 12; ++q) a.tmp[q] = (float*)(h->adj + A.tmp + q * A.field);
   float** g[12] = {&a.gA11, &a.gA13, &a.gA15, &a.gA33, &a.gA35, &a.gB15, &a.gB35, &a.gB55, &a.gdtrx, &a.gdtrz, &a.ggxp, &a.ggzp};
   for (int q = 0; q < 12; ++q) *g[q] = (float*)(h->adj + A.g + q * A.field);
   a.srcacc = (float*)(h->adj + A.acc);
   a.srcfn = (const float*)(h->base + L.off_src);
-  a.nstep = h->cfg.nstep; a.si = h->have_force_src ? e.io.si : -1; a.sk = e.io.sk;
+  a.nstep = h->cfg.nstep; a.si = h->have_force_src ? c.io.si : -1; a.sk = c.io.sk;
   a.rec = (const int*)(h->base + L.off_rec); a.nrec = h->cfg.nrec; a.resid = h->adj_resid;
+  a.ctl = (const Ctl*)(h->base + L.off_ctl);
   for (int64_t s = nsteps - 1; s >= 0; --s) {
     const S2State S = s2_state_at(A, slots + A.state * (size_t)s);
     const S2State S1 = s2_state_at(A, slots + A.state * (size_t)(s + 1));
-    const S2State Ln = s2_state_at(A, h->adj + A.lam[h->adj_cur]);
-    const S2State Lc = s2_state_at(A, h->adj + A.lam[1 - h->adj_cur]);
-    s2_adj_step(a, S, S1, Ln, Lc, (int)(s0 + s), h->stream);
-    h->adj_cur ^= 1;
+    const S2State Ln = s2_state_at(A, h->adj + A.lam[cur]);
+    const S2State Lc = s2_state_at(A, h->adj + A.lam[1 - cur]);
+    s2_adj_step(a, S, S1, Ln, Lc, (int)s, stream);
+    cur ^= 1;
   }
-  CK(cudaGetLastError());
+  return cudaGetLastError();
+}
+
+// One seismic2 segment: slot 0 <- the handle's state, the step base, then
+// the segment's work, replayed from a CUDA graph captured on the handle's
+// private stream when it has one (one capture per segment length and
+// starting adjoint state; the graph is dropped with the handle's others).
+int s2_adjoint_segment(sfd_handle* h, int64_t nsteps) {
+  const int64_t s0 = h->step;
+  const S2AdjLayout A = s2_adj_layout(h, h->adj_seg);
+  const Layout& L = h->L;
+  int r = s2_save_state(h, A, h->adj + A.slots);
+  if (r) return r;
+  k_begin<<<std::min(1024, (L.nslots + 255) / 256 + 1), 256, 0, h->stream>>>((Ctl*)(h->base + L.off_ctl),
+                                                                            (float*)(h->base + L.off_slots), L.nslots, (int)s0);
+  if (!h->cap_stream) {
+    CK(s2_segment_work(h, A, nsteps, h->adj_cur, h->stream));
+  } else {
+    const bool reuse = h->adj_graph && h->adj_graph_n == nsteps && h->adj_graph_cur == h->adj_cur &&
+                       h->adj_graph_work == h->adj && h->adj_graph_resid == h->adj_resid &&
+                       h->adj_graph_seg == h->adj_seg;
+    if (!reuse) {
+      if (h->adj_graph) { cudaGraphExecDestroy(h->adj_graph); h->adj_graph = nullptr; }
+      cudaGraph_t g = nullptr;
+      CK(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
+      const cudaError_t ew = s2_segment_work(h, A, nsteps, h->adj_cur, h->cap_stream);
+      const cudaError_t ec = cudaStreamEndCapture(h->cap_stream, &g);
+      if (ew != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(ew, "seismic2 adjoint segment"); }
+      if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture");
+      const cudaError_t ei = cudaGraphInstantiate(&h->adj_graph, g, 0);
+      cudaGraphDestroy(g);
+      if (ei != cudaSuccess) { h->adj_graph = nullptr; return cuda_fail(ei, "cudaGraphInstantiate"); }
+      h->adj_graph_n = nsteps; h->adj_graph_cur = h->adj_cur; h->adj_graph_work = h->adj;
+      h->adj_graph_resid = h->adj_resid; h->adj_graph_seg = h->adj_seg;
+    }
+    CK(cudaGraphLaunch(h->adj_graph, h->stream));
+  }
+  h->adj_cur ^= (int)(nsteps & 1);
   return SFD_OK;
 }
 
