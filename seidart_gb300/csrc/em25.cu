@@ -42,9 +42,12 @@ constexpr int RING = 4;              // staged planes per block
 constexpr int HALO3 = 3 * VH * VW;   // three fields with the halo
 constexpr int OWN3 = 3 * BZ * BX;    // three fields of the own cells
 constexpr int OWN = 736;             // own cells after the halo, 128-byte aligned
-constexpr int STAGE = OWN + OWN3;    // 4480 bytes
+constexpr int PSI = OWN + OWN3;      // the two y-strip memory variables of the kernel
+constexpr int YTB = PSI + 2 * BZ * BX;  // the y table around the plane: 6 rows x 4 entries from j & ~3
+constexpr int STAGE = YTB + 32;      // 5632 bytes
 constexpr int FH = VH * VW;          // one field of a halo tile
-static_assert(OWN >= HALO3 && (OWN * 4) % 128 == 0 && (STAGE * 4) % 128 == 0, "stage alignment");
+static_assert(OWN >= HALO3 && (OWN * 4) % 128 == 0 && (PSI * 4) % 128 == 0 && (YTB * 4) % 128 == 0 &&
+                  (STAGE * 4) % 128 == 0, "stage alignment");
 
 __device__ void em25_wait_failed(const Em25Args& a, uint64_t* full, int n, int np) {
   atomicExch(const_cast<int*>(&a.io.ctl->err), 1);
@@ -77,10 +80,14 @@ __global__ void __launch_bounds__(BX * BZ) em25_h_tma_kernel(const __grid_consta
     float* st = stage + (n % RING) * STAGE;
     uint64_t* bar = full + n % RING;
     const int j = j0 + n;
-    const bool own = j < j1;
-    tma::bar_arrive_expect(bar, (own ? (HALO3 + OWN3) * 4u : HALO3 * 4u) + a.stall_tx);
-    tma::load_4d(st, &a.tm_halo, bar, i0 - HX, j, k0 - 1, 0);       // Ex Ey Ez
-    if (own) tma::load_4d(st + OWN, &a.tm_own, bar, i0, j, k0, 3);  // Hx Hy Hz
+    const bool own = j < j1, ys = own && in_strip(j, NY, W);
+    tma::bar_arrive_expect(bar, (HALO3 + (own ? OWN3 + 24 : 0) + (ys ? 2 * BZ * BX : 0)) * 4u + a.stall_tx);
+    tma::load_4d(st, &a.tm_halo, bar, i0 - HX, j, k0 - 1, 0);  // Ex Ey Ez
+    if (own) {
+      tma::load_4d(st + OWN, &a.tm_own, bar, i0, j, k0, 3);  // Hx Hy Hz
+      tma::load_2d(st + YTB, &a.tm_ytab, bar, j & ~3, 0);
+    }
+    if (ys) tma::load_4d(st + PSI, &a.tm_ypsi_e, bar, i0, strip_idx(j, NY, W), k0, 0);  // dEz_dy dEx_dy
   };
   if (tid == 0)
     for (int n = 0; n < min(RING, np); ++n) issue(n);
@@ -123,13 +130,14 @@ __global__ void __launch_bounds__(BX * BZ) em25_h_tma_kernel(const __grid_consta
       const size_t mx = ((size_t)k * NY + j) * (2 * W) + xsi;
       const size_t my = ((size_t)k * (2 * W) + (ys ? strip_idx(j, NY, W) : 0)) * P + i;
       const size_t mz = ((size_t)zsi * NY + j) * P + i;
-      const float iky = a.Y.ik[j], ady = a.Y.ad[j], by = a.Y.b[j];
-      const float ikyh = a.Y.ikh[j], adyh = a.Y.adh[j], byh = a.Y.bh[j];
+      const float* yt = E + YTB + (j & 3);  // rows ik ad b ikh adh bh of the y table
+      const float iky = yt[0], ady = yt[4], by = yt[8], ikyh = yt[12], adyh = yt[16], byh = yt[20];
+      const float* Y = E + PSI;             // dEz_dy, dEx_dy of this plane (y strips)
       const float ex = E[hc], ey = E[FH + hc], ez = E[2 * FH + hc];
       {  // Hx, :904-917
         const float d1 = ez - En[2 * FH + hc];  // dEz/dy
         float v1 = d1 * ikyh;
-        if (ys) { const float m = byh * mEz_y_[my] + adyh * d1; mEz_y_[my] = m; v1 += m; }
+        if (ys) { const float m = byh * Y[oc] + adyh * d1; mEz_y_[my] = m; v1 += m; }
         const float d2 = E[FH + hc + VW] - ey;  // dEy/dz
         float v2 = d2 * ikzh;
         if (zs) { const float m = bzh * mEy_z_[mz] + adzh * d2; mEy_z_[mz] = m; v2 += m; }
@@ -149,7 +157,7 @@ __global__ void __launch_bounds__(BX * BZ) em25_h_tma_kernel(const __grid_consta
       if (hz_rows) {  // Hz, :946-960 (k >= 1)
         const float d1 = En[hc] - ex;  // dEx/dy
         float v1 = d1 * iky;
-        if (ys) { const float m = by * mEx_y_[my] + ady * d1; mEx_y_[my] = m; v1 += m; }
+        if (ys) { const float m = by * Y[BZ * BX + oc] + ady * d1; mEx_y_[my] = m; v1 += m; }
         const float d2 = ey - E[FH + hc + 1];  // dEy/dx
         float v2 = d2 * ikx;
         if (xs) { const float m = bx * mEy_x_[mx] + adx * d2; mEy_x_[mx] = m; v2 += m; }
@@ -193,9 +201,12 @@ __global__ void __launch_bounds__(BX * BZ) em25_e_tma_kernel(const __grid_consta
     float* st = stage + (n % RING) * STAGE;
     uint64_t* bar = full + n % RING;
     const int j = j0 + n;
-    tma::bar_arrive_expect(bar, (HALO3 + OWN3) * 4u + a.stall_tx);
+    const bool ys = in_strip(j, NY, W);
+    tma::bar_arrive_expect(bar, (HALO3 + OWN3 + 24 + (ys ? 2 * BZ * BX : 0)) * 4u + a.stall_tx);
     tma::load_4d(st, &a.tm_halo, bar, i0 - HX, j, k0 - 1, 3);  // Hx Hy Hz
     tma::load_4d(st + OWN, &a.tm_own, bar, i0, j, k0, 0);     // Ex Ey Ez
+    tma::load_2d(st + YTB, &a.tm_ytab, bar, j & ~3, 0);
+    if (ys) tma::load_4d(st + PSI, &a.tm_ypsi_h, bar, i0, strip_idx(j, NY, W), k0, 0);  // dHz_dy dHx_dy
   };
   if (tid == 0)
     for (int n = 0; n < min(RING, np); ++n) issue(n);
@@ -250,13 +261,15 @@ __global__ void __launch_bounds__(BX * BZ) em25_e_tma_kernel(const __grid_consta
       const size_t mx = ((size_t)k * NY + j) * (2 * W) + xsi;
       const size_t my = ((size_t)k * (2 * W) + (ys ? strip_idx(j, NY, W) : 0)) * P + i;
       const size_t mz = ((size_t)zsi * NY + j) * P + i;
-      const float ikyh = a.Y.ikh[j], adyh = a.Y.adh[j], byh = a.Y.bh[j];
+      const float* yt = H + YTB + (j & 3);  // rows ik ad b ikh adh bh of the y table
+      const float ikyh = yt[12], adyh = yt[16], byh = yt[20];
+      const float* Y = H + PSI;             // dHz_dy, dHx_dy of this plane (y strips)
       const float hx = H[hc], hy = H[FH + hc], hz = H[2 * FH + hc];
       float ex = E[oc], ey = E[OWN3 / 3 + oc], ez = E[2 * (OWN3 / 3) + oc];
       if (XEx && j >= 1 && j <= NY - 2) {  // :971-984
         const float d1 = hz - phz;  // dHz/dy
         float v1 = d1 * ikyh;
-        if (ys) { const float m = byh * mHz_y_[my] + adyh * d1; mHz_y_[my] = m; v1 += m; }
+        if (ys) { const float m = byh * Y[oc] + adyh * d1; mHz_y_[my] = m; v1 += m; }
         const float d2 = H[FH + hc - VW] - hy;  // dHy/dz
         float v2 = d2 * ikz;
         if (zs) { const float m = bz * mHy_z_[mz] + adz * d2; mHy_z_[mz] = m; v2 += m; }
@@ -274,7 +287,7 @@ __global__ void __launch_bounds__(BX * BZ) em25_e_tma_kernel(const __grid_consta
       if (XEz && j >= 1 && j <= NY - 2) {  // :1015-1029
         const float d1 = phx - hx;  // dHx/dy
         float v1 = d1 * ikyh;
-        if (ys) { const float m = byh * mHx_y_[my] + adyh * d1; mHx_y_[my] = m; v1 += m; }
+        if (ys) { const float m = byh * Y[BZ * BX + oc] + adyh * d1; mHx_y_[my] = m; v1 += m; }
         const float d2 = hy - H[FH + hc - 1];  // dHy/dx
         float v2 = d2 * ikxh;
         if (xs) { const float m = bxh * mHy_x_[mx] + adxh * d2; mHy_x_[mx] = m; v2 += m; }
@@ -347,9 +360,24 @@ void em25_half2(const Em25Args& a, const Launch& L, int rel, cudaStream_t s) {
   em25_e_tma_kernel<<<L.grid, L.block, RING * STAGE * sizeof(float), s>>>(a, rel);
 }
 
-bool em25_make_maps(Em25Args& a, size_t field_stride) {
-  return encode_field_map(&a.tm_halo, a.Ex, a.NX, a.NY, a.NZ, a.P, field_stride, 6, VW, VH, 3) &&
-         encode_field_map(&a.tm_own, a.Ex, a.NX, a.NY, a.NZ, a.P, field_stride, 6, BX, BZ, 3);
+bool em25_make_maps(Em25Args& a, size_t field_stride, const float* ytab) {
+  if (!(encode_field_map(&a.tm_halo, a.Ex, a.NX, a.NY, a.NZ, a.P, field_stride, 6, VW, VH, 3) &&
+        encode_field_map(&a.tm_own, a.Ex, a.NX, a.NY, a.NZ, a.P, field_stride, 6, BX, BZ, 3)))
+    return false;
+  // the y-strip memory variables (layout [k][2W][P]) each kernel reads: two arrays
+  auto ypsi = [&](CUtensorMap* m, float* m0, float* m1) {
+    const size_t d = (size_t)((char*)m1 - (char*)m0);
+    if (d % 16) return false;
+    const cuuint64_t dims[4] = {(cuuint64_t)a.NX, (cuuint64_t)(2 * a.W), (cuuint64_t)a.NZ, 2};
+    const cuuint64_t strides[3] = {(cuuint64_t)a.P * 4, (cuuint64_t)2 * a.W * a.P * 4, (cuuint64_t)d};
+    const cuuint32_t box[4] = {BX, 1, BZ, 2};
+    return encode_tiled(m, m0, 4, dims, strides, box);
+  };
+  if (!ypsi(&a.tm_ypsi_e, a.mEz_y, a.mEx_y) || !ypsi(&a.tm_ypsi_h, a.mHz_y, a.mHx_y)) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)axis_stride(a.NY), 6};
+  const cuuint64_t strides[1] = {(cuuint64_t)axis_stride(a.NY) * 4};
+  const cuuint32_t box[2] = {4, 6};
+  return encode_tiled(&a.tm_ytab, (void*)ytab, 2, dims, strides, box);
 }
 
 void em25_finalize(const Em25Args& a, int t_last, cudaStream_t s) {

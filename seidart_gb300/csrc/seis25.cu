@@ -65,12 +65,21 @@ constexpr int HALO3 = 3 * VH * VW;     // velocities with the halo
 constexpr int HALO6 = 6 * VH * VW;     // stresses with the halo
 constexpr int OWN3 = 3 * BZ * BX;
 constexpr int OWN6 = 6 * BZ * BX;
-constexpr int S_OWN = 736;             // stress stage: own stresses after the velocity halo, 128-byte aligned
-constexpr int S_STAGE = S_OWN + OWN6;  // 6016 bytes
-constexpr int V_OWN = HALO6;           // velocity stage: own velocities after the stress halo
-constexpr int V_STAGE = V_OWN + OWN3;  // 7296 bytes
-static_assert(S_OWN >= HALO3 && (S_OWN * 4) % 128 == 0 && (S_STAGE * 4) % 128 == 0, "stage alignment");
-static_assert((V_OWN * 4) % 128 == 0 && (V_STAGE * 4) % 128 == 0, "stage alignment");
+constexpr int YT = 24;                 // the y table around the plane: 6 rows x 4 entries from j & ~3
+// stress stage: velocities with the halo, own stresses, y-strip memory variables, y table
+constexpr int S_OWN = 736;             // 128-byte aligned after the halo
+constexpr int S_PSI = S_OWN + OWN6;
+constexpr int S_YT = S_PSI + OWN3;
+constexpr int S_STAGE = S_YT + 32;     // 7680 bytes
+// velocity stage: stresses with the halo, own velocities, y-strip memory variables, y table
+constexpr int V_OWN = HALO6;
+constexpr int V_PSI = V_OWN + OWN3;
+constexpr int V_YT = V_PSI + OWN3;
+constexpr int V_STAGE = V_YT + 32;     // 8960 bytes
+static_assert(S_OWN >= HALO3 && (S_OWN * 4) % 128 == 0 && (S_PSI * 4) % 128 == 0 && (S_YT * 4) % 128 == 0 &&
+                  (S_STAGE * 4) % 128 == 0, "stage alignment");
+static_assert((V_OWN * 4) % 128 == 0 && (V_PSI * 4) % 128 == 0 && (V_YT * 4) % 128 == 0 && (V_STAGE * 4) % 128 == 0,
+              "stage alignment");
 
 // Records a wait that ran out and lets the copies this block already issued
 // land (each again within the limit) before its shared memory is released.
@@ -107,10 +116,14 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS)
     float* st = stage + (n % RING) * S_STAGE;
     uint64_t* bar = full + n % RING;
     const int j = j0 + n;
-    const bool own = j < j1;
-    tma::bar_arrive_expect(bar, (own ? (HALO3 + OWN6) * 4u : HALO3 * 4u) + a.stall_tx);
+    const bool own = j < j1, ys = own && in_strip(j, NY, W);
+    tma::bar_arrive_expect(bar, (HALO3 + (own ? OWN6 + YT : 0) + (ys ? OWN3 : 0)) * 4u + a.stall_tx);
     tma::load_4d(st, &a.tm_vhalo, bar, i0 - HX, j, k0 - 1, 0);
-    if (own) tma::load_4d(st + S_OWN, &a.tm_sown, bar, i0, j, k0, 3);
+    if (own) {
+      tma::load_4d(st + S_OWN, &a.tm_sown, bar, i0, j, k0, 3);
+      tma::load_2d(st + S_YT, &a.tm_ytab, bar, j & ~3, 0);
+    }
+    if (ys) tma::load_4d(st + S_PSI, &a.tm_ypsi_v, bar, i0, strip_idx(j, NY, W), k0, 0);
   };
   if (tid == 0)
     for (int n = 0; n < min(RING, np); ++n) issue(n);
@@ -187,11 +200,11 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS)
       const size_t mz = ((size_t)zsi * NY + j) * P + i;
       float mvxx = 0, mvyx = 0, mvzx = 0, mvxy = 0, mvyy = 0, mvzy = 0, mvxz = 0, mvyz = 0, mvzz = 0;
       if (xs) { mvxx = MVXX[mx]; mvyx = MVYX[mx]; mvzx = MVZX[mx]; }
-      if (ys) { mvxy = MVXY[my]; mvyy = MVYY[my]; mvzy = MVZY[my]; }
+      if (ys) { const float* Y = V + S_PSI; mvxy = Y[oc]; mvyy = Y[OWN3 / 3 + oc]; mvzy = Y[2 * (OWN3 / 3) + oc]; }
       if (zs) { mvxz = MVXZ[mz]; mvyz = MVYZ[mz]; mvzz = MVZZ[mz]; }
       const bool l1 = L1 && j >= 1, l2 = L2 && j <= NY - 2, l3 = L3 && j >= 1, l4 = L4 && j <= NY - 2;
-      const float iky = a.Y.ik[j], ikyh = a.Y.ikh[j], ady = a.Y.ad[j], adyh = a.Y.adh[j];
-      const float by = a.Y.b[j], byh = a.Y.bh[j];
+      const float* yt = V + S_YT + (j & 3);  // rows ik ad b ikh adh bh of the y table
+      const float iky = yt[0], ady = yt[4], by = yt[8], ikyh = yt[12], adyh = yt[16], byh = yt[20];
       if (l1) {  // sigmaxx, sigmayy, sigmazz: x+, y-, z- differences (:616-678)
         const float dxx = xpx - cvx, dyx = xpy - cvy, dzx = xpz - cvz;
         const float dyy = cvy - pvy, dxy = cvx - pvx, dzy = cvz - pvz;
@@ -302,10 +315,14 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_VELOCITY_BLOCKS)
     float* st = stage + (n % RING) * V_STAGE;
     uint64_t* bar = full + n % RING;
     const int j = j0 + n;
-    const bool own = j < j1;
-    tma::bar_arrive_expect(bar, (own ? (HALO6 + OWN3) * 4u : HALO6 * 4u) + a.stall_tx);
+    const bool own = j < j1, ys = own && in_strip(j, NY, W);
+    tma::bar_arrive_expect(bar, (HALO6 + (own ? OWN3 + YT : 0) + (ys ? OWN3 : 0)) * 4u + a.stall_tx);
     tma::load_4d(st, &a.tm_shalo, bar, i0 - HX, j, k0 - 1, 3);
-    if (own) tma::load_4d(st + V_OWN, &a.tm_vown, bar, i0, j, k0, 0);
+    if (own) {
+      tma::load_4d(st + V_OWN, &a.tm_vown, bar, i0, j, k0, 0);
+      tma::load_2d(st + V_YT, &a.tm_ytab, bar, j & ~3, 0);
+    }
+    if (ys) tma::load_4d(st + V_PSI, &a.tm_ypsi_s, bar, i0, strip_idx(j, NY, W), k0, 0);
   };
   if (tid == 0)
     for (int n = 0; n < min(RING, np); ++n) issue(n);
@@ -363,8 +380,8 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_VELOCITY_BLOCKS)
       const size_t mx = ((size_t)k * NY + j) * (2 * W) + xsi;
       const size_t my = ((size_t)k * (2 * W) + (ys ? strip_idx(j, NY, W) : 0)) * P + i;
       const size_t mz = ((size_t)zsi * NY + j) * P + i;
-      const float iky = a.Y.ik[j], ikyh = a.Y.ikh[j], ady = a.Y.ad[j], adyh = a.Y.adh[j];
-      const float by = a.Y.b[j], byh = a.Y.bh[j];
+      const float* yt = S + V_YT + (j & 3);  // rows ik ad b ikh adh bh of the y table
+      const float iky = yt[0], ady = yt[4], by = yt[8], ikyh = yt[12], adyh = yt[16], byh = yt[20];
       float vx = V[oc], vy = V[OWN3 / 3 + oc], vz = V[2 * (OWN3 / 3) + oc];
       const bool ux = Vx && j >= 1, uy = Vy && j <= NY - 2, uz = Vz && j >= 1;
       float m1x = 0.f, m1y = 0.f, m1z = 0.f, m2x = 0.f, m2y = 0.f, m2z = 0.f, m3x = 0.f, m3y = 0.f, m3z = 0.f;
@@ -373,10 +390,11 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_VELOCITY_BLOCKS)
         if (uy) m2x = MSXYX[mx];
         if (uz) m3x = MSXZX[mx];
       }
-      if (ys) {
-        if (ux) m1y = MSXYY[my];
-        if (uy) m2y = MSYYY[my];
-        if (uz) m3y = MSYZY[my];
+      if (ys) {  // staged: syy_y sxy_y syz_y
+        const float* Y = S + V_PSI;
+        m2y = Y[oc];
+        m1y = Y[OWN3 / 3 + oc];
+        m3y = Y[2 * (OWN3 / 3) + oc];
       }
       if (zs) {
         if (ux) m1z = MSXZZ[mz];
@@ -455,12 +473,29 @@ void seis25_half2(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s)
   seis25_velocity_tma_kernel<<<L.grid, L.block, RING * V_STAGE * sizeof(float), s>>>(a, rel);
 }
 
-bool seis25_make_maps(Seis25Args& a, size_t field_stride) {
+bool seis25_make_maps(Seis25Args& a, size_t field_stride, const float* ytab) {
   auto make = [&](CUtensorMap* m, int bx, int bz, int nf) {
     return encode_field_map(m, a.vx, a.NX, a.NY, a.NZ, a.P, field_stride, 9, bx, bz, nf);
   };
-  return make(&a.tm_vhalo, VW, VH, 3) && make(&a.tm_sown, BX, BZ, 6) && make(&a.tm_shalo, VW, VH, 6) &&
-         make(&a.tm_vown, BX, BZ, 3);
+  if (!(make(&a.tm_vhalo, VW, VH, 3) && make(&a.tm_sown, BX, BZ, 6) && make(&a.tm_shalo, VW, VH, 6) &&
+        make(&a.tm_vown, BX, BZ, 3)))
+    return false;
+  // y-strip memory variables (layout [k][2W][P]): three equally spaced arrays per kernel
+  auto ypsi = [&](CUtensorMap* m, float* m0, float* m1, float* m2) {
+    const size_t d = (size_t)((char*)m1 - (char*)m0);
+    if ((size_t)((char*)m2 - (char*)m1) != d || d % 16) return false;
+    const cuuint64_t dims[4] = {(cuuint64_t)a.NX, (cuuint64_t)(2 * a.W), (cuuint64_t)a.NZ, 3};
+    const cuuint64_t strides[3] = {(cuuint64_t)a.P * 4, (cuuint64_t)2 * a.W * a.P * 4, (cuuint64_t)d};
+    const cuuint32_t box[4] = {BX, 1, BZ, 3};
+    return encode_tiled(m, m0, 4, dims, strides, box);
+  };
+  if (!ypsi(&a.tm_ypsi_v, a.m_vx_y, a.m_vy_y, a.m_vz_y) || !ypsi(&a.tm_ypsi_s, a.m_syy_y, a.m_sxy_y, a.m_syz_y))
+    return false;
+  // the y table: 6 rows (ik ad b ikh adh bh) of axis_stride(NY) floats
+  const cuuint64_t dims[2] = {(cuuint64_t)axis_stride(a.NY), 6};
+  const cuuint64_t strides[1] = {(cuuint64_t)axis_stride(a.NY) * 4};
+  const cuuint32_t box[2] = {4, 6};
+  return encode_tiled(&a.tm_ytab, (void*)ytab, 2, dims, strides, box);
 }
 
 void seis25_finalize(const Seis25Args& a, int t_last, cudaStream_t s) {

@@ -497,7 +497,7 @@ bool bind_args(sfd_handle* h) {
       a.io = io;
       a.wait_ns = h->wait_ns;
       a.stall_tx = h->stall_waits ? 16u : 0u;
-      if (!seis25_make_maps(a, L.fsz)) return false;
+      if (!seis25_make_maps(a, L.fsz, h->axis(1))) return false;
       h->launch = seis25_launch(a);
       break;
     }
@@ -516,7 +516,7 @@ bool bind_args(sfd_handle* h) {
       a.io = io;
       a.wait_ns = h->wait_ns;
       a.stall_tx = h->stall_waits ? 16u : 0u;
-      if (!em25_make_maps(a, L.fsz)) return false;
+      if (!em25_make_maps(a, L.fsz, h->axis(1))) return false;
       h->launch = em25_launch(a);
       break;
     }

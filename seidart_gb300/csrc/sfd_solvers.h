@@ -101,6 +101,9 @@ struct Seis25Args {
   // cells (stress kernel), stresses with a halo and the velocities of the own
   // cells (velocity kernel)
   CUtensorMap tm_vhalo, tm_sown, tm_shalo, tm_vown;
+  // the y-strip memory variables of each kernel (three arrays, equally
+  // spaced) and the y axis table, staged with the planes
+  CUtensorMap tm_ypsi_v, tm_ypsi_s, tm_ytab;
   unsigned long long wait_ns;  // bound of each wait for a staged tile
   unsigned stall_tx;           // test aid: extra bytes each stage expects (0; > 0 makes the waits run out)
 };
@@ -118,6 +121,9 @@ struct Em25Args {
   // TMA descriptors of the six fields as one (NX, NY, NZ, 6) FP32 tensor
   // (em25_make_maps): three fields with a halo, three of the own cells
   CUtensorMap tm_halo, tm_own;
+  // the y-strip memory variables each kernel reads (dEz_dy dEx_dy; dHz_dy
+  // dHx_dy) and the y axis table, staged with the planes
+  CUtensorMap tm_ypsi_e, tm_ypsi_h, tm_ytab;
   unsigned long long wait_ns;  // bound of each wait for a staged tile
   unsigned stall_tx;           // test aid: extra bytes each stage expects (0; > 0 makes the waits run out)
 };
@@ -196,7 +202,7 @@ void seis2_finalize(const Seis2Args& a, int t_last, cudaStream_t s);
 
 // Encodes a's four tensor maps over its field array (fields contiguous,
 // `field_stride` floats apart); false when the driver refuses one.
-bool seis25_make_maps(Seis25Args& a, size_t field_stride);
+bool seis25_make_maps(Seis25Args& a, size_t field_stride, const float* ytab);
 Launch seis25_launch(const Seis25Args& a);
 void seis25_half1(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s);
 void seis25_half2(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s);
@@ -207,7 +213,10 @@ void seis25_finalize(const Seis25Args& a, int t_last, cudaStream_t s);
 // apart) with boxes of box_x x 1 x box_z x box_f (tma_maps.cu).
 bool encode_field_map(CUtensorMap* map, void* base, int NX, int NY, int NZ, int P, size_t field_stride, int nfields,
                       int box_x, int box_z, int box_f);
-bool em25_make_maps(Em25Args& a, size_t field_stride);
+// Any FP32 tiled map: rank dims (innermost first), rank - 1 byte strides.
+bool encode_tiled(CUtensorMap* map, void* base, int rank, const cuuint64_t* dims, const cuuint64_t* strides,
+                  const cuuint32_t* box);
+bool em25_make_maps(Em25Args& a, size_t field_stride, const float* ytab);
 Launch em25_launch(const Em25Args& a);
 void em25_half1(const Em25Args& a, const Launch& L, int rel, cudaStream_t s);
 void em25_half2(const Em25Args& a, const Launch& L, int rel, cudaStream_t s);
