@@ -57,6 +57,7 @@ constexpr int BX = 32, BZ = 4;
 #define SEIS25_VELOCITY_BLOCKS 6
 #endif
 
+constexpr int CSTRIDE = 44;            // floats per thread of the stiffness table: 11 float4 slots (odd: no bank conflicts)
 constexpr int HX = 4;                  // x halo of the staged tiles (16 bytes)
 constexpr int VW = BX + 2 * HX;        // 40 floats per staged row
 constexpr int VH = BZ + 2;             // rows k0 - 1 .. k0 + BZ
@@ -93,7 +94,7 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS)
     seis25_stress_tma_kernel(const __grid_constant__ Seis25Args a, int rel) {
   extern __shared__ __align__(128) float stage[];
   __shared__ __align__(8) uint64_t full[RING];
-  __shared__ float sC[33 * BX * BZ];
+  __shared__ __align__(16) float sC[CSTRIDE * BX * BZ];
   const Ctl* ctl = a.io.ctl;
   const int t = ctl->base + rel;
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && t > ctl->run_start) {
@@ -136,20 +137,33 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS)
   const bool L4 = inside && (k <= NZ - 2) && (i <= NX - 2);
   const bool active = L1 || L2 || L3 || L4;
   const int ic = inside ? i : 0, kc = inside ? k : 0;
+  // the column's 33 stiffness averages, each thread's in its own row of
+  // CSTRIDE floats: a loop's coefficients start on a 16-byte boundary and
+  // are read back four at a time (slots 0-14 loop 1, 16-21 loop 2, 24-29
+  // loop 3, 32-37 loop 4)
+  float* const cs = sC + tid * CSTRIDE;
   {
     const size_t cpl = (size_t)NZ * P, cpc = (size_t)kc * P + ic;
     auto cf = [&](int q, bool on) { return on ? __ldg(a.C + q * cpl + cpc) : 0.0f; };
 #pragma unroll
-    for (int q = 0; q < 15; ++q) sC[q * BX * BZ + tid] = cf(q, L1);
+    for (int q = 0; q < 15; ++q) cs[q] = cf(q, L1);
 #pragma unroll
-    for (int q = 15; q < 21; ++q) sC[q * BX * BZ + tid] = cf(q, L2);
+    for (int q = 15; q < 21; ++q) cs[q + 1] = cf(q, L2);
 #pragma unroll
-    for (int q = 21; q < 27; ++q) sC[q * BX * BZ + tid] = cf(q, L3);
+    for (int q = 21; q < 27; ++q) cs[q + 3] = cf(q, L3);
 #pragma unroll
-    for (int q = 27; q < 33; ++q) sC[q * BX * BZ + tid] = cf(q, L4);
+    for (int q = 27; q < 33; ++q) cs[q + 5] = cf(q, L4);
   }
-  const volatile float* cc = sC + tid;
-  auto C = [&](int q) -> float { return cc[q * BX * BZ]; };
+  const uint32_t cs_addr = tma::smem_addr(cs);
+  // four coefficients from shared memory at each use (held in registers for
+  // the whole march they would cap the kernel's occupancy)
+  auto C4 = [&](int g) -> float4 {
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(cs_addr + 16 * g));
+    return v;
+  };
 
   const bool xs = inside && in_strip(i, NX, W), zs = inside && in_strip(k, NZ, W);
   const int xsi = xs ? strip_idx(i, NX, W) : 0;
@@ -215,12 +229,13 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS)
         const float vxx = dxx * ikxh + mvxx, vyx = dyx * ikxh + mvyx, vzx = dzx * ikxh + mvzx;
         const float vyy = dyy * iky + mvyy, vxy = dxy * iky + mvxy, vzy = dzy * iky + mvzy;
         const float vzz = dzz * ikz + mvzz, vxz = dxz * ikz + mvxz, vyz = dyz * ikz + mvyz;
-        SXX[c] = S[oc] + (C(0) * vxx + C(1) * vyy + C(2) * vzz + C(3) * (vyz + vzy) + C(4) * (vxz + vzx) +
-                          C(5) * (a.legacy ? vxy + vzy : vxy + vyx));  // Q4, :657
-        SYY[c] = S[OWN6 / 6 + oc] + (C(1) * vxx + C(6) * vyy + C(7) * vzz + C(8) * (vyz + vzy) +
-                                     C(9) * (vxz + vzx) + C(10) * (vyx + vxy));
-        SZZ[c] = S[2 * (OWN6 / 6) + oc] + (C(2) * vxx + C(7) * vyy + C(11) * vzz + C(12) * (vyz + vzy) +
-                                           C(13) * (vxz + vzx) + C(14) * (vyx + vxy));
+        const float4 c0 = C4(0), c1 = C4(1), c2 = C4(2), c3 = C4(3);  // C(0) .. C(14)
+        SXX[c] = S[oc] + (c0.x * vxx + c0.y * vyy + c0.z * vzz + c0.w * (vyz + vzy) + c1.x * (vxz + vzx) +
+                          c1.y * (a.legacy ? vxy + vzy : vxy + vyx));  // Q4, :657
+        SYY[c] = S[OWN6 / 6 + oc] + (c0.y * vxx + c1.z * vyy + c1.w * vzz + c2.x * (vyz + vzy) +
+                                     c2.y * (vxz + vzx) + c2.z * (vyx + vxy));
+        SZZ[c] = S[2 * (OWN6 / 6) + oc] + (c0.z * vxx + c1.w * vyy + c2.w * vzz + c3.x * (vyz + vzy) +
+                                           c3.y * (vxz + vzx) + c3.z * (vyx + vxy));
       }
       if (l2) {  // sigmaxy: x-, y+, z- (:681-725)
         const float dxx = cvx - xmx, dyx = cvy - xmy, dzx = cvz - xmz;
@@ -233,8 +248,9 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS)
         const float vyy = dyy * ikyh + mvyy, vxy = dxy * ikyh + mvxy, vzy = dzy * ikyh + mvzy;
         const float vzz = dzz * ikzh + mvzz, vyz = dyz * ikzh + mvyz;
         const float vzx = dzx * a.idx, vxz = dxz * a.idz;  // left unscaled, :701-707
-        SXY[c] = S[3 * (OWN6 / 6) + oc] + (C(15) * vxx + C(16) * vyy + C(17) * vzz + C(18) * (vzy + vyz) +
-                                           C(19) * (vzx + vxz) + C(20) * (vyx + vxy));
+        const float4 c4 = C4(4), c5 = C4(5);  // C(15) .. C(20)
+        SXY[c] = S[3 * (OWN6 / 6) + oc] + (c4.x * vxx + c4.y * vyy + c4.z * vzz + c4.w * (vzy + vyz) +
+                                           c5.x * (vzx + vxz) + c5.y * (vyx + vxy));
       }
       if (l3) {  // sigmaxz: x-, y-, z+ (:728-771)
         const float dxx = cvx - xmx, dyx = cvy - xmy, dzx = cvz - xmz;
@@ -246,9 +262,10 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS)
         const float vxx = dxx * ikx + mvxx, vyx = dyx * ikx + mvyx, vzx = dzx * ikx + mvzx;
         const float vyy = dyy * iky + mvyy, vxy = dxy * iky + mvxy, vzy = dzy * iky + mvzy;
         const float vzz = dzz * ikzh + mvzz, vxz = dxz * ikzh + mvxz, vyz = dyz * ikzh + mvyz;
-        SXZ[c] = S[4 * (OWN6 / 6) + oc] + (C(21) * vxx + C(22) * vyy + C(23) * vzz +
-                                           C(24) * (a.legacy ? vxz + vzx : vyz + vzy) +  // Q4, :766
-                                           C(25) * (vxz + vzx) + C(26) * (vxy + vyx));
+        const float4 c6 = C4(6), c7 = C4(7);  // C(21) .. C(26)
+        SXZ[c] = S[4 * (OWN6 / 6) + oc] + (c6.x * vxx + c6.y * vyy + c6.z * vzz +
+                                           c6.w * (a.legacy ? vxz + vzx : vyz + vzy) +  // Q4, :766
+                                           c7.x * (vxz + vzx) + c7.y * (vxy + vyx));
       }
       if (l4) {  // sigmayz: x+, y+, z+ (:774-815)
         const float dxx = xpx - cvx, dyx = xpy - cvy, dzx = xpz - cvz;
@@ -260,8 +277,9 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS)
         const float vxx = dxx * ikxh + mvxx, vyx = dyx * ikxh + mvyx, vzx = dzx * ikxh + mvzx;
         const float vyy = dyy * ikyh + mvyy, vxy = dxy * ikyh + mvxy, vzy = dzy * ikyh + mvzy;
         const float vzz = dzz * ikzh + mvzz, vxz = dxz * ikzh + mvxz, vyz = dyz * ikzh + mvyz;
-        SYZ[c] = S[5 * (OWN6 / 6) + oc] + (C(27) * vxx + C(28) * vyy + C(29) * vzz + C(30) * (vyz + vzy) +
-                                           C(31) * (vxz + vzx) + C(32) * (vyx + vxy));
+        const float4 c8 = C4(8), c9 = C4(9);  // C(27) .. C(32)
+        SYZ[c] = S[5 * (OWN6 / 6) + oc] + (c8.x * vxx + c8.y * vyy + c8.z * vzz + c8.w * (vyz + vzy) +
+                                           c9.x * (vxz + vzx) + c9.y * (vyx + vxy));
       }
       if (xs) { MVXX[mx] = mvxx; MVYX[mx] = mvyx; MVZX[mx] = mvzx; }
       if (ys) { MVXY[my] = mvxy; MVYY[my] = mvyy; MVZY[my] = mvzy; }
