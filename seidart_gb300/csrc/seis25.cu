@@ -492,6 +492,14 @@ void seis25_half2(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s)
 }
 
 bool seis25_make_maps(Seis25Args& a, size_t field_stride, const float* ytab) {
+  // the stress kernel's static table and staging ring exceed the default 48 KB
+  if (cudaFuncSetAttribute(seis25_stress_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           RING * S_STAGE * (int)sizeof(float)) != cudaSuccess ||
+      cudaFuncSetAttribute(seis25_velocity_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           RING * V_STAGE * (int)sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
   auto make = [&](CUtensorMap* m, int bx, int bz, int nf) {
     return encode_field_map(m, a.vx, a.NX, a.NY, a.NZ, a.P, field_stride, 9, bx, bz, nf);
   };

@@ -866,7 +866,7 @@ int32_t create_handle(const sfd_config* cfg, void* dev_state, size_t state_bytes
   if (!bind_args(h)) {
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
     delete h;
-    return fail(SFD_ERR_CUDA, "cuTensorMapEncodeTiled refused the 2.5-D field tiles");
+    return fail(SFD_ERR_CUDA, "could not set up the 2.5-D kernels' staged tiles (tensor maps or shared-memory size)");
   }
   e = cudaMemsetAsync(h->base, 0, L.total, h->stream);
   if (e != cudaSuccess) { cudaStreamDestroy(h->cap_stream); delete h; return cuda_fail(e, "cudaMemsetAsync"); }
