@@ -62,10 +62,6 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
   const int nxt = (te.x >> 16) - x0, nzt = (te.y >> 16) - z0;
   const int TW = (nxt + 3) & ~3, TZ = nzt;  // this tile's shared-memory layout
   const int TXT = TW >> 2, TYT = (TZ + RB - 1) / RB, SX = TXT + 1;
-  // row strides of the exchange arrays, padded so that a warp's accesses spread
-  // over the banks whichever groups its threads own: an odd number of float4
-  // slots per row (rows) and an odd number of floats per row (columns)
-  const int RW = 4 * (TXT | 1), CW = SX | 1;
   const int nc4 = TXT;
   // row edges are indexed by tile row and global x, column edges by the index
   // in the tile row and global z, so a tile row may be cut unlike its neighbours
@@ -109,12 +105,12 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
   float* sCBx = sCAx + CS;
   float* sCAz = sCBx + CS;
   float* sCBz = sCAz + CS;
-  float* sExRow = sCBz + CS;                // [TYT+1][RW]: first Ex row of thread row ty; row TYT = tile below
-  float* sHyRow = sExRow + (TYT + 1) * RW;  // [TYT+1][RW]: row ty+1 = last Hy row of thread row ty; row 0 = tile above
-  // scalar arrays last: every array above starts on a 16-byte boundary (RW is a multiple of 4)
-  float* sEzCol = sHyRow + (TYT + 1) * RW;  // [TZ][CW]: first Ez column of thread column tx; column TXT = tile right
-  float* sHyCol = sEzCol + TZ * CW;         // [TZ][CW]: column tx+1 = last Hy column of tx; column 0 = tile left
-  const int nsm = 8 * CS + 2 * (TYT + 1) * RW + 2 * TZ * CW;
+  float* sExRow = sCBz + CS;                // [TYT+1][TW]: first Ex row of thread row ty; row TYT = tile below
+  float* sHyRow = sExRow + (TYT + 1) * TW;  // [TYT+1][TW]: row ty+1 = last Hy row of thread row ty; row 0 = tile above
+  // scalar arrays last: every array above starts on a 16-byte boundary (TW is a multiple of 4)
+  float* sEzCol = sHyRow + (TYT + 1) * TW;  // [TZ][SX]: first Ez column of thread column tx; column TXT = tile right
+  float* sHyCol = sEzCol + TZ * SX;         // [TZ][SX]: column tx+1 = last Hy column of tx; column 0 = tile left
+  const int nsm = 8 * CS + 2 * (TYT + 1) * TW + 2 * TZ * SX;
   const int NZp = a.r.NZp;
   // edge words: field 0 = first Ex row / first Ez column, 1 = last Hy row / column
   auto erow = [&](int par, int f, int b) { return a.r.erow + (size_t)((par * 2 + f) * kResMaxTiles1D + b) * P; };
@@ -191,7 +187,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
       m[j] = mm;
       // all four cells updated, none on a Dirichlet plane
       plain = plain && (mm & 0xffffffu) == 0x000fffu;
-      sEzCol[row * CW + tx] = ez[j].x;
+      sEzCol[row * SX + tx] = ez[j].x;
       if (left && tx == 0) ll_put1(ecol(0, 0, bx) + k, ez[j].x, 1u);
     }
     plain = plain && se < 0;  // ... nor the source
@@ -199,7 +195,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
 #pragma unroll
     for (int j = 0; j < RB; ++j) anyzs |= zs[j];
     fast = plain && !xs && !anyzs;  // and none in a strip
-    sts4(sExRow + ty * RW + 4 * tx, ex[0]);
+    sts4(sExRow + ty * TW + 4 * tx, ex[0]);
     if (up && rbase == 0) ll_put4(erow(0, 0, bz) + i0, ex[0], 1u);
   }
   // receivers of this tile
@@ -214,8 +210,8 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
     }
   }
   if (xwarp) {  // edges of the tiles below and to the right for step 0
-    if (!fetch_edges(down ? erow(0, 0, bz + 1) + x0 : nullptr, sExRow + TYT * RW, down ? 4 * nc4 : 0,
-                     right ? ecol(0, 0, bx + 1) + z0 : nullptr, sEzCol + TXT, CW, right ? nzt : 0, 1u + a.tag_bias, ctl,
+    if (!fetch_edges(down ? erow(0, 0, bz + 1) + x0 : nullptr, sExRow + TYT * TW, down ? 4 * nc4 : 0,
+                     right ? ecol(0, 0, bx + 1) + z0 : nullptr, sEzCol + TXT, SX, right ? nzt : 0, 1u + a.tag_bias, ctl,
                      a.limit_ns) &&
         (tid & 31) == 0)
       s_abort = 1;
@@ -248,14 +244,14 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
 
     // ================= H half-step (electromagfdtd.f95:249-262)
     if (cell) {
-      const float4 exb = lds4(sExRow + (ty + 1) * RW + 4 * tx);
+      const float4 exb = lds4(sExRow + (ty + 1) * TW + 4 * tx);
 #pragma unroll
       for (int j = 0; j < RB; ++j) {
         if (j >= nrows) continue;
         const int row = rbase + j, k = z0 + row, so = 4 * (j * kResCellThreads + tid);
         float4 exn = exb;
         if (j + 1 < RB && j + 1 < nrows) exn = ex[j + 1 < RB ? j + 1 : j];
-        const float ezn = sEzCol[row * CW + tx + 1];
+        const float ezn = sEzCol[row * SX + tx + 1];
         float4 hv;
         if (fast) {
 #pragma unroll
@@ -307,14 +303,14 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
           }
         }
         hy[j] = hv;
-        sHyCol[row * CW + tx + 1] = hv.w;
+        sHyCol[row * SX + tx + 1] = hv.w;
         if (right && tx == TXT - 1) ll_put1(ecol(par, 1, bx) + k, hv.w, tag);
-        if (j == RB - 1) sts4(sHyRow + (ty + 1) * RW + 4 * tx, hv);
+        if (j == RB - 1) sts4(sHyRow + (ty + 1) * TW + 4 * tx, hv);
         if (down && row == nzt - 1) ll_put4(erow(par, 1, bz) + i0, hv, tag);
       }
     } else if (xwarp) {  // Hy row above and column on the left for this step's E half
       if (!fetch_edges(up ? erow(par, 1, bz - 1) + x0 : nullptr, sHyRow, up ? 4 * nc4 : 0,
-                       left ? ecol(par, 1, bx - 1) + z0 : nullptr, sHyCol, CW, left ? nzt : 0, tag + a.tag_bias, ctl,
+                       left ? ecol(par, 1, bx - 1) + z0 : nullptr, sHyCol, SX, left ? nzt : 0, tag + a.tag_bias, ctl,
                        a.limit_ns) &&
           (tid & 31) == 0)
         s_abort = 1;
@@ -327,14 +323,14 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
 
     // ================= E half-step, source, Dirichlet planes, norm (:273-321)
     if (cell) {
-      const float4 hmt = lds4(sHyRow + ty * RW + 4 * tx);
+      const float4 hmt = lds4(sHyRow + ty * TW + 4 * tx);
 #pragma unroll
       for (int j = 0; j < RB; ++j) {
         if (j >= nrows) continue;
         const int row = rbase + j, k = z0 + row, so = 4 * (j * kResCellThreads + tid);
         float4 hm = hmt;
         if (j > 0) hm = hy[j > 0 ? j - 1 : 0];
-        const float hl = sHyCol[row * CW + tx];
+        const float hl = sHyCol[row * SX + tx];
         const float4 h = hy[j];
         const float4 cxa = lds4(sCAx + so), cxb = lds4(sCBx + so), cza = lds4(sCAz + so), czb = lds4(sCBz + so);
         if (fast) {
@@ -403,10 +399,10 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
             if (xs) sts2(sMHyx + so + 2 * hh, px);
           }
         }
-        sEzCol[row * CW + tx] = ez[j].x;
+        sEzCol[row * SX + tx] = ez[j].x;
         if (left && tx == 0) ll_put1(ecol(par ^ 1, 0, bx) + k, ez[j].x, tag + 1u);
       }
-      sts4(sExRow + ty * RW + 4 * tx, ex[0]);
+      sts4(sExRow + ty * TW + 4 * tx, ex[0]);
       if (up && rbase == 0) ll_put4(erow(par ^ 1, 0, bz) + i0, ex[0], tag + 1u);
       if (DUMP) {  // the state after step t, each thread its own cells; Hy before its planes are zeroed
         char* d = a.dump.base + (size_t)(s + 1) * a.dump.stride;
@@ -498,8 +494,8 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
           }
       }
     } else if (xwarp && s + 1 < a.nsteps) {  // Ex row below and Ez column to the right for step s+1
-      if (!fetch_edges(down ? erow(par ^ 1, 0, bz + 1) + x0 : nullptr, sExRow + TYT * RW, down ? 4 * nc4 : 0,
-                       right ? ecol(par ^ 1, 0, bx + 1) + z0 : nullptr, sEzCol + TXT, CW, right ? nzt : 0, tag + 1u + a.tag_bias,
+      if (!fetch_edges(down ? erow(par ^ 1, 0, bz + 1) + x0 : nullptr, sExRow + TYT * TW, down ? 4 * nc4 : 0,
+                       right ? ecol(par ^ 1, 0, bx + 1) + z0 : nullptr, sEzCol + TXT, SX, right ? nzt : 0, tag + 1u + a.tag_bias,
                        ctl, a.limit_ns) &&
           (tid & 31) == 0)
         s_abort = 1;
@@ -541,8 +537,8 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
 }  // namespace
 
 size_t em2_resident_smem(int TW, int TZ) {
-  const size_t TXT = (size_t)TW / 4, RW = 4 * (TXT | 1), CW = (TXT + 1) | 1, TYT = ((size_t)TZ + kResRows - 1) / kResRows;
-  return sizeof(float) * (32 * (size_t)kResRows * kResCellThreads + 2 * (TYT + 1) * RW + 2 * (size_t)TZ * CW);
+  const size_t SX = (size_t)TW / 4 + 1, TYT = ((size_t)TZ + kResRows - 1) / kResRows;
+  return sizeof(float) * (32 * (size_t)kResRows * kResCellThreads + 2 * (TYT + 1) * TW + 2 * (size_t)TZ * SX);
 }
 
 namespace {
