@@ -406,6 +406,41 @@ __device__ __forceinline__ S2Stress seis2_stress_cell(const Seis2Step& a, int i,
   return o;
 }
 
+// The three stresses at (i, k) for a cell off the CPML strips, off the
+// Dirichlet planes and away from the source: both stress loops without
+// memory variables or masks (the operations the general path performs on
+// such a cell).
+template <bool RO>
+__device__ __forceinline__ void seis2_stress_plain(const Seis2Step& a, int i, int k, float& sxx, float& szz,
+                                                   float& sxz) {
+  const int P = a.P;
+  const int c = k * P + i;
+  const float ikx = __ldg(a.X.ik + i), ikxh = __ldg(a.X.ikh + i);
+  const float ikz = __ldg(a.Z.ik + k), ikzh = __ldg(a.Z.ikh + k);
+  const float vx0 = fld<RO>(a.vx0 + c), vz0 = fld<RO>(a.vz0 + c);
+  const float vxl = fld<RO>(a.vx0 + c - 1), vxr = fld<RO>(a.vx0 + c + 1);
+  const float vxu = fld<RO>(a.vx0 + c - P), vxd = fld<RO>(a.vx0 + c + P);
+  const float vzl = fld<RO>(a.vz0 + c - 1), vzr = fld<RO>(a.vz0 + c + 1);
+  const float vzu = fld<RO>(a.vz0 + c - P), vzd = fld<RO>(a.vz0 + c + P);
+  sxx = fld<RO>(a.sxx0 + c);
+  szz = fld<RO>(a.szz0 + c);
+  sxz = fld<RO>(a.sxz0 + c);
+  {  // :247-283
+    const float dvx_dx = (vxr - vx0) * ikxh, dvz_dz = (vz0 - vzu) * ikz;
+    const float dvz_dx = (vzr - vz0) * ikx, dvx_dz = (vx0 - vxu) * ikzh;
+    const float A11 = __ldg(a.A11 + c), A13 = __ldg(a.A13 + c), A15 = __ldg(a.A15 + c);
+    const float A33 = __ldg(a.A33 + c), A35 = __ldg(a.A35 + c);
+    const float shear = dvz_dx + dvx_dz;
+    sxx = sxx + (A11 * dvx_dx + A13 * dvz_dz + A15 * shear);
+    szz = szz + (A13 * dvx_dx + A33 * dvz_dz + A35 * shear);
+  }
+  {  // :285-312
+    const float dvx_dx = (vx0 - vxl) * ikxh, dvz_dz = (vzd - vz0) * ikz;
+    const float dvz_dx = (vz0 - vzl) * ikx, dvx_dz = (vxd - vx0) * ikzh;
+    sxz = sxz + (__ldg(a.B15 + c) * dvx_dx + __ldg(a.B35 + c) * dvz_dz + __ldg(a.B55 + c) * (dvz_dx + dvx_dz));
+  }
+}
+
 template <int ZB, bool RO>
 __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, int by, int gridx,
                                            float (*sS)[8 * ZB + 2][34]) {
@@ -427,32 +462,12 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
                     !(a.io.si >= x0 && a.io.si < x0 + 32 && a.io.sk >= z0 && a.io.sk < z0 + 8 * ZB);
   // ---- stress half-step on owned cells (stored) ...
   if (fast) {
-    const float ikx = __ldg(a.X.ik + i), ikxh = __ldg(a.X.ikh + i);
 #pragma unroll
     for (int r = 0; r < ZB; ++r) {
       const int k = z0 + ty + 8 * r;
       const int c = k * P + i;
-      const float ikz = __ldg(a.Z.ik + k), ikzh = __ldg(a.Z.ikh + k);
-      const float vx0 = fld<RO>(a.vx0 + c), vz0 = fld<RO>(a.vz0 + c);
-      const float vxl = fld<RO>(a.vx0 + c - 1), vxr = fld<RO>(a.vx0 + c + 1);
-      const float vxu = fld<RO>(a.vx0 + c - P), vxd = fld<RO>(a.vx0 + c + P);
-      const float vzl = fld<RO>(a.vz0 + c - 1), vzr = fld<RO>(a.vz0 + c + 1);
-      const float vzu = fld<RO>(a.vz0 + c - P), vzd = fld<RO>(a.vz0 + c + P);
-      float sxx = fld<RO>(a.sxx0 + c), szz = fld<RO>(a.szz0 + c), sxz = fld<RO>(a.sxz0 + c);
-      {  // :247-283
-        const float dvx_dx = (vxr - vx0) * ikxh, dvz_dz = (vz0 - vzu) * ikz;
-        const float dvz_dx = (vzr - vz0) * ikx, dvx_dz = (vx0 - vxu) * ikzh;
-        const float A11 = __ldg(a.A11 + c), A13 = __ldg(a.A13 + c), A15 = __ldg(a.A15 + c);
-        const float A33 = __ldg(a.A33 + c), A35 = __ldg(a.A35 + c);
-        const float shear = dvz_dx + dvx_dz;
-        sxx = sxx + (A11 * dvx_dx + A13 * dvz_dz + A15 * shear);
-        szz = szz + (A13 * dvx_dx + A33 * dvz_dz + A35 * shear);
-      }
-      {  // :285-312
-        const float dvx_dx = (vx0 - vxl) * ikxh, dvz_dz = (vzd - vz0) * ikz;
-        const float dvz_dx = (vz0 - vzl) * ikx, dvx_dz = (vxd - vx0) * ikzh;
-        sxz = sxz + (__ldg(a.B15 + c) * dvx_dx + __ldg(a.B35 + c) * dvz_dz + __ldg(a.B55 + c) * (dvz_dx + dvx_dz));
-      }
+      float sxx, szz, sxz;
+      seis2_stress_plain<RO>(a, i, k, sxx, szz, sxz);
       a.sxx1[c] = sxx;
       a.szz1[c] = szz;
       a.sxz1[c] = sxz;
@@ -489,7 +504,13 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
   }
   }
   // ... and on the halo ring (shared memory only): warps 0-3 take the top
-  // row, bottom row, left column and right column, one cell per lane.
+  // row, bottom row, left column and right column, one cell per lane.  When
+  // the ring too lies off the strips, the planes and the source, it takes
+  // the short path of the owned cells: the ring is these warps' fifth row of
+  // work, and the general path would make it the longest.
+  const bool fast_ring = fast && x0 - 1 >= lo && x0 + 32 <= NX - 1 - lo && x0 + 32 <= NX - 2 && z0 - 1 >= lo &&
+                         z0 + 8 * ZB <= NZ - 1 - lo && z0 + 8 * ZB <= NZ - 2 &&
+                         !(a.io.si >= x0 - 1 && a.io.si <= x0 + 32 && a.io.sk >= z0 - 1 && a.io.sk <= z0 + 8 * ZB);
   if (ty < 4) {
     for (int q = tx; q < (ty < 2 ? 32 : 8 * ZB); q += 32) {
       int hi, hk, si, sk;
@@ -497,7 +518,13 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
       else if (ty == 1) { hi = x0 + q; hk = z0 + 8 * ZB; si = q + 1; sk = 8 * ZB + 1; }
       else if (ty == 2) { hi = x0 - 1; hk = z0 + q; si = 0; sk = q + 1; }
       else { hi = x0 + 32; hk = z0 + q; si = 33; sk = q + 1; }
-      if (hi >= 0 && hi < NX && hk >= 0 && hk < NZ) {
+      if (fast_ring) {
+        float sxx, szz, sxz;
+        seis2_stress_plain<RO>(a, hi, hk, sxx, szz, sxz);
+        sS[0][sk][si] = sxx;
+        sS[1][sk][si] = szz;
+        sS[2][sk][si] = sxz;
+      } else if (hi >= 0 && hi < NX && hk >= 0 && hk < NZ) {
         const S2Stress s = seis2_stress_cell<RO>(a, hi, hk, t);
         sS[0][sk][si] = s.sxx;
         sS[1][sk][si] = s.szz;
