@@ -6,8 +6,10 @@ position and reads one receiver column back per shot
 builds and runs the model for source i and extracts receiver i;
 ``co_run`` stacks the columns into ``co_image[time step, source]``).
 
-Here the shots a process owns advance together in one batched launch
-(:mod:`seidart_gb300.batch`): shots of one model share its coefficient
+Here the shots a process owns run on the GPU by the fastest form each can
+take (:func:`gpu_runner`): a shot whose grid fits on chip runs alone in one
+launch, the others advance together in one batched launch
+(:mod:`seidart_gb300.batch`); shots of one model share its coefficient
 planes on the device.  Shots are independent, so several GPUs -- one
 process per GPU under ``torch.distributed`` -- split them with no exchange
 on the data path:
@@ -121,14 +123,25 @@ def default_device(group=None) -> str:
     return "cuda"
 
 
-def gpu_runner(cases, device=None) -> List[np.ndarray]:
-    """Receiver traces (nstep, nch, nrec) of each case.  The 2-D single-pass
-    kinds advance together in one batched launch per run, cases that hold
-    the same model planes (the same array object) sharing one copy of the
-    coefficients; 2.5-D cases run one after another.  ``device`` defaults to
-    :func:`default_device`."""
+def gpu_runner(cases, device=None, schedule: str = "auto") -> List[np.ndarray]:
+    """Receiver traces (nstep, nch, nrec) of each case.  ``device`` defaults
+    to :func:`default_device`.  2.5-D cases run one after another.  For the
+    2-D single-pass kinds, ``schedule``:
+
+    * ``"auto"`` (default): a case whose grid runs on chip (one launch for
+      the whole run, :meth:`FDTDSolver.on_chip`) runs alone, one after
+      another -- on chip a shot runs faster than any tile of a batched
+      launch streaming from HBM; the others advance together in one batched
+      launch per shot length;
+    * ``"batch"``: every 2-D case in the batched launch;
+    * ``"sequential"``: every case alone, in its own default form.
+
+    Cases that hold the same model planes (the same array object) share one
+    copy of the coefficients."""
     from .batch import Batch, autotune
     from .solver import FDTDSolver, run_shot
+    if schedule not in ("auto", "batch", "sequential"):
+        raise ValueError("schedule must be 'auto', 'batch' or 'sequential'")
     device = default_device() if device is None else device
 
     out: List[Optional[np.ndarray]] = [None] * len(cases)
@@ -136,37 +149,54 @@ def gpu_runner(cases, device=None) -> List[np.ndarray]:
     for q, c in enumerate(cases):
         if q not in two_d:
             out[q] = run_shot(c.grid, c.planes, c.profiles, c.src_ijk, c.srcfn, c.rec_ijk, device=device)
-    if two_d:
+    if not two_d:
+        return out
+    solvers: Dict[int, FDTDSolver] = {}
+    owner = {}
+    try:
+        for q in two_d:
+            c = cases[q]
+            s = FDTDSolver(c.grid, c.nstep, len(c.rec_ijk), device=device)
+            solvers[q] = s
+            if id(c.planes) in owner:
+                s.share_model(owner[id(c.planes)])
+            else:
+                s.set_model(c.planes)
+                owner[id(c.planes)] = s
+            s.set_cpml(c.profiles)
+            s.set_source(c.src_ijk, c.srcfn)
+            s.set_receivers(c.rec_ijk)
+        batched = []
+        for q in two_d:
+            s = solvers[q]
+            if schedule == "sequential" or (schedule == "auto" and s.on_chip() is not None):
+                s.run(cases[q].nstep)
+                s.status()
+                out[q] = s.traces()
+            else:
+                batched.append(q)
         by_len: Dict[int, List[int]] = {}
-        for q in two_d:  # one batch per shot length: a batch advances all its models together
+        for q in batched:  # one batch per shot length: a batch advances all its models together
             by_len.setdefault(cases[q].nstep, []).append(q)
         for nstep, qs in by_len.items():
-            solvers, owner = [], {}
+            if len(qs) == 1:
+                s = solvers[qs[0]]
+                s.run(nstep)
+                s.status()
+                out[qs[0]] = s.traces()
+                continue
+            b = Batch([solvers[q] for q in qs])
             try:
+                autotune(b, steps=4)
+                b.run(nstep)
+                b.status()
                 for q in qs:
-                    c = cases[q]
-                    s = FDTDSolver(c.grid, c.nstep, len(c.rec_ijk), device=device)
-                    solvers.append(s)
-                    if id(c.planes) in owner:
-                        s.share_model(owner[id(c.planes)])
-                    else:
-                        s.set_model(c.planes)
-                        owner[id(c.planes)] = s
-                    s.set_cpml(c.profiles)
-                    s.set_source(c.src_ijk, c.srcfn)
-                    s.set_receivers(c.rec_ijk)
-                b = Batch(solvers)
-                try:
-                    autotune(b, steps=4)
-                    b.run(nstep)
-                    b.status()
-                    for q, s in zip(qs, solvers):
-                        out[q] = s.traces()
-                finally:
-                    b.close()
+                    out[q] = solvers[q].traces()
             finally:
-                for s in solvers:
-                    s.close()
+                b.close()
+    finally:
+        for s in solvers.values():
+            s.close()
     return out
 
 
@@ -209,8 +239,9 @@ class CommonOffset:
 
     ``co_run()`` returns ``co_image`` of shape (time steps, sources), as the
     reference's ``co_run`` builds it, on rank 0 (None on other ranks).  The
-    shots share the model's coefficient planes and run in one batched launch
-    per rank."""
+    shots share the model's coefficient planes and run through
+    :func:`gpu_runner`: one after another on chip when the grid fits, else
+    in one batched launch per rank."""
 
     def __init__(self, grid, planes, profiles, srcfn, source_ijk, receiver_ijk, channel: str, device=None,
                  runner: Optional[Callable] = None, group=None):

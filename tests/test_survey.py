@@ -173,19 +173,21 @@ def test_two_rank_gradient_is_the_sum_over_shots(tmp_path):
 
 
 @pytest.mark.gpu
-def test_gpu_runner_batches_shots_like_the_oracle(gpu):
+@pytest.mark.parametrize("schedule", ["auto", "batch"])
+def test_gpu_runner_batches_shots_like_the_oracle(gpu, schedule):
     cases = _survey_cases()
-    got = survey.run_survey(cases)
+    got = survey.run_survey(cases, runner=lambda cs: survey.gpu_runner(cs, schedule=schedule))
     for c, tr in zip(cases, got):
         e = rel_l2(tr, run_oracle(c)[1])
         assert e <= 1e-5, f"{c.name}: rel L2 {e:.2e}"
 
 
 @pytest.mark.gpu
-def test_gpu_runner_with_a_model_too_large_for_chip(gpu):
-    """A seismic2 grid too large for the on-chip form (700 x 600 cells) in
-    one batched launch with shots and a small model that fit on chip, all
-    against the oracle."""
+@pytest.mark.parametrize("schedule", ["auto", "batch"])
+def test_gpu_runner_with_a_model_too_large_for_chip(gpu, schedule):
+    """A seismic2 grid too large for the on-chip form (700 x 600 cells) with
+    shots and a small model that fit on chip (auto: those run alone on chip;
+    batch: all in one batched launch), all against the oracle."""
     from helpers import make_solver
     big = sy.small_case(SEISMIC2, seed=13, nx=700, nz=600, npml=10, nstep=40, nrec=6)
     cases = _survey_cases() + [big]
@@ -193,7 +195,7 @@ def test_gpu_runner_with_a_model_too_large_for_chip(gpu):
         assert s.on_chip() is None
     with make_solver(cases[-2]) as s:
         assert s.on_chip() is not None
-    got = survey.run_survey(cases)
+    got = survey.run_survey(cases, runner=lambda cs: survey.gpu_runner(cs, schedule=schedule))
     for c, tr in zip(cases, got):
         e = rel_l2(tr, run_oracle(c)[1])
         assert e <= 1e-5, f"{c.name}: rel L2 {e:.2e}"
