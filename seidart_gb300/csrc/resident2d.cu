@@ -545,7 +545,10 @@ namespace {
 
 // Cost model of the planner, in four-cell groups: a group in a CPML strip or
 // on a boundary plane takes the longer update.
-constexpr double kGeneralCost = 4.0;
+#ifndef SFD_RES_GENERAL_COST
+#define SFD_RES_GENERAL_COST 4.0
+#endif
+constexpr double kGeneralCost = SFD_RES_GENERAL_COST;
 
 // Cut n items of weight 1 + beta * gen[q] into `parts` runs of about equal
 // weight; bounds[0] = 0, bounds[parts] = n.  False if a run would be empty.
