@@ -6,11 +6,10 @@ position and reads one receiver column back per shot
 builds and runs the model for source i and extracts receiver i;
 ``co_run`` stacks the columns into ``co_image[time step, source]``).
 
-Here the shots a process owns run on the GPU by the fastest form each can
-take (:func:`gpu_runner`): a shot whose grid fits on chip runs alone in one
-launch, the others advance together in one batched launch
-(:mod:`seidart_gb300.batch`); shots of one model share its coefficient
-planes on the device.  Shots are independent, so several GPUs -- one
+Here the shots a process owns run on the GPU one after another, each in its
+fastest form (:func:`gpu_runner`; on chip where the grid fits), or, on
+request, together in one batched launch (:mod:`seidart_gb300.batch`);
+shots of one model share its coefficient planes on the device.  Shots are independent, so several GPUs -- one
 process per GPU under ``torch.distributed`` -- split them with no exchange
 on the data path:
 
@@ -123,25 +122,31 @@ def default_device(group=None) -> str:
     return "cuda"
 
 
-def gpu_runner(cases, device=None, schedule: str = "auto") -> List[np.ndarray]:
+def gpu_runner(cases, device=None, schedule: str = "sequential") -> List[np.ndarray]:
     """Receiver traces (nstep, nch, nrec) of each case.  ``device`` defaults
     to :func:`default_device`.  2.5-D cases run one after another.  For the
     2-D single-pass kinds, ``schedule``:
 
-    * ``"auto"`` (default): a case whose grid runs on chip (one launch for
-      the whole run, :meth:`FDTDSolver.on_chip`) runs alone, one after
-      another -- on chip a shot runs faster than any tile of a batched
-      launch streaming from HBM; the others advance together in one batched
-      launch per shot length;
-    * ``"batch"``: every 2-D case in the batched launch;
-    * ``"sequential"``: every case alone, in its own default form.
+    * ``"sequential"`` (default): every case alone, one after another, each
+      in its own default form -- the whole run in one launch on chip where
+      the grid fits, else one launch per step;
+    * ``"batch"``: all of them advancing together in one persistent launch
+      per shot length (:mod:`seidart_gb300.batch`).
+
+    On the 80-model survey of 64 electromag2 shots (1040 x 540) and 16
+    seismic2 models (200-1200 x 100-600 cells), 4000 steps, the sequential
+    schedule took 1.90 s and the batch 2.37 s (wall clock, set-up
+    included): on chip a shot runs faster than a batch tile streaming from
+    HBM, and a grid too large for the chip runs its own launches at least as
+    fast as the batch kernel's register-capped tiles.  Running the models
+    that fit on chip alone and batching the rest took 2.08 s.
 
     Cases that hold the same model planes (the same array object) share one
     copy of the coefficients."""
     from .batch import Batch, autotune
     from .solver import FDTDSolver, run_shot
-    if schedule not in ("auto", "batch", "sequential"):
-        raise ValueError("schedule must be 'auto', 'batch' or 'sequential'")
+    if schedule not in ("sequential", "batch"):
+        raise ValueError("schedule must be 'sequential' or 'batch'")
     device = default_device() if device is None else device
 
     out: List[Optional[np.ndarray]] = [None] * len(cases)
@@ -169,7 +174,7 @@ def gpu_runner(cases, device=None, schedule: str = "auto") -> List[np.ndarray]:
         batched = []
         for q in two_d:
             s = solvers[q]
-            if schedule == "sequential" or (schedule == "auto" and s.on_chip() is not None):
+            if schedule == "sequential":
                 s.run(cases[q].nstep)
                 s.status()
                 out[q] = s.traces()
@@ -240,8 +245,7 @@ class CommonOffset:
     ``co_run()`` returns ``co_image`` of shape (time steps, sources), as the
     reference's ``co_run`` builds it, on rank 0 (None on other ranks).  The
     shots share the model's coefficient planes and run through
-    :func:`gpu_runner`: one after another on chip when the grid fits, else
-    in one batched launch per rank."""
+    :func:`gpu_runner`."""
 
     def __init__(self, grid, planes, profiles, srcfn, source_ijk, receiver_ijk, channel: str, device=None,
                  runner: Optional[Callable] = None, group=None):

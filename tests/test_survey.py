@@ -173,7 +173,7 @@ def test_two_rank_gradient_is_the_sum_over_shots(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("schedule", ["auto", "batch"])
+@pytest.mark.parametrize("schedule", ["sequential", "batch"])
 def test_gpu_runner_batches_shots_like_the_oracle(gpu, schedule):
     cases = _survey_cases()
     got = survey.run_survey(cases, runner=lambda cs: survey.gpu_runner(cs, schedule=schedule))
@@ -183,11 +183,12 @@ def test_gpu_runner_batches_shots_like_the_oracle(gpu, schedule):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("schedule", ["auto", "batch"])
+@pytest.mark.parametrize("schedule", ["sequential", "batch"])
 def test_gpu_runner_with_a_model_too_large_for_chip(gpu, schedule):
     """A seismic2 grid too large for the on-chip form (700 x 600 cells) with
-    shots and a small model that fit on chip (auto: those run alone on chip;
-    batch: all in one batched launch), all against the oracle."""
+    shots and a small model that fit on chip (sequential: each alone in its
+    default form; batch: all in one batched launch), all against the
+    oracle."""
     from helpers import make_solver
     big = sy.small_case(SEISMIC2, seed=13, nx=700, nz=600, npml=10, nstep=40, nrec=6)
     cases = _survey_cases() + [big]
