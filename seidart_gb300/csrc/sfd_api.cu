@@ -369,6 +369,9 @@ namespace {
 // L2, and more, smaller blocks keep more loads in flight (measured on the
 // 440 x 240 seismic2 and 1040 x 540 electromag2 grids).
 int single_pass_zb(int kind, int nx, int nz) {
+#ifdef SFD_SP_ZB
+  return SFD_SP_ZB;  // build-time override for tuning sweeps
+#endif
   const long tw = kind == SFD_ELECTROMAG2 ? 128 : 32;  // tile width
   const long tiles2 = ((nx + tw - 1) / tw) * (long)((nz + 15) / 16);
   return tiles2 >= 8L * 152 ? 2 : 1;
