@@ -56,7 +56,8 @@ __device__ void em25_wait_failed(const Em25Args& a, uint64_t* full, int n, int n
 }
 
 __global__ void __launch_bounds__(BX * BZ) em25_h_tma_kernel(const __grid_constant__ Em25Args a, int rel) {
-  extern __shared__ __align__(128) float stage[];
+  extern __shared__ __align__(128) unsigned char stage_raw[];
+  float* const stage = tma::aligned_stage(stage_raw);
   __shared__ __align__(8) uint64_t full[RING];
   const Ctl* ctl = a.io.ctl;
   const int t = ctl->base + rel;
@@ -177,7 +178,8 @@ __global__ void __launch_bounds__(BX * BZ) em25_h_tma_kernel(const __grid_consta
 }
 
 __global__ void __launch_bounds__(BX * BZ) em25_e_tma_kernel(const __grid_constant__ Em25Args a, int rel) {
-  extern __shared__ __align__(128) float stage[];
+  extern __shared__ __align__(128) unsigned char stage_raw[];
+  float* const stage = tma::aligned_stage(stage_raw);
   __shared__ __align__(8) uint64_t full[RING];
   const int t = a.io.ctl->base + rel;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
@@ -353,11 +355,11 @@ Launch em25_launch(const Em25Args& a) {
 }
 
 void em25_half1(const Em25Args& a, const Launch& L, int rel, cudaStream_t s) {
-  em25_h_tma_kernel<<<L.grid, L.block, RING * STAGE * sizeof(float), s>>>(a, rel);
+  em25_h_tma_kernel<<<L.grid, L.block, RING * STAGE * sizeof(float) + tma::kStageSlack, s>>>(a, rel);
 }
 
 void em25_half2(const Em25Args& a, const Launch& L, int rel, cudaStream_t s) {
-  em25_e_tma_kernel<<<L.grid, L.block, RING * STAGE * sizeof(float), s>>>(a, rel);
+  em25_e_tma_kernel<<<L.grid, L.block, RING * STAGE * sizeof(float) + tma::kStageSlack, s>>>(a, rel);
 }
 
 bool em25_make_maps(Em25Args& a, size_t field_stride, const float* ytab) {

@@ -92,7 +92,8 @@ __device__ void staged_wait_failed(const Seis25Args& a, uint64_t* full, int n, i
 
 __global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS)
     seis25_stress_tma_kernel(const __grid_constant__ Seis25Args a, int rel) {
-  extern __shared__ __align__(128) float stage[];
+  extern __shared__ __align__(128) unsigned char stage_raw[];
+  float* const stage = tma::aligned_stage(stage_raw);
   __shared__ __align__(8) uint64_t full[RING];
   __shared__ __align__(16) float sC[CSTRIDE * BX * BZ];
   const Ctl* ctl = a.io.ctl;
@@ -309,7 +310,8 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS)
 
 __global__ void __launch_bounds__(BX * BZ, SEIS25_VELOCITY_BLOCKS)
     seis25_velocity_tma_kernel(const __grid_constant__ Seis25Args a, int rel) {
-  extern __shared__ __align__(128) float stage[];
+  extern __shared__ __align__(128) unsigned char stage_raw[];
+  float* const stage = tma::aligned_stage(stage_raw);
   __shared__ __align__(8) uint64_t full[RING];
   const int t = a.io.ctl->base + rel;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
@@ -484,19 +486,19 @@ Launch seis25_launch(const Seis25Args& a) {
 }
 
 void seis25_half1(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s) {
-  seis25_stress_tma_kernel<<<L.grid, L.block, RING * S_STAGE * sizeof(float), s>>>(a, rel);
+  seis25_stress_tma_kernel<<<L.grid, L.block, RING * S_STAGE * sizeof(float) + tma::kStageSlack, s>>>(a, rel);
 }
 
 void seis25_half2(const Seis25Args& a, const Launch& L, int rel, cudaStream_t s) {
-  seis25_velocity_tma_kernel<<<L.grid, L.block, RING * V_STAGE * sizeof(float), s>>>(a, rel);
+  seis25_velocity_tma_kernel<<<L.grid, L.block, RING * V_STAGE * sizeof(float) + tma::kStageSlack, s>>>(a, rel);
 }
 
 bool seis25_make_maps(Seis25Args& a, size_t field_stride, const float* ytab) {
   // the stress kernel's static table and staging ring exceed the default 48 KB
   if (cudaFuncSetAttribute(seis25_stress_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           RING * S_STAGE * (int)sizeof(float)) != cudaSuccess ||
+                           RING * S_STAGE * (int)sizeof(float) + tma::kStageSlack) != cudaSuccess ||
       cudaFuncSetAttribute(seis25_velocity_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           RING * V_STAGE * (int)sizeof(float)) != cudaSuccess) {
+                           RING * V_STAGE * (int)sizeof(float) + tma::kStageSlack) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }

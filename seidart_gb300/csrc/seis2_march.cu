@@ -48,7 +48,8 @@ __device__ void march_wait_failed(const Seis2Step& a, uint64_t* full, int n, int
 
 __global__ void __launch_bounds__(MT, 4)
     seis2_march_kernel(const __grid_constant__ Seis2Step a, const __grid_constant__ Seis2March mm, int rel) {
-  extern __shared__ __align__(128) float stage[];
+  extern __shared__ __align__(128) unsigned char stage_raw[];
+  float* const stage = tma::aligned_stage(stage_raw);
   __shared__ float sN[3][3][MX];  // new sxx szz sxz of rows r-2, r-1, r (by r mod 3)
   __shared__ __align__(8) uint64_t full[RING];
   const Ctl* ctl = a.io.ctl;
@@ -289,7 +290,7 @@ __global__ void __launch_bounds__(MT, 4)
 bool seis2_march_prepare(const Seis2Step& a, size_t field_stride, const float* coef, size_t coef_plane,
                          Seis2March* out) {
   if (cudaFuncSetAttribute(seis2_march_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           RING * STAGE * (int)sizeof(float)) != cudaSuccess) {
+                           RING * STAGE * (int)sizeof(float) + tma::kStageSlack) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
@@ -313,7 +314,7 @@ Launch seis2_march_launch(const Seis2Step& a, int seg) {
 }
 
 void seis2_march(const Seis2Step& a, const Seis2March& m, const Launch& L, int rel, cudaStream_t s) {
-  seis2_march_kernel<<<L.grid, L.block, RING * STAGE * sizeof(float), s>>>(a, m, rel);
+  seis2_march_kernel<<<L.grid, L.block, RING * STAGE * sizeof(float) + tma::kStageSlack, s>>>(a, m, rel);
 }
 
 }  // namespace sfd

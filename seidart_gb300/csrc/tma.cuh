@@ -21,6 +21,17 @@ __device__ __forceinline__ unsigned long long now_ns() {
   return t;
 }
 
+// The dynamic shared memory of a kernel begins after its static shared
+// variables, at whatever offset their sizes leave, whatever alignment the
+// extern declaration states.  Staging rings start at the first 128-byte
+// boundary of it (TMA needs 16-byte aligned destinations); the launches ask
+// for kStageSlack bytes more than the ring.
+constexpr int kStageSlack = 128;
+__device__ __forceinline__ float* aligned_stage(unsigned char* raw) {
+  const uint32_t a = smem_addr(raw);
+  return reinterpret_cast<float*>(raw + ((128u - (a & 127u)) & 127u));
+}
+
 __device__ __forceinline__ void bar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
 }
