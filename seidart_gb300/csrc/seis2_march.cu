@@ -32,12 +32,17 @@ constexpr int MT = 128;               // threads per block
 constexpr int MW = 124;               // own columns per block
 constexpr int MX = 132;               // staged columns: x0 - 4 .. x0 + 127
 constexpr int RING = 5;
-constexpr int ST_V = 0;               // vx vz of the stage's velocity row
-constexpr int ST_S = 2 * MX;          // sxx szz sxz (old) of its stress row
-constexpr int ST_CS = 5 * MX;         // A11 A13 A15 A33 A35 B15 B35 B55 of its stress row
-constexpr int ST_CV = 13 * MX;        // dtrx dtrz gxp gzp of its velocity row
-constexpr int STAGE = 17 * MX + 28;   // 2272 floats, 128-byte multiple
-static_assert((STAGE * 4) % 128 == 0 && (MX * 4) % 16 == 0, "stage alignment");
+// Each box lands on a 128-byte boundary of the stage (the alignment a
+// tensor copy's shared-memory destination needs).
+constexpr int ST_V = 0;               // vx vz of the stage's velocity row (2 x 132 floats)
+constexpr int ST_S = 288;             // sxx szz sxz (old) of its stress row (3 x 132)
+constexpr int ST_CS = 704;            // A11 A13 A15 A33 A35 B15 B35 B55 of its stress row (8 x 132)
+constexpr int ST_CV = 1760;           // dtrx dtrz gxp gzp of its velocity row (4 x 132)
+constexpr int STAGE = 2304;           // 9216 bytes
+static_assert(ST_S >= 2 * MX && ST_CS >= ST_S + 3 * MX && ST_CV >= ST_CS + 8 * MX && STAGE >= ST_CV + 4 * MX,
+              "stage layout");
+static_assert(ST_S % 32 == 0 && ST_CS % 32 == 0 && ST_CV % 32 == 0 && STAGE % 32 == 0 && (MX * 4) % 16 == 0,
+              "128-byte aligned boxes");
 constexpr uint32_t V_BYTES = 2 * MX * 4, SC_BYTES = 15 * MX * 4;
 
 __device__ void march_wait_failed(const Seis2Step& a, uint64_t* full, int n, int nst, unsigned long long limit) {
@@ -65,6 +70,11 @@ __global__ void __launch_bounds__(MT, 4)
   const int slot = blockIdx.y * gridDim.x + blockIdx.x;
   float norm = 0.0f;
   if (k0 >= k1) {  // the whole block
+    block_norm_to_slot(norm, a.io.slots, slot);
+    return;
+  }
+  if (tma::smem_addr(stage) & 127u) {  // the ring's base must be 128-byte aligned: record, copy nothing, leave
+    if (tx == 0) atomicExch(&a.io.ctl->err, 1);
     block_norm_to_slot(norm, a.io.slots, slot);
     return;
   }

@@ -24,8 +24,9 @@ __device__ __forceinline__ unsigned long long now_ns() {
 // The dynamic shared memory of a kernel begins after its static shared
 // variables, at whatever offset their sizes leave, whatever alignment the
 // extern declaration states.  Staging rings start at the first 128-byte
-// boundary of it (TMA needs 16-byte aligned destinations); the launches ask
-// for kStageSlack bytes more than the ring.
+// boundary of it, and every box of a stage lies on a 128-byte boundary too
+// (the alignment a tensor copy's shared-memory destination needs); the
+// launches ask for kStageSlack bytes more than the ring.
 constexpr int kStageSlack = 128;
 __device__ __forceinline__ float* aligned_stage(unsigned char* raw) {
   const uint32_t a = smem_addr(raw);
@@ -71,9 +72,9 @@ __device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity, unsigne
 }
 
 // 4-D tile load: the box of `map` at coordinates (c0, c1, c2, c3), innermost
-// first, into shared memory at `dst`; completion counted on `bar`.  c0 times
-// the element size must be a multiple of 16 bytes; boxes reaching outside the
-// tensor read zeros there.
+// first, into shared memory at `dst` (128-byte aligned); completion counted on
+// `bar`.  c0 times the element size must be a multiple of 16 bytes; boxes
+// reaching outside the tensor read zeros there.
 __device__ __forceinline__ void load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2,
                                         int c3) {
   asm volatile(
