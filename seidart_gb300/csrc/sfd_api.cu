@@ -304,9 +304,6 @@ struct sfd_handle_s {
   int zb = 2;           // rows per thread of the single-pass tiles
   Em2Step em2s[2];      // [p]: reads copy p, writes copy 1-p
   Seis2Step s2s[2];
-  bool s2march = false;   // single-pass seismic2 steps by the z-march (large grids)
-  Seis2March s2m[2];      // its tensor maps over copy p
-  Launch march_launch;
   Launch launch1;       // single-pass geometry
   int res_state = 0;    // on-chip runs: 0 not yet checked, 1 usable, -1 not usable
   ResPlan res_plan;     // electromag2
@@ -480,23 +477,6 @@ bool bind_args(sfd_handle* h) {
       }
       h->zb = single_pass_zb(c.kind, NX, NZ);
       if (h->single) h->launch1 = seis2_step_launch(h->s2s[0], h->zb);
-      // grids that give the z-march at least two blocks per SM take it
-      // (seis2_march.cu); smaller ones keep the tiles
-      h->s2march = false;
-#ifndef SFD_NO_MARCH  // build-time switch for timing the tiles against the march
-      if (h->single && (long)((NX + 123) / 124) * ((NZ + 15) / 16) >= 2L * 152) {
-        const long bxn = (NX + 123) / 124;
-        const int seg = std::max(16, (int)((NZ * bxn + 152 * 6 - 1) / (152 * 6)));
-        for (int p = 0; p < 2; ++p) {
-          if (!seis2_march_prepare(h->s2s[p], L.fsz, h->coef(0), L.coef_plane, &h->s2m[p])) return false;
-          h->s2m[p].seg = seg;
-          h->s2m[p].wait_ns = h->wait_ns;
-          h->s2m[p].stall_tx = h->stall_waits ? 16u : 0u;
-        }
-        h->s2march = true;
-        h->march_launch = seis2_march_launch(h->s2s[0], seg);
-      }
-#endif
       break;
     }
     case SFD_SEISMIC25: {
@@ -575,7 +555,6 @@ void set_atten(sfd_handle* h, int atten) {
 // One single-pass step reading copy p (graph capture passes p explicitly).
 void launch_step(sfd_handle* h, int p, int rel, cudaStream_t s) {
   if (h->cfg.kind == SFD_ELECTROMAG2) em2_step(h->em2s[p], h->launch1, h->zb, rel, s);
-  else if (h->s2march) seis2_march(h->s2s[p], h->s2m[p], h->march_launch, rel, s);
   else seis2_step(h->s2s[p], h->launch1, h->zb, rel, s);
 }
 
@@ -890,7 +869,7 @@ int32_t create_handle(const sfd_config* cfg, void* dev_state, size_t state_bytes
   if (!bind_args(h)) {
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
     delete h;
-    return fail(SFD_ERR_CUDA, "could not set up the staged tiles (tensor maps or shared-memory size)");
+    return fail(SFD_ERR_CUDA, "could not set up the 2.5-D kernels' staged tiles (tensor maps or shared-memory size)");
   }
   e = cudaMemsetAsync(h->base, 0, L.total, h->stream);
   if (e != cudaSuccess) { cudaStreamDestroy(h->cap_stream); delete h; return cuda_fail(e, "cudaMemsetAsync"); }
@@ -1592,8 +1571,8 @@ int32_t sfd_status(sfd_handle* h, int64_t* step, double* maxnorm) {
   if (maxnorm) *maxnorm = (double)ctl.maxnorm;
   if (ctl.err)
     return fail(SFD_ERR_TIMEOUT,
-                (h->cfg.kind == SFD_SEISMIC25 || h->cfg.kind == SFD_ELECTROMAG25 || h->s2march)
-                    ? "step: a staged tile did not arrive within %.3g s"
+                (h->cfg.kind == SFD_SEISMIC25 || h->cfg.kind == SFD_ELECTROMAG25)
+                    ? "2.5-D step: a staged tile did not arrive within %.3g s"
                                              : "on-chip run: a neighbouring tile did not answer within %.3g s",
                 (double)h->wait_ns * 1e-9);
   if (!(ctl.maxnorm <= 1.0e25f))
@@ -1608,7 +1587,6 @@ int32_t sfd_set_wait_limit(sfd_handle* h, int64_t ns) {
   h->wait_ns = ns == 0 ? kDefaultWaitNs : (unsigned long long)ns;
   h->s25.wait_ns = h->wait_ns;
   h->em25.wait_ns = h->wait_ns;
-  h->s2m[0].wait_ns = h->s2m[1].wait_ns = h->wait_ns;
   invalidate_graph(h);
   return SFD_OK;
 }
@@ -1619,7 +1597,6 @@ int32_t sfd_test_stall_waits(sfd_handle* h, int32_t on) {
   h->stall_waits = on != 0;
   h->s25.stall_tx = h->stall_waits ? 16u : 0u;
   h->em25.stall_tx = h->stall_waits ? 16u : 0u;
-  h->s2m[0].stall_tx = h->s2m[1].stall_tx = h->stall_waits ? 16u : 0u;
   invalidate_graph(h);
   return SFD_OK;
 }
@@ -2514,14 +2491,6 @@ int32_t sfd_share_model(sfd_handle* dst, const sfd_handle* src) {
         t.B55 = e.B55; t.dtrx = e.dtrx; t.dtrz = e.dtrz; t.gxp = e.gxp; t.gzp = e.gzp;
       }
       set_atten(dst, src->s2.atten);
-      if (dst->s2march)  // the z-march stages the shared coefficient planes
-        for (int p = 0; p < 2; ++p) {
-          Seis2March m = dst->s2m[p];
-          if (!seis2_march_prepare(dst->s2s[p], dst->L.fsz, src->coef(0), src->L.coef_plane, &m))
-            return fail(SFD_ERR_CUDA, "could not set up the seismic2 z-march's staged rows");
-          dst->s2m[p].tm_cs = m.tm_cs;
-          dst->s2m[p].tm_cv = m.tm_cv;
-        }
       break;
     }
     default:

@@ -161,16 +161,6 @@ struct Seis2Step {
   IoArgs io;
 };
 
-// The z-march form of the seismic2 single-pass step (seis2_march.cu): TMA
-// descriptors over one copy of the fields (vx vz sxx szz sxz) and over the
-// twelve coefficient planes, and the march's rows per block.
-struct Seis2March {
-  CUtensorMap tm_v, tm_s, tm_cs, tm_cv;
-  int seg;
-  unsigned stall_tx;           // test aid: extra bytes each stage expects (0; > 0 makes the waits run out)
-  unsigned long long wait_ns;  // bound of each wait for a staged row
-};
-
 // A material table passed by value to the coefficient kernels of
 // sfd_set_model_ids: nmat rows of the kind's model planes, FP64.
 constexpr int kMatTableMax = 2048;
@@ -189,11 +179,6 @@ struct Launch {
   dim3 grid, block;
   int nslots;
 };
-
-bool seis2_march_prepare(const Seis2Step& a, size_t field_stride, const float* coef, size_t coef_plane,
-                         Seis2March* out);
-Launch seis2_march_launch(const Seis2Step& a, int seg);
-void seis2_march(const Seis2Step& a, const Seis2March& m, const Launch& L, int rel, cudaStream_t s);
 
 Launch em2c_launch(const Em2cArgs& a);
 void em2c_half1(const Em2cArgs& a, const Launch& L, int rel, cudaStream_t s);

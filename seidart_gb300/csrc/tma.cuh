@@ -84,15 +84,6 @@ __device__ __forceinline__ void load_4d(void* dst, const CUtensorMap* map, uint6
       : "memory");
 }
 
-// 3-D tile load, as load_4d.
-__device__ __forceinline__ void load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], "
-      "[%2];" ::"r"(smem_addr(dst)),
-      "l"(map), "r"(smem_addr(bar)), "r"(c0), "r"(c1), "r"(c2)
-      : "memory");
-}
-
 // 2-D tile load, as load_4d.
 __device__ __forceinline__ void load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1) {
   asm volatile(

@@ -1,8 +1,7 @@
-"""The z-march form of the single-pass seismic2 step (seis2_march.cu), which
-grids large enough to give it two blocks per SM take when they do not run on
-chip, against the FP64 oracle: the default physics, the legacy quirks, a
-density method with a moment-tensor source, and attenuation; and against the
-two-pass form of the same handle."""
+"""seismic2 one launch per step (the single-pass tiles) on grids too large to
+run on chip, against the FP64 oracle: the default physics, the legacy
+quirks, a density method with a moment-tensor source, NZ > NX, and
+attenuation; and against the two-pass form of the same handle."""
 import numpy as np
 import pytest
 
@@ -13,17 +12,10 @@ from seidart_gb300.solver import FLAG_STREAMING, FLAG_TWO_PASS
 pytestmark = pytest.mark.gpu
 
 
-def _takes_march(nx, nz):
-    """The handle's rule (sfd_api.cu, bind_args): 124-column blocks x 16-row
-    segments >= 2 x 152."""
-    return ((nx + 123) // 124) * ((nz + 15) // 16) >= 2 * 152
-
-
 def _case(seed=21, nx=1310, nz=530, **kw):
     c = sy.small_case(SEISMIC2, seed=seed, nx=nx, nz=nz, npml=10, nstep=110, nrec=12)
     for k, v in kw.items():
         setattr(c, k, v)
-    assert _takes_march(nx, nz)
     return c
 
 
@@ -36,7 +28,7 @@ def _run(case, flags):
 
 
 @pytest.mark.parametrize("variant", ["default", "legacy", "harmonic+stress", "nz>nx"])
-def test_march_matches_oracle(gpu, variant):
+def test_large_grid_matches_oracle(gpu, variant):
     if variant == "legacy":
         case = _case(legacy=True)
     elif variant == "harmonic+stress":
@@ -55,7 +47,7 @@ def test_march_matches_oracle(gpu, variant):
         assert rel_l2(f, st.fields[q]) <= 1e-5, q
 
 
-def test_march_agrees_with_two_pass(gpu):
+def test_large_grid_agrees_with_two_pass(gpu):
     case = _case(seed=24)
     ta, fa = _run(case, FLAG_STREAMING)
     tb, fb = _run(case, FLAG_TWO_PASS)
@@ -64,7 +56,7 @@ def test_march_agrees_with_two_pass(gpu):
         assert rel_l2(a, b) <= 1e-6
 
 
-def test_march_graph_chunks_and_split_runs(gpu):
+def test_large_grid_graph_chunks_and_split_runs(gpu):
     """Runs split across the 32-step graph chunks and odd lengths."""
     case = _case(seed=25)
     with make_solver(case, flags=FLAG_STREAMING) as s:

@@ -104,26 +104,3 @@ def test_2p5d_staged_tiles_time_out(gpu, kind):
     _, ref, _, _ = run_oracle(case)
     assert rel_l2(tr, ref) <= 1e-5
 
-
-def test_seismic2_march_staged_rows_time_out(gpu):
-    """The z-march form of the seismic2 step (large grids, one launch per
-    step) waits on mbarriers for its TMA-staged rows."""
-    from seidart_gb300.solver import FLAG_STREAMING
-    L = _lib.lib()
-    case = sy.small_case(SEISMIC2, seed=9, nx=1310, nz=530, npml=10, nstep=40)
-    with make_solver(case, flags=FLAG_STREAMING) as s:
-        s.set_wait_limit(LIMIT_NS)
-        assert L.sfd_test_stall_waits(s._h, 1) == 0
-        s.run(3)
-        with pytest.raises(SfdError) as e:
-            s.status()
-        assert e.value.code == SFD_ERR_TIMEOUT
-        assert "staged tile" in str(e.value)
-        assert L.sfd_test_stall_waits(s._h, 0) == 0
-        s.set_wait_limit(0)
-        s.reset()
-        s.run(case.nstep)
-        s.status()
-        tr = s.traces()
-    _, ref, _, _ = run_oracle(case)
-    assert rel_l2(tr, ref) <= 1e-5
