@@ -396,7 +396,8 @@ def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000, 
 def bench_adjoint(device, ckpt_every=200, nstep=6000, fd_cells=0):
     """Adjoint gradient on the layered electromag2 model (6000 steps, 100 receivers): misfit against
     the unperturbed model's traces, current model with six +-5% Gaussian blobs in eps11 and eps33
-    (seed 6), checkpoints every 200 steps with recompute.  Reports backward / forward wall time."""
+    (seed 6), checkpoints every 200 steps with recompute.  Reports backward / forward wall time, and
+    the same for the recompute-free form that keeps every forward state."""
     import torch
     from seidart_gb300 import synthetic as sy
     from seidart_gb300.adjoint import TraceModel
@@ -435,13 +436,33 @@ def bench_adjoint(device, ckpt_every=200, nstep=6000, fd_cells=0):
     s.status()
     t_plain = time.perf_counter() - t0
     m.close()
+    # the recompute-free form: every forward state kept in HBM, the backward pass only sweeps
+    mr = TraceModel(case.grid, base, case.profiles, case.src_ijk, case.srcfn, case.rec_ijk, device=device,
+                    record=True)
+    mr.backward(mr.forward(cur[0], cur[2], cur[3]) - d_obs)  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tr_r = mr.forward(cur[0], cur[2], cur[3])
+    torch.cuda.synchronize()
+    t_fwd_r = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    r11, r33, rs, _ = mr.backward(tr_r - d_obs)
+    t_bwd_r = time.perf_counter() - t0
+    work_gb = mr.work.numel() / 1e9
+    mr.close()
+    rec_err = max(float(np.linalg.norm(a - b) / np.linalg.norm(a)) for a, b in ((g11, r11), (g33, r33), (gs, rs)))
     misfit = 0.5 * float((resid.double() ** 2).sum())
     out = {"workload": f"electromag2 1040x540 x {nstep} steps, gradient wrt eps11, eps33, sigma per cell",
            "forward_s": round(t_plain, 4), "forward_with_checkpoints_s": round(t_fwd, 4),
            "adjoint_s": round(t_bwd, 4), "adjoint_over_forward": round(t_bwd / t_plain, 3),
            "whole_gradient_over_forward": round((t_fwd + t_bwd) / t_plain, 3),
            "checkpoints_every": ckpt_every, "misfit": misfit,
-           "grad_abs_max": [float(np.abs(g).max()) for g in (g11, g33, gs)]}
+           "grad_abs_max": [float(np.abs(g).max()) for g in (g11, g33, gs)],
+           "recorded": {"form": "every forward state kept in device memory, no recompute (sfd_adjoint_record)",
+                        "forward_recording_s": round(t_fwd_r, 4), "adjoint_s": round(t_bwd_r, 4),
+                        "adjoint_over_forward": round(t_bwd_r / t_plain, 3),
+                        "whole_gradient_over_forward": round((t_fwd_r + t_bwd_r) / t_plain, 3),
+                        "workspace_gb": round(work_gb, 2), "grad_rel_l2_vs_checkpointed": rec_err}}
     if fd_cells:
         out["parity_fd"] = adjoint_fd_check(case, base, cur, (g11, g33, gs), fd_cells)
     return out

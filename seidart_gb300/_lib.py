@@ -27,7 +27,7 @@ EXPORTS = (
     "sfd_get_field_async", "sfd_encode_field_i16",
     "sfd_get_memory", "sfd_run", "sfd_status", "sfd_get_traces", "sfd_traces_device", "sfd_field_device", "sfd_launch_half",
     "sfd_on_chip", "sfd_set_wait_limit", "sfd_test_stall_waits",
-    "sfd_destroy", "sfd_checkpoint_bytes", "sfd_checkpoint_save", "sfd_checkpoint_load", "sfd_run_checkpointed",
+    "sfd_destroy", "sfd_checkpoint_bytes", "sfd_checkpoint_save", "sfd_checkpoint_load", "sfd_run_checkpointed", "sfd_adjoint_record",
     "sfd_adjoint_bytes",
     "sfd_adjoint_begin", "sfd_adjoint_segment", "sfd_adjoint_gradient", "sfd_batch_scratch_bytes", "sfd_batch_create", "sfd_batch_set_tiling", "sfd_batch_run",
     "sfd_batch_status", "sfd_batch_set_wait_limit", "sfd_batch_test_stall_waits", "sfd_batch_destroy", "sfd_electromag2_run_static",

@@ -12,6 +12,9 @@ it with its state on chip (``csrc/resident_adj.cu``); otherwise one launch per
 step does each (``csrc/adjoint_em2.cu``).  ``flags`` are the solver's
 (``FLAG_STREAMING`` selects the per-step form).  ``sfd_adjoint_gradient`` then
 applies the FP64 chain rule from the update coefficients to the model planes.
+With ``record=True`` the forward pass instead keeps every step's state in
+device memory (``sfd_adjoint_record``; about 6.7 MB a step on a 1040 x 540
+grid) and the backward pass is the adjoint sweep alone, with no recompute.
 
 ``traces = TraceMisfit.apply(eps11, eps33, sigma, model)`` is differentiable
 in torch: ``eps11``, ``eps33``, ``sigma`` (sig11 = sig33) are per-cell
@@ -48,6 +51,7 @@ def _declare(L):
         ("sfd_adjoint_bytes", i32, [P, i32, C.POINTER(sz)]),
         ("sfd_adjoint_begin", i32, [P, P, sz, i32, P]),
         ("sfd_adjoint_segment", i32, [P, i64]),
+        ("sfd_adjoint_record", i32, [P, i64]),
         ("sfd_adjoint_gradient", i32, [P, C.POINTER(C.c_double), i64]),
     ]:
         f = getattr(L, name)
@@ -65,7 +69,7 @@ class _Checkpointed:
     nplanes = 0
 
     def __init__(self, grid: GridSpec, base_planes, profiles, src_ijk, srcfn, rec_ijk, ckpt_every, device, flags,
-                 **solver_kw):
+                 record=False, **solver_kw):
         import torch
 
         self.grid = grid
@@ -73,7 +77,9 @@ class _Checkpointed:
         self.src_ijk = src_ijk
         self.srcfn = np.asarray(srcfn, dtype=np.float64)
         self.nstep = self.srcfn.shape[1]
-        self.ckpt_every = int(ckpt_every)
+        self.record = bool(record)
+        self._recorded = False
+        self.ckpt_every = self.nstep if self.record else int(ckpt_every)
         self.solver = FDTDSolver(grid, self.nstep, len(rec_ijk), device=device, flags=flags, **solver_kw)
         self.solver.set_model(self.base)
         self.solver.set_cpml(profiles)
@@ -86,7 +92,9 @@ class _Checkpointed:
         nb = C.c_size_t()
         check(L.sfd_checkpoint_bytes(h, C.byref(nb)))
         self.nseg = (self.nstep + self.ckpt_every - 1) // self.ckpt_every
-        self.ckpt = torch.empty((self.nseg, int(nb.value)), dtype=torch.uint8, device=self.solver.device)
+        self.ckpt = torch.empty((0 if self.record else self.nseg, int(nb.value)), dtype=torch.uint8,
+                                device=self.solver.device)
+        self.resid = torch.zeros((self.nstep, 2, len(rec_ijk)), dtype=torch.float32, device=self.solver.device)
         nb2 = C.c_size_t()
         check(L.sfd_adjoint_bytes(h, self.ckpt_every, C.byref(nb2)))
         self.work = torch.empty(int(nb2.value), dtype=torch.uint8, device=self.solver.device)
@@ -96,25 +104,40 @@ class _Checkpointed:
         s.set_model(planes)
         s.set_source(self.src_ijk, self.srcfn)  # the amplitude is divided by the model at the source
         s.reset()
-        check(self._L.sfd_run_checkpointed(s._h, self.nstep, C.c_void_p(self.ckpt.data_ptr()),
-                                           C.c_size_t(self.ckpt.stride(0)), self.ckpt_every))
+        if self.record:  # every state kept: the backward pass only sweeps
+            check(self._L.sfd_adjoint_begin(s._h, C.c_void_p(self.work.data_ptr()), C.c_size_t(self.work.numel()),
+                                            self.nstep, C.c_void_p(self.resid.data_ptr())))
+            check(self._L.sfd_adjoint_record(s._h, self.nstep))
+            self._recorded = True
+        else:
+            check(self._L.sfd_run_checkpointed(s._h, self.nstep, C.c_void_p(self.ckpt.data_ptr()),
+                                               C.c_size_t(self.ckpt.stride(0)), self.ckpt_every))
         s.status()
         return s.traces_tensor().clone()
 
     def _gradient(self, resid):
-        import torch
-
-        r = resid.detach().to(device=self.solver.device, dtype=torch.float32).contiguous()
         h = self.solver._h
+        self.resid.copy_(resid.detach().reshape(self.resid.shape))
+        if self.record:
+            if not self._recorded:
+                raise RuntimeError("a recorded backward pass needs the forward pass right before it")
+            self._recorded = False
+            check(self._L.sfd_adjoint_segment(h, self.nstep))
+            return self._planes()
         check(self._L.sfd_adjoint_begin(h, C.c_void_p(self.work.data_ptr()), C.c_size_t(self.work.numel()),
-                                        self.ckpt_every, C.c_void_p(r.data_ptr())))
+                                        self.ckpt_every, C.c_void_p(self.resid.data_ptr())))
         for q in reversed(range(self.nseg)):
             start = q * self.ckpt_every
             n = min(self.ckpt_every, self.nstep - start)
             check(self._L.sfd_checkpoint_load(h, C.c_void_p(self.ckpt[q].data_ptr()), start))
             check(self._L.sfd_adjoint_segment(h, n))
+        return self._planes()
+
+    def _planes(self):
+        import torch
+
         g = np.empty((self.nplanes, self.grid.nz, self.grid.nx))
-        check(self._L.sfd_adjoint_gradient(h, g.ctypes.data_as(C.POINTER(C.c_double)), g.size))
+        check(self._L.sfd_adjoint_gradient(self.solver._h, g.ctypes.data_as(C.POINTER(C.c_double)), g.size))
         torch.cuda.synchronize(self.solver.device)
         return g
 
@@ -127,14 +150,18 @@ class TraceModel(_Checkpointed):
 
     ``base_planes``: (6, NZ, NX) FP64 model (eps11 eps13 eps33 sig11 sig13 sig33);
     eps13 and sig13 stay fixed, the other planes are replaced by the inputs.
-    ``flags`` are the solver's; the handle must be single-pass.
+    ``flags`` are the solver's; the handle must be single-pass.  ``record``
+    keeps every step's state from the forward pass (the grid must run on
+    chip) so that ``backward`` needs no recompute; each ``backward`` then
+    follows its own ``forward``.
     """
 
     nplanes = 6
 
     def __init__(self, grid: GridSpec, base_planes, profiles, src_ijk, srcfn, rec_ijk, ckpt_every=200,
-                 device="cuda", flags=0):
-        super().__init__(grid, base_planes, profiles, src_ijk, srcfn, rec_ijk, ckpt_every, device, flags)
+                 device="cuda", flags=0, record=False):
+        super().__init__(grid, base_planes, profiles, src_ijk, srcfn, rec_ijk, ckpt_every, device, flags,
+                         record=record)
 
     def planes_for(self, eps11, eps33, sigma):
         p = self.base.copy()

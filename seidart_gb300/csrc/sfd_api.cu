@@ -328,6 +328,8 @@ struct sfd_handle_s {
   char* adj = nullptr;
   int adj_seg = 0;
   int adj_cur = 0;
+  int64_t adj_rec_s0 = 0;  // sfd_adjoint_record: the recorded run's first step and length (0: none)
+  int64_t adj_rec_n = 0;
   const float* adj_resid = nullptr;
   int adj_res_state = 0;  // on-chip adjoint sweeps: 0 not yet checked, 1 usable, -1 not usable
   Em2Args em2;
@@ -930,6 +932,7 @@ extern "C" {
 int32_t sfd_set_model_ids(sfd_handle* h, const int32_t* dev_ids, int32_t nmat, const double* table, int64_t count) {
   g_err.clear();
   if (!h || !dev_ids || !table) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  h->adj_rec_n = 0;  // the recorded states no longer follow from the handle
   const sfd_config& c = h->cfg;
   if (c.kind == SFD_ELECTROMAG2C)
     return fail(SFD_ERR_BAD_ARG, "material-id models are implemented for the real-valued kinds");
@@ -989,6 +992,7 @@ int32_t sfd_set_model_ids(sfd_handle* h, const int32_t* dev_ids, int32_t nmat, c
 int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
   g_err.clear();
   if (!h || !planes) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  h->adj_rec_n = 0;  // the recorded states no longer follow from the handle
   const sfd_config& c = h->cfg;
   const int NX = c.nx, NZ = c.nz;
   const size_t N2 = (size_t)NX * NZ;
@@ -1247,6 +1251,7 @@ int32_t sfd_set_model(sfd_handle* h, const double* planes, int64_t count) {
 int32_t sfd_set_cpml2d(sfd_handle* h, const double* fields, int64_t count) {
   g_err.clear();
   if (!h || !fields) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  h->adj_rec_n = 0;  // the recorded states no longer follow from the handle
   const sfd_config& c = h->cfg;
   if (!cpml2d(c)) return fail(SFD_ERR_STATE, "sfd_set_cpml2d needs a handle created with SFD_FLAG_CPML_2D");
   const size_t N2 = (size_t)c.nx * c.nz;
@@ -1274,6 +1279,7 @@ int32_t sfd_set_cpml2d(sfd_handle* h, const double* fields, int64_t count) {
 int32_t sfd_set_cpml(sfd_handle* h, const double* prof, int64_t count) {
   g_err.clear();
   if (!h || !prof) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  h->adj_rec_n = 0;  // the recorded states no longer follow from the handle
   const sfd_config& c = h->cfg;
   if (cpml2d(c)) return fail(SFD_ERR_STATE, "a SFD_FLAG_CPML_2D handle takes its CPML from sfd_set_cpml2d");
   const bool three = is3(c.kind);
@@ -1322,6 +1328,7 @@ int32_t sfd_set_source(sfd_handle* h, int32_t i, int32_t j, int32_t k, const dou
                        int32_t nstep) {
   g_err.clear();
   if (!h || !srcfn) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  h->adj_rec_n = 0;  // the recorded states no longer follow from the handle
   const sfd_config& c = h->cfg;
   if (!h->have_model) return fail(SFD_ERR_STATE, "sfd_set_source needs the model (sfd_set_model) first");
   if (ncomp != nsrc(c.kind)) return fail(SFD_ERR_BAD_ARG, "source needs %d components, got %d", nsrc(c.kind), ncomp);
@@ -1364,6 +1371,7 @@ int32_t sfd_set_stress_source(sfd_handle* h, int32_t i, int32_t j, int32_t k, co
                               int32_t nstep) {
   g_err.clear();
   if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
+  h->adj_rec_n = 0;  // the recorded states no longer follow from the handle
   const sfd_config& c = h->cfg;
   const int ns = nstress(c.kind);
   if (!ns) return fail(SFD_ERR_BAD_ARG, "stress sources apply to the seismic kinds only");
@@ -1416,6 +1424,7 @@ int32_t sfd_set_receivers(sfd_handle* h, const int32_t* ijk, int32_t nrec) {
 int32_t sfd_reset(sfd_handle* h) {
   g_err.clear();
   if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
+  h->adj_rec_n = 0;  // the recorded states no longer follow from the handle
   const Layout& L = h->L;
   CK(cudaMemsetAsync(h->base + L.off_fields, 0, L.off_coef - L.off_fields, h->stream));
   CK(cudaMemsetAsync(h->base + L.off_traces, 0, L.off_slots - L.off_traces, h->stream));
@@ -1427,6 +1436,7 @@ int32_t sfd_reset(sfd_handle* h) {
 int32_t sfd_set_field(sfd_handle* h, int32_t field, const float* host, int64_t count) {
   g_err.clear();
   if (!h || !host) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  h->adj_rec_n = 0;  // the recorded states no longer follow from the handle
   const sfd_config& c = h->cfg;
   if (field < 0 || field >= nfields(c.kind)) return fail(SFD_ERR_BAD_ARG, "field %d out of range", field);
   if (count != (int64_t)c.nx * c.ny * c.nz) return fail(SFD_ERR_BAD_ARG, "field needs %d*%d*%d values", c.nx, c.ny, c.nz);
@@ -1509,6 +1519,7 @@ int32_t sfd_get_memory(sfd_handle* h, int32_t index, float* host, int64_t count)
 int32_t sfd_run(sfd_handle* h, int64_t nsteps) {
   g_err.clear();
   if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");
+  h->adj_rec_n = 0;  // the recorded states no longer follow from the handle
   if (!h->have_model || !h->have_cpml) return fail(SFD_ERR_STATE, "sfd_run needs sfd_set_model and sfd_set_cpml first");
   if (nsteps < 0) return fail(SFD_ERR_BAD_ARG, "nsteps must be >= 0");
   if (h->step + nsteps > h->cfg.nstep)
@@ -2197,6 +2208,7 @@ int32_t sfd_checkpoint_save(sfd_handle* h, void* dev_dst) {
 int32_t sfd_checkpoint_load(sfd_handle* h, const void* dev_src, int64_t step) {
   g_err.clear();
   if (!h || !dev_src) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  h->adj_rec_n = 0;  // the recorded states no longer follow from the handle
   if (step < 0 || step > h->cfg.nstep) return fail(SFD_ERR_BAD_ARG, "step %lld out of range", (long long)step);
   const char* d = (const char*)dev_src;
   const size_t fb = sizeof(float) * h->L.fsz;
@@ -2285,8 +2297,117 @@ int32_t sfd_adjoint_begin(sfd_handle* h, void* dev_work, size_t bytes, int32_t s
   h->adj_seg = seg_steps;
   h->adj_cur = 0;
   h->adj_resid = dev_resid;
+  h->adj_rec_n = 0;
   CK(cudaMemsetAsync(h->adj, 0, adj_slots(h, seg_steps), h->stream));  // adjoint states, gradients, accumulators
   CK(cudaMemsetAsync(&((Ctl*)(h->base + h->L.off_ctl))->err, 0, sizeof(int), h->stream));
+  return SFD_OK;
+}
+
+// Adjoint slot 0 <- the handle's forward state.
+static int em2_save_slot0(sfd_handle* h, const AdjLayout& A) {
+  const Layout& L = h->L;
+  const AdjState S0 = adj_state_at(A, h->adj + A.slots);
+  const size_t fb = sizeof(float) * L.fsz;
+  CK(cudaMemcpyAsync(S0.Ex, h->f(0), fb, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(S0.Ez, h->f(1), fb, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(S0.Hy, h->f(2), fb, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(S0.A, h->m(0), sizeof(float) * L.mem_sz[0], cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(S0.B, h->m(1), sizeof(float) * L.mem_sz[1], cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(S0.C, h->m(2), sizeof(float) * L.mem_sz[2], cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(S0.D, h->m(3), sizeof(float) * L.mem_sz[3], cudaMemcpyDeviceToDevice, h->stream));
+  return SFD_OK;
+}
+
+// Offsets of Ex Ez Hy A B C D inside one adjoint slot.
+static void em2_slot_offsets(const AdjLayout& A, size_t off[7]) {
+  const size_t F = A.field, ZS = A.zstrip, XS = A.xstrip;
+  const size_t o[7] = {0, F, 2 * F, 3 * F, 3 * F + 2 * ZS, 3 * F + ZS, 3 * F + 2 * ZS + XS};
+  for (int q = 0; q < 7; ++q) off[q] = o[q];
+}
+
+// The on-chip forward run from slot 0 (the state before step s0) that dumps
+// the state after step s0 + s into slot s + 1 and leaves the handle's state
+// as it was.
+static Em2Resident em2_dump_args(sfd_handle* h, const AdjLayout& A, int64_t s0, int64_t nsteps) {
+  const AdjState S0 = adj_state_at(A, h->adj + A.slots);
+  Em2Resident fr = resident_args(h, nsteps);
+  fr.Ex = S0.Ex; fr.Ez = S0.Ez; fr.Hy = S0.Hy;
+  fr.mExz = S0.A; fr.mEzx = S0.B; fr.mHyz = S0.C; fr.mHyx = S0.D;
+  fr.t0 = (int)s0;
+  fr.dump.base = h->adj + A.slots;
+  fr.dump.stride = A.state;
+  em2_slot_offsets(A, fr.dump.off);
+  return fr;
+}
+
+// The on-chip adjoint sweep of steps s0 + nsteps - 1 down to s0 over the
+// states in slots 0 .. nsteps, in place on the current adjoint state.
+static int em2_adjoint_sweep_on_chip(sfd_handle* h, const AdjLayout& A, int64_t s0, int64_t nsteps) {
+  const Layout& L = h->L;
+  const AdjState Lc = adj_state_at(A, h->adj + A.lam[h->adj_cur]);
+  const Em2Args& e = h->em2;
+  const Em2Resident fr = resident_args(h, nsteps);
+  Em2AdjResident ar;
+  ar.NX = h->cfg.nx; ar.NZ = h->cfg.nz; ar.P = L.P; ar.W = L.W;
+  ar.Lx = Lc.Ex; ar.Lz = Lc.Ez; ar.Lh = Lc.Hy; ar.LA = Lc.A; ar.LB = Lc.B; ar.LC = Lc.C; ar.LD = Lc.D;
+  ar.CAx = e.CAx; ar.CBx = e.CBx; ar.CAz = e.CAz; ar.CBz = e.CBz;
+  ar.X = e.X; ar.Z = e.Z; ar.dbH = e.dbH;
+  ar.gCAx = (float*)(h->adj + A.g[0]); ar.gCBx = (float*)(h->adj + A.g[1]);
+  ar.gCAz = (float*)(h->adj + A.g[2]); ar.gCBz = (float*)(h->adj + A.g[3]);
+  ar.srcacc = (float*)(h->adj + A.acc);
+  ar.srcfn = (const float*)(h->base + L.off_src);
+  ar.nstep = h->cfg.nstep; ar.si = e.io.si; ar.sk = e.io.sk;
+  ar.rec = (const int*)(h->base + L.off_rec); ar.nrec = h->cfg.nrec; ar.resid = h->adj_resid;
+  ar.slots = h->adj + A.slots;
+  ar.stride = A.state;
+  em2_slot_offsets(A, ar.off);
+  ar.s0 = (int)s0;
+  ar.nsteps = (int)nsteps;
+  ar.ctl = (Ctl*)(h->base + L.off_ctl);
+  ar.plan = h->res_plan;
+  ar.r = fr.r;
+  ar.limit_ns = fr.limit_ns;
+  CK(cudaMemsetAsync(h->base + L.off_res, 0, res_scratch_bytes(L.P, L.NZ), h->stream));
+  CK(em2_adj_resident_launch(ar, h->stream));
+  CK(cudaGetLastError());
+  return SFD_OK;
+}
+
+int32_t sfd_adjoint_record(sfd_handle* h, int64_t nsteps) {
+  g_err.clear();
+  int r = adj_check(h);
+  if (r) return r;
+  if (!h->adj) return fail(SFD_ERR_STATE, "call sfd_adjoint_begin first");
+  if (h->cfg.kind != SFD_ELECTROMAG2 || !adjoint_on_chip(h))
+    return fail(SFD_ERR_BAD_ARG, "sfd_adjoint_record needs an electromag2 handle whose runs stay on chip");
+  if (nsteps < 1 || nsteps > h->adj_seg)
+    return fail(SFD_ERR_BAD_ARG, "recorded run of %lld steps outside [1, %d]", (long long)nsteps, h->adj_seg);
+  if (h->step + nsteps > h->cfg.nstep) return fail(SFD_ERR_BAD_ARG, "recorded run goes past the source length");
+  const AdjLayout A = adj_layout(h, h->adj_seg);
+  const Layout& L = h->L;
+  Ctl* ctl = (Ctl*)(h->base + L.off_ctl);
+  float* slots = (float*)(h->base + L.off_slots);
+  r = em2_save_slot0(h, A);
+  if (r) return r;
+  k_begin<<<std::min(1024, (L.nslots + 255) / 256 + 1), 256, 0, h->stream>>>(ctl, slots, L.nslots, (int)h->step);
+  CK(cudaMemsetAsync(h->base + L.off_res, 0, res_scratch_bytes(L.P, L.NZ), h->stream));
+  const Em2Resident own = resident_args(h, nsteps);
+  CK(em2_resident_launch(em2_dump_args(h, A, h->step, nsteps), h->stream));  // receivers recorded as in sfd_run
+  k_reduce_slots<<<1, 1024, 0, h->stream>>>(ctl, slots, L.nslots);
+  // the dumping launch keeps the handle's state: take the last slot's
+  const AdjState Sn = adj_state_at(A, h->adj + A.slots + A.state * (size_t)nsteps);
+  const size_t fb = sizeof(float) * L.fsz;
+  CK(cudaMemcpyAsync(own.Ex, Sn.Ex, fb, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(own.Ez, Sn.Ez, fb, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(own.Hy, Sn.Hy, fb, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(own.mExz, Sn.A, sizeof(float) * L.mem_sz[0], cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(own.mEzx, Sn.B, sizeof(float) * L.mem_sz[1], cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(own.mHyz, Sn.C, sizeof(float) * L.mem_sz[2], cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(own.mHyx, Sn.D, sizeof(float) * L.mem_sz[3], cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaGetLastError());
+  h->adj_rec_s0 = h->step;
+  h->adj_rec_n = nsteps;
+  h->step += nsteps;
   return SFD_OK;
 }
 
@@ -2296,64 +2417,27 @@ int32_t sfd_adjoint_segment(sfd_handle* h, int64_t nsteps) {
   if (r) return r;
   if (!h->adj) return fail(SFD_ERR_STATE, "call sfd_adjoint_begin first");
   if (nsteps < 1 || nsteps > h->adj_seg) return fail(SFD_ERR_BAD_ARG, "segment of %lld steps outside [1, %d]", (long long)nsteps, h->adj_seg);
+  if (h->adj_rec_n == nsteps && h->adj_rec_s0 + nsteps == h->step) {
+    // sfd_adjoint_record ran these steps and kept every state: sweep only
+    h->adj_rec_n = 0;
+    return em2_adjoint_sweep_on_chip(h, adj_layout(h, h->adj_seg), h->adj_rec_s0, nsteps);
+  }
+  h->adj_rec_n = 0;
   const int64_t s0 = h->step;
   if (s0 + nsteps > h->cfg.nstep) return fail(SFD_ERR_BAD_ARG, "segment runs past the source length");
   if (h->cfg.kind == SFD_SEISMIC2) return s2_adjoint_segment(h, nsteps);
   const AdjLayout A = adj_layout(h, h->adj_seg);
   const Layout& L = h->L;
   const int NX = h->cfg.nx, NZ = h->cfg.nz;
-  // slot 0 <- current forward state
-  AdjState S0 = adj_state_at(A, h->adj + A.slots);
-  const size_t fb = sizeof(float) * L.fsz;
-  CK(cudaMemcpyAsync(S0.Ex, h->f(0), fb, cudaMemcpyDeviceToDevice, h->stream));
-  CK(cudaMemcpyAsync(S0.Ez, h->f(1), fb, cudaMemcpyDeviceToDevice, h->stream));
-  CK(cudaMemcpyAsync(S0.Hy, h->f(2), fb, cudaMemcpyDeviceToDevice, h->stream));
-  CK(cudaMemcpyAsync(S0.A, h->m(0), sizeof(float) * L.mem_sz[0], cudaMemcpyDeviceToDevice, h->stream));
-  CK(cudaMemcpyAsync(S0.B, h->m(1), sizeof(float) * L.mem_sz[1], cudaMemcpyDeviceToDevice, h->stream));
-  CK(cudaMemcpyAsync(S0.C, h->m(2), sizeof(float) * L.mem_sz[2], cudaMemcpyDeviceToDevice, h->stream));
-  CK(cudaMemcpyAsync(S0.D, h->m(3), sizeof(float) * L.mem_sz[3], cudaMemcpyDeviceToDevice, h->stream));
+  r = em2_save_slot0(h, A);
+  if (r) return r;
   if (adjoint_on_chip(h)) {
     // forward recompute on chip: slot s + 1 <- the state after step s0 + s
-    Em2Resident fr = resident_args(h, nsteps);
-    fr.Ex = S0.Ex; fr.Ez = S0.Ez; fr.Hy = S0.Hy;
-    fr.mExz = S0.A; fr.mEzx = S0.B; fr.mHyz = S0.C; fr.mHyx = S0.D;
-    fr.t0 = (int)s0;
+    Em2Resident fr = em2_dump_args(h, A, s0, nsteps);
     fr.io.nrec = 0;
-    fr.dump.base = h->adj + A.slots;
-    fr.dump.stride = A.state;
-    const size_t F = A.field, ZS = A.zstrip, XS = A.xstrip;
-    const size_t off[7] = {0, F, 2 * F, 3 * F, 3 * F + 2 * ZS, 3 * F + ZS, 3 * F + 2 * ZS + XS};  // Ex Ez Hy A B C D
-    for (int q = 0; q < 7; ++q) fr.dump.off[q] = off[q];
-    const size_t rb = res_scratch_bytes(L.P, L.NZ);
-    CK(cudaMemsetAsync(h->base + L.off_res, 0, rb, h->stream));
+    CK(cudaMemsetAsync(h->base + L.off_res, 0, res_scratch_bytes(L.P, L.NZ), h->stream));
     CK(em2_resident_launch(fr, h->stream));
-    // adjoint sweep on chip, in place on the current adjoint state
-    const AdjState Lc = adj_state_at(A, h->adj + A.lam[h->adj_cur]);
-    const Em2Args& e = h->em2;
-    Em2AdjResident ar;
-    ar.NX = NX; ar.NZ = NZ; ar.P = L.P; ar.W = L.W;
-    ar.Lx = Lc.Ex; ar.Lz = Lc.Ez; ar.Lh = Lc.Hy; ar.LA = Lc.A; ar.LB = Lc.B; ar.LC = Lc.C; ar.LD = Lc.D;
-    ar.CAx = e.CAx; ar.CBx = e.CBx; ar.CAz = e.CAz; ar.CBz = e.CBz;
-    ar.X = e.X; ar.Z = e.Z; ar.dbH = e.dbH;
-    ar.gCAx = (float*)(h->adj + A.g[0]); ar.gCBx = (float*)(h->adj + A.g[1]);
-    ar.gCAz = (float*)(h->adj + A.g[2]); ar.gCBz = (float*)(h->adj + A.g[3]);
-    ar.srcacc = (float*)(h->adj + A.acc);
-    ar.srcfn = (const float*)(h->base + L.off_src);
-    ar.nstep = h->cfg.nstep; ar.si = e.io.si; ar.sk = e.io.sk;
-    ar.rec = (const int*)(h->base + L.off_rec); ar.nrec = h->cfg.nrec; ar.resid = h->adj_resid;
-    ar.slots = h->adj + A.slots;
-    ar.stride = A.state;
-    for (int q = 0; q < 7; ++q) ar.off[q] = off[q];
-    ar.s0 = (int)s0;
-    ar.nsteps = (int)nsteps;
-    ar.ctl = (Ctl*)(h->base + L.off_ctl);
-    ar.plan = h->res_plan;
-    ar.r = fr.r;
-    ar.limit_ns = fr.limit_ns;
-    CK(cudaMemsetAsync(h->base + L.off_res, 0, rb, h->stream));
-    CK(em2_adj_resident_launch(ar, h->stream));
-    CK(cudaGetLastError());
-    return SFD_OK;
+    return em2_adjoint_sweep_on_chip(h, A, s0, nsteps);
   }
   // forward recompute: slot s -> slot s+1
   k_begin<<<std::min(1024, (L.nslots + 255) / 256 + 1), 256, 0, h->stream>>>((Ctl*)(h->base + L.off_ctl),

@@ -195,3 +195,55 @@ def test_run_checkpointed_matches_save_and_run(gpu, flags):
     (ca, ta, ea), (cb, tb, eb) = out
     assert np.array_equal(ca, cb)
     assert np.array_equal(ta, tb) and np.array_equal(ea, eb)
+
+
+@pytest.mark.parametrize("grid", ["small", "layered"])
+def test_recorded_adjoint_matches_checkpointed(gpu, grid):
+    """sfd_adjoint_record keeps every forward state so that the backward pass
+    is the sweep alone.  Its forward pass is the same on-chip kernel as a run
+    (traces and final state bit for bit) and its states are the ones the
+    checkpointed form recomputes, so the gradients agree to rounding."""
+    import torch
+    if grid == "small":
+        case, cur, d_obs, _ = _setup()
+        d_obs_t = lambda tr: torch.as_tensor(d_obs, dtype=torch.float32, device=tr.device)
+    else:
+        case = sy.electromag2_layers(nstep=300)
+        case.planes[5] = case.planes[3]
+        cur = case.planes.copy()
+        cur[0] = cur[0] * 1.02
+        d_obs_t = lambda tr: torch.zeros_like(tr)
+    out = []
+    for record in (False, True):
+        m = TraceModel(case.grid, cur, case.profiles, case.src_ijk, case.srcfn, case.rec_ijk, ckpt_every=70,
+                       record=record)
+        try:
+            assert m.solver.on_chip() is not None
+            tr = m.forward(cur[0], cur[2], cur[3])
+            ex = m.solver.field("Ex")
+            _, _, _, g6 = m.backward(tr - d_obs_t(tr))
+            if record:
+                with pytest.raises(RuntimeError):
+                    m.backward(tr - d_obs_t(tr))
+            out.append((tr.cpu().numpy(), ex, g6))
+        finally:
+            m.close()
+    (ta, ea, ga), (tb, eb, gb) = out
+    assert np.array_equal(ta, tb) and np.array_equal(ea, eb)
+    for q in (0, 2, 3, 5):
+        err = np.linalg.norm(ga[q] - gb[q]) / np.linalg.norm(ga[q])
+        assert err <= 1e-6, f"plane {q}: relative L2 {err:.3e}"
+
+
+def test_record_refused_off_chip(gpu):
+    """A handle whose runs are not on chip cannot record: the C call says so."""
+    from seidart_gb300._lib import SfdError
+    from seidart_gb300.solver import FLAG_STREAMING
+    case, cur, _, _ = _setup()
+    m = TraceModel(case.grid, cur, case.profiles, case.src_ijk, case.srcfn, case.rec_ijk, flags=FLAG_STREAMING,
+                   record=True)
+    try:
+        with pytest.raises(SfdError, match="on chip"):
+            m.forward(cur[0], cur[2], cur[3])
+    finally:
+        m.close()
