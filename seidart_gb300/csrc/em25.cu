@@ -8,6 +8,7 @@
 // The H faces (:1057-1078) are zeroed at the end of a Fortran step, after the
 // E update has read them; half1 treats the previous H on those faces as zero
 // and the finalize kernels zero them in memory at the end of each run.
+#include <type_traits>
 #include "sfd_solvers.h"
 #include "tma.cuh"
 
@@ -48,6 +49,14 @@ constexpr int STAGE = YTB + 32;      // 5632 bytes
 constexpr int FH = VH * VW;          // one field of a halo tile
 static_assert(OWN >= HALO3 && (OWN * 4) % 128 == 0 && (PSI * 4) % 128 == 0 && (YTB * 4) % 128 == 0 &&
                   (STAGE * 4) % 128 == 0, "stage alignment");
+
+// Whether every column of the block at (i0, k0) lies off the x and z CPML
+// strips and two cells or more inside the grid (off every Dirichlet face of
+// E and H: 1 <= i <= NX - 3, 1 <= k <= NZ - 3).
+__device__ __forceinline__ bool block_interior(int i0, int k0, int NX, int NZ, int W) {
+  return i0 >= max(W, 1) && i0 + BX - 1 <= min(NX - W - 1, NX - 3) && k0 >= max(W, 1) &&
+         k0 + BZ - 1 <= min(NZ - W - 1, NZ - 3);
+}
 
 __device__ void em25_wait_failed(const Em25Args& a, uint64_t* full, int n, int np) {
   atomicExch(const_cast<int*>(&a.io.ctl->err), 1);
@@ -94,19 +103,20 @@ __global__ void __launch_bounds__(BX * BZ) em25_h_tma_kernel(const __grid_consta
     for (int n = 0; n < min(RING, np); ++n) issue(n);
 
   const int i = i0 + tx, k = k0 + ty;
-  const bool active = i <= NX - 2 && k <= NZ - 2;
-  const int ic = active ? i : 0, kc = active ? k : 0;
-  const bool xs = active && in_strip(i, NX, W), zs = active && in_strip(k, NZ, W);
-  const int xsi = xs ? strip_idx(i, NX, W) : 0;
-  const int zsi = zs ? strip_idx(k, NZ, W) : 0;
+  const bool activec = i <= NX - 2 && k <= NZ - 2;
+  const int ic = activec ? i : 0, kc = activec ? k : 0;
+  const bool xsc = activec && in_strip(i, NX, W), zsc = activec && in_strip(k, NZ, W);
+  const int xsi = xsc ? strip_idx(i, NX, W) : 0;
+  const int zsi = zsc ? strip_idx(k, NZ, W) : 0;
   const float ikx = a.X.ik[ic], adx = a.X.ad[ic], bx = a.X.b[ic];
   const float ikz = a.Z.ik[kc], adz = a.Z.ad[kc], bz = a.Z.b[kc];
   const float ikzh = a.Z.ikh[kc], adzh = a.Z.adh[kc], bzh = a.Z.bh[kc];
   const float dbH = a.dbH;
-  const bool hz_rows = (k >= 1);
-  const bool fx_x = (i == 0) || (k == 0) || (k == NZ - 2);
-  const bool fy_x = (i == 0) || (i == NX - 2) || (k == 0) || (k == NZ - 2);
-  const bool fz_x = (i == 0) || (i == NX - 2) || (k == 0);
+  const bool hz_rowsc = (k >= 1);
+  const bool fx_xc = (i == 0) || (k == 0) || (k == NZ - 2);
+  const bool fy_xc = (i == 0) || (i == NX - 2) || (k == 0) || (k == NZ - 2);
+  const bool fz_xc = (i == 0) || (i == NX - 2) || (k == 0);
+  const bool interior = block_interior(i0, k0, NX, NZ, W);
   float* __restrict__ Hx_ = a.Hx;
   float* __restrict__ Hy_ = a.Hy;
   float* __restrict__ Hz_ = a.Hz;
@@ -119,6 +129,12 @@ __global__ void __launch_bounds__(BX * BZ) em25_h_tma_kernel(const __grid_consta
   const int hc = (ty + 1) * VW + tx + HX;  // own cell in a halo tile
   const int oc = ty * BX + tx;             // own cell in an own-cells tile
   size_t c = ((size_t)kc * NY + j0) * P + ic;
+  // The march, compiled twice: for blocks of interior columns only (I: no x
+  // or z memory variables, no faces) and for the others.
+  auto march = [&](auto interior_tag) {
+  constexpr bool I = decltype(interior_tag)::value;
+  const bool active = I || activec, xs = !I && xsc, zs = !I && zsc, hz_rows = I || hz_rowsc;
+  const bool fx_x = !I && fx_xc, fy_x = !I && fy_xc, fz_x = !I && fz_xc;
   for (int n = 0; n < j1 - j0; ++n, c += P) {
     const int j = j0 + n;
     bool ok = tma::bar_wait(full + n % RING, (n / RING) & 1, a.wait_ns);
@@ -175,6 +191,9 @@ __global__ void __launch_bounds__(BX * BZ) em25_h_tma_kernel(const __grid_consta
       issue(n + RING);
     }
   }
+  };
+  if (interior) march(std::true_type{});
+  else march(std::false_type{});
 }
 
 __global__ void __launch_bounds__(BX * BZ) em25_e_tma_kernel(const __grid_constant__ Em25Args a, int rel) {
@@ -214,11 +233,11 @@ __global__ void __launch_bounds__(BX * BZ) em25_e_tma_kernel(const __grid_consta
     for (int n = 0; n < min(RING, np); ++n) issue(n);
 
   const int i = i0 + tx, k = k0 + ty;
-  const bool inside = i < NX && k < NZ;
-  const int ic = inside ? i : 0, kc = inside ? k : 0;
-  const bool XEx = inside && (k >= 1) && (k <= NZ - 2) && (i <= NX - 2);
-  const bool XEy = inside && (k >= 1) && (k <= NZ - 2) && (i >= 1) && (i <= NX - 2);
-  const bool XEz = inside && (k <= NZ - 2) && (i >= 1) && (i <= NX - 2);
+  const bool insidec = i < NX && k < NZ;
+  const int ic = insidec ? i : 0, kc = insidec ? k : 0;
+  const bool XEx = insidec && (k >= 1) && (k <= NZ - 2) && (i <= NX - 2);
+  const bool XEy = insidec && (k >= 1) && (k <= NZ - 2) && (i >= 1) && (i <= NX - 2);
+  const bool XEz = insidec && (k <= NZ - 2) && (i >= 1) && (i <= NX - 2);
   const size_t pc = (size_t)kc * P + ic;
   float caX = 0, cbX = 0, caY = 0, cbY = 0, caZ = 0, cbZ = 0;
   if (XEx) { caX = a.caEx[pc]; cbX = a.cbEx[pc]; }
@@ -230,15 +249,16 @@ __global__ void __launch_bounds__(BX * BZ) em25_e_tma_kernel(const __grid_consta
     caZ = (4.f * a.caEz[pc] + a.caEz[pc - 1] + a.caEz[pc + P]) / 6.f;
     cbZ = (4.f * a.cbEz[pc] + a.cbEz[pc - 1] + a.cbEz[pc + P]) / 6.f;
   }
-  const bool xs = inside && in_strip(i, NX, W), zs = inside && in_strip(k, NZ, W);
-  const int xsi = xs ? strip_idx(i, NX, W) : 0;
-  const int zsi = zs ? strip_idx(k, NZ, W) : 0;
+  const bool xsc = insidec && in_strip(i, NX, W), zsc = insidec && in_strip(k, NZ, W);
+  const int xsi = xsc ? strip_idx(i, NX, W) : 0;
+  const int zsi = zsc ? strip_idx(k, NZ, W) : 0;
   const float ikxh = a.X.ikh[ic], adxh = a.X.adh[ic], bxh = a.X.bh[ic];
   const float ikz = a.Z.ik[kc], adz = a.Z.ad[kc], bz = a.Z.b[kc];
   const float ikzh = a.Z.ikh[kc], adzh = a.Z.adh[kc], bzh = a.Z.bh[kc];
-  const bool fEx = (i == 0) || (i == NX - 2) || (k == 0) || (k == NZ - 1);
-  const bool fEy = (i == 0) || (i == NX - 1) || (k == 0) || (k == NZ - 1);
-  const bool fEz = (i == 0) || (i == NX - 1) || (k == 0) || (k == NZ - 2);
+  const bool fExc = (i == 0) || (i == NX - 2) || (k == 0) || (k == NZ - 1);
+  const bool fEyc = (i == 0) || (i == NX - 1) || (k == 0) || (k == NZ - 1);
+  const bool fEzc = (i == 0) || (i == NX - 1) || (k == 0) || (k == NZ - 2);
+  const bool interior = block_interior(i0, k0, NX, NZ, W);
   float* __restrict__ Ex_ = a.Ex;
   float* __restrict__ Ey_ = a.Ey;
   float* __restrict__ Ez_ = a.Ez;
@@ -252,7 +272,13 @@ __global__ void __launch_bounds__(BX * BZ) em25_e_tma_kernel(const __grid_consta
   const int oc = ty * BX + tx;
   size_t c = ((size_t)kc * NY + j0) * P + ic;
   float phx = 0.f, phz = 0.f;  // Hx, Hz of the plane before
-  if (inside && j0 >= 1) { phx = __ldg(a.Hx + c - P); phz = __ldg(a.Hz + c - P); }
+  if (insidec && j0 >= 1) { phx = __ldg(a.Hx + c - P); phz = __ldg(a.Hz + c - P); }
+  // compiled twice, as the H kernel's march
+  auto march = [&](auto interior_tag) {
+  constexpr bool I = decltype(interior_tag)::value;
+  const bool inside = I || insidec, xs = !I && xsc, zs = !I && zsc;
+  const bool XEx_ = I || XEx, XEy_ = I || XEy, XEz_ = I || XEz;
+  const bool fEx = !I && fExc, fEy = !I && fEyc, fEz = !I && fEzc;
   for (int n = 0; n < np; ++n, c += P) {
     const int j = j0 + n;
     const bool ok = tma::bar_wait(full + n % RING, (n / RING) & 1, a.wait_ns);
@@ -268,7 +294,7 @@ __global__ void __launch_bounds__(BX * BZ) em25_e_tma_kernel(const __grid_consta
       const float* Y = H + PSI;             // dHz_dy, dHx_dy of this plane (y strips)
       const float hx = H[hc], hy = H[FH + hc], hz = H[2 * FH + hc];
       float ex = E[oc], ey = E[OWN3 / 3 + oc], ez = E[2 * (OWN3 / 3) + oc];
-      if (XEx && j >= 1 && j <= NY - 2) {  // :971-984
+      if (XEx_ && j >= 1 && j <= NY - 2) {  // :971-984
         const float d1 = hz - phz;  // dHz/dy
         float v1 = d1 * ikyh;
         if (ys) { const float m = byh * Y[oc] + adyh * d1; mHz_y_[my] = m; v1 += m; }
@@ -277,7 +303,7 @@ __global__ void __launch_bounds__(BX * BZ) em25_e_tma_kernel(const __grid_consta
         if (zs) { const float m = bz * mHy_z_[mz] + adz * d2; mHy_z_[mz] = m; v2 += m; }
         ex = caX * ex + cbX * (v1 + v2);
       }
-      if (XEy && j <= NY - 2) {  // :988-1007
+      if (XEy_ && j <= NY - 2) {  // :988-1007
         const float d1 = H[2 * FH + hc - 1] - hz;  // dHz/dx
         float v1 = d1 * ikxh;
         if (xs) { const float m = bxh * mHz_x_[mx] + adxh * d1; mHz_x_[mx] = m; v1 += m; }
@@ -286,7 +312,7 @@ __global__ void __launch_bounds__(BX * BZ) em25_e_tma_kernel(const __grid_consta
         if (zs) { const float m = bzh * mHx_z_[mz] + adzh * d2; mHx_z_[mz] = m; v2 += m; }
         ey = caY * ey + cbY * (v1 + v2);
       }
-      if (XEz && j >= 1 && j <= NY - 2) {  // :1015-1029
+      if (XEz_ && j >= 1 && j <= NY - 2) {  // :1015-1029
         const float d1 = phx - hx;  // dHx/dy
         float v1 = d1 * ikyh;
         if (ys) { const float m = byh * Y[BZ * BX + oc] + adyh * d1; mHx_y_[my] = m; v1 += m; }
@@ -319,6 +345,9 @@ __global__ void __launch_bounds__(BX * BZ) em25_e_tma_kernel(const __grid_consta
       issue(n + RING);
     }
   }
+  };
+  if (interior) march(std::true_type{});
+  else march(std::false_type{});
   block_norm_to_slot(norm, a.io.slots, slot);
 }
 

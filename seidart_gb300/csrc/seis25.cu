@@ -38,6 +38,7 @@
 // values the Fortran's loop bounds leave there.  Staging replaced a plain
 // y-march whose every step waited a memory round trip (0.682 against 0.587
 // ms per step on the 630 x 70 x 330 grid).
+#include <type_traits>
 #include "sfd_solvers.h"
 #include "tma.cuh"
 
@@ -81,6 +82,13 @@ static_assert(S_OWN >= HALO3 && (S_OWN * 4) % 128 == 0 && (S_PSI * 4) % 128 == 0
                   (S_STAGE * 4) % 128 == 0, "stage alignment");
 static_assert((V_OWN * 4) % 128 == 0 && (V_PSI * 4) % 128 == 0 && (V_YT * 4) % 128 == 0 && (V_STAGE * 4) % 128 == 0,
               "stage alignment");
+
+// Whether every column of the block at (i0, k0) lies off the x and z CPML
+// strips and off the boundary planes (1 <= i <= NX - 2, 1 <= k <= NZ - 2).
+__device__ __forceinline__ bool block_interior(int i0, int k0, int NX, int NZ, int W) {
+  return i0 >= max(W, 1) && i0 + BX - 1 <= min(NX - W - 1, NX - 2) && k0 >= max(W, 1) &&
+         k0 + BZ - 1 <= min(NZ - W - 1, NZ - 2);
+}
 
 // Records a wait that ran out and lets the copies this block already issued
 // land (each again within the limit) before its shared memory is released.
@@ -132,11 +140,11 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS)
 
   const int i = i0 + tx, k = k0 + ty;
   const bool inside = i < NX && k < NZ;
-  const bool L1 = inside && (k >= 1) && (i <= NX - 2);
-  const bool L2 = inside && (k >= 1) && (i >= 1);
-  const bool L3 = inside && (k <= NZ - 2) && (i >= 1);
-  const bool L4 = inside && (k <= NZ - 2) && (i <= NX - 2);
-  const bool active = L1 || L2 || L3 || L4;
+  const bool L1c = inside && (k >= 1) && (i <= NX - 2);
+  const bool L2c = inside && (k >= 1) && (i >= 1);
+  const bool L3c = inside && (k <= NZ - 2) && (i >= 1);
+  const bool L4c = inside && (k <= NZ - 2) && (i <= NX - 2);
+  const bool activec = L1c || L2c || L3c || L4c;
   const int ic = inside ? i : 0, kc = inside ? k : 0;
   // the column's 33 stiffness averages, each thread's in its own row of
   // CSTRIDE floats: a loop's coefficients start on a 16-byte boundary and
@@ -147,13 +155,13 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS)
     const size_t cpl = (size_t)NZ * P, cpc = (size_t)kc * P + ic;
     auto cf = [&](int q, bool on) { return on ? __ldg(a.C + q * cpl + cpc) : 0.0f; };
 #pragma unroll
-    for (int q = 0; q < 15; ++q) cs[q] = cf(q, L1);
+    for (int q = 0; q < 15; ++q) cs[q] = cf(q, L1c);
 #pragma unroll
-    for (int q = 15; q < 21; ++q) cs[q + 1] = cf(q, L2);
+    for (int q = 15; q < 21; ++q) cs[q + 1] = cf(q, L2c);
 #pragma unroll
-    for (int q = 21; q < 27; ++q) cs[q + 3] = cf(q, L3);
+    for (int q = 21; q < 27; ++q) cs[q + 3] = cf(q, L3c);
 #pragma unroll
-    for (int q = 27; q < 33; ++q) cs[q + 5] = cf(q, L4);
+    for (int q = 27; q < 33; ++q) cs[q + 5] = cf(q, L4c);
   }
   const uint32_t cs_addr = tma::smem_addr(cs);
   // four coefficients from shared memory at each use (held in registers for
@@ -166,13 +174,14 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS)
     return v;
   };
 
-  const bool xs = inside && in_strip(i, NX, W), zs = inside && in_strip(k, NZ, W);
-  const int xsi = xs ? strip_idx(i, NX, W) : 0;
-  const int zsi = zs ? strip_idx(k, NZ, W) : 0;
+  const bool xsc = inside && in_strip(i, NX, W), zsc = inside && in_strip(k, NZ, W);
+  const int xsi = xsc ? strip_idx(i, NX, W) : 0;
+  const int zsi = zsc ? strip_idx(k, NZ, W) : 0;
   const float ikx = a.X.ik[ic], ikxh = a.X.ikh[ic], adx = a.X.ad[ic], adxh = a.X.adh[ic];
   const float bx = a.X.b[ic], bxh = a.X.bh[ic];
   const float ikz = a.Z.ik[kc], ikzh = a.Z.ikh[kc], adz = a.Z.ad[kc], adzh = a.Z.adh[kc];
   const float bz = a.Z.b[kc], bzh = a.Z.bh[kc];
+  const bool interior = block_interior(i0, k0, NX, NZ, W);
   float* __restrict__ SXX = a.sxx;
   float* __restrict__ SYY = a.syy;
   float* __restrict__ SZZ = a.szz;
@@ -190,9 +199,16 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS)
   float* __restrict__ MVZZ = a.m_vz_z;
   size_t c = ((size_t)kc * NY + j0) * P + ic;
   float pvx = 0.f, pvy = 0.f, pvz = 0.f;
-  if (active && j0 >= 1) { pvx = __ldg(a.vx + c - P); pvy = __ldg(a.vy + c - P); pvz = __ldg(a.vz + c - P); }
+  if (activec && j0 >= 1) { pvx = __ldg(a.vx + c - P); pvy = __ldg(a.vy + c - P); pvz = __ldg(a.vz + c - P); }
   const int hc = (ty + 1) * VW + tx + HX;  // own cell in a halo tile
   const int oc = ty * BX + tx;             // own cell in an own-cells tile
+  // The march, compiled twice: for blocks whose columns all lie off the x
+  // and z strips and the boundary planes (I: every loop updates every
+  // column, no x or z memory variables) and for the others.
+  auto march = [&](auto interior_tag) {
+  constexpr bool I = decltype(interior_tag)::value;
+  const bool xs = !I && xsc, zs = !I && zsc;
+  const bool L1 = I || L1c, L2 = I || L2c, L3 = I || L3c, L4 = I || L4c, active = I || activec;
   for (int n = 0; n < j1 - j0; ++n, c += P) {
     const int j = j0 + n;
     const bool more = n + 1 < np;
@@ -306,6 +322,9 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_STRESS_BLOCKS)
       issue(n + RING);
     }
   }
+  };
+  if (interior) march(std::true_type{});
+  else march(std::false_type{});
 }
 
 __global__ void __launch_bounds__(BX * BZ, SEIS25_VELOCITY_BLOCKS)
@@ -348,24 +367,25 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_VELOCITY_BLOCKS)
     for (int n = 0; n < min(RING, np); ++n) issue(n);
 
   const int i = i0 + tx, k = k0 + ty;
-  const bool inside = i < NX && k < NZ;
-  const int ic = inside ? i : 0, kc = inside ? k : 0;
-  const bool Vx = inside && (k >= 1) && (i >= 1);
-  const bool Vy = inside && (k >= 1) && (i <= NX - 2);
-  const bool Vz = inside && (k <= NZ - 2) && (i <= NX - 2);
+  const bool insidec = i < NX && k < NZ;
+  const int ic = insidec ? i : 0, kc = insidec ? k : 0;
+  const bool Vx = insidec && (k >= 1) && (i >= 1);
+  const bool Vy = insidec && (k >= 1) && (i <= NX - 2);
+  const bool Vz = insidec && (k <= NZ - 2) && (i <= NX - 2);
   const size_t pc = (size_t)kc * P + ic;
   const size_t p2 = (size_t)NZ * P;
   const float dtrx = Vx ? a.dtr[pc] : 0.f, dtry = Vy ? a.dtr[p2 + pc] : 0.f, dtrz = Vz ? a.dtr[2 * p2 + pc] : 0.f;
   float gx = 1.f, gy = 1.f, gz = 1.f;
-  if (a.atten && inside) { gx = a.gp[pc]; gy = a.gp[p2 + pc]; gz = a.gp[2 * p2 + pc]; }
-  const bool xs = inside && in_strip(i, NX, W), zs = inside && in_strip(k, NZ, W);
-  const int xsi = xs ? strip_idx(i, NX, W) : 0;
-  const int zsi = zs ? strip_idx(k, NZ, W) : 0;
+  if (a.atten && insidec) { gx = a.gp[pc]; gy = a.gp[p2 + pc]; gz = a.gp[2 * p2 + pc]; }
+  const bool xsc = insidec && in_strip(i, NX, W), zsc = insidec && in_strip(k, NZ, W);
+  const int xsi = xsc ? strip_idx(i, NX, W) : 0;
+  const int zsi = zsc ? strip_idx(k, NZ, W) : 0;
   const float ikx = a.X.ik[ic], ikxh = a.X.ikh[ic], adx = a.X.ad[ic], adxh = a.X.adh[ic];
   const float bx = a.X.b[ic], bxh = a.X.bh[ic];
   const float ikz = a.Z.ik[kc], ikzh = a.Z.ikh[kc], adz = a.Z.ad[kc], adzh = a.Z.adh[kc];
   const float bz = a.Z.b[kc], bzh = a.Z.bh[kc];
-  const bool xface = (i == 0) || (i == NX - 1) || (k == 0) || (k == NZ - 1);
+  const bool xfacec = (i == 0) || (i == NX - 1) || (k == 0) || (k == NZ - 1);
+  const bool interior = block_interior(i0, k0, NX, NZ, W);
   float* __restrict__ VX = a.vx;
   float* __restrict__ VY = a.vy;
   float* __restrict__ VZ = a.vz;
@@ -380,10 +400,15 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_VELOCITY_BLOCKS)
   float* __restrict__ MSZZZ = a.m_szz_z;
   size_t c = ((size_t)kc * NY + j0) * P + ic;
   float psxy = 0.f, psyz = 0.f;
-  if (inside && j0 >= 1) { psxy = __ldg(a.sxy + c - P); psyz = __ldg(a.syz + c - P); }
+  if (insidec && j0 >= 1) { psxy = __ldg(a.sxy + c - P); psyz = __ldg(a.syz + c - P); }
   const int hc = (ty + 1) * VW + tx + HX;
   const int oc = ty * BX + tx;
   constexpr int F = VH * VW;  // one field of a halo tile
+  // compiled twice, as the stress kernel's march
+  auto march = [&](auto interior_tag) {
+  constexpr bool I = decltype(interior_tag)::value;
+  const bool inside = I || insidec, xs = !I && xsc, zs = !I && zsc, xface = !I && xfacec;
+  const bool Vxm = I || Vx, Vym = I || Vy, Vzm = I || Vz;
   for (int n = 0; n < j1 - j0; ++n, c += P) {
     const int j = j0 + n;
     const bool more = n + 1 < np;
@@ -403,7 +428,7 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_VELOCITY_BLOCKS)
       const float* yt = S + V_YT + (j & 3);  // rows ik ad b ikh adh bh of the y table
       const float iky = yt[0], ady = yt[4], by = yt[8], ikyh = yt[12], adyh = yt[16], byh = yt[20];
       float vx = V[oc], vy = V[OWN3 / 3 + oc], vz = V[2 * (OWN3 / 3) + oc];
-      const bool ux = Vx && j >= 1, uy = Vy && j <= NY - 2, uz = Vz && j >= 1;
+      const bool ux = Vxm && j >= 1, uy = Vym && j <= NY - 2, uz = Vzm && j >= 1;
       float m1x = 0.f, m1y = 0.f, m1z = 0.f, m2x = 0.f, m2y = 0.f, m2z = 0.f, m3x = 0.f, m3y = 0.f, m3z = 0.f;
       if (xs) {
         if (ux) m1x = MSXXX[mx];
@@ -467,6 +492,9 @@ __global__ void __launch_bounds__(BX * BZ, SEIS25_VELOCITY_BLOCKS)
       issue(n + RING);
     }
   }
+  };
+  if (interior) march(std::true_type{});
+  else march(std::false_type{});
   block_norm_to_slot(norm, a.io.slots, slot);
 }
 

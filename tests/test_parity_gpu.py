@@ -44,6 +44,8 @@ CASES = [
     (SEISMIC25, 1, 50, 34, 26, 7, 70, 0),
     (ELECTROMAG25, 0, 37, 29, 21, 5, 90, 0),
     (ELECTROMAG25, 1, 50, 34, 26, 7, 70, 0),
+    (SEISMIC25, 2, 100, 30, 20, 5, 60, 0),     # wide enough for blocks of interior columns only
+    (ELECTROMAG25, 2, 100, 30, 20, 5, 60, 0),
 ]
 
 
