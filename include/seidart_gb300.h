@@ -27,7 +27,9 @@
  *   - Material arrays are FP64 (NX, NZ) planes; in 2.5-D they are y-invariant,
  *     as in the Fortran (seismicfdtd.f95:399-405, electromagfdtd.f95:633-638).
  *   - Fields are computed in FP32 on the GPU.  dt, the CPML profiles and the
- *     derived update coefficients are computed in FP64 on the host.
+ *     derived update coefficients are computed in FP64 on the host (the
+ *     profiles and the source time functions optionally in FP64 on the device:
+ *     sfd_set_cpml_params, sfd_set_source_wavelet).
  *   - The library never allocates device memory: the caller passes one device
  *     buffer of sfd_state_bytes() bytes that holds every field, CPML memory
  *     variable, coefficient, source and trace of the handle.
@@ -228,6 +230,42 @@ int32_t sfd_set_stress_source(sfd_handle* h, int32_t i, int32_t j, int32_t k, co
  * the model files each shot of the driver's survey loop reads
  * (src/seidart/simulations/common_offset.py:143-176). */
 int32_t sfd_share_model(sfd_handle* dst, const sfd_handle* src);
+
+/* ---- Input assembly on the device ------------------------------------------
+ * The source time functions and the CPML profiles formed on the GPU in FP64
+ * (then stored in FP32 as sfd_set_source / sfd_set_cpml store them), so a
+ * caller that loops over models or shots passes a few parameters instead of
+ * the arrays.  Replaces the driver's host-side wavelet and cpml_parameters
+ * (src/seidart/routines/sourcefunction.py:25-57, 239-300;
+ * definitions.py:862-998) and the .dat round trips of their results. */
+#define SFD_WAVELET_GAUS0 0 /* Gaussian, width 0.2 / (pi f0) */
+#define SFD_WAVELET_GAUS1 1 /* Ricker */
+#define SFD_WAVELET_GAUS2 2 /* the driver's 'gaus2' form */
+/* The source (stress = 0, as sfd_set_source) or the stress source (stress =
+ * 1, as sfd_set_stress_source) at (i, j, k): component c at step t is
+ * comp[c] * amp * w(t dt) / max_t |w(t dt)|, w the driver's wavelet of type
+ * stype and centre frequency f0 (sourcefunction.py:25-57 on the time vector
+ * arange(nstep) * dt, :262; comp the rotation or moment-tensor factors of
+ * :276-300).  ncomp as for sfd_set_source / sfd_set_stress_source; not for
+ * ELECTROMAG2C. */
+int32_t sfd_set_source_wavelet(sfd_handle* h, int32_t stress, int32_t i, int32_t j, int32_t k, int32_t stype,
+                               double f0, double amp, const double* comp, int32_t ncomp);
+
+/* CPML profile parameters: per axis (x, [y,] z) the largest conductivity
+ * sig_max (seidart_gb300.cpml.sigma_alpha_max gives the driver's and the
+ * legacy writer's), and for all axes alpha_max, kappa_max and the exponents
+ * NP, NPA; mode 0 = the driver's profiles (distance rescaled to 1 at the
+ * outer cell, interior b = 1), 1 = the legacy writer's (interior b = 0). */
+typedef struct sfd_cpml_params {
+  double sig_max[3];
+  double alpha_max;
+  double kappa_max;
+  double NP, NPA;
+  int32_t mode;
+} sfd_cpml_params;
+/* The profiles of sfd_set_cpml computed on the device from the parameters
+ * (seidart_gb300/cpml.py's axis_profile on every axis). */
+int32_t sfd_set_cpml_params(sfd_handle* h, const sfd_cpml_params* p);
 
 /* Receiver cells, host int32 (i, j, k) triples, nrec = cfg.nrec. */
 int32_t sfd_set_receivers(sfd_handle* h, const int32_t* ijk, int32_t nrec);

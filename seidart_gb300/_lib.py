@@ -23,7 +23,7 @@ SFD_OK, SFD_ERR_BAD_ARG, SFD_ERR_STATE, SFD_ERR_CUDA, SFD_ERR_UNSTABLE, SFD_ERR_
 EXPORTS = (
     "sfd_version", "sfd_last_error", "sfd_model_planes", "sfd_num_fields", "sfd_num_channels",
     "sfd_num_memory", "sfd_state_bytes", "sfd_create", "sfd_set_model", "sfd_set_model_ids", "sfd_set_cpml", "sfd_set_cpml2d",
-    "sfd_set_source", "sfd_set_stress_source", "sfd_share_model", "sfd_set_receivers", "sfd_reset", "sfd_set_field", "sfd_get_field",
+    "sfd_set_source", "sfd_set_stress_source", "sfd_set_source_wavelet", "sfd_set_cpml_params", "sfd_share_model", "sfd_set_receivers", "sfd_reset", "sfd_set_field", "sfd_get_field",
     "sfd_get_field_async", "sfd_encode_field_i16",
     "sfd_get_memory", "sfd_run", "sfd_status", "sfd_get_traces", "sfd_traces_device", "sfd_field_device", "sfd_launch_half",
     "sfd_on_chip", "sfd_set_wait_limit", "sfd_test_stall_waits",
@@ -56,6 +56,15 @@ class SfdConfig(C.Structure):
     ]
 
 
+class SfdCpmlParams(C.Structure):
+    _fields_ = [
+        ("sig_max", C.c_double * 3), ("alpha_max", C.c_double), ("kappa_max", C.c_double),
+        ("NP", C.c_double), ("NPA", C.c_double), ("mode", C.c_int32),
+    ]
+
+
+WAVELETS = {"gaus0": 0, "gaus1": 1, "gaus2": 2}
+
 _lock = threading.Lock()
 _lib = None
 
@@ -79,6 +88,8 @@ def _declare(lib):
         "sfd_set_cpml2d": (i32, [P, dp, i64]),
         "sfd_set_source": (i32, [P, i32, i32, i32, dp, i32, i32]),
         "sfd_set_stress_source": (i32, [P, i32, i32, i32, dp, i32, i32]),
+        "sfd_set_source_wavelet": (i32, [P, i32, i32, i32, i32, i32, C.c_double, C.c_double, dp, i32]),
+        "sfd_set_cpml_params": (i32, [P, C.POINTER(SfdCpmlParams)]),
         "sfd_set_receivers": (i32, [P, ip, i32]),
         "sfd_share_model": (i32, [P, P]),
         "sfd_reset": (i32, [P]),

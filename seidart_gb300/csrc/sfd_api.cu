@@ -1404,6 +1404,88 @@ int32_t sfd_set_stress_source(sfd_handle* h, int32_t i, int32_t j, int32_t k, co
   return SFD_OK;
 }
 
+int32_t sfd_set_source_wavelet(sfd_handle* h, int32_t stress, int32_t i, int32_t j, int32_t k, int32_t stype,
+                               double f0, double amp, const double* comp, int32_t ncomp) {
+  g_err.clear();
+  if (!h || !comp) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  h->adj_rec_n = 0;  // the recorded states no longer follow from the handle
+  const sfd_config& c = h->cfg;
+  if (c.kind == SFD_ELECTROMAG2C) return fail(SFD_ERR_BAD_ARG, "electromag2c sources come through sfd_set_source");
+  if (stype < SFD_WAVELET_GAUS0 || stype > SFD_WAVELET_GAUS2) return fail(SFD_ERR_BAD_ARG, "unknown wavelet type %d", stype);
+  if (!(f0 > 0.0) || !std::isfinite(f0) || !std::isfinite(amp))
+    return fail(SFD_ERR_BAD_ARG, "the wavelet needs a positive finite f0 and a finite amplitude");
+  const int want = stress ? nstress(c.kind) : nsrc(c.kind);
+  if (stress && !want) return fail(SFD_ERR_BAD_ARG, "stress sources apply to the seismic kinds only");
+  if (ncomp != want) return fail(SFD_ERR_BAD_ARG, "the source needs %d components, got %d", want, ncomp);
+  if (!all_finite(comp, (size_t)ncomp)) return fail(SFD_ERR_BAD_ARG, "component factors contain NaN or Inf");
+  if (!stress && !h->have_model) return fail(SFD_ERR_STATE, "sfd_set_source_wavelet needs the model (sfd_set_model) first");
+  const bool three = is3(c.kind);
+  if (i < 1 || i > c.nx - 3 || k < 1 || k > c.nz - 3 || (three && (j < 1 || j > c.ny - 3)) || (!three && j != 0))
+    return fail(SFD_ERR_BAD_ARG, "source cell (%d,%d,%d) must lie inside the grid, away from its outer two planes", i, j, k);
+  if (stress ? (h->have_force_src && !same_source_cell(h, i, j, k)) : (h->have_ssrc && !same_source_cell(h, i, j, k)))
+    return fail(SFD_ERR_BAD_ARG, "the force and stress sources must share one cell");
+  WaveletComp wc;
+  wc.n = ncomp;
+  const size_t n = (size_t)i + (size_t)c.nx * k;
+  for (int q = 0; q < ncomp; ++q) {
+    wc.comp[q] = comp[q];
+    wc.div[q] = 1.0;
+    if (!stress) {
+      int r = source_divisor(h, q, n, &wc.div[q]);
+      if (r) return r;
+    }
+  }
+  const size_t rows = stress ? (size_t)ncomp : (size_t)nchan(c.kind);
+  float* out = (float*)(h->base + h->L.off_src) + (stress ? (size_t)nchan(c.kind) * c.nstep : 0);
+  CK(cudaMemsetAsync(out, 0, sizeof(float) * rows * c.nstep, h->stream));
+  CK(wavelet_launch(stype, f0, c.dt, c.nstep, amp, wc, out, (size_t)c.nstep, h->stream));
+  if (stress) {
+    h->have_ssrc = true;
+    set_io_ssrc(h);
+  } else {
+    h->have_force_src = true;
+  }
+  set_io_source(h, i, j, k);
+  invalidate_graph(h);
+  return SFD_OK;
+}
+
+int32_t sfd_set_cpml_params(sfd_handle* h, const sfd_cpml_params* p) {
+  g_err.clear();
+  if (!h || !p) return fail(SFD_ERR_BAD_ARG, "NULL argument");
+  h->adj_rec_n = 0;  // the recorded states no longer follow from the handle
+  const sfd_config& c = h->cfg;
+  if (cpml2d(c)) return fail(SFD_ERR_STATE, "a SFD_FLAG_CPML_2D handle takes its CPML from sfd_set_cpml2d");
+  if (p->mode != 0 && p->mode != 1) return fail(SFD_ERR_BAD_ARG, "CPML mode must be 0 (driver) or 1 (legacy)");
+  const bool three = is3(c.kind);
+  const double vals[7] = {p->sig_max[0], three ? p->sig_max[1] : 0.0, p->sig_max[2], p->alpha_max, p->kappa_max,
+                          p->NP, p->NPA};
+  for (double v : vals)
+    if (!std::isfinite(v) || v < 0.0) return fail(SFD_ERR_BAD_ARG, "CPML parameters must be finite and >= 0");
+  if (c.npml < 1) return fail(SFD_ERR_BAD_ARG, "CPML profiles need npml >= 1");
+  const int lens[3] = {c.nx, three ? c.ny : c.nz, c.nz};
+  const double deltas[3] = {c.dx, three ? c.dy : c.dz, c.dz};
+  const double sig[3] = {p->sig_max[0], three ? p->sig_max[1] : p->sig_max[2], p->sig_max[2]};
+  const int nax = three ? 3 : 2;
+  const bool seismic = c.kind == SFD_SEISMIC2 || c.kind == SFD_SEISMIC25;
+  for (int a = 0; a < nax; ++a) {
+    CpmlAxisArgs ax;
+    ax.n = lens[a]; ax.npml = c.npml; ax.delta = deltas[a]; ax.dt = c.dt; ax.sig_max = sig[a];
+    ax.alpha_max = p->alpha_max; ax.kappa_max = p->kappa_max; ax.NP = p->NP; ax.NPA = p->NPA;
+    ax.seismic = seismic; ax.legacy = p->mode;
+    const int st = axis_stride(lens[a]);
+    CK(cudaMemsetAsync(h->axis(a), 0, sizeof(float) * 6 * (size_t)st, h->stream));
+    CK(cpml_axis_launch(ax, h->axis(a), st, h->stream));
+  }
+  float* q3 = (float*)(h->base + h->L.off_q3);
+  CK(cudaMemsetAsync(q3, 0, sizeof(float) * c.nz, h->stream));
+  if (c.kind == SFD_SEISMIC2)  // b_x_half read at the z index, seismicfdtd.f95:255
+    CK(cpml_q3_launch(h->axis(0) + 5 * (size_t)axis_stride(c.nx), c.nx, c.nz, q3, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->have_cpml = true;
+  return SFD_OK;
+}
+
 int32_t sfd_set_receivers(sfd_handle* h, const int32_t* ijk, int32_t nrec) {
   g_err.clear();
   if (!h) return fail(SFD_ERR_BAD_ARG, "NULL handle");

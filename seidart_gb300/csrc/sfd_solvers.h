@@ -241,6 +241,25 @@ Launch seis2_step_launch(const Seis2Step& a, int zb);
 void seis2_step(const Seis2Step& a, const Launch& L, int zb, int rel, cudaStream_t s);
 void seis2_step_finalize(const Seis2Step& a, int t_last, cudaStream_t s);
 
+// Input assembly on the device (inputs.cu).  A source time function: one
+// FP32 row of nstep values per component q, comp[q] * amp * the peak-
+// normalised wavelet, times dt, over div[q].
+struct WaveletComp {
+  int n;
+  double comp[6];
+  double div[6];
+};
+cudaError_t wavelet_launch(int stype, double f0, double dt, int nstep, double amp, const WaveletComp& wc, float* out,
+                           size_t stride, cudaStream_t s);
+// One axis of CPML profiles into its FP32 table (6 rows of st floats).
+struct CpmlAxisArgs {
+  int n, npml;
+  double delta, dt, sig_max, alpha_max, kappa_max, NP, NPA;
+  int seismic, legacy;
+};
+cudaError_t cpml_axis_launch(const CpmlAxisArgs& p, float* tab, int st, cudaStream_t s);
+cudaError_t cpml_q3_launch(const float* bxh, int nx, int nz, float* q3, cudaStream_t s);
+
 // Block-floating int16 encoding of one field (snapshot.cu): minmax[0..1] <-
 // the field's min and max, out <- the dense x-fastest int16 codes.  rows =
 // NY * NZ rows of NX values at pitch P.  Queued on stream s.

@@ -210,6 +210,34 @@ class FDTDSolver:
             raise ValueError(f"2-D CPML fields must be (6, {self.grid.nz}, {self.grid.nx})")
         check(self._L.sfd_set_cpml2d(self._h, _dptr(arr), arr.size))
 
+    def set_cpml_params(self, sig_max, alpha_max, kappa_max=5.0, NP=2.0, NPA=2.0, mode="driver") -> None:
+        """CPML profiles computed on the device (``sfd_set_cpml_params``):
+        ``sig_max`` per axis (x, z) or (x, y, z), as ``cpml.sigma_alpha_max``
+        gives them; the other parameters as ``cpml.axis_profile``."""
+        sm = [float(v) for v in sig_max]
+        if len(sm) == 2:
+            sm = [sm[0], 0.0, sm[1]]
+        if len(sm) != 3:
+            raise ValueError("sig_max needs one value per axis")
+        if mode not in ("driver", "legacy"):
+            raise ValueError(f"unknown CPML mode {mode!r}")
+        prm = _lib.SfdCpmlParams((C.c_double * 3)(*sm), float(alpha_max), float(kappa_max), float(NP), float(NPA),
+                                 0 if mode == "driver" else 1)
+        check(self._L.sfd_set_cpml_params(self._h, C.byref(prm)))
+
+    def set_source_wavelet(self, ijk, f0, amp=1.0, comp=None, stype="gaus1", stress=False) -> None:
+        """Source time functions formed on the device (``sfd_set_source_wavelet``):
+        component c is ``comp[c] * amp * w(t)`` with ``w`` the driver's
+        peak-normalised wavelet ``stype`` of centre frequency ``f0`` on the
+        time vector ``arange(nstep) * dt``.  ``stress`` sets the stress source
+        (moment-tensor factors in ``comp``) instead of the force source."""
+        if stype not in _lib.WAVELETS:
+            raise ValueError(f"unknown wavelet {stype!r}")
+        c = np.ascontiguousarray(comp if comp is not None else [1.0], dtype=np.float64)
+        i, j, k = (int(v) for v in ijk)
+        check(self._L.sfd_set_source_wavelet(self._h, int(bool(stress)), i, j, k, _lib.WAVELETS[stype], float(f0),
+                                             float(amp), _dptr(c), c.size))
+
     def share_model(self, other: "FDTDSolver") -> None:
         """Read ``other``'s update coefficients instead of a copy (shots of one model)."""
         check(self._L.sfd_share_model(self._h, other._h))
