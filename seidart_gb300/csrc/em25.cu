@@ -196,7 +196,10 @@ __global__ void __launch_bounds__(BX * BZ) em25_h_tma_kernel(const __grid_consta
   else march(std::false_type{});
 }
 
-__global__ void __launch_bounds__(BX * BZ) em25_e_tma_kernel(const __grid_constant__ Em25Args a, int rel) {
+// 8 blocks per SM (64 registers, no spills): 0.2985 against 0.305 ms per
+// step at the 72 registers and 7 blocks the compiler picks by itself (the
+// 630 x 70 x 330 grid).
+__global__ void __launch_bounds__(BX * BZ, 8) em25_e_tma_kernel(const __grid_constant__ Em25Args a, int rel) {
   extern __shared__ __align__(128) unsigned char stage_raw[];
   float* const stage = tma::aligned_stage(stage_raw);
   __shared__ __align__(8) uint64_t full[RING];
