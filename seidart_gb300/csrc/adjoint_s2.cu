@@ -19,16 +19,23 @@
 // with the update coefficients of sfd_set_model (A, B: stiffness averages x
 // dt; dtrx, dtrz: dt over the densities; gxp, gzp: 1 - gamma).  The adjoint
 // step is its exact transpose in reverse order, written as gathers (each
-// thread writes only its own cells) in three kernels:
-//   s2adj_v: the velocity half transposed at each cell: the adjoint of the
+// thread writes only its own cells) in three phases:
+//   v: the velocity half transposed at each cell (after the step's residual
+//            is added at the receiver cells): the adjoint of the
 //            stress memory variables, the differences' adjoints lc1, lc2,
 //            ld1, ld2 (scratch planes), the velocity parts gxp lvx, gzp lvz
 //            and the gradients of dtrx, dtrz, gxp, gzp and the source;
-//   s2adj_s: the stresses' adjoints (gathering lc, ld), the stress half
+//   s: the stresses' adjoints (gathering lc, ld), the stress half
 //            transposed at each cell: the adjoint of the velocity-gradient
 //            memory variables, la1..la4 and lb1..lb4 (scratch planes) and the
 //            gradients of the A and B coefficients;
-//   s2adj_g: the velocities' adjoints, gathering la, lb.
+//   g: the velocities' adjoints, gathering la, lb.
+// The g phase of one step and the v phase of the step before it read and
+// write only their own cell's adjoint values (their neighbours' come from
+// the s phase's scratch planes and the forward states), so one kernel runs
+// both at each cell: a segment of n steps is one v kernel, then n s kernels
+// and n - 1 fused g + v kernels in turn, then one g kernel.  The residual
+// is added by the v phase at the cell's receivers (a per-cell list).
 // The FP64 numpy restatement (oracle/numpy_adjoint.py, seismic2_gradient)
 // follows the same steps.  The forward states of a checkpoint segment are
 // recomputed by the handle's own runs, one step at a time.
@@ -48,26 +55,22 @@ __device__ __forceinline__ int mz_idx(int i, int k, int NZ, int P, int W) { retu
 // 11 dvz_dx (x), the last four of the sigmaxz loop.
 enum { P1 = 0, P2 = 1, P4 = 2, P3 = 3, R1 = 4, R4 = 5, R3 = 6, R2 = 7, Q1 = 8, Q2 = 9, Q4 = 10, Q3 = 11 };
 
-__global__ void s2adj_inject(S2Adj a, S2State Ln, int rel) {
-  const int t = a.ctl->base + rel;
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= a.nrec) return;
-  const size_t c = (size_t)a.rec[3 * r + 2] * a.P + a.rec[3 * r];
-  atomicAdd(Ln.vx + c, a.resid[((size_t)t * 2 + 0) * a.nrec + r]);
-  atomicAdd(Ln.vz + c, a.resid[((size_t)t * 2 + 1) * a.nrec + r]);
-}
-
-__global__ void __launch_bounds__(BX * BY) s2adj_v(S2Adj a, S2State S, S2State S1, S2State Ln, S2State Lc, int rel) {
-  const int t = a.ctl->base + rel;
-  const int i = blockIdx.x * BX + threadIdx.x, k = blockIdx.y * BY + threadIdx.y;
+// The v phase of step t at (i, k): S the forward state before the step, S1
+// after it, Ln the adjoint of S1 (without the step's residual), Lc that of S.
+__device__ __forceinline__ void v_cell(const S2Adj& a, const S2State& S, const S2State& S1, const S2State& Ln,
+                                       const S2State& Lc, int t, int i, int k) {
   const int NX = a.NX, NZ = a.NZ, P = a.P, W = a.W;
-  if (i >= NX || k >= NZ) return;
   const size_t c = (size_t)k * P + i;
   const bool xs = in_strip(i, NX, W), zs = in_strip(k, NZ, W);
   const int mx = xs ? mx_idx(i, k, NX, W) : 0, mz = zs ? mz_idx(i, k, NZ, P, W) : 0;
   const bool inner = i >= 1 && i <= NX - 2 && k >= 1 && k <= NZ - 2;
   const bool vxr = k >= 1 && i >= 1, vzr = k <= NZ - 2 && i <= NX - 2;
-  const float lvx = inner ? Ln.vx[c] : 0.f, lvz = inner ? Ln.vz[c] : 0.f;
+  float lvx = inner ? Ln.vx[c] : 0.f, lvz = inner ? Ln.vz[c] : 0.f;
+  if (inner)  // this step's residual at the cell's receivers (the traces sample vx', vz')
+    for (int r = a.recmap[c]; r >= 0; r = a.recnext[r]) {
+      lvx += a.resid[((size_t)t * 2 + 0) * a.nrec + r];
+      lvz += a.resid[((size_t)t * 2 + 1) * a.nrec + r];
+    }
   float lc1 = 0.f, lc2 = 0.f, ld1 = 0.f, ld2 = 0.f;
   if (vxr) {  // vx loop transposed
     const float lg = a.dtrx[c] * lvx;
@@ -219,10 +222,9 @@ __global__ void __launch_bounds__(BX * BY) s2adj_s(S2Adj a, S2State S, S2State S
   }
 }
 
-__global__ void __launch_bounds__(BX * BY) s2adj_g(S2Adj a, S2State Lc) {
-  const int i = blockIdx.x * BX + threadIdx.x, k = blockIdx.y * BY + threadIdx.y;
+// The g phase at (i, k): Lc's velocities gain the gathered la, lb terms.
+__device__ __forceinline__ void g_cell(const S2Adj& a, const S2State& Lc, int i, int k) {
   const int NX = a.NX, NZ = a.NZ, P = a.P;
-  if (i >= NX || k >= NZ) return;
   const size_t c = (size_t)k * P + i;
   auto T = [&](int q, int di, int dk) -> float {
     const int ii = i + di, kk = k + dk;
@@ -239,15 +241,71 @@ __global__ void __launch_bounds__(BX * BY) s2adj_g(S2Adj a, S2State Lc) {
   Lc.vz[c] += gvz;
 }
 
+__global__ void __launch_bounds__(BX * BY) s2adj_v(S2Adj a, S2State S, S2State S1, S2State Ln, S2State Lc, int rel) {
+  const int i = blockIdx.x * BX + threadIdx.x, k = blockIdx.y * BY + threadIdx.y;
+  if (i < a.NX && k < a.NZ) v_cell(a, S, S1, Ln, Lc, a.ctl->base + rel, i, k);
+}
+
+__global__ void __launch_bounds__(BX * BY) s2adj_g(S2Adj a, S2State Lc) {
+  const int i = blockIdx.x * BX + threadIdx.x, k = blockIdx.y * BY + threadIdx.y;
+  if (i < a.NX && k < a.NZ) g_cell(a, Lc, i, k);
+}
+
+// g of step base + rel + 1 on G, then v of step base + rel (S, S1, Ln = G, Lc).
+__global__ void __launch_bounds__(BX * BY) s2adj_gv(S2Adj a, S2State G, S2State S, S2State S1, S2State Lc, int rel) {
+  const int i = blockIdx.x * BX + threadIdx.x, k = blockIdx.y * BY + threadIdx.y;
+  if (i >= a.NX || k >= a.NZ) return;
+  g_cell(a, G, i, k);
+  v_cell(a, S, S1, G, Lc, a.ctl->base + rel, i, k);
+}
+
+// The receiver lists of the cells: receivers visited from the last to the
+// first, so each cell's list starts at its smallest index (one thread: a
+// fixed order, whatever the receivers share).
+__global__ void s2adj_recmap(const int* rec, int nrec, int P, int* recmap, int* recnext) {
+  if (threadIdx.x || blockIdx.x) return;
+  for (int r = nrec - 1; r >= 0; --r) {
+    const size_t c = (size_t)rec[3 * r + 2] * P + rec[3 * r];
+    recnext[r] = recmap[c];
+    recmap[c] = r;
+  }
+}
+
 }  // namespace
 
-void s2_adj_step(const S2Adj& a, const S2State& S, const S2State& S1, const S2State& Ln, const S2State& Lc, int rel,
-                 cudaStream_t s) {
-  if (a.nrec > 0) s2adj_inject<<<(a.nrec + 127) / 128, 128, 0, s>>>(a, Ln, rel);
+cudaError_t s2_adj_recmap(const int* rec, int nrec, int P, int NZ, int* recmap, int* recnext, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(recmap, 0xff, sizeof(int) * (size_t)P * NZ, s);  // -1 everywhere
+  if (e == cudaSuccess && nrec > 0) {
+    s2adj_recmap<<<1, 1, 0, s>>>(rec, nrec, P, recmap, recnext);
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
+void s2_adj_sweep(const S2Adj& a, char* slots, size_t stride, const S2Offsets& off, char* lam0, char* lam1, int cur,
+                  int nsteps, cudaStream_t s) {
+  auto state = [&](char* base) {
+    S2State S;
+    float** f[5] = {&S.vx, &S.vz, &S.sxx, &S.szz, &S.sxz};
+    for (int q = 0; q < 5; ++q) *f[q] = (float*)(base + off.o[q]);
+    for (int m = 0; m < 12; ++m) S.m[m] = (float*)(base + off.o[5 + m]);
+    return S;
+  };
+  char* lam[2] = {lam0, lam1};
   const dim3 b(BX, BY), g((a.NX + BX - 1) / BX, (a.NZ + BY - 1) / BY);
-  s2adj_v<<<g, b, 0, s>>>(a, S, S1, Ln, Lc, rel);
-  s2adj_s<<<g, b, 0, s>>>(a, S, S1, Ln, Lc);
-  s2adj_g<<<g, b, 0, s>>>(a, Lc);
+  const int last = nsteps - 1;
+  s2adj_v<<<g, b, 0, s>>>(a, state(slots + stride * (size_t)last), state(slots + stride * (size_t)nsteps),
+                          state(lam[cur]), state(lam[cur ^ 1]), last);
+  for (int st = last; st >= 0; --st) {  // step base + st: Ln = lam[cur], Lc = lam[cur ^ 1]
+    const S2State S = state(slots + stride * (size_t)st), S1 = state(slots + stride * (size_t)(st + 1));
+    const S2State Ln = state(lam[cur]), Lc = state(lam[cur ^ 1]);
+    s2adj_s<<<g, b, 0, s>>>(a, S, S1, Ln, Lc);
+    if (st > 0)  // the next step back: its Ln is this step's Lc, its Lc this step's Ln
+      s2adj_gv<<<g, b, 0, s>>>(a, Lc, state(slots + stride * (size_t)(st - 1)), S, Ln, st - 1);
+    else
+      s2adj_g<<<g, b, 0, s>>>(a, Lc);
+    cur ^= 1;
+  }
 }
 
 }  // namespace sfd

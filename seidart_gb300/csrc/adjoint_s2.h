@@ -24,16 +24,28 @@ struct S2Adj {
   float* srcacc;       // sum_t (lam_vx f_x(t) + lam_vz f_z(t)) at the source cell, f the scaled amplitudes
   const float* srcfn;  // scaled source amplitudes [2][nstep]
   int nstep, si, sk;
-  const int* rec;
+  const int* recmap;   // per cell (pitch P): its first receiver, or -1
+  const int* recnext;  // per receiver: the next one at the same cell, or -1
   int nrec;
   const float* resid;  // dJ/d(trace) [nstep][2][nrec]
   const Ctl* ctl;      // its base + a step's relative index = the step
 };
 
-// One reverse step t = a.ctl->base + rel: S is the forward state before step
-// t, S1 the state after it; Ln the adjoint of S1 (receives this step's
-// residual), Lc the adjoint of S written in full.
-void s2_adj_step(const S2Adj& a, const S2State& S, const S2State& S1, const S2State& Ln, const S2State& Lc, int rel,
-                 cudaStream_t s);
+// Byte offsets of vx vz sxx szz sxz and the twelve memory variables inside
+// one state (forward slots and adjoint states alike).
+struct S2Offsets {
+  size_t o[17];
+};
+
+// The adjoint steps base + nsteps - 1 down to base (base = a.ctl->base) of
+// one segment: slot s (at slots + s * stride) holds the forward state before
+// step base + s, slot nsteps the state after the last; lam[cur] is the
+// adjoint of that last state, and the adjoint states alternate, so the
+// segment ends in lam[cur ^ (nsteps & 1)].  Queued on stream s.
+void s2_adj_sweep(const S2Adj& a, char* slots, size_t stride, const S2Offsets& off, char* lam0, char* lam1, int cur,
+                  int nsteps, cudaStream_t s);
+// recmap (P * NZ cells) and recnext (nrec) of S2Adj from the device receiver
+// list rec ((i, j, k) triples).
+cudaError_t s2_adj_recmap(const int* rec, int nrec, int P, int NZ, int* recmap, int* recnext, cudaStream_t s);
 
 }  // namespace sfd

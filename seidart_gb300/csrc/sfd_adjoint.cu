@@ -95,7 +95,7 @@ int adj_check(const sfd_handle* h) {
 // slots.  A state holds vx vz sxx szz sxz (full grid) and the twelve memory
 // variables (their strips), each array 256-byte aligned.
 struct S2AdjLayout {
-  size_t field, mem[12], state, lam[2], tmp, g, acc, slots, total;
+  size_t field, mem[12], state, lam[2], tmp, g, acc, recmap, recnext, slots, total;
 };
 
 S2AdjLayout s2_adj_layout(const sfd_handle* h, int seg) {
@@ -111,6 +111,8 @@ S2AdjLayout s2_adj_layout(const sfd_handle* h, int seg) {
   A.tmp = o; o += 12 * A.field;
   A.g = o; o += 12 * A.field;
   A.acc = o; o += 256;
+  A.recmap = o; o += align256(sizeof(int) * L.P * (size_t)h->cfg.nz);
+  A.recnext = o; o += align256(sizeof(int) * (size_t)std::max(1, h->cfg.nrec));
   A.slots = o; o += A.state * (size_t)(seg + 1);
   A.total = o;
   return A;
@@ -198,16 +200,13 @@ cudaError_t s2_segment_work(sfd_handle* h, const S2AdjLayout& A, int64_t nsteps,
   a.srcacc = (float*)(h->adj + A.acc);
   a.srcfn = (const float*)(h->base + L.off_src);
   a.nstep = h->cfg.nstep; a.si = h->have_force_src ? c.io.si : -1; a.sk = c.io.sk;
-  a.rec = (const int*)(h->base + L.off_rec); a.nrec = h->cfg.nrec; a.resid = h->adj_resid;
+  a.recmap = (const int*)(h->adj + A.recmap); a.recnext = (const int*)(h->adj + A.recnext);
+  a.nrec = h->cfg.nrec; a.resid = h->adj_resid;
   a.ctl = (const Ctl*)(h->base + L.off_ctl);
-  for (int64_t s = nsteps - 1; s >= 0; --s) {
-    const S2State S = s2_state_at(A, slots + A.state * (size_t)s);
-    const S2State S1 = s2_state_at(A, slots + A.state * (size_t)(s + 1));
-    const S2State Ln = s2_state_at(A, h->adj + A.lam[cur]);
-    const S2State Lc = s2_state_at(A, h->adj + A.lam[1 - cur]);
-    s2_adj_step(a, S, S1, Ln, Lc, (int)s, stream);
-    cur ^= 1;
-  }
+  S2Offsets off;
+  for (int q = 0; q < 5; ++q) off.o[q] = q * A.field;
+  for (int m = 0; m < 12; ++m) off.o[5 + m] = A.mem[m];
+  s2_adj_sweep(a, slots, A.state, off, h->adj + A.lam[0], h->adj + A.lam[1], cur, (int)nsteps, stream);
   return cudaGetLastError();
 }
 
@@ -447,6 +446,11 @@ int32_t sfd_adjoint_begin(sfd_handle* h, void* dev_work, size_t bytes, int32_t s
   h->adj_rec_n = 0;
   CK(cudaMemsetAsync(h->adj, 0, adj_slots(h, seg_steps), h->stream));  // adjoint states, gradients, accumulators
   CK(cudaMemsetAsync(&((Ctl*)(h->base + h->L.off_ctl))->err, 0, sizeof(int), h->stream));
+  if (h->cfg.kind == SFD_SEISMIC2) {  // each cell's receivers, for the residual of the adjoint's v phase
+    const S2AdjLayout A = s2_adj_layout(h, seg_steps);
+    CK(s2_adj_recmap((const int*)(h->base + h->L.off_rec), h->cfg.nrec, h->L.P, h->cfg.nz, (int*)(h->adj + A.recmap),
+                     (int*)(h->adj + A.recnext), h->stream));
+  }
   return SFD_OK;
 }
 

@@ -134,3 +134,30 @@ def test_unsupported_physics_is_refused(gpu, opts):
         assert "corrected physics" in L.sfd_last_error().decode()
     finally:
         s.close()
+
+
+def test_shared_and_boundary_receivers(gpu):
+    """Receivers that share a cell add their residuals there, and a receiver
+    on a Dirichlet plane (whose trace is zero) adds none: the GPU gradient
+    against the FP64 numpy adjoint with such a receiver set."""
+    import dataclasses
+    from oracle import numpy_adjoint as na
+    density = "arithmetic"
+    case, prof, ssrc, cur, _, _ = _setup(density, seed=31)
+    g = case.grid
+    rec = np.array(case.rec_ijk, dtype=np.int32).copy()
+    rec[1] = rec[0]                      # two receivers at one cell
+    rec[2] = (0, 0, g.nz // 2)           # on the x = 0 plane
+    rec[3] = rec[5]
+    case = dataclasses.replace(case, rec_ijk=rec)
+    src = (case.src_ijk[0], case.src_ijk[2])
+    _, d_obs, _, _ = oracle.run(SEISMIC2, g, case.planes, prof, case.src_ijk, case.srcfn, rec, case.nstep,
+                                density=density, stress_src=ssrc)
+    tr64, states, _ = na.seismic2_forward(g.nx, g.nz, g.dx, g.dz, g.dt, prof, cur, src, case.srcfn, case.nstep, rec,
+                                          density=density, stress_src=ssrc)
+    ref = na.seismic2_gradient(g.nx, g.nz, g.dx, g.dz, g.dt, prof, cur, src, case.srcfn, rec, states, tr64 - d_obs,
+                               density=density, stress_src=ssrc)
+    _, g9 = _gpu_gradient(case, cur, ssrc, d_obs, density, 0, 50)
+    for q in range(9):
+        err = np.linalg.norm(g9[q] - ref[q]) / np.linalg.norm(ref[q])
+        assert err <= 3e-3, f"plane {q}: relative L2 {err:.3e}"
