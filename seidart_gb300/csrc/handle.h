@@ -81,6 +81,7 @@ struct sfd_handle_s {
   cudaGraphExec_t adj_graph = nullptr;
   int64_t adj_graph_n = 0;
   int adj_graph_cur = 0, adj_graph_seg = 0;
+  bool adj_graph_sweep_only = false;  // the graph holds the sweep alone (the recompute ran on chip)
   const char* adj_graph_work = nullptr;
   const float* adj_graph_resid = nullptr;
   bool have_model = false, have_cpml = false;
@@ -160,8 +161,9 @@ void begin_run(sfd_handle_s* h, int64_t step);
 void reduce_norms(sfd_handle_s* h);
 // Whether this handle's runs go on chip (decided once per handle).
 bool resident_usable(sfd_handle_s* h);
-// The on-chip electromag2 run of nsteps steps from the handle's state.
+// The on-chip electromag2 and seismic2 runs of nsteps steps from the handle's state.
 Em2Resident resident_args(const sfd_handle_s* h, int64_t nsteps);
+Seis2Resident seis2_resident_args(const sfd_handle_s* h, int64_t nsteps);
 // The FP64 model planes, expanded from the material ids if the model came as ids.
 int ensure_model_planes(sfd_handle_s* h);
 

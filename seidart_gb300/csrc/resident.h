@@ -142,6 +142,15 @@ struct Seis2ResPlan {
   size_t smem;  // dynamic shared memory of the largest tile
 };
 
+// A seismic2 run that writes the state after each step s into slot s + 1
+// (base + (s + 1) * stride): vx vz sxx szz sxz at off[0..4], the twelve
+// memory variables (sfd_num_memory order, on their strips) at off[5..16].
+struct S2Dump {
+  char* base;
+  size_t stride;
+  size_t off[17];
+};
+
 struct Seis2Resident {
   int NX, NZ, P, W, atten, legacy;
   float *vx, *vz, *sxx, *szz, *sxz;        // current copy: read before, written after the run
@@ -157,6 +166,7 @@ struct Seis2Resident {
   int t0, nsteps;
   unsigned long long limit_ns;
   unsigned tag_bias;  // added to every awaited edge tag; 0 except in the timeout test aid
+  S2Dump dump;        // base != nullptr: dump every step's state, leave the loaded state as it was
 };
 
 // Tiling of an NX x NZ seismic2 grid for `max_ctas` CTAs of at most

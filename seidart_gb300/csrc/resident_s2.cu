@@ -100,6 +100,9 @@ enum : int {
   kESLast = 5     // sxz last row (tile below), sxx last column (tile right)
 };
 
+// DUMP: a recompute for the adjoint -- every step's state written to its
+// slot, the loaded state not written back.
+template <bool DUMP>
 __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __grid_constant__ Seis2Resident a) {
   extern __shared__ __align__(16) float smem[];
   __shared__ int s_abort, s_nrec;
@@ -468,9 +471,39 @@ __global__ void __launch_bounds__(kS2Threads, 1) seis2_resident_kernel(const __g
       ok = false;
       break;
     }
+    if (DUMP) {  // the state after step t into slot s + 1 (streaming stores: read once, by the adjoint)
+      char* slot = a.dump.base + a.dump.stride * (size_t)(s + 1);
+      auto arr = [&](int q) { return reinterpret_cast<float*>(slot + a.dump.off[q]); };
+      for (int q = tid; q < CS; q += kS2Threads) {
+        const int lr = q / tw, lc = q - lr * tw, k = z0 + lr, i = x0 + lc, f = fi(lr, lc);
+        const size_t g = (size_t)k * P + i;
+        __stcs(arr(0) + g, VX[f]);
+        __stcs(arr(1) + g, VZ[f]);
+        __stcs(arr(2) + g, SXX[f]);
+        __stcs(arr(3) + g, SZZ[f]);
+        __stcs(arr(4) + g, SXZ[f]);
+        if (in_strip(i, NX, W)) {
+          const size_t mx = (size_t)k * (2 * W) + strip_idx(i, NX, W);
+          const int xm[6] = {0, 3, 4, 6, 8, 11};
+#pragma unroll
+          for (int e = 0; e < 6; ++e) __stcs(arr(5 + xm[e]) + mx, M[xm[e] * CS + q]);
+        }
+        if (in_strip(k, NZ, W)) {
+          const size_t mz = (size_t)strip_idx(k, NZ, W) * P + i;
+          const int zm[6] = {1, 2, 5, 7, 9, 10};
+#pragma unroll
+          for (int e = 0; e < 6; ++e) __stcs(arr(5 + zm[e]) + mz, M[zm[e] * CS + q]);
+        }
+      }
+      __syncthreads();  // the next step's stresses overwrite what the dump reads
+    }
   }
   if (ok && xwarp && a.nsteps > 0) record(a.t0 + a.nsteps - 1);
   if (!ok) return;  // the state is left as it was loaded; the host reports the timeout
+  if (DUMP) {
+    block_norm_to_slot(nrm, a.io.slots, blockIdx.x);
+    return;
+  }
 
   // ---- write the tile back
   for (int q = tid; q < CS; q += kS2Threads) {
@@ -535,15 +568,23 @@ bool seis2_resident_plan(int NX, int NZ, int max_ctas, size_t max_smem, Seis2Res
 }
 
 cudaError_t seis2_resident_prepare(const Seis2ResPlan& plan, int* ctas_per_sm) {
-  cudaError_t e = res_allow_max_smem((const void*)seis2_resident_kernel);
-  if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, seis2_resident_kernel, kS2Threads, plan.smem);
+  const void* fns[2] = {(const void*)seis2_resident_kernel<false>, (const void*)seis2_resident_kernel<true>};
+  int n = 1 << 30;
+  for (const void* fn : fns) {
+    cudaError_t e = res_allow_max_smem(fn);
+    int q = 0;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, fn, kS2Threads, plan.smem);
+    if (e != cudaSuccess) return e;
+    n = std::min(n, q);
+  }
+  *ctas_per_sm = n;
+  return cudaSuccess;
 }
 
 cudaError_t seis2_resident_launch(const Seis2Resident& a, cudaStream_t s) {
   void* args[] = {(void*)&a};
-  return cudaLaunchCooperativeKernel((const void*)seis2_resident_kernel, dim3(a.plan.ntx * a.plan.ntz),
-                                     dim3(kS2Threads), args, a.plan.smem, s);
+  const void* fn = a.dump.base ? (const void*)seis2_resident_kernel<true> : (const void*)seis2_resident_kernel<false>;
+  return cudaLaunchCooperativeKernel(fn, dim3(a.plan.ntx * a.plan.ntz), dim3(kS2Threads), args, a.plan.smem, s);
 }
 
 }  // namespace sfd

@@ -151,11 +151,14 @@ size_t adj_slots(const sfd_handle* h, int seg) {
 // the handle's or its adjoint workspace's and every step index is relative
 // to the control block's base, so a capture of it replays for any segment of
 // the same length.
-cudaError_t s2_segment_work(sfd_handle* h, const S2AdjLayout& A, int64_t nsteps, int cur, cudaStream_t stream) {
+cudaError_t s2_segment_work(sfd_handle* h, const S2AdjLayout& A, int64_t nsteps, int cur, bool recompute,
+                            cudaStream_t stream) {
   const Layout& L = h->L;
   char* slots = h->adj + A.slots;
   cudaError_t e = cudaSuccess;
-  if (h->single) {  // the single-pass step kernel between slots; its in-place memory variables copied ahead
+  if (!recompute) {
+    // the slots already hold the segment's states (the on-chip recompute)
+  } else if (h->single) {  // the single-pass step kernel between slots; its in-place memory variables copied ahead
     Seis2Step st = h->s2s[0];
     st.io.nrec = 0;
     for (int64_t s = 0; s < nsteps && e == cudaSuccess; ++s) {
@@ -214,23 +217,44 @@ cudaError_t s2_segment_work(sfd_handle* h, const S2AdjLayout& A, int64_t nsteps,
 // the segment's work, replayed from a CUDA graph captured on the handle's
 // private stream when it has one (one capture per segment length and
 // starting adjoint state; the graph is dropped with the handle's others).
+// A handle whose runs go on chip recomputes the segment in one on-chip
+// launch (resident_s2.cu, dumping every step's state) ahead of the graph,
+// which then holds the adjoint steps alone.
 int s2_adjoint_segment(sfd_handle* h, int64_t nsteps) {
   const int64_t s0 = h->step;
   const S2AdjLayout A = s2_adj_layout(h, h->adj_seg);
   int r = s2_save_state(h, A, h->adj + A.slots);
   if (r) return r;
   begin_run(h, s0);
+  const bool on_chip = resident_usable(h);
+  if (on_chip) {  // the recompute as one on-chip launch that writes every step's state into its slot
+    const Layout& L = h->L;
+    const S2State S0 = s2_state_at(A, h->adj + A.slots);
+    Seis2Resident fr = seis2_resident_args(h, nsteps);
+    fr.vx = S0.vx; fr.vz = S0.vz; fr.sxx = S0.sxx; fr.szz = S0.szz; fr.sxz = S0.sxz;
+    fr.m_vxx = S0.m[0]; fr.m_vzz = S0.m[1]; fr.m_vxz = S0.m[2]; fr.m_vzx = S0.m[3];
+    fr.m_sxx_x = S0.m[4]; fr.m_szz_z = S0.m[5]; fr.m_sxz_x = S0.m[6]; fr.m_sxz_z = S0.m[7];
+    fr.m2_vxx = S0.m[8]; fr.m2_vzz = S0.m[9]; fr.m2_vxz = S0.m[10]; fr.m2_vzx = S0.m[11];
+    fr.t0 = (int)s0;
+    fr.io.nrec = 0;
+    fr.dump.base = h->adj + A.slots;
+    fr.dump.stride = A.state;
+    for (int q = 0; q < 5; ++q) fr.dump.off[q] = q * A.field;
+    for (int m = 0; m < 12; ++m) fr.dump.off[5 + m] = A.mem[m];
+    CK(cudaMemsetAsync(h->base + L.off_res, 0, res_scratch_bytes(L.P, L.NZ, res_edge_fields(h->cfg.kind)), h->stream));
+    CK(seis2_resident_launch(fr, h->stream));
+  }
   if (!h->cap_stream) {
-    CK(s2_segment_work(h, A, nsteps, h->adj_cur, h->stream));
+    CK(s2_segment_work(h, A, nsteps, h->adj_cur, !on_chip, h->stream));
   } else {
     const bool reuse = h->adj_graph && h->adj_graph_n == nsteps && h->adj_graph_cur == h->adj_cur &&
                        h->adj_graph_work == h->adj && h->adj_graph_resid == h->adj_resid &&
-                       h->adj_graph_seg == h->adj_seg;
+                       h->adj_graph_seg == h->adj_seg && h->adj_graph_sweep_only == on_chip;
     if (!reuse) {
       if (h->adj_graph) { cudaGraphExecDestroy(h->adj_graph); h->adj_graph = nullptr; }
       cudaGraph_t g = nullptr;
       CK(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
-      const cudaError_t ew = s2_segment_work(h, A, nsteps, h->adj_cur, h->cap_stream);
+      const cudaError_t ew = s2_segment_work(h, A, nsteps, h->adj_cur, !on_chip, h->cap_stream);
       const cudaError_t ec = cudaStreamEndCapture(h->cap_stream, &g);
       if (ew != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(ew, "seismic2 adjoint segment"); }
       if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture");
@@ -238,7 +262,7 @@ int s2_adjoint_segment(sfd_handle* h, int64_t nsteps) {
       cudaGraphDestroy(g);
       if (ei != cudaSuccess) { h->adj_graph = nullptr; return cuda_fail(ei, "cudaGraphInstantiate"); }
       h->adj_graph_n = nsteps; h->adj_graph_cur = h->adj_cur; h->adj_graph_work = h->adj;
-      h->adj_graph_resid = h->adj_resid; h->adj_graph_seg = h->adj_seg;
+      h->adj_graph_resid = h->adj_resid; h->adj_graph_seg = h->adj_seg; h->adj_graph_sweep_only = on_chip;
     }
     CK(cudaGraphLaunch(h->adj_graph, h->stream));
   }

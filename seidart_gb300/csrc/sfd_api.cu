@@ -617,6 +617,7 @@ Seis2Resident seis2_resident_args(const sfd_handle* h, int64_t nsteps) {
   r.nsteps = (int)nsteps;
   r.limit_ns = h->wait_ns;
   r.tag_bias = h->stall_waits ? kStallTagBias : 0u;
+  r.dump = S2Dump{nullptr, 0, {}};
   return r;
 }
 
