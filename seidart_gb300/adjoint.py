@@ -14,7 +14,8 @@ step does each (``csrc/adjoint_em2.cu``).  ``flags`` are the solver's
 applies the FP64 chain rule from the update coefficients to the model planes.
 With ``record=True`` the forward pass instead keeps every step's state in
 device memory (``sfd_adjoint_record``; about 6.7 MB a step on a 1040 x 540
-grid) and the backward pass is the adjoint sweep alone, with no recompute.
+electromag2 grid, 2.5 MB on a 440 x 240 seismic2 one) and the backward pass
+is the adjoint sweep alone, with no recompute.
 
 ``traces = TraceMisfit.apply(eps11, eps33, sigma, model)`` is differentiable
 in torch: ``eps11``, ``eps33``, ``sigma`` (sig11 = sig33) are per-cell
@@ -22,8 +23,9 @@ in torch: ``eps11``, ``eps33``, ``sigma`` (sig11 = sig33) are per-cell
 
 ``SeismicTraceModel`` does the same for a seismic2 shot (any of the solver's
 step forms, the corrected physics with 1-D CPML profiles, any density
-method): the backward pass recomputes each segment by the solver's own steps
-and runs the transposed step (``csrc/adjoint_s2.cu``) over it, and the
+method): the backward pass recomputes each segment (in one on-chip launch
+when the grid runs on chip, else by the solver's own steps) and runs the
+transposed step (``csrc/adjoint_s2.cu``) over it, and the
 gradient covers all nine model planes (c11 c13 c15 c33 c35 c55 rho gamma_x
 gamma_z).  ``traces = SeismicTraceMisfit.apply(planes, model)`` is its torch
 function for a (9, NZ, NX) FP64 tensor.
@@ -188,15 +190,16 @@ class SeismicTraceModel(_Checkpointed):
     ``base_planes``: (9, NZ, NX) FP64, the model before the first ``forward``.
     ``density`` is the density averaging method; ``stress_srcfn`` (3, nstep)
     adds the moment-tensor source at the force source's cell.  ``flags`` are
-    the solver's (any step form).
+    the solver's (any step form).  ``record`` keeps every step's state from
+    the forward pass, as for ``TraceModel`` (the grid must run on chip).
     """
 
     nplanes = 9
 
     def __init__(self, grid: GridSpec, base_planes, profiles, src_ijk, srcfn, rec_ijk, ckpt_every=200,
-                 device="cuda", flags=0, density="arithmetic", stress_srcfn=None):
+                 device="cuda", flags=0, density="arithmetic", stress_srcfn=None, record=False):
         super().__init__(grid, base_planes, profiles, src_ijk, srcfn, rec_ijk, ckpt_every, device, flags,
-                         density=density)
+                         record=record, density=density)
         if stress_srcfn is not None:
             self.solver.set_stress_source(src_ijk, stress_srcfn)
 

@@ -220,27 +220,36 @@ cudaError_t s2_segment_work(sfd_handle* h, const S2AdjLayout& A, int64_t nsteps,
 // A handle whose runs go on chip recomputes the segment in one on-chip
 // launch (resident_s2.cu, dumping every step's state) ahead of the graph,
 // which then holds the adjoint steps alone.
-int s2_adjoint_segment(sfd_handle* h, int64_t nsteps) {
-  const int64_t s0 = h->step;
+// The on-chip seismic2 run of nsteps steps from slot 0 (the state before
+// step s0) that writes the state after step s0 + s into slot s + 1 and
+// leaves slot 0 as it was; receivers as the handle's.
+Seis2Resident s2_dump_args(const sfd_handle* h, const S2AdjLayout& A, int64_t s0, int64_t nsteps) {
+  const S2State S0 = s2_state_at(A, h->adj + A.slots);
+  Seis2Resident fr = seis2_resident_args(h, nsteps);
+  fr.vx = S0.vx; fr.vz = S0.vz; fr.sxx = S0.sxx; fr.szz = S0.szz; fr.sxz = S0.sxz;
+  fr.m_vxx = S0.m[0]; fr.m_vzz = S0.m[1]; fr.m_vxz = S0.m[2]; fr.m_vzx = S0.m[3];
+  fr.m_sxx_x = S0.m[4]; fr.m_szz_z = S0.m[5]; fr.m_sxz_x = S0.m[6]; fr.m_sxz_z = S0.m[7];
+  fr.m2_vxx = S0.m[8]; fr.m2_vzz = S0.m[9]; fr.m2_vxz = S0.m[10]; fr.m2_vzx = S0.m[11];
+  fr.t0 = (int)s0;
+  fr.dump.base = h->adj + A.slots;
+  fr.dump.stride = A.state;
+  for (int q = 0; q < 5; ++q) fr.dump.off[q] = q * A.field;
+  for (int m = 0; m < 12; ++m) fr.dump.off[5 + m] = A.mem[m];
+  return fr;
+}
+
+int s2_adjoint_segment(sfd_handle* h, int64_t nsteps, bool recorded, int64_t s0) {
   const S2AdjLayout A = s2_adj_layout(h, h->adj_seg);
-  int r = s2_save_state(h, A, h->adj + A.slots);
-  if (r) return r;
+  if (!recorded) {
+    int r = s2_save_state(h, A, h->adj + A.slots);
+    if (r) return r;
+  }
   begin_run(h, s0);
-  const bool on_chip = resident_usable(h);
-  if (on_chip) {  // the recompute as one on-chip launch that writes every step's state into its slot
+  const bool on_chip = recorded || resident_usable(h);
+  if (on_chip && !recorded) {  // the recompute as one on-chip launch that writes every step's state into its slot
     const Layout& L = h->L;
-    const S2State S0 = s2_state_at(A, h->adj + A.slots);
-    Seis2Resident fr = seis2_resident_args(h, nsteps);
-    fr.vx = S0.vx; fr.vz = S0.vz; fr.sxx = S0.sxx; fr.szz = S0.szz; fr.sxz = S0.sxz;
-    fr.m_vxx = S0.m[0]; fr.m_vzz = S0.m[1]; fr.m_vxz = S0.m[2]; fr.m_vzx = S0.m[3];
-    fr.m_sxx_x = S0.m[4]; fr.m_szz_z = S0.m[5]; fr.m_sxz_x = S0.m[6]; fr.m_sxz_z = S0.m[7];
-    fr.m2_vxx = S0.m[8]; fr.m2_vzz = S0.m[9]; fr.m2_vxz = S0.m[10]; fr.m2_vzx = S0.m[11];
-    fr.t0 = (int)s0;
+    Seis2Resident fr = s2_dump_args(h, A, s0, nsteps);
     fr.io.nrec = 0;
-    fr.dump.base = h->adj + A.slots;
-    fr.dump.stride = A.state;
-    for (int q = 0; q < 5; ++q) fr.dump.off[q] = q * A.field;
-    for (int m = 0; m < 12; ++m) fr.dump.off[5 + m] = A.mem[m];
     CK(cudaMemsetAsync(h->base + L.off_res, 0, res_scratch_bytes(L.P, L.NZ, res_edge_fields(h->cfg.kind)), h->stream));
     CK(seis2_resident_launch(fr, h->stream));
   }
@@ -553,11 +562,38 @@ int32_t sfd_adjoint_record(sfd_handle* h, int64_t nsteps) {
   int r = adj_check(h);
   if (r) return r;
   if (!h->adj) return fail(SFD_ERR_STATE, "call sfd_adjoint_begin first");
-  if (h->cfg.kind != SFD_ELECTROMAG2 || !adjoint_on_chip(h))
-    return fail(SFD_ERR_BAD_ARG, "sfd_adjoint_record needs an electromag2 handle whose runs stay on chip");
+  if (h->cfg.kind == SFD_ELECTROMAG2 ? !adjoint_on_chip(h) : !resident_usable(h))
+    return fail(SFD_ERR_BAD_ARG, "sfd_adjoint_record needs a handle whose runs stay on chip");
   if (nsteps < 1 || nsteps > h->adj_seg)
     return fail(SFD_ERR_BAD_ARG, "recorded run of %lld steps outside [1, %d]", (long long)nsteps, h->adj_seg);
   if (h->step + nsteps > h->cfg.nstep) return fail(SFD_ERR_BAD_ARG, "recorded run goes past the source length");
+  if (h->cfg.kind == SFD_SEISMIC2) {
+    const S2AdjLayout A = s2_adj_layout(h, h->adj_seg);
+    const Layout& L = h->L;
+    r = s2_save_state(h, A, h->adj + A.slots);
+    if (r) return r;
+    begin_run(h, h->step);
+    CK(cudaMemsetAsync(h->base + L.off_res, 0, res_scratch_bytes(L.P, L.NZ, res_edge_fields(h->cfg.kind)), h->stream));
+    const Seis2Resident own = seis2_resident_args(h, nsteps);
+    CK(seis2_resident_launch(s2_dump_args(h, A, h->step, nsteps), h->stream));  // receivers recorded as in sfd_run
+    reduce_norms(h);
+    // the dumping launch keeps the handle's state: take the last slot's
+    const S2State Sn = s2_state_at(A, h->adj + A.slots + A.state * (size_t)nsteps);
+    float* dst[17] = {own.vx, own.vz, own.sxx, own.szz, own.sxz, own.m_vxx, own.m_vzz, own.m_vxz, own.m_vzx,
+                      own.m_sxx_x, own.m_szz_z, own.m_sxz_x, own.m_sxz_z, own.m2_vxx, own.m2_vzz, own.m2_vxz,
+                      own.m2_vzx};
+    const float* src[17] = {Sn.vx, Sn.vz, Sn.sxx, Sn.szz, Sn.sxz, Sn.m[0], Sn.m[1], Sn.m[2], Sn.m[3], Sn.m[4], Sn.m[5],
+                            Sn.m[6], Sn.m[7], Sn.m[8], Sn.m[9], Sn.m[10], Sn.m[11]};
+    for (int q = 0; q < 17; ++q) {
+      const size_t n = q < 5 ? L.fsz : L.mem_sz[q - 5];
+      CK(cudaMemcpyAsync(dst[q], src[q], sizeof(float) * n, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    CK(cudaGetLastError());
+    h->adj_rec_s0 = h->step;
+    h->adj_rec_n = nsteps;
+    h->step += nsteps;
+    return SFD_OK;
+  }
   const AdjLayout A = adj_layout(h, h->adj_seg);
   const Layout& L = h->L;
   r = em2_save_slot0(h, A);
@@ -593,12 +629,13 @@ int32_t sfd_adjoint_segment(sfd_handle* h, int64_t nsteps) {
   if (h->adj_rec_n == nsteps && h->adj_rec_s0 + nsteps == h->step) {
     // sfd_adjoint_record ran these steps and kept every state: sweep only
     h->adj_rec_n = 0;
+    if (h->cfg.kind == SFD_SEISMIC2) return s2_adjoint_segment(h, nsteps, true, h->adj_rec_s0);
     return em2_adjoint_sweep_on_chip(h, adj_layout(h, h->adj_seg), h->adj_rec_s0, nsteps);
   }
   h->adj_rec_n = 0;
   const int64_t s0 = h->step;
   if (s0 + nsteps > h->cfg.nstep) return fail(SFD_ERR_BAD_ARG, "segment runs past the source length");
-  if (h->cfg.kind == SFD_SEISMIC2) return s2_adjoint_segment(h, nsteps);
+  if (h->cfg.kind == SFD_SEISMIC2) return s2_adjoint_segment(h, nsteps, false, s0);
   const AdjLayout A = adj_layout(h, h->adj_seg);
   const Layout& L = h->L;
   const int NX = h->cfg.nx, NZ = h->cfg.nz;

@@ -161,3 +161,29 @@ def test_shared_and_boundary_receivers(gpu):
     for q in range(9):
         err = np.linalg.norm(g9[q] - ref[q]) / np.linalg.norm(ref[q])
         assert err <= 3e-3, f"plane {q}: relative L2 {err:.3e}"
+
+
+def test_recorded_adjoint_matches_checkpointed(gpu):
+    """sfd_adjoint_record on a seismic2 handle: the forward pass keeps every
+    step's state (traces and final state as a plain run's), the backward pass
+    only sweeps, and the gradient equals the checkpointed one to rounding."""
+    import torch
+    density = "harmonic"
+    case, prof, ssrc, cur, d_obs, _ = _setup(density, seed=37)
+    out = []
+    for record in (False, True):
+        m = SeismicTraceModel(case.grid, cur, case.profiles, case.src_ijk, case.srcfn, case.rec_ijk, ckpt_every=45,
+                              density=density, stress_srcfn=ssrc, record=record)
+        try:
+            assert m.solver.on_chip() is not None
+            tr = m.forward(cur)
+            vx = m.solver.field("vx")
+            g = m.backward(tr - torch.as_tensor(d_obs, dtype=torch.float32, device=tr.device))
+            out.append((tr.cpu().numpy(), vx, g))
+        finally:
+            m.close()
+    (ta, va, ga), (tb, vb, gb) = out
+    assert np.array_equal(ta, tb) and np.array_equal(va, vb)
+    for q in range(9):
+        err = np.linalg.norm(ga[q] - gb[q]) / np.linalg.norm(ga[q])
+        assert err <= 1e-6, f"plane {q}: relative L2 {err:.3e}"
