@@ -412,13 +412,15 @@ int32_t sfd_run_checkpointed(sfd_handle* h, int64_t nsteps, void* dev_ckpt, size
 int32_t sfd_adjoint_bytes(const sfd_handle* h, int32_t seg_steps, size_t* bytes);
 int32_t sfd_adjoint_begin(sfd_handle* h, void* dev_work, size_t bytes, int32_t seg_steps, const float* dev_resid);
 int32_t sfd_adjoint_segment(sfd_handle* h, int64_t nsteps);
-/* The recompute-free form (electromag2 handles whose runs are on chip):
- * after sfd_adjoint_begin with seg_steps >= n, sfd_adjoint_record(h, n) is
- * the forward run of n steps (receivers recorded, the handle advanced as by
- * sfd_run) that also keeps every step's state in the workspace; fill the
- * residual, then sfd_adjoint_segment(h, n) right after it runs the adjoint
- * sweep over those states without recomputing them.  The workspace then
- * holds n+1 states (about 6.7 MB each on a 1040 x 540 grid). */
+/* The recompute-free form (electromag2 and seismic2 handles whose runs are
+ * on chip): after sfd_adjoint_begin with seg_steps >= n,
+ * sfd_adjoint_record(h, n) is the forward run of n steps (receivers
+ * recorded, the handle advanced as by sfd_run) that also keeps every step's
+ * state in the workspace; fill the residual, then sfd_adjoint_segment(h, n)
+ * right after it runs the adjoint sweep over those states without
+ * recomputing them.  The workspace then holds n+1 states (about 6.7 MB each
+ * on a 1040 x 540 electromag2 grid, 2.5 MB on a 440 x 240 seismic2 one).
+ * On chip, a seismic2 segment's recompute is itself one launch. */
 int32_t sfd_adjoint_record(sfd_handle* h, int64_t nsteps);
 /* Host FP64 planes: electromag2 dJ/d(eps11 eps13 eps33 sig11 sig13 sig33),
  * 6*NX*NZ values; seismic2 dJ/d(c11 c13 c15 c33 c35 c55 rho gamma_x
