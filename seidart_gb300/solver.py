@@ -430,3 +430,75 @@ def run_shot(grid: GridSpec, planes, profiles, src_ijk, srcfn, rec_ijk, nsteps=N
         s.run(nstep if nsteps is None else nsteps)
         s.status()
         return s.traces()
+
+
+
+class ShotPipeline:
+    """Runs many shots through two handles on two streams in turn, so a
+    shot's host work (the FP64 model folding) and its uploads run while the
+    GPU is still stepping the shot before; the GPU runs the shots one after
+    another.  The handles persist between :meth:`run` calls and are reused
+    while the grid, the number of steps and of receivers stay the same (a
+    long-running caller keeps them warm); :meth:`close` releases them."""
+
+    def __init__(self, device="cuda", legacy: bool = False, density: str = "arithmetic"):
+        import torch
+        self.device = torch.device(device)
+        self.streams = [torch.cuda.Stream(self.device), torch.cuda.Stream(self.device)]
+        self.solvers = [None, None]
+        self.opts = {"legacy": legacy, "density": density}
+
+    def _solver(self, k, grid, nstep, nrec):
+        s = self.solvers[k]
+        if s is not None and s.grid == grid and s.nstep == nstep and s.nrec == nrec:
+            s.reset()
+            return s
+        if s is not None:
+            s.close()
+        opts = self.opts if grid.kind in (SEISMIC2, SEISMIC25) else {}
+        s = self.solvers[k] = FDTDSolver(grid, nstep, nrec, device=self.device, stream=self.streams[k], **opts)
+        return s
+
+    def run(self, shots):
+        """Each shot is a tuple (grid, planes, profiles, src_ijk, srcfn,
+        rec_ijk), host arrays in as for :func:`run_shot`; yields each shot's
+        host traces, in order, as soon as they are back (UnstableError like
+        the Fortran stop)."""
+        pending = None
+        for n, (grid, planes, profiles, src_ijk, srcfn, rec_ijk) in enumerate(shots):
+            srcfn = np.asarray(srcfn, dtype=np.float64)
+            rec = np.asarray(rec_ijk, dtype=np.int32).reshape(-1, 3)
+            s = self._solver(n & 1, grid, srcfn.shape[1], rec.shape[0])
+            s.set_model(planes)
+            s.set_cpml(profiles)
+            s.set_source(src_ijk, srcfn)
+            s.set_receivers(rec)
+            s.run(srcfn.shape[1])  # queued behind the previous shot's run
+            if pending is not None:
+                pending.status()
+                yield pending.traces()
+            pending = s
+        if pending is not None:
+            pending.status()
+            yield pending.traces()
+
+    def close(self) -> None:
+        for k, s in enumerate(self.solvers):
+            if s is not None:
+                s.close()
+                self.solvers[k] = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def run_shots(shots, device="cuda", legacy: bool = False, density: str = "arithmetic"):
+    """Traces of many shots, in order, through a :class:`ShotPipeline` made
+    for the call: each shot is a tuple (grid, planes, profiles, src_ijk,
+    srcfn, rec_ijk), host arrays in and host traces out as for
+    :func:`run_shot`."""
+    with ShotPipeline(device, legacy, density) as p:
+        yield from p.run(shots)
