@@ -129,25 +129,30 @@ def gpu_runner(cases, device=None, schedule: str = "sequential") -> List[np.ndar
 
     * ``"sequential"`` (default): every case alone, one after another, each
       in its own default form -- the whole run in one launch on chip where
-      the grid fits, else one launch per step;
+      the grid fits, else one launch per step -- through a
+      :class:`~seidart_gb300.solver.ShotPipeline` (two handles in turn, a
+      case's host work overlapping the previous case's run);
     * ``"batch"``: all of them advancing together in one persistent launch
       per shot length (:mod:`seidart_gb300.batch`).
 
     On the 80-model survey of 64 electromag2 shots (1040 x 540) and 16
     seismic2 models (200-1200 x 100-600 cells), 4000 steps, the sequential
-    schedule took 1.90 s and the batch 2.37 s (wall clock, set-up
+    schedule took 1.73 s and the batch 2.40 s (wall clock, set-up
     included): on chip a shot runs faster than a batch tile streaming from
     HBM, and a grid too large for the chip runs its own launches at least as
     fast as the batch kernel's register-capped tiles.  Running the models
     that fit on chip alone and batching the rest took 2.08 s.
 
-    Cases that hold the same model planes (the same array object) share one
-    copy of the coefficients."""
+    In the batch schedule, cases that hold the same model planes (the same
+    array object) share one copy of the coefficients."""
     from .batch import Batch, autotune
-    from .solver import FDTDSolver, run_shot
+    from .solver import FDTDSolver, ShotPipeline, run_shot
     if schedule not in ("sequential", "batch"):
         raise ValueError("schedule must be 'sequential' or 'batch'")
     device = default_device() if device is None else device
+    if schedule == "sequential":
+        with ShotPipeline(device) as p:
+            return list(p.run((c.grid, c.planes, c.profiles, c.src_ijk, c.srcfn, c.rec_ijk) for c in cases))
 
     out: List[Optional[np.ndarray]] = [None] * len(cases)
     two_d = [q for q, c in enumerate(cases) if c.grid.kind in (SEISMIC2, ELECTROMAG2)]
@@ -171,17 +176,8 @@ def gpu_runner(cases, device=None, schedule: str = "sequential") -> List[np.ndar
             s.set_cpml(c.profiles)
             s.set_source(c.src_ijk, c.srcfn)
             s.set_receivers(c.rec_ijk)
-        batched = []
-        for q in two_d:
-            s = solvers[q]
-            if schedule == "sequential":
-                s.run(cases[q].nstep)
-                s.status()
-                out[q] = s.traces()
-            else:
-                batched.append(q)
         by_len: Dict[int, List[int]] = {}
-        for q in batched:  # one batch per shot length: a batch advances all its models together
+        for q in two_d:  # one batch per shot length: a batch advances all its models together
             by_len.setdefault(cases[q].nstep, []).append(q)
         for nstep, qs in by_len.items():
             if len(qs) == 1:
