@@ -368,6 +368,17 @@ def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000, 
     for s in step_solvers:
         s.close()
     step_agg = cells * nstep / (step_ms / 1e3) / 1e9
+    # ... and the survey runner's default: every model in its default form,
+    # through the two-handle shot pipeline (wall clock, set-up included)
+    from seidart_gb300 import survey
+    survey.gpu_runner(cases[:2] + cases[-2:], device=device)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    surv_traces = survey.gpu_runner(cases, device=device)
+    torch.cuda.synchronize()
+    surv_s = time.perf_counter() - t0
+    num3 = sum(float(((tp.astype(np.float64) - tb) ** 2).sum()) for tp, tb in zip(surv_traces, batched_traces))
+    den3 = sum(float((tp.astype(np.float64) ** 2).sum()) for tp in surv_traces)
     out = {"workload": f"64 electromag2 shots 1040x540 + 16 seismic2 models (nx 200-1200, nz 100-600) x {nstep} steps",
            "value": round(value, 3), "unit": METRIC, "ms_per_run": round(ms, 2), "cells": cells,
            "bytes_per_cell_update": round(step_bytes / cells, 2),
@@ -382,6 +393,11 @@ def bench_batched(device, flush, stream, peak, plain_value, runs=2, nstep=4000, 
                                    "form": "each model alone, one launch per step (SFD_FLAG_STREAMING)",
                                    "traces_rel_l2_vs_batched": (num2 / den2) ** 0.5 if den2 > 0 else None},
            "vs_per_step_aggregate": round(value / step_agg, 3),
+           "survey_pipeline": {"value": round(cells * nstep / surv_s / 1e9, 3), "unit": METRIC,
+                               "s": round(surv_s, 3),
+                               "form": "survey.gpu_runner (default): each model in its default form through "
+                                       "solver.ShotPipeline, wall clock with the set-up",
+                               "traces_rel_l2_vs_batched": (num3 / den3) ** 0.5 if den3 > 0 else None},
            "tiling": {"rows_per_thread": tune["tiling"][0], "blocks_per_sm": tune["tiling"][1],
                       "candidates_ms_per_step": {k: round(v * 1e3, 4) for k, v in tune["timings"].items()}},
            "launches_per_run": 3}
