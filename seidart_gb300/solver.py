@@ -451,7 +451,6 @@ class ShotPipeline:
     def _solver(self, k, grid, nstep, nrec):
         s = self.solvers[k]
         if s is not None and s.grid == grid and s.nstep == nstep and s.nrec == nrec:
-            s.reset()
             return s
         if s is not None:
             s.close()
@@ -469,10 +468,14 @@ class ShotPipeline:
             srcfn = np.asarray(srcfn, dtype=np.float64)
             rec = np.asarray(rec_ijk, dtype=np.int32).reshape(-1, 3)
             s = self._solver(n & 1, grid, srcfn.shape[1], rec.shape[0])
+            # the setters only copy (and wait for their own copies); the state
+            # is cleared after them, because the clearing kernels cannot start
+            # before the previous shot's run leaves the SMs
             s.set_model(planes)
             s.set_cpml(profiles)
             s.set_source(src_ijk, srcfn)
             s.set_receivers(rec)
+            s.reset()
             s.run(srcfn.shape[1])  # queued behind the previous shot's run
             if pending is not None:
                 pending.status()
