@@ -879,6 +879,12 @@ def run_ours(args):
                               nstep=args.time_steps if args.time_steps != 6000 else 300)
             c.name = "electromag2c random 1960x1460"
             rec = bench_plain(c, device, flush, stream, peak, em2c_bytes, args.steps, args.warmup)
+        elif args.only == "seismic2_large":  # a grid too large for the chip: one launch per step
+            from seidart_gb300 import SEISMIC2
+            c = sy.small_case(SEISMIC2, seed=3, nx=2040, nz=1540, npml=20,
+                              nstep=args.time_steps if args.time_steps != 6000 else 100, nrec=10)
+            c.name = "seismic2 random 2000x1500"
+            rec = bench_plain(c, device, flush, stream, peak, seis2_bytes, args.steps, args.warmup)
         elif args.only == "batched":
             tiling = tuple(int(v) for v in args.batch_tiling.split("x")) if args.batch_tiling else None
             rec = bench_batched(device, flush, stream, peak, None, runs=args.steps,
@@ -1072,7 +1078,7 @@ def main(argv=None):
                     help="time steps per headline shot (6000 = the workload; smaller only for profiler runs)")
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--only", choices=["seismic2", "seismic25", "batched", "adjoint", "seismic2_adjoint",
-                                       "electromag2_step", "electromag25", "electromag2c"],
+                                       "electromag2_step", "electromag25", "electromag2c", "seismic2_large"],
                     help="run one secondary leg alone and print its record (for profiler runs)")
     ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--skip-parity", action="store_true",
