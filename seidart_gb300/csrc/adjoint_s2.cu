@@ -65,72 +65,108 @@ __device__ __forceinline__ void v_cell(const S2Adj& a, const S2State& S, const S
   const int mx = xs ? mx_idx(i, k, NX, W) : 0, mz = zs ? mz_idx(i, k, NZ, P, W) : 0;
   const bool inner = i >= 1 && i <= NX - 2 && k >= 1 && k <= NZ - 2;
   const bool vxr = k >= 1 && i >= 1, vzr = k <= NZ - 2 && i <= NX - 2;
+  const bool src = i == a.si && k == a.sk;
+  // ---- loads (every one before the first store, as in s2adj_s)
   float lvx = inner ? Ln.vx[c] : 0.f, lvz = inner ? Ln.vz[c] : 0.f;
   if (inner)  // this step's residual at the cell's receivers (the traces sample vx', vz')
     for (int r = a.recmap[c]; r >= 0; r = a.recnext[r]) {
       lvx += a.resid[((size_t)t * 2 + 0) * a.nrec + r];
       lvz += a.resid[((size_t)t * 2 + 1) * a.nrec + r];
     }
+  const float ikx = a.X.ik[i], ikz = a.Z.ik[k], ikxh = a.X.ikh[i], ikzh = a.Z.ikh[k];
+  const float lnR1 = xs ? Ln.m[R1][mx] : 0.f, lnR2 = zs ? Ln.m[R2][mz] : 0.f;
+  const float lnR3 = xs ? Ln.m[R3][mx] : 0.f, lnR4 = zs ? Ln.m[R4][mz] : 0.f;
+  float dtrx = 0.f, sxx_c = 0.f, sxx_l = 0.f, sxz_c = 0.f, sxz_u = 0.f, adx = 0.f, bx = 0.f, adz = 0.f, bz = 0.f,
+        s1R1 = 0.f, s1R2 = 0.f, gdtrx = 0.f;
+  if (vxr) {
+    dtrx = a.dtrx[c];
+    sxx_c = S1.sxx[c]; sxx_l = S1.sxx[c - 1]; sxz_c = S1.sxz[c]; sxz_u = S1.sxz[c - P];
+    if (xs) { adx = a.X.ad[i]; bx = a.X.b[i]; s1R1 = S1.m[R1][mx]; }
+    if (zs) { adz = a.Z.ad[k]; bz = a.Z.b[k]; s1R2 = S1.m[R2][mz]; }
+    if (inner) gdtrx = a.gdtrx[c];
+  }
+  float dtrz = 0.f, sxz_c2 = 0.f, sxz_r = 0.f, szz_c = 0.f, szz_d = 0.f, adxh = 0.f, bxh = 0.f, adzh = 0.f,
+        bzh = 0.f, s1R3 = 0.f, s1R4 = 0.f, gdtrz = 0.f;
+  if (vzr) {
+    dtrz = a.dtrz[c];
+    sxz_c2 = S1.sxz[c]; sxz_r = S1.sxz[c + 1]; szz_c = S1.szz[c]; szz_d = S1.szz[c + P];
+    if (xs) { adxh = a.X.adh[i]; bxh = a.X.bh[i]; s1R3 = S1.m[R3][mx]; }
+    if (zs) { adzh = a.Z.adh[k]; bzh = a.Z.bh[k]; s1R4 = S1.m[R4][mz]; }
+    if (inner) gdtrz = a.gdtrz[c];
+  }
+  float ggxp = 0.f, ggzp = 0.f, vx0 = 0.f, vz0 = 0.f;
+  if (inner) { ggxp = a.ggxp[c]; ggzp = a.ggzp[c]; vx0 = S.vx[c]; vz0 = S.vz[c]; }
+  const float gxp = a.gxp[c], gzp = a.gzp[c];
+  float fx = 0.f, fz = 0.f, acc = 0.f;
+  if (src) { fx = a.srcfn[t]; fz = a.srcfn[a.nstep + t]; acc = *a.srcacc; }
+  // ---- arithmetic
   float lc1 = 0.f, lc2 = 0.f, ld1 = 0.f, ld2 = 0.f;
+  float oR1 = lnR1, oR2 = lnR2, oR3 = lnR3, oR4 = lnR4;  // the memory variables' adjoints (strip cells)
   if (vxr) {  // vx loop transposed
-    const float lg = a.dtrx[c] * lvx;
-    const float c1 = S1.sxx[c] - S1.sxx[c - 1], c2 = S1.sxz[c] - S1.sxz[c - P];
-    float g = c1 * a.X.ik[i] + c2 * a.Z.ik[k];
-    lc1 = a.X.ik[i] * lg;
-    lc2 = a.Z.ik[k] * lg;
+    const float lg = dtrx * lvx;
+    const float c1 = sxx_c - sxx_l, c2 = sxz_c - sxz_u;
+    float g = c1 * ikx + c2 * ikz;
+    lc1 = ikx * lg;
+    lc2 = ikz * lg;
     if (xs) {
-      const float tt = Ln.m[R1][mx] + lg;
-      lc1 += a.X.ad[i] * tt;
-      Lc.m[R1][mx] = a.X.b[i] * tt;
-      g += S1.m[R1][mx];
+      const float tt = lnR1 + lg;
+      lc1 += adx * tt;
+      oR1 = bx * tt;
+      g += s1R1;
     }
     if (zs) {
-      const float tt = Ln.m[R2][mz] + lg;
-      lc2 += a.Z.ad[k] * tt;
-      Lc.m[R2][mz] = a.Z.b[k] * tt;
-      g += S1.m[R2][mz];
+      const float tt = lnR2 + lg;
+      lc2 += adz * tt;
+      oR2 = bz * tt;
+      g += s1R2;
     }
-    if (inner) a.gdtrx[c] += lvx * g;
-  } else {
-    if (xs) Lc.m[R1][mx] = Ln.m[R1][mx];
-    if (zs) Lc.m[R2][mz] = Ln.m[R2][mz];
+    if (inner) gdtrx += lvx * g;
   }
   if (vzr) {  // vz loop transposed
-    const float lh = a.dtrz[c] * lvz;
-    const float d1 = S1.sxz[c + 1] - S1.sxz[c], d2 = S1.szz[c + P] - S1.szz[c];
-    float h = d1 * a.X.ikh[i] + d2 * a.Z.ikh[k];
-    ld1 = a.X.ikh[i] * lh;
-    ld2 = a.Z.ikh[k] * lh;
+    const float lh = dtrz * lvz;
+    const float d1 = sxz_r - sxz_c2, d2 = szz_d - szz_c;
+    float h = d1 * ikxh + d2 * ikzh;
+    ld1 = ikxh * lh;
+    ld2 = ikzh * lh;
     if (xs) {
-      const float tt = Ln.m[R3][mx] + lh;
-      ld1 += a.X.adh[i] * tt;
-      Lc.m[R3][mx] = a.X.bh[i] * tt;
-      h += S1.m[R3][mx];
+      const float tt = lnR3 + lh;
+      ld1 += adxh * tt;
+      oR3 = bxh * tt;
+      h += s1R3;
     }
     if (zs) {
-      const float tt = Ln.m[R4][mz] + lh;
-      ld2 += a.Z.adh[k] * tt;
-      Lc.m[R4][mz] = a.Z.bh[k] * tt;
-      h += S1.m[R4][mz];
+      const float tt = lnR4 + lh;
+      ld2 += adzh * tt;
+      oR4 = bzh * tt;
+      h += s1R4;
     }
-    if (inner) a.gdtrz[c] += lvz * h;
-  } else {
-    if (xs) Lc.m[R3][mx] = Ln.m[R3][mx];
-    if (zs) Lc.m[R4][mz] = Ln.m[R4][mz];
+    if (inner) gdtrz += lvz * h;
   }
   if (inner) {
-    a.ggxp[c] += lvx * S.vx[c];
-    a.ggzp[c] += lvz * S.vz[c];
+    ggxp += lvx * vx0;
+    ggzp += lvz * vz0;
   }
-  if (i == a.si && k == a.sk) *a.srcacc += lvx * a.srcfn[t] + lvz * a.srcfn[a.nstep + t];
-  Lc.vx[c] = a.gxp[c] * lvx;  // the velocities' own parts; s2adj_g adds the stencil terms
-  Lc.vz[c] = a.gzp[c] * lvz;
+  // ---- stores
+  if (xs) { Lc.m[R1][mx] = oR1; Lc.m[R3][mx] = oR3; }
+  if (zs) { Lc.m[R2][mz] = oR2; Lc.m[R4][mz] = oR4; }
+  if (vxr && inner) a.gdtrx[c] = gdtrx;
+  if (vzr && inner) a.gdtrz[c] = gdtrz;
+  if (inner) {
+    a.ggxp[c] = ggxp;
+    a.ggzp[c] = ggzp;
+  }
+  if (src) *a.srcacc = acc + (lvx * fx + lvz * fz);
+  Lc.vx[c] = gxp * lvx;  // the velocities' own parts; the g phase adds the stencil terms
+  Lc.vz[c] = gzp * lvz;
   a.tmp[0][c] = lc1;
   a.tmp[1][c] = lc2;
   a.tmp[2][c] = ld1;
   a.tmp[3][c] = ld2;
 }
 
+// Every load of a cell first, then the arithmetic, then the stores: the
+// arrays are distinct, but the compiler cannot know that and would keep
+// each load behind the stores before it.
 __global__ void __launch_bounds__(BX * BY) s2adj_s(S2Adj a, S2State S, S2State S1, S2State Ln, S2State Lc) {
   const int i = blockIdx.x * BX + threadIdx.x, k = blockIdx.y * BY + threadIdx.y;
   const int NX = a.NX, NZ = a.NZ, P = a.P, W = a.W;
@@ -140,80 +176,124 @@ __global__ void __launch_bounds__(BX * BY) s2adj_s(S2Adj a, S2State S, S2State S
   const float* lc2 = a.tmp[1];
   const float* ld1 = a.tmp[2];
   const float* ld2 = a.tmp[3];
-  // the stresses' adjoints: the next state's plus the velocity half's differences
-  const float lsxx = Ln.sxx[c] + lc1[c] - (i + 1 < NX ? lc1[c + 1] : 0.f);
-  const float lszz = Ln.szz[c] - ld2[c] + (k >= 1 ? ld2[c - P] : 0.f);
-  const float lsxz = Ln.sxz[c] - ld1[c] + (i >= 1 ? ld1[c - 1] : 0.f) + lc2[c] - (k + 1 < NZ ? lc2[c + P] : 0.f);
-  Lc.sxx[c] = lsxx;
-  Lc.szz[c] = lszz;
-  Lc.sxz[c] = lsxz;
+  const bool l2 = k <= NZ - 2 && i >= 1, l1 = k >= 1 && i <= NX - 2;
   const bool xs = in_strip(i, NX, W), zs = in_strip(k, NZ, W);
   const int mx = xs ? mx_idx(i, k, NX, W) : 0, mz = zs ? mz_idx(i, k, NZ, P, W) : 0;
   // (memory variable, strip is x, ik, ad, b) of the four differences of a loop
   const int pm[4] = {P1, P2, P3, P4}, qm[4] = {Q1, Q2, Q3, Q4};
   const bool isx[4] = {true, false, true, false};
+  // ---- loads
+  const float lnsxx = Ln.sxx[c], lnszz = Ln.szz[c], lnsxz = Ln.sxz[c];
+  const float lc1c = lc1[c], lc1r = i + 1 < NX ? lc1[c + 1] : 0.f;
+  const float ld2c = ld2[c], ld2u = k >= 1 ? ld2[c - P] : 0.f;
+  const float ld1c = ld1[c], ld1l = i >= 1 ? ld1[c - 1] : 0.f;
+  const float lc2c = lc2[c], lc2d = k + 1 < NZ ? lc2[c + P] : 0.f;
   const float ik[4] = {a.X.ikh[i], a.Z.ik[k], a.X.ik[i], a.Z.ikh[k]};
   const float ad[4] = {a.X.adh[i], a.Z.ad[k], a.X.ad[i], a.Z.adh[k]};
   const float bb[4] = {a.X.bh[i], a.Z.b[k], a.X.b[i], a.Z.bh[k]};
+  const float vxc = S.vx[c], vzc = S.vz[c];
+  float vxl = 0.f, vzd = 0.f, vzl = 0.f, vxd = 0.f, B15 = 0.f, B35 = 0.f, B55 = 0.f, gB15 = 0.f, gB35 = 0.f,
+        gB55 = 0.f;
+  if (l2) {
+    vxl = S.vx[c - 1]; vzd = S.vz[c + P]; vzl = S.vz[c - 1]; vxd = S.vx[c + P];
+    B15 = a.B15[c]; B35 = a.B35[c]; B55 = a.B55[c];
+    gB15 = a.gB15[c]; gB35 = a.gB35[c]; gB55 = a.gB55[c];
+  }
+  float vxr = 0.f, vzu = 0.f, vzr = 0.f, vxu = 0.f, A11 = 0.f, A13 = 0.f, A15 = 0.f, A33 = 0.f, A35 = 0.f;
+  float gA11 = 0.f, gA13 = 0.f, gA15 = 0.f, gA33 = 0.f, gA35 = 0.f;
+  if (l1) {
+    vxr = S.vx[c + 1]; vzu = S.vz[c - P]; vzr = S.vz[c + 1]; vxu = S.vx[c - P];
+    A11 = a.A11[c]; A13 = a.A13[c]; A15 = a.A15[c]; A33 = a.A33[c]; A35 = a.A35[c];
+    gA11 = a.gA11[c]; gA13 = a.gA13[c]; gA15 = a.gA15[c]; gA33 = a.gA33[c]; gA35 = a.gA35[c];
+  }
+  float s1q[4], lnq[4], s1p[4], lnp[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const bool on = isx[q] ? xs : zs;
+    const int m = isx[q] ? mx : mz;
+    s1q[q] = on && l2 ? S1.m[qm[q]][m] : 0.f;
+    lnq[q] = on ? Ln.m[qm[q]][m] : 0.f;
+    s1p[q] = on && l1 ? S1.m[pm[q]][m] : 0.f;
+    lnp[q] = on ? Ln.m[pm[q]][m] : 0.f;
+  }
+  // ---- the stresses' adjoints: the next state's plus the velocity half's differences
+  const float lsxx = lnsxx + lc1c - lc1r;
+  const float lszz = lnszz - ld2c + ld2u;
+  const float lsxz = lnsxz - ld1c + ld1l + lc2c - lc2d;
   float la[4] = {0.f, 0.f, 0.f, 0.f}, lb[4] = {0.f, 0.f, 0.f, 0.f};
-  if (k <= NZ - 2 && i >= 1) {  // loop 2 transposed
+  float outq[4], outp[4];  // the memory variables' adjoints to store (strip cells)
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    outq[q] = lnq[q];
+    outp[q] = lnp[q];
+  }
+  if (l2) {  // loop 2 transposed
     const float lf = lsxz;
-    const float d[4] = {S.vx[c] - S.vx[c - 1], S.vz[c + P] - S.vz[c], S.vz[c] - S.vz[c - 1], S.vx[c + P] - S.vx[c]};
+    const float d[4] = {vxc - vxl, vzd - vzc, vzc - vzl, vxd - vxc};
     float f[4];
-    const float lfq[4] = {a.B15[c] * lf, a.B35[c] * lf, a.B55[c] * lf, a.B55[c] * lf};
+    const float lfq[4] = {B15 * lf, B35 * lf, B55 * lf, B55 * lf};
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const bool on = isx[q] ? xs : zs;
-      const int m = isx[q] ? mx : mz;
-      f[q] = d[q] * ik[q] + (on ? S1.m[qm[q]][m] : 0.f);
+      f[q] = d[q] * ik[q] + (on ? s1q[q] : 0.f);
       lb[q] = ik[q] * lfq[q];
       if (on) {
-        const float tt = Ln.m[qm[q]][m] + lfq[q];
+        const float tt = lnq[q] + lfq[q];
         lb[q] += ad[q] * tt;
-        Lc.m[qm[q]][m] = bb[q] * tt;
+        outq[q] = bb[q] * tt;
       }
     }
-    a.gB15[c] += lf * f[0];
-    a.gB35[c] += lf * f[1];
-    a.gB55[c] += lf * (f[2] + f[3]);
-  } else {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const bool on = isx[q] ? xs : zs;
-      const int m = isx[q] ? mx : mz;
-      if (on) Lc.m[qm[q]][m] = Ln.m[qm[q]][m];
-    }
+    gB15 += lf * f[0];
+    gB35 += lf * f[1];
+    gB55 += lf * (f[2] + f[3]);
   }
-  if (k >= 1 && i <= NX - 2) {  // loop 1 transposed
+  if (l1) {  // loop 1 transposed
     const float ls = lsxx, lz = lszz;
-    const float d[4] = {S.vx[c + 1] - S.vx[c], S.vz[c] - S.vz[c - P], S.vz[c + 1] - S.vz[c], S.vx[c] - S.vx[c - P]};
+    const float d[4] = {vxr - vxc, vzc - vzu, vzr - vzc, vxc - vxu};
     float e[4];
-    const float A15e = a.A15[c] * ls + a.A35[c] * lz;
-    const float le[4] = {a.A11[c] * ls + a.A13[c] * lz, a.A13[c] * ls + a.A33[c] * lz, A15e, A15e};
+    const float A15e = A15 * ls + A35 * lz;
+    const float le[4] = {A11 * ls + A13 * lz, A13 * ls + A33 * lz, A15e, A15e};
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const bool on = isx[q] ? xs : zs;
-      const int m = isx[q] ? mx : mz;
-      e[q] = d[q] * ik[q] + (on ? S1.m[pm[q]][m] : 0.f);
+      e[q] = d[q] * ik[q] + (on ? s1p[q] : 0.f);
       la[q] = ik[q] * le[q];
       if (on) {
-        const float tt = Ln.m[pm[q]][m] + le[q];
+        const float tt = lnp[q] + le[q];
         la[q] += ad[q] * tt;
-        Lc.m[pm[q]][m] = bb[q] * tt;
+        outp[q] = bb[q] * tt;
       }
     }
-    a.gA11[c] += ls * e[0];
-    a.gA13[c] += ls * e[1] + lz * e[0];
-    a.gA15[c] += ls * (e[2] + e[3]);
-    a.gA33[c] += lz * e[1];
-    a.gA35[c] += lz * (e[2] + e[3]);
-  } else {
+    gA11 += ls * e[0];
+    gA13 += ls * e[1] + lz * e[0];
+    gA15 += ls * (e[2] + e[3]);
+    gA33 += lz * e[1];
+    gA35 += lz * (e[2] + e[3]);
+  }
+  // ---- stores
+  Lc.sxx[c] = lsxx;
+  Lc.szz[c] = lszz;
+  Lc.sxz[c] = lsxz;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const bool on = isx[q] ? xs : zs;
-      const int m = isx[q] ? mx : mz;
-      if (on) Lc.m[pm[q]][m] = Ln.m[pm[q]][m];
+  for (int q = 0; q < 4; ++q) {
+    const bool on = isx[q] ? xs : zs;
+    const int m = isx[q] ? mx : mz;
+    if (on) {
+      Lc.m[qm[q]][m] = outq[q];
+      Lc.m[pm[q]][m] = outp[q];
     }
+  }
+  if (l2) {
+    a.gB15[c] = gB15;
+    a.gB35[c] = gB35;
+    a.gB55[c] = gB55;
+  }
+  if (l1) {
+    a.gA11[c] = gA11;
+    a.gA13[c] = gA13;
+    a.gA15[c] = gA15;
+    a.gA33[c] = gA33;
+    a.gA35[c] = gA35;
   }
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
