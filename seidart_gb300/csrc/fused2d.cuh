@@ -146,7 +146,8 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
                     !(a.io.si >= x0 && a.io.si < x0 + 128 && a.io.sk >= z0 && a.io.sk < z0 + 8 * ZB);
 
   // ---- H half-step on the owned rows
-  if (fast) {
+  if (fast) {  // every row computed before the first store (the stores would hold back later loads)
+    float4 hv[ZB];
 #pragma unroll
     for (int r = 0; r < ZB; ++r) {
       const int k = z0 + ty + 8 * r;
@@ -155,17 +156,19 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
       float ez_next = __shfl_down_sync(0xffffffffu, ez.x, 1);
       if (tx == 31) ez_next = fld<RO>(a.Ez0 + c0 + 4);
       const float ikz = __ldg(a.Z.ik + k);
-      float4 hv;
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const float dEx = el(exn, e) - el(ex, e);
         const float vz = dEx * ikz;
         const float dEz = (e < 3 ? el(ez, e + 1) : ez_next) - el(ez, e);
         const float vx = dEz * el(ikx4, e);
-        el(hv, e) = el(hy, e) + a.dbH * (vx + vz);
+        el(hv[r], e) = el(hy, e) + a.dbH * (vx + vz);
       }
-      st4(a.Hy1 + c0, hv);
-      *reinterpret_cast<float4*>(&sH[ty + 8 * r + 1][sx]) = hv;
+    }
+#pragma unroll
+    for (int r = 0; r < ZB; ++r) {
+      st4(a.Hy1 + (z0 + ty + 8 * r) * P + i0, hv[r]);
+      *reinterpret_cast<float4*>(&sH[ty + 8 * r + 1][sx]) = hv[r];
     }
   } else {
 #pragma unroll
@@ -216,7 +219,8 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
   __syncthreads();
   // ---- E half-step, source, Dirichlet, norm on the owned rows
   float norm = 0.0f;
-  if (fast) {
+  if (fast) {  // every row computed before the first store (the stores would hold back later loads)
+    float4 exr[ZB], ezr[ZB];
 #pragma unroll
     for (int r = 0; r < ZB; ++r) {
       const int k = z0 + ty + 8 * r;
@@ -238,8 +242,14 @@ __device__ __forceinline__ void em2_tile(const Em2Step& a, int t, int bx, int by
         el(ez, e) = ezv;
         norm = fmaxf(norm, norm_monitor(exv, ezv));
       }
-      st4(a.Ex1 + c0, ex);
-      st4(a.Ez1 + c0, ez);
+      exr[r] = ex;
+      ezr[r] = ez;
+    }
+#pragma unroll
+    for (int r = 0; r < ZB; ++r) {
+      const int c0 = (z0 + ty + 8 * r) * P + i0;
+      st4(a.Ex1 + c0, exr[r]);
+      st4(a.Ez1 + c0, ezr[r]);
     }
   } else {
 #pragma unroll
@@ -461,19 +471,19 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
                     z0 + 8 * ZB - 1 <= NZ - 1 - lo && z0 + 8 * ZB - 1 <= NZ - 2 &&
                     !(a.io.si >= x0 && a.io.si < x0 + 32 && a.io.sk >= z0 && a.io.sk < z0 + 8 * ZB);
   // ---- stress half-step on owned cells (stored) ...
-  if (fast) {
+  if (fast) {  // every row computed before the first store (the stores would hold back later loads)
+    float sxx[ZB], szz[ZB], sxz[ZB];
+#pragma unroll
+    for (int r = 0; r < ZB; ++r) seis2_stress_plain<RO>(a, i, z0 + ty + 8 * r, sxx[r], szz[r], sxz[r]);
 #pragma unroll
     for (int r = 0; r < ZB; ++r) {
-      const int k = z0 + ty + 8 * r;
-      const int c = k * P + i;
-      float sxx, szz, sxz;
-      seis2_stress_plain<RO>(a, i, k, sxx, szz, sxz);
-      a.sxx1[c] = sxx;
-      a.szz1[c] = szz;
-      a.sxz1[c] = sxz;
-      sS[0][ty + 8 * r + 1][tx + 1] = sxx;
-      sS[1][ty + 8 * r + 1][tx + 1] = szz;
-      sS[2][ty + 8 * r + 1][tx + 1] = sxz;
+      const int c = (z0 + ty + 8 * r) * P + i;
+      a.sxx1[c] = sxx[r];
+      a.szz1[c] = szz[r];
+      a.sxz1[c] = sxz[r];
+      sS[0][ty + 8 * r + 1][tx + 1] = sxx[r];
+      sS[1][ty + 8 * r + 1][tx + 1] = szz[r];
+      sS[2][ty + 8 * r + 1][tx + 1] = sxz[r];
     }
   } else {
 #pragma unroll
@@ -535,7 +545,8 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
   __syncthreads();
   // ---- velocity half-step on owned cells (seismicfdtd.f95:317-379)
   float norm = 0.0f;
-  if (fast) {
+  if (fast) {  // every row computed before the first store (the stores would hold back later loads)
+    float vxr[ZB], vzr[ZB];
     const float ikx = __ldg(a.X.ik + i), ikxh = __ldg(a.X.ikh + i);
 #pragma unroll
     for (int r = 0; r < ZB; ++r) {
@@ -551,9 +562,15 @@ __device__ __forceinline__ void seis2_tile(const Seis2Step& a, int t, int bx, in
       }
       vx = vx + (v1 + v2) * __ldg(a.dtrx + c);
       vz = vz + (w1 + w2) * __ldg(a.dtrz + c);
-      a.vx1[c] = vx;
-      a.vz1[c] = vz;
+      vxr[r] = vx;
+      vzr[r] = vz;
       norm = fmaxf(norm, norm_monitor(vx, vz));
+    }
+#pragma unroll
+    for (int r = 0; r < ZB; ++r) {
+      const int c = (z0 + ty + 8 * r) * P + i;
+      a.vx1[c] = vxr[r];
+      a.vz1[c] = vzr[r];
     }
   } else {
 #pragma unroll
