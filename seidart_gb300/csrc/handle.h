@@ -95,6 +95,7 @@ struct sfd_handle_s {
   sfd::Launch launch1;       // single-pass geometry
   int res_state = 0;    // on-chip runs: 0 not yet checked, 1 usable, -1 not usable
   sfd::ResPlan res_plan;     // electromag2
+  sfd::ResPlan res_plan_adj;  // electromag2, the adjoint sweep's (no three-row tiles)
   sfd::Seis2ResPlan s2_plan;  // seismic2
   int64_t step = 0;
   unsigned long long wait_ns = sfd::kDefaultWaitNs;  // longest wait of an on-chip run for a neighbouring tile

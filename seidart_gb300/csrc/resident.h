@@ -24,13 +24,19 @@ constexpr int kResMaxTiles = 256;
 constexpr int kResThreads = 512;
 constexpr int kResCellThreads = kResThreads - 32;
 constexpr int kResRows = 2;
+// Rows per thread in an electromag2 tile of interior cells only (no CPML
+// strip, no Dirichlet plane), whose cells all take the short update: the
+// planner gives such tiles more cells than the others, so that the tiles
+// with the longer strip and boundary updates can be made smaller.
+constexpr int kResRows3 = 3;
 // Receivers a CTA lists in shared memory; a tile holding more scans the
 // whole receiver list every step instead.
 constexpr int kResMaxLocalRec = 256;
 
 // Tiling of one on-chip run: ntz tile rows, each cut into its own tiles.
 // tile[b] packs x0 | x1 << 16, z0 | z1 << 16, row | (index in row) << 16 and
-// the tile count of its row; column bounds are multiples of 4 (except NX).
+// the tile count of its row | (interior tile: kResRows3 rows per thread) << 16;
+// column bounds are multiples of 4 (except NX).
 // Tiles that hold CPML strip or boundary cells take the longer update and are
 // made smaller.
 struct ResPlan {
@@ -177,9 +183,12 @@ cudaError_t seis2_resident_launch(const Seis2Resident& a, cudaStream_t s);
 
 // Pick the tiling of an NX x NZ electromag2 grid with npml-cell strips for
 // `max_ctas` CTAs of at most `max_smem` bytes of shared memory.  Returns
-// false when the grid does not fit on chip.
-bool em2_resident_plan(int NX, int NZ, int npml, int max_ctas, size_t max_smem, ResPlan* out);
-size_t em2_resident_smem(int TW, int TZ);
+// false when the grid does not fit on chip.  rows3: tiles of interior cells
+// may take kResRows3 rows per thread (the forward kernel's plans; the adjoint
+// sweep's tiles all take kResRows).
+bool em2_resident_plan(int NX, int NZ, int npml, int max_ctas, size_t max_smem, ResPlan* out, bool rows3);
+// Dynamic shared memory of a TW x TZ tile with RB rows per thread.
+size_t em2_resident_smem(int TW, int TZ, int RB);
 // Set the kernel's shared-memory limit (once per device) and return how many
 // CTAs of `smem` bytes fit on one SM.
 cudaError_t em2_resident_prepare(const ResPlan& plan, int* ctas_per_sm);

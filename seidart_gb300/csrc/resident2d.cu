@@ -46,15 +46,17 @@ using namespace res;
 
 namespace {
 
-// MODE 0: a run; 1: a recompute for the adjoint (every step's state dumped,
-// the handle's state kept); 2: a run that also saves checkpoints.
-template <int MODE>
-__global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __grid_constant__ Em2Resident a) {
+// One CTA's tile for the whole run.  MODE 0: a run; 1: a recompute for the
+// adjoint (every step's state dumped, the handle's state kept); 2: a run that
+// also saves checkpoints.  RB rows per thread: kResRows in general, kResRows3
+// in the tiles the planner marks as interior (no CPML strip cell, no
+// Dirichlet plane; the source may lie inside), which take the short update
+// path only and so hold half as many cells again per thread.
+template <int MODE, int RB>
+__device__ __forceinline__ void em2_resident_tile(const Em2Resident& a, float* smem, int& s_abort, int& s_nrec,
+                                                  int* s_rec) {
   constexpr bool DUMP = MODE == 1, CKPT = MODE == 2;
-  constexpr int RB = kResRows;
-  extern __shared__ __align__(16) float smem[];
-  __shared__ int s_abort, s_nrec;
-  __shared__ int s_rec[2 * kResMaxLocalRec];  // (receiver, tile cell) pairs
+  constexpr bool INTERIOR = RB == kResRows3;
   const int NX = a.NX, NZ = a.NZ, P = a.P, W = a.W;
   const int tile = blockIdx.x;
   const int4 te = a.plan.tile[tile];
@@ -65,7 +67,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
   const int nc4 = TXT;
   // row edges are indexed by tile row and global x, column edges by the index
   // in the tile row and global z, so a tile row may be cut unlike its neighbours
-  const bool up = bz > 0, down = bz < a.plan.ntz - 1, left = bx > 0, right = bx < te.w - 1;
+  const bool up = bz > 0, down = bz < a.plan.ntz - 1, left = bx > 0, right = bx < (te.w & 0xffff) - 1;
   const int tid = threadIdx.x;
   const bool xwarp = tid >= kResCellThreads;
   // Threads take the tile's groups (four columns x RB rows) in class order --
@@ -97,11 +99,12 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
   // thread tid is the float4 at so = 4 (j * kResCellThreads + tid), so a warp's
   // accesses are conflict-free whichever groups its threads own.
   const int CS = 4 * RB * kResCellThreads;
+  constexpr int NPSI = INTERIOR ? 0 : 4;  // an interior tile has no memory variables
   float* sMExz = smem;  // CPML memory variables of strip cells
   float* sMEzx = sMExz + CS;
   float* sMHyz = sMEzx + CS;
   float* sMHyx = sMHyz + CS;
-  float* sCAx = sMHyx + CS;  // update coefficients
+  float* sCAx = smem + NPSI * CS;  // update coefficients
   float* sCBx = sCAx + CS;
   float* sCAz = sCBx + CS;
   float* sCBz = sCAz + CS;
@@ -110,7 +113,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
   // scalar arrays last: every array above starts on a 16-byte boundary (TW is a multiple of 4)
   float* sEzCol = sHyRow + (TYT + 1) * TW;  // [TZ][SX]: first Ez column of thread column tx; column TXT = tile right
   float* sHyCol = sEzCol + TZ * SX;         // [TZ][SX]: column tx+1 = last Hy column of tx; column 0 = tile left
-  const int nsm = 8 * CS + 2 * (TYT + 1) * TW + 2 * TZ * SX;
+  const int nsm = (NPSI + 4) * CS + 2 * (TYT + 1) * TW + 2 * TZ * SX;
   const int NZp = a.r.NZp;
   // edge words: field 0 = first Ex row / first Ez column, 1 = last Hy row / column
   auto erow = [&](int par, int f, int b) { return a.r.erow + (size_t)((par * 2 + f) * kResMaxTiles1D + b) * P; };
@@ -158,7 +161,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
       sts4(sCBz + so, ld4(a.CBz + gg));
       ikz[j] = __ldg(a.Z.ik + k);
       ikzh[j] = __ldg(a.Z.ikh + k);
-      zs[j] = in_strip(k, NZ, W);
+      zs[j] = !INTERIOR && in_strip(k, NZ, W);
       if (zs[j]) {
         const int zrow = strip_idx(k, NZ, W) * P + i0;
         sts4(sMExz + so, ld4(a.mExz + zrow));
@@ -170,7 +173,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
         const int i = i0 + e;
         if (i >= NX) continue;
         mm |= 1u << (kMCELL + e);
-        if (in_strip(i, NX, W)) {
+        if (!INTERIOR && in_strip(i, NX, W)) {
           xs = true;
           const int q = k * (2 * W) + strip_idx(i, NX, W);
           sMEzx[so + e] = a.mEzx[q];
@@ -234,6 +237,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
     }
   }
   const float dbH = a.dbH;
+  const bool hsrc = se >= 0;
 
   float nrm = 0.0f;
   bool ok = s_abort == 0;
@@ -253,14 +257,14 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
         if (j + 1 < RB && j + 1 < nrows) exn = ex[j + 1 < RB ? j + 1 : j];
         const float ezn = sEzCol[row * SX + tx + 1];
         float4 hv;
-        if (fast) {
+        if (INTERIOR || fast) {
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
             const float dEx = el(exn, e) - el(ex[j], e);
             const float dEz = (e < 3 ? el(ez[j], e + 1) : ezn) - el(ez[j], e);
             el(hv, e) = el(hy[j], e) + dbH * (dEz * el(ikx4, e) + dEx * ikz[j]);
           }
-        } else {  // strip, bound or plane cells: two cells at a time, masks applied as selects
+        } else if constexpr (!INTERIOR) {  // strip, bound or plane cells: two cells at a time, masks applied as selects
           const unsigned mj = m[j];
           const bool hall = ((mj >> kMH) & 15u) == 15u;
           float adz = 0.0f, bzc = 0.0f;
@@ -333,18 +337,23 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
         const float hl = sHyCol[row * SX + tx];
         const float4 h = hy[j];
         const float4 cxa = lds4(sCAx + so), cxb = lds4(sCBx + so), cza = lds4(sCAz + so), czb = lds4(sCBz + so);
-        if (fast) {
+        if (INTERIOR || fast) {
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
             const float dHz = el(h, e) - el(hm, e);
             const float exv = el(cxa, e) * el(ex[j], e) + el(cxb, e) * (dHz * ikzh[j]);
             const float dHx = el(h, e) - (e == 0 ? hl : el(h, e - 1));
             const float ezv = el(cza, e) * el(ez[j], e) + el(czb, e) * (dHx * el(ikxh4, e));
-            el(ex[j], e) = exv;
-            el(ez[j], e) = ezv;
-            nrm = fmaxf(nrm, norm_monitor(exv, ezv));
+            float exs = exv, ezs = ezv;
+            if (INTERIOR && hsrc && 4 * j + e == se) {  // :300-301, the source inside an interior tile
+              exs += a.io.src[t];
+              ezs += a.io.src[a.io.nstep + t];
+            }
+            el(ex[j], e) = exs;
+            el(ez[j], e) = ezs;
+            nrm = fmaxf(nrm, norm_monitor(exs, ezs));
           }
-        } else {  // strip, bound or plane cells: two cells at a time, masks applied as selects
+        } else if constexpr (!INTERIOR) {  // strip, bound or plane cells: two cells at a time, masks applied as selects
           const unsigned mj = m[j];
           const bool rowplain = (mj & 0xffffffu) == 0x000fffu;
           float adz = 0.0f, bzc = 0.0f;
@@ -433,7 +442,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
           }
         }
       }
-      if (!plain) {  // the stored Hy keeps its Dirichlet planes at zero, after every row's E used it
+      if (!INTERIOR && !plain) {  // the stored Hy keeps its Dirichlet planes at zero, after every row's E used it
 #pragma unroll
         for (int j = 0; j < RB; ++j)
 #pragma unroll
@@ -462,7 +471,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
               __stcs((float*)(d + a.ckpt.off[3]) + zrow, sMExz[so + e]);
               __stcs((float*)(d + a.ckpt.off[5]) + zrow, sMHyz[so + e]);
             }
-            if (in_strip(i, NX, W)) {
+            if (!INTERIOR && in_strip(i, NX, W)) {
               const int q = k * (2 * W) + strip_idx(i, NX, W);
               __stcs((float*)(d + a.ckpt.off[4]) + q, sMEzx[so + e]);
               __stcs((float*)(d + a.ckpt.off[6]) + q, sMHyx[so + e]);
@@ -523,7 +532,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const int i = i0 + e;
-        if (i < NX && in_strip(i, NX, W)) {
+        if (!INTERIOR && i < NX && in_strip(i, NX, W)) {
           const int q = k * (2 * W) + strip_idx(i, NX, W);
           a.mEzx[q] = sMEzx[so + e];
           a.mHyx[q] = sMHyx[so + e];
@@ -534,21 +543,37 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __gr
   block_norm_to_slot(nrm, a.io.slots, tile);
 }
 
+template <int MODE>
+__global__ void __launch_bounds__(kResThreads, 1) em2_resident_kernel(const __grid_constant__ Em2Resident a) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ int s_abort, s_nrec;
+  __shared__ int s_rec[2 * kResMaxLocalRec];  // (receiver, tile cell) pairs
+  if (a.plan.tile[blockIdx.x].w >> 16) em2_resident_tile<MODE, kResRows3>(a, smem, s_abort, s_nrec, s_rec);
+  else em2_resident_tile<MODE, kResRows>(a, smem, s_abort, s_nrec, s_rec);
+}
+
 }  // namespace
 
-size_t em2_resident_smem(int TW, int TZ) {
-  const size_t SX = (size_t)TW / 4 + 1, TYT = ((size_t)TZ + kResRows - 1) / kResRows;
-  return sizeof(float) * (32 * (size_t)kResRows * kResCellThreads + 2 * (TYT + 1) * TW + 2 * (size_t)TZ * SX);
+size_t em2_resident_smem(int TW, int TZ, int RB) {
+  const size_t SX = (size_t)TW / 4 + 1, TYT = ((size_t)TZ + RB - 1) / RB;
+  const size_t arrays = RB == kResRows3 ? 4 : 8;  // coefficients, and the memory variables outside interior tiles
+  return sizeof(float) * (4 * arrays * (size_t)RB * kResCellThreads + 2 * (TYT + 1) * TW + 2 * (size_t)TZ * SX);
 }
 
 namespace {
 
 // Cost model of the planner, in four-cell groups: a group in a CPML strip or
-// on a boundary plane takes the longer update.
+// on a boundary plane takes the longer update, this many times an interior
+// group's.  The forward kernel's weight with interior three-row tiles, and
+// the adjoint sweep's (kResRows everywhere); build-time tunables, the
+// defaults measured best on the 1040 x 540 grid (forward: 4.26 us per step
+// at 6, 4.35 at 4, 4.50 with no three-row tiles, same box).
 #ifndef SFD_RES_GENERAL_COST
-#define SFD_RES_GENERAL_COST 4.0
+#define SFD_RES_GENERAL_COST 6.0
 #endif
-constexpr double kGeneralCost = SFD_RES_GENERAL_COST;
+#ifndef SFD_RES_ADJ_GENERAL_COST
+#define SFD_RES_ADJ_GENERAL_COST 4.0
+#endif
 
 // Cut n items of weight 1 + beta * gen[q] into `parts` runs of about equal
 // weight; bounds[0] = 0, bounds[parts] = n.  False if a run would be empty.
@@ -570,8 +595,9 @@ bool cut_weighted(int n, const std::vector<int>& gen, double beta, int parts, in
 
 }  // namespace
 
-bool em2_resident_plan(int NX, int NZ, int npml, int max_ctas, size_t max_smem, ResPlan* out) {
+bool em2_resident_plan(int NX, int NZ, int npml, int max_ctas, size_t max_smem, ResPlan* out, bool rows3) {
   const int W = npml;
+  const double kGeneralCost = rows3 ? SFD_RES_GENERAL_COST : SFD_RES_ADJ_GENERAL_COST;
   const int ng = (NX + 3) / 4;  // four-cell column groups
   std::vector<int> gcol(ng), grow(NZ);
   for (int g = 0; g < ng; ++g) {
@@ -584,34 +610,43 @@ bool em2_resident_plan(int NX, int NZ, int npml, int max_ctas, size_t max_smem, 
   for (int k = 0; k < NZ; ++k) pr[k + 1] = pr[k] + grow[k];
   max_ctas = std::min(max_ctas, kResMaxTiles);
 
+  // Whether a tile of ngp groups and nr rows fits one CTA with RB rows per thread.
+  auto fits = [&](int ngp, int nr, int RB) {
+    return ngp * ((nr + RB - 1) / RB) <= kResCellThreads && 4 * ngp + nr <= 32 * kResFetchPerLane &&
+           em2_resident_smem(4 * ngp, nr, RB) <= max_smem;
+  };
   // Cut tile row [z0, z1) into tiles of cost <= C, greedily from the left;
   // returns the tile count (or a count above max_ctas if impossible) and
-  // the group bounds in `cuts`.
-  auto cut_row = [&](int z0, int z1, double C, std::vector<int>* cuts) {
+  // the group bounds in `cuts`, and in `inner` whether each tile is interior
+  // (kResRows3 rows per thread).
+  auto cut_row = [&](int z0, int z1, double C, std::vector<int>* cuts, std::vector<char>* inner) {
     const int nr = z1 - z0, gr = pr[z1] - pr[z0];
+    const bool band3 = rows3 && gr == 0;  // no strip or boundary row in the band
     int count = 0, g0 = 0;
+    bool in3 = band3;  // the open tile holds interior groups only
     double cost = 0.0;
     if (cuts) cuts->assign(1, 0);
+    if (inner) inner->clear();
     for (int g = 0; g < ng; ++g) {
       const double cg = gcol[g] ? kGeneralCost * nr : gr * kGeneralCost + (nr - gr);
-      const int ngp = g - g0 + 1;
-      const int trows = (nr + kResRows - 1) / kResRows;
-      const bool over = cost + cg + 1.0 + nr > C || ngp * trows > kResCellThreads ||
-                        4 * ngp + nr > 32 * kResFetchPerLane || em2_resident_smem(4 * ngp, nr) > max_smem;
+      bool in3g = in3 && !gcol[g];
+      const bool over = cost + cg + 1.0 + nr > C || !fits(g - g0 + 1, nr, in3g ? kResRows3 : kResRows);
       if (over && g > g0) {
         ++count;
         if (cuts) cuts->push_back(g);
+        if (inner) inner->push_back(in3);
         g0 = g;
         cost = 0.0;
+        in3g = band3 && !gcol[g];
       }
-      const int ngp1 = g - g0 + 1;
-      if (ngp1 * trows > kResCellThreads || 4 * ngp1 + nr > 32 * kResFetchPerLane ||
-          em2_resident_smem(4 * ngp1, nr) > max_smem || cg + 1.0 + nr > C)
+      if (!fits(g - g0 + 1, nr, in3g ? kResRows3 : kResRows) || cg + 1.0 + nr > C)
         return max_ctas + 1;  // one group alone does not fit
+      in3 = in3g;
       cost += cg + 1.0;
     }
     ++count;
     if (cuts) cuts->push_back(ng);
+    if (inner) inner->push_back(in3);
     return count > kResMaxTiles1D ? max_ctas + 1 : count;
   };
 
@@ -626,7 +661,7 @@ bool em2_resident_plan(int NX, int NZ, int npml, int max_ctas, size_t max_smem, 
       double lo = 0.0, hi = 1e12;
       auto tiles_at = [&](double C) {
         int total = 0;
-        for (int r = 0; r < ntz && total <= max_ctas; ++r) total += cut_row(rb[r], rb[r + 1], C, nullptr);
+        for (int r = 0; r < ntz && total <= max_ctas; ++r) total += cut_row(rb[r], rb[r + 1], C, nullptr, nullptr);
         return total;
       };
       if (tiles_at(hi) > max_ctas) continue;
@@ -647,13 +682,14 @@ bool em2_resident_plan(int NX, int NZ, int npml, int max_ctas, size_t max_smem, 
   out->ntiles = 0;
   out->smem = 0;
   std::vector<int> cuts;
+  std::vector<char> inner;
   for (int r = 0; r < best_ntz; ++r) {
     const int z0 = best_rows[r], z1 = best_rows[r + 1];
-    const int n = cut_row(z0, z1, best, &cuts);
+    const int n = cut_row(z0, z1, best, &cuts, &inner);
     for (int c = 0; c < n; ++c) {
       const int x0 = 4 * cuts[c], x1 = std::min(NX, 4 * cuts[c + 1]);
-      out->tile[out->ntiles++] = make_int4(x0 | (x1 << 16), z0 | (z1 << 16), r | (c << 16), n);
-      out->smem = std::max(out->smem, em2_resident_smem((x1 - x0 + 3) & ~3, z1 - z0));
+      out->tile[out->ntiles++] = make_int4(x0 | (x1 << 16), z0 | (z1 << 16), r | (c << 16), n | (inner[c] << 16));
+      out->smem = std::max(out->smem, em2_resident_smem((x1 - x0 + 3) & ~3, z1 - z0, inner[c] ? kResRows3 : kResRows));
     }
   }
   return true;

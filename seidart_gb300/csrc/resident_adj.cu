@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(kResThreads, 1) em2_adj_resident_kernel(const 
   const int nxt = (te.x >> 16) - x0, nzt = (te.y >> 16) - z0;
   const int TW = (nxt + 3) & ~3, TZ = nzt;
   const int TXT = TW >> 2, TYT = (TZ + RB - 1) / RB, SX = TXT + 1;
-  const bool up = bz > 0, down = bz < a.plan.ntz - 1, left = bx > 0, right = bx < te.w - 1;
+  const bool up = bz > 0, down = bz < a.plan.ntz - 1, left = bx > 0, right = bx < (te.w & 0xffff) - 1;
   const int tid = threadIdx.x;
   const bool xwarp = tid >= kResCellThreads;
   int cls = 3;

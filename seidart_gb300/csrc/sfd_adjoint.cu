@@ -68,7 +68,7 @@ bool adjoint_on_chip(sfd_handle* h) {
   h->adj_res_state = -1;
   if (!resident_usable(h)) return false;
   int per_sm = 0;
-  if (em2_adj_resident_prepare(h->res_plan, h->cfg.nx, h->cfg.nz, h->L.W, &per_sm) != cudaSuccess || per_sm < 1) {
+  if (em2_adj_resident_prepare(h->res_plan_adj, h->cfg.nx, h->cfg.nz, h->L.W, &per_sm) != cudaSuccess || per_sm < 1) {
     cudaGetLastError();
     return false;
   }
@@ -548,7 +548,7 @@ static int em2_adjoint_sweep_on_chip(sfd_handle* h, const AdjLayout& A, int64_t 
   ar.s0 = (int)s0;
   ar.nsteps = (int)nsteps;
   ar.ctl = (Ctl*)(h->base + L.off_ctl);
-  ar.plan = h->res_plan;
+  ar.plan = h->res_plan_adj;
   ar.r = fr.r;
   ar.limit_ns = fr.limit_ns;
   CK(cudaMemsetAsync(h->base + L.off_res, 0, res_scratch_bytes(L.P, L.NZ), h->stream));

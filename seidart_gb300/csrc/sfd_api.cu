@@ -534,32 +534,34 @@ bool resident_usable(sfd_handle* h) {
   }
   // Plans are searched once per grid shape and device (the search takes
   // tens of milliseconds; a survey creates one handle per shot).
+  // The forward kernel's plan (interior tiles with kResRows3 rows per
+  // thread) and the adjoint sweep's (kResRows everywhere).
   struct PlanKey {
     int nx, nz, npml, ctas, dev;
     size_t smem;
+    bool rows3;
   };
   static std::mutex plan_mu;
   static std::vector<std::pair<PlanKey, std::pair<bool, ResPlan>>> plans;
-  const PlanKey key{h->cfg.nx, h->cfg.nz, h->cfg.npml, std::min(nsm, h->L.nslots), dev, (size_t)optin - static_smem};
+  auto plan_for = [&](bool rows3, ResPlan* plan) {
+    const PlanKey key{h->cfg.nx, h->cfg.nz, h->cfg.npml, std::min(nsm, h->L.nslots), dev, (size_t)optin - static_smem,
+                      rows3};
+    {
+      std::lock_guard<std::mutex> lock(plan_mu);
+      for (const auto& e : plans)
+        if (e.first.nx == key.nx && e.first.nz == key.nz && e.first.npml == key.npml && e.first.ctas == key.ctas &&
+            e.first.dev == key.dev && e.first.smem == key.smem && e.first.rows3 == key.rows3) {
+          *plan = e.second.second;
+          return e.second.first;
+        }
+    }
+    const bool fits = em2_resident_plan(key.nx, key.nz, key.npml, key.ctas, key.smem, plan, rows3);
+    std::lock_guard<std::mutex> lock(plan_mu);
+    plans.push_back({key, {fits, *plan}});
+    return fits;
+  };
   ResPlan plan;
-  bool fits = false, cached = false;
-  {
-    std::lock_guard<std::mutex> lock(plan_mu);
-    for (const auto& e : plans)
-      if (e.first.nx == key.nx && e.first.nz == key.nz && e.first.npml == key.npml && e.first.ctas == key.ctas &&
-          e.first.dev == key.dev && e.first.smem == key.smem) {
-        fits = e.second.first;
-        plan = e.second.second;
-        cached = true;
-        break;
-      }
-  }
-  if (!cached) {
-    fits = em2_resident_plan(key.nx, key.nz, key.npml, key.ctas, key.smem, &plan);
-    std::lock_guard<std::mutex> lock(plan_mu);
-    plans.push_back({key, {fits, plan}});
-  }
-  if (!fits) return false;
+  if (!plan_for(true, &plan) || !plan_for(false, &h->res_plan_adj)) return false;
   int per_sm = 0;
   if (em2_resident_prepare(plan, &per_sm) != cudaSuccess || per_sm < 1) {
     cudaGetLastError();

@@ -230,9 +230,14 @@ def test_recorded_adjoint_matches_checkpointed(gpu, grid):
             m.close()
     (ta, ea, ga), (tb, eb, gb) = out
     assert np.array_equal(ta, tb) and np.array_equal(ea, eb)
-    for q in (0, 2, 3, 5):
+    # The recorded form sweeps the whole run at once, the checkpointed form
+    # one segment at a time, so each cell's per-step products are summed in
+    # a different grouping; the conductivity plane's sums cancel the most
+    # (measured: 1e-7 for the permittivity planes, 4e-7 to 1.3e-6 for it,
+    # depending on the forward tiling's rounding).
+    for q, tol in ((0, 1e-6), (2, 1e-6), (3, 3e-6), (5, 1e-6)):
         err = np.linalg.norm(ga[q] - gb[q]) / np.linalg.norm(ga[q])
-        assert err <= 1e-6, f"plane {q}: relative L2 {err:.3e}"
+        assert err <= tol, f"plane {q}: relative L2 {err:.3e}"
 
 
 def test_record_refused_off_chip(gpu):

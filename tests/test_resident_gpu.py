@@ -79,3 +79,17 @@ def test_many_receivers_in_one_tile(gpu):
     block = [(x, 0, z) for z in range(200, 220) for x in range(500, 520)]
     case.rec_ijk = np.array(block + [(30, 0, 30), (500, 0, 200)], dtype=np.int32)
     _compare(case, (60,))
+
+
+@pytest.mark.parametrize("src", [(520, 0, 270), (37 * 4 + 2, 0, 300), (800, 0, 22 + 3 * 30)])
+def test_source_inside_interior_tiles(gpu, src):
+    """The headline grid's interior tiles hold three rows per thread and take
+    the short update only; the source cell in one of them (mid-grid, and near
+    the top and the right of the interior) is injected there, and receivers
+    around it and on its row read the same fields as the per-step kernels."""
+    case = sy.electromag2_layers(nstep=90)
+    x, _, z = src
+    rec = [(x + dx, 0, z + dz) for dx in (-5, 0, 3) for dz in (-4, 0, 2)] + [(q, 0, z) for q in range(30, 1000, 37)]
+    case.rec_ijk = np.array(rec, dtype=np.int32)
+    case.src_ijk = src
+    _compare(case, (45, 45))
