@@ -724,6 +724,20 @@ def run_times(solver, nstep, stream, n=3):
     return tot / n
 
 
+def profile_value(name, key):
+    """A number recorded in profiles/<name>.md as a "key: N" line, else None."""
+    p = ROOT / "profiles" / f"{name}.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.strip().startswith(key + ":"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
 def profile_traffic(name):
     """dram bytes per launch recorded in profiles/<name>.md ("dram_bytes_per_launch: N"), else None."""
     p = ROOT / "profiles" / f"{name}.md"
@@ -937,6 +951,18 @@ def run_ours(args):
                 "algorithmic_bytes_per_launch": int(per_launch),
                 "kernel_ms": round(kms, 5),
                 "note": note}
+    issue = profile_value(f"{dom_name}_1040x540", "issue_active_pct")
+    if issue is not None and dom_name == "em2_resident_kernel":
+        # the on-chip kernel's own bound, from its ncu summary of the same workload: the
+        # time per step if every SM sub-partition issued an instruction every cycle, and
+        # the share of the warps' stalls spent at the block barriers
+        bar = profile_value(f"{dom_name}_1040x540", "barrier_stall_per_issue")
+        tot = profile_value(f"{dom_name}_1040x540", "total_stall_per_issue")
+        us = kms * 1e3 / case.nstep
+        roofline["on_chip"] = {"bound": "issue", "issue_active": round(issue / 100, 4),
+                               "issue_bound_us_per_step": round(us * issue / 100, 3), "us_per_step": round(us, 3),
+                               "barrier_share_of_stalls": round(bar / tot, 3) if bar and tot else None,
+                               "source": f"profiles/{dom_name}_1040x540.md (ncu --set full)"}
     step_achieved = byts["step"] / (step_ms / 1e3) / 1e9
     roofline_step = {"bytes_per_cell_update": round(byts["per_cell_step"], 2),
                      "achieved": round(step_achieved, 1), "frac": round(step_achieved / peak, 4), "unit": "GB/s"}
