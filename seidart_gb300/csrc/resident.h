@@ -18,9 +18,9 @@ namespace sfd {
 constexpr int kResMaxTiles1D = 32;
 // Largest number of tiles (CTAs, at most one per SM) of one on-chip run.
 constexpr int kResMaxTiles = 256;
-// Threads of a CTA: up to 15 warps own the cells (four cells of kResRows rows
-// per thread), the last warp moves the tile's edges to and from the
-// neighbouring tiles.
+// Threads of a CTA: up to 15 warps own the cells (four cells of kResRows
+// rows per thread, kResRows3 in interior electromag2 tiles), the last warp
+// moves the tile's edges to and from the neighbouring tiles.
 constexpr int kResThreads = 512;
 constexpr int kResCellThreads = kResThreads - 32;
 constexpr int kResRows = 2;
